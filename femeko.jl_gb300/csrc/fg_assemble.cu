@@ -1,0 +1,741 @@
+// Element kernels and the deterministic row gather.
+//
+// Assembly runs in two passes, neither of which uses atomics:
+//   1. an element kernel computes each element's local matrix (and/or a local
+//      vector) and writes local row a of element k to incidence position
+//      recpos[a][k] -- the incidence records of a node are contiguous per SELL
+//      slice, so the second pass reads them coalesced;
+//   2. a row kernel (one thread per matrix row) walks its incidence records in
+//      (element, local node) order and adds each value into the row slot given by
+//      the precomputed slot byte.  The order of every sum is fixed by the mesh, so
+//      results are bit-identical from run to run.
+//
+// Reference formulas (paths relative to the reference repository):
+//   P1 stiffness      src/FEM3D.jl:59-76       VE f (grad phi_a . grad phi_b)
+//   P1 mass           src/FEM3D.jl:466-492     VE/20 (1 + delta_ab)
+//   P1 tangent        src/FEM3D.jl:79-119      VE dmu/|H| (H.grad phi_a)(H.grad phi_b)
+//   2D stiffness/mass src/FEM2D.jl:48-76,139-161
+//   P2 stiffness      src/FEM3D.jl:324-376, src/FEM2D.jl:80-115 (equal weights at the nodes)
+//   P2 mass           src/FEM3D.jl:494-561, src/FEM2D.jl:163-229 (Gauss rules below)
+#include <type_traits>
+
+#include "fg_common.cuh"
+
+// ------------------------------------------------------------------ helpers
+template <int NPE, typename R>
+__device__ __forceinline__ void store_row(R *rec, int64_t pos, const R *v) {
+#pragma unroll
+  for (int j = 0; j < NPE; ++j) rec[pos * NPE + j] = v[j];
+}
+template <>
+__device__ __forceinline__ void store_row<4, double>(double *rec, int64_t pos, const double *v) {
+  double2 *d = reinterpret_cast<double2 *>(rec + pos * 4);
+  d[0] = make_double2(v[0], v[1]);
+  d[1] = make_double2(v[2], v[3]);
+}
+template <>
+__device__ __forceinline__ void store_row<4, float>(float *rec, int64_t pos, const float *v) {
+  *reinterpret_cast<float4 *>(rec + pos * 4) = make_float4(v[0], v[1], v[2], v[3]);
+}
+
+// ------------------------------------------------------------------ P1 tetrahedra
+// kind: ASM_STIFF   Ke = f VE G G^T
+//       ASM_MASS    Ke = f VE/20 (1 + delta)
+//       ASM_TANGENT Ke = VE dmu/|H| (H.g_a)(H.g_b)
+//       ASM_HEAT    Ke = cm VE/20 (1 + delta) + cs f VE G G^T
+template <typename R>
+__global__ void k_elem_tet4(int kind, int64_t nt, const double *__restrict__ geo, const double *__restrict__ f,
+                            const double *__restrict__ H, const double *__restrict__ dmu, double cm, double cs,
+                            const int *__restrict__ recpos, R *__restrict__ rec) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt) return;
+  double g[4][3];
+#pragma unroll
+  for (int c = 0; c < 12; ++c) g[c / 3][c % 3] = geo[(int64_t)c * nt + k];
+  double VE = geo[12 * nt + k];
+  double fk = f ? f[k] : 1.0;
+  double Ke[4][4];
+  if (kind == ASM_MASS || kind == ASM_HEAT) {
+    double mfac = (kind == ASM_MASS ? fk : cm) * VE / 20.0;
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) Ke[a][b] = mfac * (a == b ? 2.0 : 1.0);
+  }
+  if (kind == ASM_STIFF || kind == ASM_HEAT) {
+    double s = (kind == ASM_STIFF ? fk : cs * fk) * VE;
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = a; b < 4; ++b) {
+        double v = s * (g[a][0] * g[b][0] + g[a][1] * g[b][1] + g[a][2] * g[b][2]);
+        if (kind == ASM_HEAT) { Ke[a][b] += v; if (b != a) Ke[b][a] += v; }
+        else { Ke[a][b] = v; Ke[b][a] = v; }
+      }
+  }
+  if (kind == ASM_TANGENT) {
+    double hx = H[3 * k], hy = H[3 * k + 1], hz = H[3 * k + 2];
+    double hn = sqrt(hx * hx + hy * hy + hz * hz);
+    double s = (hn > 0.0) ? VE * dmu[k] / hn : 0.0;
+    double ah[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) ah[a] = hx * g[a][0] + hy * g[a][1] + hz * g[a][2];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) Ke[a][b] = s * ah[a] * ah[b];
+  }
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    R row[4];
+#pragma unroll
+    for (int b = 0; b < 4; ++b) row[b] = (R)Ke[a][b];
+    store_row<4, R>(rec, recpos[(int64_t)a * nt + k], row);
+  }
+}
+
+// ------------------------------------------------------------------ P1 triangles
+template <typename R>
+__global__ void k_elem_tri3(int kind, int64_t nt, const double *__restrict__ geo, const double *__restrict__ f,
+                            double cm, double cs, const int *__restrict__ recpos, R *__restrict__ rec) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt) return;
+  double g[3][2];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) g[c / 2][c % 2] = geo[(int64_t)c * nt + k];
+  double VE = geo[6 * nt + k];
+  double fk = f ? f[k] : 1.0;
+  double Ke[3][3] = {{0}};
+  if (kind == ASM_MASS || kind == ASM_HEAT) {
+    double mfac = (kind == ASM_MASS ? fk : cm) * VE / 12.0;
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) Ke[a][b] = mfac * (a == b ? 2.0 : 1.0);
+  }
+  if (kind == ASM_STIFF || kind == ASM_HEAT) {
+    double s = (kind == ASM_STIFF ? fk : cs * fk) * VE;
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) Ke[a][b] += s * (g[a][0] * g[b][0] + g[a][1] * g[b][1]);
+  }
+  for (int a = 0; a < 3; ++a) {
+    R row[3];
+    for (int b = 0; b < 3; ++b) row[b] = (R)Ke[a][b];
+    store_row<3, R>(rec, recpos[(int64_t)a * nt + k], row);
+  }
+}
+
+// ------------------------------------------------------------------ second order
+// The reference builds each P2 basis function by solving the Vandermonde system of
+// the element's nodes (src/FEM3D.jl:21-37, src/FEM2D.jl:28-45).  Here the same
+// system is inverted once per element with Gauss-Jordan and partial pivoting, in
+// coordinates shifted to the first vertex (same basis functions, better
+// conditioned).  Column a of the inverse holds the coefficients of node a's basis.
+template <int N>
+__device__ bool gj_inverse(double *A, double *Inv) {
+  for (int r = 0; r < N; ++r)
+    for (int c = 0; c < N; ++c) Inv[r * N + c] = (r == c) ? 1.0 : 0.0;
+  for (int c = 0; c < N; ++c) {
+    int piv = c;
+    double best = fabs(A[c * N + c]);
+    for (int r = c + 1; r < N; ++r) {
+      double v = fabs(A[r * N + c]);
+      if (v > best) { best = v; piv = r; }
+    }
+    if (best == 0.0) return false;
+    if (piv != c)
+      for (int q = 0; q < N; ++q) {
+        double t0 = A[c * N + q]; A[c * N + q] = A[piv * N + q]; A[piv * N + q] = t0;
+        double t1 = Inv[c * N + q]; Inv[c * N + q] = Inv[piv * N + q]; Inv[piv * N + q] = t1;
+      }
+    double inv = 1.0 / A[c * N + c];
+    for (int q = 0; q < N; ++q) { A[c * N + q] *= inv; Inv[c * N + q] *= inv; }
+    for (int r = 0; r < N; ++r) {
+      if (r == c) continue;
+      double l = A[r * N + c];
+      if (l == 0.0) continue;
+      for (int q = 0; q < N; ++q) { A[r * N + q] -= l * A[c * N + q]; Inv[r * N + q] -= l * Inv[c * N + q]; }
+    }
+  }
+  return true;
+}
+
+// 15-point rule of src/FEM3D.jl:710-745 (GaussQuadrature3D(4)); the table is the
+// published one and is kept alike.  Weights are divided by 6 as in the reference.
+__constant__ double c_gq3_pts[15][3] = {
+    {0.2500000000000000, 0.2500000000000000, 0.2500000000000000},
+    {0.0000000000000000, 0.3333333333333333, 0.3333333333333333},
+    {0.3333333333333333, 0.3333333333333333, 0.3333333333333333},
+    {0.3333333333333333, 0.3333333333333333, 0.0000000000000000},
+    {0.3333333333333333, 0.0000000000000000, 0.3333333333333333},
+    {0.7272727272727273, 0.0909090909090909, 0.0909090909090909},
+    {0.0909090909090909, 0.0909090909090909, 0.0909090909090909},
+    {0.0909090909090909, 0.0909090909090909, 0.7272727272727273},
+    {0.0909090909090909, 0.7272727272727273, 0.0909090909090909},
+    {0.4334498464263357, 0.0665501535736643, 0.0665501535736643},
+    {0.0665501535736643, 0.4334498464263357, 0.0665501535736643},
+    {0.0665501535736643, 0.0665501535736643, 0.4334498464263357},
+    {0.0665501535736643, 0.4334498464263357, 0.4334498464263357},
+    {0.4334498464263357, 0.0665501535736643, 0.4334498464263357},
+    {0.4334498464263357, 0.4334498464263357, 0.0665501535736643}};
+__constant__ double c_gq3_w[15] = {0.1817020685825351, 0.0361607142857143, 0.0361607142857143, 0.0361607142857143,
+                                   0.0361607142857143, 0.0698714945161738, 0.0698714945161738, 0.0698714945161738,
+                                   0.0698714945161738, 0.0656948493683187, 0.0656948493683187, 0.0656948493683187,
+                                   0.0656948493683187, 0.0656948493683187, 0.0656948493683187};
+// 6-point rule of src/FEM2D.jl:483-497 (GaussQuadrature2D(4)), weights summing to 1.
+__constant__ double c_gq2_pts[6][2] = {{0.445948490915965, 0.445948490915965}, {0.445948490915965, 0.108103018168070},
+                                       {0.108103018168070, 0.445948490915965}, {0.091576213509771, 0.091576213509771},
+                                       {0.091576213509771, 0.816847572980459}, {0.816847572980459, 0.091576213509771}};
+__constant__ double c_gq2_w[6] = {0.223381589678011, 0.223381589678011, 0.223381589678011,
+                                  0.109951743655322, 0.109951743655322, 0.109951743655322};
+
+// P2 tetrahedron (10 nodes).  ASM_STIFF: equal-weight rule over the 10 nodes, /10
+// (src/FEM3D.jl:344-364).  ASM_MASS: 15-point rule, w = W_q/6 * VE * F
+// (src/FEM3D.jl:518-541); full_phi = 0 evaluates only S1 + S2 x + S3 y + S4 z of
+// each basis polynomial in global coordinates, as the reference's line break at
+// :529-531 makes Julia do.
+__global__ void k_elem_tet10(int kind, int full_phi, int64_t nt, const double *__restrict__ p,
+                             const int *__restrict__ t, const double *__restrict__ geo, const double *__restrict__ f,
+                             const int *__restrict__ recpos, double *__restrict__ rec, int *flags) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt) return;
+  int nds[10];
+  for (int a = 0; a < 10; ++a) nds[a] = t[(int64_t)a * nt + k];
+  double x0 = p[3 * nds[0]], y0 = p[3 * nds[0] + 1], z0 = p[3 * nds[0] + 2];
+  double X[10], Y[10], Z[10];
+  double V[100], S[100];
+  for (int r = 0; r < 10; ++r) {
+    X[r] = p[3 * nds[r]] - x0; Y[r] = p[3 * nds[r] + 1] - y0; Z[r] = p[3 * nds[r] + 2] - z0;
+    double row[10] = {1.0, X[r], Y[r], Z[r], X[r] * X[r], X[r] * Y[r], X[r] * Z[r], Y[r] * Y[r], Y[r] * Z[r], Z[r] * Z[r]};
+    for (int c = 0; c < 10; ++c) V[r * 10 + c] = row[c];
+  }
+  if (!gj_inverse<10>(V, S)) { atomicOr(flags, FLAG_DEGENERATE); return; }
+  // S[c*10 + a] = coefficient c of node a's basis (shifted coordinates)
+  double VE = geo[12 * nt + k];
+  double fk = f ? f[k] : 1.0;
+  double Ke[10][10];
+  for (int i = 0; i < 10; ++i)
+    for (int j = 0; j < 10; ++j) Ke[i][j] = 0.0;
+  if (kind == ASM_STIFF) {
+    for (int n = 0; n < 10; ++n) {
+      double dx[10], dy[10], dz[10];
+      for (int a = 0; a < 10; ++a) {
+        const double s1 = S[10 + a], s2 = S[20 + a], s3 = S[30 + a], s4 = S[40 + a], s5 = S[50 + a],
+                     s6 = S[60 + a], s7 = S[70 + a], s8 = S[80 + a], s9 = S[90 + a];
+        dx[a] = s1 + 2 * s4 * X[n] + s5 * Y[n] + s6 * Z[n];
+        dy[a] = s2 + 2 * s7 * Y[n] + s5 * X[n] + s8 * Z[n];
+        dz[a] = s3 + 2 * s9 * Z[n] + s6 * X[n] + s8 * Y[n];
+      }
+      for (int i = 0; i < 10; ++i)
+        for (int j = i; j < 10; ++j) Ke[i][j] += dx[i] * dx[j] + dy[i] * dy[j] + dz[i] * dz[j];
+    }
+    for (int i = 0; i < 10; ++i)
+      for (int j = i; j < 10; ++j) { Ke[i][j] = Ke[i][j] / 10.0 * fk * VE; Ke[j][i] = Ke[i][j]; }
+  } else {
+    // global-coordinate constant and linear coefficients (value and gradient at the origin)
+    double e1 = p[3 * nds[1]] - x0, e2 = p[3 * nds[2]] - x0, e3 = p[3 * nds[3]] - x0;
+    double f1 = p[3 * nds[1] + 1] - y0, f2 = p[3 * nds[2] + 1] - y0, f3 = p[3 * nds[3] + 1] - y0;
+    double g1 = p[3 * nds[1] + 2] - z0, g2 = p[3 * nds[2] + 2] - z0, g3 = p[3 * nds[3] + 2] - z0;
+    double lin[10][4];
+    if (!full_phi) {
+      double ox = -x0, oy = -y0, oz = -z0;
+      for (int a = 0; a < 10; ++a) {
+        const double *c = S;
+        double s0 = c[a], s1 = c[10 + a], s2 = c[20 + a], s3 = c[30 + a], s4 = c[40 + a], s5 = c[50 + a],
+               s6 = c[60 + a], s7 = c[70 + a], s8 = c[80 + a], s9 = c[90 + a];
+        lin[a][0] = s0 + s1 * ox + s2 * oy + s3 * oz + s4 * ox * ox + s5 * ox * oy + s6 * ox * oz + s7 * oy * oy +
+                    s8 * oy * oz + s9 * oz * oz;
+        lin[a][1] = s1 + 2 * s4 * ox + s5 * oy + s6 * oz;
+        lin[a][2] = s2 + 2 * s7 * oy + s5 * ox + s8 * oz;
+        lin[a][3] = s3 + 2 * s9 * oz + s6 * ox + s8 * oy;
+      }
+    }
+    for (int q = 0; q < 15; ++q) {
+      double xi = c_gq3_pts[q][0], eta = c_gq3_pts[q][1], ze = c_gq3_pts[q][2];
+      double Xq = e1 * xi + e2 * eta + e3 * ze, Yq = f1 * xi + f2 * eta + f3 * ze, Zq = g1 * xi + g2 * eta + g3 * ze;
+      double phi[10];
+      for (int a = 0; a < 10; ++a) {
+        if (full_phi) {
+          phi[a] = S[a] + S[10 + a] * Xq + S[20 + a] * Yq + S[30 + a] * Zq + S[40 + a] * Xq * Xq +
+                   S[50 + a] * Xq * Yq + S[60 + a] * Xq * Zq + S[70 + a] * Yq * Yq + S[80 + a] * Yq * Zq +
+                   S[90 + a] * Zq * Zq;
+        } else {
+          phi[a] = lin[a][0] + lin[a][1] * (Xq + x0) + lin[a][2] * (Yq + y0) + lin[a][3] * (Zq + z0);
+        }
+      }
+      double w = c_gq3_w[q] / 6.0 * VE;
+      for (int i = 0; i < 10; ++i)
+        for (int j = i; j < 10; ++j) Ke[i][j] += w * phi[i] * phi[j] * fk;
+    }
+    for (int i = 0; i < 10; ++i)
+      for (int j = i + 1; j < 10; ++j) Ke[j][i] = Ke[i][j];
+  }
+  for (int a = 0; a < 10; ++a) store_row<10, double>(rec, recpos[(int64_t)a * nt + k], Ke[a]);
+}
+
+// P2 triangle (6 nodes).  ASM_STIFF: 6-node equal-weight rule, /6
+// (src/FEM2D.jl:95-107).  ASM_MASS: 6-point rule, w = weight * VE (src/FEM2D.jl:192-212).
+__global__ void k_elem_tri6(int kind, int64_t nt, const double *__restrict__ p, const int *__restrict__ t,
+                            const double *__restrict__ geo, const double *__restrict__ f,
+                            const int *__restrict__ recpos, double *__restrict__ rec, int *flags) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt) return;
+  int nds[6];
+  for (int a = 0; a < 6; ++a) nds[a] = t[(int64_t)a * nt + k];
+  double x0 = p[3 * nds[0]], y0 = p[3 * nds[0] + 1];
+  double X[6], Y[6], V[36], S[36];
+  for (int r = 0; r < 6; ++r) {
+    X[r] = p[3 * nds[r]] - x0; Y[r] = p[3 * nds[r] + 1] - y0;
+    double row[6] = {1.0, X[r], Y[r], X[r] * X[r], X[r] * Y[r], Y[r] * Y[r]};
+    for (int c = 0; c < 6; ++c) V[r * 6 + c] = row[c];
+  }
+  if (!gj_inverse<6>(V, S)) { atomicOr(flags, FLAG_DEGENERATE); return; }
+  double VE = geo[6 * nt + k];
+  double fk = f ? f[k] : 1.0;
+  double Ke[6][6];
+  for (int i = 0; i < 6; ++i)
+    for (int j = 0; j < 6; ++j) Ke[i][j] = 0.0;
+  if (kind == ASM_STIFF) {
+    for (int n = 0; n < 6; ++n) {
+      double dx[6], dy[6];
+      for (int a = 0; a < 6; ++a) {
+        dx[a] = S[6 + a] + 2 * S[18 + a] * X[n] + S[24 + a] * Y[n];
+        dy[a] = S[12 + a] + S[24 + a] * X[n] + 2 * S[30 + a] * Y[n];
+      }
+      for (int i = 0; i < 6; ++i)
+        for (int j = i; j < 6; ++j) Ke[i][j] += dx[i] * dx[j] + dy[i] * dy[j];
+    }
+    for (int i = 0; i < 6; ++i)
+      for (int j = i; j < 6; ++j) { Ke[i][j] = Ke[i][j] / 6.0 * VE * fk; Ke[j][i] = Ke[i][j]; }
+  } else {
+    double e1 = p[3 * nds[1]] - x0, e2 = p[3 * nds[2]] - x0;
+    double f1 = p[3 * nds[1] + 1] - y0, f2 = p[3 * nds[2] + 1] - y0;
+    for (int q = 0; q < 6; ++q) {
+      double xi = c_gq2_pts[q][0], eta = c_gq2_pts[q][1];
+      double Xq = e1 * xi + e2 * eta, Yq = f1 * xi + f2 * eta;
+      double phi[6];
+      for (int a = 0; a < 6; ++a)
+        phi[a] = S[a] + S[6 + a] * Xq + S[12 + a] * Yq + S[18 + a] * Xq * Xq + S[24 + a] * Xq * Yq + S[30 + a] * Yq * Yq;
+      double w = c_gq2_w[q] * VE;
+      for (int i = 0; i < 6; ++i)
+        for (int j = i; j < 6; ++j) Ke[i][j] += w * phi[i] * phi[j] * fk;
+    }
+    for (int i = 0; i < 6; ++i)
+      for (int j = i + 1; j < 6; ++j) Ke[j][i] = Ke[i][j];
+  }
+  for (int a = 0; a < 6; ++a) store_row<6, double>(rec, recpos[(int64_t)a * nt + k], Ke[a]);
+}
+
+// ------------------------------------------------------------------ Newton element pass
+// From the potential u: H = -sum u_a grad phi_a, |H|, mu and dmu (Froehlich law for
+// nl elements, mu_lin otherwise), the energy density integral of H dB times VE, the
+// residual records (K_e u_e)_a = -VE mu grad(phi_a).H and the Jacobian records
+// J_ab = VE mu grad(phi_a).grad(phi_b) + VE dmu/|H| (H.grad phi_a)(H.grad phi_b).
+// Follows Magnetostatics/NewtonRaphson.jl:154-207 and src/FEM3D.jl:79-119.  In
+// mixed precision the Jacobian records are formed in FP32 (they feed the FP32
+// operator only); H, mu and the residual stay FP64.
+template <typename R>
+__global__ void k_elem_newton(int64_t nt, const double *__restrict__ geo, const int *__restrict__ t,
+                              const double *__restrict__ u, const uint8_t *__restrict__ nl,
+                              const double *__restrict__ mu_lin, double Ms, double Hk, const int *__restrict__ recpos,
+                              R *__restrict__ rec, double *__restrict__ rec_r, double *__restrict__ mu_out,
+                              double *__restrict__ dmu_out, double *__restrict__ H_out, double *__restrict__ w_out,
+                              int *flags) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt) return;
+  double g[4][3];
+#pragma unroll
+  for (int c = 0; c < 12; ++c) g[c / 3][c % 3] = geo[(int64_t)c * nt + k];
+  double VE = geo[12 * nt + k];
+  double uu[4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) uu[a] = u[t[(int64_t)a * nt + k]];
+  double hx = 0, hy = 0, hz = 0;
+#pragma unroll
+  for (int a = 0; a < 4; ++a) { hx -= uu[a] * g[a][0]; hy -= uu[a] * g[a][1]; hz -= uu[a] * g[a][2]; }
+  double h = sqrt(hx * hx + hy * hy + hz * hz);
+  double mu, dmu, w;
+  if (nl[k]) {
+    double den = Hk + h;
+    mu = FG_MU0 * (1.0 + Ms / den);
+    dmu = -FG_MU0 * Ms / (den * den);
+    w = FG_MU0 * (0.5 * h * h + Ms * Hk * (log1p(h / Hk) + Hk / den - 1.0));
+  } else {
+    mu = mu_lin[k];
+    dmu = 0.0;
+    w = 0.5 * mu * h * h;
+  }
+  if (!isfinite(mu) || !isfinite(dmu)) atomicOr(flags, FLAG_NAN);
+  mu_out[k] = mu;
+  dmu_out[k] = dmu;
+  H_out[3 * k] = hx; H_out[3 * k + 1] = hy; H_out[3 * k + 2] = hz;
+  w_out[k] = w * VE;
+  double ah[4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) ah[a] = hx * g[a][0] + hy * g[a][1] + hz * g[a][2];
+  double vm = VE * mu;
+  double ct = (h > 0.0) ? VE * dmu / h : 0.0;
+  int pos[4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    pos[a] = recpos[(int64_t)a * nt + k];
+    rec_r[pos[a]] = -vm * ah[a];
+  }
+  if (std::is_same<R, float>::value) {
+    float gf[4][3], ahf[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      ahf[a] = (float)ah[a];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) gf[a][d] = (float)g[a][d];
+    }
+    float vmf = (float)vm, ctf = (float)ct;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      R row[4];
+#pragma unroll
+      for (int b = 0; b < 4; ++b)
+        row[b] = (R)(vmf * (gf[a][0] * gf[b][0] + gf[a][1] * gf[b][1] + gf[a][2] * gf[b][2]) + ctf * ahf[a] * ahf[b]);
+      store_row<4, R>(rec, pos[a], row);
+    }
+  } else {
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      R row[4];
+#pragma unroll
+      for (int b = 0; b < 4; ++b)
+        row[b] = (R)(vm * (g[a][0] * g[b][0] + g[a][1] * g[b][1] + g[a][2] * g[b][2]) + ct * ah[a] * ah[b]);
+      store_row<4, R>(rec, pos[a], row);
+    }
+  }
+}
+
+// (K_e x_e)_a for the stiffness (coef * VE G G^T) or mass (coef VE/20 (1+delta)) or
+// both (heat: cm M + cs K).  Vector records only.
+__global__ void k_elem_apply_tet4(int kind, int64_t nt, const double *__restrict__ geo, const int *__restrict__ t,
+                                  const double *__restrict__ coef, double cm, double cs, const double *__restrict__ x,
+                                  const int *__restrict__ recpos, double *__restrict__ rec_r) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt) return;
+  double VE = geo[12 * nt + k];
+  double xx[4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) xx[a] = x[t[(int64_t)a * nt + k]];
+  double ck = coef ? coef[k] : 1.0;
+  double out[4] = {0, 0, 0, 0};
+  if (kind == ASM_STIFF || kind == ASM_HEAT) {
+    double g[4][3];
+#pragma unroll
+    for (int c = 0; c < 12; ++c) g[c / 3][c % 3] = geo[(int64_t)c * nt + k];
+    double gx = 0, gy = 0, gz = 0;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) { gx += xx[a] * g[a][0]; gy += xx[a] * g[a][1]; gz += xx[a] * g[a][2]; }
+    double s = (kind == ASM_STIFF ? ck : cs * ck) * VE;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) out[a] = s * (g[a][0] * gx + g[a][1] * gy + g[a][2] * gz);
+  }
+  if (kind == ASM_MASS || kind == ASM_HEAT) {
+    double mfac = (kind == ASM_MASS ? ck : cm) * VE / 20.0;
+    double sum = xx[0] + xx[1] + xx[2] + xx[3];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) out[a] += mfac * (sum + xx[a]);
+  }
+#pragma unroll
+  for (int a = 0; a < 4; ++a) rec_r[recpos[(int64_t)a * nt + k]] = out[a];
+}
+
+__global__ void k_hfield_tet4(int64_t nt, const double *__restrict__ geo, const int *__restrict__ t,
+                              const double *__restrict__ u, double *__restrict__ H) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt) return;
+  double hx = 0, hy = 0, hz = 0;
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    double ua = u[t[(int64_t)a * nt + k]];
+    hx -= ua * geo[(int64_t)(3 * a) * nt + k];
+    hy -= ua * geo[(int64_t)(3 * a + 1) * nt + k];
+    hz -= ua * geo[(int64_t)(3 * a + 2) * nt + k];
+  }
+  H[3 * k] = hx; H[3 * k + 1] = hy; H[3 * k + 2] = hz;
+}
+
+// ------------------------------------------------------------------ row gather
+// One thread per row.  Walks the row's incidence records (SELL layout, pads marked
+// 0xFF) and accumulates into a per-thread slot array in shared memory, then writes
+// the row once: SELL (FP64 and/or FP32), or CSR order for export.  Dirichlet rows
+// become identity rows when apply_bc is set.  Also writes the Jacobi inverse
+// diagonal and the vector-record sum (scaled by vsign, zeroed on Dirichlet rows).
+template <int NPE, typename R, typename A>
+__global__ void k_row_sum(int64_t nv, const int *__restrict__ in_ptr, const int *__restrict__ in_len,
+                          const uint8_t *__restrict__ in_slot, const R *__restrict__ rec,
+                          const double *__restrict__ rec_r, const int *__restrict__ sl_ptr,
+                          const int *__restrict__ sl_len, const int *__restrict__ rowptr,
+                          const uint8_t *__restrict__ diagk, const uint8_t *__restrict__ fixed, int apply_bc,
+                          double *__restrict__ out64, float *__restrict__ out32, double *__restrict__ outcsr,
+                          double *__restrict__ dinv64, float *__restrict__ dinv32, double *__restrict__ vout,
+                          double vsign, int zero_fixed_vec) {
+  extern __shared__ unsigned char smem_raw[];
+  A *acc = reinterpret_cast<A *>(smem_raw) + threadIdx.x;
+  const int bs = blockDim.x;
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nv) return;
+  int s = (int)(i / FG_SLICE), lane = (int)(i % FG_SLICE);
+  int L = sl_len[s];
+  const bool want_mat = (rec != nullptr);
+  if (want_mat)
+    for (int q = 0; q < L; ++q) acc[q * bs] = (A)0;
+  double vacc = 0.0;
+  int64_t base = in_ptr[s] + lane;
+  int ilen = in_len[s];
+  for (int mm = 0; mm < ilen; ++mm) {
+    int64_t pos = base + (int64_t)mm * FG_SLICE;
+    uint8_t sl[NPE];
+    if (NPE == 4) {
+      uint32_t w = reinterpret_cast<const uint32_t *>(in_slot)[pos];
+      sl[0] = w & 0xFF; sl[1] = (w >> 8) & 0xFF; sl[2] = (w >> 16) & 0xFF; sl[3] = (w >> 24) & 0xFF;
+    } else {
+#pragma unroll
+      for (int j = 0; j < NPE; ++j) sl[j] = in_slot[pos * NPE + j];
+    }
+    if (sl[0] == 0xFF) continue;  // pad
+    if (rec_r) vacc += rec_r[pos];
+    if (want_mat) {
+      if (NPE == 4 && sizeof(R) == 8) {
+        const double2 *d = reinterpret_cast<const double2 *>(rec + pos * 4);
+        double2 v01 = d[0], v23 = d[1];
+        acc[sl[0] * bs] += (A)v01.x; acc[sl[1] * bs] += (A)v01.y;
+        acc[sl[2] * bs] += (A)v23.x; acc[sl[3] * bs] += (A)v23.y;
+      } else if (NPE == 4 && sizeof(R) == 4) {
+        float4 v = *reinterpret_cast<const float4 *>(rec + pos * 4);
+        acc[sl[0] * bs] += (A)v.x; acc[sl[1] * bs] += (A)v.y;
+        acc[sl[2] * bs] += (A)v.z; acc[sl[3] * bs] += (A)v.w;
+      } else {
+#pragma unroll
+        for (int j = 0; j < NPE; ++j) acc[sl[j] * bs] += (A)rec[pos * NPE + j];
+      }
+    }
+  }
+  const bool fx = fixed && fixed[i];
+  if (vout) vout[i] = (zero_fixed_vec && fx) ? 0.0 : vsign * vacc;
+  if (!want_mat) return;
+  int dk = diagk[i];
+  if (apply_bc && fx)
+    for (int q = 0; q < L; ++q) acc[q * bs] = (q == dk) ? (A)1 : (A)0;
+  int64_t sb = sl_ptr[s] + lane;
+  if (out64)
+    for (int q = 0; q < L; ++q) out64[sb + (int64_t)q * FG_SLICE] = (double)acc[q * bs];
+  if (out32)
+    for (int q = 0; q < L; ++q) out32[sb + (int64_t)q * FG_SLICE] = (float)acc[q * bs];
+  if (outcsr) {
+    int rb = rowptr[i], len = rowptr[i + 1] - rb;
+    for (int q = 0; q < len; ++q) outcsr[rb + q] = (double)acc[q * bs];
+  }
+  double d = (double)acc[dk * bs];
+  double di = (apply_bc && fx) ? 0.0 : (d != 0.0 ? 1.0 / d : 0.0);
+  if (dinv64) dinv64[i] = di;
+  if (dinv32) dinv32[i] = (float)di;
+}
+
+// ------------------------------------------------------------------ host side
+void fg_ensure_records(fg_mesh *m) {
+  if (!m->rec) m->rec = dev_alloc<double>(m, (size_t)m->ninc * m->npe);
+  if (!m->rec_r) m->rec_r = dev_alloc<double>(m, (size_t)m->ninc);
+}
+
+static void ensure_operator(fg_mesh *m, bool want64, bool want32) {
+  if (want64 && !m->val64) m->val64 = dev_alloc<double>(m, (size_t)m->nsell);
+  if (want32 && !m->val32) m->val32 = dev_alloc<float>(m, (size_t)m->nsell);
+  if (!m->dinv64) m->dinv64 = dev_alloc<double>(m, (size_t)m->nv);
+  if (!m->dinv32) m->dinv32 = dev_alloc<float>(m, (size_t)m->nv);
+}
+
+template <int NPE, typename R, typename A>
+static void launch_row(fg_mesh *m, const R *rec, const double *rec_r, int apply_bc, double *out64, float *out32,
+                       double *outcsr, double *dinv64, float *dinv32, double *vout, double vsign, int zero_fixed_vec) {
+  int L = std::max(m->maxrow, 1);
+  int block = (L * (int)sizeof(A) * 128 <= 48 * 1024) ? 128 : 64;
+  size_t smem = (size_t)block * L * sizeof(A);
+  auto kern = k_row_sum<NPE, R, A>;
+  if (smem > 48 * 1024) FG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  kern<<<grid_for(m->nv, block), block, smem, m->stream>>>(
+      m->nv, m->in_ptr, m->in_len, m->in_slot, rec, rec_r, m->sl_ptr, m->sl_len, m->rowptr, m->diagk,
+      m->has_fixed ? m->fixed : nullptr, apply_bc, out64, out32, outcsr, dinv64, dinv32, vout, vsign, zero_fixed_vec);
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(1);
+}
+
+template <typename R, typename A>
+static void launch_row_any(fg_mesh *m, const R *rec, const double *rec_r, int apply_bc, double *out64, float *out32,
+                           double *outcsr, double *dinv64, float *dinv32, double *vout, double vsign,
+                           int zero_fixed_vec) {
+  switch (m->npe) {
+    case 3: launch_row<3, R, A>(m, rec, rec_r, apply_bc, out64, out32, outcsr, dinv64, dinv32, vout, vsign, zero_fixed_vec); break;
+    case 4: launch_row<4, R, A>(m, rec, rec_r, apply_bc, out64, out32, outcsr, dinv64, dinv32, vout, vsign, zero_fixed_vec); break;
+    case 6: launch_row<6, R, A>(m, rec, rec_r, apply_bc, out64, out32, outcsr, dinv64, dinv32, vout, vsign, zero_fixed_vec); break;
+    default: launch_row<10, R, A>(m, rec, rec_r, apply_bc, out64, out32, outcsr, dinv64, dinv32, vout, vsign, zero_fixed_vec); break;
+  }
+}
+
+// Element pass (FP64 records) for the given kind.
+static void launch_elem(fg_mesh *m, int kind, const double *d_f, const double *d_H, const double *d_dmu, double cm,
+                        double cs, int full_phi) {
+  fg_ensure_records(m);
+  double *rec = static_cast<double *>(m->rec);
+  unsigned g = grid_for(m->nt, 128);
+  switch (m->npe) {
+    case 4: k_elem_tet4<double><<<g, 128, 0, m->stream>>>(kind, m->nt, m->geo, d_f, d_H, d_dmu, cm, cs, m->recpos, rec); break;
+    case 3:
+      FG_REQUIRE(kind != ASM_TANGENT, FG_UNSUPPORTED, "tangent stiffness is defined for tetrahedra");
+      k_elem_tri3<double><<<g, 128, 0, m->stream>>>(kind, m->nt, m->geo, d_f, cm, cs, m->recpos, rec);
+      break;
+    case 10:
+      FG_REQUIRE(kind == ASM_STIFF || kind == ASM_MASS, FG_UNSUPPORTED, "P2: stiffness and mass only");
+      k_elem_tet10<<<grid_for(m->nt, 64), 64, 0, m->stream>>>(kind, full_phi, m->nt, m->p, m->t, m->geo, d_f,
+                                                               m->recpos, rec, m->flags);
+      break;
+    default:
+      FG_REQUIRE(kind == ASM_STIFF || kind == ASM_MASS, FG_UNSUPPORTED, "P2: stiffness and mass only");
+      k_elem_tri6<<<grid_for(m->nt, 64), 64, 0, m->stream>>>(kind, m->nt, m->p, m->t, m->geo, d_f, m->recpos, rec,
+                                                              m->flags);
+      break;
+  }
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(1);
+}
+
+void fg_assemble_operator(fg_mesh *m, int kind, const double *d_f, const double *d_H, const double *d_dmu,
+                          double c_mass, double c_stiff, int full_phi, int layout, bool want64, bool want32,
+                          bool apply_bc) {
+  launch_elem(m, kind, d_f, d_H, d_dmu, c_mass, c_stiff, full_phi);
+  const double *rec = static_cast<const double *>(m->rec);
+  if (layout == OUT_CSR) {
+    if (!m->csrval) m->csrval = dev_alloc<double>(m, (size_t)m->nnz);
+    launch_row_any<double, double>(m, rec, nullptr, 0, nullptr, nullptr, m->csrval, nullptr, nullptr, nullptr, 0.0, 0);
+  } else {
+    ensure_operator(m, want64, want32);
+    launch_row_any<double, double>(m, rec, nullptr, apply_bc ? 1 : 0, want64 ? m->val64 : nullptr,
+                                   want32 ? m->val32 : nullptr, nullptr, m->dinv64, m->dinv32, nullptr, 0.0, 0);
+  }
+}
+
+void fg_newton_assemble(fg_mesh *m, const double *d_u, double Ms, double Hk, bool mixed, double *d_F) {
+  FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "Newton magnetostatics needs P1 tetrahedra");
+  fg_ensure_records(m);
+  ensure_operator(m, !mixed, mixed);
+  unsigned g = grid_for(m->nt, 128);
+  if (mixed) {
+    float *rec = static_cast<float *>(m->rec);
+    k_elem_newton<float><<<g, 128, 0, m->stream>>>(m->nt, m->geo, m->t, d_u, m->nl, m->mu_lin, Ms, Hk, m->recpos, rec,
+                                                   m->rec_r, m->mu, m->dmu, m->H, m->wdens, m->flags);
+    FG_CUDA_TRY(cudaGetLastError());
+    FG_LAUNCHED(1);
+    launch_row<4, float, float>(m, rec, m->rec_r, 1, nullptr, m->val32, nullptr, nullptr, m->dinv32, d_F, -1.0, 1);
+  } else {
+    double *rec = static_cast<double *>(m->rec);
+    k_elem_newton<double><<<g, 128, 0, m->stream>>>(m->nt, m->geo, m->t, d_u, m->nl, m->mu_lin, Ms, Hk, m->recpos,
+                                                    rec, m->rec_r, m->mu, m->dmu, m->H, m->wdens, m->flags);
+    FG_CUDA_TRY(cudaGetLastError());
+    FG_LAUNCHED(1);
+    launch_row<4, double, double>(m, rec, m->rec_r, 1, m->val64, nullptr, nullptr, m->dinv64, nullptr, d_F, -1.0, 1);
+  }
+}
+
+void fg_apply_operator_vec(fg_mesh *m, int kind, const double *d_coef, double c_mass, double c_stiff,
+                           const double *d_x, double *d_y, bool zero_fixed) {
+  FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "matrix-free apply needs P1 tetrahedra");
+  fg_ensure_records(m);
+  k_elem_apply_tet4<<<grid_for(m->nt, 128), 128, 0, m->stream>>>(kind, m->nt, m->geo, m->t, d_coef, c_mass, c_stiff,
+                                                                  d_x, m->recpos, m->rec_r);
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(1);
+  launch_row<4, double, double>(m, nullptr, m->rec_r, 0, nullptr, nullptr, nullptr, nullptr, nullptr, d_y, 1.0,
+                                zero_fixed ? 1 : 0);
+}
+
+void fg_hfield_dev(fg_mesh *m, const double *d_u, double *d_H) {
+  FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "H field needs P1 tetrahedra");
+  k_hfield_tet4<<<grid_for(m->nt, 256), 256, 0, m->stream>>>(m->nt, m->geo, m->t, d_u, d_H);
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(1);
+}
+
+// ------------------------------------------------------------------ C ABI
+static double *upload_opt(fg_mesh *m, const double *h, size_t n, double *&tmp) {
+  if (!h) return nullptr;
+  FG_CUDA_TRY(cudaMalloc(&tmp, sizeof(double) * n));
+  FG_CUDA_TRY(cudaMemcpyAsync(tmp, h, sizeof(double) * n, cudaMemcpyHostToDevice, m->stream));
+  return tmp;
+}
+
+static fg_status export_csr(fg_mesh *m, double *nzval, const char *where) {
+  FG_CUDA_TRY(cudaMemcpyAsync(nzval, m->csrval, sizeof(double) * (size_t)m->nnz, cudaMemcpyDeviceToHost, m->stream));
+  fg_sync(m);
+  fg_check_flags(m, where);
+  return FG_OK;
+}
+
+extern "C" fg_status fg_stiffness(fg_mesh *m, const double *f, double *nzval) {
+  double *tf = nullptr;
+  fg_status st = fg_guard([&]() -> fg_status {
+    FG_REQUIRE(m && nzval, FG_BAD_ARG, "fg_stiffness: null pointer");
+    double *df = upload_opt(m, f, (size_t)m->nt, tf);
+    fg_assemble_operator(m, ASM_STIFF, df, nullptr, nullptr, 0.0, 0.0, 0, OUT_CSR, false, false, false);
+    return export_csr(m, nzval, "fg_stiffness");
+  });
+  if (tf) cudaFree(tf);
+  return st;
+}
+
+extern "C" fg_status fg_mass(fg_mesh *m, const double *f, int32_t full_phi, double *nzval) {
+  double *tf = nullptr;
+  fg_status st = fg_guard([&]() -> fg_status {
+    FG_REQUIRE(m && nzval, FG_BAD_ARG, "fg_mass: null pointer");
+    double *df = upload_opt(m, f, (size_t)m->nt, tf);
+    fg_assemble_operator(m, ASM_MASS, df, nullptr, nullptr, 0.0, 0.0, full_phi, OUT_CSR, false, false, false);
+    return export_csr(m, nzval, "fg_mass");
+  });
+  if (tf) cudaFree(tf);
+  return st;
+}
+
+extern "C" fg_status fg_tangent(fg_mesh *m, const double *H, const double *dmu, double *nzval) {
+  double *tH = nullptr, *td = nullptr;
+  fg_status st = fg_guard([&]() -> fg_status {
+    FG_REQUIRE(m && H && dmu && nzval, FG_BAD_ARG, "fg_tangent: null pointer");
+    FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "fg_tangent: P1 tetrahedra only (src/FEM3D.jl:79-119)");
+    double *dH = upload_opt(m, H, 3 * (size_t)m->nt, tH);
+    double *dd = upload_opt(m, dmu, (size_t)m->nt, td);
+    fg_assemble_operator(m, ASM_TANGENT, nullptr, dH, dd, 0.0, 0.0, 0, OUT_CSR, false, false, false);
+    return export_csr(m, nzval, "fg_tangent");
+  });
+  if (tH) cudaFree(tH);
+  if (td) cudaFree(td);
+  return st;
+}
+
+__global__ void k_local_tet4(int64_t nt, const double *__restrict__ geo, const double *__restrict__ f,
+                             double *__restrict__ Ak) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt) return;
+  double g[4][3];
+  for (int c = 0; c < 12; ++c) g[c / 3][c % 3] = geo[(int64_t)c * nt + k];
+  double s = (f ? f[k] : 1.0) * geo[12 * nt + k];
+  for (int b = 0; b < 4; ++b)
+    for (int a = 0; a < 4; ++a) Ak[16 * k + 4 * b + a] = s * (g[a][0] * g[b][0] + g[a][1] * g[b][1] + g[a][2] * g[b][2]);
+}
+
+extern "C" fg_status fg_local_stiffness(fg_mesh *m, const double *f, double *Ak) {
+  double *tf = nullptr, *dA = nullptr;
+  fg_status st = fg_guard([&]() -> fg_status {
+    FG_REQUIRE(m && Ak, FG_BAD_ARG, "fg_local_stiffness: null pointer");
+    FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "fg_local_stiffness: P1 tetrahedra only");
+    double *df = upload_opt(m, f, (size_t)m->nt, tf);
+    FG_CUDA_TRY(cudaMalloc(&dA, sizeof(double) * 16 * (size_t)m->nt));
+    k_local_tet4<<<grid_for(m->nt, 256), 256, 0, m->stream>>>(m->nt, m->geo, df, dA);
+    FG_CUDA_TRY(cudaGetLastError());
+    FG_CUDA_TRY(cudaMemcpyAsync(Ak, dA, sizeof(double) * 16 * (size_t)m->nt, cudaMemcpyDeviceToHost, m->stream));
+    fg_sync(m);
+    return FG_OK;
+  });
+  if (tf) cudaFree(tf);
+  if (dA) cudaFree(dA);
+  return st;
+}

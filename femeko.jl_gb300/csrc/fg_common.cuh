@@ -1,0 +1,206 @@
+// Internal definitions shared by the translation units of libfemeko_gpu.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/femeko_gpu.h"
+
+#define FG_MU0 (3.14159265358979323846 * 4e-7)
+
+// ---------------------------------------------------------------- errors
+void fg_set_error(const std::string &msg);
+
+struct FgError {
+  fg_status code;
+  std::string msg;
+};
+
+#define FG_CUDA_TRY(call)                                                                    \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess)                                                                   \
+      throw FgError{FG_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)};            \
+  } while (0)
+
+#define FG_REQUIRE(cond, code, msg)                                                          \
+  do {                                                                                       \
+    if (!(cond)) throw FgError{code, msg};                                                   \
+  } while (0)
+
+// Runs body, converting exceptions into a status (nothing crosses the C ABI).
+template <class F>
+static inline fg_status fg_guard(F &&body) {
+  try {
+    return body();
+  } catch (const FgError &e) {
+    fg_set_error(e.msg);
+    return e.code;
+  } catch (const std::exception &e) {
+    fg_set_error(e.what());
+    return FG_CUDA;
+  } catch (...) {
+    fg_set_error("unknown error");
+    return FG_CUDA;
+  }
+}
+
+// ---------------------------------------------------------------- device flags
+enum {
+  FLAG_BAD_INDEX = 1,   // node index outside [0, nv)
+  FLAG_DEGENERATE = 2,  // zero-volume element
+  FLAG_ROW_OVERFLOW = 4,// a row longer than the supported maximum
+  FLAG_NAN = 8,         // NaN/Inf in a permeability or residual
+  FLAG_DUP_NODE = 16    // an element lists the same node twice
+};
+
+// Longest matrix row the pattern builder accepts (slot positions fit a byte).
+constexpr int FG_MAX_ROW = 255;
+constexpr int FG_SLICE = 32;  // rows per SELL slice
+constexpr int FG_RED_BLOCKS = 4096;
+
+// ---------------------------------------------------------------- device scratch
+// Scalars of one CG run (device doubles)
+enum {
+  S_RZ = 0,    // r.z
+  S_PQ,        // p.q
+  S_ALPHA,
+  S_BETA,
+  S_RR,        // r.r
+  S_BB,        // b.b
+  S_TOL2,      // stop when r.r <= TOL2
+  S_SCALE,     // mixed: scale applied to the FP64 residual before the FP32 solve
+  S_NSCAL = 16
+};
+enum { I_DONE = 0, I_ITERS, I_MAXIT, I_STATUS, I_NINT = 8 };
+
+// Reduction workspace: per-block partials and an arrival counter for the
+// "last block finishes the sum" pattern (the sum runs in block order, so results
+// do not depend on scheduling).
+struct RedWs {
+  double *partials;   // FG_RED_BLOCKS * 4
+  unsigned int *counter;
+};
+
+// A block of CG iterations captured as a CUDA graph.
+struct GraphCache {
+  cudaGraphExec_t exec = nullptr;
+  const void *key[8] = {nullptr};
+  int iters = 0;
+};
+
+struct fg_mesh {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+  int64_t nv = 0, nt = 0;
+  int npe = 0, dim = 0, nvert = 0;
+
+  // mesh on the device
+  double *p = nullptr;       // 3 x nv (AoS, as given)
+  int *t = nullptr;          // npe x nt stored SoA: t[a*nt + k]
+  uint8_t *fixed = nullptr;  // nv Dirichlet mask (0/1)
+  bool has_fixed = false;
+  double *geo = nullptr;     // P1: SoA per element, (nvert*dim gradients + volume) x nt
+  int ngeo = 0;
+
+  // CSR pattern (structural)
+  int *rowptr = nullptr;     // nv+1
+  int *colidx = nullptr;     // nnz
+  int64_t nnz = 0;
+  int maxrow = 0;
+
+  // SELL-32 matrix layout (rows in natural order, columns padded with the row itself)
+  int nslices = 0;
+  int *sl_ptr = nullptr;     // nslices+1 offsets into sl_col / values
+  int *sl_len = nullptr;     // nslices: longest row of the slice
+  int *sl_col = nullptr;     // nsell
+  int64_t nsell = 0;
+  uint8_t *diagk = nullptr;  // nv: position of the diagonal in its row
+  int *rowlen = nullptr;     // nv
+
+  // incidence (node -> element-local slot) in SELL-32 layout
+  int *in_ptr = nullptr;     // nslices+1
+  int *in_len = nullptr;     // nslices
+  int64_t ninc = 0;          // padded count
+  uint8_t *in_slot = nullptr;// ninc * npe slot positions (0xFF on pads)
+  int *recpos = nullptr;     // nt * npe (SoA: [a*nt + k]) -> incidence position
+  int maxdeg = 0;
+
+  // records written by the element kernels, summed by the row kernel
+  void *rec = nullptr;       // ninc * npe (double or float)
+  double *rec_r = nullptr;   // ninc vector records
+
+  // operator values (SELL layout) and Jacobi preconditioner
+  double *val64 = nullptr;
+  float *val32 = nullptr;
+  double *dinv64 = nullptr;
+  float *dinv32 = nullptr;
+  double *csrval = nullptr;  // nnz, export buffer
+
+  // per-element state (Newton)
+  double *mu = nullptr, *dmu = nullptr, *H = nullptr, *wdens = nullptr;
+  double *mu_lin = nullptr;
+  uint8_t *nl = nullptr;
+
+  // vectors
+  double *v64[12] = {nullptr};
+  float *v32[8] = {nullptr};
+
+  // reductions and CG control
+  RedWs red{};
+  double *scal = nullptr;     // S_NSCAL
+  int *ictl = nullptr;        // I_NINT
+  int *flags = nullptr;       // device error flags
+  double *hbuf = nullptr;     // pinned host mirror for small readbacks (64 doubles)
+  int *hint = nullptr;        // pinned host ints (16)
+
+  GraphCache graph[4];
+  std::vector<void *> extra;  // allocations released at destroy
+};
+
+// ---------------------------------------------------------------- helpers
+template <class T>
+static inline T *dev_alloc(fg_mesh *m, size_t count) {
+  void *ptr = nullptr;
+  if (count == 0) count = 1;
+  FG_CUDA_TRY(cudaMalloc(&ptr, count * sizeof(T)));
+  if (m) m->extra.push_back(ptr);
+  return static_cast<T *>(ptr);
+}
+
+static inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
+
+// Host-side count of kernel launches issued by this library (graph replays count
+// every kernel node).
+void fg_count_launch(long long n);
+#define FG_LAUNCHED(n) fg_count_launch(n)
+
+void fg_check_flags(fg_mesh *m, const char *where);
+void fg_sync(fg_mesh *m);
+
+// assembly (fg_assemble.cu)
+enum AsmKind { ASM_STIFF = 0, ASM_MASS = 1, ASM_TANGENT = 2, ASM_HEAT = 3 };
+enum OutLayout { OUT_SELL = 0, OUT_CSR = 1 };
+void fg_assemble_operator(fg_mesh *m, int kind, const double *d_f, const double *d_H, const double *d_dmu,
+                          double c_mass, double c_stiff, int full_phi, int layout, bool want64, bool want32,
+                          bool apply_bc);
+void fg_ensure_records(fg_mesh *m);
+void fg_newton_assemble(fg_mesh *m, const double *d_u, double Ms, double Hk, bool mixed, double *d_F);
+void fg_apply_operator_vec(fg_mesh *m, int kind, const double *d_coef, double c_mass, double c_stiff,
+                           const double *d_x, double *d_y, bool zero_fixed);
+void fg_hfield_dev(fg_mesh *m, const double *d_u, double *d_H);
+
+// solve (fg_solve.cu)
+double fg_norm2_dev(fg_mesh *m, const double *x, int64_t n, bool mask_fixed);
+double fg_dot_dev(fg_mesh *m, const double *x, const double *y, int64_t n, bool mask_fixed);
+// Solves A x = b (A = the handle's operator, SELL layout) on free rows.  b, x are FP64
+// device vectors; x holds the initial guess.  Returns iterations; stats filled.
+int fg_pcg_solve(fg_mesh *m, const double *d_b, double *d_x, const fg_solve_opts &o, fg_solve_stats *st,
+                 bool newton_inner);
+void fg_spmv64_dev(fg_mesh *m, const double *x, double *y);

@@ -1,0 +1,227 @@
+// Magnetostatic solvers on the P1 tetrahedral operator: the linear solve of
+// Magnetostatics/magneticField.jl:89-132 (and the ccall scalarPotential of
+// Femeko_jl_C++/Magnetostatics/magnetostatics.cpp:49-95) and the Newton-Raphson
+// iteration of Magnetostatics/NewtonRaphson.jl:109-214, both with Dirichlet rows.
+//
+// Newton step: the element pass computes H, mu, dmu, the residual F = -K(mu(u)) u and
+// the Jacobian K(mu) + At(H, dmu) in one launch; the row pass sums them.  The inner
+// increment solve J du = F runs to a relative residual inner_rtol in FP32 (mixed)
+// or FP64; F is always FP64, so the Newton loop is the iterative refinement.
+// Step control follows src/FEM3D.jl:123-152 (alpha = 1, 0.9, 0.81, ... while the
+// residual grows and alpha > min_step), applied either to the frozen secant
+// (FG_LS_REFERENCE, the reference's lineSearch) or to the true residual
+// (FG_LS_RESIDUAL).
+#include <cmath>
+#include <utility>
+
+#include "fg_common.cuh"
+
+__global__ void k_axpby64(int64_t n, double a, const double *__restrict__ x, double b, const double *__restrict__ y,
+                          double *__restrict__ out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = a * x[i] + b * y[i];
+}
+
+extern "C" void fg_newton_opts_default(fg_newton_opts *o) {
+  if (!o) return;
+  o->precision = FG_MIXED;
+  o->maxit = 100;
+  o->tol_update = 1e-8;
+  o->inner_rtol = 1e-4;
+  o->cg_maxiter = 200000;
+  o->line_search = FG_LS_RESIDUAL;
+  o->min_step = 1e-4;
+  o->Ms = 1.2e6;
+  o->Hk = 500.0;
+  o->check_every = 32;
+  o->use_graph = 1;
+}
+
+static void upload(fg_mesh *m, void *dst, const void *src, size_t bytes) {
+  FG_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, m->stream));
+}
+static void download(fg_mesh *m, void *dst, const void *src, size_t bytes) {
+  FG_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, m->stream));
+}
+static double *vec64(fg_mesh *m, int j) {
+  if (!m->v64[j]) m->v64[j] = dev_alloc<double>(m, (size_t)m->nv);
+  return m->v64[j];
+}
+
+static void ensure_element_state(fg_mesh *m) {
+  if (!m->mu) m->mu = dev_alloc<double>(m, (size_t)m->nt);
+  if (!m->dmu) m->dmu = dev_alloc<double>(m, (size_t)m->nt);
+  if (!m->H) m->H = dev_alloc<double>(m, 3 * (size_t)m->nt);
+  if (!m->wdens) m->wdens = dev_alloc<double>(m, (size_t)m->nt);
+  if (!m->mu_lin) m->mu_lin = dev_alloc<double>(m, (size_t)m->nt);
+  if (!m->nl) m->nl = dev_alloc<uint8_t>(m, (size_t)m->nt);
+}
+
+// Device-resident Newton solve; u (device) holds the initial guess and receives the
+// solution.  Element state (H, mu, dmu) is left at the solution.
+static int newton_dev(fg_mesh *m, double *d_u, const fg_newton_opts &o, fg_newton_stats *st) {
+  const bool mixed = o.precision == FG_MIXED;
+  double *d_du = vec64(m, 8), *d_F = vec64(m, 9), *d_ut = vec64(m, 10), *d_Ft = vec64(m, 11);
+  fg_solve_opts so;
+  fg_solve_opts_default(&so);
+  so.precision = o.precision;
+  so.inner_rtol = o.inner_rtol;
+  so.maxiter = o.cg_maxiter;
+  so.check_every = o.check_every;
+  so.use_graph = o.use_graph;
+  const int64_t nv = m->nv;
+  const unsigned g = grid_for(nv, 256);
+  cudaEvent_t e0, e1;
+  FG_CUDA_TRY(cudaEventCreate(&e0));
+  FG_CUDA_TRY(cudaEventCreate(&e1));
+  FG_CUDA_TRY(cudaEventRecord(e0, m->stream));
+
+  fg_newton_assemble(m, d_u, o.Ms, o.Hk, mixed, d_F);
+  fg_check_flags(m, "fg_newton_magnetostatics");
+  double rF = fg_norm2_dev(m, d_F, nv, true);
+  int it = 0, cg_total = 0, trials = 0, converged = 0, status = 0;
+  double ratio = 0.0, alpha = 0.0;
+  for (it = 1; it <= o.maxit; ++it) {
+    if (rF == 0.0) { converged = 1; ratio = 0.0; break; }
+    FG_CUDA_TRY(cudaMemsetAsync(d_du, 0, sizeof(double) * (size_t)nv, m->stream));
+    fg_solve_stats cst{};
+    fg_pcg_solve(m, d_F, d_du, so, &cst, true);
+    cg_total += cst.iterations;
+    alpha = 1.0;
+    if (o.line_search == FG_LS_RESIDUAL || o.line_search == FG_LS_NONE) {
+      double rt = 0.0;
+      for (;;) {
+        k_axpby64<<<g, 256, 0, m->stream>>>(nv, 1.0, d_u, alpha, d_du, d_ut);
+        FG_LAUNCHED(1);
+        fg_newton_assemble(m, d_ut, o.Ms, o.Hk, mixed, d_Ft);
+        rt = fg_norm2_dev(m, d_Ft, nv, true);
+        ++trials;
+        if (o.line_search == FG_LS_NONE || !(rt > rF && alpha > o.min_step)) break;
+        alpha *= 0.9;
+      }
+      if (alpha < o.min_step) {
+        // no decrease: keep u (src/FEM3D.jl:144-147) and restore the state at u
+        fg_newton_assemble(m, d_u, o.Ms, o.Hk, mixed, d_F);
+        status = 1;
+        alpha = 0.0;
+        break;
+      }
+      // accept: u <- ut, F <- Ft (copy keeps the caller's u buffer in place)
+      FG_CUDA_TRY(cudaMemcpyAsync(d_u, d_ut, sizeof(double) * (size_t)nv, cudaMemcpyDeviceToDevice, m->stream));
+      std::swap(m->v64[9], m->v64[11]);
+      d_F = m->v64[9];
+      d_Ft = m->v64[11];
+      rF = rt;
+    } else {
+      // reference lineSearch: w = K(mu) du with the secant at the current mu
+      double *w = d_Ft;
+      fg_apply_operator_vec(m, ASM_STIFF, m->mu, 0.0, 0.0, d_du, w, true);
+      double rt = 0.0;
+      for (;;) {
+        k_axpby64<<<g, 256, 0, m->stream>>>(nv, 1.0, d_F, -alpha, w, d_ut);
+        FG_LAUNCHED(1);
+        rt = fg_norm2_dev(m, d_ut, nv, true);
+        ++trials;
+        if (!(rt > rF && alpha > o.min_step)) break;
+        alpha *= 0.9;
+      }
+      if (alpha < o.min_step) { status = 1; alpha = 0.0; break; }
+      k_axpby64<<<g, 256, 0, m->stream>>>(nv, 1.0, d_u, alpha, d_du, d_u);
+      FG_LAUNCHED(1);
+      fg_newton_assemble(m, d_u, o.Ms, o.Hk, mixed, d_F);
+      rF = fg_norm2_dev(m, d_F, nv, true);
+    }
+    fg_check_flags(m, "fg_newton_magnetostatics");
+    double dn = alpha * fg_norm2_dev(m, d_du, nv, false);
+    double un = fg_norm2_dev(m, d_u, nv, false);
+    ratio = (un > 0.0) ? dn / un : dn;
+    if (!std::isfinite(ratio)) throw FgError{FG_NAN, "Newton update is not finite"};
+    if (ratio <= o.tol_update) { converged = 1; break; }
+  }
+  double energy = fg_dot_dev(m, m->wdens, nullptr, m->nt, false);
+  FG_CUDA_TRY(cudaEventRecord(e1, m->stream));
+  fg_sync(m);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) {
+    st->newton_iters = std::min(it, o.maxit);
+    st->cg_iters = cg_total;
+    st->converged = converged;
+    st->trials = trials;
+    st->update_ratio = ratio;
+    st->residual = rF;
+    st->alpha = alpha;
+    st->energy = energy;
+    st->ms = ms;
+  }
+  (void)status;
+  return converged ? 0 : 1;
+}
+
+extern "C" fg_status fg_newton_magnetostatics(fg_mesh *m, const uint8_t *nl, const double *mu_lin, const double *u0,
+                                              const fg_newton_opts *o, double *u, double *H, double *mu,
+                                              fg_newton_stats *s) {
+  return fg_guard([&]() -> fg_status {
+    FG_REQUIRE(m && nl && mu_lin && u0 && u, FG_BAD_ARG, "fg_newton_magnetostatics: null pointer");
+    FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "fg_newton_magnetostatics: P1 tetrahedra only");
+    fg_newton_opts opts;
+    fg_newton_opts_default(&opts);
+    if (o) opts = *o;
+    FG_REQUIRE(opts.Hk > 0.0 && opts.tol_update > 0.0 && opts.maxit > 0, FG_BAD_ARG,
+               "fg_newton_magnetostatics: bad options");
+    ensure_element_state(m);
+    upload(m, m->nl, nl, (size_t)m->nt);
+    upload(m, m->mu_lin, mu_lin, sizeof(double) * (size_t)m->nt);
+    double *d_u = vec64(m, 7);
+    upload(m, d_u, u0, sizeof(double) * (size_t)m->nv);
+    int rc = newton_dev(m, d_u, opts, s);
+    download(m, u, d_u, sizeof(double) * (size_t)m->nv);
+    if (H) download(m, H, m->H, sizeof(double) * 3 * (size_t)m->nt);
+    if (mu) download(m, mu, m->mu, sizeof(double) * (size_t)m->nt);
+    fg_sync(m);
+    return rc == 0 ? FG_OK : FG_NOT_CONVERGED;
+  });
+}
+
+extern "C" fg_status fg_magnetostatics_linear(fg_mesh *m, const double *mu, const double *u_in,
+                                              const fg_solve_opts *o, double *u, double *H, fg_solve_stats *s) {
+  return fg_guard([&]() -> fg_status {
+    FG_REQUIRE(m && mu && u_in && u, FG_BAD_ARG, "fg_magnetostatics_linear: null pointer");
+    FG_REQUIRE(m->npe == 4 || m->npe == 3, FG_UNSUPPORTED, "fg_magnetostatics_linear: P1 elements only");
+    fg_solve_opts opts;
+    fg_solve_opts_default(&opts);
+    if (o) opts = *o;
+    ensure_element_state(m);
+    upload(m, m->mu_lin, mu, sizeof(double) * (size_t)m->nt);
+    const bool mixed = opts.precision == FG_MIXED;
+    fg_assemble_operator(m, ASM_STIFF, m->mu_lin, nullptr, nullptr, 0.0, 0.0, 0, OUT_SELL, true, mixed, true);
+    double *d_x = vec64(m, 7), *d_b = vec64(m, 9);
+    upload(m, d_x, u_in, sizeof(double) * (size_t)m->nv);
+    FG_CUDA_TRY(cudaMemsetAsync(d_b, 0, sizeof(double) * (size_t)m->nv, m->stream));
+    int status = fg_pcg_solve(m, d_b, d_x, opts, s, false);
+    download(m, u, d_x, sizeof(double) * (size_t)m->nv);
+    if (H) {
+      FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "H output: P1 tetrahedra only");
+      fg_hfield_dev(m, d_x, m->H);
+      download(m, H, m->H, sizeof(double) * 3 * (size_t)m->nt);
+    }
+    fg_sync(m);
+    fg_check_flags(m, "fg_magnetostatics_linear");
+    return status == 0 ? FG_OK : FG_NOT_CONVERGED;
+  });
+}
+
+extern "C" fg_status fg_hfield(fg_mesh *m, const double *u, double *H) {
+  return fg_guard([&]() -> fg_status {
+    FG_REQUIRE(m && u && H, FG_BAD_ARG, "fg_hfield: null pointer");
+    ensure_element_state(m);
+    double *d_u = vec64(m, 7);
+    upload(m, d_u, u, sizeof(double) * (size_t)m->nv);
+    fg_hfield_dev(m, d_u, m->H);
+    download(m, H, m->H, sizeof(double) * 3 * (size_t)m->nt);
+    fg_sync(m);
+    return FG_OK;
+  });
+}

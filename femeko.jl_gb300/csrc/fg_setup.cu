@@ -1,0 +1,507 @@
+// Mesh upload, structural pattern, element-to-slot map and P1 geometry.
+//
+// The reference rebuilds its sparse structure on every assembly: 16 (36, 100)
+// COO->CSC passes in src/FEM3D.jl:47-53 and one sparse(I,J,V) per Newton step in
+// Magnetostatics/NewtonRaphson.jl:115-161.  Here the pattern is built once per mesh
+// on the GPU and every later assembly writes values straight into it:
+//
+//   * incidence lists node -> (element, local node), sorted by (element, local);
+//   * the structural CSR pattern (all element node pairs, rows sorted, the pattern
+//     sparse(I,J,V) keeps), plus the same rows in SELL-32 layout (slices of 32 rows
+//     stored column-major, so a warp reads 32 consecutive entries);
+//   * for every incidence, the position of each element node inside the row
+//     (one byte per node) and, per (element, local node), the incidence position
+//     the element kernels write their local row to;
+//   * per element the gradients of the P1 (barycentric) basis and the volume,
+//     computed once in FP64 from the inverse Jacobian.  The reference solves a
+//     4x4 (3x3) Vandermonde system per node instead (src/FEM3D.jl:5-17,
+//     src/FEM2D.jl:5-25); the coefficients are the same functions.
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+
+#include "fg_common.cuh"
+
+#include <atomic>
+static std::atomic<long long> g_launches{0};
+void fg_count_launch(long long n) { g_launches += n; }
+extern "C" int64_t fg_kernel_launches(void) { return g_launches.load(); }
+
+static thread_local std::string g_err;
+void fg_set_error(const std::string &msg) { g_err = msg; }
+
+extern "C" const char *fg_last_error(void) { return g_err.c_str(); }
+extern "C" int32_t fg_version(void) { return 10; }
+
+extern "C" fg_status fg_device_info(char *name, int32_t name_len, int32_t *sm_count) {
+  return fg_guard([&]() -> fg_status {
+    int dev = 0;
+    FG_CUDA_TRY(cudaGetDevice(&dev));
+    cudaDeviceProp prop;
+    FG_CUDA_TRY(cudaGetDeviceProperties(&prop, dev));
+    if (name && name_len > 0) {
+      strncpy(name, prop.name, (size_t)name_len - 1);
+      name[name_len - 1] = 0;
+    }
+    if (sm_count) *sm_count = prop.multiProcessorCount;
+    return FG_OK;
+  });
+}
+
+void fg_sync(fg_mesh *m) { FG_CUDA_TRY(cudaStreamSynchronize(m->stream)); }
+
+void fg_check_flags(fg_mesh *m, const char *where) {
+  int h = 0;
+  FG_CUDA_TRY(cudaMemcpyAsync(&h, m->flags, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
+  fg_sync(m);
+  if (!h) return;
+  FG_CUDA_TRY(cudaMemsetAsync(m->flags, 0, sizeof(int), m->stream));
+  std::string w(where);
+  if (h & FLAG_BAD_INDEX) throw FgError{FG_BAD_MESH, w + ": node index out of range"};
+  if (h & FLAG_DUP_NODE) throw FgError{FG_BAD_MESH, w + ": an element repeats a node"};
+  if (h & FLAG_DEGENERATE) throw FgError{FG_BAD_MESH, w + ": degenerate (zero-volume) element"};
+  if (h & FLAG_ROW_OVERFLOW) throw FgError{FG_BAD_MESH, w + ": a matrix row exceeds 255 entries"};
+  if (h & FLAG_NAN) throw FgError{FG_NAN, w + ": NaN/Inf in permeability or residual"};
+  throw FgError{FG_BAD_MESH, w + ": device error flag"};
+}
+
+// ------------------------------------------------------------------ kernels
+// t (npe x nt, column-major, index_base) -> SoA 0-based, with range checks.
+__global__ void k_convert_t(const int32_t *__restrict__ traw, int *__restrict__ t, int64_t nt, int npe, int64_t nv,
+                            int base, int *flags) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt) return;
+  int nodes[10];
+  int bad = 0;
+  for (int a = 0; a < npe; ++a) {
+    int v = traw[k * npe + a] - base;
+    if (v < 0 || v >= nv) { bad |= FLAG_BAD_INDEX; v = 0; }
+    nodes[a] = v;
+    t[(int64_t)a * nt + k] = v;
+  }
+  for (int a = 0; a < npe; ++a)
+    for (int b = a + 1; b < npe; ++b)
+      if (nodes[a] == nodes[b]) bad |= FLAG_DUP_NODE;
+  if (bad) atomicOr(flags, bad);
+}
+
+__global__ void k_count_deg(const int *__restrict__ t, int64_t nt, int npe, int *__restrict__ deg) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt) return;
+  for (int a = 0; a < npe; ++a) atomicAdd(&deg[t[(int64_t)a * nt + k]], 1);
+}
+
+__global__ void k_fill_inc(const int *__restrict__ t, int64_t nt, int npe, const int *__restrict__ iptr,
+                           int *__restrict__ cursor, int *__restrict__ inc) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt) return;
+  for (int a = 0; a < npe; ++a) {
+    int v = t[(int64_t)a * nt + k];
+    int pos = iptr[v] + atomicAdd(&cursor[v], 1);
+    inc[pos] = (int)(k * npe + a);
+  }
+}
+
+// Sort each node's incidence list by (element, local) so that every later pass
+// visits contributions in one fixed order (deterministic sums).
+__global__ void k_sort_inc(const int *__restrict__ iptr, int *__restrict__ inc, int64_t nv) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nv) return;
+  int b = iptr[i], e = iptr[i + 1];
+  for (int q = b + 1; q < e; ++q) {
+    int key = inc[q];
+    int r = q - 1;
+    while (r >= b && inc[r] > key) { inc[r + 1] = inc[r]; --r; }
+    inc[r + 1] = key;
+  }
+}
+
+// Sorted unique neighbour set of node i (the nodes of its incident elements).
+template <int CAP>
+__device__ int gather_row(int64_t i, const int *__restrict__ iptr, const int *__restrict__ inc,
+                          const int *__restrict__ t, int64_t nt, int npe, int *nb, int *flags) {
+  int len = 0;
+  for (int q = iptr[i]; q < iptr[i + 1]; ++q) {
+    int key = inc[q];
+    int64_t k = key / npe;
+    for (int a = 0; a < npe; ++a) {
+      int v = t[(int64_t)a * nt + k];
+      // binary search for v in nb[0, len)
+      int lo = 0, hi = len;
+      while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (nb[mid] < v) lo = mid + 1; else hi = mid;
+      }
+      if (lo < len && nb[lo] == v) continue;
+      if (len >= CAP) { atomicOr(flags, FLAG_ROW_OVERFLOW); return len; }
+      for (int r = len; r > lo; --r) nb[r] = nb[r - 1];
+      nb[lo] = v;
+      ++len;
+    }
+  }
+  return len;
+}
+
+template <int CAP>
+__global__ void k_row_count(const int *__restrict__ iptr, const int *__restrict__ inc, const int *__restrict__ t,
+                            int64_t nt, int npe, int64_t nv, int *__restrict__ rowlen, int *flags) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nv) return;
+  int nb[CAP];
+  rowlen[i] = gather_row<CAP>(i, iptr, inc, t, nt, npe, nb, flags);
+}
+
+template <int CAP>
+__global__ void k_row_fill(const int *__restrict__ iptr, const int *__restrict__ inc, const int *__restrict__ t,
+                           int64_t nt, int npe, int64_t nv, const int *__restrict__ rowptr,
+                           const int *__restrict__ sl_ptr, const int *__restrict__ sl_len, int *__restrict__ colidx,
+                           int *__restrict__ sl_col, uint8_t *__restrict__ diagk, int *flags) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nv) return;
+  int nb[CAP];
+  int len = gather_row<CAP>(i, iptr, inc, t, nt, npe, nb, flags);
+  int rb = rowptr[i];
+  int s = (int)(i / FG_SLICE), lane = (int)(i % FG_SLICE);
+  int sb = sl_ptr[s] + lane, sl = sl_len[s];
+  int dk = 0;
+  for (int k = 0; k < len; ++k) {
+    colidx[rb + k] = nb[k];
+    sl_col[sb + k * FG_SLICE] = nb[k];
+    if (nb[k] == (int)i) dk = k;
+  }
+  for (int k = len; k < sl; ++k) sl_col[sb + k * FG_SLICE] = (int)i;
+  diagk[i] = (uint8_t)dk;
+}
+
+// Incidence in SELL layout: record position per (element, local node) and the
+// slot (position in the row) of each node of the element.
+__global__ void k_slots(const int *__restrict__ iptr, const int *__restrict__ inc, const int *__restrict__ t,
+                        int64_t nt, int npe, int64_t nv, const int *__restrict__ rowptr,
+                        const int *__restrict__ colidx, const int *__restrict__ in_ptr, const int *__restrict__ in_len,
+                        int *__restrict__ recpos, uint8_t *__restrict__ in_slot) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nv) return;
+  int s = (int)(i / FG_SLICE), lane = (int)(i % FG_SLICE);
+  int base = in_ptr[s] + lane, ilen = in_len[s];
+  int rb = rowptr[i], re = rowptr[i + 1];
+  int deg = iptr[i + 1] - iptr[i];
+  for (int m = 0; m < ilen; ++m) {
+    int64_t pos = base + (int64_t)m * FG_SLICE;
+    if (m >= deg) {
+      for (int j = 0; j < npe; ++j) in_slot[pos * npe + j] = 0xFF;
+      continue;
+    }
+    int key = inc[iptr[i] + m];
+    int64_t k = key / npe;
+    int a = key % npe;
+    recpos[(int64_t)a * nt + k] = (int)pos;
+    for (int j = 0; j < npe; ++j) {
+      int v = t[(int64_t)j * nt + k];
+      int lo = rb, hi = re;
+      while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (colidx[mid] < v) lo = mid + 1; else hi = mid;
+      }
+      in_slot[pos * npe + j] = (uint8_t)(lo - rb);
+    }
+  }
+}
+
+// P1 tetrahedron geometry from the inverse Jacobian (FP64): gradients of the four
+// barycentric functions (12 values) and the volume |det J| / 6
+// (src/mesh.jl:484-505).  SoA: geo[c*nt + k], c = 3*a + d for gradients, 12 = volume.
+__global__ void k_geom_tet(const double *__restrict__ p, const int *__restrict__ t, int64_t nt,
+                           double *__restrict__ geo, int *flags) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt) return;
+  int n0 = t[k], n1 = t[nt + k], n2 = t[2 * nt + k], n3 = t[3 * nt + k];
+  double x0 = p[3 * n0], y0 = p[3 * n0 + 1], z0 = p[3 * n0 + 2];
+  double a1 = p[3 * n1] - x0, a2 = p[3 * n2] - x0, a3 = p[3 * n3] - x0;
+  double b1 = p[3 * n1 + 1] - y0, b2 = p[3 * n2 + 1] - y0, b3 = p[3 * n3 + 1] - y0;
+  double c1 = p[3 * n1 + 2] - z0, c2 = p[3 * n2 + 2] - z0, c3 = p[3 * n3 + 2] - z0;
+  // J = [a1 a2 a3; b1 b2 b3; c1 c2 c3] (columns = edges); rows of J^-1 are the
+  // gradients of lambda_1..3.
+  double C11 = b2 * c3 - b3 * c2, C12 = b3 * c1 - b1 * c3, C13 = b1 * c2 - b2 * c1;
+  double C21 = a3 * c2 - a2 * c3, C22 = a1 * c3 - a3 * c1, C23 = a2 * c1 - a1 * c2;
+  double C31 = a2 * b3 - a3 * b2, C32 = a3 * b1 - a1 * b3, C33 = a1 * b2 - a2 * b1;
+  double det = a1 * C11 + a2 * C12 + a3 * C13;
+  if (det == 0.0) { atomicOr(flags, FLAG_DEGENERATE); det = 1.0; }
+  double inv = 1.0 / det;
+  // grad lambda_1 = (C11, C21, C31)/det, lambda_2 = (C12, C22, C32)/det, lambda_3 = (C13, C23, C33)/det
+  double g1x = C11 * inv, g1y = C21 * inv, g1z = C31 * inv;
+  double g2x = C12 * inv, g2y = C22 * inv, g2z = C32 * inv;
+  double g3x = C13 * inv, g3y = C23 * inv, g3z = C33 * inv;
+  geo[0 * nt + k] = -(g1x + g2x + g3x);
+  geo[1 * nt + k] = -(g1y + g2y + g3y);
+  geo[2 * nt + k] = -(g1z + g2z + g3z);
+  geo[3 * nt + k] = g1x; geo[4 * nt + k] = g1y; geo[5 * nt + k] = g1z;
+  geo[6 * nt + k] = g2x; geo[7 * nt + k] = g2y; geo[8 * nt + k] = g2z;
+  geo[9 * nt + k] = g3x; geo[10 * nt + k] = g3y; geo[11 * nt + k] = g3z;
+  geo[12 * nt + k] = fabs(det) / 6.0;
+}
+
+// P1 triangle geometry: gradients of the three barycentric functions (6 values)
+// and the area |det J| / 2.  geo[c*nt + k], c = 2*a + d, 6 = area.
+__global__ void k_geom_tri(const double *__restrict__ p, const int *__restrict__ t, int64_t nt,
+                           double *__restrict__ geo, int *flags) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt) return;
+  int n0 = t[k], n1 = t[nt + k], n2 = t[2 * nt + k];
+  double x0 = p[3 * n0], y0 = p[3 * n0 + 1];
+  double a1 = p[3 * n1] - x0, a2 = p[3 * n2] - x0;
+  double b1 = p[3 * n1 + 1] - y0, b2 = p[3 * n2 + 1] - y0;
+  double det = a1 * b2 - a2 * b1;
+  if (det == 0.0) { atomicOr(flags, FLAG_DEGENERATE); det = 1.0; }
+  double inv = 1.0 / det;
+  double g1x = b2 * inv, g1y = -a2 * inv;
+  double g2x = -b1 * inv, g2y = a1 * inv;
+  geo[0 * nt + k] = -(g1x + g2x);
+  geo[1 * nt + k] = -(g1y + g2y);
+  geo[2 * nt + k] = g1x; geo[3 * nt + k] = g1y;
+  geo[4 * nt + k] = g2x; geo[5 * nt + k] = g2y;
+  geo[6 * nt + k] = 0.5 * fabs(det);
+}
+
+// ------------------------------------------------------------------ host side
+static void exclusive_scan_host(const std::vector<int> &in, std::vector<int64_t> &out) {
+  out.resize(in.size() + 1);
+  out[0] = 0;
+  for (size_t i = 0; i < in.size(); ++i) out[i + 1] = out[i] + in[i];
+}
+
+static void free_mesh(fg_mesh *m) {
+  if (!m) return;
+  for (int g = 0; g < 4; ++g)
+    if (m->graph[g].exec) cudaGraphExecDestroy(m->graph[g].exec);
+  for (void *ptr : m->extra) cudaFree(ptr);
+  if (m->hbuf) cudaFreeHost(m->hbuf);
+  if (m->hint) cudaFreeHost(m->hint);
+  if (m->ev0) cudaEventDestroy(m->ev0);
+  if (m->ev1) cudaEventDestroy(m->ev1);
+  if (m->stream) cudaStreamDestroy(m->stream);
+  delete m;
+}
+
+extern "C" fg_status fg_mesh_create(const double *p, int64_t nv, const int32_t *t, int64_t nt,
+                                    int32_t nodes_per_elem, int32_t index_base, fg_mesh **out) {
+  fg_mesh *m = nullptr;
+  fg_status st = fg_guard([&]() -> fg_status {
+    FG_REQUIRE(out != nullptr && p != nullptr && t != nullptr, FG_BAD_ARG, "fg_mesh_create: null pointer");
+    *out = nullptr;
+    int npe = nodes_per_elem;
+    FG_REQUIRE(npe == 3 || npe == 4 || npe == 6 || npe == 10, FG_BAD_ARG,
+               "fg_mesh_create: nodes_per_elem must be 3, 4, 6 or 10");
+    FG_REQUIRE(index_base == 0 || index_base == 1, FG_BAD_ARG, "fg_mesh_create: index_base must be 0 or 1");
+    FG_REQUIRE(nv > 0 && nt > 0, FG_BAD_ARG, "fg_mesh_create: empty mesh");
+    FG_REQUIRE(nv < (int64_t)1 << 30 && nt * npe < (int64_t)1 << 31, FG_BAD_ARG, "fg_mesh_create: mesh too large");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) throw FgError{FG_NO_DEVICE, "no CUDA device"};
+    m = new fg_mesh();
+    FG_CUDA_TRY(cudaGetDevice(&m->device));
+    FG_CUDA_TRY(cudaDeviceGetAttribute(&m->sm_count, cudaDevAttrMultiProcessorCount, m->device));
+    FG_CUDA_TRY(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
+    FG_CUDA_TRY(cudaEventCreate(&m->ev0));
+    FG_CUDA_TRY(cudaEventCreate(&m->ev1));
+    m->nv = nv;
+    m->nt = nt;
+    m->npe = npe;
+    m->dim = (npe == 3 || npe == 6) ? 2 : 3;
+    m->nvert = m->dim + 1;
+    cudaStream_t s = m->stream;
+
+    m->flags = dev_alloc<int>(m, 4);
+    FG_CUDA_TRY(cudaMemsetAsync(m->flags, 0, 4 * sizeof(int), s));
+    m->p = dev_alloc<double>(m, 3 * (size_t)nv);
+    FG_CUDA_TRY(cudaMemcpyAsync(m->p, p, sizeof(double) * 3 * (size_t)nv, cudaMemcpyHostToDevice, s));
+    int32_t *traw = nullptr;
+    FG_CUDA_TRY(cudaMalloc(&traw, sizeof(int32_t) * (size_t)nt * npe));
+    FG_CUDA_TRY(cudaMemcpyAsync(traw, t, sizeof(int32_t) * (size_t)nt * npe, cudaMemcpyHostToDevice, s));
+    m->t = dev_alloc<int>(m, (size_t)nt * npe);
+    k_convert_t<<<grid_for(nt, 256), 256, 0, s>>>(traw, m->t, nt, npe, nv, index_base, m->flags);
+    FG_CUDA_TRY(cudaGetLastError());
+    fg_check_flags(m, "fg_mesh_create");
+    cudaFree(traw);
+
+    // incidence lists
+    int *deg = nullptr, *cursor = nullptr, *iptr = nullptr, *inc = nullptr;
+    FG_CUDA_TRY(cudaMalloc(&deg, sizeof(int) * (size_t)nv));
+    FG_CUDA_TRY(cudaMemsetAsync(deg, 0, sizeof(int) * (size_t)nv, s));
+    k_count_deg<<<grid_for(nt, 256), 256, 0, s>>>(m->t, nt, npe, deg);
+    std::vector<int> hdeg(nv);
+    FG_CUDA_TRY(cudaMemcpyAsync(hdeg.data(), deg, sizeof(int) * (size_t)nv, cudaMemcpyDeviceToHost, s));
+    fg_sync(m);
+    std::vector<int64_t> hiptr;
+    exclusive_scan_host(hdeg, hiptr);
+    std::vector<int> hiptr32(nv + 1);
+    for (int64_t i = 0; i <= nv; ++i) hiptr32[i] = (int)hiptr[i];
+    m->maxdeg = *std::max_element(hdeg.begin(), hdeg.end());
+    FG_CUDA_TRY(cudaMalloc(&iptr, sizeof(int) * (size_t)(nv + 1)));
+    FG_CUDA_TRY(cudaMalloc(&inc, sizeof(int) * (size_t)nt * npe));
+    FG_CUDA_TRY(cudaMemcpyAsync(iptr, hiptr32.data(), sizeof(int) * (size_t)(nv + 1), cudaMemcpyHostToDevice, s));
+    cursor = deg;
+    FG_CUDA_TRY(cudaMemsetAsync(cursor, 0, sizeof(int) * (size_t)nv, s));
+    k_fill_inc<<<grid_for(nt, 256), 256, 0, s>>>(m->t, nt, npe, iptr, cursor, inc);
+    k_sort_inc<<<grid_for(nv, 128), 128, 0, s>>>(iptr, inc, nv);
+    FG_CUDA_TRY(cudaGetLastError());
+
+    // row lengths of the structural pattern
+    m->rowlen = dev_alloc<int>(m, (size_t)nv);
+    int cap_needed = std::min<int64_t>((int64_t)m->maxdeg * npe, FG_MAX_ROW);
+    bool big = cap_needed > 128;
+    if (big)
+      k_row_count<FG_MAX_ROW><<<grid_for(nv, 64), 64, 0, s>>>(iptr, inc, m->t, nt, npe, nv, m->rowlen, m->flags);
+    else
+      k_row_count<128><<<grid_for(nv, 128), 128, 0, s>>>(iptr, inc, m->t, nt, npe, nv, m->rowlen, m->flags);
+    FG_CUDA_TRY(cudaGetLastError());
+    fg_check_flags(m, "fg_mesh_create");
+    std::vector<int> hrl(nv);
+    FG_CUDA_TRY(cudaMemcpyAsync(hrl.data(), m->rowlen, sizeof(int) * (size_t)nv, cudaMemcpyDeviceToHost, s));
+    fg_sync(m);
+    std::vector<int64_t> hrowptr;
+    exclusive_scan_host(hrl, hrowptr);
+    m->nnz = hrowptr[nv];
+    FG_REQUIRE(m->nnz < ((int64_t)1 << 31), FG_BAD_ARG, "fg_mesh_create: pattern too large");
+    m->maxrow = *std::max_element(hrl.begin(), hrl.end());
+    std::vector<int> hrp32(nv + 1);
+    for (int64_t i = 0; i <= nv; ++i) hrp32[i] = (int)hrowptr[i];
+
+    // SELL-32 slices for the matrix and for the incidence records
+    m->nslices = (int)((nv + FG_SLICE - 1) / FG_SLICE);
+    std::vector<int> hsl_len(m->nslices), hin_len(m->nslices), hsl_ptr(m->nslices + 1), hin_ptr(m->nslices + 1);
+    int64_t acc = 0, acc2 = 0;
+    for (int sl = 0; sl < m->nslices; ++sl) {
+      int mx = 0, md = 0;
+      for (int64_t r = (int64_t)sl * FG_SLICE; r < std::min<int64_t>(nv, (int64_t)(sl + 1) * FG_SLICE); ++r) {
+        mx = std::max(mx, hrl[r]);
+        md = std::max(md, hdeg[r]);
+      }
+      hsl_len[sl] = mx;
+      hin_len[sl] = md;
+      hsl_ptr[sl] = (int)acc;
+      hin_ptr[sl] = (int)acc2;
+      acc += (int64_t)mx * FG_SLICE;
+      acc2 += (int64_t)md * FG_SLICE;
+      FG_REQUIRE(acc < ((int64_t)1 << 31) && acc2 * npe < ((int64_t)1 << 31), FG_BAD_ARG,
+                 "fg_mesh_create: padded layout too large");
+    }
+    hsl_ptr[m->nslices] = (int)acc;
+    hin_ptr[m->nslices] = (int)acc2;
+    m->nsell = acc;
+    m->ninc = acc2;
+
+    m->rowptr = dev_alloc<int>(m, (size_t)nv + 1);
+    m->colidx = dev_alloc<int>(m, (size_t)m->nnz);
+    m->sl_ptr = dev_alloc<int>(m, (size_t)m->nslices + 1);
+    m->sl_len = dev_alloc<int>(m, (size_t)m->nslices);
+    m->sl_col = dev_alloc<int>(m, (size_t)m->nsell);
+    m->diagk = dev_alloc<uint8_t>(m, (size_t)nv);
+    m->in_ptr = dev_alloc<int>(m, (size_t)m->nslices + 1);
+    m->in_len = dev_alloc<int>(m, (size_t)m->nslices);
+    m->in_slot = dev_alloc<uint8_t>(m, (size_t)m->ninc * npe);
+    m->recpos = dev_alloc<int>(m, (size_t)nt * npe);
+    FG_CUDA_TRY(cudaMemcpyAsync(m->rowptr, hrp32.data(), sizeof(int) * (size_t)(nv + 1), cudaMemcpyHostToDevice, s));
+    FG_CUDA_TRY(cudaMemcpyAsync(m->sl_ptr, hsl_ptr.data(), sizeof(int) * (m->nslices + 1), cudaMemcpyHostToDevice, s));
+    FG_CUDA_TRY(cudaMemcpyAsync(m->sl_len, hsl_len.data(), sizeof(int) * m->nslices, cudaMemcpyHostToDevice, s));
+    FG_CUDA_TRY(cudaMemcpyAsync(m->in_ptr, hin_ptr.data(), sizeof(int) * (m->nslices + 1), cudaMemcpyHostToDevice, s));
+    FG_CUDA_TRY(cudaMemcpyAsync(m->in_len, hin_len.data(), sizeof(int) * m->nslices, cudaMemcpyHostToDevice, s));
+    if (big)
+      k_row_fill<FG_MAX_ROW><<<grid_for(nv, 64), 64, 0, s>>>(iptr, inc, m->t, nt, npe, nv, m->rowptr, m->sl_ptr,
+                                                             m->sl_len, m->colidx, m->sl_col, m->diagk, m->flags);
+    else
+      k_row_fill<128><<<grid_for(nv, 128), 128, 0, s>>>(iptr, inc, m->t, nt, npe, nv, m->rowptr, m->sl_ptr,
+                                                         m->sl_len, m->colidx, m->sl_col, m->diagk, m->flags);
+    k_slots<<<grid_for(nv, 128), 128, 0, s>>>(iptr, inc, m->t, nt, npe, nv, m->rowptr, m->colidx, m->in_ptr,
+                                              m->in_len, m->recpos, m->in_slot);
+    FG_CUDA_TRY(cudaGetLastError());
+
+    // geometry of the vertex simplex
+    m->ngeo = (m->dim == 3) ? 13 : 7;
+    m->geo = dev_alloc<double>(m, (size_t)m->ngeo * nt);
+    if (m->dim == 3)
+      k_geom_tet<<<grid_for(nt, 256), 256, 0, s>>>(m->p, m->t, nt, m->geo, m->flags);
+    else
+      k_geom_tri<<<grid_for(nt, 256), 256, 0, s>>>(m->p, m->t, nt, m->geo, m->flags);
+    FG_CUDA_TRY(cudaGetLastError());
+    fg_check_flags(m, "fg_mesh_create");
+    cudaFree(deg);
+    cudaFree(iptr);
+    cudaFree(inc);
+
+    // control and reduction workspace
+    m->red.partials = dev_alloc<double>(m, ((size_t)grid_for(nv, 256) + FG_RED_BLOCKS) * 4);
+    m->red.counter = dev_alloc<unsigned int>(m, 16);
+    FG_CUDA_TRY(cudaMemsetAsync(m->red.counter, 0, 16 * sizeof(unsigned int), s));
+    m->scal = dev_alloc<double>(m, S_NSCAL);
+    m->ictl = dev_alloc<int>(m, I_NINT);
+    FG_CUDA_TRY(cudaMallocHost(&m->hbuf, 64 * sizeof(double)));
+    FG_CUDA_TRY(cudaMallocHost(&m->hint, 16 * sizeof(int)));
+    fg_sync(m);
+    *out = m;
+    m = nullptr;
+    return FG_OK;
+  });
+  if (m) free_mesh(m);
+  return st;
+}
+
+extern "C" fg_status fg_mesh_destroy(fg_mesh *m) {
+  return fg_guard([&]() -> fg_status {
+    if (!m) return FG_OK;
+    cudaStreamSynchronize(m->stream);
+    free_mesh(m);
+    return FG_OK;
+  });
+}
+
+extern "C" fg_status fg_mesh_nnz(const fg_mesh *m, int64_t *nnz, int32_t *max_row) {
+  return fg_guard([&]() -> fg_status {
+    FG_REQUIRE(m != nullptr, FG_BAD_ARG, "fg_mesh_nnz: null handle");
+    if (nnz) *nnz = m->nnz;
+    if (max_row) *max_row = m->maxrow;
+    return FG_OK;
+  });
+}
+
+extern "C" fg_status fg_mesh_set_dirichlet(fg_mesh *m, const uint8_t *fixed) {
+  return fg_guard([&]() -> fg_status {
+    FG_REQUIRE(m != nullptr, FG_BAD_ARG, "fg_mesh_set_dirichlet: null handle");
+    if (!m->fixed) m->fixed = dev_alloc<uint8_t>(m, (size_t)m->nv);
+    if (fixed) {
+      FG_CUDA_TRY(cudaMemcpyAsync(m->fixed, fixed, (size_t)m->nv, cudaMemcpyHostToDevice, m->stream));
+      m->has_fixed = true;
+    } else {
+      FG_CUDA_TRY(cudaMemsetAsync(m->fixed, 0, (size_t)m->nv, m->stream));
+      m->has_fixed = false;
+    }
+    fg_sync(m);
+    return FG_OK;
+  });
+}
+
+extern "C" fg_status fg_mesh_volumes(fg_mesh *m, double *VE) {
+  return fg_guard([&]() -> fg_status {
+    FG_REQUIRE(m != nullptr && VE != nullptr, FG_BAD_ARG, "fg_mesh_volumes: null pointer");
+    int c = (m->dim == 3) ? 12 : 6;
+    FG_CUDA_TRY(cudaMemcpyAsync(VE, m->geo + (size_t)c * m->nt, sizeof(double) * (size_t)m->nt,
+                                cudaMemcpyDeviceToHost, m->stream));
+    fg_sync(m);
+    return FG_OK;
+  });
+}
+
+extern "C" fg_status fg_csc_pattern(const fg_mesh *mc, int64_t *colptr, int32_t *rowval, int32_t index_base) {
+  return fg_guard([&]() -> fg_status {
+    fg_mesh *m = const_cast<fg_mesh *>(mc);
+    FG_REQUIRE(m != nullptr && colptr != nullptr && rowval != nullptr, FG_BAD_ARG, "fg_csc_pattern: null pointer");
+    FG_REQUIRE(index_base == 0 || index_base == 1, FG_BAD_ARG, "fg_csc_pattern: index_base must be 0 or 1");
+    std::vector<int> rp(m->nv + 1);
+    FG_CUDA_TRY(cudaMemcpyAsync(rp.data(), m->rowptr, sizeof(int) * (size_t)(m->nv + 1), cudaMemcpyDeviceToHost,
+                                m->stream));
+    FG_CUDA_TRY(cudaMemcpyAsync(rowval, m->colidx, sizeof(int) * (size_t)m->nnz, cudaMemcpyDeviceToHost, m->stream));
+    fg_sync(m);
+    for (int64_t i = 0; i <= m->nv; ++i) colptr[i] = rp[i] + index_base;
+    if (index_base)
+      for (int64_t q = 0; q < m->nnz; ++q) rowval[q] += 1;
+    return FG_OK;
+  });
+}

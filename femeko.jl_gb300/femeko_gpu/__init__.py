@@ -1,0 +1,225 @@
+"""Host-side mirror of Femeko's FEM hot-path interface on top of libfemeko_gpu.so.
+
+Names, argument meaning and return types follow the reference functions, so a
+script written against the reference reads the same:
+
+==============================  =============================================  ==========================
+this module                     reference (Femeko.jl)                          returns
+==============================  =============================================  ==========================
+stiffnessMatrix(mesh, f)        src/FEM3D.jl:40-56                             scipy CSC (SparseMatrixCSC)
+localStiffnessMatrix(mesh, f)   src/FEM3D.jl:59-76                             (16, nt) ndarray
+tangentialStiffnessMatrix       src/FEM3D.jl:79-119                            scipy CSC
+massMatrix(mesh)                src/FEM3D.jl:466-492                           scipy CSC
+stiffnessMatrix2D / massMatrix2D  src/FEM2D.jl:48-76, 139-161                  scipy CSC
+quadraticStiffnessMatrix        src/FEM3D.jl:378-395                           scipy CSC
+quadraticMassMatrix             src/FEM3D.jl:494-561                           scipy CSC
+quadraticStiffnessMatrix2D      src/FEM2D.jl:117-137                           scipy CSC
+quadraticMassMatrix2D           src/FEM2D.jl:163-229                           scipy CSC
+cg(A, b)                        IterativeSolvers.cg (e.g. run.jl:141)          ndarray
+magnetostatics_linear           Magnetostatics/magneticField.jl:89-132         (u, H, stats)
+newton_magnetostatics           Magnetostatics/NewtonRaphson.jl:109-214        (u, H, mu, stats)
+hfield(mesh, u)                 Magnetostatics/magneticField.jl:111-124        (3, nt) ndarray
+==============================  =============================================  ==========================
+
+The mesh argument is a :class:`femeko_gpu.mesh.MESH` (the reference struct's fields).
+The first GPU call on a mesh uploads it and builds the sparse pattern once; the
+device handle is cached on the mesh object.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import scipy.sparse as sp
+
+from . import _lib as L
+from .mesh import MESH, MU0, box_tet_mesh, box_tri_mesh  # noqa: F401
+
+__all__ = [
+    "GPUMesh", "gpu_mesh", "stiffnessMatrix", "localStiffnessMatrix", "tangentialStiffnessMatrix", "massMatrix",
+    "stiffnessMatrix2D", "massMatrix2D", "quadraticStiffnessMatrix", "quadraticMassMatrix",
+    "quadraticStiffnessMatrix2D", "quadraticMassMatrix2D", "cg", "spmv", "magnetostatics_linear",
+    "newton_magnetostatics", "hfield", "solve_opts", "newton_opts", "MESH", "MU0", "box_tet_mesh", "box_tri_mesh",
+]
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+class GPUMesh:
+    """Owns one fg_mesh handle: the mesh, its pattern and its work buffers on the GPU."""
+
+    def __init__(self, mesh: MESH, dirichlet: bool = True):
+        lib = L.lib()
+        self.mesh = mesh
+        self._p = _c(mesh.p.T, np.float64)          # 3 x nv column-major
+        self._t = _c(mesh.t.T, np.int32)            # npe x nt column-major
+        h = C.c_void_p()
+        L.check(lib.fg_mesh_create(L.ptr(self._p), mesh.nv, L.ptr(self._t), mesh.nt, mesh.npe, 0, C.byref(h)))
+        self.h = h
+        nnz, mr = C.c_int64(), C.c_int32()
+        L.check(lib.fg_mesh_nnz(h, C.byref(nnz), C.byref(mr)))
+        self.nnz, self.max_row = nnz.value, mr.value
+        colptr = np.zeros(mesh.nv + 1, dtype=np.int64)
+        rowval = np.zeros(self.nnz, dtype=np.int32)
+        L.check(lib.fg_csc_pattern(h, L.ptr(colptr), L.ptr(rowval), 0))
+        self.colptr, self.rowval = colptr, rowval
+        if dirichlet and mesh.boundary_nodes is not None:
+            self.set_dirichlet(mesh.dirichlet_mask())
+
+    def set_dirichlet(self, fixed):
+        f = None if fixed is None else _c(fixed, np.uint8)
+        L.check(L.lib().fg_mesh_set_dirichlet(self.h, L.ptr(f)))
+
+    def volumes(self):
+        VE = np.zeros(self.mesh.nt)
+        L.check(L.lib().fg_mesh_volumes(self.h, L.ptr(VE)))
+        return VE
+
+    def csc(self, vals):
+        n = self.mesh.nv
+        return sp.csc_matrix((vals, self.rowval.copy(), self.colptr.copy()), shape=(n, n))
+
+    def close(self):
+        if getattr(self, "h", None):
+            L.lib().fg_mesh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def gpu_mesh(mesh: MESH) -> GPUMesh:
+    g = getattr(mesh, "_gpu", None)
+    if g is None or g.h is None:
+        g = GPUMesh(mesh)
+        object.__setattr__(mesh, "_gpu", g)
+    return g
+
+
+def _assemble(mesh, fn, *args):
+    g = gpu_mesh(mesh)
+    vals = np.zeros(g.nnz)
+    L.check(fn(g.h, *args, L.ptr(vals)))
+    return g.csc(vals)
+
+
+def stiffnessMatrix(mesh: MESH, f=None):
+    """Global stiffness matrix; P1/P2, tetrahedra or triangles by ``mesh.t``'s rows."""
+    fv = None if f is None else _c(f, np.float64)
+    return _assemble(mesh, L.lib().fg_stiffness, L.ptr(fv))
+
+
+stiffnessMatrix2D = stiffnessMatrix
+quadraticStiffnessMatrix = stiffnessMatrix
+quadraticStiffnessMatrix2D = stiffnessMatrix
+
+
+def massMatrix(mesh: MESH, F=None, full_phi: bool = False):
+    """Global mass matrix.  For P2 tetrahedra ``full_phi=False`` reproduces the
+    reference's linear-part-only basis evaluation (src/FEM3D.jl:529-531)."""
+    fv = None if F is None else _c(F, np.float64)
+    return _assemble(mesh, L.lib().fg_mass, L.ptr(fv), int(full_phi))
+
+
+massMatrix2D = massMatrix
+quadraticMassMatrix = massMatrix
+quadraticMassMatrix2D = massMatrix
+
+
+def tangentialStiffnessMatrix(mesh: MESH, H_vec, dmu):
+    H = _c(np.asarray(H_vec, dtype=np.float64).T, np.float64)   # 3 x nt column-major
+    d = _c(dmu, np.float64)
+    return _assemble(mesh, L.lib().fg_tangent, L.ptr(H), L.ptr(d))
+
+
+def localStiffnessMatrix(mesh: MESH, f=None):
+    g = gpu_mesh(mesh)
+    fv = None if f is None else _c(f, np.float64)
+    Ak = np.zeros(16 * mesh.nt)
+    L.check(L.lib().fg_local_stiffness(g.h, L.ptr(fv), L.ptr(Ak)))
+    return Ak.reshape(mesh.nt, 16).T
+
+
+def solve_opts(precision="fp64", rtol=1e-10, maxiter=1_000_000, inner_rtol=1e-5, check_every=32, use_graph=True):
+    o = L.SolveOpts()
+    L.lib().fg_solve_opts_default(C.byref(o))
+    o.precision = L.FG_MIXED if precision == "mixed" else L.FG_FP64
+    o.rtol, o.maxiter, o.inner_rtol = rtol, maxiter, inner_rtol
+    o.check_every, o.use_graph = check_every, int(use_graph)
+    return o
+
+
+def newton_opts(precision="mixed", tol_update=1e-8, maxit=100, inner_rtol=1e-4, cg_maxiter=200_000,
+                line_search="residual", min_step=1e-4, Ms=1.2e6, Hk=500.0, check_every=32, use_graph=True):
+    o = L.NewtonOpts()
+    L.lib().fg_newton_opts_default(C.byref(o))
+    o.precision = L.FG_MIXED if precision == "mixed" else L.FG_FP64
+    o.tol_update, o.maxit, o.inner_rtol, o.cg_maxiter = tol_update, maxit, inner_rtol, cg_maxiter
+    o.line_search = {"none": L.FG_LS_NONE, "reference": L.FG_LS_REFERENCE, "residual": L.FG_LS_RESIDUAL}[line_search]
+    o.min_step, o.Ms, o.Hk, o.check_every, o.use_graph = min_step, Ms, Hk, check_every, int(use_graph)
+    return o
+
+
+def cg(A, b, x0=None, reltol=1e-10, maxiter=1_000_000, precision="fp64", return_stats=False, **kw):
+    """Jacobi-preconditioned CG on a symmetric sparse matrix (IterativeSolvers.cg drop-in)."""
+    A = sp.csc_matrix(A)
+    n = A.shape[0]
+    colptr = _c(A.indptr, np.int64)
+    rowval = _c(A.indices, np.int64)
+    nz = _c(A.data, np.float64)
+    x = np.zeros(n) if x0 is None else _c(x0, np.float64).copy()
+    o = solve_opts(precision=precision, rtol=reltol, maxiter=maxiter, **kw)
+    s = L.SolveStats()
+    st = L.lib().fg_cg_csc(n, L.ptr(colptr), L.ptr(rowval), L.ptr(nz), 0, L.ptr(_c(b, np.float64)), L.ptr(x),
+                           C.byref(o), C.byref(s))
+    L.check(st, allow_not_converged=True)
+    return (x, L.stats_dict(s)) if return_stats else x
+
+
+def spmv(A, x):
+    A = sp.csc_matrix(A)
+    n = A.shape[0]
+    y = np.zeros(n)
+    L.check(L.lib().fg_spmv_csc(n, L.ptr(_c(A.indptr, np.int64)), L.ptr(_c(A.indices, np.int64)),
+                                L.ptr(_c(A.data, np.float64)), 0, L.ptr(_c(x, np.float64)), L.ptr(y)))
+    return y
+
+
+def magnetostatics_linear(mesh: MESH, mu, u_in, precision="fp64", rtol=1e-10, **kw):
+    """K(mu) u = 0 on interior rows with u = u_in on the Dirichlet rows."""
+    g = gpu_mesh(mesh)
+    u = np.zeros(mesh.nv)
+    H = np.zeros(3 * mesh.nt)
+    o = solve_opts(precision=precision, rtol=rtol, **kw)
+    s = L.SolveStats()
+    st = L.lib().fg_magnetostatics_linear(g.h, L.ptr(_c(mu, np.float64)), L.ptr(_c(u_in, np.float64)), C.byref(o),
+                                          L.ptr(u), L.ptr(H), C.byref(s))
+    L.check(st, allow_not_converged=True)
+    return u, H.reshape(mesh.nt, 3).T, L.stats_dict(s)
+
+
+def newton_magnetostatics(mesh: MESH, nl, mu_lin, u0, **kw):
+    """Nonlinear Newton-Raphson magnetostatics; returns (u, H, mu, stats)."""
+    g = gpu_mesh(mesh)
+    u = np.zeros(mesh.nv)
+    H = np.zeros(3 * mesh.nt)
+    mu = np.zeros(mesh.nt)
+    o = newton_opts(**kw)
+    s = L.NewtonStats()
+    st = L.lib().fg_newton_magnetostatics(g.h, L.ptr(_c(nl, np.uint8)), L.ptr(_c(mu_lin, np.float64)),
+                                          L.ptr(_c(u0, np.float64)), C.byref(o), L.ptr(u), L.ptr(H), L.ptr(mu),
+                                          C.byref(s))
+    L.check(st, allow_not_converged=True)
+    return u, H.reshape(mesh.nt, 3).T, mu, L.stats_dict(s)
+
+
+def hfield(mesh: MESH, u):
+    g = gpu_mesh(mesh)
+    H = np.zeros(3 * mesh.nt)
+    L.check(L.lib().fg_hfield(g.h, L.ptr(_c(u, np.float64)), L.ptr(H)))
+    return H.reshape(mesh.nt, 3).T

@@ -1,0 +1,199 @@
+/*
+ * femeko_gpu.h -- C ABI of libfemeko_gpu.so, the GB300 (sm_103a) engine for
+ * Femeko's FEM hot path: P1/P2 tetrahedral and triangle assembly, the nonlinear
+ * permeability / Newton-tangent rebuild, and the sparse CG solve.
+ *
+ * Conventions
+ *  - Plain pointers and sizes only.  Host pointers are caller-owned and are read
+ *    or written before the call returns.  Device memory is owned by the handle.
+ *  - Arrays use Julia's column-major layouts: p is 3 x nv (p[3*i + c]),
+ *    t is npe x nt (t[npe*k + a]), H is 3 x nt.  index_base (0 or 1) lets Julia
+ *    pass mesh.t (Int32, 1-based) without a copy.
+ *  - Sparse matrices are SparseMatrixCSC-compatible: colptr (nv+1), rowval (nnz),
+ *    nzval (nnz), rows sorted within each column.  Every matrix here is
+ *    symmetric, so the same arrays are also its CSR form.
+ *  - Every function returns an fg_status; nothing throws across the ABI.
+ *    fg_last_error() describes the last failure on the calling thread.
+ *  - One handle per thread; calls on one handle are serialised on its stream.
+ *
+ * Reference interfaces each entry point replaces are cited as file:line of the
+ * Femeko.jl repository.
+ */
+#ifndef FEMEKO_GPU_H
+#define FEMEKO_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum fg_status {
+  FG_OK = 0,
+  FG_NOT_CONVERGED = 1, /* iteration cap reached; outputs hold the last iterate */
+  FG_NAN = 2,           /* a NaN/Inf appeared (Magnetostatics/NewtonRaphson.jl:210-212) */
+  FG_BAD_ARG = 3,
+  FG_BAD_MESH = 4,      /* node index out of range, degenerate element, row too long */
+  FG_CUDA = 5,
+  FG_NO_DEVICE = 6,
+  FG_UNSUPPORTED = 7
+} fg_status;
+
+/* element kinds = nodes per element */
+enum { FG_TRI3 = 3, FG_TET4 = 4, FG_TRI6 = 6, FG_TET10 = 10 };
+/* precision of a solve */
+enum { FG_FP64 = 0, FG_MIXED = 1 };
+/* Newton step control */
+enum {
+  FG_LS_NONE = 0,      /* full step */
+  FG_LS_REFERENCE = 1, /* src/FEM3D.jl:123-152: backtracking on ||RHS - A(u+a du)|| with the frozen secant A */
+  FG_LS_RESIDUAL = 2   /* same backtracking rule on the true nonlinear residual */
+};
+/* SpMV kernel selection */
+enum { FG_SPMV_AUTO = 0, FG_SPMV_SELL = 1, FG_SPMV_CSR_VECTOR = 2 };
+
+typedef struct fg_mesh fg_mesh;
+
+typedef struct fg_solve_opts {
+  int32_t precision;   /* FG_FP64 or FG_MIXED (FP32 matrix/vectors, FP64 refinement) */
+  double rtol;         /* FP64 relative residual target ||b - A x|| <= rtol ||b|| */
+  int32_t maxiter;     /* cap on CG iterations (inner iterations in total) */
+  double inner_rtol;   /* mixed: FP32 PCG target per refinement step */
+  int32_t check_every; /* iterations per graph launch between convergence checks (even) */
+  int32_t use_graph;   /* 1: replay each block of iterations as a CUDA graph */
+  int32_t spmv;        /* FG_SPMV_* */
+  int32_t rows_per_warp; /* CSR vector kernel: 1, 2, 4 or 8 rows per warp */
+} fg_solve_opts;
+
+typedef struct fg_solve_stats {
+  int32_t iterations;  /* CG iterations (all refinement steps) */
+  int32_t refinements; /* FP64 refinement steps (mixed) */
+  int32_t converged;
+  int32_t pad_;
+  double relres;       /* final FP64 relative residual */
+  double ms;           /* device time of the solve (CUDA events) */
+} fg_solve_stats;
+
+typedef struct fg_newton_opts {
+  int32_t precision;   /* inner CG precision: FG_FP64 or FG_MIXED */
+  int32_t maxit;       /* Newton iteration cap (Magnetostatics/NewtonRaphson.jl:38: 100) */
+  double tol_update;   /* stop when ||a du|| <= tol_update ||u|| */
+  double inner_rtol;   /* relative residual of each inner (increment) solve */
+  int32_t cg_maxiter;  /* inner CG cap per Newton step */
+  int32_t line_search; /* FG_LS_* */
+  double min_step;     /* smallest accepted step (src/FEM3D.jl:123: 1e-4) */
+  double Ms, Hk;       /* Froehlich law mu(H) = mu0 (1 + Ms/(Hk + |H|)) */
+  int32_t check_every;
+  int32_t use_graph;
+} fg_newton_opts;
+
+typedef struct fg_newton_stats {
+  int32_t newton_iters;
+  int32_t cg_iters;
+  int32_t converged;
+  int32_t trials;      /* line-search trials in total */
+  double update_ratio; /* last ||a du|| / ||u|| */
+  double residual;     /* last ||F|| on free rows */
+  double alpha;        /* last accepted step */
+  double energy;       /* integral of H dB (src/magneticProperties.jl:252-309, closed form) */
+  double ms;           /* device time of the solve */
+} fg_newton_stats;
+
+/* Defaults matching the reference behaviour / the published path settings. */
+void fg_solve_opts_default(fg_solve_opts *o);
+void fg_newton_opts_default(fg_newton_opts *o);
+
+const char *fg_last_error(void);
+int32_t fg_version(void);
+/* Name and SM count of the current CUDA device. */
+fg_status fg_device_info(char *name, int32_t name_len, int32_t *sm_count);
+
+/* ---------------------------------------------------------------------- mesh */
+/* Uploads a mesh and builds, once, the structural CSR pattern (all element node
+ * pairs, as the single sparse(I,J,V) of Magnetostatics/NewtonRaphson.jl:161),
+ * the element-to-slot map and the P1 geometry.  Replaces the index work of
+ * Magnetostatics/NewtonRaphson.jl:115-127 and the per-call abcd solves of
+ * src/FEM3D.jl:5-17.  nodes_per_elem: 4 (P1 tet), 3 (P1 tri), 10 (P2 tet),
+ * 6 (P2 tri).  p is 3 x nv (z ignored for triangles). */
+fg_status fg_mesh_create(const double *p, int64_t nv, const int32_t *t, int64_t nt, int32_t nodes_per_elem,
+                         int32_t index_base, fg_mesh **out);
+fg_status fg_mesh_destroy(fg_mesh *m);
+/* nnz of the structural pattern and the longest row. */
+fg_status fg_mesh_nnz(const fg_mesh *m, int64_t *nnz, int32_t *max_row);
+/* Dirichlet rows (fixed[i] != 0); NULL clears. */
+fg_status fg_mesh_set_dirichlet(fg_mesh *m, const uint8_t *fixed);
+/* Element volumes (areas for triangles): src/mesh.jl:484-505 elementVolume. */
+fg_status fg_mesh_volumes(fg_mesh *m, double *VE);
+/* Pattern in SparseMatrixCSC form (colptr nv+1, rowval nnz) with the given base. */
+fg_status fg_csc_pattern(const fg_mesh *m, int64_t *colptr, int32_t *rowval, int32_t index_base);
+
+/* ------------------------------------------------------------------ assembly */
+/* Values in the order of fg_csc_pattern (nnz doubles). */
+/* src/FEM3D.jl:40-56 stiffnessMatrix, src/FEM2D.jl:48-76 stiffnessMatrix2D,
+ * src/FEM3D.jl:378-395 quadraticStiffnessMatrix, src/FEM2D.jl:117-137
+ * quadraticStiffnessMatrix2D.  f: per-element coefficient (NULL = ones). */
+fg_status fg_stiffness(fg_mesh *m, const double *f, double *nzval);
+/* src/FEM3D.jl:466-492 massMatrix, src/FEM2D.jl:139-161 massMatrix2D,
+ * src/FEM3D.jl:494-561 quadraticMassMatrix (full_phi = 0 reproduces the
+ * reference's linear-part-only phi of :529-531, 1 evaluates the full quadratic),
+ * src/FEM2D.jl:163-229 quadraticMassMatrix2D.  f: per-element factor or NULL. */
+fg_status fg_mass(fg_mesh *m, const double *f, int32_t full_phi, double *nzval);
+/* src/FEM3D.jl:79-119 tangentialStiffnessMatrix (P1 tet): H is 3 x nt, dmu nt.
+ * Where |H| = 0 the stored term is its limit 0. */
+fg_status fg_tangent(fg_mesh *m, const double *H, const double *dmu, double *nzval);
+/* src/FEM3D.jl:59-76 localStiffnessMatrix: Ak (npe*npe x nt, column k holds the
+ * element matrix in column-major order). */
+fg_status fg_local_stiffness(fg_mesh *m, const double *f, double *Ak);
+
+/* ------------------------------------------------------------------- solvers */
+/* Drop-in for IterativeSolvers.cg(A, b) (Magnetostatics/2DmagneticField.jl:139,
+ * Micromagnetics/LL.jl:185, Femeko_jl_C++/Magnetostatics/run.jl:141) and Eigen's
+ * ConjugateGradient (Femeko_jl_C++/Magnetostatics/magnetostatics.cpp:26-38) on a
+ * symmetric SparseMatrixCSC{Float64,Int64}: Jacobi-preconditioned CG.
+ * x holds the initial guess on entry. */
+fg_status fg_cg_csc(int64_t n, const int64_t *colptr, const int64_t *rowval, const double *nzval, int32_t index_base,
+                    const double *b, double *x, const fg_solve_opts *o, fg_solve_stats *s);
+/* y = A x for the same CSC input (one call = upload + SpMV + download). */
+fg_status fg_spmv_csc(int64_t n, const int64_t *colptr, const int64_t *rowval, const double *nzval,
+                      int32_t index_base, const double *x, double *y);
+
+/* Linear magnetostatics (Magnetostatics/magneticField.jl:89-132 and
+ * Femeko_jl_C++/Magnetostatics/magnetostatics.cpp:49-95 scalarPotential) with the
+ * Dirichlet rows set by fg_mesh_set_dirichlet: K(mu) u = 0 on free rows, u fixed
+ * to u_in on Dirichlet rows (u_in also seeds the free rows).  mu is absolute
+ * permeability per element.  H (3 x nt) may be NULL. */
+fg_status fg_magnetostatics_linear(fg_mesh *m, const double *mu, const double *u_in, const fg_solve_opts *o,
+                                   double *u, double *H, fg_solve_stats *s);
+/* Nonlinear Newton-Raphson magnetostatics (Magnetostatics/NewtonRaphson.jl:109-214):
+ * nl[k] != 0 marks Froehlich elements, the others use mu_lin[k]; u0 gives the
+ * Dirichlet values and the initial guess.  Outputs u (nv), H (3 x nt), mu (nt);
+ * H and mu may be NULL. */
+fg_status fg_newton_magnetostatics(fg_mesh *m, const uint8_t *nl, const double *mu_lin, const double *u0,
+                                   const fg_newton_opts *o, double *u, double *H, double *mu, fg_newton_stats *s);
+/* H = -sum u_a grad(phi_a) per element (Magnetostatics/magneticField.jl:111-124). */
+fg_status fg_hfield(fg_mesh *m, const double *u, double *H);
+
+/* One call from host arrays, the shape of the ccall boundary scalarPotential
+ * (Femeko_jl_C++/Magnetostatics/magnetostatics.cpp:49-95, called from
+ * Femeko_jl_C++/Magnetostatics/run.jl:66-79) for the Newton solve of
+ * Magnetostatics/NewtonRaphson.jl:109-214: uploads the P1 mesh (p 3 x nv, t 4 x nt),
+ * builds the pattern, solves, downloads u/H/mu and releases the device memory.
+ * fixed marks Dirichlet nodes (u0 holds their values). */
+fg_status fg_scalar_potential_newton(const double *p, int64_t nv, const int32_t *t, int64_t nt, int32_t index_base,
+                                     const uint8_t *fixed, const uint8_t *nl, const double *mu_lin, const double *u0,
+                                     const fg_newton_opts *o, double *u, double *H, double *mu, fg_newton_stats *s);
+
+/* ------------------------------------------------------------- diagnostics */
+/* Kernel launches issued by this library so far (graph replays count every node). */
+int64_t fg_kernel_launches(void);
+/* Average device time of one launch of a hot kernel on the handle's current
+ * operator: which = 0 CG SpMV, 1 CG vector update, 2 Newton element pass + row
+ * gather.  No reference counterpart (used for roofline reporting). */
+fg_status fg_bench_kernel(fg_mesh *m, int32_t which, int32_t precision, int32_t reps, double *ms_per_launch);
+/* Padded sizes of the device layouts: SELL-32 matrix entries, incidence records, slices. */
+fg_status fg_mesh_layout(const fg_mesh *m, int64_t *nsell, int64_t *ninc, int32_t *nslices);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FEMEKO_GPU_H */

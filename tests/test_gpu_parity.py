@@ -1,0 +1,154 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle.
+
+Bar: sparse patterns bit-exact (structural pattern of sparse(I,J,V)); FP64 values
+within 1e-12 relative to the largest entry; solves within the stated tolerances.
+"""
+import numpy as np
+import pytest
+
+import femeko_gpu as fg
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+REL_VAL = 1e-12
+
+
+def rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def same_pattern(A, B):
+    return np.array_equal(A.indptr, B.indptr) and np.array_equal(A.indices, B.indices)
+
+
+@pytest.fixture(scope="module")
+def tet():
+    return fg.box_tet_mesh(6, seed=5)
+
+
+def test_stiffness_p1(tet):
+    f = np.random.default_rng(1).uniform(0.5, 2.0, tet.nt)
+    Kg, Ko = fg.stiffnessMatrix(tet, f), O.stiffnessMatrix(tet, f)
+    assert same_pattern(Kg, Ko)
+    assert rel(Kg.data, Ko.data) < REL_VAL
+
+
+def test_stiffness_unjittered_pattern_and_zeros():
+    m = fg.box_tet_mesh(3, seed=0, jitter=0.0)
+    Kg, Ko = fg.stiffnessMatrix(m), O.stiffnessMatrix(m)
+    assert same_pattern(Kg, Ko)
+    assert rel(Kg.data, Ko.data) < REL_VAL
+    # entries that the chained sparse `+` of src/FEM3D.jl:51 would drop
+    Kd = O.stiffnessMatrix(m, drop_zeros=True)
+    Kg2 = Kg.copy()
+    Kg2.data[np.abs(Kg2.data) <= 1e-14 * np.abs(Kg2.data).max()] = 0.0
+    Kg2.eliminate_zeros()
+    assert same_pattern(Kg2, Kd)
+
+
+def test_mass_tangent_local(tet):
+    Mg, Mo = fg.massMatrix(tet), O.massMatrix(tet)
+    assert same_pattern(Mg, Mo) and rel(Mg.data, Mo.data) < REL_VAL
+    rng = np.random.default_rng(2)
+    H = rng.normal(size=(3, tet.nt)) * 1e3
+    H[:, :5] = 0.0  # |H| = 0 elements: the limit 0 is stored
+    dmu = -rng.uniform(1e-10, 1e-9, tet.nt)
+    Tg, To = fg.tangentialStiffnessMatrix(tet, H, dmu), O.tangentialStiffnessMatrix(tet, H, dmu)
+    assert same_pattern(Tg, To) and rel(Tg.data, To.data) < REL_VAL
+    Ag, Ao = fg.localStiffnessMatrix(tet), O.localStiffnessMatrix(tet)
+    assert rel(Ag, Ao) < REL_VAL
+    assert rel(fg.gpu_mesh(tet).volumes(), tet.VE) < 1e-14
+
+
+def test_p1_triangles():
+    m = fg.box_tri_mesh(7, seed=3)
+    mu = np.random.default_rng(3).uniform(1, 3, m.nt)
+    Kg, Ko = fg.stiffnessMatrix2D(m, mu), O.stiffnessMatrix2D(m, mu)
+    assert same_pattern(Kg, Ko) and rel(Kg.data, Ko.data) < REL_VAL
+    Mg, Mo = fg.massMatrix2D(m), O.massMatrix2D(m)
+    assert same_pattern(Mg, Mo) and rel(Mg.data, Mo.data) < REL_VAL
+
+
+def test_p2_tets():
+    m = fg.box_tet_mesh(3, seed=4, order=2)
+    Kg, Ko = fg.quadraticStiffnessMatrix(m), O.quadraticStiffnessMatrix(m)
+    assert same_pattern(Kg, Ko) and rel(Kg.data, Ko.data) < 1e-11
+    for full in (False, True):
+        Mg, Mo = fg.quadraticMassMatrix(m, full_phi=full), O.quadraticMassMatrix(m, full_phi=full)
+        assert same_pattern(Mg, Mo)
+        # the linear-part-only variant is evaluated in global coordinates: looser bound
+        assert rel(Mg.data, Mo.data) < (1e-11 if full else 1e-9)
+
+
+def test_p2_triangles():
+    m = fg.box_tri_mesh(4, seed=4, order=2)
+    Kg, Ko = fg.quadraticStiffnessMatrix2D(m), O.quadraticStiffnessMatrix2D(m)
+    assert same_pattern(Kg, Ko) and rel(Kg.data, Ko.data) < 1e-11
+    Mg, Mo = fg.quadraticMassMatrix2D(m), O.quadraticMassMatrix2D(m)
+    assert same_pattern(Mg, Mo) and rel(Mg.data, Mo.data) < 1e-11
+
+
+def test_assembly_deterministic(tet):
+    f = np.random.default_rng(7).uniform(0.5, 2.0, tet.nt)
+    a = fg.stiffnessMatrix(tet, f).data
+    b = fg.stiffnessMatrix(tet, f).data
+    assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_cg_csc(tet, precision):
+    K = O.stiffnessMatrix(tet) + O.massMatrix(tet)
+    b = np.random.default_rng(8).normal(size=tet.nv)
+    x, st = fg.cg(K, b, reltol=1e-10, precision=precision, return_stats=True)
+    xo, it, rr = O.pcg(K, b, tol=1e-12)
+    assert st["converged"]
+    assert np.linalg.norm(K @ x - b) / np.linalg.norm(b) < 1.5e-10
+    assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-8
+
+
+def test_spmv(tet):
+    K = O.stiffnessMatrix(tet)
+    x = np.random.default_rng(9).normal(size=tet.nv)
+    assert rel(fg.spmv(K, x), K @ x) < 1e-13
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_linear_magnetostatics(precision):
+    m = fg.box_tet_mesh(10, seed=6)
+    mu = np.where(m.elementID == 2, 1000 * fg.MU0, fg.MU0)
+    u0 = -m.p[0].copy()
+    ug, Hg, st = fg.magnetostatics_linear(m, mu, u0, precision=precision, rtol=1e-10)
+    uo, Ho, it = O.linear_magnetostatics(m, u0, mu, cg_tol=1e-12)
+    assert st["converged"]
+    assert np.linalg.norm(Hg - Ho) / np.linalg.norm(Ho) < 1e-8
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("line_search", ["residual", "reference"])
+def test_newton(precision, line_search):
+    m = fg.box_tet_mesh(12, seed=2)
+    nl = (m.elementID == 2).astype(np.uint8)
+    mu_lin = np.full(m.nt, fg.MU0)
+    u0 = -(np.array([8e4, 0.0, 0.0])[:, None] * m.p).sum(axis=0)
+    ug, Hg, mug, st = fg.newton_magnetostatics(m, nl, mu_lin, u0, precision=precision, line_search=line_search)
+    uo, Ho, muo, so = O.newton(m, u0, nl, mu_lin, 1.2e6, 500.0, cg_tol=1e-12, line_search="residual")
+    assert st["converged"], st
+    assert np.linalg.norm(Hg - Ho) / np.linalg.norm(Ho) < 1e-8
+    assert np.linalg.norm(ug - uo) / np.linalg.norm(uo) < 1e-8
+    assert np.abs(mug - muo).max() / muo.max() < 1e-8
+
+
+def test_hfield(tet):
+    u = np.random.default_rng(10).normal(size=tet.nv)
+    assert rel(fg.hfield(tet, u), O.hfield(tet, u)) < 1e-12
+
+
+def test_bad_mesh_reports_error():
+    import femeko_gpu._lib as L
+    m = fg.box_tet_mesh(2)
+    m.t = m.t.copy()
+    m.t[0, 0] = m.nv + 5  # out of range: caught by the upload kernel's range check
+    with pytest.raises(L.FemekoGPUError) as e:
+        fg.GPUMesh(m)
+    assert e.value.status == L.FG_BAD_MESH
