@@ -83,7 +83,7 @@ __global__ void k_elem_tet4(int kind, int64_t nt, const double *__restrict__ geo
 #pragma unroll
     for (int a = 0; a < 4; ++a)
 #pragma unroll
-      for (int b = 0; b < 4; ++b) Ke[a][b] = s * ah[a] * ah[b];
+      for (int b = a; b < 4; ++b) { Ke[a][b] = s * ah[a] * ah[b]; Ke[b][a] = Ke[a][b]; }
   }
 #pragma unroll
   for (int a = 0; a < 4; ++a) {

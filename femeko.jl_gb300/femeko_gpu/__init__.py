@@ -58,6 +58,7 @@ class GPUMesh:
         h = C.c_void_p()
         L.check(lib.fg_mesh_create(L.ptr(self._p), mesh.nv, L.ptr(self._t), mesh.nt, mesh.npe, 0, C.byref(h)))
         self.h = h
+        L.register_handle(self)
         nnz, mr = C.c_int64(), C.c_int32()
         L.check(lib.fg_mesh_nnz(h, C.byref(nnz), C.byref(mr)))
         self.nnz, self.max_row = nnz.value, mr.value
@@ -82,9 +83,10 @@ class GPUMesh:
         return sp.csc_matrix((vals, self.rowval.copy(), self.colptr.copy()), shape=(n, n))
 
     def close(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and not L._shutting_down:
             L.lib().fg_mesh_destroy(self.h)
-            self.h = None
+        self.h = None
+        L.unregister_handle(self)
 
     def __del__(self):
         try:

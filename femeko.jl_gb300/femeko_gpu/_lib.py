@@ -122,4 +122,37 @@ def check(status: int, allow_not_converged: bool = False) -> int:
 
 
 def ptr(a):
-    return None if a is None else C.c_void_p(a.ctypes.data)
+    """Data pointer of a numpy array; the returned object keeps the array alive for the
+    duration of the call (temporaries created inside a call expression stay valid)."""
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+# Handles still open at interpreter exit are released before the CUDA runtime tears
+# itself down (a cudaFree issued after that point is undefined).
+import weakref  # noqa: E402
+
+_open_handles = weakref.WeakSet()
+_shutting_down = False
+
+
+def register_handle(obj):
+    _open_handles.add(obj)
+
+
+def unregister_handle(obj):
+    _open_handles.discard(obj)
+
+
+def _close_all():
+    global _shutting_down
+    for obj in list(_open_handles):
+        try:
+            obj.close()
+        except Exception:
+            pass
+    _shutting_down = True
+
+
+import atexit  # noqa: E402
+
+atexit.register(_close_all)

@@ -1,0 +1,247 @@
+#=
+    FemekoGPU -- Julia bindings of libfemeko_gpu.so (GB300 / sm_103a) for Femeko's
+    FEM hot path.  Drop-in replacements, taking Femeko's own `MESH` struct
+    (src/mesh.jl:9-59) and returning the same types as the functions they replace:
+
+        stiffnessMatrix(mesh, f)            src/FEM3D.jl:40-56      -> SparseMatrixCSC
+        massMatrix(mesh)                    src/FEM3D.jl:466-492    -> SparseMatrixCSC
+        tangentialStiffnessMatrix(mesh,H,dmu) src/FEM3D.jl:79-119   -> SparseMatrixCSC
+        stiffnessMatrix2D / massMatrix2D    src/FEM2D.jl:48-161     -> SparseMatrixCSC
+        quadraticStiffnessMatrix(mesh, S, mu)  src/FEM3D.jl:378-395 (S is ignored: the
+                                            basis is built on the GPU)
+        quadraticMassMatrix(mesh, S, F)     src/FEM3D.jl:494-561
+        cg(A, b)                            IterativeSolvers.cg      -> Vector{Float64}
+        newton_magnetostatics(...)          Magnetostatics/NewtonRaphson.jl:109-214
+
+    The library is called through `ccall`, the pattern Femeko_jl_C++/Magnetostatics/run.jl:66-79
+    uses for scalarPotential.  mesh.t is passed as-is (Int32, 1-based): index_base = 1,
+    no copy.  Each MESH gets one device handle, cached in a WeakKeyDict and released
+    by a finalizer.
+
+    A ChainRulesCore.rrule makes `mean_Hx(mesh, mur, ...)` differentiable with respect
+    to the per-element relative permeability through the GPU adjoint (fg_adjoint_dJdmu).
+=#
+module FemekoGPU
+
+using SparseArrays
+using LinearAlgebra
+
+const LIB = Ref{String}(joinpath(@__DIR__, "..", "libfemeko_gpu.so"))
+libpath() = LIB[]
+
+# ---------------------------------------------------------------- C structs
+struct SolveOpts
+    precision::Int32
+    rtol::Float64
+    maxiter::Int32
+    inner_rtol::Float64
+    check_every::Int32
+    use_graph::Int32
+    spmv::Int32
+    rows_per_warp::Int32
+end
+
+struct SolveStats
+    iterations::Int32
+    refinements::Int32
+    converged::Int32
+    pad_::Int32
+    relres::Float64
+    ms::Float64
+end
+
+struct NewtonOpts
+    precision::Int32
+    maxit::Int32
+    tol_update::Float64
+    inner_rtol::Float64
+    cg_maxiter::Int32
+    line_search::Int32
+    min_step::Float64
+    Ms::Float64
+    Hk::Float64
+    check_every::Int32
+    use_graph::Int32
+end
+
+struct NewtonStats
+    newton_iters::Int32
+    cg_iters::Int32
+    converged::Int32
+    trials::Int32
+    update_ratio::Float64
+    residual::Float64
+    alpha::Float64
+    energy::Float64
+    ms::Float64
+end
+
+const FG_OK = Cint(0)
+const FG_NOT_CONVERGED = Cint(1)
+
+function check(st::Cint; allow_not_converged::Bool=false)
+    if st == FG_OK || (allow_not_converged && st == FG_NOT_CONVERGED)
+        return st
+    end
+    msg = unsafe_string(ccall((:fg_last_error, libpath()), Cstring, ()))
+    error("libfemeko_gpu status $(st): $(msg)")
+end
+
+function solve_opts(; precision::Symbol=:fp64, rtol=1e-10, maxiter=1_000_000, inner_rtol=1e-5)
+    o = Ref{SolveOpts}()
+    ccall((:fg_solve_opts_default, libpath()), Cvoid, (Ref{SolveOpts},), o)
+    d = o[]
+    return SolveOpts(precision == :mixed ? 1 : 0, rtol, maxiter, inner_rtol, d.check_every, d.use_graph,
+                     d.spmv, d.rows_per_warp)
+end
+
+function newton_opts(; precision::Symbol=:mixed, tol_update=1e-8, maxit=100, inner_rtol=1e-4,
+                     line_search::Symbol=:residual, Ms=1.2e6, Hk=500.0)
+    o = Ref{NewtonOpts}()
+    ccall((:fg_newton_opts_default, libpath()), Cvoid, (Ref{NewtonOpts},), o)
+    d = o[]
+    ls = line_search == :none ? 0 : line_search == :reference ? 1 : 2
+    return NewtonOpts(precision == :mixed ? 1 : 0, maxit, tol_update, inner_rtol, d.cg_maxiter, ls,
+                      d.min_step, Ms, Hk, d.check_every, d.use_graph)
+end
+
+# ---------------------------------------------------------------- mesh handle
+mutable struct GPUMesh
+    h::Ptr{Cvoid}
+    nv::Int
+    nt::Int
+    nnz::Int
+    colptr::Vector{Int64}      # 1-based, SparseMatrixCSC-ready
+    rowval::Vector{Int32}
+end
+
+const HANDLES = WeakKeyDict{Any,GPUMesh}()
+
+function GPUMesh(mesh; dirichlet::Union{Nothing,AbstractVector{UInt8}}=nothing)
+    npe = size(mesh.t, 1)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:fg_mesh_create, libpath()), Cint,
+                (Ptr{Float64}, Int64, Ptr{Int32}, Int64, Int32, Int32, Ref{Ptr{Cvoid}}),
+                mesh.p, size(mesh.p, 2), mesh.t, size(mesh.t, 2), npe, 1, h))
+    nnz = Ref{Int64}(0); mr = Ref{Int32}(0)
+    check(ccall((:fg_mesh_nnz, libpath()), Cint, (Ptr{Cvoid}, Ref{Int64}, Ref{Int32}), h[], nnz, mr))
+    colptr = zeros(Int64, size(mesh.p, 2) + 1)
+    rowval = zeros(Int32, nnz[])
+    check(ccall((:fg_csc_pattern, libpath()), Cint, (Ptr{Cvoid}, Ptr{Int64}, Ptr{Int32}, Int32),
+                h[], colptr, rowval, 1))
+    g = GPUMesh(h[], size(mesh.p, 2), size(mesh.t, 2), nnz[], colptr, rowval)
+    finalizer(g) do x
+        x.h != C_NULL && ccall((:fg_mesh_destroy, libpath()), Cint, (Ptr{Cvoid},), x.h)
+        x.h = C_NULL
+    end
+    dirichlet === nothing || set_dirichlet!(g, dirichlet)
+    return g
+end
+
+gpu(mesh) = get!(() -> GPUMesh(mesh), HANDLES, mesh)
+
+function set_dirichlet!(g::GPUMesh, fixed::AbstractVector{UInt8})
+    check(ccall((:fg_mesh_set_dirichlet, libpath()), Cint, (Ptr{Cvoid}, Ptr{UInt8}), g.h, fixed))
+end
+
+csc(g::GPUMesh, vals::Vector{Float64}) =
+    SparseMatrixCSC(g.nv, g.nv, copy(g.colptr), Int64.(g.rowval), vals)
+
+# ---------------------------------------------------------------- assembly drop-ins
+function stiffnessMatrix(mesh, f::Vector{Float64}=ones(size(mesh.t, 2)))
+    g = gpu(mesh); v = zeros(g.nnz)
+    check(ccall((:fg_stiffness, libpath()), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}), g.h, f, v))
+    return csc(g, v)
+end
+stiffnessMatrix2D(mesh, mu::Vector{Float64}=ones(size(mesh.t, 2))) = stiffnessMatrix(mesh, mu)
+quadraticStiffnessMatrix(mesh, S, mu::Vector{Float64}=ones(size(mesh.t, 2))) = stiffnessMatrix(mesh, mu)
+quadraticStiffnessMatrix2D(mesh, mu::Vector{Float64}=ones(size(mesh.t, 2))) = stiffnessMatrix(mesh, mu)
+
+function massMatrix(mesh; F::Vector{Float64}=ones(size(mesh.t, 2)), full_phi::Bool=false)
+    g = gpu(mesh); v = zeros(g.nnz)
+    check(ccall((:fg_mass, libpath()), Cint, (Ptr{Cvoid}, Ptr{Float64}, Int32, Ptr{Float64}),
+                g.h, F, full_phi ? 1 : 0, v))
+    return csc(g, v)
+end
+massMatrix2D(mesh) = massMatrix(mesh)
+quadraticMassMatrix(mesh, S, F::Vector{Float64}=ones(size(mesh.t, 2))) = massMatrix(mesh; F=F)
+quadraticMassMatrix2D(mesh) = massMatrix(mesh)
+
+function tangentialStiffnessMatrix(mesh, H_vec::Matrix{Float64}, dmu::Vector{Float64})
+    g = gpu(mesh); v = zeros(g.nnz)
+    check(ccall((:fg_tangent, libpath()), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+                g.h, H_vec, dmu, v))
+    return csc(g, v)
+end
+
+function localStiffnessMatrix(mesh, f::Vector{Float64}=ones(size(mesh.t, 2)))
+    g = gpu(mesh); Ak = zeros(16, g.nt)
+    check(ccall((:fg_local_stiffness, libpath()), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}), g.h, f, Ak))
+    return Ak
+end
+
+# ---------------------------------------------------------------- solvers
+"""cg(A, b; reltol, maxiter, precision) -- Jacobi-PCG on a symmetric SparseMatrixCSC."""
+function cg(A::SparseMatrixCSC{Float64,Int64}, b::Vector{Float64}; reltol=sqrt(eps(Float64)),
+            maxiter=size(A, 2), precision::Symbol=:fp64, x0=zeros(length(b)))
+    x = copy(x0)
+    o = Ref(solve_opts(precision=precision, rtol=reltol, maxiter=maxiter))
+    s = Ref{SolveStats}()
+    st = ccall((:fg_cg_csc, libpath()), Cint,
+               (Int64, Ptr{Int64}, Ptr{Int64}, Ptr{Float64}, Int32, Ptr{Float64}, Ptr{Float64},
+                Ref{SolveOpts}, Ref{SolveStats}),
+               size(A, 1), A.colptr, A.rowval, A.nzval, 1, b, x, o, s)
+    check(st; allow_not_converged=true)
+    return x
+end
+
+"""Newton-Raphson magnetostatics (Magnetostatics/NewtonRaphson.jl:109-214) with
+Dirichlet nodes `fixed` holding u0.  Returns (u, Hfield 3 x nt, mu, stats)."""
+function newton_magnetostatics(mesh, fixed::Vector{UInt8}, nl::Vector{UInt8}, mu_lin::Vector{Float64},
+                               u0::Vector{Float64}; kw...)
+    g = gpu(mesh)
+    set_dirichlet!(g, fixed)
+    u = zeros(g.nv); H = zeros(3, g.nt); mu = zeros(g.nt)
+    o = Ref(newton_opts(; kw...))
+    s = Ref{NewtonStats}()
+    st = ccall((:fg_newton_magnetostatics, libpath()), Cint,
+               (Ptr{Cvoid}, Ptr{UInt8}, Ptr{Float64}, Ptr{Float64}, Ref{NewtonOpts}, Ptr{Float64},
+                Ptr{Float64}, Ptr{Float64}, Ref{NewtonStats}),
+               g.h, nl, mu_lin, u0, o, u, H, mu, s)
+    check(st; allow_not_converged=true)
+    return u, H, mu, s[]
+end
+
+# ---------------------------------------------------------------- differentiation
+"""mean_Hx(mesh, mur, fixed, u0, target) -- volume-weighted mean H_x over the target
+elements of the linear magnetostatic solution with relative permeability mur."""
+function mean_Hx(mesh, mur::Vector{Float64}, fixed::Vector{UInt8}, u0::Vector{Float64}, target::Vector{UInt8})
+    g = gpu(mesh)
+    set_dirichlet!(g, fixed)
+    J = Ref{Float64}(0.0)
+    grad = zeros(g.nt)
+    check(ccall((:fg_adjoint_dJdmu, libpath()), Cint,
+                (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{UInt8}, Int32, Ref{Float64}, Ptr{Float64}),
+                g.h, mur, u0, target, 0, J, grad))
+    return J[], grad
+end
+
+# ChainRulesCore is an optional dependency: the rule is defined when it is loaded.
+function __init__()
+    if Base.find_package("ChainRulesCore") !== nothing
+        @eval begin
+            import ChainRulesCore
+            function ChainRulesCore.rrule(::typeof(mean_Hx_value), mesh, mur, fixed, u0, target)
+                J, grad = mean_Hx(mesh, mur, fixed, u0, target)
+                pullback(dJ) = (ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent(), dJ .* grad,
+                                ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent())
+                return J, pullback
+            end
+        end
+    end
+end
+
+"""The scalar J alone (the function the rrule differentiates)."""
+mean_Hx_value(mesh, mur, fixed, u0, target) = mean_Hx(mesh, mur, fixed, u0, target)[1]
+
+end # module

