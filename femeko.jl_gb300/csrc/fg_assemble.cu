@@ -379,6 +379,7 @@ __global__ void k_elem_newton(int64_t nt, const double *__restrict__ geo, const 
     pos[a] = recpos[(int64_t)a * nt + k];
     rec_r[pos[a]] = -vm * ah[a];
   }
+  if (rec == nullptr) return;  // residual-only pass (line-search trial)
   if (std::is_same<R, float>::value) {
     float gf[4][3], ahf[4];
 #pragma unroll
@@ -616,11 +617,21 @@ void fg_assemble_operator(fg_mesh *m, int kind, const double *d_f, const double 
   }
 }
 
-void fg_newton_assemble(fg_mesh *m, const double *d_u, double Ms, double Hk, bool mixed, double *d_F) {
+void fg_newton_assemble(fg_mesh *m, const double *d_u, double Ms, double Hk, bool mixed, double *d_F,
+                        bool want_jacobian) {
   FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "Newton magnetostatics needs P1 tetrahedra");
   fg_ensure_records(m);
   ensure_operator(m, !mixed, mixed);
   unsigned g = grid_for(m->nt, 128);
+  if (!want_jacobian) {
+    // element state + residual only: the row pass sums the vector records
+    k_elem_newton<double><<<g, 128, 0, m->stream>>>(m->nt, m->geo, m->t, d_u, m->nl, m->mu_lin, Ms, Hk, m->recpos,
+                                                    nullptr, m->rec_r, m->mu, m->dmu, m->H, m->wdens, m->flags);
+    FG_CUDA_TRY(cudaGetLastError());
+    FG_LAUNCHED(1);
+    launch_row<4, double, double>(m, nullptr, m->rec_r, 0, nullptr, nullptr, nullptr, nullptr, nullptr, d_F, -1.0, 1);
+    return;
+  }
   if (mixed) {
     float *rec = static_cast<float *>(m->rec);
     k_elem_newton<float><<<g, 128, 0, m->stream>>>(m->nt, m->geo, m->t, d_u, m->nl, m->mu_lin, Ms, Hk, m->recpos, rec,

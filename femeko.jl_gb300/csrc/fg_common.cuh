@@ -191,7 +191,11 @@ void fg_assemble_operator(fg_mesh *m, int kind, const double *d_f, const double 
                           double c_mass, double c_stiff, int full_phi, int layout, bool want64, bool want32,
                           bool apply_bc);
 void fg_ensure_records(fg_mesh *m);
-void fg_newton_assemble(fg_mesh *m, const double *d_u, double Ms, double Hk, bool mixed, double *d_F);
+// Element pass + row gather at potential d_u: element state (H, mu, dmu, energy
+// density), the residual F = -K(mu(u)) u (FP64) and, when want_jacobian, the
+// Jacobian K + At in the operator (FP32 when mixed) with its Jacobi diagonal.
+void fg_newton_assemble(fg_mesh *m, const double *d_u, double Ms, double Hk, bool mixed, double *d_F,
+                        bool want_jacobian = true);
 void fg_apply_operator_vec(fg_mesh *m, int kind, const double *d_coef, double c_mass, double c_stiff,
                            const double *d_x, double *d_y, bool zero_fixed);
 void fg_hfield_dev(fg_mesh *m, const double *d_u, double *d_H);

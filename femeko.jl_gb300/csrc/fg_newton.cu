@@ -88,12 +88,17 @@ static int newton_dev(fg_mesh *m, double *d_u, const fg_newton_opts &o, fg_newto
     fg_pcg_solve(m, d_F, d_du, so, &cst, true);
     cg_total += cst.iterations;
     alpha = 1.0;
+    bool need_jacobian = false;
     if (o.line_search == FG_LS_RESIDUAL || o.line_search == FG_LS_NONE) {
+      // trials evaluate the residual only; the Jacobian is rebuilt once a step is
+      // accepted (and only if the iteration continues)
+      const bool trial_jacobian = (o.line_search == FG_LS_NONE);
+      need_jacobian = !trial_jacobian;
       double rt = 0.0;
       for (;;) {
         k_axpby64<<<g, 256, 0, m->stream>>>(nv, 1.0, d_u, alpha, d_du, d_ut);
         FG_LAUNCHED(1);
-        fg_newton_assemble(m, d_ut, o.Ms, o.Hk, mixed, d_Ft);
+        fg_newton_assemble(m, d_ut, o.Ms, o.Hk, mixed, d_Ft, trial_jacobian);
         rt = fg_norm2_dev(m, d_Ft, nv, true);
         ++trials;
         if (o.line_search == FG_LS_NONE || !(rt > rF && alpha > o.min_step)) break;
@@ -137,6 +142,7 @@ static int newton_dev(fg_mesh *m, double *d_u, const fg_newton_opts &o, fg_newto
     ratio = (un > 0.0) ? dn / un : dn;
     if (!std::isfinite(ratio)) throw FgError{FG_NAN, "Newton update is not finite"};
     if (ratio <= o.tol_update) { converged = 1; break; }
+    if (need_jacobian) fg_newton_assemble(m, d_u, o.Ms, o.Hk, mixed, d_F, true);
   }
   double energy = fg_dot_dev(m, m->wdens, nullptr, m->nt, false);
   FG_CUDA_TRY(cudaEventRecord(e1, m->stream));

@@ -55,12 +55,24 @@ __device__ __forceinline__ void block_sum(double (&v)[N], double (*sh)[32]) {
   }
 }
 
-// Compensated FP32 block sum, returned as double in thread 0.
+// Per-thread accumulators: a plain FP64 sum for FP64 vectors, a compensated
+// (TwoSum) FP32 pair for FP32 vectors.
+template <typename S>
+struct Acc;
+template <>
+struct Acc<double> {
+  double v = 0.0;
+  __device__ __forceinline__ void add(double x) { v += x; }
+};
+template <>
+struct Acc<float> {
+  ff v{0.f, 0.f};
+  __device__ __forceinline__ void add(float x) { v = ff_add(v, ff{x, 0.f}); }
+};
+
+// Compensated FP32 block sum of (hi, lo) pairs, returned as double in thread 0.
 template <int N>
-__device__ __forceinline__ void block_sum_f(const float (&in)[N], double (&out)[N], ff (*sh)[32]) {
-  ff v[N];
-#pragma unroll
-  for (int j = 0; j < N; ++j) v[j] = ff{in[j], 0.f};
+__device__ __forceinline__ void block_sum_ff(ff (&v)[N], double (&out)[N], ff (*sh)[32]) {
 #pragma unroll
   for (int j = 0; j < N; ++j)
 #pragma unroll
@@ -88,6 +100,23 @@ __device__ __forceinline__ void block_sum_f(const float (&in)[N], double (&out)[
   }
 }
 
+// Block sum of per-thread accumulators; thread 0 gets the totals as doubles.
+template <typename S, int N>
+__device__ __forceinline__ void block_sum_acc(Acc<S> *a, double (&out)[N]) {
+  if (sizeof(S) == 4) {
+    __shared__ ff shf[N][32];
+    ff v[N];
+#pragma unroll
+    for (int j = 0; j < N; ++j) v[j] = reinterpret_cast<Acc<float> *>(a)[j].v;
+    block_sum_ff<N>(v, out, shf);
+  } else {
+    __shared__ double shd[N][32];
+#pragma unroll
+    for (int j = 0; j < N; ++j) out[j] = reinterpret_cast<Acc<double> *>(a)[j].v;
+    block_sum<N>(out, shd);
+  }
+}
+
 // Block partials -> the last block to arrive sums them in block order.  Returns true
 // in thread 0 of the last block, with the totals in tot.
 template <int N>
@@ -104,17 +133,18 @@ __device__ __forceinline__ bool grid_finish(const double (&v)[N], double *partia
   __syncthreads();
   if (!s_last) return false;
   __threadfence();
-  // sum in block order, one warp
-  if (threadIdx.x < 32) {
+  // The whole last block loads the partials (independent loads, one pass), then a
+  // fixed-shape tree: the order of the sum depends only on the grid size.
+  double acc[N];
 #pragma unroll
-    for (int j = 0; j < N; ++j) {
-      double acc = 0.0;
-      for (unsigned b = threadIdx.x; b < gridDim.x; b += 32) acc += ((volatile double *)partials)[(size_t)b * N + j];
+  for (int j = 0; j < N; ++j) acc[j] = 0.0;
+  for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x)
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-      tot[j] = acc;
-    }
-  }
+    for (int j = 0; j < N; ++j) acc[j] += __ldcg(partials + (size_t)b * N + j);
+  __shared__ double shfin[N][32];
+  block_sum<N>(acc, shfin);
+#pragma unroll
+  for (int j = 0; j < N; ++j) tot[j] = acc[j];
   if (threadIdx.x == 0) *counter = 0u;
   return threadIdx.x == 0;
 }
@@ -128,9 +158,9 @@ __global__ void __launch_bounds__(256) k_cg_spmv(int64_t n, const int *__restric
                                                  double *scal, int *ictl, double *partials, unsigned *counter) {
   if (ictl[I_DONE]) return;
   const S beta = (S)scal[S_BETA];
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  S prod = 0;
-  if (i < n) {
+  Acc<S> prod;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     int s = (int)(i >> 5), lane = (int)(i & 31);
     int64_t base = sl_ptr[s] + lane;
     int L = sl_len[s];
@@ -144,18 +174,10 @@ __global__ void __launch_bounds__(256) k_cg_spmv(int64_t n, const int *__restric
     S pi = fma(beta, p[i], z[i]);
     pn[i] = pi;
     q[i] = acc;
-    prod = pi * acc;
+    prod.add(pi * acc);
   }
   double part[1];
-  if (sizeof(S) == 4) {
-    __shared__ ff shf[1][32];
-    float in[1] = {(float)prod};
-    block_sum_f<1>(in, part, shf);
-  } else {
-    __shared__ double shd[1][32];
-    part[0] = (double)prod;
-    block_sum<1>(part, shd);
-  }
+  block_sum_acc<S, 1>(&prod, part);
   double tot[1];
   if (grid_finish<1>(part, partials, counter, tot)) {
     scal[S_PQ] = tot[0];
@@ -170,29 +192,20 @@ __global__ void __launch_bounds__(256) k_cg_update(int64_t n, S *__restrict__ x,
                                                    double *scal, int *ictl, double *partials, unsigned *counter) {
   if (ictl[I_DONE]) return;
   const S alpha = (S)scal[S_ALPHA];
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  S rz = 0, rr = 0;
-  if (i < n) {
+  Acc<S> a2[2];
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     S xi = fma(alpha, pn[i], x[i]);
     S ri = fma(-alpha, q[i], r[i]);
     S zi = dinv[i] * ri;
     x[i] = xi;
     r[i] = ri;
     z[i] = zi;
-    rz = ri * zi;
-    rr = ri * ri;
+    a2[0].add(ri * zi);
+    a2[1].add(ri * ri);
   }
   double part[2];
-  if (sizeof(S) == 4) {
-    __shared__ ff shf[2][32];
-    float in[2] = {(float)rz, (float)rr};
-    block_sum_f<2>(in, part, shf);
-  } else {
-    __shared__ double shd[2][32];
-    part[0] = (double)rz;
-    part[1] = (double)rr;
-    block_sum<2>(part, shd);
-  }
+  block_sum_acc<S, 2>(a2, part);
   double tot[2];
   if (grid_finish<2>(part, partials, counter, tot)) {
     double rzo = scal[S_RZ];
@@ -215,17 +228,17 @@ __global__ void __launch_bounds__(256) k_cg_init(int64_t n, const double *__rest
                                                  S *__restrict__ p, const S *__restrict__ dinv, double tol2_rel,
                                                  int maxit, double *scal, int *ictl, double *partials,
                                                  unsigned *counter) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double rz = 0, rr = 0;
-  if (i < n) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     S ri = (S)(scale * rin[i]);
     S zi = dinv[i] * ri;
     x[i] = 0;
     r[i] = ri;
     z[i] = zi;
     p[i] = 0;
-    rz = (double)ri * (double)zi;
-    rr = (double)ri * (double)ri;
+    rz += (double)ri * (double)zi;
+    rr += (double)ri * (double)ri;
   }
   __shared__ double shd[2][32];
   double part[2] = {rz, rr};
@@ -254,9 +267,9 @@ __global__ void __launch_bounds__(256) k_spmv_sell(int64_t n, const int *__restr
                                                    const double *__restrict__ b, double *__restrict__ y,
                                                    const uint8_t *__restrict__ fixed, int slot, double *scal,
                                                    double *partials, unsigned *counter) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double rr = 0.0;
-  if (i < n) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     int s = (int)(i >> 5), lane = (int)(i & 31);
     int64_t base = sl_ptr[s] + lane;
     int L = sl_len[s];
@@ -267,7 +280,7 @@ __global__ void __launch_bounds__(256) k_spmv_sell(int64_t n, const int *__restr
     double v = b ? b[i] - acc : acc;
     if (fixed && fixed[i]) v = 0.0;
     y[i] = v;
-    rr = v * v;
+    rr += v * v;
   }
   if (slot < 0) return;
   __shared__ double shd[1][32];
@@ -293,11 +306,19 @@ __global__ void __launch_bounds__(256) k_dot64(int64_t n, const double *__restri
 // x += scale * d
 template <typename S>
 __global__ void k_axpy_to64(int64_t n, double scale, const S *__restrict__ d, double *__restrict__ x) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) x[i] += scale * (double)d[i];
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] += scale * (double)d[i];
 }
 
 // ------------------------------------------------------------------ host helpers
+// Grid of the row-parallel reduction kernels: at most 8 blocks of 256 threads per SM,
+// rows visited with a grid-stride loop, so the last block sums a few hundred partials.
+static unsigned cg_grid(const fg_mesh *m) {
+  unsigned g = grid_for(m->nv, 256);
+  unsigned cap = 8u * (unsigned)(m->sm_count > 0 ? m->sm_count : 152);
+  return g < cap ? g : cap;
+}
+
 static unsigned red_grid(int64_t n) {
   unsigned g = grid_for(n, 256);
   return g > (unsigned)FG_RED_BLOCKS ? (unsigned)FG_RED_BLOCKS : g;
@@ -320,7 +341,7 @@ double fg_norm2_dev(fg_mesh *m, const double *x, int64_t n, bool mask_fixed) {
 
 void fg_spmv64_dev(fg_mesh *m, const double *x, double *y) {
   FG_REQUIRE(m->val64 != nullptr, FG_BAD_ARG, "no FP64 operator assembled");
-  k_spmv_sell<double><<<grid_for(m->nv, 256), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val64,
+  k_spmv_sell<double><<<cg_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val64,
                                                                      x, nullptr, y, nullptr, -1, m->scal,
                                                                      m->red.partials, m->red.counter);
   FG_CUDA_TRY(cudaGetLastError());
@@ -348,7 +369,7 @@ template <typename V, typename S>
 static void launch_iteration(fg_mesh *m, const V *val, const S *dinv, S **v, bool odd) {
   S *p = odd ? v[4] : v[3];
   S *pn = odd ? v[3] : v[4];
-  unsigned g = grid_for(m->nv, 256);
+  unsigned g = cg_grid(m);
   k_cg_spmv<V, S><<<g, 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col, val, v[2], p, pn, v[5], m->scal,
                                             m->ictl, m->red.partials, m->red.counter);
   k_cg_update<S><<<g, 256, 0, m->stream>>>(m->nv, v[0], v[1], v[2], pn, v[5], dinv, m->scal, m->ictl,
@@ -416,7 +437,7 @@ int fg_pcg_solve(fg_mesh *m, const double *d_b, double *d_x, const fg_solve_opts
       rn = fg_norm2_dev(m, r64, m->nv, true);
     } else {
       FG_REQUIRE(m->val64 != nullptr, FG_BAD_ARG, "refinement needs the FP64 operator");
-      k_spmv_sell<double><<<grid_for(m->nv, 256), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col,
+      k_spmv_sell<double><<<cg_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col,
                                                                          m->val64, d_x, d_b, r64, fx, 9, m->scal,
                                                                          m->red.partials, m->red.counter);
       FG_CUDA_TRY(cudaGetLastError());
@@ -435,7 +456,7 @@ int fg_pcg_solve(fg_mesh *m, const double *d_b, double *d_x, const fg_solve_opts
     if (newton_inner) inner = o.inner_rtol;
     int maxit = o.maxiter - total;
     int ist = 0, its = 0;
-    unsigned g = grid_for(m->nv, 256);
+    unsigned g = cg_grid(m);
     if (mixed) {
       float **v = cg_vectors<float>(m);
       k_cg_init<float><<<g, 256, 0, m->stream>>>(m->nv, r64, 1.0 / rn, v[0], v[1], v[2], v[3], m->dinv32,
@@ -499,6 +520,7 @@ static fg_mesh *matrix_handle(int64_t n, const int64_t *colptr, const int64_t *r
   fg_mesh *m = new fg_mesh();
   try {
     FG_CUDA_TRY(cudaGetDevice(&m->device));
+    FG_CUDA_TRY(cudaDeviceGetAttribute(&m->sm_count, cudaDevAttrMultiProcessorCount, m->device));
     FG_CUDA_TRY(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
     FG_CUDA_TRY(cudaEventCreate(&m->ev0));
     FG_CUDA_TRY(cudaEventCreate(&m->ev1));
@@ -609,8 +631,8 @@ extern "C" fg_status fg_spmv_csc(int64_t n, const int64_t *colptr, const int64_t
 }
 
 __global__ void k_fill64(int64_t n, double v, double *__restrict__ x) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) x[i] = v;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = v;
 }
 
 // Average duration of one CG kernel launch on the handle's current operator
@@ -618,7 +640,7 @@ __global__ void k_fill64(int64_t n, double v, double *__restrict__ x) {
 fg_status fg_bench_cg_kernel(fg_mesh *m, int which, int precision, int reps, double *ms_per_launch) {
   const bool mixed = precision == FG_MIXED;
   FG_REQUIRE(mixed ? m->val32 != nullptr : m->val64 != nullptr, FG_BAD_ARG, "operator not assembled");
-  unsigned g = grid_for(m->nv, 256);
+  unsigned g = cg_grid(m);
   if (!m->v64[6]) m->v64[6] = dev_alloc<double>(m, (size_t)m->nv);
   k_fill64<<<g, 256, 0, m->stream>>>(m->nv, 1.0, m->v64[6]);
   auto body = [&](int n) {
