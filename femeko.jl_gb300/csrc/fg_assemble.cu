@@ -325,88 +325,133 @@ __global__ void k_elem_tri6(int kind, int64_t nt, const double *__restrict__ p, 
 }
 
 // ------------------------------------------------------------------ Newton element pass
-// From the potential u: H = -sum u_a grad phi_a, |H|, mu and dmu (Froehlich law for
-// nl elements, mu_lin otherwise), the energy density integral of H dB times VE, the
-// residual records (K_e u_e)_a = -VE mu grad(phi_a).H and the Jacobian records
-// J_ab = VE mu grad(phi_a).grad(phi_b) + VE dmu/|H| (H.grad phi_a)(H.grad phi_b).
-// Follows Magnetostatics/NewtonRaphson.jl:154-207 and src/FEM3D.jl:79-119.  In
-// mixed precision the Jacobian records are formed in FP32 (they feed the FP32
-// operator only); H, mu and the residual stay FP64.
+// |x|^-1/2 and 1/x in FP64 by Newton-Raphson refinement of the FP32 hardware
+// estimate (rsqrtf / __frcp_rn): y <- y (3 - x y^2) / 2 and r <- r (2 - x r), two
+// steps each.  Each step squares the relative error, so two steps take the ~1e-7 FP32
+// estimate below FP64 rounding.  On GB300 an FP64 operation is ~64x dearer than an
+// FP32 one, and these replace the FP64 square root and division of the element pass.
+// Arguments outside the FP32 normal range take the FP64 library path.
+__device__ __forceinline__ double rsqrt_nr(double x) {
+  if (!(x > 1e-30 && x < 1e30)) return (x > 0.0) ? 1.0 / sqrt(x) : 0.0;
+  double y = (double)rsqrtf((float)x);
+  y = y * fma(-0.5 * x * y, y, 1.5);
+  y = y * fma(-0.5 * x * y, y, 1.5);
+  return y;
+}
+__device__ __forceinline__ double rcp_nr(double x) {
+  if (!(fabs(x) > 1e-30 && fabs(x) < 1e30)) return 1.0 / x;
+  double r = (double)__frcp_rn((float)x);
+  r = fma(r, fma(-x, r, 1.0), r);
+  r = fma(r, fma(-x, r, 1.0), r);
+  return r;
+}
+
+// From the potential u (Magnetostatics/NewtonRaphson.jl:154-207, src/FEM3D.jl:79-119),
+// with the element Gram matrix G_ab = grad(phi_a).grad(phi_b) precomputed per mesh:
+//   w_a = (G u)_a = -H.grad(phi_a), evaluated on u - u_0 (G's rows sum to zero),
+//   |H|^2 = u.w,  mu and dmu (Froehlich law for nl elements, mu_lin otherwise),
+//   residual records (K_e u_e)_a = VE mu w_a,
+//   Jacobian records J_ab = VE mu G_ab + VE dmu/|H| w_a w_b.
+// The Jacobian records are skipped when rec is null (line-search trials) and are
+// formed in FP32 when R is float (they feed the FP32 operator only); the residual,
+// |H| and mu stay FP64.
 template <typename R>
-__global__ void k_elem_newton(int64_t nt, const double *__restrict__ geo, const int *__restrict__ t,
-                              const double *__restrict__ u, const uint8_t *__restrict__ nl,
-                              const double *__restrict__ mu_lin, double Ms, double Hk, const int *__restrict__ recpos,
-                              R *__restrict__ rec, double *__restrict__ rec_r, double *__restrict__ mu_out,
-                              double *__restrict__ dmu_out, double *__restrict__ H_out, double *__restrict__ w_out,
-                              int *flags) {
+__global__ void __launch_bounds__(128) k_elem_newton(int64_t nt, const double *__restrict__ geo,
+                                                     const int *__restrict__ t, const double *__restrict__ u,
+                                                     const uint8_t *__restrict__ nl,
+                                                     const double *__restrict__ mu_lin, double Ms, double Hk,
+                                                     const int *__restrict__ recpos, R *__restrict__ rec,
+                                                     double *__restrict__ rec_r, double *__restrict__ mu_out,
+                                                     double *__restrict__ dmu_out, int *flags) {
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nt) return;
-  double g[4][3];
+  double G[10];
 #pragma unroll
-  for (int c = 0; c < 12; ++c) g[c / 3][c % 3] = geo[(int64_t)c * nt + k];
-  double VE = geo[12 * nt + k];
+  for (int c = 0; c < 10; ++c) G[c] = geo[(int64_t)(13 + c) * nt + k];
+  const double VE = geo[12 * nt + k];
   double uu[4];
 #pragma unroll
   for (int a = 0; a < 4; ++a) uu[a] = u[t[(int64_t)a * nt + k]];
-  double hx = 0, hy = 0, hz = 0;
-#pragma unroll
-  for (int a = 0; a < 4; ++a) { hx -= uu[a] * g[a][0]; hy -= uu[a] * g[a][1]; hz -= uu[a] * g[a][2]; }
-  double h = sqrt(hx * hx + hy * hy + hz * hz);
-  double mu, dmu, w;
+  const double d1 = uu[1] - uu[0], d2 = uu[2] - uu[0], d3 = uu[3] - uu[0];
+  // G upper triangle: 0:00 1:01 2:02 3:03 4:11 5:12 6:13 7:22 8:23 9:33
+  double w[4];
+  w[0] = G[1] * d1 + G[2] * d2 + G[3] * d3;
+  w[1] = G[4] * d1 + G[5] * d2 + G[6] * d3;
+  w[2] = G[5] * d1 + G[7] * d2 + G[8] * d3;
+  w[3] = G[6] * d1 + G[8] * d2 + G[9] * d3;
+  const double h2 = fmax(d1 * w[1] + d2 * w[2] + d3 * w[3], 0.0);
+  const double ih = rsqrt_nr(h2);  // 1/|H| (0 when H = 0)
+  const double h = h2 * ih;
+  double mu, dmu;
   if (nl[k]) {
-    double den = Hk + h;
-    mu = FG_MU0 * (1.0 + Ms / den);
-    dmu = -FG_MU0 * Ms / (den * den);
-    w = FG_MU0 * (0.5 * h * h + Ms * Hk * (log1p(h / Hk) + Hk / den - 1.0));
+    const double inv = rcp_nr(Hk + h);
+    mu = FG_MU0 * fma(Ms, inv, 1.0);
+    dmu = -FG_MU0 * Ms * inv * inv;
   } else {
     mu = mu_lin[k];
     dmu = 0.0;
-    w = 0.5 * mu * h * h;
   }
   if (!isfinite(mu) || !isfinite(dmu)) atomicOr(flags, FLAG_NAN);
   mu_out[k] = mu;
   dmu_out[k] = dmu;
-  H_out[3 * k] = hx; H_out[3 * k + 1] = hy; H_out[3 * k + 2] = hz;
-  w_out[k] = w * VE;
-  double ah[4];
-#pragma unroll
-  for (int a = 0; a < 4; ++a) ah[a] = hx * g[a][0] + hy * g[a][1] + hz * g[a][2];
-  double vm = VE * mu;
-  double ct = (h > 0.0) ? VE * dmu / h : 0.0;
+  const double vm = VE * mu;
   int pos[4];
 #pragma unroll
   for (int a = 0; a < 4; ++a) {
     pos[a] = recpos[(int64_t)a * nt + k];
-    rec_r[pos[a]] = -vm * ah[a];
+    rec_r[pos[a]] = vm * w[a];
   }
   if (rec == nullptr) return;  // residual-only pass (line-search trial)
+  const double ct = VE * dmu * ih;
   if (std::is_same<R, float>::value) {
-    float gf[4][3], ahf[4];
+    float Gf[10], wf[4];
 #pragma unroll
-    for (int a = 0; a < 4; ++a) {
-      ahf[a] = (float)ah[a];
+    for (int c = 0; c < 10; ++c) Gf[c] = (float)G[c];
 #pragma unroll
-      for (int d = 0; d < 3; ++d) gf[a][d] = (float)g[a][d];
-    }
-    float vmf = (float)vm, ctf = (float)ct;
+    for (int a = 0; a < 4; ++a) wf[a] = (float)w[a];
+    const float vmf = (float)vm, ctf = (float)ct;
+    const int idx[4][4] = {{0, 1, 2, 3}, {1, 4, 5, 6}, {2, 5, 7, 8}, {3, 6, 8, 9}};
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
       R row[4];
+      const float ca = ctf * wf[a];
 #pragma unroll
-      for (int b = 0; b < 4; ++b)
-        row[b] = (R)(vmf * (gf[a][0] * gf[b][0] + gf[a][1] * gf[b][1] + gf[a][2] * gf[b][2]) + ctf * ahf[a] * ahf[b]);
+      for (int b = 0; b < 4; ++b) row[b] = (R)fmaf(ca, wf[b], vmf * Gf[idx[a][b]]);
       store_row<4, R>(rec, pos[a], row);
     }
   } else {
+    const int idx[4][4] = {{0, 1, 2, 3}, {1, 4, 5, 6}, {2, 5, 7, 8}, {3, 6, 8, 9}};
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
       R row[4];
+      const double ca = ct * w[a];
 #pragma unroll
-      for (int b = 0; b < 4; ++b)
-        row[b] = (R)(vm * (g[a][0] * g[b][0] + g[a][1] * g[b][1] + g[a][2] * g[b][2]) + ct * ah[a] * ah[b]);
+      for (int b = 0; b < 4; ++b) row[b] = (R)fma(ca, w[b], vm * G[idx[a][b]]);
       store_row<4, R>(rec, pos[a], row);
     }
   }
+}
+
+// Energy density integral of H dB times VE (src/magneticProperties.jl:252-309, FEMM
+// style) in closed form: linear elements mu |H|^2 / 2, Froehlich elements
+// mu0 [|H|^2/2 + Ms Hk (ln(1 + |H|/Hk) + Hk/(Hk + |H|) - 1)].
+__global__ void k_energy_tet4(int64_t nt, const double *__restrict__ geo, const int *__restrict__ t,
+                              const double *__restrict__ u, const uint8_t *__restrict__ nl,
+                              const double *__restrict__ mu_lin, double Ms, double Hk, double *__restrict__ wout) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt) return;
+  double hx = 0, hy = 0, hz = 0;
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    double ua = u[t[(int64_t)a * nt + k]];
+    hx -= ua * geo[(int64_t)(3 * a) * nt + k];
+    hy -= ua * geo[(int64_t)(3 * a + 1) * nt + k];
+    hz -= ua * geo[(int64_t)(3 * a + 2) * nt + k];
+  }
+  double h2 = hx * hx + hy * hy + hz * hz, h = sqrt(h2), wd;
+  if (nl[k]) wd = FG_MU0 * (0.5 * h2 + Ms * Hk * (log1p(h / Hk) + Hk / (Hk + h) - 1.0));
+  else wd = 0.5 * mu_lin[k] * h2;
+  wout[k] = wd * geo[12 * nt + k];
 }
 
 // (K_e x_e)_a for the stiffness (coef * VE G G^T) or mass (coef VE/20 (1+delta)) or
@@ -479,7 +524,7 @@ __global__ void k_row_sum(int64_t nv, const int *__restrict__ in_ptr, const int 
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nv) return;
   int s = (int)(i / FG_SLICE), lane = (int)(i % FG_SLICE);
-  int L = sl_len[s];
+  int L = FG_GROUP * sl_len[s];
   const bool want_mat = (rec != nullptr);
   if (want_mat)
     for (int q = 0; q < L; ++q) acc[q * bs] = (A)0;
@@ -520,11 +565,18 @@ __global__ void k_row_sum(int64_t nv, const int *__restrict__ in_ptr, const int 
   int dk = diagk[i];
   if (apply_bc && fx)
     for (int q = 0; q < L; ++q) acc[q * bs] = (q == dk) ? (A)1 : (A)0;
-  int64_t sb = sl_ptr[s] + lane;
+  int64_t sb = sl_ptr[s];
   if (out64)
-    for (int q = 0; q < L; ++q) out64[sb + (int64_t)q * FG_SLICE] = (double)acc[q * bs];
+    for (int q = 0; q < L; q += 2) {
+      int64_t p0 = sell_pos(sb, lane, q);
+      *reinterpret_cast<double2 *>(out64 + p0) = make_double2((double)acc[q * bs], (double)acc[(q + 1) * bs]);
+    }
   if (out32)
-    for (int q = 0; q < L; ++q) out32[sb + (int64_t)q * FG_SLICE] = (float)acc[q * bs];
+    for (int q = 0; q < L; q += 4) {
+      int64_t p0 = sell_pos(sb, lane, q);
+      *reinterpret_cast<float4 *>(out32 + p0) = make_float4((float)acc[q * bs], (float)acc[(q + 1) * bs],
+                                                            (float)acc[(q + 2) * bs], (float)acc[(q + 3) * bs]);
+    }
   if (outcsr) {
     int rb = rowptr[i], len = rowptr[i + 1] - rb;
     for (int q = 0; q < len; ++q) outcsr[rb + q] = (double)acc[q * bs];
@@ -544,14 +596,21 @@ void fg_ensure_records(fg_mesh *m) {
 static void ensure_operator(fg_mesh *m, bool want64, bool want32) {
   if (want64 && !m->val64) m->val64 = dev_alloc<double>(m, (size_t)m->nsell);
   if (want32 && !m->val32) m->val32 = dev_alloc<float>(m, (size_t)m->nsell);
-  if (!m->dinv64) m->dinv64 = dev_alloc<double>(m, (size_t)m->nv);
-  if (!m->dinv32) m->dinv32 = dev_alloc<float>(m, (size_t)m->nv);
+  // the Jacobi diagonals are read 4 rows at a time: padded rows stay 0
+  if (!m->dinv64) {
+    m->dinv64 = dev_alloc<double>(m, (size_t)m->nvp);
+    FG_CUDA_TRY(cudaMemsetAsync(m->dinv64, 0, sizeof(double) * (size_t)m->nvp, m->stream));
+  }
+  if (!m->dinv32) {
+    m->dinv32 = dev_alloc<float>(m, (size_t)m->nvp);
+    FG_CUDA_TRY(cudaMemsetAsync(m->dinv32, 0, sizeof(float) * (size_t)m->nvp, m->stream));
+  }
 }
 
 template <int NPE, typename R, typename A>
 static void launch_row(fg_mesh *m, const R *rec, const double *rec_r, int apply_bc, double *out64, float *out32,
                        double *outcsr, double *dinv64, float *dinv32, double *vout, double vsign, int zero_fixed_vec) {
-  int L = std::max(m->maxrow, 1);
+  int L = std::max(m->maxrow4, FG_GROUP);
   int block = (L * (int)sizeof(A) * 128 <= 48 * 1024) ? 128 : 64;
   size_t smem = (size_t)block * L * sizeof(A);
   auto kern = k_row_sum<NPE, R, A>;
@@ -626,7 +685,7 @@ void fg_newton_assemble(fg_mesh *m, const double *d_u, double Ms, double Hk, boo
   if (!want_jacobian) {
     // element state + residual only: the row pass sums the vector records
     k_elem_newton<double><<<g, 128, 0, m->stream>>>(m->nt, m->geo, m->t, d_u, m->nl, m->mu_lin, Ms, Hk, m->recpos,
-                                                    nullptr, m->rec_r, m->mu, m->dmu, m->H, m->wdens, m->flags);
+                                                    nullptr, m->rec_r, m->mu, m->dmu, m->flags);
     FG_CUDA_TRY(cudaGetLastError());
     FG_LAUNCHED(1);
     launch_row<4, double, double>(m, nullptr, m->rec_r, 0, nullptr, nullptr, nullptr, nullptr, nullptr, d_F, -1.0, 1);
@@ -635,14 +694,14 @@ void fg_newton_assemble(fg_mesh *m, const double *d_u, double Ms, double Hk, boo
   if (mixed) {
     float *rec = static_cast<float *>(m->rec);
     k_elem_newton<float><<<g, 128, 0, m->stream>>>(m->nt, m->geo, m->t, d_u, m->nl, m->mu_lin, Ms, Hk, m->recpos, rec,
-                                                   m->rec_r, m->mu, m->dmu, m->H, m->wdens, m->flags);
+                                                   m->rec_r, m->mu, m->dmu, m->flags);
     FG_CUDA_TRY(cudaGetLastError());
     FG_LAUNCHED(1);
     launch_row<4, float, float>(m, rec, m->rec_r, 1, nullptr, m->val32, nullptr, nullptr, m->dinv32, d_F, -1.0, 1);
   } else {
     double *rec = static_cast<double *>(m->rec);
     k_elem_newton<double><<<g, 128, 0, m->stream>>>(m->nt, m->geo, m->t, d_u, m->nl, m->mu_lin, Ms, Hk, m->recpos,
-                                                    rec, m->rec_r, m->mu, m->dmu, m->H, m->wdens, m->flags);
+                                                    rec, m->rec_r, m->mu, m->dmu, m->flags);
     FG_CUDA_TRY(cudaGetLastError());
     FG_LAUNCHED(1);
     launch_row<4, double, double>(m, rec, m->rec_r, 1, m->val64, nullptr, nullptr, m->dinv64, nullptr, d_F, -1.0, 1);
@@ -659,6 +718,13 @@ void fg_apply_operator_vec(fg_mesh *m, int kind, const double *d_coef, double c_
   FG_LAUNCHED(1);
   launch_row<4, double, double>(m, nullptr, m->rec_r, 0, nullptr, nullptr, nullptr, nullptr, nullptr, d_y, 1.0,
                                 zero_fixed ? 1 : 0);
+}
+
+void fg_energy_dev(fg_mesh *m, const double *d_u, double Ms, double Hk) {
+  k_energy_tet4<<<grid_for(m->nt, 256), 256, 0, m->stream>>>(m->nt, m->geo, m->t, d_u, m->nl, m->mu_lin, Ms, Hk,
+                                                              m->wdens);
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(1);
 }
 
 void fg_hfield_dev(fg_mesh *m, const double *d_u, double *d_H) {

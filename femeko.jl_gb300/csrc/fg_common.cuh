@@ -58,8 +58,14 @@ enum {
 };
 
 // Longest matrix row the pattern builder accepts (slot positions fit a byte).
-constexpr int FG_MAX_ROW = 255;
+constexpr int FG_MAX_ROW = 252;
 constexpr int FG_SLICE = 32;  // rows per SELL slice
+constexpr int FG_GROUP = 4;   // row slots per 128-bit group
+
+// Position of slot q of the row with lane `lane` in a slice starting at `base`.
+__host__ __device__ __forceinline__ int64_t sell_pos(int64_t base, int lane, int q) {
+  return base + ((int64_t)(q >> 2) * FG_SLICE + lane) * FG_GROUP + (q & 3);
+}
 constexpr int FG_RED_BLOCKS = 4096;
 
 // ---------------------------------------------------------------- device scratch
@@ -115,12 +121,20 @@ struct fg_mesh {
   int64_t nnz = 0;
   int maxrow = 0;
 
-  // SELL-32 matrix layout (rows in natural order, columns padded with the row itself)
+  // SELL-32x4 matrix layout (rows in natural order): slice s holds rows 32s..32s+31;
+  // its entries are stored in groups of 4 consecutive row slots, group-major, lane
+  // within the group, so a thread loads 4 entries of its row with one 128-bit load
+  // and a warp's loads are contiguous.  Rows are padded to 4*sl_len[s] slots with
+  // the row's own column and value 0.  Entry (row i, slot q) sits at sell_pos().
   int nslices = 0;
+  int64_t nvp = 0;           // rows padded to whole slices (vector length)
   int *sl_ptr = nullptr;     // nslices+1 offsets into sl_col / values
-  int *sl_len = nullptr;     // nslices: longest row of the slice
-  int *sl_col = nullptr;     // nsell
+  int *sl_len = nullptr;     // nslices: groups of 4 slots per row in the slice
+  int *sl_col = nullptr;     // nsell absolute column indices
+  int16_t *sl_dcol = nullptr;// nsell column - row, when every |column - row| < 32768
+  bool use_dcol = false;
   int64_t nsell = 0;
+  int maxrow4 = 0;           // longest row rounded up to a multiple of 4
   uint8_t *diagk = nullptr;  // nv: position of the diagonal in its row
   int *rowlen = nullptr;     // nv
 
@@ -199,6 +213,8 @@ void fg_newton_assemble(fg_mesh *m, const double *d_u, double Ms, double Hk, boo
 void fg_apply_operator_vec(fg_mesh *m, int kind, const double *d_coef, double c_mass, double c_stiff,
                            const double *d_x, double *d_y, bool zero_fixed);
 void fg_hfield_dev(fg_mesh *m, const double *d_u, double *d_H);
+// Energy density integral times VE per element into m->wdens (from the potential).
+void fg_energy_dev(fg_mesh *m, const double *d_u, double Ms, double Hk);
 
 // solve (fg_solve.cu)
 double fg_norm2_dev(fg_mesh *m, const double *x, int64_t n, bool mask_fixed);

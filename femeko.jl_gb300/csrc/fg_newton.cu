@@ -89,11 +89,12 @@ static int newton_dev(fg_mesh *m, double *d_u, const fg_newton_opts &o, fg_newto
     cg_total += cst.iterations;
     alpha = 1.0;
     bool need_jacobian = false;
-    if (o.line_search == FG_LS_RESIDUAL || o.line_search == FG_LS_NONE) {
+    if (o.line_search != FG_LS_REFERENCE) {
       // trials evaluate the residual only; the Jacobian is rebuilt once a step is
       // accepted (and only if the iteration continues)
       const bool trial_jacobian = (o.line_search == FG_LS_NONE);
       need_jacobian = !trial_jacobian;
+      const double f0 = rF * rF;
       double rt = 0.0;
       for (;;) {
         k_axpby64<<<g, 256, 0, m->stream>>>(nv, 1.0, d_u, alpha, d_du, d_ut);
@@ -102,7 +103,16 @@ static int newton_dev(fg_mesh *m, double *d_u, const fg_newton_opts &o, fg_newto
         rt = fg_norm2_dev(m, d_Ft, nv, true);
         ++trials;
         if (o.line_search == FG_LS_NONE || !(rt > rF && alpha > o.min_step)) break;
-        alpha *= 0.9;
+        if (o.line_search == FG_LS_QUADRATIC) {
+          // minimiser of the quadratic through f(0) = |F|^2, f'(0) = -2|F|^2 (Newton
+          // direction) and f(alpha), kept in [0.1, 0.5] alpha (Dennis & Schnabel,
+          // backtracking by quadratic interpolation)
+          const double c = (rt * rt - f0 + 2.0 * f0 * alpha) / (alpha * alpha);
+          const double anew = (c > 0.0) ? f0 / c : 0.5 * alpha;
+          alpha = std::min(std::max(anew, 0.1 * alpha), 0.5 * alpha);
+        } else {
+          alpha *= 0.9;
+        }
       }
       if (alpha < o.min_step) {
         // no decrease: keep u (src/FEM3D.jl:144-147) and restore the state at u
@@ -144,6 +154,7 @@ static int newton_dev(fg_mesh *m, double *d_u, const fg_newton_opts &o, fg_newto
     if (ratio <= o.tol_update) { converged = 1; break; }
     if (need_jacobian) fg_newton_assemble(m, d_u, o.Ms, o.Hk, mixed, d_F, true);
   }
+  fg_energy_dev(m, d_u, o.Ms, o.Hk);
   double energy = fg_dot_dev(m, m->wdens, nullptr, m->nt, false);
   FG_CUDA_TRY(cudaEventRecord(e1, m->stream));
   fg_sync(m);
@@ -184,7 +195,10 @@ extern "C" fg_status fg_newton_magnetostatics(fg_mesh *m, const uint8_t *nl, con
     upload(m, d_u, u0, sizeof(double) * (size_t)m->nv);
     int rc = newton_dev(m, d_u, opts, s);
     download(m, u, d_u, sizeof(double) * (size_t)m->nv);
-    if (H) download(m, H, m->H, sizeof(double) * 3 * (size_t)m->nt);
+    if (H) {
+      fg_hfield_dev(m, d_u, m->H);
+      download(m, H, m->H, sizeof(double) * 3 * (size_t)m->nt);
+    }
     if (mu) download(m, mu, m->mu, sizeof(double) * (size_t)m->nt);
     fg_sync(m);
     return rc == 0 ? FG_OK : FG_NOT_CONVERGED;

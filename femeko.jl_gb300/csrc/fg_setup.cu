@@ -155,21 +155,29 @@ template <int CAP>
 __global__ void k_row_fill(const int *__restrict__ iptr, const int *__restrict__ inc, const int *__restrict__ t,
                            int64_t nt, int npe, int64_t nv, const int *__restrict__ rowptr,
                            const int *__restrict__ sl_ptr, const int *__restrict__ sl_len, int *__restrict__ colidx,
-                           int *__restrict__ sl_col, uint8_t *__restrict__ diagk, int *flags) {
+                           int *__restrict__ sl_col, int16_t *__restrict__ sl_dcol, uint8_t *__restrict__ diagk,
+                           int *flags) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nv) return;
   int nb[CAP];
   int len = gather_row<CAP>(i, iptr, inc, t, nt, npe, nb, flags);
   int rb = rowptr[i];
   int s = (int)(i / FG_SLICE), lane = (int)(i % FG_SLICE);
-  int sb = sl_ptr[s] + lane, sl = sl_len[s];
+  int64_t sb = sl_ptr[s];
+  int slots = FG_GROUP * sl_len[s];
   int dk = 0;
-  for (int k = 0; k < len; ++k) {
-    colidx[rb + k] = nb[k];
-    sl_col[sb + k * FG_SLICE] = nb[k];
-    if (nb[k] == (int)i) dk = k;
+  bool wide = false;
+  for (int k = 0; k < slots; ++k) {
+    int c = (k < len) ? nb[k] : (int)i;  // pads point at the row itself (value 0)
+    if (k < len) colidx[rb + k] = c;
+    int64_t pos = sell_pos(sb, lane, k);
+    sl_col[pos] = c;
+    int d = c - (int)i;
+    if (d < -32768 || d > 32767) { wide = true; d = 0; }
+    sl_dcol[pos] = (int16_t)d;
+    if (c == (int)i && k < len) dk = k;
   }
-  for (int k = len; k < sl; ++k) sl_col[sb + k * FG_SLICE] = (int)i;
+  if (wide) atomicOr(flags + 1, 1);
   diagk[i] = (uint8_t)dk;
 }
 
@@ -238,6 +246,14 @@ __global__ void k_geom_tet(const double *__restrict__ p, const int *__restrict__
   geo[6 * nt + k] = g2x; geo[7 * nt + k] = g2y; geo[8 * nt + k] = g2z;
   geo[9 * nt + k] = g3x; geo[10 * nt + k] = g3y; geo[11 * nt + k] = g3z;
   geo[12 * nt + k] = fabs(det) / 6.0;
+  // Gram matrix G_ab = grad(phi_a).grad(phi_b), upper triangle row by row (10 values):
+  // VE * G is the element stiffness for unit coefficient, the matrix the reference
+  // computes once per mesh as Ak (Magnetostatics/NewtonRaphson.jl:112).
+  double g[4][3] = {{-(g1x + g2x + g3x), -(g1y + g2y + g3y), -(g1z + g2z + g3z)},
+                    {g1x, g1y, g1z}, {g2x, g2y, g2z}, {g3x, g3y, g3z}};
+  int c = 13;
+  for (int a = 0; a < 4; ++a)
+    for (int b = a; b < 4; ++b) geo[(int64_t)(c++) * nt + k] = g[a][0] * g[b][0] + g[a][1] * g[b][1] + g[a][2] * g[b][2];
 }
 
 // P1 triangle geometry: gradients of the three barycentric functions (6 values)
@@ -375,11 +391,12 @@ extern "C" fg_status fg_mesh_create(const double *p, int64_t nv, const int32_t *
         mx = std::max(mx, hrl[r]);
         md = std::max(md, hdeg[r]);
       }
-      hsl_len[sl] = mx;
+      int groups = std::max(1, (mx + FG_GROUP - 1) / FG_GROUP);
+      hsl_len[sl] = groups;
       hin_len[sl] = md;
       hsl_ptr[sl] = (int)acc;
       hin_ptr[sl] = (int)acc2;
-      acc += (int64_t)mx * FG_SLICE;
+      acc += (int64_t)groups * FG_GROUP * FG_SLICE;
       acc2 += (int64_t)md * FG_SLICE;
       FG_REQUIRE(acc < ((int64_t)1 << 31) && acc2 * npe < ((int64_t)1 << 31), FG_BAD_ARG,
                  "fg_mesh_create: padded layout too large");
@@ -394,6 +411,9 @@ extern "C" fg_status fg_mesh_create(const double *p, int64_t nv, const int32_t *
     m->sl_ptr = dev_alloc<int>(m, (size_t)m->nslices + 1);
     m->sl_len = dev_alloc<int>(m, (size_t)m->nslices);
     m->sl_col = dev_alloc<int>(m, (size_t)m->nsell);
+    m->sl_dcol = dev_alloc<int16_t>(m, (size_t)m->nsell);
+    m->nvp = (int64_t)m->nslices * FG_SLICE;
+    m->maxrow4 = (m->maxrow + FG_GROUP - 1) / FG_GROUP * FG_GROUP;
     m->diagk = dev_alloc<uint8_t>(m, (size_t)nv);
     m->in_ptr = dev_alloc<int>(m, (size_t)m->nslices + 1);
     m->in_len = dev_alloc<int>(m, (size_t)m->nslices);
@@ -406,16 +426,24 @@ extern "C" fg_status fg_mesh_create(const double *p, int64_t nv, const int32_t *
     FG_CUDA_TRY(cudaMemcpyAsync(m->in_len, hin_len.data(), sizeof(int) * m->nslices, cudaMemcpyHostToDevice, s));
     if (big)
       k_row_fill<FG_MAX_ROW><<<grid_for(nv, 64), 64, 0, s>>>(iptr, inc, m->t, nt, npe, nv, m->rowptr, m->sl_ptr,
-                                                             m->sl_len, m->colidx, m->sl_col, m->diagk, m->flags);
+                                                             m->sl_len, m->colidx, m->sl_col, m->sl_dcol, m->diagk,
+                                                             m->flags);
     else
       k_row_fill<128><<<grid_for(nv, 128), 128, 0, s>>>(iptr, inc, m->t, nt, npe, nv, m->rowptr, m->sl_ptr,
-                                                         m->sl_len, m->colidx, m->sl_col, m->diagk, m->flags);
+                                                         m->sl_len, m->colidx, m->sl_col, m->sl_dcol, m->diagk,
+                                                         m->flags);
+    {
+      int wide = 0;
+      FG_CUDA_TRY(cudaMemcpyAsync(&wide, m->flags + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+      fg_sync(m);
+      m->use_dcol = (wide == 0);  // 16-bit column offsets when the bandwidth allows
+    }
     k_slots<<<grid_for(nv, 128), 128, 0, s>>>(iptr, inc, m->t, nt, npe, nv, m->rowptr, m->colidx, m->in_ptr,
                                               m->in_len, m->recpos, m->in_slot);
     FG_CUDA_TRY(cudaGetLastError());
 
     // geometry of the vertex simplex
-    m->ngeo = (m->dim == 3) ? 13 : 7;
+    m->ngeo = (m->dim == 3) ? 23 : 7;
     m->geo = dev_alloc<double>(m, (size_t)m->ngeo * nt);
     if (m->dim == 3)
       k_geom_tet<<<grid_for(nt, 256), 256, 0, s>>>(m->p, m->t, nt, m->geo, m->flags);

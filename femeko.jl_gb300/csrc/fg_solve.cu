@@ -1,20 +1,33 @@
-// SpMV and Jacobi-preconditioned CG on the SELL-32 operator.
+// SpMV and Jacobi-preconditioned CG on the SELL-32x4 operator.
 //
 // The reference solves with IterativeSolvers.cg (Magnetostatics/2DmagneticField.jl:139,
 // Micromagnetics/LL.jl:185, Femeko_jl_C++/Magnetostatics/run.jl:141) or Eigen's
-// diagonal-preconditioned ConjugateGradient (magnetostatics.cpp:26-38).  Here one CG
-// iteration is two kernels:
-//   k_cg_spmv   q = A pn with pn = z + beta p formed on the fly (no separate p pass),
-//               p.q reduced in the same launch, alpha computed by the last block;
-//   k_cg_update x += alpha pn, r -= alpha q, z = D^-1 r, r.z and r.r reduced, beta and
-//               the stopping test computed by the last block.
-// Scalars never leave the device; the host reads the "done" flag once per block of
-// iterations, and each block can be replayed as a CUDA graph.
+// diagonal-preconditioned ConjugateGradient (magnetostatics.cpp:26-38).
 //
-// Mixed precision: the operator values and the CG vectors are FP32; dot products
-// are accumulated with compensated FP32 sums inside a block and FP64 across blocks.
-// An FP64 residual b - A x (FP64 operator) drives iterative refinement around the
-// FP32 solves.  In the Newton solver the Newton loop itself is that refinement.
+// Layout: one thread per row; a row's slots come in groups of 4, so each group is one
+// 128-bit load of values (float4, or two double2) and one load of column indices
+// (int4, or short4 holding column - row when the matrix bandwidth fits 16 bits).
+// A warp's group loads are contiguous (512 B of FP32 values).
+//
+// Mixed precision (FP32 operator and vectors), two kernels per iteration:
+//   k_cg32_spmv   q = A pn with pn = z + beta p formed on the fly; p and z are
+//                 stored interleaved (one 8-byte gather per entry); p.q reduced,
+//                 alpha computed by the last block to finish;
+//   k_cg32_update x += alpha pn, r -= alpha q, z = D^-1 r on 4 rows per thread
+//                 (128-bit loads), r.z and r.r reduced, beta and the stopping test
+//                 computed by the last block.
+// Dot products use compensated (TwoSum) FP32 sums per thread and per block and FP64
+// across blocks.
+//
+// FP64 operator and vectors, three kernels per iteration (q = A p, the vector
+// update, p = z + beta p): on GB300 an FP64 FMA costs ~64 FP32 FMAs, so forming
+// z + beta p at every gathered entry would double the SpMV's FP64 work.
+//
+// Scalars never leave the device; the host reads the "done" flag once per block of
+// iterations, each block replayed as a CUDA graph.  An FP64 residual b - A x (FP64
+// operator) drives iterative refinement around the FP32 solves; in the Newton solver
+// the Newton loop itself is that refinement.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -100,25 +113,19 @@ __device__ __forceinline__ void block_sum_ff(ff (&v)[N], double (&out)[N], ff (*
   }
 }
 
-// Block sum of per-thread accumulators; thread 0 gets the totals as doubles.
-template <typename S, int N>
-__device__ __forceinline__ void block_sum_acc(Acc<S> *a, double (&out)[N]) {
-  if (sizeof(S) == 4) {
-    __shared__ ff shf[N][32];
-    ff v[N];
+template <int N>
+__device__ __forceinline__ void block_sum_acc(const Acc<float> (&a)[N], double (&out)[N]) {
+  __shared__ ff shf[N][32];
+  ff v[N];
 #pragma unroll
-    for (int j = 0; j < N; ++j) v[j] = reinterpret_cast<Acc<float> *>(a)[j].v;
-    block_sum_ff<N>(v, out, shf);
-  } else {
-    __shared__ double shd[N][32];
-#pragma unroll
-    for (int j = 0; j < N; ++j) out[j] = reinterpret_cast<Acc<double> *>(a)[j].v;
-    block_sum<N>(out, shd);
-  }
+  for (int j = 0; j < N; ++j) v[j] = a[j].v;
+  block_sum_ff<N>(v, out, shf);
 }
 
-// Block partials -> the last block to arrive sums them in block order.  Returns true
-// in thread 0 of the last block, with the totals in tot.
+// Block partials -> the last block to arrive sums them.  Returns true in thread 0 of
+// the last block, with the totals in tot.  The whole last block loads the partials
+// (independent loads), then a fixed-shape tree: the order of the sum depends only on
+// the grid size, so results are reproducible.
 template <int N>
 __device__ __forceinline__ bool grid_finish(const double (&v)[N], double *partials, unsigned *counter,
                                             double (&tot)[N]) {
@@ -133,8 +140,6 @@ __device__ __forceinline__ bool grid_finish(const double (&v)[N], double *partia
   __syncthreads();
   if (!s_last) return false;
   __threadfence();
-  // The whole last block loads the partials (independent loads, one pass), then a
-  // fixed-shape tree: the order of the sum depends only on the grid size.
   double acc[N];
 #pragma unroll
   for (int j = 0; j < N; ++j) acc[j] = 0.0;
@@ -149,35 +154,63 @@ __device__ __forceinline__ bool grid_finish(const double (&v)[N], double *partia
   return threadIdx.x == 0;
 }
 
-// ------------------------------------------------------------------ CG kernels
-template <typename V, typename S>
-__global__ void __launch_bounds__(256) k_cg_spmv(int64_t n, const int *__restrict__ sl_ptr,
-                                                 const int *__restrict__ sl_len, const int *__restrict__ col,
-                                                 const V *__restrict__ val, const S *__restrict__ z,
-                                                 const S *__restrict__ p, S *__restrict__ pn, S *__restrict__ q,
-                                                 double *scal, int *ictl, double *partials, unsigned *counter) {
+// ------------------------------------------------------------------ index helpers
+// Column loads: absolute int32 columns (int4 per group) or 16-bit offsets from the
+// row (short4 per group).
+struct ColAbs {
+  typedef int T;
+  typedef int4 T4;
+  static __device__ __forceinline__ int col(T c, int64_t) { return c; }
+};
+struct ColRel {
+  typedef int16_t T;
+  typedef short4 T4;
+  static __device__ __forceinline__ int col(T c, int64_t row) { return (int)row + (int)c; }
+};
+
+__device__ __forceinline__ int4 ld_cols(const int4 *p) { return __ldg(p); }
+__device__ __forceinline__ short4 ld_cols(const short4 *p) { return __ldg(p); }
+
+// ------------------------------------------------------------------ FP32 CG kernels
+template <class CI>
+__global__ void __launch_bounds__(256) k_cg32_spmv(int64_t n, const int *__restrict__ sl_ptr,
+                                                   const int *__restrict__ sl_len,
+                                                   const typename CI::T *__restrict__ col,
+                                                   const float *__restrict__ val, const float2 *__restrict__ pz_in,
+                                                   float2 *__restrict__ pz_out, float *__restrict__ q, double *scal,
+                                                   int *ictl, double *partials, unsigned *counter) {
   if (ictl[I_DONE]) return;
-  const S beta = (S)scal[S_BETA];
-  Acc<S> prod;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    int s = (int)(i >> 5), lane = (int)(i & 31);
-    int64_t base = sl_ptr[s] + lane;
-    int L = sl_len[s];
-    S acc = 0;
+  const float beta = (float)scal[S_BETA];
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  Acc<float> prod[1];
+  if (i < n) {
+    const int s = (int)(i >> 5), lane = (int)(i & 31);
+    const int64_t base = (int64_t)sl_ptr[s] + lane * FG_GROUP;
+    const int G = sl_len[s];
+    const float4 *v4 = reinterpret_cast<const float4 *>(val + base);
+    const typename CI::T4 *c4 = reinterpret_cast<const typename CI::T4 *>(col + base);
+    float acc = 0.f;
 #pragma unroll 4
-    for (int k = 0; k < L; ++k) {
-      int c = __ldg(col + base + (int64_t)k * FG_SLICE);
-      S xv = fma(beta, p[c], z[c]);
-      acc = fma((S)__ldg(val + base + (int64_t)k * FG_SLICE), xv, acc);
+    for (int g = 0; g < G; ++g) {
+      const float4 vv = __ldg(v4 + (int64_t)g * FG_SLICE);
+      const typename CI::T4 cc = ld_cols(c4 + (int64_t)g * FG_SLICE);
+      const float2 a = __ldg(pz_in + CI::col(cc.x, i));
+      const float2 b = __ldg(pz_in + CI::col(cc.y, i));
+      const float2 c = __ldg(pz_in + CI::col(cc.z, i));
+      const float2 d = __ldg(pz_in + CI::col(cc.w, i));
+      acc = fmaf(vv.x, fmaf(beta, a.x, a.y), acc);
+      acc = fmaf(vv.y, fmaf(beta, b.x, b.y), acc);
+      acc = fmaf(vv.z, fmaf(beta, c.x, c.y), acc);
+      acc = fmaf(vv.w, fmaf(beta, d.x, d.y), acc);
     }
-    S pi = fma(beta, p[i], z[i]);
-    pn[i] = pi;
+    const float2 own = __ldg(pz_in + i);
+    const float pi = fmaf(beta, own.x, own.y);
+    reinterpret_cast<float *>(pz_out)[2 * i] = pi;   // p of the next pair
     q[i] = acc;
-    prod.add(pi * acc);
+    prod[0].add(pi * acc);
   }
   double part[1];
-  block_sum_acc<S, 1>(&prod, part);
+  block_sum_acc<1>(prod, part);
   double tot[1];
   if (grid_finish<1>(part, partials, counter, tot)) {
     scal[S_PQ] = tot[0];
@@ -185,58 +218,66 @@ __global__ void __launch_bounds__(256) k_cg_spmv(int64_t n, const int *__restric
   }
 }
 
-template <typename S>
-__global__ void __launch_bounds__(256) k_cg_update(int64_t n, S *__restrict__ x, S *__restrict__ r,
-                                                   S *__restrict__ z, const S *__restrict__ pn,
-                                                   const S *__restrict__ q, const S *__restrict__ dinv,
-                                                   double *scal, int *ictl, double *partials, unsigned *counter) {
-  if (ictl[I_DONE]) return;
-  const S alpha = (S)scal[S_ALPHA];
-  Acc<S> a2[2];
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    S xi = fma(alpha, pn[i], x[i]);
-    S ri = fma(-alpha, q[i], r[i]);
-    S zi = dinv[i] * ri;
-    x[i] = xi;
-    r[i] = ri;
-    z[i] = zi;
-    a2[0].add(ri * zi);
-    a2[1].add(ri * ri);
-  }
-  double part[2];
-  block_sum_acc<S, 2>(a2, part);
-  double tot[2];
-  if (grid_finish<2>(part, partials, counter, tot)) {
-    double rzo = scal[S_RZ];
-    scal[S_BETA] = (rzo != 0.0) ? tot[0] / rzo : 0.0;
-    scal[S_RZ] = tot[0];
-    scal[S_RR] = tot[1];
-    int it = ictl[I_ITERS] + 1;
-    ictl[I_ITERS] = it;
-    if (!isfinite(tot[1])) { ictl[I_STATUS] = 2; ictl[I_DONE] = 1; }
-    else if (tot[1] <= scal[S_TOL2]) { ictl[I_STATUS] = 0; ictl[I_DONE] = 1; }
-    else if (it >= ictl[I_MAXIT]) { ictl[I_STATUS] = 1; ictl[I_DONE] = 1; }
-  }
+// Common tail of the vector-update kernels: beta, the iteration count and the
+// stopping test (r.r <= TOL2, non-finite, or the iteration cap).
+__device__ __forceinline__ void cg_finish_update(const double (&tot)[2], double *scal, int *ictl) {
+  double rzo = scal[S_RZ];
+  scal[S_BETA] = (rzo != 0.0) ? tot[0] / rzo : 0.0;
+  scal[S_RZ] = tot[0];
+  scal[S_RR] = tot[1];
+  int it = ictl[I_ITERS] + 1;
+  ictl[I_ITERS] = it;
+  if (!isfinite(tot[1])) { ictl[I_STATUS] = 2; ictl[I_DONE] = 1; }
+  else if (tot[1] <= scal[S_TOL2]) { ictl[I_STATUS] = 0; ictl[I_DONE] = 1; }
+  else if (it >= ictl[I_MAXIT]) { ictl[I_STATUS] = 1; ictl[I_DONE] = 1; }
 }
 
-// r = scale * rin (FP64 -> S), x = 0, z = D^-1 r, p = 0; reduces r.z and r.r and
-// sets the CG scalars.  tol2_rel: stop when r.r <= tol2_rel * r0.r0.
-template <typename S>
-__global__ void __launch_bounds__(256) k_cg_init(int64_t n, const double *__restrict__ rin, double scale,
-                                                 S *__restrict__ x, S *__restrict__ r, S *__restrict__ z,
-                                                 S *__restrict__ p, const S *__restrict__ dinv, double tol2_rel,
-                                                 int maxit, double *scal, int *ictl, double *partials,
-                                                 unsigned *counter) {
+// Four rows per thread; n4 = padded rows / 4 (padded entries are zero).
+__global__ void __launch_bounds__(256) k_cg32_update(int64_t n4, float4 *__restrict__ x, float4 *__restrict__ r,
+                                                     const float4 *__restrict__ q, const float4 *__restrict__ dinv,
+                                                     float4 *__restrict__ pz, double *scal, int *ictl,
+                                                     double *partials, unsigned *counter) {
+  if (ictl[I_DONE]) return;
+  const float alpha = (float)scal[S_ALPHA];
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  Acc<float> a2[2];
+  if (j < n4) {
+    float4 xx = x[j], rr = r[j];
+    const float4 qq = q[j], dd = dinv[j];
+    float4 pz0 = pz[2 * j], pz1 = pz[2 * j + 1];   // (p0, z0, p1, z1), (p2, z2, p3, z3)
+    xx.x = fmaf(alpha, pz0.x, xx.x); xx.y = fmaf(alpha, pz0.z, xx.y);
+    xx.z = fmaf(alpha, pz1.x, xx.z); xx.w = fmaf(alpha, pz1.z, xx.w);
+    rr.x = fmaf(-alpha, qq.x, rr.x); rr.y = fmaf(-alpha, qq.y, rr.y);
+    rr.z = fmaf(-alpha, qq.z, rr.z); rr.w = fmaf(-alpha, qq.w, rr.w);
+    pz0.y = dd.x * rr.x; pz0.w = dd.y * rr.y; pz1.y = dd.z * rr.z; pz1.w = dd.w * rr.w;
+    x[j] = xx;
+    r[j] = rr;
+    pz[2 * j] = pz0;
+    pz[2 * j + 1] = pz1;
+    a2[0].add(rr.x * pz0.y); a2[0].add(rr.y * pz0.w); a2[0].add(rr.z * pz1.y); a2[0].add(rr.w * pz1.w);
+    a2[1].add(rr.x * rr.x); a2[1].add(rr.y * rr.y); a2[1].add(rr.z * rr.z); a2[1].add(rr.w * rr.w);
+  }
+  double part[2];
+  block_sum_acc<2>(a2, part);
+  double tot[2];
+  if (grid_finish<2>(part, partials, counter, tot)) cg_finish_update(tot, scal, ictl);
+}
+
+// r = scale * rin, z = D^-1 r, (p, z) = (0, z), x = 0; r.z and r.r set the scalars.
+// Stop when r.r <= tol2_rel * r0.r0.
+__global__ void __launch_bounds__(256) k_cg32_init(int64_t n, int64_t np, const double *__restrict__ rin,
+                                                   double scale, float *__restrict__ x, float *__restrict__ r,
+                                                   float2 *__restrict__ pz, const float *__restrict__ dinv,
+                                                   double tol2_rel, int maxit, double *scal, int *ictl,
+                                                   double *partials, unsigned *counter) {
   double rz = 0, rr = 0;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    S ri = (S)(scale * rin[i]);
-    S zi = dinv[i] * ri;
-    x[i] = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < np; i += stride) {
+    float ri = (i < n) ? (float)(scale * rin[i]) : 0.f;
+    float zi = dinv[i] * ri;
+    x[i] = 0.f;
     r[i] = ri;
-    z[i] = zi;
-    p[i] = 0;
+    pz[i] = make_float2(0.f, zi);
     rz += (double)ri * (double)zi;
     rr += (double)ri * (double)ri;
   }
@@ -257,30 +298,153 @@ __global__ void __launch_bounds__(256) k_cg_init(int64_t n, const double *__rest
   }
 }
 
-// ------------------------------------------------------------------ FP64 helpers
-// y = A x (SELL FP64); with b != null computes r = b - A x; rows with fixed[i] are
-// set to 0 when zero_fixed.  Reduces r.r into scal[slot] when slot >= 0.
-template <typename V>
-__global__ void __launch_bounds__(256) k_spmv_sell(int64_t n, const int *__restrict__ sl_ptr,
-                                                   const int *__restrict__ sl_len, const int *__restrict__ col,
-                                                   const V *__restrict__ val, const double *__restrict__ x,
-                                                   const double *__restrict__ b, double *__restrict__ y,
-                                                   const uint8_t *__restrict__ fixed, int slot, double *scal,
-                                                   double *partials, unsigned *counter) {
-  double rr = 0.0;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    int s = (int)(i >> 5), lane = (int)(i & 31);
-    int64_t base = sl_ptr[s] + lane;
-    int L = sl_len[s];
+// ------------------------------------------------------------------ FP64 CG kernels
+template <class CI>
+__global__ void __launch_bounds__(256) k_cg64_spmv(int64_t n, const int *__restrict__ sl_ptr,
+                                                   const int *__restrict__ sl_len,
+                                                   const typename CI::T *__restrict__ col,
+                                                   const double *__restrict__ val, const double *__restrict__ p,
+                                                   double *__restrict__ q, double *scal, int *ictl, double *partials,
+                                                   unsigned *counter) {
+  if (ictl[I_DONE]) return;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double prod = 0.0;
+  if (i < n) {
+    const int s = (int)(i >> 5), lane = (int)(i & 31);
+    const int64_t base = (int64_t)sl_ptr[s] + lane * FG_GROUP;
+    const int G = sl_len[s];
+    const double2 *v2 = reinterpret_cast<const double2 *>(val + base);
+    const typename CI::T4 *c4 = reinterpret_cast<const typename CI::T4 *>(col + base);
     double acc = 0.0;
 #pragma unroll 4
-    for (int k = 0; k < L; ++k)
-      acc = fma((double)__ldg(val + base + (int64_t)k * FG_SLICE), x[__ldg(col + base + (int64_t)k * FG_SLICE)], acc);
+    for (int g = 0; g < G; ++g) {
+      const double2 va = __ldg(v2 + (int64_t)g * 2 * FG_SLICE);
+      const double2 vb = __ldg(v2 + (int64_t)g * 2 * FG_SLICE + 1);
+      const typename CI::T4 cc = ld_cols(c4 + (int64_t)g * FG_SLICE);
+      acc = fma(va.x, __ldg(p + CI::col(cc.x, i)), acc);
+      acc = fma(va.y, __ldg(p + CI::col(cc.y, i)), acc);
+      acc = fma(vb.x, __ldg(p + CI::col(cc.z, i)), acc);
+      acc = fma(vb.y, __ldg(p + CI::col(cc.w, i)), acc);
+    }
+    q[i] = acc;
+    prod = p[i] * acc;
+  }
+  __shared__ double shd[1][32];
+  double part[1] = {prod};
+  block_sum<1>(part, shd);
+  double tot[1];
+  if (grid_finish<1>(part, partials, counter, tot)) {
+    scal[S_PQ] = tot[0];
+    scal[S_ALPHA] = (tot[0] != 0.0) ? scal[S_RZ] / tot[0] : 0.0;
+  }
+}
+
+// Four rows per thread (two double2 per vector).
+__global__ void __launch_bounds__(256) k_cg64_update(int64_t n4, double2 *__restrict__ x, double2 *__restrict__ r,
+                                                     double2 *__restrict__ z, const double2 *__restrict__ p,
+                                                     const double2 *__restrict__ q, const double2 *__restrict__ dinv,
+                                                     double *scal, int *ictl, double *partials, unsigned *counter) {
+  if (ictl[I_DONE]) return;
+  const double alpha = scal[S_ALPHA];
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double rz = 0.0, rrs = 0.0;
+  if (j < n4) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int64_t k = 2 * j + h;
+      double2 xx = x[k], rr = r[k];
+      const double2 pp = p[k], qq = q[k], dd = dinv[k];
+      xx.x = fma(alpha, pp.x, xx.x); xx.y = fma(alpha, pp.y, xx.y);
+      rr.x = fma(-alpha, qq.x, rr.x); rr.y = fma(-alpha, qq.y, rr.y);
+      double2 zz = make_double2(dd.x * rr.x, dd.y * rr.y);
+      x[k] = xx;
+      r[k] = rr;
+      z[k] = zz;
+      rz += rr.x * zz.x + rr.y * zz.y;
+      rrs += rr.x * rr.x + rr.y * rr.y;
+    }
+  }
+  __shared__ double shd[2][32];
+  double part[2] = {rz, rrs};
+  block_sum<2>(part, shd);
+  double tot[2];
+  if (grid_finish<2>(part, partials, counter, tot)) cg_finish_update(tot, scal, ictl);
+}
+
+__global__ void __launch_bounds__(256) k_cg64_pupd(int64_t n2, const double2 *__restrict__ z, double2 *__restrict__ p,
+                                                   const double *scal, const int *ictl) {
+  if (ictl[I_DONE]) return;
+  const double beta = scal[S_BETA];
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n2) {
+    double2 zz = z[j], pp = p[j];
+    p[j] = make_double2(fma(beta, pp.x, zz.x), fma(beta, pp.y, zz.y));
+  }
+}
+
+__global__ void __launch_bounds__(256) k_cg64_init(int64_t n, int64_t np, const double *__restrict__ rin,
+                                                   double scale, double *__restrict__ x, double *__restrict__ r,
+                                                   double *__restrict__ z, double *__restrict__ p,
+                                                   const double *__restrict__ dinv, double tol2_rel, int maxit,
+                                                   double *scal, int *ictl, double *partials, unsigned *counter) {
+  double rz = 0, rr = 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < np; i += stride) {
+    double ri = (i < n) ? scale * rin[i] : 0.0;
+    double zi = dinv[i] * ri;
+    x[i] = 0.0;
+    r[i] = ri;
+    z[i] = zi;
+    p[i] = zi;
+    rz += ri * zi;
+    rr += ri * ri;
+  }
+  __shared__ double shd[2][32];
+  double part[2] = {rz, rr};
+  block_sum<2>(part, shd);
+  double tot[2];
+  if (grid_finish<2>(part, partials, counter, tot)) {
+    scal[S_RZ] = tot[0];
+    scal[S_RR] = tot[1];
+    scal[S_BETA] = 0.0;
+    scal[S_ALPHA] = 0.0;
+    scal[S_TOL2] = tol2_rel * tot[1];
+    ictl[I_ITERS] = 0;
+    ictl[I_MAXIT] = maxit;
+    ictl[I_STATUS] = 0;
+    ictl[I_DONE] = (tot[1] <= scal[S_TOL2] || tot[1] == 0.0) ? 1 : 0;
+  }
+}
+
+// ------------------------------------------------------------------ FP64 helpers
+// y = A x (FP64 operator); with b != null, r = b - A x.  Rows with fixed[i] are set
+// to 0.  Reduces r.r into scal[slot] when slot >= 0.
+template <class CI>
+__global__ void __launch_bounds__(256) k_spmv64(int64_t n, const int *__restrict__ sl_ptr,
+                                                const int *__restrict__ sl_len, const typename CI::T *__restrict__ col,
+                                                const double *__restrict__ val, const double *__restrict__ x,
+                                                const double *__restrict__ b, double *__restrict__ y,
+                                                const uint8_t *__restrict__ fixed, int slot, double *scal,
+                                                double *partials, unsigned *counter) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double rr = 0.0;
+  if (i < n) {
+    const int s = (int)(i >> 5), lane = (int)(i & 31);
+    const int64_t base = (int64_t)sl_ptr[s] + lane * FG_GROUP;
+    const int G = sl_len[s];
+    double acc = 0.0;
+    for (int g = 0; g < G; ++g) {
+      const typename CI::T4 cc = ld_cols(reinterpret_cast<const typename CI::T4 *>(col + base) + (int64_t)g * FG_SLICE);
+      const double *vg = val + base + (int64_t)g * FG_GROUP * FG_SLICE;
+      acc = fma(vg[0], x[CI::col(cc.x, i)], acc);
+      acc = fma(vg[1], x[CI::col(cc.y, i)], acc);
+      acc = fma(vg[2], x[CI::col(cc.z, i)], acc);
+      acc = fma(vg[3], x[CI::col(cc.w, i)], acc);
+    }
     double v = b ? b[i] - acc : acc;
     if (fixed && fixed[i]) v = 0.0;
     y[i] = v;
-    rr += v * v;
+    rr = v * v;
   }
   if (slot < 0) return;
   __shared__ double shd[1][32];
@@ -310,19 +474,18 @@ __global__ void k_axpy_to64(int64_t n, double scale, const S *__restrict__ d, do
     x[i] += scale * (double)d[i];
 }
 
-// ------------------------------------------------------------------ host helpers
-// Grid of the row-parallel reduction kernels: at most 8 blocks of 256 threads per SM,
-// rows visited with a grid-stride loop, so the last block sums a few hundred partials.
-static unsigned cg_grid(const fg_mesh *m) {
-  unsigned g = grid_for(m->nv, 256);
-  unsigned cap = 8u * (unsigned)(m->sm_count > 0 ? m->sm_count : 152);
-  return g < cap ? g : cap;
+__global__ void k_fill64(int64_t n, double v, double *__restrict__ x) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = v;
 }
 
+// ------------------------------------------------------------------ host helpers
 static unsigned red_grid(int64_t n) {
   unsigned g = grid_for(n, 256);
   return g > (unsigned)FG_RED_BLOCKS ? (unsigned)FG_RED_BLOCKS : g;
 }
+static unsigned row_grid(const fg_mesh *m) { return grid_for(m->nv, 256); }
+static unsigned quad_grid(const fg_mesh *m) { return grid_for(m->nvp / 4, 256); }
 
 double fg_dot_dev(fg_mesh *m, const double *x, const double *y, int64_t n, bool mask_fixed) {
   const int slot = 8;
@@ -339,53 +502,91 @@ double fg_norm2_dev(fg_mesh *m, const double *x, int64_t n, bool mask_fixed) {
   return std::sqrt(fg_dot_dev(m, x, x, n, mask_fixed));
 }
 
-void fg_spmv64_dev(fg_mesh *m, const double *x, double *y) {
+static void spmv64_launch(fg_mesh *m, const double *x, const double *b, double *y, const uint8_t *fx, int slot) {
   FG_REQUIRE(m->val64 != nullptr, FG_BAD_ARG, "no FP64 operator assembled");
-  k_spmv_sell<double><<<cg_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val64,
-                                                                     x, nullptr, y, nullptr, -1, m->scal,
-                                                                     m->red.partials, m->red.counter);
+  if (m->use_dcol)
+    k_spmv64<ColRel><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, m->val64, x, b, y,
+                                                         fx, slot, m->scal, m->red.partials, m->red.counter);
+  else
+    k_spmv64<ColAbs><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val64, x, b, y,
+                                                         fx, slot, m->scal, m->red.partials, m->red.counter);
   FG_CUDA_TRY(cudaGetLastError());
   FG_LAUNCHED(1);
 }
 
-// CG vectors: FP64 set uses v64[0..5], FP32 set uses v32[0..5]:
-// 0 x(correction), 1 r, 2 z, 3 p, 4 pn, 5 q
-template <typename S>
-static S **cg_vectors(fg_mesh *m);
-template <>
-double **cg_vectors<double>(fg_mesh *m) {
-  for (int j = 0; j < 6; ++j)
-    if (!m->v64[j]) m->v64[j] = dev_alloc<double>(m, (size_t)m->nv);
-  return m->v64;
+void fg_spmv64_dev(fg_mesh *m, const double *x, double *y) { spmv64_launch(m, x, nullptr, y, nullptr, -1); }
+
+// CG vectors, padded to whole slices and zeroed once (pads stay zero).
+// FP32 set: v32[0] x, v32[1] r, v32[2] q, v32[3] (p,z) pair 0, v32[4] (p,z) pair 1.
+// FP64 set: v64[0] x, v64[1] r, v64[2] z, v64[3] p, v64[4] q.
+static void ensure_cg32(fg_mesh *m) {
+  for (int j = 0; j < 5; ++j)
+    if (!m->v32[j]) {
+      size_t len = (size_t)m->nvp * (j >= 3 ? 2 : 1);
+      m->v32[j] = dev_alloc<float>(m, len);
+      FG_CUDA_TRY(cudaMemsetAsync(m->v32[j], 0, sizeof(float) * len, m->stream));
+    }
 }
-template <>
-float **cg_vectors<float>(fg_mesh *m) {
-  for (int j = 0; j < 6; ++j)
-    if (!m->v32[j]) m->v32[j] = dev_alloc<float>(m, (size_t)m->nv);
-  return m->v32;
+static void ensure_cg64(fg_mesh *m) {
+  for (int j = 0; j < 5; ++j)
+    if (!m->v64[j]) {
+      m->v64[j] = dev_alloc<double>(m, (size_t)m->nvp);
+      FG_CUDA_TRY(cudaMemsetAsync(m->v64[j], 0, sizeof(double) * (size_t)m->nvp, m->stream));
+    }
 }
 
-template <typename V, typename S>
-static void launch_iteration(fg_mesh *m, const V *val, const S *dinv, S **v, bool odd) {
-  S *p = odd ? v[4] : v[3];
-  S *pn = odd ? v[3] : v[4];
-  unsigned g = cg_grid(m);
-  k_cg_spmv<V, S><<<g, 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col, val, v[2], p, pn, v[5], m->scal,
-                                            m->ictl, m->red.partials, m->red.counter);
-  k_cg_update<S><<<g, 256, 0, m->stream>>>(m->nv, v[0], v[1], v[2], pn, v[5], dinv, m->scal, m->ictl,
-                                           m->red.partials, m->red.counter);
+static void launch_iter32(fg_mesh *m, bool odd) {
+  float2 *pz_in = reinterpret_cast<float2 *>(odd ? m->v32[4] : m->v32[3]);
+  float2 *pz_out = reinterpret_cast<float2 *>(odd ? m->v32[3] : m->v32[4]);
+  if (m->use_dcol)
+    k_cg32_spmv<ColRel><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, m->val32, pz_in,
+                                                            pz_out, m->v32[2], m->scal, m->ictl, m->red.partials,
+                                                            m->red.counter);
+  else
+    k_cg32_spmv<ColAbs><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val32, pz_in,
+                                                            pz_out, m->v32[2], m->scal, m->ictl, m->red.partials,
+                                                            m->red.counter);
+  k_cg32_update<<<quad_grid(m), 256, 0, m->stream>>>(
+      m->nvp / 4, reinterpret_cast<float4 *>(m->v32[0]), reinterpret_cast<float4 *>(m->v32[1]),
+      reinterpret_cast<const float4 *>(m->v32[2]), reinterpret_cast<const float4 *>(m->dinv32),
+      reinterpret_cast<float4 *>(pz_out), m->scal, m->ictl, m->red.partials, m->red.counter);
 }
 
-// Runs inner PCG iterations until the device sets "done".  Returns iterations.
-template <typename V, typename S>
-static int run_cg(fg_mesh *m, const V *val, const S *dinv, const fg_solve_opts &o, int maxit, int *status) {
-  S **v = cg_vectors<S>(m);
+static void launch_iter64(fg_mesh *m) {
+  if (m->use_dcol)
+    k_cg64_spmv<ColRel><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, m->val64,
+                                                            m->v64[3], m->v64[4], m->scal, m->ictl, m->red.partials,
+                                                            m->red.counter);
+  else
+    k_cg64_spmv<ColAbs><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val64,
+                                                            m->v64[3], m->v64[4], m->scal, m->ictl, m->red.partials,
+                                                            m->red.counter);
+  k_cg64_update<<<quad_grid(m), 256, 0, m->stream>>>(
+      m->nvp / 4, reinterpret_cast<double2 *>(m->v64[0]), reinterpret_cast<double2 *>(m->v64[1]),
+      reinterpret_cast<double2 *>(m->v64[2]), reinterpret_cast<const double2 *>(m->v64[3]),
+      reinterpret_cast<const double2 *>(m->v64[4]), reinterpret_cast<const double2 *>(m->dinv64), m->scal, m->ictl,
+      m->red.partials, m->red.counter);
+  k_cg64_pupd<<<grid_for(m->nvp / 2, 256), 256, 0, m->stream>>>(m->nvp / 2, reinterpret_cast<const double2 *>(m->v64[2]),
+                                                                reinterpret_cast<double2 *>(m->v64[3]), m->scal,
+                                                                m->ictl);
+}
+
+// Runs CG iterations until the device sets "done".  Returns the iteration count.
+static int run_cg(fg_mesh *m, bool mixed, const fg_solve_opts &o, int *status) {
   int block = o.check_every > 0 ? o.check_every : 32;
   if (block & 1) ++block;
-  int gslot = (sizeof(S) == 4 ? 1 : 0);
-  GraphCache &gc = m->graph[gslot];
-  const void *key[4] = {val, dinv, v[0], (const void *)(intptr_t)block};
-  bool use_graph = o.use_graph != 0;
+  const int per_iter = mixed ? 2 : 3;
+  GraphCache &gc = m->graph[mixed ? 1 : 0];
+  const void *key[4] = {mixed ? (const void *)m->val32 : (const void *)m->val64,
+                        mixed ? (const void *)m->v32[0] : (const void *)m->v64[0], (const void *)(intptr_t)block,
+                        (const void *)(intptr_t)m->use_dcol};
+  const bool use_graph = o.use_graph != 0;
+  auto enqueue_block = [&]() {
+    for (int it = 0; it < block; ++it) {
+      if (mixed) launch_iter32(m, it & 1);
+      else launch_iter64(m);
+    }
+  };
   if (use_graph) {
     bool match = gc.exec && gc.iters == block;
     for (int j = 0; j < 4 && match; ++j) match = (gc.key[j] == key[j]);
@@ -393,7 +594,7 @@ static int run_cg(fg_mesh *m, const V *val, const S *dinv, const fg_solve_opts &
       if (gc.exec) { cudaGraphExecDestroy(gc.exec); gc.exec = nullptr; }
       cudaGraph_t graph;
       FG_CUDA_TRY(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
-      for (int it = 0; it < block; ++it) launch_iteration<V, S>(m, val, dinv, v, it & 1);
+      enqueue_block();
       FG_CUDA_TRY(cudaStreamEndCapture(m->stream, &graph));
       FG_CUDA_TRY(cudaGraphInstantiate(&gc.exec, graph, 0));
       cudaGraphDestroy(graph);
@@ -404,26 +605,52 @@ static int run_cg(fg_mesh *m, const V *val, const S *dinv, const fg_solve_opts &
   for (;;) {
     if (use_graph) {
       FG_CUDA_TRY(cudaGraphLaunch(gc.exec, m->stream));
-      FG_LAUNCHED(2 * block);
     } else {
-      for (int it = 0; it < block; ++it) launch_iteration<V, S>(m, val, dinv, v, it & 1);
+      enqueue_block();
       FG_CUDA_TRY(cudaGetLastError());
-      FG_LAUNCHED(2 * block);
     }
+    FG_LAUNCHED((long long)per_iter * block);
     FG_CUDA_TRY(cudaMemcpyAsync(m->hint, m->ictl, sizeof(int) * 4, cudaMemcpyDeviceToHost, m->stream));
     fg_sync(m);
     if (m->hint[I_DONE]) break;
-    (void)maxit;
   }
   if (status) *status = m->hint[I_STATUS];
   return m->hint[I_ITERS];
+}
+
+// Inner solve of A d = scale * r64 from d = 0 to relative residual `inner`, then
+// x += d / scale.  Returns iterations; *ist = 0 converged, 1 cap, 2 non-finite.
+static int inner_solve(fg_mesh *m, bool mixed, const double *r64, double rn, double inner, int maxit,
+                       const fg_solve_opts &o, double *d_x, int *ist) {
+  unsigned g = red_grid(m->nvp);
+  int its;
+  if (mixed) {
+    ensure_cg32(m);
+    k_cg32_init<<<g, 256, 0, m->stream>>>(m->nv, m->nvp, r64, 1.0 / rn, m->v32[0], m->v32[1],
+                                          reinterpret_cast<float2 *>(m->v32[3]), m->dinv32, inner * inner, maxit,
+                                          m->scal, m->ictl, m->red.partials, m->red.counter);
+    FG_CUDA_TRY(cudaGetLastError());
+    its = run_cg(m, true, o, ist);
+    k_axpy_to64<float><<<red_grid(m->nv), 256, 0, m->stream>>>(m->nv, rn, m->v32[0], d_x);
+  } else {
+    ensure_cg64(m);
+    k_cg64_init<<<g, 256, 0, m->stream>>>(m->nv, m->nvp, r64, 1.0 / rn, m->v64[0], m->v64[1], m->v64[2], m->v64[3],
+                                          m->dinv64, inner * inner, maxit, m->scal, m->ictl, m->red.partials,
+                                          m->red.counter);
+    FG_CUDA_TRY(cudaGetLastError());
+    its = run_cg(m, false, o, ist);
+    k_axpy_to64<double><<<red_grid(m->nv), 256, 0, m->stream>>>(m->nv, rn, m->v64[0], d_x);
+  }
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(2);
+  return its;
 }
 
 int fg_pcg_solve(fg_mesh *m, const double *d_b, double *d_x, const fg_solve_opts &o, fg_solve_stats *st,
                  bool newton_inner) {
   const bool mixed = o.precision == FG_MIXED;
   FG_REQUIRE(mixed ? m->val32 != nullptr : m->val64 != nullptr, FG_BAD_ARG, "operator not assembled");
-  if (!m->v64[6]) m->v64[6] = dev_alloc<double>(m, (size_t)m->nv);
+  if (!m->v64[6]) m->v64[6] = dev_alloc<double>(m, (size_t)m->nvp);
   double *r64 = m->v64[6];
   const uint8_t *fx = m->has_fixed ? m->fixed : nullptr;
   FG_CUDA_TRY(cudaEventRecord(m->ev0, m->stream));
@@ -437,11 +664,7 @@ int fg_pcg_solve(fg_mesh *m, const double *d_b, double *d_x, const fg_solve_opts
       rn = fg_norm2_dev(m, r64, m->nv, true);
     } else {
       FG_REQUIRE(m->val64 != nullptr, FG_BAD_ARG, "refinement needs the FP64 operator");
-      k_spmv_sell<double><<<cg_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col,
-                                                                         m->val64, d_x, d_b, r64, fx, 9, m->scal,
-                                                                         m->red.partials, m->red.counter);
-      FG_CUDA_TRY(cudaGetLastError());
-      FG_LAUNCHED(1);
+      spmv64_launch(m, d_x, d_b, r64, fx, 9);
       FG_CUDA_TRY(cudaMemcpyAsync(m->hbuf, m->scal + 9, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
       fg_sync(m);
       rn = std::sqrt(m->hbuf[0]);
@@ -454,29 +677,8 @@ int fg_pcg_solve(fg_mesh *m, const double *d_b, double *d_x, const fg_solve_opts
     double rel = target / rn;  // inner relative target that would finish the job
     double inner = mixed ? std::max(rel, o.inner_rtol) : rel;
     if (newton_inner) inner = o.inner_rtol;
-    int maxit = o.maxiter - total;
-    int ist = 0, its = 0;
-    unsigned g = cg_grid(m);
-    if (mixed) {
-      float **v = cg_vectors<float>(m);
-      k_cg_init<float><<<g, 256, 0, m->stream>>>(m->nv, r64, 1.0 / rn, v[0], v[1], v[2], v[3], m->dinv32,
-                                                 inner * inner, maxit, m->scal, m->ictl, m->red.partials,
-                                                 m->red.counter);
-      FG_CUDA_TRY(cudaGetLastError());
-      its = run_cg<float, float>(m, m->val32, m->dinv32, o, maxit, &ist);
-      k_axpy_to64<float><<<g, 256, 0, m->stream>>>(m->nv, rn, v[0], d_x);
-    } else {
-      double **v = cg_vectors<double>(m);
-      k_cg_init<double><<<g, 256, 0, m->stream>>>(m->nv, r64, 1.0 / rn, v[0], v[1], v[2], v[3], m->dinv64,
-                                                  inner * inner, maxit, m->scal, m->ictl, m->red.partials,
-                                                  m->red.counter);
-      FG_CUDA_TRY(cudaGetLastError());
-      its = run_cg<double, double>(m, m->val64, m->dinv64, o, maxit, &ist);
-      k_axpy_to64<double><<<g, 256, 0, m->stream>>>(m->nv, rn, v[0], d_x);
-    }
-    FG_CUDA_TRY(cudaGetLastError());
-    FG_LAUNCHED(2);
-    total += its;
+    int ist = 0;
+    total += inner_solve(m, mixed, r64, rn, inner, o.maxiter - total, o, d_x, &ist);
     ++refinements;
     if (ist == 2) { status = 2; break; }
     if (newton_inner) { status = ist; break; }
@@ -510,7 +712,7 @@ extern "C" void fg_solve_opts_default(fg_solve_opts *o) {
 }
 
 // A standalone operator from a symmetric CSC matrix: a handle with the pattern and
-// values but no mesh.
+// values in SELL-32x4 layout but no mesh.
 static fg_mesh *matrix_handle(int64_t n, const int64_t *colptr, const int64_t *rowval, const double *nzval, int base,
                               bool want32) {
   FG_REQUIRE(n > 0 && n < ((int64_t)1 << 30), FG_BAD_ARG, "matrix size out of range");
@@ -527,52 +729,63 @@ static fg_mesh *matrix_handle(int64_t n, const int64_t *colptr, const int64_t *r
     m->nv = n;
     m->nnz = nnz;
     m->nslices = (int)((n + FG_SLICE - 1) / FG_SLICE);
+    m->nvp = (int64_t)m->nslices * FG_SLICE;
     std::vector<int> sl_len(m->nslices), sl_ptr(m->nslices + 1);
     int64_t acc = 0;
     for (int s = 0; s < m->nslices; ++s) {
-      int mx = 1;
+      int64_t mx = 1;
       for (int64_t r = (int64_t)s * FG_SLICE; r < std::min<int64_t>(n, (int64_t)(s + 1) * FG_SLICE); ++r)
         mx = std::max<int64_t>(mx, colptr[r + 1] - colptr[r]);
-      sl_len[s] = mx;
+      int groups = (int)((mx + FG_GROUP - 1) / FG_GROUP);
+      sl_len[s] = groups;
       sl_ptr[s] = (int)acc;
-      acc += (int64_t)mx * FG_SLICE;
+      acc += (int64_t)groups * FG_GROUP * FG_SLICE;
       FG_REQUIRE(acc < ((int64_t)1 << 31), FG_BAD_ARG, "padded matrix too large");
     }
     sl_ptr[m->nslices] = (int)acc;
     m->nsell = acc;
     std::vector<int> col(acc);
+    std::vector<int16_t> dcol(acc, 0);
     std::vector<double> val(acc, 0.0);
-    std::vector<double> dinv(n, 0.0);
+    std::vector<double> dinv(m->nvp, 0.0);
+    bool wide = false;
     for (int64_t r = 0; r < n; ++r) {
       int s = (int)(r / FG_SLICE), lane = (int)(r % FG_SLICE);
       int64_t b = colptr[r] - base, e = colptr[r + 1] - base;
       int k = 0;
-      for (int64_t q = b; q < e; ++q, ++k) {
-        int64_t c = rowval[q] - base;
+      double diag = 0.0;
+      for (int64_t qq = b; qq < e; ++qq, ++k) {
+        int64_t c = rowval[qq] - base;
         FG_REQUIRE(c >= 0 && c < n, FG_BAD_ARG, "row index out of range");
-        col[sl_ptr[s] + lane + (int64_t)k * FG_SLICE] = (int)c;
-        val[sl_ptr[s] + lane + (int64_t)k * FG_SLICE] = nzval[q];
-        if (c == r) dinv[r] += nzval[q];
+        int64_t pos = sell_pos(sl_ptr[s], lane, k);
+        col[pos] = (int)c;
+        val[pos] = nzval[qq];
+        int64_t d = c - r;
+        if (d < -32768 || d > 32767) wide = true; else dcol[pos] = (int16_t)d;
+        if (c == r) diag += nzval[qq];
       }
-      for (; k < sl_len[s]; ++k) col[sl_ptr[s] + lane + (int64_t)k * FG_SLICE] = (int)r;
-      dinv[r] = dinv[r] != 0.0 ? 1.0 / dinv[r] : 0.0;
+      for (; k < FG_GROUP * sl_len[s]; ++k) col[sell_pos(sl_ptr[s], lane, k)] = (int)r;
+      dinv[r] = diag != 0.0 ? 1.0 / diag : 0.0;
     }
+    m->use_dcol = !wide;
     m->sl_ptr = dev_alloc<int>(m, (size_t)m->nslices + 1);
     m->sl_len = dev_alloc<int>(m, (size_t)m->nslices);
     m->sl_col = dev_alloc<int>(m, (size_t)acc);
+    m->sl_dcol = dev_alloc<int16_t>(m, (size_t)acc);
     m->val64 = dev_alloc<double>(m, (size_t)acc);
-    m->dinv64 = dev_alloc<double>(m, (size_t)n);
+    m->dinv64 = dev_alloc<double>(m, (size_t)m->nvp);
     FG_CUDA_TRY(cudaMemcpyAsync(m->sl_ptr, sl_ptr.data(), sizeof(int) * (m->nslices + 1), cudaMemcpyHostToDevice, m->stream));
     FG_CUDA_TRY(cudaMemcpyAsync(m->sl_len, sl_len.data(), sizeof(int) * m->nslices, cudaMemcpyHostToDevice, m->stream));
     FG_CUDA_TRY(cudaMemcpyAsync(m->sl_col, col.data(), sizeof(int) * acc, cudaMemcpyHostToDevice, m->stream));
+    FG_CUDA_TRY(cudaMemcpyAsync(m->sl_dcol, dcol.data(), sizeof(int16_t) * acc, cudaMemcpyHostToDevice, m->stream));
     FG_CUDA_TRY(cudaMemcpyAsync(m->val64, val.data(), sizeof(double) * acc, cudaMemcpyHostToDevice, m->stream));
-    FG_CUDA_TRY(cudaMemcpyAsync(m->dinv64, dinv.data(), sizeof(double) * n, cudaMemcpyHostToDevice, m->stream));
+    FG_CUDA_TRY(cudaMemcpyAsync(m->dinv64, dinv.data(), sizeof(double) * m->nvp, cudaMemcpyHostToDevice, m->stream));
     if (want32) {
       std::vector<float> v32(val.begin(), val.end()), d32(dinv.begin(), dinv.end());
       m->val32 = dev_alloc<float>(m, (size_t)acc);
-      m->dinv32 = dev_alloc<float>(m, (size_t)n);
+      m->dinv32 = dev_alloc<float>(m, (size_t)m->nvp);
       FG_CUDA_TRY(cudaMemcpyAsync(m->val32, v32.data(), sizeof(float) * acc, cudaMemcpyHostToDevice, m->stream));
-      FG_CUDA_TRY(cudaMemcpyAsync(m->dinv32, d32.data(), sizeof(float) * n, cudaMemcpyHostToDevice, m->stream));
+      FG_CUDA_TRY(cudaMemcpyAsync(m->dinv32, d32.data(), sizeof(float) * m->nvp, cudaMemcpyHostToDevice, m->stream));
     }
     m->red.partials = dev_alloc<double>(m, ((size_t)grid_for(n, 256) + FG_RED_BLOCKS) * 4);
     m->red.counter = dev_alloc<unsigned int>(m, 16);
@@ -630,55 +843,68 @@ extern "C" fg_status fg_spmv_csc(int64_t n, const int64_t *colptr, const int64_t
   return st;
 }
 
-__global__ void k_fill64(int64_t n, double v, double *__restrict__ x) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    x[i] = v;
-}
-
-// Average duration of one CG kernel launch on the handle's current operator
-// (events on the handle's stream).  Leaves the CG vectors in an unspecified state.
+// Average duration of one CG kernel launch on the handle's current operator (events
+// on the handle's stream): which = 0 the SpMV, 1 the vector update.  Leaves the CG
+// vectors in an unspecified state.
 fg_status fg_bench_cg_kernel(fg_mesh *m, int which, int precision, int reps, double *ms_per_launch) {
   const bool mixed = precision == FG_MIXED;
   FG_REQUIRE(mixed ? m->val32 != nullptr : m->val64 != nullptr, FG_BAD_ARG, "operator not assembled");
-  unsigned g = cg_grid(m);
-  if (!m->v64[6]) m->v64[6] = dev_alloc<double>(m, (size_t)m->nv);
-  k_fill64<<<g, 256, 0, m->stream>>>(m->nv, 1.0, m->v64[6]);
+  if (!m->v64[6]) m->v64[6] = dev_alloc<double>(m, (size_t)m->nvp);
+  k_fill64<<<red_grid(m->nv), 256, 0, m->stream>>>(m->nv, 1.0, m->v64[6]);
+  // a CG state that never reports "done": r = 1, tolerance 0, huge iteration cap
+  if (mixed) {
+    ensure_cg32(m);
+    k_cg32_init<<<red_grid(m->nvp), 256, 0, m->stream>>>(m->nv, m->nvp, m->v64[6], 1.0, m->v32[0], m->v32[1],
+                                                         reinterpret_cast<float2 *>(m->v32[3]), m->dinv32, 0.0,
+                                                         1 << 30, m->scal, m->ictl, m->red.partials, m->red.counter);
+  } else {
+    ensure_cg64(m);
+    k_cg64_init<<<red_grid(m->nvp), 256, 0, m->stream>>>(m->nv, m->nvp, m->v64[6], 1.0, m->v64[0], m->v64[1],
+                                                         m->v64[2], m->v64[3], m->dinv64, 0.0, 1 << 30, m->scal,
+                                                         m->ictl, m->red.partials, m->red.counter);
+  }
+  FG_LAUNCHED(2);
   auto body = [&](int n) {
     for (int r = 0; r < n; ++r) {
       if (mixed) {
-        float **v = cg_vectors<float>(m);
-        if (which == 0)
-          k_cg_spmv<float, float><<<g, 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val32, v[2],
-                                                            v[3], v[4], v[5], m->scal, m->ictl, m->red.partials,
-                                                            m->red.counter);
-        else
-          k_cg_update<float><<<g, 256, 0, m->stream>>>(m->nv, v[0], v[1], v[2], v[4], v[5], m->dinv32, m->scal,
-                                                       m->ictl, m->red.partials, m->red.counter);
+        float2 *pz0 = reinterpret_cast<float2 *>(m->v32[3]), *pz1 = reinterpret_cast<float2 *>(m->v32[4]);
+        if (which == 0) {
+          if (m->use_dcol)
+            k_cg32_spmv<ColRel><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, m->val32,
+                                                                    pz0, pz1, m->v32[2], m->scal, m->ictl,
+                                                                    m->red.partials, m->red.counter);
+          else
+            k_cg32_spmv<ColAbs><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val32,
+                                                                    pz0, pz1, m->v32[2], m->scal, m->ictl,
+                                                                    m->red.partials, m->red.counter);
+        } else {
+          k_cg32_update<<<quad_grid(m), 256, 0, m->stream>>>(
+              m->nvp / 4, reinterpret_cast<float4 *>(m->v32[0]), reinterpret_cast<float4 *>(m->v32[1]),
+              reinterpret_cast<const float4 *>(m->v32[2]), reinterpret_cast<const float4 *>(m->dinv32),
+              reinterpret_cast<float4 *>(pz1), m->scal, m->ictl, m->red.partials, m->red.counter);
+        }
       } else {
-        double **v = cg_vectors<double>(m);
-        if (which == 0)
-          k_cg_spmv<double, double><<<g, 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val64,
-                                                              v[2], v[3], v[4], v[5], m->scal, m->ictl,
-                                                              m->red.partials, m->red.counter);
-        else
-          k_cg_update<double><<<g, 256, 0, m->stream>>>(m->nv, v[0], v[1], v[2], v[4], v[5], m->dinv64, m->scal,
-                                                        m->ictl, m->red.partials, m->red.counter);
+        if (which == 0) {
+          if (m->use_dcol)
+            k_cg64_spmv<ColRel><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, m->val64,
+                                                                    m->v64[3], m->v64[4], m->scal, m->ictl,
+                                                                    m->red.partials, m->red.counter);
+          else
+            k_cg64_spmv<ColAbs><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val64,
+                                                                    m->v64[3], m->v64[4], m->scal, m->ictl,
+                                                                    m->red.partials, m->red.counter);
+        } else {
+          k_cg64_update<<<quad_grid(m), 256, 0, m->stream>>>(
+              m->nvp / 4, reinterpret_cast<double2 *>(m->v64[0]), reinterpret_cast<double2 *>(m->v64[1]),
+              reinterpret_cast<double2 *>(m->v64[2]), reinterpret_cast<const double2 *>(m->v64[3]),
+              reinterpret_cast<const double2 *>(m->v64[4]), reinterpret_cast<const double2 *>(m->dinv64), m->scal,
+              m->ictl, m->red.partials, m->red.counter);
+        }
       }
     }
     FG_LAUNCHED(n);
   };
-  // a CG state that never reports "done": zero vectors, huge iteration cap
-  if (mixed) {
-    float **v = cg_vectors<float>(m);
-    k_cg_init<float><<<g, 256, 0, m->stream>>>(m->nv, m->v64[6], 1.0, v[0], v[1], v[2], v[3], m->dinv32, 0.0,
-                                               1 << 30, m->scal, m->ictl, m->red.partials, m->red.counter);
-  } else {
-    double **v = cg_vectors<double>(m);
-    k_cg_init<double><<<g, 256, 0, m->stream>>>(m->nv, m->v64[6], 1.0, v[0], v[1], v[2], v[3], m->dinv64, 0.0,
-                                                1 << 30, m->scal, m->ictl, m->red.partials, m->red.counter);
-  }
   FG_CUDA_TRY(cudaMemsetAsync(m->ictl, 0, sizeof(int), m->stream));  // clear "done"
-  FG_LAUNCHED(1);
   body(3);
   FG_CUDA_TRY(cudaEventRecord(m->ev0, m->stream));
   body(reps);

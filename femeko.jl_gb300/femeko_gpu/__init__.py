@@ -162,7 +162,8 @@ def newton_opts(precision="mixed", tol_update=1e-8, maxit=100, inner_rtol=1e-4, 
     L.lib().fg_newton_opts_default(C.byref(o))
     o.precision = L.FG_MIXED if precision == "mixed" else L.FG_FP64
     o.tol_update, o.maxit, o.inner_rtol, o.cg_maxiter = tol_update, maxit, inner_rtol, cg_maxiter
-    o.line_search = {"none": L.FG_LS_NONE, "reference": L.FG_LS_REFERENCE, "residual": L.FG_LS_RESIDUAL}[line_search]
+    o.line_search = {"none": L.FG_LS_NONE, "reference": L.FG_LS_REFERENCE, "residual": L.FG_LS_RESIDUAL,
+                     "quadratic": L.FG_LS_QUADRATIC}[line_search]
     o.min_step, o.Ms, o.Hk, o.check_every, o.use_graph = min_step, Ms, Hk, check_every, int(use_graph)
     return o
 

@@ -16,7 +16,7 @@ FG_OK, FG_NOT_CONVERGED, FG_NAN, FG_BAD_ARG, FG_BAD_MESH, FG_CUDA, FG_NO_DEVICE,
 STATUS_NAMES = {0: "FG_OK", 1: "FG_NOT_CONVERGED", 2: "FG_NAN", 3: "FG_BAD_ARG", 4: "FG_BAD_MESH", 5: "FG_CUDA",
                 6: "FG_NO_DEVICE", 7: "FG_UNSUPPORTED"}
 FG_FP64, FG_MIXED = 0, 1
-FG_LS_NONE, FG_LS_REFERENCE, FG_LS_RESIDUAL = 0, 1, 2
+FG_LS_NONE, FG_LS_REFERENCE, FG_LS_RESIDUAL, FG_LS_QUADRATIC = 0, 1, 2, 3
 
 
 class FemekoGPUError(RuntimeError):

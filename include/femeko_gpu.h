@@ -47,7 +47,9 @@ enum { FG_FP64 = 0, FG_MIXED = 1 };
 enum {
   FG_LS_NONE = 0,      /* full step */
   FG_LS_REFERENCE = 1, /* src/FEM3D.jl:123-152: backtracking on ||RHS - A(u+a du)|| with the frozen secant A */
-  FG_LS_RESIDUAL = 2   /* same backtracking rule on the true nonlinear residual */
+  FG_LS_RESIDUAL = 2,  /* same backtracking rule on the true nonlinear residual */
+  FG_LS_QUADRATIC = 3  /* true residual, next step from the minimiser of a quadratic fit
+                          of |F(u + a du)|^2, kept in [0.1, 0.5] of the last step */
 };
 /* SpMV kernel selection */
 enum { FG_SPMV_AUTO = 0, FG_SPMV_SELL = 1, FG_SPMV_CSR_VECTOR = 2 };

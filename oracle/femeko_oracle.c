@@ -710,7 +710,8 @@ static void nr_state(const double *p, const int *t, int nv, long nt, const doubl
 /*   0: full step;                                                                   */
 /*   1: src/FEM3D.jl:123-152 lineSearch on the frozen secant A (reference behaviour); */
 /*   2: the same backtracking (alpha *= 0.9 while the residual grows, alpha >= 1e-4)  */
-/*      on the true nonlinear residual ||F(u + alpha du)||.                          */
+/*      on the true nonlinear residual ||F(u + alpha du)||;                          */
+/*   3: the true residual with quadratic-interpolation backtracking (same acceptance). */
 /* Per element: nl[k] != 0 -> Froehlich(Ms, Hk); else mu = mu_lin[k] (absolute).       */
 /* Stops when ||alpha du|| <= tol_update ||u|| (2-norms over all nodes).               */
 /* Outputs: u (in: initial guess incl. boundary values), H (3 x nt), mu (nt).          */
@@ -761,9 +762,20 @@ int or_newton(const double *p, const int *t, int nv, long nt, const double *VE, 
         nr_state(p, t, nv, nt, Ak, fixed, nl, mu_lin, Ms, Hk, ref_bug_hz, ut, Ht, mut, dmut, Acsc, cpn, rin, Avn, Ft);
         res = sqrt(dot_masked(nv, Ft, Ft, fixed));
         if (ls_mode == 0 || !(res > r0 && alf > 1e-4)) break;
-        alf *= 0.9;
+        if (ls_mode == 3) {
+          /* quadratic interpolation of f(a) = |F(u + a du)|^2 through f(0), f'(0) = -2 f(0)
+             and f(alf); next step kept in [0.1, 0.5] alf (Dennis & Schnabel) */
+          double f0 = r0 * r0;
+          double c = (res * res - f0 + 2.0 * f0 * alf) / (alf * alf);
+          double anew = (c > 0.0) ? f0 / c : 0.5 * alf;
+          if (anew < 0.1 * alf) anew = 0.1 * alf;
+          if (anew > 0.5 * alf) anew = 0.5 * alf;
+          alf = anew;
+        } else {
+          alf *= 0.9;
+        }
       }
-      if (ls_mode == 2 && alf < 1e-4) alf = 0.0;
+      if ((ls_mode == 2 || ls_mode == 3) && alf < 1e-4) alf = 0.0;
       if (alf > 0.0) {
         memcpy(u, ut, sizeof(double) * nv); memcpy(F, Ft, sizeof(double) * nv);
         memcpy(H, Ht, sizeof(double) * 3 * (size_t)nt); memcpy(mu, mut, sizeof(double) * nt);

@@ -274,7 +274,7 @@ def energy(mesh, H, nl, mu_lin, Ms=0.0, Hk=1.0):
                            _c(mu_lin, np.float64), Ms, Hk)
 
 
-LS_MODES = {"none": 0, "reference": 1, "residual": 2}
+LS_MODES = {"none": 0, "reference": 1, "residual": 2, "quadratic": 3}
 
 
 def newton(mesh, u0, nl, mu_lin, Ms, Hk, tol_update=1e-8, maxit=100, cg_tol=1e-12, cg_maxit=200000,

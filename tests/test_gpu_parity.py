@@ -157,6 +157,25 @@ def test_newton_reference_line_search_same_iterates():
     assert np.linalg.norm(Hg - Ho) / np.linalg.norm(Ho) < 1e-8
 
 
+def test_newton_quadratic_line_search_same_fixed_point():
+    m, nl, mu_lin, u0 = newton_case()
+    ug, Hg, mug, st = fg.newton_magnetostatics(m, nl, mu_lin, u0, precision="mixed", line_search="quadratic")
+    uo, Ho, muo, so = O.newton(m, u0, nl, mu_lin, 1.2e6, 500.0, cg_tol=1e-12, line_search="quadratic")
+    assert st["converged"] and so["converged"]
+    assert np.linalg.norm(Hg - Ho) / np.linalg.norm(Ho) < 1e-8
+
+
+def test_froehlich_permeability_matches_ieee_formula():
+    """mu returned by the Newton solve (FP64 reciprocal and reciprocal square root by
+    Newton-Raphson refinement) against the formula evaluated with IEEE division and
+    square root on the same field."""
+    m, nl, mu_lin, u0 = newton_case()
+    ug, Hg, mug, st = fg.newton_magnetostatics(m, nl, mu_lin, u0, precision="fp64")
+    h = np.sqrt((Hg * Hg).sum(axis=0))
+    mu_ref = np.where(nl == 1, fg.MU0 * (1.0 + 1.2e6 / (500.0 + h)), mu_lin)
+    assert np.abs(mug - mu_ref).max() / mu_ref.max() < 1e-13
+
+
 def test_newton_reference_line_search_mixed():
     m, nl, mu_lin, u0 = newton_case()
     ug, Hg, mug, st = fg.newton_magnetostatics(m, nl, mu_lin, u0, precision="mixed", line_search="reference")
