@@ -35,6 +35,10 @@ extern "C" void fg_newton_opts_default(fg_newton_opts *o) {
   o->Hk = 500.0;
   o->check_every = 32;
   o->use_graph = 1;
+  o->forcing = FG_FORCING_EW;
+  o->reserved_ = 0;
+  o->eta_min = 1e-6;
+  o->eta_max = 0.1;
 }
 
 static void upload(fg_mesh *m, void *dst, const void *src, size_t bytes) {
@@ -81,8 +85,20 @@ static int newton_dev(fg_mesh *m, double *d_u, const fg_newton_opts &o, fg_newto
   double rF = fg_norm2_dev(m, d_F, nv, true);
   int it = 0, cg_total = 0, trials = 0, converged = 0, status = 0;
   double ratio = 0.0, alpha = 0.0;
+  double eta = (o.forcing == FG_FORCING_EW) ? o.eta_max : o.inner_rtol, rF_prev = -1.0;
   for (it = 1; it <= o.maxit; ++it) {
     if (rF == 0.0) { converged = 1; ratio = 0.0; break; }
+    if (o.forcing == FG_FORCING_EW && rF_prev > 0.0) {
+      // Eisenstat & Walker (1996), choice 2 with gamma = 0.9, exponent 2 and their
+      // safeguard against a too-fast decrease of eta
+      const double gam = 0.9;
+      double e = gam * (rF / rF_prev) * (rF / rF_prev);
+      const double sg = gam * eta * eta;
+      if (sg > 0.1) e = std::max(e, sg);
+      eta = std::min(std::max(e, o.eta_min), o.eta_max);
+    }
+    so.inner_rtol = eta;
+    rF_prev = rF;
     FG_CUDA_TRY(cudaMemsetAsync(d_du, 0, sizeof(double) * (size_t)nv, m->stream));
     fg_solve_stats cst{};
     fg_pcg_solve(m, d_F, d_du, so, &cst, true);

@@ -190,18 +190,48 @@ __global__ void __launch_bounds__(256) k_cg32_spmv(int64_t n, const int *__restr
     const float4 *v4 = reinterpret_cast<const float4 *>(val + base);
     const typename CI::T4 *c4 = reinterpret_cast<const typename CI::T4 *>(col + base);
     float acc = 0.f;
+    if (G <= 4) {
+      // rows of up to 16 slots (tetrahedral meshes): issue every value/column load,
+      // then every gather, then the FMAs, so one row has all its loads in flight
+      float4 vv[4];
+      typename CI::T4 cc[4];
+#pragma unroll
+      for (int g = 0; g < 4; ++g)
+        if (g < G) {
+          vv[g] = __ldg(v4 + (int64_t)g * FG_SLICE);
+          cc[g] = ld_cols(c4 + (int64_t)g * FG_SLICE);
+        }
+      float2 pzg[4][4];
+#pragma unroll
+      for (int g = 0; g < 4; ++g)
+        if (g < G) {
+          pzg[g][0] = __ldg(pz_in + CI::col(cc[g].x, i));
+          pzg[g][1] = __ldg(pz_in + CI::col(cc[g].y, i));
+          pzg[g][2] = __ldg(pz_in + CI::col(cc[g].z, i));
+          pzg[g][3] = __ldg(pz_in + CI::col(cc[g].w, i));
+        }
+#pragma unroll
+      for (int g = 0; g < 4; ++g)
+        if (g < G) {
+          acc = fmaf(vv[g].x, fmaf(beta, pzg[g][0].x, pzg[g][0].y), acc);
+          acc = fmaf(vv[g].y, fmaf(beta, pzg[g][1].x, pzg[g][1].y), acc);
+          acc = fmaf(vv[g].z, fmaf(beta, pzg[g][2].x, pzg[g][2].y), acc);
+          acc = fmaf(vv[g].w, fmaf(beta, pzg[g][3].x, pzg[g][3].y), acc);
+        }
+    } else {
 #pragma unroll 4
-    for (int g = 0; g < G; ++g) {
-      const float4 vv = __ldg(v4 + (int64_t)g * FG_SLICE);
-      const typename CI::T4 cc = ld_cols(c4 + (int64_t)g * FG_SLICE);
-      const float2 a = __ldg(pz_in + CI::col(cc.x, i));
-      const float2 b = __ldg(pz_in + CI::col(cc.y, i));
-      const float2 c = __ldg(pz_in + CI::col(cc.z, i));
-      const float2 d = __ldg(pz_in + CI::col(cc.w, i));
-      acc = fmaf(vv.x, fmaf(beta, a.x, a.y), acc);
-      acc = fmaf(vv.y, fmaf(beta, b.x, b.y), acc);
-      acc = fmaf(vv.z, fmaf(beta, c.x, c.y), acc);
-      acc = fmaf(vv.w, fmaf(beta, d.x, d.y), acc);
+      for (int g = 0; g < G; ++g) {
+        const float4 vv = __ldg(v4 + (int64_t)g * FG_SLICE);
+        const typename CI::T4 cc = ld_cols(c4 + (int64_t)g * FG_SLICE);
+        const float2 a = __ldg(pz_in + CI::col(cc.x, i));
+        const float2 b = __ldg(pz_in + CI::col(cc.y, i));
+        const float2 c = __ldg(pz_in + CI::col(cc.z, i));
+        const float2 d = __ldg(pz_in + CI::col(cc.w, i));
+        acc = fmaf(vv.x, fmaf(beta, a.x, a.y), acc);
+        acc = fmaf(vv.y, fmaf(beta, b.x, b.y), acc);
+        acc = fmaf(vv.z, fmaf(beta, c.x, c.y), acc);
+        acc = fmaf(vv.w, fmaf(beta, d.x, d.y), acc);
+      }
     }
     const float2 own = __ldg(pz_in + i);
     const float pi = fmaf(beta, own.x, own.y);

@@ -157,9 +157,14 @@ def solve_opts(precision="fp64", rtol=1e-10, maxiter=1_000_000, inner_rtol=1e-5,
 
 
 def newton_opts(precision="mixed", tol_update=1e-8, maxit=100, inner_rtol=1e-4, cg_maxiter=200_000,
-                line_search="residual", min_step=1e-4, Ms=1.2e6, Hk=500.0, check_every=32, use_graph=True):
+                line_search="residual", min_step=1e-4, Ms=1.2e6, Hk=500.0, check_every=32, use_graph=True,
+                forcing="ew", eta_min=1e-6, eta_max=0.1):
+    """Newton options.  forcing="ew": Eisenstat-Walker inner tolerances in
+    [eta_min, eta_max]; forcing="fixed": every inner solve to inner_rtol."""
     o = L.NewtonOpts()
     L.lib().fg_newton_opts_default(C.byref(o))
+    o.forcing = {"fixed": 0, "ew": 1}[forcing]
+    o.eta_min, o.eta_max = eta_min, eta_max
     o.precision = L.FG_MIXED if precision == "mixed" else L.FG_FP64
     o.tol_update, o.maxit, o.inner_rtol, o.cg_maxiter = tol_update, maxit, inner_rtol, cg_maxiter
     o.line_search = {"none": L.FG_LS_NONE, "reference": L.FG_LS_REFERENCE, "residual": L.FG_LS_RESIDUAL,

@@ -40,7 +40,8 @@ class NewtonOpts(C.Structure):
     _fields_ = [("precision", C.c_int32), ("maxit", C.c_int32), ("tol_update", C.c_double),
                 ("inner_rtol", C.c_double), ("cg_maxiter", C.c_int32), ("line_search", C.c_int32),
                 ("min_step", C.c_double), ("Ms", C.c_double), ("Hk", C.c_double), ("check_every", C.c_int32),
-                ("use_graph", C.c_int32)]
+                ("use_graph", C.c_int32), ("forcing", C.c_int32), ("reserved_", C.c_int32), ("eta_min", C.c_double),
+                ("eta_max", C.c_double)]
 
 
 class NewtonStats(C.Structure):

@@ -62,6 +62,10 @@ struct NewtonOpts
     Hk::Float64
     check_every::Int32
     use_graph::Int32
+    forcing::Int32          # 0 fixed inner_rtol, 1 Eisenstat-Walker
+    reserved_::Int32
+    eta_min::Float64
+    eta_max::Float64
 end
 
 struct NewtonStats
@@ -100,9 +104,9 @@ function newton_opts(; precision::Symbol=:mixed, tol_update=1e-8, maxit=100, inn
     o = Ref{NewtonOpts}()
     ccall((:fg_newton_opts_default, libpath()), Cvoid, (Ref{NewtonOpts},), o)
     d = o[]
-    ls = line_search == :none ? 0 : line_search == :reference ? 1 : 2
+    ls = line_search == :none ? 0 : line_search == :reference ? 1 : line_search == :quadratic ? 3 : 2
     return NewtonOpts(precision == :mixed ? 1 : 0, maxit, tol_update, inner_rtol, d.cg_maxiter, ls,
-                      d.min_step, Ms, Hk, d.check_every, d.use_graph)
+                      d.min_step, Ms, Hk, d.check_every, d.use_graph, d.forcing, 0, d.eta_min, d.eta_max)
 end
 
 # ---------------------------------------------------------------- mesh handle

@@ -87,7 +87,14 @@ typedef struct fg_newton_opts {
   double Ms, Hk;       /* Froehlich law mu(H) = mu0 (1 + Ms/(Hk + |H|)) */
   int32_t check_every;
   int32_t use_graph;
+  int32_t forcing;     /* inner tolerance: FG_FORCING_FIXED (inner_rtol) or
+                          FG_FORCING_EW (Eisenstat-Walker, clamped to [eta_min, eta_max]) */
+  int32_t reserved_;
+  double eta_min, eta_max;
 } fg_newton_opts;
+
+/* inner-tolerance (forcing term) rules of the Newton solver */
+enum { FG_FORCING_FIXED = 0, FG_FORCING_EW = 1 };
 
 typedef struct fg_newton_stats {
   int32_t newton_iters;

@@ -719,8 +719,8 @@ static void nr_state(const double *p, const int *t, int nv, long nt, const doubl
 /* last residual norm, last alpha, converged flag.                                     */
 int or_newton(const double *p, const int *t, int nv, long nt, const double *VE, const unsigned char *fixed,
               const unsigned char *nl, const double *mu_lin, double Ms, double Hk, double tol_update, int maxit,
-              double cg_tol, int cg_maxit, int ref_bug_hz, int ls_mode, double *u, double *H, double *mu,
-              double *stats) {
+              double cg_tol, int cg_maxit, int ref_bug_hz, int ls_mode, int forcing, double eta_min,
+              double eta_max, double *u, double *H, double *mu, double *stats) {
   size_t m16 = 16 * (size_t)nt;
   double *Ak = (double *)malloc(sizeof(double) * m16);
   or_local_stiffness(p, t, nt, VE, NULL, Ak);                      /* NewtonRaphson.jl:112 */
@@ -742,15 +742,24 @@ int or_newton(const double *p, const int *t, int nv, long nt, const double *VE, 
   int total_cg = 0, it, converged = 0;
   double ratio = 0.0, res = 0.0, alf = 0.0;
   nr_state(p, t, nv, nt, Ak, fixed, nl, mu_lin, Ms, Hk, ref_bug_hz, u, H, mu, dmu, Acsc, cp, ri, Av, F);
+  double eta = forcing ? eta_max : cg_tol, r_prev = -1.0;
   for (it = 1; it <= maxit; ++it) {
+    double r0 = sqrt(dot_masked(nv, F, F, fixed));
+    if (forcing && r_prev > 0.0) {
+      /* Eisenstat & Walker (1996) choice 2: gamma (|F_k|/|F_k-1|)^2, gamma = 0.9,
+         safeguarded by gamma eta^2 when that exceeds 0.1, clamped to [eta_min, eta_max] */
+      double e = 0.9 * (r0 / r_prev) * (r0 / r_prev), sg = 0.9 * eta * eta;
+      if (sg > 0.1 && sg > e) e = sg;
+      eta = e < eta_min ? eta_min : (e > eta_max ? eta_max : e);
+    }
+    r_prev = r0;
     or_tangent(p, t, nv, nt, VE, H, dmu, 0, cpt, rit, Atv);         /* :165 */
     long nnz = cp[nv];
     for (long q = 0; q < nnz; ++q) Atv[q] += Av[q];                  /* A + At, same pattern */
     memset(du, 0, sizeof(double) * nv);
     double rr;
-    int its = or_pcg(nv, cp, ri, Atv, F, du, fixed, cg_tol, cg_maxit, &rr);  /* :171-172 */
+    int its = or_pcg(nv, cp, ri, Atv, F, du, fixed, eta, cg_maxit, &rr);  /* :171-172 */
     total_cg += (its < 0) ? cg_maxit : its;
-    double r0 = sqrt(dot_masked(nv, F, F, fixed));
     if (ls_mode == 1) {
       alf = line_search(nv, cp, ri, Av, F, du, fixed, 1e-4, &res);  /* :175 */
       for (int i = 0; i < nv; ++i) u[i] += alf * du[i];
