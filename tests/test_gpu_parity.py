@@ -150,7 +150,7 @@ def test_newton_reference_line_search_same_iterates():
     linearly; with tight inner solves the GPU follows the oracle's iterates."""
     m, nl, mu_lin, u0 = newton_case()
     ug, Hg, mug, st = fg.newton_magnetostatics(m, nl, mu_lin, u0, precision="fp64", line_search="reference",
-                                               inner_rtol=1e-12)
+                                               forcing="fixed", inner_rtol=1e-12)
     uo, Ho, muo, so = O.newton(m, u0, nl, mu_lin, 1.2e6, 500.0, cg_tol=1e-12, line_search="reference")
     assert st["converged"] and so["converged"]
     assert st["newton_iters"] == so["newton_iters"]
