@@ -241,6 +241,11 @@ def run_ours(args):
     nsell, ninc, nsl = C.c_int64(), C.c_int64(), C.c_int32()
     lib.fg_mesh_layout(g.h, C.byref(nsell), C.byref(ninc), C.byref(nsl))
     fg.newton_magnetostatics(mesh, nl, mu_lin, u0, precision="mixed")   # leaves J32 on the handle
+    chosen = C.c_int32()
+    variants_us = np.zeros(4)
+    L.check(lib.fg_autotune(g.h, L.FG_MIXED, C.byref(chosen), L.ptr(variants_us), 4))
+    autotune = {"spmv32_variants_us": [round(float(v), 2) for v in variants_us], "chosen": int(chosen.value),
+                "names": ["loop/256", "hoist/256", "loop/128", "loop/512"]}
     ms_spmv = C.c_double()
     L.check(lib.fg_bench_kernel(g.h, 0, L.FG_MIXED, 200, C.byref(ms_spmv)))
     kernels_us = {"cg32_spmv": ms_spmv.value * 1e3}
@@ -325,7 +330,7 @@ def run_ours(args):
             "mixed_over_fp64": value / fp64_value,
             "accuracy_vs_fp64_gpu": {"H_rel": herr, "u_rel": uerr, "energy_rel": werr},
             "newton_iters": sm["newton_iters"], "cg_iters": sm["cg_iters"], "trials": sm["trials"],
-            "roofline": roofline, "kernels_us": kernels_us, "cpu_baseline": cpu, "e2e": e2e,
+            "roofline": roofline, "kernels_us": kernels_us, "autotune": autotune, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(launches),
             "clocks": res["mixed"]["clocks"], "clocks_fp64": res["fp64"]["clocks"],
             "setup_s": {"mesh_generate": t_gen, "mesh_create_pattern": t_setup},

@@ -362,7 +362,7 @@ __global__ void __launch_bounds__(128) k_elem_newton(int64_t nt, const double *_
                                                      const double *__restrict__ mu_lin, double Ms, double Hk,
                                                      const int *__restrict__ recpos, R *__restrict__ rec,
                                                      double *__restrict__ rec_r, double *__restrict__ mu_out,
-                                                     double *__restrict__ dmu_out, int *flags) {
+                                                     double *__restrict__ dmu_out, int tangent, int *flags) {
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nt) return;
   double G[10];
@@ -379,11 +379,12 @@ __global__ void __launch_bounds__(128) k_elem_newton(int64_t nt, const double *_
   w[1] = G[4] * d1 + G[5] * d2 + G[6] * d3;
   w[2] = G[5] * d1 + G[7] * d2 + G[8] * d3;
   w[3] = G[6] * d1 + G[8] * d2 + G[9] * d3;
-  const double h2 = fmax(d1 * w[1] + d2 * w[2] + d3 * w[3], 0.0);
-  const double ih = rsqrt_nr(h2);  // 1/|H| (0 when H = 0)
-  const double h = h2 * ih;
-  double mu, dmu;
+  // |H| only matters where mu depends on it (linear elements skip it: dmu = 0)
+  double mu, dmu, ih = 0.0;
   if (nl[k]) {
+    const double h2 = fmax(d1 * w[1] + d2 * w[2] + d3 * w[3], 0.0);
+    ih = rsqrt_nr(h2);  // 1/|H| (0 when H = 0)
+    const double h = h2 * ih;
     const double inv = rcp_nr(Hk + h);
     mu = FG_MU0 * fma(Ms, inv, 1.0);
     dmu = -FG_MU0 * Ms * inv * inv;
@@ -402,7 +403,7 @@ __global__ void __launch_bounds__(128) k_elem_newton(int64_t nt, const double *_
     rec_r[pos[a]] = vm * w[a];
   }
   if (rec == nullptr) return;  // residual-only pass (line-search trial)
-  const double ct = VE * dmu * ih;
+  const double ct = tangent ? VE * dmu * ih : 0.0;  // 0: secant (Picard) Jacobian
   if (std::is_same<R, float>::value) {
     float Gf[10], wf[4];
 #pragma unroll
@@ -677,7 +678,8 @@ void fg_assemble_operator(fg_mesh *m, int kind, const double *d_f, const double 
 }
 
 void fg_newton_assemble(fg_mesh *m, const double *d_u, double Ms, double Hk, bool mixed, double *d_F,
-                        bool want_jacobian) {
+                        bool want_jacobian, bool tangent) {
+  const int tg = tangent ? 1 : 0;
   FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "Newton magnetostatics needs P1 tetrahedra");
   fg_ensure_records(m);
   ensure_operator(m, !mixed, mixed);
@@ -685,7 +687,7 @@ void fg_newton_assemble(fg_mesh *m, const double *d_u, double Ms, double Hk, boo
   if (!want_jacobian) {
     // element state + residual only: the row pass sums the vector records
     k_elem_newton<double><<<g, 128, 0, m->stream>>>(m->nt, m->geo, m->t, d_u, m->nl, m->mu_lin, Ms, Hk, m->recpos,
-                                                    nullptr, m->rec_r, m->mu, m->dmu, m->flags);
+                                                    nullptr, m->rec_r, m->mu, m->dmu, tg, m->flags);
     FG_CUDA_TRY(cudaGetLastError());
     FG_LAUNCHED(1);
     launch_row<4, double, double>(m, nullptr, m->rec_r, 0, nullptr, nullptr, nullptr, nullptr, nullptr, d_F, -1.0, 1);
@@ -694,14 +696,14 @@ void fg_newton_assemble(fg_mesh *m, const double *d_u, double Ms, double Hk, boo
   if (mixed) {
     float *rec = static_cast<float *>(m->rec);
     k_elem_newton<float><<<g, 128, 0, m->stream>>>(m->nt, m->geo, m->t, d_u, m->nl, m->mu_lin, Ms, Hk, m->recpos, rec,
-                                                   m->rec_r, m->mu, m->dmu, m->flags);
+                                                   m->rec_r, m->mu, m->dmu, tg, m->flags);
     FG_CUDA_TRY(cudaGetLastError());
     FG_LAUNCHED(1);
     launch_row<4, float, float>(m, rec, m->rec_r, 1, nullptr, m->val32, nullptr, nullptr, m->dinv32, d_F, -1.0, 1);
   } else {
     double *rec = static_cast<double *>(m->rec);
     k_elem_newton<double><<<g, 128, 0, m->stream>>>(m->nt, m->geo, m->t, d_u, m->nl, m->mu_lin, Ms, Hk, m->recpos,
-                                                    rec, m->rec_r, m->mu, m->dmu, m->flags);
+                                                    rec, m->rec_r, m->mu, m->dmu, tg, m->flags);
     FG_CUDA_TRY(cudaGetLastError());
     FG_LAUNCHED(1);
     launch_row<4, double, double>(m, rec, m->rec_r, 1, m->val64, nullptr, nullptr, m->dinv64, nullptr, d_F, -1.0, 1);

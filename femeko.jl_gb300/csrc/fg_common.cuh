@@ -175,6 +175,8 @@ struct fg_mesh {
   int *hint = nullptr;        // pinned host ints (16)
 
   GraphCache graph[4];
+  int spmv_variant32 = 0;     // FP32 CG SpMV variant chosen by the autotuner
+  bool tuned32 = false;
   std::vector<void *> extra;  // allocations released at destroy
 };
 
@@ -209,7 +211,7 @@ void fg_ensure_records(fg_mesh *m);
 // density), the residual F = -K(mu(u)) u (FP64) and, when want_jacobian, the
 // Jacobian K + At in the operator (FP32 when mixed) with its Jacobi diagonal.
 void fg_newton_assemble(fg_mesh *m, const double *d_u, double Ms, double Hk, bool mixed, double *d_F,
-                        bool want_jacobian = true);
+                        bool want_jacobian = true, bool tangent = true);
 void fg_apply_operator_vec(fg_mesh *m, int kind, const double *d_coef, double c_mass, double c_stiff,
                            const double *d_x, double *d_y, bool zero_fixed);
 void fg_hfield_dev(fg_mesh *m, const double *d_u, double *d_H);

@@ -36,7 +36,7 @@ extern "C" void fg_newton_opts_default(fg_newton_opts *o) {
   o->check_every = 32;
   o->use_graph = 1;
   o->forcing = FG_FORCING_EW;
-  o->reserved_ = 0;
+  o->picard_steps = 2;
   o->eta_min = 1e-6;
   o->eta_max = 0.1;
 }
@@ -80,7 +80,7 @@ static int newton_dev(fg_mesh *m, double *d_u, const fg_newton_opts &o, fg_newto
   FG_CUDA_TRY(cudaEventCreate(&e1));
   FG_CUDA_TRY(cudaEventRecord(e0, m->stream));
 
-  fg_newton_assemble(m, d_u, o.Ms, o.Hk, mixed, d_F);
+  fg_newton_assemble(m, d_u, o.Ms, o.Hk, mixed, d_F, true, o.picard_steps <= 0);
   fg_check_flags(m, "fg_newton_magnetostatics");
   double rF = fg_norm2_dev(m, d_F, nv, true);
   int it = 0, cg_total = 0, trials = 0, converged = 0, status = 0;
@@ -99,6 +99,9 @@ static int newton_dev(fg_mesh *m, double *d_u, const fg_newton_opts &o, fg_newto
     }
     so.inner_rtol = eta;
     rF_prev = rF;
+    // the Jacobian assembled for the next iteration carries the tangent term once the
+    // Picard steps are done
+    const bool next_tangent = (it >= o.picard_steps);
     FG_CUDA_TRY(cudaMemsetAsync(d_du, 0, sizeof(double) * (size_t)nv, m->stream));
     fg_solve_stats cst{};
     fg_pcg_solve(m, d_F, d_du, so, &cst, true);
@@ -115,7 +118,7 @@ static int newton_dev(fg_mesh *m, double *d_u, const fg_newton_opts &o, fg_newto
       for (;;) {
         k_axpby64<<<g, 256, 0, m->stream>>>(nv, 1.0, d_u, alpha, d_du, d_ut);
         FG_LAUNCHED(1);
-        fg_newton_assemble(m, d_ut, o.Ms, o.Hk, mixed, d_Ft, trial_jacobian);
+        fg_newton_assemble(m, d_ut, o.Ms, o.Hk, mixed, d_Ft, trial_jacobian, next_tangent);
         rt = fg_norm2_dev(m, d_Ft, nv, true);
         ++trials;
         if (o.line_search == FG_LS_NONE || !(rt > rF && alpha > o.min_step)) break;
@@ -132,7 +135,7 @@ static int newton_dev(fg_mesh *m, double *d_u, const fg_newton_opts &o, fg_newto
       }
       if (alpha < o.min_step) {
         // no decrease: keep u (src/FEM3D.jl:144-147) and restore the state at u
-        fg_newton_assemble(m, d_u, o.Ms, o.Hk, mixed, d_F);
+        fg_newton_assemble(m, d_u, o.Ms, o.Hk, mixed, d_F, true, it > o.picard_steps);
         status = 1;
         alpha = 0.0;
         break;
@@ -159,7 +162,7 @@ static int newton_dev(fg_mesh *m, double *d_u, const fg_newton_opts &o, fg_newto
       if (alpha < o.min_step) { status = 1; alpha = 0.0; break; }
       k_axpby64<<<g, 256, 0, m->stream>>>(nv, 1.0, d_u, alpha, d_du, d_u);
       FG_LAUNCHED(1);
-      fg_newton_assemble(m, d_u, o.Ms, o.Hk, mixed, d_F);
+      fg_newton_assemble(m, d_u, o.Ms, o.Hk, mixed, d_F, true, next_tangent);
       rF = fg_norm2_dev(m, d_F, nv, true);
     }
     fg_check_flags(m, "fg_newton_magnetostatics");
@@ -168,7 +171,7 @@ static int newton_dev(fg_mesh *m, double *d_u, const fg_newton_opts &o, fg_newto
     ratio = (un > 0.0) ? dn / un : dn;
     if (!std::isfinite(ratio)) throw FgError{FG_NAN, "Newton update is not finite"};
     if (ratio <= o.tol_update) { converged = 1; break; }
-    if (need_jacobian) fg_newton_assemble(m, d_u, o.Ms, o.Hk, mixed, d_F, true);
+    if (need_jacobian) fg_newton_assemble(m, d_u, o.Ms, o.Hk, mixed, d_F, true, next_tangent);
   }
   fg_energy_dev(m, d_u, o.Ms, o.Hk);
   double energy = fg_dot_dev(m, m->wdens, nullptr, m->nt, false);

@@ -456,7 +456,7 @@ extern "C" fg_status fg_mesh_create(const double *p, int64_t nv, const int32_t *
     cudaFree(inc);
 
     // control and reduction workspace
-    m->red.partials = dev_alloc<double>(m, ((size_t)grid_for(nv, 256) + FG_RED_BLOCKS) * 4);
+    m->red.partials = dev_alloc<double>(m, ((size_t)grid_for(nv, 64) + FG_RED_BLOCKS) * 4);
     m->red.counter = dev_alloc<unsigned int>(m, 16);
     FG_CUDA_TRY(cudaMemsetAsync(m->red.counter, 0, 16 * sizeof(unsigned int), s));
     m->scal = dev_alloc<double>(m, S_NSCAL);

@@ -172,8 +172,11 @@ __device__ __forceinline__ int4 ld_cols(const int4 *p) { return __ldg(p); }
 __device__ __forceinline__ short4 ld_cols(const short4 *p) { return __ldg(p); }
 
 // ------------------------------------------------------------------ FP32 CG kernels
-template <class CI>
-__global__ void __launch_bounds__(256) k_cg32_spmv(int64_t n, const int *__restrict__ sl_ptr,
+// HOIST: issue all value/column loads of a row, then all gathers (rows of up to 16
+// slots); otherwise a 4x-unrolled loop.  BS: threads per block.  The autotuner picks
+// the variant per operator.
+template <class CI, bool HOIST, int BS>
+__global__ void __launch_bounds__(BS) k_cg32_spmv(int64_t n, const int *__restrict__ sl_ptr,
                                                    const int *__restrict__ sl_len,
                                                    const typename CI::T *__restrict__ col,
                                                    const float *__restrict__ val, const float2 *__restrict__ pz_in,
@@ -190,7 +193,7 @@ __global__ void __launch_bounds__(256) k_cg32_spmv(int64_t n, const int *__restr
     const float4 *v4 = reinterpret_cast<const float4 *>(val + base);
     const typename CI::T4 *c4 = reinterpret_cast<const typename CI::T4 *>(col + base);
     float acc = 0.f;
-    if (G <= 4) {
+    if (HOIST && G <= 4) {
       // rows of up to 16 slots (tetrahedral meshes): issue every value/column load,
       // then every gather, then the FMAs, so one row has all its loads in flight
       float4 vv[4];
@@ -565,17 +568,33 @@ static void ensure_cg64(fg_mesh *m) {
     }
 }
 
+// FP32 SpMV variants (block size x load scheduling) for the autotuner.
+constexpr int FG_N_SPMV32 = 4;
+static const char *spmv32_names[FG_N_SPMV32] = {"loop/256", "hoist/256", "loop/128", "loop/512"};
+
+template <class CI>
+static void spmv32_variant(fg_mesh *m, int v, const typename CI::T *col, const float2 *pz_in, float2 *pz_out) {
+  auto args = [&](auto kern, int bs) {
+    kern<<<grid_for(m->nv, bs), bs, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, col, m->val32, pz_in, pz_out,
+                                                     m->v32[2], m->scal, m->ictl, m->red.partials, m->red.counter);
+  };
+  switch (v) {
+    case 1: args(k_cg32_spmv<CI, true, 256>, 256); break;
+    case 2: args(k_cg32_spmv<CI, false, 128>, 128); break;
+    case 3: args(k_cg32_spmv<CI, false, 512>, 512); break;
+    default: args(k_cg32_spmv<CI, false, 256>, 256); break;
+  }
+}
+
+static void launch_spmv32(fg_mesh *m, int v, const float2 *pz_in, float2 *pz_out) {
+  if (m->use_dcol) spmv32_variant<ColRel>(m, v, m->sl_dcol, pz_in, pz_out);
+  else spmv32_variant<ColAbs>(m, v, m->sl_col, pz_in, pz_out);
+}
+
 static void launch_iter32(fg_mesh *m, bool odd) {
   float2 *pz_in = reinterpret_cast<float2 *>(odd ? m->v32[4] : m->v32[3]);
   float2 *pz_out = reinterpret_cast<float2 *>(odd ? m->v32[3] : m->v32[4]);
-  if (m->use_dcol)
-    k_cg32_spmv<ColRel><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, m->val32, pz_in,
-                                                            pz_out, m->v32[2], m->scal, m->ictl, m->red.partials,
-                                                            m->red.counter);
-  else
-    k_cg32_spmv<ColAbs><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val32, pz_in,
-                                                            pz_out, m->v32[2], m->scal, m->ictl, m->red.partials,
-                                                            m->red.counter);
+  launch_spmv32(m, m->spmv_variant32, pz_in, pz_out);
   k_cg32_update<<<quad_grid(m), 256, 0, m->stream>>>(
       m->nvp / 4, reinterpret_cast<float4 *>(m->v32[0]), reinterpret_cast<float4 *>(m->v32[1]),
       reinterpret_cast<const float4 *>(m->v32[2]), reinterpret_cast<const float4 *>(m->dinv32),
@@ -648,6 +667,8 @@ static int run_cg(fg_mesh *m, bool mixed, const fg_solve_opts &o, int *status) {
   return m->hint[I_ITERS];
 }
 
+fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_variant);
+
 // Inner solve of A d = scale * r64 from d = 0 to relative residual `inner`, then
 // x += d / scale.  Returns iterations; *ist = 0 converged, 1 cap, 2 non-finite.
 static int inner_solve(fg_mesh *m, bool mixed, const double *r64, double rn, double inner, int maxit,
@@ -656,6 +677,15 @@ static int inner_solve(fg_mesh *m, bool mixed, const double *r64, double rn, dou
   int its;
   if (mixed) {
     ensure_cg32(m);
+    if (o.spmv > 0 && o.spmv <= FG_N_SPMV32) {
+      if (m->spmv_variant32 != o.spmv - 1 && m->graph[1].exec) {
+        cudaGraphExecDestroy(m->graph[1].exec);
+        m->graph[1].exec = nullptr;
+      }
+      m->spmv_variant32 = o.spmv - 1;
+    } else if (!m->tuned32) {
+      fg_autotune_spmv32(m, 20, nullptr, nullptr);
+    }
     k_cg32_init<<<g, 256, 0, m->stream>>>(m->nv, m->nvp, r64, 1.0 / rn, m->v32[0], m->v32[1],
                                           reinterpret_cast<float2 *>(m->v32[3]), m->dinv32, inner * inner, maxit,
                                           m->scal, m->ictl, m->red.partials, m->red.counter);
@@ -738,7 +768,7 @@ extern "C" void fg_solve_opts_default(fg_solve_opts *o) {
   o->check_every = 32;
   o->use_graph = 1;
   o->spmv = FG_SPMV_AUTO;
-  o->rows_per_warp = 4;
+  o->reserved_ = 0;
 }
 
 // A standalone operator from a symmetric CSC matrix: a handle with the pattern and
@@ -817,7 +847,7 @@ static fg_mesh *matrix_handle(int64_t n, const int64_t *colptr, const int64_t *r
       FG_CUDA_TRY(cudaMemcpyAsync(m->val32, v32.data(), sizeof(float) * acc, cudaMemcpyHostToDevice, m->stream));
       FG_CUDA_TRY(cudaMemcpyAsync(m->dinv32, d32.data(), sizeof(float) * m->nvp, cudaMemcpyHostToDevice, m->stream));
     }
-    m->red.partials = dev_alloc<double>(m, ((size_t)grid_for(n, 256) + FG_RED_BLOCKS) * 4);
+    m->red.partials = dev_alloc<double>(m, ((size_t)grid_for(n, 64) + FG_RED_BLOCKS) * 4);
     m->red.counter = dev_alloc<unsigned int>(m, 16);
     FG_CUDA_TRY(cudaMemsetAsync(m->red.counter, 0, 16 * sizeof(unsigned int), m->stream));
     m->scal = dev_alloc<double>(m, S_NSCAL);
@@ -899,14 +929,7 @@ fg_status fg_bench_cg_kernel(fg_mesh *m, int which, int precision, int reps, dou
       if (mixed) {
         float2 *pz0 = reinterpret_cast<float2 *>(m->v32[3]), *pz1 = reinterpret_cast<float2 *>(m->v32[4]);
         if (which == 0) {
-          if (m->use_dcol)
-            k_cg32_spmv<ColRel><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, m->val32,
-                                                                    pz0, pz1, m->v32[2], m->scal, m->ictl,
-                                                                    m->red.partials, m->red.counter);
-          else
-            k_cg32_spmv<ColAbs><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val32,
-                                                                    pz0, pz1, m->v32[2], m->scal, m->ictl,
-                                                                    m->red.partials, m->red.counter);
+          launch_spmv32(m, m->spmv_variant32, pz0, pz1);
         } else {
           k_cg32_update<<<quad_grid(m), 256, 0, m->stream>>>(
               m->nvp / 4, reinterpret_cast<float4 *>(m->v32[0]), reinterpret_cast<float4 *>(m->v32[1]),
@@ -945,4 +968,56 @@ fg_status fg_bench_cg_kernel(fg_mesh *m, int which, int precision, int reps, dou
   FG_CUDA_TRY(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
   *ms_per_launch = ms / reps;
   return FG_OK;
+}
+
+// Autotuner: times every FP32 CG SpMV variant (block size x load scheduling) on the
+// handle's current operator with CUDA events and keeps the fastest for the handle.
+// Runs once per handle at its first mixed-precision solve (or on request).
+fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_variant) {
+  FG_REQUIRE(m->val32 != nullptr, FG_BAD_ARG, "autotune: no FP32 operator assembled");
+  ensure_cg32(m);
+  if (!m->v64[6]) m->v64[6] = dev_alloc<double>(m, (size_t)m->nvp);
+  k_fill64<<<red_grid(m->nv), 256, 0, m->stream>>>(m->nv, 1.0, m->v64[6]);
+  k_cg32_init<<<red_grid(m->nvp), 256, 0, m->stream>>>(m->nv, m->nvp, m->v64[6], 1.0, m->v32[0], m->v32[1],
+                                                       reinterpret_cast<float2 *>(m->v32[3]), m->dinv32, 0.0, 1 << 30,
+                                                       m->scal, m->ictl, m->red.partials, m->red.counter);
+  FG_LAUNCHED(2);
+  FG_CUDA_TRY(cudaMemsetAsync(m->ictl, 0, sizeof(int), m->stream));
+  float2 *pz0 = reinterpret_cast<float2 *>(m->v32[3]), *pz1 = reinterpret_cast<float2 *>(m->v32[4]);
+  int best = 0;
+  double best_us = 1e30;
+  for (int v = 0; v < FG_N_SPMV32; ++v) {
+    for (int r = 0; r < 3; ++r) launch_spmv32(m, v, pz0, pz1);
+    FG_CUDA_TRY(cudaEventRecord(m->ev0, m->stream));
+    for (int r = 0; r < reps; ++r) launch_spmv32(m, v, pz0, pz1);
+    FG_CUDA_TRY(cudaEventRecord(m->ev1, m->stream));
+    FG_CUDA_TRY(cudaGetLastError());
+    FG_LAUNCHED(reps + 3);
+    fg_sync(m);
+    float ms = 0.f;
+    FG_CUDA_TRY(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
+    double us = 1e3 * ms / reps;
+    if (us_per_variant) us_per_variant[v] = us;
+    if (us < best_us) { best_us = us; best = v; }
+  }
+  m->spmv_variant32 = best;
+  m->tuned32 = true;
+  if (m->graph[1].exec) { cudaGraphExecDestroy(m->graph[1].exec); m->graph[1].exec = nullptr; }
+  if (chosen) *chosen = best;
+  return FG_OK;
+}
+
+extern "C" fg_status fg_autotune(fg_mesh *m, int32_t precision, int32_t *variant, double *us_per_variant,
+                                 int32_t n_slots) {
+  return fg_guard([&]() -> fg_status {
+    FG_REQUIRE(m != nullptr, FG_BAD_ARG, "fg_autotune: null handle");
+    FG_REQUIRE(precision == FG_MIXED, FG_UNSUPPORTED, "fg_autotune: FP32 operator variants only");
+    double us[FG_N_SPMV32];
+    int chosen = 0;
+    fg_status st = fg_autotune_spmv32(m, 50, &chosen, us);
+    if (variant) *variant = chosen;
+    if (us_per_variant)
+      for (int v = 0; v < FG_N_SPMV32 && v < n_slots; ++v) us_per_variant[v] = us[v];
+    return st;
+  });
 }

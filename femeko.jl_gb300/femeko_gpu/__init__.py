@@ -147,23 +147,27 @@ def localStiffnessMatrix(mesh: MESH, f=None):
     return Ak.reshape(mesh.nt, 16).T
 
 
-def solve_opts(precision="fp64", rtol=1e-10, maxiter=1_000_000, inner_rtol=1e-5, check_every=32, use_graph=True):
+def solve_opts(precision="fp64", rtol=1e-10, maxiter=1_000_000, inner_rtol=1e-5, check_every=32, use_graph=True,
+               spmv=0):
+    """Linear-solve options; spmv = 0 autotunes the FP32 SpMV, 1..4 forces a variant."""
     o = L.SolveOpts()
     L.lib().fg_solve_opts_default(C.byref(o))
     o.precision = L.FG_MIXED if precision == "mixed" else L.FG_FP64
     o.rtol, o.maxiter, o.inner_rtol = rtol, maxiter, inner_rtol
-    o.check_every, o.use_graph = check_every, int(use_graph)
+    o.check_every, o.use_graph, o.spmv = check_every, int(use_graph), int(spmv)
     return o
 
 
 def newton_opts(precision="mixed", tol_update=1e-8, maxit=100, inner_rtol=1e-4, cg_maxiter=200_000,
                 line_search="residual", min_step=1e-4, Ms=1.2e6, Hk=500.0, check_every=32, use_graph=True,
-                forcing="ew", eta_min=1e-6, eta_max=0.1):
+                forcing="ew", eta_min=1e-6, eta_max=0.1, picard_steps=2):
     """Newton options.  forcing="ew": Eisenstat-Walker inner tolerances in
-    [eta_min, eta_max]; forcing="fixed": every inner solve to inner_rtol."""
+    [eta_min, eta_max]; forcing="fixed": every inner solve to inner_rtol.
+    picard_steps: first iterations without the tangent term."""
     o = L.NewtonOpts()
     L.lib().fg_newton_opts_default(C.byref(o))
     o.forcing = {"fixed": 0, "ew": 1}[forcing]
+    o.picard_steps = int(picard_steps)
     o.eta_min, o.eta_max = eta_min, eta_max
     o.precision = L.FG_MIXED if precision == "mixed" else L.FG_FP64
     o.tol_update, o.maxit, o.inner_rtol, o.cg_maxiter = tol_update, maxit, inner_rtol, cg_maxiter

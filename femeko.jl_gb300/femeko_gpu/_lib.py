@@ -28,7 +28,7 @@ class FemekoGPUError(RuntimeError):
 class SolveOpts(C.Structure):
     _fields_ = [("precision", C.c_int32), ("rtol", C.c_double), ("maxiter", C.c_int32), ("inner_rtol", C.c_double),
                 ("check_every", C.c_int32), ("use_graph", C.c_int32), ("spmv", C.c_int32),
-                ("rows_per_warp", C.c_int32)]
+                ("reserved_", C.c_int32)]
 
 
 class SolveStats(C.Structure):
@@ -40,7 +40,7 @@ class NewtonOpts(C.Structure):
     _fields_ = [("precision", C.c_int32), ("maxit", C.c_int32), ("tol_update", C.c_double),
                 ("inner_rtol", C.c_double), ("cg_maxiter", C.c_int32), ("line_search", C.c_int32),
                 ("min_step", C.c_double), ("Ms", C.c_double), ("Hk", C.c_double), ("check_every", C.c_int32),
-                ("use_graph", C.c_int32), ("forcing", C.c_int32), ("reserved_", C.c_int32), ("eta_min", C.c_double),
+                ("use_graph", C.c_int32), ("forcing", C.c_int32), ("picard_steps", C.c_int32), ("eta_min", C.c_double),
                 ("eta_max", C.c_double)]
 
 
@@ -81,6 +81,7 @@ SIGNATURES = {
                                    _vp, C.POINTER(NewtonStats)],
     "fg_bench_kernel": [_vp, _i32, _i32, _i32, C.POINTER(_d)],
     "fg_mesh_layout": [_vp, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i32)],
+    "fg_autotune": [_vp, _i32, C.POINTER(_i32), _vp, _i32],
 }
 VOID_FUNCS = {"fg_solve_opts_default": [C.POINTER(SolveOpts)], "fg_newton_opts_default": [C.POINTER(NewtonOpts)]}
 

@@ -38,7 +38,7 @@ struct SolveOpts
     check_every::Int32
     use_graph::Int32
     spmv::Int32
-    rows_per_warp::Int32
+    reserved_::Int32
 end
 
 struct SolveStats
@@ -63,7 +63,7 @@ struct NewtonOpts
     check_every::Int32
     use_graph::Int32
     forcing::Int32          # 0 fixed inner_rtol, 1 Eisenstat-Walker
-    reserved_::Int32
+    picard_steps::Int32     # first iterations without the tangent term
     eta_min::Float64
     eta_max::Float64
 end
@@ -96,7 +96,7 @@ function solve_opts(; precision::Symbol=:fp64, rtol=1e-10, maxiter=1_000_000, in
     ccall((:fg_solve_opts_default, libpath()), Cvoid, (Ref{SolveOpts},), o)
     d = o[]
     return SolveOpts(precision == :mixed ? 1 : 0, rtol, maxiter, inner_rtol, d.check_every, d.use_graph,
-                     d.spmv, d.rows_per_warp)
+                     d.spmv, 0)
 end
 
 function newton_opts(; precision::Symbol=:mixed, tol_update=1e-8, maxit=100, inner_rtol=1e-4,
@@ -106,7 +106,8 @@ function newton_opts(; precision::Symbol=:mixed, tol_update=1e-8, maxit=100, inn
     d = o[]
     ls = line_search == :none ? 0 : line_search == :reference ? 1 : line_search == :quadratic ? 3 : 2
     return NewtonOpts(precision == :mixed ? 1 : 0, maxit, tol_update, inner_rtol, d.cg_maxiter, ls,
-                      d.min_step, Ms, Hk, d.check_every, d.use_graph, d.forcing, 0, d.eta_min, d.eta_max)
+                      d.min_step, Ms, Hk, d.check_every, d.use_graph, d.forcing, d.picard_steps, d.eta_min,
+                      d.eta_max)
 end
 
 # ---------------------------------------------------------------- mesh handle

@@ -51,8 +51,11 @@ enum {
   FG_LS_QUADRATIC = 3  /* true residual, next step from the minimiser of a quadratic fit
                           of |F(u + a du)|^2, kept in [0.1, 0.5] of the last step */
 };
-/* SpMV kernel selection */
-enum { FG_SPMV_AUTO = 0, FG_SPMV_SELL = 1, FG_SPMV_CSR_VECTOR = 2 };
+/* FP32 CG SpMV kernel: FG_SPMV_AUTO lets the autotuner time the variants on the
+ * first mixed solve of a handle and keep the fastest; k = 1..4 forces variant k-1
+ * (1: 4x-unrolled loop, 256 threads; 2: all row loads issued first, 256 threads;
+ *  3: loop, 128 threads; 4: loop, 512 threads). */
+enum { FG_SPMV_AUTO = 0 };
 
 typedef struct fg_mesh fg_mesh;
 
@@ -63,8 +66,8 @@ typedef struct fg_solve_opts {
   double inner_rtol;   /* mixed: FP32 PCG target per refinement step */
   int32_t check_every; /* iterations per graph launch between convergence checks (even) */
   int32_t use_graph;   /* 1: replay each block of iterations as a CUDA graph */
-  int32_t spmv;        /* FG_SPMV_* */
-  int32_t rows_per_warp; /* CSR vector kernel: 1, 2, 4 or 8 rows per warp */
+  int32_t spmv;        /* FG_SPMV_AUTO or a forced variant 1..4 */
+  int32_t reserved_;
 } fg_solve_opts;
 
 typedef struct fg_solve_stats {
@@ -89,7 +92,9 @@ typedef struct fg_newton_opts {
   int32_t use_graph;
   int32_t forcing;     /* inner tolerance: FG_FORCING_FIXED (inner_rtol) or
                           FG_FORCING_EW (Eisenstat-Walker, clamped to [eta_min, eta_max]) */
-  int32_t reserved_;
+  int32_t picard_steps; /* first iterations without the tangent term (secant/Picard
+                           steps; the reference's first iteration is one,
+                           Magnetostatics/NewtonRaphson.jl:164-168) */
   double eta_min, eta_max;
 } fg_newton_opts;
 
@@ -199,6 +204,11 @@ int64_t fg_kernel_launches(void);
  * operator: which = 0 CG SpMV, 1 CG vector update, 2 Newton element pass + row
  * gather.  No reference counterpart (used for roofline reporting). */
 fg_status fg_bench_kernel(fg_mesh *m, int32_t which, int32_t precision, int32_t reps, double *ms_per_launch);
+/* Autotuner: times the FP32 CG SpMV variants on the handle's current FP32 operator
+ * (assemble one first, e.g. by a mixed solve) and keeps the fastest for the handle.
+ * variant receives the chosen index (0-based), us_per_variant (n_slots entries, may
+ * be NULL) the measured microseconds per launch.  No reference counterpart. */
+fg_status fg_autotune(fg_mesh *m, int32_t precision, int32_t *variant, double *us_per_variant, int32_t n_slots);
 /* Padded sizes of the device layouts: SELL-32 matrix entries, incidence records, slices. */
 fg_status fg_mesh_layout(const fg_mesh *m, int64_t *nsell, int64_t *ninc, int32_t *nslices);
 

@@ -720,7 +720,7 @@ static void nr_state(const double *p, const int *t, int nv, long nt, const doubl
 int or_newton(const double *p, const int *t, int nv, long nt, const double *VE, const unsigned char *fixed,
               const unsigned char *nl, const double *mu_lin, double Ms, double Hk, double tol_update, int maxit,
               double cg_tol, int cg_maxit, int ref_bug_hz, int ls_mode, int forcing, double eta_min,
-              double eta_max, double *u, double *H, double *mu, double *stats) {
+              double eta_max, int picard_steps, double *u, double *H, double *mu, double *stats) {
   size_t m16 = 16 * (size_t)nt;
   double *Ak = (double *)malloc(sizeof(double) * m16);
   or_local_stiffness(p, t, nt, VE, NULL, Ak);                      /* NewtonRaphson.jl:112 */
@@ -753,9 +753,13 @@ int or_newton(const double *p, const int *t, int nv, long nt, const double *VE, 
       eta = e < eta_min ? eta_min : (e > eta_max ? eta_max : e);
     }
     r_prev = r0;
-    or_tangent(p, t, nv, nt, VE, H, dmu, 0, cpt, rit, Atv);         /* :165 */
     long nnz = cp[nv];
-    for (long q = 0; q < nnz; ++q) Atv[q] += Av[q];                  /* A + At, same pattern */
+    if (it > picard_steps) {
+      or_tangent(p, t, nv, nt, VE, H, dmu, 0, cpt, rit, Atv);       /* :165 */
+      for (long q = 0; q < nnz; ++q) Atv[q] += Av[q];                /* A + At, same pattern */
+    } else {
+      memcpy(Atv, Av, sizeof(double) * (size_t)nnz);                 /* :167 At = 0 (Picard step) */
+    }
     memset(du, 0, sizeof(double) * nv);
     double rr;
     int its = or_pcg(nv, cp, ri, Atv, F, du, fixed, eta, cg_maxit, &rr);  /* :171-172 */

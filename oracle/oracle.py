@@ -85,7 +85,7 @@ def lib():
         L.or_newton.restype = C.c_int
         L.or_newton.argtypes = [_dp, _ip, C.c_int, C.c_long, _dp, _bp, _bp, _dp, C.c_double, C.c_double,
                                 C.c_double, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
-                                C.c_double, _dp, _dp, _dp, _dp]
+                                C.c_double, C.c_int, _dp, _dp, _dp, _dp]
         L.or_linear_magnetostatics.restype = C.c_int
         L.or_linear_magnetostatics.argtypes = [_dp, _ip, C.c_int, C.c_long, _dp, _bp, _dp, C.c_double, C.c_int,
                                                _dp, _vp, C.POINTER(C.c_int)]
@@ -279,9 +279,10 @@ LS_MODES = {"none": 0, "reference": 1, "residual": 2, "quadratic": 3}
 
 
 def newton(mesh, u0, nl, mu_lin, Ms, Hk, tol_update=1e-8, maxit=100, cg_tol=1e-12, cg_maxit=200000,
-           ref_bug_hz=False, line_search="residual", forcing="fixed", eta_min=1e-6, eta_max=0.1):
+           ref_bug_hz=False, line_search="residual", forcing="fixed", eta_min=1e-6, eta_max=0.1, picard_steps=0):
     """Dirichlet Newton-Raphson magnetostatics; returns (u, H 3 x nt, mu, stats dict).
-    forcing="fixed" solves every increment to cg_tol; "ew" uses Eisenstat-Walker tolerances."""
+    forcing="fixed" solves every increment to cg_tol; "ew" uses Eisenstat-Walker tolerances.
+    picard_steps: first iterations with the secant operator only (no tangent term)."""
     p, t = _pt(mesh)
     u = _c(u0, np.float64).copy()
     H = np.zeros(3 * mesh.nt)
@@ -289,7 +290,8 @@ def newton(mesh, u0, nl, mu_lin, Ms, Hk, tol_update=1e-8, maxit=100, cg_tol=1e-1
     st = np.zeros(6)
     lib().or_newton(p, t, mesh.nv, mesh.nt, _c(mesh.VE, np.float64), mesh.dirichlet_mask(), _c(nl, np.uint8),
                     _c(mu_lin, np.float64), Ms, Hk, tol_update, maxit, cg_tol, cg_maxit, int(ref_bug_hz),
-                    LS_MODES[line_search], {"fixed": 0, "ew": 1}[forcing], eta_min, eta_max, u, H, mu, st)
+                    LS_MODES[line_search], {"fixed": 0, "ew": 1}[forcing], eta_min, eta_max, int(picard_steps), u,
+                    H, mu, st)
     stats = dict(newton_iters=int(st[0]), cg_iters=int(st[1]), update_ratio=st[2], residual=st[3], alpha=st[4],
                  converged=bool(st[5]))
     return u, H.reshape(mesh.nt, 3).T, mu, stats

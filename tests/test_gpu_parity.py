@@ -150,10 +150,22 @@ def test_newton_reference_line_search_same_iterates():
     linearly; with tight inner solves the GPU follows the oracle's iterates."""
     m, nl, mu_lin, u0 = newton_case()
     ug, Hg, mug, st = fg.newton_magnetostatics(m, nl, mu_lin, u0, precision="fp64", line_search="reference",
-                                               forcing="fixed", inner_rtol=1e-12)
+                                               forcing="fixed", inner_rtol=1e-12, picard_steps=0)
     uo, Ho, muo, so = O.newton(m, u0, nl, mu_lin, 1.2e6, 500.0, cg_tol=1e-12, line_search="reference")
     assert st["converged"] and so["converged"]
     assert st["newton_iters"] == so["newton_iters"]
+    assert np.linalg.norm(Hg - Ho) / np.linalg.norm(Ho) < 1e-8
+
+
+def test_newton_same_iterates_as_oracle_with_picard_and_ew():
+    """The default algorithm (2 Picard steps, Eisenstat-Walker inner tolerances,
+    residual backtracking) in FP64 follows the oracle's Newton iterates."""
+    m, nl, mu_lin, u0 = newton_case()
+    ug, Hg, mug, st = fg.newton_magnetostatics(m, nl, mu_lin, u0, precision="fp64")
+    uo, Ho, muo, so = O.newton(m, u0, nl, mu_lin, 1.2e6, 500.0, forcing="ew", picard_steps=2)
+    assert st["converged"] and so["converged"]
+    assert st["newton_iters"] == so["newton_iters"]
+    assert abs(st["cg_iters"] - so["cg_iters"]) <= 0.05 * so["cg_iters"] + 5
     assert np.linalg.norm(Hg - Ho) / np.linalg.norm(Ho) < 1e-8
 
 
@@ -183,6 +195,25 @@ def test_newton_reference_line_search_mixed():
     assert st["converged"]
     # stopped by the update norm while converging linearly: within 1e-6 of the fixed point
     assert np.linalg.norm(Hg - Ho) / np.linalg.norm(Ho) < 1e-6
+
+
+def test_autotune_and_forced_variants_agree():
+    """Every FP32 SpMV variant gives the same Newton solution (same arithmetic per row)."""
+    import ctypes as C
+    import femeko_gpu._lib as L
+    m, nl, mu_lin, u0 = newton_case(10, 3)
+    K = O.stiffnessMatrix(m) + O.massMatrix(m)
+    b = np.random.default_rng(4).normal(size=m.nv)
+    xs = [fg.cg(K, b, reltol=1e-10, precision="mixed", spmv=v) for v in range(1, 5)]
+    for x in xs[1:]:
+        assert np.linalg.norm(x - xs[0]) / np.linalg.norm(xs[0]) < 1e-8
+    fg.newton_magnetostatics(m, nl, mu_lin, u0, precision="mixed")   # FP32 operator on the handle
+    g = fg.gpu_mesh(m)
+    chosen = C.c_int32(-1)
+    us = np.zeros(4)
+    L.check(L.lib().fg_autotune(g.h, L.FG_MIXED, C.byref(chosen), L.ptr(us), 4))
+    assert 0 <= chosen.value < 4 and (us > 0).all()
+    assert us[chosen.value] == us.min()
 
 
 def test_hfield(tet):
