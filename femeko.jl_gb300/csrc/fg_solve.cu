@@ -909,17 +909,17 @@ extern "C" fg_status fg_spmv_csc(int64_t n, const int64_t *colptr, const int64_t
 fg_status fg_bench_cg_kernel(fg_mesh *m, int which, int precision, int reps, double *ms_per_launch) {
   const bool mixed = precision == FG_MIXED;
   FG_REQUIRE(mixed ? m->val32 != nullptr : m->val64 != nullptr, FG_BAD_ARG, "operator not assembled");
-  if (!m->v64[6]) m->v64[6] = dev_alloc<double>(m, (size_t)m->nvp);
-  k_fill64<<<red_grid(m->nv), 256, 0, m->stream>>>(m->nv, 1.0, m->v64[6]);
+  if (!m->v64[5]) m->v64[5] = dev_alloc<double>(m, (size_t)m->nvp);
+  k_fill64<<<red_grid(m->nv), 256, 0, m->stream>>>(m->nv, 1.0, m->v64[5]);
   // a CG state that never reports "done": r = 1, tolerance 0, huge iteration cap
   if (mixed) {
     ensure_cg32(m);
-    k_cg32_init<<<red_grid(m->nvp), 256, 0, m->stream>>>(m->nv, m->nvp, m->v64[6], 1.0, m->v32[0], m->v32[1],
+    k_cg32_init<<<red_grid(m->nvp), 256, 0, m->stream>>>(m->nv, m->nvp, m->v64[5], 1.0, m->v32[0], m->v32[1],
                                                          reinterpret_cast<float2 *>(m->v32[3]), m->dinv32, 0.0,
                                                          1 << 30, m->scal, m->ictl, m->red.partials, m->red.counter);
   } else {
     ensure_cg64(m);
-    k_cg64_init<<<red_grid(m->nvp), 256, 0, m->stream>>>(m->nv, m->nvp, m->v64[6], 1.0, m->v64[0], m->v64[1],
+    k_cg64_init<<<red_grid(m->nvp), 256, 0, m->stream>>>(m->nv, m->nvp, m->v64[5], 1.0, m->v64[0], m->v64[1],
                                                          m->v64[2], m->v64[3], m->dinv64, 0.0, 1 << 30, m->scal,
                                                          m->ictl, m->red.partials, m->red.counter);
   }
@@ -976,9 +976,9 @@ fg_status fg_bench_cg_kernel(fg_mesh *m, int which, int precision, int reps, dou
 fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_variant) {
   FG_REQUIRE(m->val32 != nullptr, FG_BAD_ARG, "autotune: no FP32 operator assembled");
   ensure_cg32(m);
-  if (!m->v64[6]) m->v64[6] = dev_alloc<double>(m, (size_t)m->nvp);
-  k_fill64<<<red_grid(m->nv), 256, 0, m->stream>>>(m->nv, 1.0, m->v64[6]);
-  k_cg32_init<<<red_grid(m->nvp), 256, 0, m->stream>>>(m->nv, m->nvp, m->v64[6], 1.0, m->v32[0], m->v32[1],
+  if (!m->v64[5]) m->v64[5] = dev_alloc<double>(m, (size_t)m->nvp);
+  k_fill64<<<red_grid(m->nv), 256, 0, m->stream>>>(m->nv, 1.0, m->v64[5]);
+  k_cg32_init<<<red_grid(m->nvp), 256, 0, m->stream>>>(m->nv, m->nvp, m->v64[5], 1.0, m->v32[0], m->v32[1],
                                                        reinterpret_cast<float2 *>(m->v32[3]), m->dinv32, 0.0, 1 << 30,
                                                        m->scal, m->ictl, m->red.partials, m->red.counter);
   FG_LAUNCHED(2);
