@@ -457,8 +457,8 @@ extern "C" fg_status fg_mesh_create(const double *p, int64_t nv, const int32_t *
 
     // control and reduction workspace
     m->red.partials = dev_alloc<double>(m, ((size_t)grid_for(nv, 64) + FG_RED_BLOCKS) * 4);
-    m->red.counter = dev_alloc<unsigned int>(m, 16);
-    FG_CUDA_TRY(cudaMemsetAsync(m->red.counter, 0, 16 * sizeof(unsigned int), s));
+    m->red.counter = dev_alloc<unsigned int>(m, 128);   // two-level arrival counters
+    FG_CUDA_TRY(cudaMemsetAsync(m->red.counter, 0, 128 * sizeof(unsigned int), s));
     m->scal = dev_alloc<double>(m, S_NSCAL);
     m->ictl = dev_alloc<int>(m, I_NINT);
     FG_CUDA_TRY(cudaMallocHost(&m->hbuf, 64 * sizeof(double)));

@@ -126,6 +126,13 @@ __device__ __forceinline__ void block_sum_acc(const Acc<float> (&a)[N], double (
 // the last block, with the totals in tot.  The whole last block loads the partials
 // (independent loads), then a fixed-shape tree: the order of the sum depends only on
 // the grid size, so results are reproducible.
+// Arrival is counted in two levels so that no single counter takes one atomic per
+// block: block b arrives on counter[1 + b % 64]; the last block of each of those
+// groups arrives on counter[0]; the last of those finishes the sum and resets all
+// counters.  (Each arrival follows a __threadfence, so the finishing block sees every
+// partial.)
+constexpr int FG_ARRIVE_GROUPS = 64;
+
 template <int N>
 __device__ __forceinline__ bool grid_finish(const double (&v)[N], double *partials, unsigned *counter,
                                             double (&tot)[N]) {
@@ -134,12 +141,21 @@ __device__ __forceinline__ bool grid_finish(const double (&v)[N], double *partia
 #pragma unroll
     for (int j = 0; j < N; ++j) partials[(size_t)blockIdx.x * N + j] = v[j];
     __threadfence();
-    unsigned prev = atomicAdd(counter, 1u);
-    s_last = (prev == gridDim.x - 1);
+    const unsigned G = gridDim.x;
+    const unsigned grp = blockIdx.x % FG_ARRIVE_GROUPS;
+    const unsigned ngroups = G < FG_ARRIVE_GROUPS ? G : FG_ARRIVE_GROUPS;
+    const unsigned gsize = (G - grp + FG_ARRIVE_GROUPS - 1) / FG_ARRIVE_GROUPS;
+    bool last = false;
+    if (atomicAdd(counter + 1 + grp, 1u) == gsize - 1) {
+      __threadfence();
+      last = (atomicAdd(counter, 1u) == ngroups - 1);
+    }
+    s_last = last;
   }
   __syncthreads();
   if (!s_last) return false;
   __threadfence();
+  if (threadIdx.x <= FG_ARRIVE_GROUPS) counter[threadIdx.x] = 0u;
   double acc[N];
 #pragma unroll
   for (int j = 0; j < N; ++j) acc[j] = 0.0;
@@ -150,7 +166,6 @@ __device__ __forceinline__ bool grid_finish(const double (&v)[N], double *partia
   block_sum<N>(acc, shfin);
 #pragma unroll
   for (int j = 0; j < N; ++j) tot[j] = acc[j];
-  if (threadIdx.x == 0) *counter = 0u;
   return threadIdx.x == 0;
 }
 
@@ -848,8 +863,8 @@ static fg_mesh *matrix_handle(int64_t n, const int64_t *colptr, const int64_t *r
       FG_CUDA_TRY(cudaMemcpyAsync(m->dinv32, d32.data(), sizeof(float) * m->nvp, cudaMemcpyHostToDevice, m->stream));
     }
     m->red.partials = dev_alloc<double>(m, ((size_t)grid_for(n, 64) + FG_RED_BLOCKS) * 4);
-    m->red.counter = dev_alloc<unsigned int>(m, 16);
-    FG_CUDA_TRY(cudaMemsetAsync(m->red.counter, 0, 16 * sizeof(unsigned int), m->stream));
+    m->red.counter = dev_alloc<unsigned int>(m, 128);
+    FG_CUDA_TRY(cudaMemsetAsync(m->red.counter, 0, 128 * sizeof(unsigned int), m->stream));
     m->scal = dev_alloc<double>(m, S_NSCAL);
     m->ictl = dev_alloc<int>(m, I_NINT);
     m->flags = dev_alloc<int>(m, 4);
