@@ -163,7 +163,7 @@ struct fg_mesh {
   uint8_t *nl = nullptr;
 
   // vectors
-  double *v64[12] = {nullptr};
+  double *v64[16] = {nullptr};
   float *v32[8] = {nullptr};
 
   // reductions and CG control

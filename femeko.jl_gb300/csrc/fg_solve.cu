@@ -9,19 +9,20 @@
 // (int4, or short4 holding column - row when the matrix bandwidth fits 16 bits).
 // A warp's group loads are contiguous (512 B of FP32 values).
 //
-// Mixed precision (FP32 operator and vectors), two kernels per iteration:
-//   k_cg32_spmv   q = A pn with pn = z + beta p formed on the fly; p and z are
-//                 stored interleaved (one 8-byte gather per entry); p.q reduced,
-//                 alpha computed by the last block to finish;
-//   k_cg32_update x += alpha pn, r -= alpha q, z = D^-1 r on 4 rows per thread
-//                 (128-bit loads), r.z and r.r reduced, beta and the stopping test
-//                 computed by the last block.
-// Dot products use compensated (TwoSum) FP32 sums per thread and per block and FP64
-// across blocks.
+// The CG recurrences are those of Chronopoulos & Gear (1989): with u = D^-1 r,
+// w = A u, s = A p, one reduction per iteration (gamma = r.u, delta = w.u and r.r)
+// gives beta = gamma_new / gamma and alpha = gamma_new / (delta - beta gamma_new / alpha);
+// then s = w + beta s, p = u + beta p, x += alpha p, r -= alpha s, u = D^-1 r, w = A u.
 //
-// FP64 operator and vectors, three kernels per iteration (q = A p, the vector
-// update, p = z + beta p): on GB300 an FP64 FMA costs ~64 FP32 FMAs, so forming
-// z + beta p at every gathered entry would double the SpMV's FP64 work.
+// Mixed precision (FP32 operator and vectors): ONE kernel per iteration.  Each row
+// gathers its neighbours' (r, w, s, D^-1) -- one 16-byte load per entry, double
+// buffered -- and recomputes their new u = D^-1 (r - alpha (w + beta s)) on the fly,
+// so the vector updates and the SpMV share one pass over memory.  Dot products use
+// compensated (TwoSum) FP32 sums per thread and per block and FP64 across blocks.
+//
+// FP64 operator and vectors: two kernels per iteration (the pointwise updates, then
+// w = A u with the dot products).  On GB300 an FP64 FMA costs ~64 FP32 FMAs, so
+// recomputing u at every gathered entry would triple the SpMV's FP64 work.
 //
 // Scalars never leave the device; the host reads the "done" flag once per block of
 // iterations, each block replayed as a CUDA graph.  An FP64 residual b - A x (FP64
@@ -32,7 +33,6 @@
 #include <vector>
 
 #include "fg_common.cuh"
-
 // ------------------------------------------------------------------ reductions
 struct ff {
   float hi, lo;
@@ -186,31 +186,66 @@ struct ColRel {
 __device__ __forceinline__ int4 ld_cols(const int4 *p) { return __ldg(p); }
 __device__ __forceinline__ short4 ld_cols(const short4 *p) { return __ldg(p); }
 
-// ------------------------------------------------------------------ FP32 CG kernels
-// HOIST: issue all value/column loads of a row, then all gathers (rows of up to 16
-// slots); otherwise a 4x-unrolled loop.  BS: threads per block.  The autotuner picks
-// the variant per operator.
+
+// Scalar slots of the Chronopoulos-Gear recurrences (device doubles in scal[]):
+// S_RZ gamma = r.u, S_ALPHA, S_BETA, S_RR r.r, S_TOL2 stop threshold on r.r.
+
+// Last-block tail shared by the FP32 and FP64 iterations: from (gamma_new, delta,
+// r.r) the next alpha and beta, the iteration count and the stopping test.  The first
+// call after an initialisation (ictl[I_ITERS] < 0) sets beta = 0, alpha = gamma/delta.
+__device__ __forceinline__ void cgcg_scalars(const double (&tot)[3], double *scal, int *ictl) {
+  const double gam = tot[0], del = tot[1], rr = tot[2];
+  const int it = ictl[I_ITERS] + 1;
+  double beta = 0.0, alpha;
+  if (it == 0) {
+    alpha = (del != 0.0) ? gam / del : 0.0;
+    scal[S_TOL2] = scal[S_TOL2] * rr;  // relative threshold -> absolute, from r0.r0
+    ictl[I_DONE] = (rr == 0.0 || rr <= scal[S_TOL2]) ? 1 : 0;
+  } else {
+    const double gold = scal[S_RZ], aold = scal[S_ALPHA];
+    beta = (gold != 0.0) ? gam / gold : 0.0;
+    const double den = del - beta * gam / aold;
+    alpha = (den != 0.0) ? gam / den : 0.0;
+    if (!isfinite(rr)) { ictl[I_STATUS] = 2; ictl[I_DONE] = 1; }
+    else if (rr <= scal[S_TOL2]) { ictl[I_STATUS] = 0; ictl[I_DONE] = 1; }
+    else if (it >= ictl[I_MAXIT]) { ictl[I_STATUS] = 1; ictl[I_DONE] = 1; }
+  }
+  scal[S_RZ] = gam;
+  scal[S_RR] = rr;
+  scal[S_ALPHA] = alpha;
+  scal[S_BETA] = beta;
+  ictl[I_ITERS] = it;
+}
+
+// ------------------------------------------------------------------ FP32 CG (fused)
+// State per row in a float4 pair buffer: (r, w, s, dinv).  `first` computes
+// w0 = A u0 from (r0, -, -, dinv) with alpha = beta = 0 (then s stays 0); later
+// iterations apply the full recurrences.  HOIST: issue all loads of a row before the
+// FMAs (rows of up to 16 slots).  BS: threads per block (autotuned).
 template <class CI, bool HOIST, int BS>
-__global__ void __launch_bounds__(BS) k_cg32_spmv(int64_t n, const int *__restrict__ sl_ptr,
-                                                   const int *__restrict__ sl_len,
-                                                   const typename CI::T *__restrict__ col,
-                                                   const float *__restrict__ val, const float2 *__restrict__ pz_in,
-                                                   float2 *__restrict__ pz_out, float *__restrict__ q, double *scal,
-                                                   int *ictl, double *partials, unsigned *counter) {
+__global__ void __launch_bounds__(BS) k_cg32_iter(int64_t n, const int *__restrict__ sl_ptr,
+                                                  const int *__restrict__ sl_len,
+                                                  const typename CI::T *__restrict__ col,
+                                                  const float *__restrict__ val, const float4 *__restrict__ st_in,
+                                                  float4 *__restrict__ st_out, float *__restrict__ p,
+                                                  float *__restrict__ x, double *scal, int *ictl, double *partials,
+                                                  unsigned *counter) {
   if (ictl[I_DONE]) return;
-  const float beta = (float)scal[S_BETA];
+  const bool first = ictl[I_ITERS] < 0;
+  const float alpha = first ? 0.f : (float)scal[S_ALPHA];
+  const float beta = first ? 0.f : (float)scal[S_BETA];
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  Acc<float> prod[1];
+  Acc<float> dots[3];
   if (i < n) {
     const int s = (int)(i >> 5), lane = (int)(i & 31);
     const int64_t base = (int64_t)sl_ptr[s] + lane * FG_GROUP;
     const int G = sl_len[s];
     const float4 *v4 = reinterpret_cast<const float4 *>(val + base);
     const typename CI::T4 *c4 = reinterpret_cast<const typename CI::T4 *>(col + base);
+    // u_new of a neighbour from its (r, w, s, dinv)
+    auto unew = [&](const float4 a) { return a.w * fmaf(-alpha, fmaf(beta, a.z, a.y), a.x); };
     float acc = 0.f;
     if (HOIST && G <= 4) {
-      // rows of up to 16 slots (tetrahedral meshes): issue every value/column load,
-      // then every gather, then the FMAs, so one row has all its loads in flight
       float4 vv[4];
       typename CI::T4 cc[4];
 #pragma unroll
@@ -219,144 +254,113 @@ __global__ void __launch_bounds__(BS) k_cg32_spmv(int64_t n, const int *__restri
           vv[g] = __ldg(v4 + (int64_t)g * FG_SLICE);
           cc[g] = ld_cols(c4 + (int64_t)g * FG_SLICE);
         }
-      float2 pzg[4][4];
 #pragma unroll
       for (int g = 0; g < 4; ++g)
         if (g < G) {
-          pzg[g][0] = __ldg(pz_in + CI::col(cc[g].x, i));
-          pzg[g][1] = __ldg(pz_in + CI::col(cc[g].y, i));
-          pzg[g][2] = __ldg(pz_in + CI::col(cc[g].z, i));
-          pzg[g][3] = __ldg(pz_in + CI::col(cc[g].w, i));
-        }
-#pragma unroll
-      for (int g = 0; g < 4; ++g)
-        if (g < G) {
-          acc = fmaf(vv[g].x, fmaf(beta, pzg[g][0].x, pzg[g][0].y), acc);
-          acc = fmaf(vv[g].y, fmaf(beta, pzg[g][1].x, pzg[g][1].y), acc);
-          acc = fmaf(vv[g].z, fmaf(beta, pzg[g][2].x, pzg[g][2].y), acc);
-          acc = fmaf(vv[g].w, fmaf(beta, pzg[g][3].x, pzg[g][3].y), acc);
+          acc = fmaf(vv[g].x, unew(__ldg(st_in + CI::col(cc[g].x, i))), acc);
+          acc = fmaf(vv[g].y, unew(__ldg(st_in + CI::col(cc[g].y, i))), acc);
+          acc = fmaf(vv[g].z, unew(__ldg(st_in + CI::col(cc[g].z, i))), acc);
+          acc = fmaf(vv[g].w, unew(__ldg(st_in + CI::col(cc[g].w, i))), acc);
         }
     } else {
 #pragma unroll 4
       for (int g = 0; g < G; ++g) {
         const float4 vv = __ldg(v4 + (int64_t)g * FG_SLICE);
         const typename CI::T4 cc = ld_cols(c4 + (int64_t)g * FG_SLICE);
-        const float2 a = __ldg(pz_in + CI::col(cc.x, i));
-        const float2 b = __ldg(pz_in + CI::col(cc.y, i));
-        const float2 c = __ldg(pz_in + CI::col(cc.z, i));
-        const float2 d = __ldg(pz_in + CI::col(cc.w, i));
-        acc = fmaf(vv.x, fmaf(beta, a.x, a.y), acc);
-        acc = fmaf(vv.y, fmaf(beta, b.x, b.y), acc);
-        acc = fmaf(vv.z, fmaf(beta, c.x, c.y), acc);
-        acc = fmaf(vv.w, fmaf(beta, d.x, d.y), acc);
+        const float4 a = __ldg(st_in + CI::col(cc.x, i));
+        const float4 b = __ldg(st_in + CI::col(cc.y, i));
+        const float4 c = __ldg(st_in + CI::col(cc.z, i));
+        const float4 d = __ldg(st_in + CI::col(cc.w, i));
+        acc = fmaf(vv.x, unew(a), acc);
+        acc = fmaf(vv.y, unew(b), acc);
+        acc = fmaf(vv.z, unew(c), acc);
+        acc = fmaf(vv.w, unew(d), acc);
       }
     }
-    const float2 own = __ldg(pz_in + i);
-    const float pi = fmaf(beta, own.x, own.y);
-    reinterpret_cast<float *>(pz_out)[2 * i] = pi;   // p of the next pair
-    q[i] = acc;
-    prod[0].add(pi * acc);
+    // own row: s, p, x, r, u updates (same arithmetic as unew for the neighbours)
+    const float4 o = __ldg(st_in + i);
+    const float snew = fmaf(beta, o.z, o.y);
+    const float rnew = fmaf(-alpha, snew, o.x);
+    const float unw = o.w * rnew;
+    if (!first) {
+      const float pnew = fmaf(beta, p[i], o.w * o.x);
+      p[i] = pnew;
+      x[i] = fmaf(alpha, pnew, x[i]);
+    }
+    st_out[i] = make_float4(rnew, acc, snew, o.w);
+    dots[0].add(rnew * unw);
+    dots[1].add(acc * unw);
+    dots[2].add(rnew * rnew);
   }
-  double part[1];
-  block_sum_acc<1>(prod, part);
-  double tot[1];
-  if (grid_finish<1>(part, partials, counter, tot)) {
-    scal[S_PQ] = tot[0];
-    scal[S_ALPHA] = (tot[0] != 0.0) ? scal[S_RZ] / tot[0] : 0.0;
-  }
+  double part[3];
+  block_sum_acc<3>(dots, part);
+  double tot[3];
+  if (grid_finish<3>(part, partials, counter, tot)) cgcg_scalars(tot, scal, ictl);
 }
 
-// Common tail of the vector-update kernels: beta, the iteration count and the
-// stopping test (r.r <= TOL2, non-finite, or the iteration cap).
-__device__ __forceinline__ void cg_finish_update(const double (&tot)[2], double *scal, int *ictl) {
-  double rzo = scal[S_RZ];
-  scal[S_BETA] = (rzo != 0.0) ? tot[0] / rzo : 0.0;
-  scal[S_RZ] = tot[0];
-  scal[S_RR] = tot[1];
-  int it = ictl[I_ITERS] + 1;
-  ictl[I_ITERS] = it;
-  if (!isfinite(tot[1])) { ictl[I_STATUS] = 2; ictl[I_DONE] = 1; }
-  else if (tot[1] <= scal[S_TOL2]) { ictl[I_STATUS] = 0; ictl[I_DONE] = 1; }
-  else if (it >= ictl[I_MAXIT]) { ictl[I_STATUS] = 1; ictl[I_DONE] = 1; }
-}
-
-// Four rows per thread; n4 = padded rows / 4 (padded entries are zero).
-__global__ void __launch_bounds__(256) k_cg32_update(int64_t n4, float4 *__restrict__ x, float4 *__restrict__ r,
-                                                     const float4 *__restrict__ q, const float4 *__restrict__ dinv,
-                                                     float4 *__restrict__ pz, double *scal, int *ictl,
-                                                     double *partials, unsigned *counter) {
-  if (ictl[I_DONE]) return;
-  const float alpha = (float)scal[S_ALPHA];
-  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  Acc<float> a2[2];
-  if (j < n4) {
-    float4 xx = x[j], rr = r[j];
-    const float4 qq = q[j], dd = dinv[j];
-    float4 pz0 = pz[2 * j], pz1 = pz[2 * j + 1];   // (p0, z0, p1, z1), (p2, z2, p3, z3)
-    xx.x = fmaf(alpha, pz0.x, xx.x); xx.y = fmaf(alpha, pz0.z, xx.y);
-    xx.z = fmaf(alpha, pz1.x, xx.z); xx.w = fmaf(alpha, pz1.z, xx.w);
-    rr.x = fmaf(-alpha, qq.x, rr.x); rr.y = fmaf(-alpha, qq.y, rr.y);
-    rr.z = fmaf(-alpha, qq.z, rr.z); rr.w = fmaf(-alpha, qq.w, rr.w);
-    pz0.y = dd.x * rr.x; pz0.w = dd.y * rr.y; pz1.y = dd.z * rr.z; pz1.w = dd.w * rr.w;
-    x[j] = xx;
-    r[j] = rr;
-    pz[2 * j] = pz0;
-    pz[2 * j + 1] = pz1;
-    a2[0].add(rr.x * pz0.y); a2[0].add(rr.y * pz0.w); a2[0].add(rr.z * pz1.y); a2[0].add(rr.w * pz1.w);
-    a2[1].add(rr.x * rr.x); a2[1].add(rr.y * rr.y); a2[1].add(rr.z * rr.z); a2[1].add(rr.w * rr.w);
-  }
-  double part[2];
-  block_sum_acc<2>(a2, part);
-  double tot[2];
-  if (grid_finish<2>(part, partials, counter, tot)) cg_finish_update(tot, scal, ictl);
-}
-
-// r = scale * rin, z = D^-1 r, (p, z) = (0, z), x = 0; r.z and r.r set the scalars.
-// Stop when r.r <= tol2_rel * r0.r0.
-__global__ void __launch_bounds__(256) k_cg32_init(int64_t n, int64_t np, const double *__restrict__ rin,
-                                                   double scale, float *__restrict__ x, float *__restrict__ r,
-                                                   float2 *__restrict__ pz, const float *__restrict__ dinv,
-                                                   double tol2_rel, int maxit, double *scal, int *ictl,
-                                                   double *partials, unsigned *counter) {
-  double rz = 0, rr = 0;
+// r0 = scale * rin, state (r0, 0, 0, dinv) in both buffers, p = x = 0.  The threshold
+// tol2_rel becomes absolute (times r0.r0) in the first iteration.
+__global__ void k_cg32_init(int64_t n, int64_t np, const double *__restrict__ rin, double scale,
+                            const float *__restrict__ dinv, float4 *__restrict__ st0, float4 *__restrict__ st1,
+                            float *__restrict__ p, float *__restrict__ x, double tol2_rel, int maxit, double *scal,
+                            int *ictl) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < np; i += stride) {
-    float ri = (i < n) ? (float)(scale * rin[i]) : 0.f;
-    float zi = dinv[i] * ri;
+    const float ri = (i < n) ? (float)(scale * rin[i]) : 0.f;
+    const float4 v = make_float4(ri, 0.f, 0.f, dinv[i]);
+    st0[i] = v;
+    st1[i] = v;
+    p[i] = 0.f;
     x[i] = 0.f;
-    r[i] = ri;
-    pz[i] = make_float2(0.f, zi);
-    rz += (double)ri * (double)zi;
-    rr += (double)ri * (double)ri;
   }
-  __shared__ double shd[2][32];
-  double part[2] = {rz, rr};
-  block_sum<2>(part, shd);
-  double tot[2];
-  if (grid_finish<2>(part, partials, counter, tot)) {
-    scal[S_RZ] = tot[0];
-    scal[S_RR] = tot[1];
-    scal[S_BETA] = 0.0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    scal[S_TOL2] = tol2_rel;
     scal[S_ALPHA] = 0.0;
-    scal[S_TOL2] = tol2_rel * tot[1];
-    ictl[I_ITERS] = 0;
+    scal[S_BETA] = 0.0;
+    ictl[I_ITERS] = -1;
     ictl[I_MAXIT] = maxit;
     ictl[I_STATUS] = 0;
-    ictl[I_DONE] = (tot[1] <= scal[S_TOL2] || tot[1] == 0.0) ? 1 : 0;
+    ictl[I_DONE] = 0;
   }
 }
 
-// ------------------------------------------------------------------ FP64 CG kernels
+// ------------------------------------------------------------------ FP64 CG
+// Pointwise part: s = w + beta s, p = u + beta p, x += alpha p, r -= alpha s, u = D^-1 r
+// (two rows per thread, double2).
+__global__ void __launch_bounds__(256) k_cg64_vec(int64_t n2, double2 *__restrict__ r, const double2 *__restrict__ w,
+                                                  double2 *__restrict__ s, double2 *__restrict__ p,
+                                                  double2 *__restrict__ u, double2 *__restrict__ x,
+                                                  const double2 *__restrict__ dinv, const double *scal,
+                                                  const int *ictl) {
+  if (ictl[I_DONE]) return;
+  const double alpha = scal[S_ALPHA], beta = scal[S_BETA];
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n2) return;
+  const double2 ww = w[j], dd = dinv[j], uu = u[j];
+  double2 ss = s[j], pp = p[j], xx = x[j], rr = r[j];
+  ss.x = fma(beta, ss.x, ww.x); ss.y = fma(beta, ss.y, ww.y);
+  pp.x = fma(beta, pp.x, uu.x); pp.y = fma(beta, pp.y, uu.y);
+  xx.x = fma(alpha, pp.x, xx.x); xx.y = fma(alpha, pp.y, xx.y);
+  rr.x = fma(-alpha, ss.x, rr.x); rr.y = fma(-alpha, ss.y, rr.y);
+  s[j] = ss;
+  p[j] = pp;
+  x[j] = xx;
+  r[j] = rr;
+  u[j] = make_double2(dd.x * rr.x, dd.y * rr.y);
+}
+
+// w = A u with gamma = r.u, delta = w.u and r.r reduced; the last block sets the
+// next alpha, beta and the stopping test.
 template <class CI>
 __global__ void __launch_bounds__(256) k_cg64_spmv(int64_t n, const int *__restrict__ sl_ptr,
                                                    const int *__restrict__ sl_len,
                                                    const typename CI::T *__restrict__ col,
-                                                   const double *__restrict__ val, const double *__restrict__ p,
-                                                   double *__restrict__ q, double *scal, int *ictl, double *partials,
-                                                   unsigned *counter) {
+                                                   const double *__restrict__ val, const double *__restrict__ u,
+                                                   const double *__restrict__ r, double *__restrict__ w,
+                                                   double *scal, int *ictl, double *partials, unsigned *counter) {
   if (ictl[I_DONE]) return;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  double prod = 0.0;
+  double d3[3] = {0.0, 0.0, 0.0};
   if (i < n) {
     const int s = (int)(i >> 5), lane = (int)(i & 31);
     const int64_t base = (int64_t)sl_ptr[s] + lane * FG_GROUP;
@@ -369,98 +373,45 @@ __global__ void __launch_bounds__(256) k_cg64_spmv(int64_t n, const int *__restr
       const double2 va = __ldg(v2 + (int64_t)g * 2 * FG_SLICE);
       const double2 vb = __ldg(v2 + (int64_t)g * 2 * FG_SLICE + 1);
       const typename CI::T4 cc = ld_cols(c4 + (int64_t)g * FG_SLICE);
-      acc = fma(va.x, __ldg(p + CI::col(cc.x, i)), acc);
-      acc = fma(va.y, __ldg(p + CI::col(cc.y, i)), acc);
-      acc = fma(vb.x, __ldg(p + CI::col(cc.z, i)), acc);
-      acc = fma(vb.y, __ldg(p + CI::col(cc.w, i)), acc);
+      acc = fma(va.x, __ldg(u + CI::col(cc.x, i)), acc);
+      acc = fma(va.y, __ldg(u + CI::col(cc.y, i)), acc);
+      acc = fma(vb.x, __ldg(u + CI::col(cc.z, i)), acc);
+      acc = fma(vb.y, __ldg(u + CI::col(cc.w, i)), acc);
     }
-    q[i] = acc;
-    prod = p[i] * acc;
+    w[i] = acc;
+    const double ui = u[i], ri = r[i];
+    d3[0] = ri * ui;
+    d3[1] = acc * ui;
+    d3[2] = ri * ri;
   }
-  __shared__ double shd[1][32];
-  double part[1] = {prod};
-  block_sum<1>(part, shd);
-  double tot[1];
-  if (grid_finish<1>(part, partials, counter, tot)) {
-    scal[S_PQ] = tot[0];
-    scal[S_ALPHA] = (tot[0] != 0.0) ? scal[S_RZ] / tot[0] : 0.0;
-  }
+  __shared__ double shd[3][32];
+  block_sum<3>(d3, shd);
+  double tot[3];
+  if (grid_finish<3>(d3, partials, counter, tot)) cgcg_scalars(tot, scal, ictl);
 }
 
-// Four rows per thread (two double2 per vector).
-__global__ void __launch_bounds__(256) k_cg64_update(int64_t n4, double2 *__restrict__ x, double2 *__restrict__ r,
-                                                     double2 *__restrict__ z, const double2 *__restrict__ p,
-                                                     const double2 *__restrict__ q, const double2 *__restrict__ dinv,
-                                                     double *scal, int *ictl, double *partials, unsigned *counter) {
-  if (ictl[I_DONE]) return;
-  const double alpha = scal[S_ALPHA];
-  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  double rz = 0.0, rrs = 0.0;
-  if (j < n4) {
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int64_t k = 2 * j + h;
-      double2 xx = x[k], rr = r[k];
-      const double2 pp = p[k], qq = q[k], dd = dinv[k];
-      xx.x = fma(alpha, pp.x, xx.x); xx.y = fma(alpha, pp.y, xx.y);
-      rr.x = fma(-alpha, qq.x, rr.x); rr.y = fma(-alpha, qq.y, rr.y);
-      double2 zz = make_double2(dd.x * rr.x, dd.y * rr.y);
-      x[k] = xx;
-      r[k] = rr;
-      z[k] = zz;
-      rz += rr.x * zz.x + rr.y * zz.y;
-      rrs += rr.x * rr.x + rr.y * rr.y;
-    }
-  }
-  __shared__ double shd[2][32];
-  double part[2] = {rz, rrs};
-  block_sum<2>(part, shd);
-  double tot[2];
-  if (grid_finish<2>(part, partials, counter, tot)) cg_finish_update(tot, scal, ictl);
-}
-
-__global__ void __launch_bounds__(256) k_cg64_pupd(int64_t n2, const double2 *__restrict__ z, double2 *__restrict__ p,
-                                                   const double *scal, const int *ictl) {
-  if (ictl[I_DONE]) return;
-  const double beta = scal[S_BETA];
-  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (j < n2) {
-    double2 zz = z[j], pp = p[j];
-    p[j] = make_double2(fma(beta, pp.x, zz.x), fma(beta, pp.y, zz.y));
-  }
-}
-
-__global__ void __launch_bounds__(256) k_cg64_init(int64_t n, int64_t np, const double *__restrict__ rin,
-                                                   double scale, double *__restrict__ x, double *__restrict__ r,
-                                                   double *__restrict__ z, double *__restrict__ p,
-                                                   const double *__restrict__ dinv, double tol2_rel, int maxit,
-                                                   double *scal, int *ictl, double *partials, unsigned *counter) {
-  double rz = 0, rr = 0;
+// r = scale * rin, u = D^-1 r, s = p = x = 0 (w comes from the first SpMV).
+__global__ void k_cg64_init(int64_t n, int64_t np, const double *__restrict__ rin, double scale,
+                            const double *__restrict__ dinv, double *__restrict__ r, double *__restrict__ u,
+                            double *__restrict__ s, double *__restrict__ p, double *__restrict__ x, double tol2_rel,
+                            int maxit, double *scal, int *ictl) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < np; i += stride) {
-    double ri = (i < n) ? scale * rin[i] : 0.0;
-    double zi = dinv[i] * ri;
-    x[i] = 0.0;
+    const double ri = (i < n) ? scale * rin[i] : 0.0;
     r[i] = ri;
-    z[i] = zi;
-    p[i] = zi;
-    rz += ri * zi;
-    rr += ri * ri;
+    u[i] = dinv[i] * ri;
+    s[i] = 0.0;
+    p[i] = 0.0;
+    x[i] = 0.0;
   }
-  __shared__ double shd[2][32];
-  double part[2] = {rz, rr};
-  block_sum<2>(part, shd);
-  double tot[2];
-  if (grid_finish<2>(part, partials, counter, tot)) {
-    scal[S_RZ] = tot[0];
-    scal[S_RR] = tot[1];
-    scal[S_BETA] = 0.0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    scal[S_TOL2] = tol2_rel;
     scal[S_ALPHA] = 0.0;
-    scal[S_TOL2] = tol2_rel * tot[1];
-    ictl[I_ITERS] = 0;
+    scal[S_BETA] = 0.0;
+    ictl[I_ITERS] = -1;
     ictl[I_MAXIT] = maxit;
     ictl[I_STATUS] = 0;
-    ictl[I_DONE] = (tot[1] <= scal[S_TOL2] || tot[1] == 0.0) ? 1 : 0;
+    ictl[I_DONE] = 0;
   }
 }
 
@@ -533,7 +484,6 @@ static unsigned red_grid(int64_t n) {
   return g > (unsigned)FG_RED_BLOCKS ? (unsigned)FG_RED_BLOCKS : g;
 }
 static unsigned row_grid(const fg_mesh *m) { return grid_for(m->nv, 256); }
-static unsigned quad_grid(const fg_mesh *m) { return grid_for(m->nvp / 4, 256); }
 
 double fg_dot_dev(fg_mesh *m, const double *x, const double *y, int64_t n, bool mask_fixed) {
   const int slot = 8;
@@ -565,90 +515,100 @@ static void spmv64_launch(fg_mesh *m, const double *x, const double *b, double *
 void fg_spmv64_dev(fg_mesh *m, const double *x, double *y) { spmv64_launch(m, x, nullptr, y, nullptr, -1); }
 
 // CG vectors, padded to whole slices and zeroed once (pads stay zero).
-// FP32 set: v32[0] x, v32[1] r, v32[2] q, v32[3] (p,z) pair 0, v32[4] (p,z) pair 1.
-// FP64 set: v64[0] x, v64[1] r, v64[2] z, v64[3] p, v64[4] q.
+// FP32: v32[0] x, v32[1] p, v32[2] / v32[3] the two (r, w, s, dinv) state buffers.
+// FP64: v64[0] x, v64[1] r, v64[2] u, v64[3] s, v64[4] p, v64[12] w.
 static void ensure_cg32(fg_mesh *m) {
-  for (int j = 0; j < 5; ++j)
+  for (int j = 0; j < 4; ++j)
     if (!m->v32[j]) {
-      size_t len = (size_t)m->nvp * (j >= 3 ? 2 : 1);
+      size_t len = (size_t)m->nvp * (j >= 2 ? 4 : 1);
       m->v32[j] = dev_alloc<float>(m, len);
       FG_CUDA_TRY(cudaMemsetAsync(m->v32[j], 0, sizeof(float) * len, m->stream));
     }
 }
 static void ensure_cg64(fg_mesh *m) {
-  for (int j = 0; j < 5; ++j)
+  const int idx[6] = {0, 1, 2, 3, 4, 12};
+  for (int j : idx)
     if (!m->v64[j]) {
       m->v64[j] = dev_alloc<double>(m, (size_t)m->nvp);
       FG_CUDA_TRY(cudaMemsetAsync(m->v64[j], 0, sizeof(double) * (size_t)m->nvp, m->stream));
     }
 }
 
-// FP32 SpMV variants (block size x load scheduling) for the autotuner.
+// FP32 iteration variants (block size x load scheduling) for the autotuner.
 constexpr int FG_N_SPMV32 = 4;
-static const char *spmv32_names[FG_N_SPMV32] = {"loop/256", "hoist/256", "loop/128", "loop/512"};
 
 template <class CI>
-static void spmv32_variant(fg_mesh *m, int v, const typename CI::T *col, const float2 *pz_in, float2 *pz_out) {
-  auto args = [&](auto kern, int bs) {
-    kern<<<grid_for(m->nv, bs), bs, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, col, m->val32, pz_in, pz_out,
-                                                     m->v32[2], m->scal, m->ictl, m->red.partials, m->red.counter);
+static void iter32_variant(fg_mesh *m, int v, const typename CI::T *col, const float4 *in, float4 *out) {
+  auto go = [&](auto kern, int bs) {
+    kern<<<grid_for(m->nv, bs), bs, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, col, m->val32, in, out, m->v32[1],
+                                                     m->v32[0], m->scal, m->ictl, m->red.partials, m->red.counter);
   };
   switch (v) {
-    case 1: args(k_cg32_spmv<CI, true, 256>, 256); break;
-    case 2: args(k_cg32_spmv<CI, false, 128>, 128); break;
-    case 3: args(k_cg32_spmv<CI, false, 512>, 512); break;
-    default: args(k_cg32_spmv<CI, false, 256>, 256); break;
+    case 1: go(k_cg32_iter<CI, true, 256>, 256); break;
+    case 2: go(k_cg32_iter<CI, false, 128>, 128); break;
+    case 3: go(k_cg32_iter<CI, false, 512>, 512); break;
+    default: go(k_cg32_iter<CI, false, 256>, 256); break;
   }
 }
 
-static void launch_spmv32(fg_mesh *m, int v, const float2 *pz_in, float2 *pz_out) {
-  if (m->use_dcol) spmv32_variant<ColRel>(m, v, m->sl_dcol, pz_in, pz_out);
-  else spmv32_variant<ColAbs>(m, v, m->sl_col, pz_in, pz_out);
+static void launch_iter32(fg_mesh *m, int v, bool from_first_buffer) {
+  const float4 *in = reinterpret_cast<const float4 *>(from_first_buffer ? m->v32[2] : m->v32[3]);
+  float4 *out = reinterpret_cast<float4 *>(from_first_buffer ? m->v32[3] : m->v32[2]);
+  if (m->use_dcol) iter32_variant<ColRel>(m, v, m->sl_dcol, in, out);
+  else iter32_variant<ColAbs>(m, v, m->sl_col, in, out);
 }
 
-static void launch_iter32(fg_mesh *m, bool odd) {
-  float2 *pz_in = reinterpret_cast<float2 *>(odd ? m->v32[4] : m->v32[3]);
-  float2 *pz_out = reinterpret_cast<float2 *>(odd ? m->v32[3] : m->v32[4]);
-  launch_spmv32(m, m->spmv_variant32, pz_in, pz_out);
-  k_cg32_update<<<quad_grid(m), 256, 0, m->stream>>>(
-      m->nvp / 4, reinterpret_cast<float4 *>(m->v32[0]), reinterpret_cast<float4 *>(m->v32[1]),
-      reinterpret_cast<const float4 *>(m->v32[2]), reinterpret_cast<const float4 *>(m->dinv32),
-      reinterpret_cast<float4 *>(pz_out), m->scal, m->ictl, m->red.partials, m->red.counter);
-}
-
-static void launch_iter64(fg_mesh *m) {
+static void launch_spmv64cg(fg_mesh *m) {
   if (m->use_dcol)
     k_cg64_spmv<ColRel><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, m->val64,
-                                                            m->v64[3], m->v64[4], m->scal, m->ictl, m->red.partials,
-                                                            m->red.counter);
+                                                            m->v64[2], m->v64[1], m->v64[12], m->scal, m->ictl,
+                                                            m->red.partials, m->red.counter);
   else
     k_cg64_spmv<ColAbs><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val64,
-                                                            m->v64[3], m->v64[4], m->scal, m->ictl, m->red.partials,
-                                                            m->red.counter);
-  k_cg64_update<<<quad_grid(m), 256, 0, m->stream>>>(
-      m->nvp / 4, reinterpret_cast<double2 *>(m->v64[0]), reinterpret_cast<double2 *>(m->v64[1]),
-      reinterpret_cast<double2 *>(m->v64[2]), reinterpret_cast<const double2 *>(m->v64[3]),
-      reinterpret_cast<const double2 *>(m->v64[4]), reinterpret_cast<const double2 *>(m->dinv64), m->scal, m->ictl,
-      m->red.partials, m->red.counter);
-  k_cg64_pupd<<<grid_for(m->nvp / 2, 256), 256, 0, m->stream>>>(m->nvp / 2, reinterpret_cast<const double2 *>(m->v64[2]),
-                                                                reinterpret_cast<double2 *>(m->v64[3]), m->scal,
-                                                                m->ictl);
+                                                            m->v64[2], m->v64[1], m->v64[12], m->scal, m->ictl,
+                                                            m->red.partials, m->red.counter);
+}
+
+static void launch_vec64(fg_mesh *m) {
+  k_cg64_vec<<<grid_for(m->nvp / 2, 256), 256, 0, m->stream>>>(
+      m->nvp / 2, reinterpret_cast<double2 *>(m->v64[1]), reinterpret_cast<const double2 *>(m->v64[12]),
+      reinterpret_cast<double2 *>(m->v64[3]), reinterpret_cast<double2 *>(m->v64[4]),
+      reinterpret_cast<double2 *>(m->v64[2]), reinterpret_cast<double2 *>(m->v64[0]),
+      reinterpret_cast<const double2 *>(m->dinv64), m->scal, m->ictl);
+}
+
+// Initialisation and the first pass (w0 = A u0 and the first alpha): FP32 state
+// buffer 0 -> 1, so the iteration blocks start reading buffer 1.
+static void start_cg(fg_mesh *m, bool mixed, const double *r64, double scale, double tol2_rel, int maxit) {
+  const unsigned g = red_grid(m->nvp);
+  if (mixed) {
+    k_cg32_init<<<g, 256, 0, m->stream>>>(m->nv, m->nvp, r64, scale, m->dinv32,
+                                          reinterpret_cast<float4 *>(m->v32[2]), reinterpret_cast<float4 *>(m->v32[3]),
+                                          m->v32[1], m->v32[0], tol2_rel, maxit, m->scal, m->ictl);
+    launch_iter32(m, m->spmv_variant32, true);
+  } else {
+    k_cg64_init<<<g, 256, 0, m->stream>>>(m->nv, m->nvp, r64, scale, m->dinv64, m->v64[1], m->v64[2], m->v64[3],
+                                          m->v64[4], m->v64[0], tol2_rel, maxit, m->scal, m->ictl);
+    launch_spmv64cg(m);
+  }
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(2);
 }
 
 // Runs CG iterations until the device sets "done".  Returns the iteration count.
 static int run_cg(fg_mesh *m, bool mixed, const fg_solve_opts &o, int *status) {
   int block = o.check_every > 0 ? o.check_every : 32;
   if (block & 1) ++block;
-  const int per_iter = mixed ? 2 : 3;
+  const int per_iter = mixed ? 1 : 2;
   GraphCache &gc = m->graph[mixed ? 1 : 0];
   const void *key[4] = {mixed ? (const void *)m->val32 : (const void *)m->val64,
-                        mixed ? (const void *)m->v32[0] : (const void *)m->v64[0], (const void *)(intptr_t)block,
-                        (const void *)(intptr_t)m->use_dcol};
+                        mixed ? (const void *)(intptr_t)(m->spmv_variant32 + 1) : (const void *)m->v64[0],
+                        (const void *)(intptr_t)block, (const void *)(intptr_t)m->use_dcol};
   const bool use_graph = o.use_graph != 0;
   auto enqueue_block = [&]() {
     for (int it = 0; it < block; ++it) {
-      if (mixed) launch_iter32(m, it & 1);
-      else launch_iter64(m);
+      if (mixed) launch_iter32(m, m->spmv_variant32, (it & 1) != 0);
+      else { launch_vec64(m); launch_spmv64cg(m); }
     }
   };
   if (use_graph) {
@@ -667,6 +627,9 @@ static int run_cg(fg_mesh *m, bool mixed, const fg_solve_opts &o, int *status) {
     }
   }
   for (;;) {
+    FG_CUDA_TRY(cudaMemcpyAsync(m->hint, m->ictl, sizeof(int) * 4, cudaMemcpyDeviceToHost, m->stream));
+    fg_sync(m);
+    if (m->hint[I_DONE]) break;
     if (use_graph) {
       FG_CUDA_TRY(cudaGraphLaunch(gc.exec, m->stream));
     } else {
@@ -674,12 +637,9 @@ static int run_cg(fg_mesh *m, bool mixed, const fg_solve_opts &o, int *status) {
       FG_CUDA_TRY(cudaGetLastError());
     }
     FG_LAUNCHED((long long)per_iter * block);
-    FG_CUDA_TRY(cudaMemcpyAsync(m->hint, m->ictl, sizeof(int) * 4, cudaMemcpyDeviceToHost, m->stream));
-    fg_sync(m);
-    if (m->hint[I_DONE]) break;
   }
   if (status) *status = m->hint[I_STATUS];
-  return m->hint[I_ITERS];
+  return std::max(m->hint[I_ITERS], 0);
 }
 
 fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_variant);
@@ -688,36 +648,25 @@ fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_v
 // x += d / scale.  Returns iterations; *ist = 0 converged, 1 cap, 2 non-finite.
 static int inner_solve(fg_mesh *m, bool mixed, const double *r64, double rn, double inner, int maxit,
                        const fg_solve_opts &o, double *d_x, int *ist) {
-  unsigned g = red_grid(m->nvp);
   int its;
   if (mixed) {
     ensure_cg32(m);
     if (o.spmv > 0 && o.spmv <= FG_N_SPMV32) {
-      if (m->spmv_variant32 != o.spmv - 1 && m->graph[1].exec) {
-        cudaGraphExecDestroy(m->graph[1].exec);
-        m->graph[1].exec = nullptr;
-      }
       m->spmv_variant32 = o.spmv - 1;
     } else if (!m->tuned32) {
       fg_autotune_spmv32(m, 20, nullptr, nullptr);
     }
-    k_cg32_init<<<g, 256, 0, m->stream>>>(m->nv, m->nvp, r64, 1.0 / rn, m->v32[0], m->v32[1],
-                                          reinterpret_cast<float2 *>(m->v32[3]), m->dinv32, inner * inner, maxit,
-                                          m->scal, m->ictl, m->red.partials, m->red.counter);
-    FG_CUDA_TRY(cudaGetLastError());
+    start_cg(m, true, r64, 1.0 / rn, inner * inner, maxit);
     its = run_cg(m, true, o, ist);
     k_axpy_to64<float><<<red_grid(m->nv), 256, 0, m->stream>>>(m->nv, rn, m->v32[0], d_x);
   } else {
     ensure_cg64(m);
-    k_cg64_init<<<g, 256, 0, m->stream>>>(m->nv, m->nvp, r64, 1.0 / rn, m->v64[0], m->v64[1], m->v64[2], m->v64[3],
-                                          m->dinv64, inner * inner, maxit, m->scal, m->ictl, m->red.partials,
-                                          m->red.counter);
-    FG_CUDA_TRY(cudaGetLastError());
+    start_cg(m, false, r64, 1.0 / rn, inner * inner, maxit);
     its = run_cg(m, false, o, ist);
     k_axpy_to64<double><<<red_grid(m->nv), 256, 0, m->stream>>>(m->nv, rn, m->v64[0], d_x);
   }
   FG_CUDA_TRY(cudaGetLastError());
-  FG_LAUNCHED(2);
+  FG_LAUNCHED(1);
   return its;
 }
 
@@ -918,106 +867,74 @@ extern "C" fg_status fg_spmv_csc(int64_t n, const int64_t *colptr, const int64_t
   return st;
 }
 
+
+// ------------------------------------------------------------------ timing and tuning
+// A CG state for timing: residual of ones, zero tolerance, no iteration cap, then the
+// first pass.  Uses v64[5] as its scratch right-hand side (the refinement residual in
+// v64[6] stays untouched).
+static void timing_state(fg_mesh *m, bool mixed) {
+  if (!m->v64[5]) m->v64[5] = dev_alloc<double>(m, (size_t)m->nvp);
+  k_fill64<<<red_grid(m->nv), 256, 0, m->stream>>>(m->nv, 1.0, m->v64[5]);
+  if (mixed) ensure_cg32(m);
+  else ensure_cg64(m);
+  start_cg(m, mixed, m->v64[5], 1.0, 0.0, 1 << 30);
+  FG_LAUNCHED(1);
+}
+
 // Average duration of one CG kernel launch on the handle's current operator (events
-// on the handle's stream): which = 0 the SpMV, 1 the vector update.  Leaves the CG
-// vectors in an unspecified state.
+// on the handle's stream): which = 0 the FP32 fused iteration or the FP64 SpMV with
+// its dot products, 1 the FP64 pointwise update.  Leaves the CG vectors in an
+// unspecified state.
 fg_status fg_bench_cg_kernel(fg_mesh *m, int which, int precision, int reps, double *ms_per_launch) {
   const bool mixed = precision == FG_MIXED;
   FG_REQUIRE(mixed ? m->val32 != nullptr : m->val64 != nullptr, FG_BAD_ARG, "operator not assembled");
-  if (!m->v64[5]) m->v64[5] = dev_alloc<double>(m, (size_t)m->nvp);
-  k_fill64<<<red_grid(m->nv), 256, 0, m->stream>>>(m->nv, 1.0, m->v64[5]);
-  // a CG state that never reports "done": r = 1, tolerance 0, huge iteration cap
-  if (mixed) {
-    ensure_cg32(m);
-    k_cg32_init<<<red_grid(m->nvp), 256, 0, m->stream>>>(m->nv, m->nvp, m->v64[5], 1.0, m->v32[0], m->v32[1],
-                                                         reinterpret_cast<float2 *>(m->v32[3]), m->dinv32, 0.0,
-                                                         1 << 30, m->scal, m->ictl, m->red.partials, m->red.counter);
-  } else {
-    ensure_cg64(m);
-    k_cg64_init<<<red_grid(m->nvp), 256, 0, m->stream>>>(m->nv, m->nvp, m->v64[5], 1.0, m->v64[0], m->v64[1],
-                                                         m->v64[2], m->v64[3], m->dinv64, 0.0, 1 << 30, m->scal,
-                                                         m->ictl, m->red.partials, m->red.counter);
-  }
-  FG_LAUNCHED(2);
+  timing_state(m, mixed);
   auto body = [&](int n) {
     for (int r = 0; r < n; ++r) {
-      if (mixed) {
-        float2 *pz0 = reinterpret_cast<float2 *>(m->v32[3]), *pz1 = reinterpret_cast<float2 *>(m->v32[4]);
-        if (which == 0) {
-          launch_spmv32(m, m->spmv_variant32, pz0, pz1);
-        } else {
-          k_cg32_update<<<quad_grid(m), 256, 0, m->stream>>>(
-              m->nvp / 4, reinterpret_cast<float4 *>(m->v32[0]), reinterpret_cast<float4 *>(m->v32[1]),
-              reinterpret_cast<const float4 *>(m->v32[2]), reinterpret_cast<const float4 *>(m->dinv32),
-              reinterpret_cast<float4 *>(pz1), m->scal, m->ictl, m->red.partials, m->red.counter);
-        }
-      } else {
-        if (which == 0) {
-          if (m->use_dcol)
-            k_cg64_spmv<ColRel><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, m->val64,
-                                                                    m->v64[3], m->v64[4], m->scal, m->ictl,
-                                                                    m->red.partials, m->red.counter);
-          else
-            k_cg64_spmv<ColAbs><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val64,
-                                                                    m->v64[3], m->v64[4], m->scal, m->ictl,
-                                                                    m->red.partials, m->red.counter);
-        } else {
-          k_cg64_update<<<quad_grid(m), 256, 0, m->stream>>>(
-              m->nvp / 4, reinterpret_cast<double2 *>(m->v64[0]), reinterpret_cast<double2 *>(m->v64[1]),
-              reinterpret_cast<double2 *>(m->v64[2]), reinterpret_cast<const double2 *>(m->v64[3]),
-              reinterpret_cast<const double2 *>(m->v64[4]), reinterpret_cast<const double2 *>(m->dinv64), m->scal,
-              m->ictl, m->red.partials, m->red.counter);
-        }
-      }
+      if (mixed) launch_iter32(m, m->spmv_variant32, (r & 1) == 0 ? false : true);
+      else if (which == 0) launch_spmv64cg(m);
+      else launch_vec64(m);
     }
     FG_LAUNCHED(n);
   };
-  FG_CUDA_TRY(cudaMemsetAsync(m->ictl, 0, sizeof(int), m->stream));  // clear "done"
-  body(3);
+  body(2);
   FG_CUDA_TRY(cudaEventRecord(m->ev0, m->stream));
-  body(reps);
+  body(reps & ~1);
   FG_CUDA_TRY(cudaEventRecord(m->ev1, m->stream));
   FG_CUDA_TRY(cudaGetLastError());
   fg_sync(m);
   float ms = 0.f;
   FG_CUDA_TRY(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
-  *ms_per_launch = ms / reps;
+  *ms_per_launch = ms / (reps & ~1);
   return FG_OK;
 }
 
-// Autotuner: times every FP32 CG SpMV variant (block size x load scheduling) on the
-// handle's current operator with CUDA events and keeps the fastest for the handle.
-// Runs once per handle at its first mixed-precision solve (or on request).
+// Autotuner: times every FP32 CG iteration variant (block size x load scheduling) on
+// the handle's current operator with CUDA events and keeps the fastest for the
+// handle.  Runs once per handle at its first mixed-precision solve (or on request).
 fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_variant) {
   FG_REQUIRE(m->val32 != nullptr, FG_BAD_ARG, "autotune: no FP32 operator assembled");
-  ensure_cg32(m);
-  if (!m->v64[5]) m->v64[5] = dev_alloc<double>(m, (size_t)m->nvp);
-  k_fill64<<<red_grid(m->nv), 256, 0, m->stream>>>(m->nv, 1.0, m->v64[5]);
-  k_cg32_init<<<red_grid(m->nvp), 256, 0, m->stream>>>(m->nv, m->nvp, m->v64[5], 1.0, m->v32[0], m->v32[1],
-                                                       reinterpret_cast<float2 *>(m->v32[3]), m->dinv32, 0.0, 1 << 30,
-                                                       m->scal, m->ictl, m->red.partials, m->red.counter);
-  FG_LAUNCHED(2);
-  FG_CUDA_TRY(cudaMemsetAsync(m->ictl, 0, sizeof(int), m->stream));
-  float2 *pz0 = reinterpret_cast<float2 *>(m->v32[3]), *pz1 = reinterpret_cast<float2 *>(m->v32[4]);
+  reps = std::max(2, reps & ~1);
   int best = 0;
   double best_us = 1e30;
   for (int v = 0; v < FG_N_SPMV32; ++v) {
-    for (int r = 0; r < 3; ++r) launch_spmv32(m, v, pz0, pz1);
+    m->spmv_variant32 = v;
+    timing_state(m, true);
+    for (int r = 0; r < 2; ++r) launch_iter32(m, v, r == 1);
     FG_CUDA_TRY(cudaEventRecord(m->ev0, m->stream));
-    for (int r = 0; r < reps; ++r) launch_spmv32(m, v, pz0, pz1);
+    for (int r = 0; r < reps; ++r) launch_iter32(m, v, r & 1);
     FG_CUDA_TRY(cudaEventRecord(m->ev1, m->stream));
     FG_CUDA_TRY(cudaGetLastError());
-    FG_LAUNCHED(reps + 3);
+    FG_LAUNCHED(reps + 2);
     fg_sync(m);
     float ms = 0.f;
     FG_CUDA_TRY(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
-    double us = 1e3 * ms / reps;
+    const double us = 1e3 * ms / reps;
     if (us_per_variant) us_per_variant[v] = us;
     if (us < best_us) { best_us = us; best = v; }
   }
   m->spmv_variant32 = best;
   m->tuned32 = true;
-  if (m->graph[1].exec) { cudaGraphExecDestroy(m->graph[1].exec); m->graph[1].exec = nullptr; }
   if (chosen) *chosen = best;
   return FG_OK;
 }
