@@ -242,27 +242,36 @@ def run_ours(args):
     lib.fg_mesh_layout(g.h, C.byref(nsell), C.byref(ninc), C.byref(nsl))
     fg.newton_magnetostatics(mesh, nl, mu_lin, u0, precision="mixed")   # leaves J32 on the handle
     chosen = C.c_int32()
-    variants_us = np.zeros(4)
-    L.check(lib.fg_autotune(g.h, L.FG_MIXED, C.byref(chosen), L.ptr(variants_us), 4))
-    autotune = {"spmv32_variants_us": [round(float(v), 2) for v in variants_us], "chosen": int(chosen.value),
-                "names": ["loop/256", "hoist/256", "loop/128", "loop/512"]}
+    variants_us = np.zeros(5)
+    L.check(lib.fg_autotune(g.h, L.FG_MIXED, C.byref(chosen), L.ptr(variants_us), 5))
+    autotune = {"cg32_iteration_variants_us": [round(float(v), 2) for v in variants_us], "chosen": int(chosen.value),
+                "names": ["gather/256", "gather-hoist/256", "gather/128", "gather/512", "halo-smem"]}
     ms_spmv = C.c_double()
     L.check(lib.fg_bench_kernel(g.h, 0, L.FG_MIXED, 200, C.byref(ms_spmv)))
-    kernels_us = {"cg32_spmv": ms_spmv.value * 1e3}
-    for name, which, prec in (("cg32_update", 1, L.FG_MIXED), ("newton_assembly_f32", 2, L.FG_MIXED)):
+    kernels_us = {"cg32_iteration": ms_spmv.value * 1e3}
+    for name, which, prec in (("newton_assembly_f32", 2, L.FG_MIXED),):
         t = C.c_double()
         L.check(lib.fg_bench_kernel(g.h, which, prec, 20 if which == 2 else 200, C.byref(t)))
         kernels_us[name] = t.value * 1e3
     fg.newton_magnetostatics(mesh, nl, mu_lin, u0, precision="fp64")   # leaves J64 on the handle
+    ch64, us64 = C.c_int32(), np.zeros(2)
+    L.check(lib.fg_autotune(g.h, L.FG_FP64, C.byref(ch64), L.ptr(us64), 2))
+    autotune["cg64_spmv_variants_us"] = [round(float(v), 2) for v in us64]
+    autotune["chosen64"] = int(ch64.value)
     for name, which in (("cg64_spmv", 0), ("cg64_update", 1)):
         t = C.c_double()
         L.check(lib.fg_bench_kernel(g.h, which, L.FG_FP64, 200, C.byref(t)))
         kernels_us[name] = t.value * 1e3
     fg.newton_magnetostatics(mesh, nl, mu_lin, u0, precision="mixed")
     n = mesh.nv
-    alg_bytes = g.nnz * 8 + 16 * n       # values+columns, z/p gathers, pn/q writes (FP32)
+    # one fused FP32 CG iteration: matrix value (4 B) + 16-bit column (2 B) per stored
+    # nonzero; per row the (r, w, s, dinv) state read and written (16 + 16 B) and
+    # p, x read and written (8 + 8 B).  Neighbour-state gathers are re-reads.
+    alg_bytes = g.nnz * 6 + 48 * n
     achieved = alg_bytes / (ms_spmv.value * 1e-3) / 1e9
-    roofline = {"bound": "hbm", "kernel": "k_cg_spmv<float,float>", "achieved": achieved, "peak": peak,
+    kname = {4: "k_cg32_iter_halo"}.get(int(chosen.value), "k_cg32_iter")
+    roofline = {"bound": "hbm", "kernel": kname, "variant": autotune["names"][int(chosen.value)],
+                "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                 "traffic": args.spmv_traffic, "algorithmic_bytes": alg_bytes, "us_per_launch": ms_spmv.value * 1e3}
 

@@ -132,6 +132,13 @@ struct fg_mesh {
   int *sl_len = nullptr;     // nslices: groups of 4 slots per row in the slice
   int *sl_col = nullptr;     // nsell absolute column indices
   int16_t *sl_dcol = nullptr;// nsell column - row, when every |column - row| < 32768
+  // Halo staging: rows are taken in blocks of hrows (one CTA each); a block's distinct
+  // columns (its halo, sorted) are listed at halo_col[b * hcap ...], halo_len[b] of
+  // them, and every entry's column is also stored as its position in that list
+  // (sl_lcol), so a CTA gathers each needed vector entry once into shared memory.
+  int hrows = 0, hcap = 0, hmax = 0, nhblocks = 0;
+  int *halo_col = nullptr, *halo_len = nullptr;
+  uint16_t *sl_lcol = nullptr;
   bool use_dcol = false;
   int64_t nsell = 0;
   int maxrow4 = 0;           // longest row rounded up to a multiple of 4
@@ -175,8 +182,9 @@ struct fg_mesh {
   int *hint = nullptr;        // pinned host ints (16)
 
   GraphCache graph[4];
-  int spmv_variant32 = 0;     // FP32 CG SpMV variant chosen by the autotuner
-  bool tuned32 = false;
+  int spmv_variant32 = 0;     // FP32 CG iteration variant chosen by the autotuner
+  int spmv_variant64 = 0;     // FP64 CG SpMV variant chosen by the autotuner
+  bool tuned32 = false, tuned64 = false;
   std::vector<void *> extra;  // allocations released at destroy
 };
 
@@ -199,6 +207,8 @@ void fg_count_launch(long long n);
 
 void fg_check_flags(fg_mesh *m, const char *where);
 void fg_sync(fg_mesh *m);
+// Builds the halo lists and local column indices (needs sl_ptr/sl_len/sl_col, maxrow4).
+void fg_build_halo(fg_mesh *m);
 
 // assembly (fg_assemble.cu)
 enum AsmKind { ASM_STIFF = 0, ASM_MASS = 1, ASM_TANGENT = 2, ASM_HEAT = 3 };

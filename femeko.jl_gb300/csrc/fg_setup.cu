@@ -17,6 +17,7 @@
 //     4x4 (3x3) Vandermonde system per node instead (src/FEM3D.jl:5-17,
 //     src/FEM2D.jl:5-25); the coefficients are the same functions.
 #include <algorithm>
+#include <climits>
 #include <cstring>
 #include <mutex>
 
@@ -179,6 +180,133 @@ __global__ void k_row_fill(const int *__restrict__ iptr, const int *__restrict__
   }
   if (wide) atomicOr(flags + 1, 1);
   diagk[i] = (uint8_t)dk;
+}
+
+// Halo of a block of hrows rows: the sorted distinct columns of the block's entries
+// (pads included: they point at their own row), written to halo_col[b*cap ...], and
+// each entry's position in it (sl_lcol).  One CTA of 512 threads per block; the keys
+// are sorted in shared memory with a bitonic network (P2 = power of two >= keys).
+constexpr int FG_HALO_THREADS = 512;
+
+__global__ void __launch_bounds__(FG_HALO_THREADS)
+    k_build_halo(int64_t nv, int hrows, int slots, int P2, const int *__restrict__ sl_ptr,
+                 const int *__restrict__ sl_len, const int *__restrict__ sl_col, int cap, int *__restrict__ halo_col,
+                 int *__restrict__ halo_len, uint16_t *__restrict__ sl_lcol, int *flags) {
+  extern __shared__ int shk[];
+  int *key = shk;        // P2 sorted keys
+  int *uniq = shk + P2;  // distinct keys
+  __shared__ int wsum[FG_HALO_THREADS / 32];
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int64_t r0 = (int64_t)blockIdx.x * hrows;
+  const int nkeys = hrows * slots;
+  for (int e = tid; e < P2; e += nth) {
+    int k = INT_MAX;
+    if (e < nkeys) {
+      const int64_t row = r0 + e / slots;
+      const int q = e % slots;
+      if (row < nv) {
+        const int s = (int)(row / FG_SLICE), lane = (int)(row % FG_SLICE);
+        if (q < FG_GROUP * sl_len[s]) k = sl_col[sell_pos(sl_ptr[s], lane, q)];
+      }
+    }
+    key[e] = k;
+  }
+  __syncthreads();
+  for (int size = 2; size <= P2; size <<= 1)
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int e = tid; e < P2; e += nth) {
+        const int partner = e ^ stride;
+        if (partner > e) {
+          const bool up = ((e & size) == 0);
+          const int a = key[e], b = key[partner];
+          if ((a > b) == up) { key[e] = b; key[partner] = a; }
+        }
+      }
+      __syncthreads();
+    }
+  // distinct keys: each thread owns a contiguous chunk, counts, then a block scan
+  const int chunk = P2 / nth;  // P2 is a multiple of nth
+  const int e0 = tid * chunk;
+  int cnt = 0;
+  for (int e = e0; e < e0 + chunk; ++e)
+    if (key[e] != INT_MAX && (e == 0 || key[e] != key[e - 1])) ++cnt;
+  int incl = cnt;
+  for (int o = 1; o < 32; o <<= 1) {
+    int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if ((tid & 31) >= o) incl += v;
+  }
+  if ((tid & 31) == 31) wsum[tid >> 5] = incl;
+  __syncthreads();
+  if (tid < 32) {
+    int v = (tid < nth / 32) ? wsum[tid] : 0, w = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      int u = __shfl_up_sync(0xffffffffu, w, o);
+      if (tid >= o) w += u;
+    }
+    if (tid < nth / 32) wsum[tid] = w - v;  // exclusive warp offsets
+  }
+  __syncthreads();
+  int pos = wsum[tid >> 5] + incl - cnt;
+  for (int e = e0; e < e0 + chunk; ++e)
+    if (key[e] != INT_MAX && (e == 0 || key[e] != key[e - 1])) {
+      uniq[pos] = key[e];
+      halo_col[(int64_t)blockIdx.x * cap + pos] = key[e];
+      ++pos;
+    }
+  __shared__ int s_hl;
+  if (tid == nth - 1) s_hl = pos;  // the last chunk ends at the total count
+  __syncthreads();
+  const int hlen = s_hl;
+  if (tid == 0) {
+    halo_len[blockIdx.x] = hlen;
+    if (hlen > 65535) atomicOr(flags, FLAG_ROW_OVERFLOW);
+  }
+  // local index of every entry
+  for (int e = tid; e < nkeys; e += nth) {
+    const int64_t row = r0 + e / slots;
+    const int q = e % slots;
+    if (row >= nv) continue;
+    const int s = (int)(row / FG_SLICE), lane = (int)(row % FG_SLICE);
+    if (q >= FG_GROUP * sl_len[s]) continue;
+    const int64_t p = sell_pos(sl_ptr[s], lane, q);
+    const int c = sl_col[p];
+    int lo = 0, hi = hlen;
+    while (lo < hi) {
+      int mid = (lo + hi) >> 1;
+      if (uniq[mid] < c) lo = mid + 1; else hi = mid;
+    }
+    sl_lcol[p] = (uint16_t)lo;
+  }
+}
+
+void fg_build_halo(fg_mesh *m) {
+  const int slots = std::max(m->maxrow4, FG_GROUP);
+  // rows per CTA: the largest power of two in [32, 512] whose keys fit 8192 slots
+  int hrows = 512;
+  while (hrows > FG_SLICE && hrows * slots > 8192) hrows >>= 1;
+  const int nkeys = hrows * slots;
+  int P2 = FG_HALO_THREADS;
+  while (P2 < nkeys) P2 <<= 1;
+  FG_REQUIRE(P2 <= 16384, FG_BAD_MESH, "matrix rows too long for halo staging");
+  m->hrows = hrows;
+  m->hcap = nkeys;
+  m->nhblocks = (int)((m->nv + hrows - 1) / hrows);
+  m->halo_col = dev_alloc<int>(m, (size_t)m->nhblocks * m->hcap);
+  m->halo_len = dev_alloc<int>(m, (size_t)m->nhblocks);
+  m->sl_lcol = dev_alloc<uint16_t>(m, (size_t)m->nsell);
+  FG_CUDA_TRY(cudaMemsetAsync(m->sl_lcol, 0, sizeof(uint16_t) * (size_t)m->nsell, m->stream));
+  const size_t smem = 2 * (size_t)P2 * sizeof(int);
+  FG_CUDA_TRY(cudaFuncSetAttribute(k_build_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_build_halo<<<m->nhblocks, FG_HALO_THREADS, smem, m->stream>>>(m->nv, hrows, slots, P2, m->sl_ptr, m->sl_len,
+                                                                   m->sl_col, m->hcap, m->halo_col, m->halo_len,
+                                                                   m->sl_lcol, m->flags);
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(1);
+  std::vector<int> hl(m->nhblocks);
+  FG_CUDA_TRY(cudaMemcpyAsync(hl.data(), m->halo_len, sizeof(int) * m->nhblocks, cudaMemcpyDeviceToHost, m->stream));
+  fg_sync(m);
+  fg_check_flags(m, "halo staging");
+  m->hmax = *std::max_element(hl.begin(), hl.end());
 }
 
 // Incidence in SELL layout: record position per (element, local node) and the
@@ -438,6 +566,7 @@ extern "C" fg_status fg_mesh_create(const double *p, int64_t nv, const int32_t *
       fg_sync(m);
       m->use_dcol = (wide == 0);  // 16-bit column offsets when the bandwidth allows
     }
+    fg_build_halo(m);
     k_slots<<<grid_for(nv, 128), 128, 0, s>>>(iptr, inc, m->t, nt, npe, nv, m->rowptr, m->colidx, m->in_ptr,
                                               m->in_len, m->recpos, m->in_slot);
     FG_CUDA_TRY(cudaGetLastError());
@@ -456,7 +585,8 @@ extern "C" fg_status fg_mesh_create(const double *p, int64_t nv, const int32_t *
     cudaFree(inc);
 
     // control and reduction workspace
-    m->red.partials = dev_alloc<double>(m, ((size_t)grid_for(nv, 64) + FG_RED_BLOCKS) * 4);
+    // one slot of 4 per CTA of any row kernel (CTAs of 32 rows or more)
+    m->red.partials = dev_alloc<double>(m, ((size_t)grid_for(nv, FG_SLICE) + FG_RED_BLOCKS) * 4);
     m->red.counter = dev_alloc<unsigned int>(m, 128);   // two-level arrival counters
     FG_CUDA_TRY(cudaMemsetAsync(m->red.counter, 0, 128 * sizeof(unsigned int), s));
     m->scal = dev_alloc<double>(m, S_NSCAL);

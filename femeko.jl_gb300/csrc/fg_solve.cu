@@ -298,6 +298,71 @@ __global__ void __launch_bounds__(BS) k_cg32_iter(int64_t n, const int *__restri
   if (grid_finish<3>(part, partials, counter, tot)) cgcg_scalars(tot, scal, ictl);
 }
 
+// The same iteration with halo staging: the CTA first turns each distinct neighbour
+// state of its R rows into the new u once, into shared memory (coalesced loads of a
+// sorted column list), then every row reads its neighbours' u from shared memory
+// through 16-bit local indices.  R = rows per CTA (the halo block size).
+template <int R>
+__global__ void __launch_bounds__(R) k_cg32_iter_halo(int64_t n, const int *__restrict__ sl_ptr,
+                                                      const int *__restrict__ sl_len,
+                                                      const uint16_t *__restrict__ lcol,
+                                                      const float *__restrict__ val, const int *__restrict__ halo_col,
+                                                      const int *__restrict__ halo_len, int hcap,
+                                                      const float4 *__restrict__ st_in, float4 *__restrict__ st_out,
+                                                      float *__restrict__ p, float *__restrict__ x, double *scal,
+                                                      int *ictl, double *partials, unsigned *counter) {
+  extern __shared__ float us[];
+  if (ictl[I_DONE]) return;
+  const bool first = ictl[I_ITERS] < 0;
+  const float alpha = first ? 0.f : (float)scal[S_ALPHA];
+  const float beta = first ? 0.f : (float)scal[S_BETA];
+  {
+    const int hl = halo_len[blockIdx.x];
+    const int *hc = halo_col + (int64_t)blockIdx.x * hcap;
+    for (int h = threadIdx.x; h < hl; h += R) {
+      const float4 a = __ldg(st_in + __ldg(hc + h));
+      us[h] = a.w * fmaf(-alpha, fmaf(beta, a.z, a.y), a.x);
+    }
+  }
+  __syncthreads();
+  const int64_t i = (int64_t)blockIdx.x * R + threadIdx.x;
+  Acc<float> dots[3];
+  if (i < n) {
+    const int s = (int)(i >> 5), lane = (int)(i & 31);
+    const int64_t base = (int64_t)sl_ptr[s] + lane * FG_GROUP;
+    const int G = sl_len[s];
+    const float4 *v4 = reinterpret_cast<const float4 *>(val + base);
+    const ushort4 *c4 = reinterpret_cast<const ushort4 *>(lcol + base);
+    float acc = 0.f;
+#pragma unroll 4
+    for (int g = 0; g < G; ++g) {
+      const float4 vv = __ldg(v4 + (int64_t)g * FG_SLICE);
+      const ushort4 cc = __ldg(c4 + (int64_t)g * FG_SLICE);
+      acc = fmaf(vv.x, us[cc.x], acc);
+      acc = fmaf(vv.y, us[cc.y], acc);
+      acc = fmaf(vv.z, us[cc.z], acc);
+      acc = fmaf(vv.w, us[cc.w], acc);
+    }
+    const float4 o = __ldg(st_in + i);
+    const float snew = fmaf(beta, o.z, o.y);
+    const float rnew = fmaf(-alpha, snew, o.x);
+    const float unw = o.w * rnew;
+    if (!first) {
+      const float pnew = fmaf(beta, p[i], o.w * o.x);
+      p[i] = pnew;
+      x[i] = fmaf(alpha, pnew, x[i]);
+    }
+    st_out[i] = make_float4(rnew, acc, snew, o.w);
+    dots[0].add(rnew * unw);
+    dots[1].add(acc * unw);
+    dots[2].add(rnew * rnew);
+  }
+  double part[3];
+  block_sum_acc<3>(dots, part);
+  double tot[3];
+  if (grid_finish<3>(part, partials, counter, tot)) cgcg_scalars(tot, scal, ictl);
+}
+
 // r0 = scale * rin, state (r0, 0, 0, dinv) in both buffers, p = x = 0.  The threshold
 // tol2_rel becomes absolute (times r0.r0) in the first iteration.
 __global__ void k_cg32_init(int64_t n, int64_t np, const double *__restrict__ rin, double scale,
@@ -377,6 +442,55 @@ __global__ void __launch_bounds__(256) k_cg64_spmv(int64_t n, const int *__restr
       acc = fma(va.y, __ldg(u + CI::col(cc.y, i)), acc);
       acc = fma(vb.x, __ldg(u + CI::col(cc.z, i)), acc);
       acc = fma(vb.y, __ldg(u + CI::col(cc.w, i)), acc);
+    }
+    w[i] = acc;
+    const double ui = u[i], ri = r[i];
+    d3[0] = ri * ui;
+    d3[1] = acc * ui;
+    d3[2] = ri * ri;
+  }
+  __shared__ double shd[3][32];
+  block_sum<3>(d3, shd);
+  double tot[3];
+  if (grid_finish<3>(d3, partials, counter, tot)) cgcg_scalars(tot, scal, ictl);
+}
+
+// FP64 w = A u with halo staging of u (see k_cg32_iter_halo) and the dot products.
+template <int R>
+__global__ void __launch_bounds__(R) k_cg64_spmv_halo(int64_t n, const int *__restrict__ sl_ptr,
+                                                      const int *__restrict__ sl_len,
+                                                      const uint16_t *__restrict__ lcol,
+                                                      const double *__restrict__ val, const int *__restrict__ halo_col,
+                                                      const int *__restrict__ halo_len, int hcap,
+                                                      const double *__restrict__ u, const double *__restrict__ r,
+                                                      double *__restrict__ w, double *scal, int *ictl,
+                                                      double *partials, unsigned *counter) {
+  extern __shared__ double ud[];
+  if (ictl[I_DONE]) return;
+  {
+    const int hl = halo_len[blockIdx.x];
+    const int *hc = halo_col + (int64_t)blockIdx.x * hcap;
+    for (int h = threadIdx.x; h < hl; h += R) ud[h] = __ldg(u + __ldg(hc + h));
+  }
+  __syncthreads();
+  const int64_t i = (int64_t)blockIdx.x * R + threadIdx.x;
+  double d3[3] = {0.0, 0.0, 0.0};
+  if (i < n) {
+    const int s = (int)(i >> 5), lane = (int)(i & 31);
+    const int64_t base = (int64_t)sl_ptr[s] + lane * FG_GROUP;
+    const int G = sl_len[s];
+    const double2 *v2 = reinterpret_cast<const double2 *>(val + base);
+    const ushort4 *c4 = reinterpret_cast<const ushort4 *>(lcol + base);
+    double acc = 0.0;
+#pragma unroll 4
+    for (int g = 0; g < G; ++g) {
+      const double2 va = __ldg(v2 + (int64_t)g * 2 * FG_SLICE);
+      const double2 vb = __ldg(v2 + (int64_t)g * 2 * FG_SLICE + 1);
+      const ushort4 cc = __ldg(c4 + (int64_t)g * FG_SLICE);
+      acc = fma(va.x, ud[cc.x], acc);
+      acc = fma(va.y, ud[cc.y], acc);
+      acc = fma(vb.x, ud[cc.z], acc);
+      acc = fma(vb.y, ud[cc.w], acc);
     }
     w[i] = acc;
     const double ui = u[i], ri = r[i];
@@ -535,7 +649,8 @@ static void ensure_cg64(fg_mesh *m) {
 }
 
 // FP32 iteration variants (block size x load scheduling) for the autotuner.
-constexpr int FG_N_SPMV32 = 4;
+constexpr int FG_N_SPMV32 = 5;   // 0-3 direct gathers, 4 halo staging
+constexpr int FG_N_SPMV64 = 2;   // 0 direct gathers, 1 halo staging
 
 template <class CI>
 static void iter32_variant(fg_mesh *m, int v, const typename CI::T *col, const float4 *in, float4 *out) {
@@ -551,15 +666,51 @@ static void iter32_variant(fg_mesh *m, int v, const typename CI::T *col, const f
   }
 }
 
+// Launch of a halo kernel instantiated for the handle's rows per CTA.
+template <template <int> class K, class... Args>
+static void halo_launch(fg_mesh *m, size_t elem_bytes, Args... args) {
+  const size_t smem = (size_t)std::max(m->hmax, 1) * elem_bytes;
+  auto go = [&](auto kern, int R) {
+    if (smem > 48 * 1024)
+      FG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<m->nhblocks, R, smem, m->stream>>>(args...);
+  };
+  switch (m->hrows) {
+    case 512: go(K<512>::fn, 512); break;
+    case 256: go(K<256>::fn, 256); break;
+    case 128: go(K<128>::fn, 128); break;
+    case 64: go(K<64>::fn, 64); break;
+    default: go(K<32>::fn, 32); break;
+  }
+}
+template <int R>
+struct Iter32Halo {
+  static constexpr auto fn = k_cg32_iter_halo<R>;
+};
+template <int R>
+struct Spmv64Halo {
+  static constexpr auto fn = k_cg64_spmv_halo<R>;
+};
+
 static void launch_iter32(fg_mesh *m, int v, bool from_first_buffer) {
   const float4 *in = reinterpret_cast<const float4 *>(from_first_buffer ? m->v32[2] : m->v32[3]);
   float4 *out = reinterpret_cast<float4 *>(from_first_buffer ? m->v32[3] : m->v32[2]);
-  if (m->use_dcol) iter32_variant<ColRel>(m, v, m->sl_dcol, in, out);
+  if (v == 4)
+    halo_launch<Iter32Halo>(m, sizeof(float), m->nv, (const int *)m->sl_ptr, (const int *)m->sl_len,
+                            (const uint16_t *)m->sl_lcol, (const float *)m->val32, (const int *)m->halo_col,
+                            (const int *)m->halo_len, m->hcap, in, out, m->v32[1], m->v32[0], m->scal, m->ictl,
+                            m->red.partials, m->red.counter);
+  else if (m->use_dcol) iter32_variant<ColRel>(m, v, m->sl_dcol, in, out);
   else iter32_variant<ColAbs>(m, v, m->sl_col, in, out);
 }
 
 static void launch_spmv64cg(fg_mesh *m) {
-  if (m->use_dcol)
+  if (m->spmv_variant64 == 1)
+    halo_launch<Spmv64Halo>(m, sizeof(double), m->nv, (const int *)m->sl_ptr, (const int *)m->sl_len,
+                            (const uint16_t *)m->sl_lcol, (const double *)m->val64, (const int *)m->halo_col,
+                            (const int *)m->halo_len, m->hcap, (const double *)m->v64[2], (const double *)m->v64[1],
+                            m->v64[12], m->scal, m->ictl, m->red.partials, m->red.counter);
+  else if (m->use_dcol)
     k_cg64_spmv<ColRel><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, m->val64,
                                                             m->v64[2], m->v64[1], m->v64[12], m->scal, m->ictl,
                                                             m->red.partials, m->red.counter);
@@ -643,6 +794,7 @@ static int run_cg(fg_mesh *m, bool mixed, const fg_solve_opts &o, int *status) {
 }
 
 fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_variant);
+fg_status fg_autotune_spmv64(fg_mesh *m, int reps, int *chosen, double *us_per_variant);
 
 // Inner solve of A d = scale * r64 from d = 0 to relative residual `inner`, then
 // x += d / scale.  Returns iterations; *ist = 0 converged, 1 cap, 2 non-finite.
@@ -661,6 +813,7 @@ static int inner_solve(fg_mesh *m, bool mixed, const double *r64, double rn, dou
     k_axpy_to64<float><<<red_grid(m->nv), 256, 0, m->stream>>>(m->nv, rn, m->v32[0], d_x);
   } else {
     ensure_cg64(m);
+    if (!m->tuned64) fg_autotune_spmv64(m, 20, nullptr, nullptr);
     start_cg(m, false, r64, 1.0 / rn, inner * inner, maxit);
     its = run_cg(m, false, o, ist);
     k_axpy_to64<double><<<red_grid(m->nv), 256, 0, m->stream>>>(m->nv, rn, m->v64[0], d_x);
@@ -820,6 +973,11 @@ static fg_mesh *matrix_handle(int64_t n, const int64_t *colptr, const int64_t *r
     FG_CUDA_TRY(cudaMemsetAsync(m->flags, 0, 4 * sizeof(int), m->stream));
     FG_CUDA_TRY(cudaMallocHost(&m->hbuf, 64 * sizeof(double)));
     FG_CUDA_TRY(cudaMallocHost(&m->hint, 16 * sizeof(int)));
+    int64_t mr = 1;
+    for (int64_t r = 0; r < n; ++r) mr = std::max<int64_t>(mr, colptr[r + 1] - colptr[r]);
+    m->maxrow = (int)mr;
+    m->maxrow4 = (int)((mr + FG_GROUP - 1) / FG_GROUP * FG_GROUP);
+    if (m->maxrow4 <= 252) fg_build_halo(m);
     fg_sync(m);
   } catch (...) {
     fg_mesh_destroy(m);
@@ -918,6 +1076,10 @@ fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_v
   int best = 0;
   double best_us = 1e30;
   for (int v = 0; v < FG_N_SPMV32; ++v) {
+    if (v == 4 && !m->halo_col) {  // no halo lists for this operator
+      if (us_per_variant) us_per_variant[v] = 0.0;
+      continue;
+    }
     m->spmv_variant32 = v;
     timing_state(m, true);
     for (int r = 0; r < 2; ++r) launch_iter32(m, v, r == 1);
@@ -939,17 +1101,56 @@ fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_v
   return FG_OK;
 }
 
+// The same for the FP64 SpMV (direct gathers or halo staging).
+fg_status fg_autotune_spmv64(fg_mesh *m, int reps, int *chosen, double *us_per_variant) {
+  FG_REQUIRE(m->val64 != nullptr, FG_BAD_ARG, "autotune: no FP64 operator assembled");
+  reps = std::max(2, reps);
+  int best = 0;
+  double best_us = 1e30;
+  for (int v = 0; v < FG_N_SPMV64; ++v) {
+    if (v == 1 && !m->halo_col) {
+      if (us_per_variant) us_per_variant[v] = 0.0;
+      continue;
+    }
+    m->spmv_variant64 = v;
+    timing_state(m, false);
+    launch_spmv64cg(m);
+    FG_CUDA_TRY(cudaEventRecord(m->ev0, m->stream));
+    for (int r = 0; r < reps; ++r) launch_spmv64cg(m);
+    FG_CUDA_TRY(cudaEventRecord(m->ev1, m->stream));
+    FG_CUDA_TRY(cudaGetLastError());
+    FG_LAUNCHED(reps + 1);
+    fg_sync(m);
+    float ms = 0.f;
+    FG_CUDA_TRY(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
+    const double us = 1e3 * ms / reps;
+    if (us_per_variant) us_per_variant[v] = us;
+    if (us < best_us) { best_us = us; best = v; }
+  }
+  m->spmv_variant64 = best;
+  m->tuned64 = true;
+  if (m->graph[0].exec) { cudaGraphExecDestroy(m->graph[0].exec); m->graph[0].exec = nullptr; }
+  if (chosen) *chosen = best;
+  return FG_OK;
+}
+
 extern "C" fg_status fg_autotune(fg_mesh *m, int32_t precision, int32_t *variant, double *us_per_variant,
                                  int32_t n_slots) {
   return fg_guard([&]() -> fg_status {
     FG_REQUIRE(m != nullptr, FG_BAD_ARG, "fg_autotune: null handle");
-    FG_REQUIRE(precision == FG_MIXED, FG_UNSUPPORTED, "fg_autotune: FP32 operator variants only");
-    double us[FG_N_SPMV32];
-    int chosen = 0;
-    fg_status st = fg_autotune_spmv32(m, 50, &chosen, us);
+    double us[8] = {0};
+    int chosen = 0, nv = 0;
+    fg_status st;
+    if (precision == FG_MIXED) {
+      st = fg_autotune_spmv32(m, 50, &chosen, us);
+      nv = FG_N_SPMV32;
+    } else {
+      st = fg_autotune_spmv64(m, 50, &chosen, us);
+      nv = FG_N_SPMV64;
+    }
     if (variant) *variant = chosen;
     if (us_per_variant)
-      for (int v = 0; v < FG_N_SPMV32 && v < n_slots; ++v) us_per_variant[v] = us[v];
+      for (int v = 0; v < nv && v < n_slots; ++v) us_per_variant[v] = us[v];
     return st;
   });
 }
