@@ -365,8 +365,8 @@ def main():
     ap.add_argument("--cpu-cg-iters", type=int, default=100)
     ap.add_argument("--spmv-traffic", type=float, default=None,
                     help="DRAM bytes per SpMV launch from an ncu capture (reported as roofline.traffic)")
-    ap.add_argument("--ref-counts", type=int, nargs=3, default=[9, 9, 3900],
-                    help="(newton iterations, line-search trials, CG iterations) of the solve")
+    ap.add_argument("--ref-counts", type=int, nargs=3, default=[11, 39, 1324],
+                    help="(newton iterations, line-search trials, CG iterations) of the solve; default: the FP64 GPU solve at 96^3")
     args = ap.parse_args()
     if args.fp64_steps is None:
         args.fp64_steps = args.steps

@@ -964,7 +964,7 @@ static fg_mesh *matrix_handle(int64_t n, const int64_t *colptr, const int64_t *r
       FG_CUDA_TRY(cudaMemcpyAsync(m->val32, v32.data(), sizeof(float) * acc, cudaMemcpyHostToDevice, m->stream));
       FG_CUDA_TRY(cudaMemcpyAsync(m->dinv32, d32.data(), sizeof(float) * m->nvp, cudaMemcpyHostToDevice, m->stream));
     }
-    m->red.partials = dev_alloc<double>(m, ((size_t)grid_for(n, 64) + FG_RED_BLOCKS) * 4);
+    m->red.partials = dev_alloc<double>(m, ((size_t)grid_for(n, FG_SLICE) + FG_RED_BLOCKS) * 4);
     m->red.counter = dev_alloc<unsigned int>(m, 128);
     FG_CUDA_TRY(cudaMemsetAsync(m->red.counter, 0, 128 * sizeof(unsigned int), m->stream));
     m->scal = dev_alloc<double>(m, S_NSCAL);

@@ -51,10 +51,11 @@ enum {
   FG_LS_QUADRATIC = 3  /* true residual, next step from the minimiser of a quadratic fit
                           of |F(u + a du)|^2, kept in [0.1, 0.5] of the last step */
 };
-/* FP32 CG SpMV kernel: FG_SPMV_AUTO lets the autotuner time the variants on the
- * first mixed solve of a handle and keep the fastest; k = 1..4 forces variant k-1
- * (1: 4x-unrolled loop, 256 threads; 2: all row loads issued first, 256 threads;
- *  3: loop, 128 threads; 4: loop, 512 threads). */
+/* FP32 CG iteration kernel: FG_SPMV_AUTO lets the autotuner time the variants on
+ * the first mixed solve of a handle and keep the fastest; k = 1..5 forces variant
+ * k-1 (1: 4x-unrolled gather loop, 256 threads; 2: all row loads issued first, 256
+ * threads; 3: loop, 128 threads; 4: loop, 512 threads; 5: halo staging, the
+ * neighbour entries of a block of rows gathered once into shared memory). */
 enum { FG_SPMV_AUTO = 0 };
 
 typedef struct fg_mesh fg_mesh;
@@ -66,7 +67,7 @@ typedef struct fg_solve_opts {
   double inner_rtol;   /* mixed: FP32 PCG target per refinement step */
   int32_t check_every; /* iterations per graph launch between convergence checks (even) */
   int32_t use_graph;   /* 1: replay each block of iterations as a CUDA graph */
-  int32_t spmv;        /* FG_SPMV_AUTO or a forced variant 1..4 */
+  int32_t spmv;        /* FG_SPMV_AUTO or a forced variant 1..5 */
   int32_t reserved_;
 } fg_solve_opts;
 
@@ -204,8 +205,9 @@ int64_t fg_kernel_launches(void);
  * operator: which = 0 CG SpMV, 1 CG vector update, 2 Newton element pass + row
  * gather.  No reference counterpart (used for roofline reporting). */
 fg_status fg_bench_kernel(fg_mesh *m, int32_t which, int32_t precision, int32_t reps, double *ms_per_launch);
-/* Autotuner: times the FP32 CG SpMV variants on the handle's current FP32 operator
- * (assemble one first, e.g. by a mixed solve) and keeps the fastest for the handle.
+/* Autotuner: times the CG kernel variants of one precision on the handle's current
+ * operator (FG_MIXED: the 5 FP32 iteration variants; FG_FP64: direct gathers or halo
+ * staging for the SpMV; assemble one first, e.g. by a solve) and keeps the fastest.
  * variant receives the chosen index (0-based), us_per_variant (n_slots entries, may
  * be NULL) the measured microseconds per launch.  No reference counterpart. */
 fg_status fg_autotune(fg_mesh *m, int32_t precision, int32_t *variant, double *us_per_variant, int32_t n_slots);
