@@ -74,6 +74,7 @@ SIGNATURES = {
     "fg_local_stiffness": [_vp, _vp, _vp],
     "fg_cg_csc": [_i64, _vp, _vp, _vp, _i32, _vp, _vp, C.POINTER(SolveOpts), C.POINTER(SolveStats)],
     "fg_spmv_csc": [_i64, _vp, _vp, _vp, _i32, _vp, _vp],
+    "fg_cg_csc_noalloc": [_i64, _vp, _vp, _vp, _i32, _vp, _vp, C.POINTER(SolveOpts), _vp, C.POINTER(SolveStats)],
     "fg_magnetostatics_linear": [_vp, _vp, _vp, C.POINTER(SolveOpts), _vp, _vp, C.POINTER(SolveStats)],
     "fg_newton_magnetostatics": [_vp, _vp, _vp, _vp, C.POINTER(NewtonOpts), _vp, _vp, _vp, C.POINTER(NewtonStats)],
     "fg_hfield": [_vp, _vp, _vp],

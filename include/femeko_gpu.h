@@ -172,6 +172,25 @@ fg_status fg_cg_csc(int64_t n, const int64_t *colptr, const int64_t *rowval, con
 fg_status fg_spmv_csc(int64_t n, const int64_t *colptr, const int64_t *rowval, const double *nzval,
                       int32_t index_base, const double *x, double *y);
 
+/* The fg_cg_csc solve (FP64 Jacobi-PCG, stop at ||r|| <= rtol ||r0||) for a matrix
+ * and vectors already in DEVICE memory, allocating nothing: no cudaMalloc/cudaFree
+ * and no allocating library routine.  No counterpart in the reference.
+ * For callers that cannot allocate: a time loop re-solving a small system every
+ * step while other streams work (cudaMalloc/cudaFree may synchronise the device),
+ * or a process whose device memory is reserved by its own pool.
+ * Work space is one fixed scratch area per device inside the library:
+ * n <= FG_NOALLOC_MAX_ROWS rows (6 MiB of vectors); larger n returns FG_BAD_ARG.
+ * The first call on each device (with that device current) looks up the scratch
+ * address; make that first call before any stream capture.  Calls that overlap on
+ * one device would race on the shared scratch: a per-device host lock serialises
+ * them.  colptr/rowval/nzval/b/x are device (or managed) pointers; x holds the
+ * initial guess and receives the solution; stream may be NULL (default stream);
+ * o->precision must be FG_FP64 (o may be NULL: defaults); s->ms is host wall time. */
+#define FG_NOALLOC_MAX_ROWS ((int64_t)131072)
+fg_status fg_cg_csc_noalloc(int64_t n, const int64_t *colptr, const int64_t *rowval, const double *nzval,
+                            int32_t index_base, const double *b, double *x, const fg_solve_opts *o, void *stream,
+                            fg_solve_stats *s);
+
 /* Linear magnetostatics (Magnetostatics/magneticField.jl:89-132 and
  * Femeko_jl_C++/Magnetostatics/magnetostatics.cpp:49-95 scalarPotential) with the
  * Dirichlet rows set by fg_mesh_set_dirichlet: K(mu) u = 0 on free rows, u fixed
