@@ -242,10 +242,11 @@ def run_ours(args):
     lib.fg_mesh_layout(g.h, C.byref(nsell), C.byref(ninc), C.byref(nsl))
     fg.newton_magnetostatics(mesh, nl, mu_lin, u0, precision="mixed")   # leaves J32 on the handle
     chosen = C.c_int32()
-    variants_us = np.zeros(5)
-    L.check(lib.fg_autotune(g.h, L.FG_MIXED, C.byref(chosen), L.ptr(variants_us), 5))
+    variants_us = np.zeros(6)
+    L.check(lib.fg_autotune(g.h, L.FG_MIXED, C.byref(chosen), L.ptr(variants_us), 6))
     autotune = {"cg32_iteration_variants_us": [round(float(v), 2) for v in variants_us], "chosen": int(chosen.value),
-                "names": ["gather/256", "gather-hoist/256", "gather/128", "gather/512", "halo-smem"]}
+                "names": ["gather/256", "gather-hoist/256", "gather/128", "gather/512", "halo-smem",
+                          "halo-smem-pipelined"]}
     ms_spmv = C.c_double()
     L.check(lib.fg_bench_kernel(g.h, 0, L.FG_MIXED, 200, C.byref(ms_spmv)))
     kernels_us = {"cg32_iteration": ms_spmv.value * 1e3}
@@ -269,7 +270,7 @@ def run_ours(args):
     # p, x read and written (8 + 8 B).  Neighbour-state gathers are re-reads.
     alg_bytes = g.nnz * 6 + 48 * n
     achieved = alg_bytes / (ms_spmv.value * 1e-3) / 1e9
-    kname = {4: "k_cg32_iter_halo"}.get(int(chosen.value), "k_cg32_iter")
+    kname = {4: "k_cg32_iter_halo", 5: "k_cg32_iter_pipe"}.get(int(chosen.value), "k_cg32_iter")
     roofline = {"bound": "hbm", "kernel": kname, "variant": autotune["names"][int(chosen.value)],
                 "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,

@@ -455,6 +455,60 @@ __global__ void k_energy_tet4(int64_t nt, const double *__restrict__ geo, const 
   wout[k] = wd * geo[12 * nt + k];
 }
 
+// Objective of the adjoint: J = sum_T VE Hx / sum_T VE over the target elements, the
+// volume-weighted mean of Magnetostatics/NewtonRaphson.jl:234-240 with
+// Hx = -sum_a u_a dphi_a/dx (Magnetostatics/magneticField.jl:111-124).
+__global__ void k_objective_tet4(int64_t nt, const double *__restrict__ geo, const int *__restrict__ t,
+                                 const double *__restrict__ u, const uint8_t *__restrict__ target,
+                                 double *__restrict__ a_out, double *__restrict__ v_out) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt) return;
+  double a = 0.0, v = 0.0;
+  if (target[k]) {
+    double hx = 0.0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) hx = fma(-u[t[(int64_t)q * nt + k]], geo[(int64_t)(3 * q) * nt + k], hx);
+    v = geo[12 * nt + k];
+    a = v * hx;
+  }
+  a_out[k] = a;
+  v_out[k] = v;
+}
+
+// dJ/du_a = -sum_{T owns a} VE dphi_a/dx / vol as vector records (every element writes
+// its 4 records; zero outside the target).
+__global__ void k_objective_rhs_tet4(int64_t nt, const double *__restrict__ geo,
+                                     const uint8_t *__restrict__ target, double inv_vol,
+                                     const int *__restrict__ recpos, double *__restrict__ rec_r) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt) return;
+  const double s = target[k] ? -geo[12 * nt + k] * inv_vol : 0.0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) rec_r[recpos[(int64_t)q * nt + k]] = s * geo[(int64_t)(3 * q) * nt + k];
+}
+
+// dJ/dmu_k = -lambda^T (dK/dmu_k) u = -VE_k grad(lambda).grad(u); scale carries the
+// sign and the unit (mu0 for a gradient per relative permeability).
+__global__ void k_adjoint_grad_tet4(int64_t nt, const double *__restrict__ geo, const int *__restrict__ t,
+                                    const double *__restrict__ lam, const double *__restrict__ u, double scale,
+                                    double *__restrict__ grad) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt) return;
+  double gl[3] = {0.0, 0.0, 0.0}, gu[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int node = t[(int64_t)q * nt + k];
+    const double lq = lam[node], uq = u[node];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const double g = geo[(int64_t)(3 * q + c) * nt + k];
+      gl[c] = fma(lq, g, gl[c]);
+      gu[c] = fma(uq, g, gu[c]);
+    }
+  }
+  grad[k] = scale * geo[12 * nt + k] * (gl[0] * gu[0] + gl[1] * gu[1] + gl[2] * gu[2]);
+}
+
 // (K_e x_e)_a for the stiffness (coef * VE G G^T) or mass (coef VE/20 (1+delta)) or
 // both (heat: cm M + cs K).  Vector records only.
 __global__ void k_elem_apply_tet4(int kind, int64_t nt, const double *__restrict__ geo, const int *__restrict__ t,
@@ -732,6 +786,30 @@ void fg_energy_dev(fg_mesh *m, const double *d_u, double Ms, double Hk) {
 void fg_hfield_dev(fg_mesh *m, const double *d_u, double *d_H) {
   FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "H field needs P1 tetrahedra");
   k_hfield_tet4<<<grid_for(m->nt, 256), 256, 0, m->stream>>>(m->nt, m->geo, m->t, d_u, d_H);
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(1);
+}
+
+void fg_objective_parts_dev(fg_mesh *m, const double *d_u, const uint8_t *d_target, double *d_a, double *d_v) {
+  FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "objective needs P1 tetrahedra");
+  k_objective_tet4<<<grid_for(m->nt, 256), 256, 0, m->stream>>>(m->nt, m->geo, m->t, d_u, d_target, d_a, d_v);
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(1);
+}
+
+void fg_objective_rhs_dev(fg_mesh *m, const uint8_t *d_target, double vol, double *d_g) {
+  FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "objective needs P1 tetrahedra");
+  fg_ensure_records(m);
+  k_objective_rhs_tet4<<<grid_for(m->nt, 256), 256, 0, m->stream>>>(m->nt, m->geo, d_target, 1.0 / vol, m->recpos,
+                                                                     m->rec_r);
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(1);
+  launch_row<4, double, double>(m, nullptr, m->rec_r, 0, nullptr, nullptr, nullptr, nullptr, nullptr, d_g, 1.0, 1);
+}
+
+void fg_adjoint_grad_dev(fg_mesh *m, const double *d_lam, const double *d_u, double scale, double *d_grad) {
+  FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "adjoint gradient needs P1 tetrahedra");
+  k_adjoint_grad_tet4<<<grid_for(m->nt, 256), 256, 0, m->stream>>>(m->nt, m->geo, m->t, d_lam, d_u, scale, d_grad);
   FG_CUDA_TRY(cudaGetLastError());
   FG_LAUNCHED(1);
 }

@@ -81,7 +81,9 @@ enum {
   S_SCALE,     // mixed: scale applied to the FP64 residual before the FP32 solve
   S_NSCAL = 16
 };
-enum { I_DONE = 0, I_ITERS, I_MAXIT, I_STATUS, I_NINT = 8 };
+// CG control words; I_FAULT is set by a kernel whose asynchronous copy did not
+// complete within its bounded wait (the solve stops and reports an error).
+enum { I_DONE = 0, I_ITERS, I_MAXIT, I_STATUS, I_FAULT, I_NINT = 8 };
 
 // Reduction workspace: per-block partials and an arrival counter for the
 // "last block finishes the sum" pattern (the sum runs in block order, so results
@@ -137,6 +139,8 @@ struct fg_mesh {
   // them, and every entry's column is also stored as its position in that list
   // (sl_lcol), so a CTA gathers each needed vector entry once into shared memory.
   int hrows = 0, hcap = 0, hmax = 0, nhblocks = 0;
+  int tmax = 0;       // most matrix entries (padded slots) of one row block
+  int pipe_grid = 0;  // CTAs of the persistent pipelined iteration (0: not sized yet, -1: does not fit)
   int *halo_col = nullptr, *halo_len = nullptr;
   uint16_t *sl_lcol = nullptr;
   bool use_dcol = false;
@@ -168,6 +172,8 @@ struct fg_mesh {
   double *mu = nullptr, *dmu = nullptr, *H = nullptr, *wdens = nullptr;
   double *mu_lin = nullptr;
   uint8_t *nl = nullptr;
+  uint8_t *target = nullptr;  // nt objective mask (adjoint)
+  double *objbuf = nullptr;   // 2 x nt objective scratch (adjoint)
 
   // vectors
   double *v64[16] = {nullptr};
@@ -227,6 +233,13 @@ void fg_apply_operator_vec(fg_mesh *m, int kind, const double *d_coef, double c_
 void fg_hfield_dev(fg_mesh *m, const double *d_u, double *d_H);
 // Energy density integral times VE per element into m->wdens (from the potential).
 void fg_energy_dev(fg_mesh *m, const double *d_u, double Ms, double Hk);
+// Objective J = sum_T VE Hx / sum_T VE over the target elements: per-element parts
+// VE Hx and VE (zero outside the target) into d_a, d_v (nt each).
+void fg_objective_parts_dev(fg_mesh *m, const double *d_u, const uint8_t *d_target, double *d_a, double *d_v);
+// dJ/du (zero on Dirichlet rows) into d_g, for a target volume vol.
+void fg_objective_rhs_dev(fg_mesh *m, const uint8_t *d_target, double vol, double *d_g);
+// grad_k = scale VE_k grad(lambda).grad(u) per element.
+void fg_adjoint_grad_dev(fg_mesh *m, const double *d_lam, const double *d_u, double scale, double *d_grad);
 
 // solve (fg_solve.cu)
 double fg_norm2_dev(fg_mesh *m, const double *x, int64_t n, bool mask_fixed);

@@ -252,6 +252,100 @@ extern "C" fg_status fg_magnetostatics_linear(fg_mesh *m, const double *mu, cons
   });
 }
 
+// Adjoint sensitivity of J = volume-weighted mean Hx over the target elements with
+// respect to the per-element relative permeability.  Forward: the linear solve of
+// Magnetostatics/magneticField.jl:89-132 (nl == NULL) or the Newton solve of
+// Magnetostatics/NewtonRaphson.jl:109-214.  Adjoint: op lambda = dJ/du on the free
+// rows with op = K(mu) (linear) or the converged Newton Jacobian K(mu) + At (both
+// symmetric); then dJ/dmur_k = -mu0 VE_k grad(lambda).grad(u).  The element gradients
+// are recomputed from the stored geometry, not kept from the forward pass.
+extern "C" fg_status fg_adjoint_dJdmu(fg_mesh *m, const double *mur, const double *u0, const uint8_t *target,
+                                      const uint8_t *nl, const fg_newton_opts *o, double rtol, double *J,
+                                      double *grad, double *u, fg_adjoint_stats *s) {
+  return fg_guard([&]() -> fg_status {
+    FG_REQUIRE(m && mur && u0 && target && J && grad, FG_BAD_ARG, "fg_adjoint_dJdmu: null pointer");
+    FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "fg_adjoint_dJdmu: P1 tetrahedra only");
+    FG_REQUIRE(m->has_fixed, FG_BAD_ARG, "fg_adjoint_dJdmu: set Dirichlet nodes first (fg_mesh_set_dirichlet)");
+    FG_REQUIRE(rtol > 0.0, FG_BAD_ARG, "fg_adjoint_dJdmu: rtol must be positive");
+    fg_newton_opts opts;
+    fg_newton_opts_default(&opts);
+    if (o) opts = *o;
+    const bool mixed = opts.precision == FG_MIXED;
+    ensure_element_state(m);
+    const int64_t nt = m->nt, nv = m->nv;
+    if (!m->target) m->target = dev_alloc<uint8_t>(m, (size_t)nt);
+    if (!m->objbuf) m->objbuf = dev_alloc<double>(m, 2 * (size_t)nt);
+    upload(m, m->target, target, (size_t)nt);
+    upload(m, m->mu_lin, mur, sizeof(double) * (size_t)nt);
+    k_axpby64<<<grid_for(nt, 256), 256, 0, m->stream>>>(nt, FG_MU0, m->mu_lin, 0.0, m->mu_lin, m->mu_lin);
+    FG_LAUNCHED(1);
+    double *d_u = vec64(m, 7), *d_b = vec64(m, 9), *d_g = vec64(m, 13), *d_lam = vec64(m, 14);
+    upload(m, d_u, u0, sizeof(double) * (size_t)nv);
+    fg_solve_opts so;
+    fg_solve_opts_default(&so);
+    so.precision = opts.precision;
+    so.rtol = rtol;
+    so.maxiter = opts.cg_maxiter;
+    so.check_every = opts.check_every;
+    so.use_graph = opts.use_graph;
+    cudaEvent_t e0, e1, e2;
+    FG_CUDA_TRY(cudaEventCreate(&e0));
+    FG_CUDA_TRY(cudaEventCreate(&e1));
+    FG_CUDA_TRY(cudaEventCreate(&e2));
+    FG_CUDA_TRY(cudaEventRecord(e0, m->stream));
+    int fwd_iters = 0, newton_iters = 0, converged = 1;
+    if (!nl) {
+      fg_assemble_operator(m, ASM_STIFF, m->mu_lin, nullptr, nullptr, 0.0, 0.0, 0, OUT_SELL, true, mixed, true);
+      FG_CUDA_TRY(cudaMemsetAsync(d_b, 0, sizeof(double) * (size_t)nv, m->stream));
+      fg_solve_stats fs{};
+      converged = fg_pcg_solve(m, d_b, d_u, so, &fs, false) == 0;
+      fwd_iters = fs.iterations;
+    } else {
+      upload(m, m->nl, nl, (size_t)nt);
+      fg_newton_stats ns{};
+      converged = newton_dev(m, d_u, opts, &ns) == 0;
+      fwd_iters = ns.cg_iters;
+      newton_iters = ns.newton_iters;
+      // the Jacobian at the converged state: FP64 for the refinement residual, FP32
+      // for the inner solve when mixed
+      fg_newton_assemble(m, d_u, opts.Ms, opts.Hk, false, d_b, true, true);
+      if (mixed) fg_newton_assemble(m, d_u, opts.Ms, opts.Hk, true, d_b, true, true);
+    }
+    FG_CUDA_TRY(cudaEventRecord(e1, m->stream));
+    double *pa = m->objbuf, *pv = m->objbuf + nt;
+    fg_objective_parts_dev(m, d_u, m->target, pa, pv);
+    const double num = fg_dot_dev(m, pa, nullptr, nt, false);
+    const double vol = fg_dot_dev(m, pv, nullptr, nt, false);
+    FG_REQUIRE(vol > 0.0, FG_BAD_ARG, "fg_adjoint_dJdmu: the target selects no element");
+    *J = num / vol;
+    fg_objective_rhs_dev(m, m->target, vol, d_g);
+    FG_CUDA_TRY(cudaMemsetAsync(d_lam, 0, sizeof(double) * (size_t)nv, m->stream));
+    fg_solve_stats as{};
+    const bool adj_ok = fg_pcg_solve(m, d_g, d_lam, so, &as, false) == 0;
+    fg_adjoint_grad_dev(m, d_lam, d_u, -FG_MU0, pa);
+    FG_CUDA_TRY(cudaEventRecord(e2, m->stream));
+    download(m, grad, pa, sizeof(double) * (size_t)nt);
+    if (u) download(m, u, d_u, sizeof(double) * (size_t)nv);
+    fg_sync(m);
+    fg_check_flags(m, "fg_adjoint_dJdmu");
+    float f_ms = 0.f, a_ms = 0.f;
+    cudaEventElapsedTime(&f_ms, e0, e1);
+    cudaEventElapsedTime(&a_ms, e1, e2);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaEventDestroy(e2);
+    if (s) {
+      s->forward_iters = fwd_iters;
+      s->adjoint_iters = as.iterations;
+      s->newton_iters = newton_iters;
+      s->converged = (converged && adj_ok) ? 1 : 0;
+      s->forward_ms = f_ms;
+      s->adjoint_ms = a_ms;
+    }
+    return (converged && adj_ok) ? FG_OK : FG_NOT_CONVERGED;
+  });
+}
+
 extern "C" fg_status fg_hfield(fg_mesh *m, const double *u, double *H) {
   return fg_guard([&]() -> fg_status {
     FG_REQUIRE(m && u && H, FG_BAD_ARG, "fg_hfield: null pointer");

@@ -307,6 +307,16 @@ void fg_build_halo(fg_mesh *m) {
   fg_sync(m);
   fg_check_flags(m, "halo staging");
   m->hmax = *std::max_element(hl.begin(), hl.end());
+  // largest row block in matrix entries (the pipelined iteration stages one block)
+  std::vector<int> sp(m->nslices + 1);
+  FG_CUDA_TRY(cudaMemcpy(sp.data(), m->sl_ptr, sizeof(int) * (m->nslices + 1), cudaMemcpyDeviceToHost));
+  const int spt = hrows / FG_SLICE;
+  m->tmax = 0;
+  for (int b = 0; b < m->nhblocks; ++b) {
+    const int s0 = b * spt, s1 = std::min(s0 + spt, m->nslices);
+    m->tmax = std::max(m->tmax, sp[s1] - sp[s0]);
+  }
+  m->pipe_grid = 0;
 }
 
 // Incidence in SELL layout: record position per (element, local node) and the

@@ -32,6 +32,7 @@
 #include <cmath>
 #include <vector>
 
+#include "fg_async.cuh"
 #include "fg_common.cuh"
 // ------------------------------------------------------------------ reductions
 struct ff {
@@ -363,6 +364,173 @@ __global__ void __launch_bounds__(R) k_cg32_iter_halo(int64_t n, const int *__re
   if (grid_finish<3>(part, partials, counter, tot)) cgcg_scalars(tot, scal, ictl);
 }
 
+// The halo iteration as a persistent, software-pipelined kernel.  Each CTA walks the
+// row blocks (tiles) b = blockIdx.x, blockIdx.x + gridDim.x, ... with two shared-memory
+// stages: while tile k is computed, tile k+1's neighbour states are in flight
+// (16-byte cp.async gathers) and tile k+2's halo list, matrix values and local
+// column indices are in flight as bulk copies (cp.async.bulk completing on an
+// mbarrier).  So the loads of the next tiles overlap the current one instead of
+// waiting on each dependent gather.  Dots accumulate over the CTA's tiles and are
+// reduced once at the end.
+struct PipeArgs {
+  int64_t n;
+  int ntiles, nslices, hcap;
+  int HM, TM;  // halo entries and matrix entries per stage (capacities)
+  const int *sl_ptr, *sl_len, *halo_col, *halo_len;
+  const uint16_t *lcol;
+  const float *val;
+};
+
+__host__ __device__ __forceinline__ size_t pipe_align(size_t b) { return (b + 127) & ~(size_t)127; }
+// stage layout: halo columns (int), halo states (float4), halo u (float), values, columns
+__host__ __device__ __forceinline__ size_t pipe_stage_bytes(int HM, int TM) {
+  return pipe_align((size_t)HM * 4) + pipe_align((size_t)HM * 16) + pipe_align((size_t)HM * 4) +
+         pipe_align((size_t)TM * 4) + pipe_align((size_t)TM * 2);
+}
+
+template <int R>
+__global__ void __launch_bounds__(R) k_cg32_iter_pipe(PipeArgs a, const float4 *__restrict__ st_in,
+                                                      float4 *__restrict__ st_out, float *__restrict__ p,
+                                                      float *__restrict__ x, double *scal, int *ictl,
+                                                      double *partials, unsigned *counter) {
+  extern __shared__ __align__(128) unsigned char sm_pipe[];
+  __shared__ __align__(8) uint64_t bar[2];
+  if (ictl[I_DONE]) return;
+  const bool first = ictl[I_ITERS] < 0;
+  const float alpha = first ? 0.f : (float)scal[S_ALPHA];
+  const float beta = first ? 0.f : (float)scal[S_BETA];
+  const int tid = threadIdx.x;
+  const size_t o_hst = pipe_align((size_t)a.HM * 4), o_u = o_hst + pipe_align((size_t)a.HM * 16);
+  const size_t o_val = o_u + pipe_align((size_t)a.HM * 4), o_col = o_val + pipe_align((size_t)a.TM * 4);
+  const size_t stage = pipe_stage_bytes(a.HM, a.TM);
+  auto hidx = [&](int s) { return reinterpret_cast<int *>(sm_pipe + s * stage); };
+  auto hst = [&](int s) { return reinterpret_cast<float4 *>(sm_pipe + s * stage + o_hst); };
+  auto uh = [&](int s) { return reinterpret_cast<float *>(sm_pipe + s * stage + o_u); };
+  auto vals = [&](int s) { return reinterpret_cast<const float *>(sm_pipe + s * stage + o_val); };
+  auto cols = [&](int s) { return reinterpret_cast<const uint16_t *>(sm_pipe + s * stage + o_col); };
+  constexpr int SPT = R / FG_SLICE;  // slices per tile
+  const int K = (a.ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+  auto tile_of = [&](int k) { return (int)blockIdx.x + k * (int)gridDim.x; };
+
+  // thread 0: bulk copies of a tile's halo list, values and local columns into stage s
+  auto issue_bulk = [&](int tile, int s) {
+    const int s0 = tile * SPT, s1 = min(s0 + SPT, a.nslices);
+    const int e0 = a.sl_ptr[s0], e1 = a.sl_ptr[s1];
+    const uint32_t hb = (uint32_t)((a.halo_len[tile] * 4 + 15) & ~15);
+    const uint32_t vb = (uint32_t)(e1 - e0) * 4u, cb = (uint32_t)(e1 - e0) * 2u;
+    fence_proxy_async_smem();
+    mbar_arrive_expect_tx(&bar[s], hb + vb + cb);
+    bulk_g2s(hidx(s), a.halo_col + (int64_t)tile * a.hcap, hb, &bar[s]);
+    bulk_g2s(sm_pipe + s * stage + o_val, a.val + e0, vb, &bar[s]);
+    bulk_g2s(sm_pipe + s * stage + o_col, a.lcol + e0, cb, &bar[s]);
+  };
+  // all threads: 16-byte gathers of the tile's neighbour states into stage s
+  auto issue_gather = [&](int tile, int s) {
+    const int hl = a.halo_len[tile];
+    const int *hi = hidx(s);
+    float4 *dst = hst(s);
+    for (int h = tid; h < hl; h += R) cp_async16(dst + h, st_in + hi[h]);
+    cp_async_commit();
+  };
+
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_proxy_async_smem();
+  }
+  __syncthreads();
+  uint32_t phases = 0u;  // bit s: parity of stage s's next barrier phase
+  bool ok = true;
+  if (tid == 0) {
+    issue_bulk(tile_of(0), 0);
+    if (K > 1) issue_bulk(tile_of(1), 1);
+  }
+  ok = mbar_wait(&bar[0], 0u);
+  phases ^= 1u;
+  if (__syncthreads_or(!ok)) ok = false;
+  if (ok) issue_gather(tile_of(0), 0);
+
+  Acc<float> dots[3];
+  for (int k = 0; k < K && ok; ++k) {
+    const int s = k & 1, tile = tile_of(k);
+    const int64_t i = (int64_t)tile * R + tid;
+    // own row: issued before the waits so that they overlap them
+    float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+    float pi = 0.f, xi = 0.f;
+    int G = 0, base = 0;
+    const bool row = i < a.n;
+    if (row) {
+      o = __ldg(st_in + i);
+      if (!first) { pi = p[i]; xi = x[i]; }
+      const int sl = (int)(i >> 5);
+      G = a.sl_len[sl];
+      base = a.sl_ptr[sl] - a.sl_ptr[tile * SPT] + (int)(i & 31) * FG_GROUP;
+    }
+    const int hl = a.halo_len[tile];
+    cp_async_wait_all();
+    __syncthreads();
+    {
+      const float4 *hs = hst(s);
+      float *u = uh(s);
+      for (int h = tid; h < hl; h += R) {
+        const float4 q = hs[h];
+        u[h] = q.w * fmaf(-alpha, fmaf(beta, q.z, q.y), q.x);
+      }
+    }
+    if (k + 1 < K) {
+      const int s1 = s ^ 1;
+      const bool got = mbar_wait(&bar[s1], (phases >> s1) & 1u);
+      phases ^= 1u << s1;
+      if (__syncthreads_or(!got)) { ok = false; break; }
+      issue_gather(tile_of(k + 1), s1);
+    }
+    __syncthreads();
+    if (row) {
+      const float *v = vals(s);
+      const uint16_t *c = cols(s);
+      const float *u = uh(s);
+      float acc = 0.f;
+#pragma unroll 4
+      for (int g = 0; g < G; ++g) {
+        const float4 vv = *reinterpret_cast<const float4 *>(v + base + g * FG_SLICE * FG_GROUP);
+        const ushort4 cc = *reinterpret_cast<const ushort4 *>(c + base + g * FG_SLICE * FG_GROUP);
+        acc = fmaf(vv.x, u[cc.x], acc);
+        acc = fmaf(vv.y, u[cc.y], acc);
+        acc = fmaf(vv.z, u[cc.z], acc);
+        acc = fmaf(vv.w, u[cc.w], acc);
+      }
+      const float snew = fmaf(beta, o.z, o.y);
+      const float rnew = fmaf(-alpha, snew, o.x);
+      const float unw = o.w * rnew;
+      if (!first) {
+        const float pnew = fmaf(beta, pi, o.w * o.x);
+        p[i] = pnew;
+        x[i] = fmaf(alpha, pnew, xi);
+      }
+      st_out[i] = make_float4(rnew, acc, snew, o.w);
+      dots[0].add(rnew * unw);
+      dots[1].add(acc * unw);
+      dots[2].add(rnew * rnew);
+    }
+    __syncthreads();
+    if (k + 2 < K && tid == 0) issue_bulk(tile_of(k + 2), s);
+  }
+  if (!ok) {
+    // a bulk copy did not arrive: report, drain what is in flight (bounded), stop the CG
+    cp_async_wait_all();
+    mbar_wait(&bar[0], phases & 1u, 1 << 20);
+    mbar_wait(&bar[1], (phases >> 1) & 1u, 1 << 20);
+    if (tid == 0) {
+      atomicExch(ictl + I_FAULT, 1);
+      atomicExch(ictl + I_DONE, 1);
+    }
+  }
+  double part[3];
+  block_sum_acc<3>(dots, part);
+  double tot[3];
+  if (grid_finish<3>(part, partials, counter, tot) && ok) cgcg_scalars(tot, scal, ictl);
+}
+
 // r0 = scale * rin, state (r0, 0, 0, dinv) in both buffers, p = x = 0.  The threshold
 // tol2_rel becomes absolute (times r0.r0) in the first iteration.
 __global__ void k_cg32_init(int64_t n, int64_t np, const double *__restrict__ rin, double scale,
@@ -385,6 +553,7 @@ __global__ void k_cg32_init(int64_t n, int64_t np, const double *__restrict__ ri
     ictl[I_ITERS] = -1;
     ictl[I_MAXIT] = maxit;
     ictl[I_STATUS] = 0;
+    ictl[I_FAULT] = 0;
     ictl[I_DONE] = 0;
   }
 }
@@ -525,6 +694,7 @@ __global__ void k_cg64_init(int64_t n, int64_t np, const double *__restrict__ ri
     ictl[I_ITERS] = -1;
     ictl[I_MAXIT] = maxit;
     ictl[I_STATUS] = 0;
+    ictl[I_FAULT] = 0;
     ictl[I_DONE] = 0;
   }
 }
@@ -649,7 +819,7 @@ static void ensure_cg64(fg_mesh *m) {
 }
 
 // FP32 iteration variants (block size x load scheduling) for the autotuner.
-constexpr int FG_N_SPMV32 = 5;   // 0-3 direct gathers, 4 halo staging
+constexpr int FG_N_SPMV32 = 6;   // 0-3 direct gathers, 4 halo staging, 5 pipelined halo staging
 constexpr int FG_N_SPMV64 = 2;   // 0 direct gathers, 1 halo staging
 
 template <class CI>
@@ -692,10 +862,74 @@ struct Spmv64Halo {
   static constexpr auto fn = k_cg64_spmv_halo<R>;
 };
 
+template <int R>
+struct Iter32Pipe {
+  static constexpr auto fn = k_cg32_iter_pipe<R>;
+};
+
+// Persistent pipelined iteration: two stages of shared memory per CTA, as many CTAs
+// as fit on the GPU at once (never more than there are row blocks).  Sized on first
+// use; pipe_grid = -1 when one CTA's stages do not fit in shared memory.
+static bool pipe_available(fg_mesh *m) {
+  if (!m->halo_col) return false;
+  if (m->pipe_grid != 0) return m->pipe_grid > 0;
+  const int HM = (m->hmax + 3) & ~3;
+  const size_t smem = 2 * pipe_stage_bytes(HM, m->tmax);
+  int dev_max = 0;
+  FG_CUDA_TRY(cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, m->device));
+  if (smem + 4096 > (size_t)dev_max) { m->pipe_grid = -1; return false; }
+  int per_sm = 0;
+  auto size = [&](auto kern, int R) {
+    FG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    FG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, R, smem));
+  };
+  switch (m->hrows) {
+    case 512: size(Iter32Pipe<512>::fn, 512); break;
+    case 256: size(Iter32Pipe<256>::fn, 256); break;
+    case 128: size(Iter32Pipe<128>::fn, 128); break;
+    case 64: size(Iter32Pipe<64>::fn, 64); break;
+    default: size(Iter32Pipe<32>::fn, 32); break;
+  }
+  if (per_sm < 1) { m->pipe_grid = -1; return false; }
+  m->pipe_grid = std::min(m->nhblocks, per_sm * std::max(m->sm_count, 1));
+  return true;
+}
+
+static void pipe_launch32(fg_mesh *m, const float4 *in, float4 *out) {
+  PipeArgs a;
+  a.n = m->nv;
+  a.ntiles = m->nhblocks;
+  a.nslices = m->nslices;
+  a.hcap = m->hcap;
+  a.HM = (m->hmax + 3) & ~3;
+  a.TM = m->tmax;
+  a.sl_ptr = m->sl_ptr;
+  a.sl_len = m->sl_len;
+  a.halo_col = m->halo_col;
+  a.halo_len = m->halo_len;
+  a.lcol = m->sl_lcol;
+  a.val = m->val32;
+  const size_t smem = 2 * pipe_stage_bytes(a.HM, a.TM);
+  auto go = [&](auto kern, int R) {
+    FG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<m->pipe_grid, R, smem, m->stream>>>(a, in, out, m->v32[1], m->v32[0], m->scal, m->ictl, m->red.partials,
+                                                m->red.counter);
+  };
+  switch (m->hrows) {
+    case 512: go(Iter32Pipe<512>::fn, 512); break;
+    case 256: go(Iter32Pipe<256>::fn, 256); break;
+    case 128: go(Iter32Pipe<128>::fn, 128); break;
+    case 64: go(Iter32Pipe<64>::fn, 64); break;
+    default: go(Iter32Pipe<32>::fn, 32); break;
+  }
+}
+
 static void launch_iter32(fg_mesh *m, int v, bool from_first_buffer) {
   const float4 *in = reinterpret_cast<const float4 *>(from_first_buffer ? m->v32[2] : m->v32[3]);
   float4 *out = reinterpret_cast<float4 *>(from_first_buffer ? m->v32[3] : m->v32[2]);
-  if (v == 4)
+  if (v == 5 && pipe_available(m))
+    pipe_launch32(m, in, out);
+  else if (v >= 4)
     halo_launch<Iter32Halo>(m, sizeof(float), m->nv, (const int *)m->sl_ptr, (const int *)m->sl_len,
                             (const uint16_t *)m->sl_lcol, (const float *)m->val32, (const int *)m->halo_col,
                             (const int *)m->halo_len, m->hcap, in, out, m->v32[1], m->v32[0], m->scal, m->ictl,
@@ -752,9 +986,10 @@ static int run_cg(fg_mesh *m, bool mixed, const fg_solve_opts &o, int *status) {
   if (block & 1) ++block;
   const int per_iter = mixed ? 1 : 2;
   GraphCache &gc = m->graph[mixed ? 1 : 0];
-  const void *key[4] = {mixed ? (const void *)m->val32 : (const void *)m->val64,
+  const void *key[5] = {mixed ? (const void *)m->val32 : (const void *)m->val64,
                         mixed ? (const void *)(intptr_t)(m->spmv_variant32 + 1) : (const void *)m->v64[0],
-                        (const void *)(intptr_t)block, (const void *)(intptr_t)m->use_dcol};
+                        (const void *)(intptr_t)block, (const void *)(intptr_t)m->use_dcol,
+                        (const void *)(intptr_t)(mixed ? 0 : m->spmv_variant64 + 1)};
   const bool use_graph = o.use_graph != 0;
   auto enqueue_block = [&]() {
     for (int it = 0; it < block; ++it) {
@@ -764,7 +999,7 @@ static int run_cg(fg_mesh *m, bool mixed, const fg_solve_opts &o, int *status) {
   };
   if (use_graph) {
     bool match = gc.exec && gc.iters == block;
-    for (int j = 0; j < 4 && match; ++j) match = (gc.key[j] == key[j]);
+    for (int j = 0; j < 5 && match; ++j) match = (gc.key[j] == key[j]);
     if (!match) {
       if (gc.exec) { cudaGraphExecDestroy(gc.exec); gc.exec = nullptr; }
       cudaGraph_t graph;
@@ -774,12 +1009,13 @@ static int run_cg(fg_mesh *m, bool mixed, const fg_solve_opts &o, int *status) {
       FG_CUDA_TRY(cudaGraphInstantiate(&gc.exec, graph, 0));
       cudaGraphDestroy(graph);
       gc.iters = block;
-      for (int j = 0; j < 4; ++j) gc.key[j] = key[j];
+      for (int j = 0; j < 5; ++j) gc.key[j] = key[j];
     }
   }
   for (;;) {
-    FG_CUDA_TRY(cudaMemcpyAsync(m->hint, m->ictl, sizeof(int) * 4, cudaMemcpyDeviceToHost, m->stream));
+    FG_CUDA_TRY(cudaMemcpyAsync(m->hint, m->ictl, sizeof(int) * 5, cudaMemcpyDeviceToHost, m->stream));
     fg_sync(m);
+    FG_REQUIRE(m->hint[I_FAULT] == 0, FG_CUDA, "CG kernel: an asynchronous shared-memory copy did not complete");
     if (m->hint[I_DONE]) break;
     if (use_graph) {
       FG_CUDA_TRY(cudaGraphLaunch(gc.exec, m->stream));
@@ -804,7 +1040,11 @@ static int inner_solve(fg_mesh *m, bool mixed, const double *r64, double rn, dou
   if (mixed) {
     ensure_cg32(m);
     if (o.spmv > 0 && o.spmv <= FG_N_SPMV32) {
-      m->spmv_variant32 = o.spmv - 1;
+      // a forced variant that this operator cannot run (no halo lists, stages too
+      // large for shared memory) falls back to the plain gather kernel
+      const int v = o.spmv - 1;
+      const bool avail = v < 4 || (v == 4 && m->halo_col) || (v == 5 && pipe_available(m));
+      m->spmv_variant32 = avail ? v : 0;
     } else if (!m->tuned32) {
       fg_autotune_spmv32(m, 20, nullptr, nullptr);
     }
@@ -1076,7 +1316,7 @@ fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_v
   int best = 0;
   double best_us = 1e30;
   for (int v = 0; v < FG_N_SPMV32; ++v) {
-    if (v == 4 && !m->halo_col) {  // no halo lists for this operator
+    if ((v == 4 && !m->halo_col) || (v == 5 && !pipe_available(m))) {  // not available for this operator
       if (us_per_variant) us_per_variant[v] = 0.0;
       continue;
     }

@@ -19,6 +19,8 @@ cg(A, b)                        IterativeSolvers.cg (e.g. run.jl:141)          n
 magnetostatics_linear           Magnetostatics/magneticField.jl:89-132         (u, H, stats)
 newton_magnetostatics           Magnetostatics/NewtonRaphson.jl:109-214        (u, H, mu, stats)
 hfield(mesh, u)                 Magnetostatics/magneticField.jl:111-124        (3, nt) ndarray
+heat_be                         Heat/heat3D.jl:50-90                           (T, snapshots, stats)
+adjoint_dJdmu                   (none: gradient of NewtonRaphson.jl:234-240)   (J, grad, u, stats)
 ==============================  =============================================  ==========================
 
 The mesh argument is a :class:`femeko_gpu.mesh.MESH` (the reference struct's fields).
@@ -39,7 +41,7 @@ __all__ = [
     "GPUMesh", "gpu_mesh", "stiffnessMatrix", "localStiffnessMatrix", "tangentialStiffnessMatrix", "massMatrix",
     "stiffnessMatrix2D", "massMatrix2D", "quadraticStiffnessMatrix", "quadraticMassMatrix",
     "quadraticStiffnessMatrix2D", "quadraticMassMatrix2D", "cg", "spmv", "magnetostatics_linear",
-    "newton_magnetostatics", "hfield", "solve_opts", "newton_opts", "MESH", "MU0", "box_tet_mesh", "box_tri_mesh",
+    "newton_magnetostatics", "hfield", "heat_be", "adjoint_dJdmu", "solve_opts", "newton_opts", "MESH", "MU0", "box_tet_mesh", "box_tri_mesh",
 ]
 
 
@@ -228,6 +230,39 @@ def newton_magnetostatics(mesh: MESH, nl, mu_lin, u0, **kw):
                                           C.byref(s))
     L.check(st, allow_not_converged=True)
     return u, H.reshape(mesh.nt, 3).T, mu, L.stats_dict(s)
+
+
+def heat_be(mesh: MESH, T0, kappa, rho_c=1.0, dt=1e-3, nsteps=100, every=10, precision="fp64", rtol=1e-10, **kw):
+    """Backward-Euler heat steps (Heat/heat3D.jl:50-90) with T = 0 on the Dirichlet
+    nodes; returns (T_final, snapshots every `every` steps, stats)."""
+    g = gpu_mesh(mesh)
+    T = _c(T0, np.float64).copy()
+    nsnap = nsteps // every if every > 0 else 0
+    snaps = np.zeros((max(nsnap, 1), mesh.nv))
+    o = solve_opts(precision=precision, rtol=rtol, **kw)
+    s = L.SolveStats()
+    st = L.lib().fg_heat_be(g.h, L.ptr(_c(kappa, np.float64)), rho_c, dt, nsteps, L.ptr(T), every,
+                            L.ptr(snaps) if nsnap else None, C.byref(o), C.byref(s))
+    L.check(st, allow_not_converged=True)
+    return T, snaps[:nsnap], L.stats_dict(s)
+
+
+def adjoint_dJdmu(mesh: MESH, mur, u0, target, nl=None, rtol=1e-12, **kw):
+    """J = volume-weighted mean Hx over the target elements and dJ/dmur per element
+    through the GPU adjoint; nl = None solves the linear problem, else the Newton one.
+    Returns (J, grad, u, stats)."""
+    g = gpu_mesh(mesh)
+    grad = np.zeros(mesh.nt)
+    u = np.zeros(mesh.nv)
+    J = C.c_double()
+    o = newton_opts(**kw)
+    s = L.AdjointStats()
+    nlp = None if nl is None else L.ptr(_c(nl, np.uint8))
+    st = L.lib().fg_adjoint_dJdmu(g.h, L.ptr(_c(mur, np.float64)), L.ptr(_c(u0, np.float64)),
+                                  L.ptr(_c(target, np.uint8)), nlp, C.byref(o), rtol, C.byref(J), L.ptr(grad),
+                                  L.ptr(u), C.byref(s))
+    L.check(st, allow_not_converged=True)
+    return J.value, grad, u, L.stats_dict(s)
 
 
 def hfield(mesh: MESH, u):

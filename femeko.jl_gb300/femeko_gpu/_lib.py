@@ -50,6 +50,11 @@ class NewtonStats(C.Structure):
                 ("alpha", C.c_double), ("energy", C.c_double), ("ms", C.c_double)]
 
 
+class AdjointStats(C.Structure):
+    _fields_ = [("forward_iters", C.c_int32), ("adjoint_iters", C.c_int32), ("newton_iters", C.c_int32),
+                ("converged", C.c_int32), ("forward_ms", C.c_double), ("adjoint_ms", C.c_double)]
+
+
 def stats_dict(s) -> dict:
     return {name: getattr(s, name) for name, _ in s._fields_ if name != "pad_"}
 
@@ -78,6 +83,9 @@ SIGNATURES = {
     "fg_magnetostatics_linear": [_vp, _vp, _vp, C.POINTER(SolveOpts), _vp, _vp, C.POINTER(SolveStats)],
     "fg_newton_magnetostatics": [_vp, _vp, _vp, _vp, C.POINTER(NewtonOpts), _vp, _vp, _vp, C.POINTER(NewtonStats)],
     "fg_hfield": [_vp, _vp, _vp],
+    "fg_heat_be": [_vp, _vp, _d, _d, _i32, _vp, _i32, _vp, C.POINTER(SolveOpts), C.POINTER(SolveStats)],
+    "fg_adjoint_dJdmu": [_vp, _vp, _vp, _vp, _vp, C.POINTER(NewtonOpts), _d, C.POINTER(_d), _vp, _vp,
+                         C.POINTER(AdjointStats)],
     "fg_scalar_potential_newton": [_vp, _i64, _vp, _i64, _i32, _vp, _vp, _vp, _vp, C.POINTER(NewtonOpts), _vp, _vp,
                                    _vp, C.POINTER(NewtonStats)],
     "fg_bench_kernel": [_vp, _i32, _i32, _i32, C.POINTER(_d)],

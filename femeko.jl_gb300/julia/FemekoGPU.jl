@@ -218,16 +218,35 @@ function newton_magnetostatics(mesh, fixed::Vector{UInt8}, nl::Vector{UInt8}, mu
 end
 
 # ---------------------------------------------------------------- differentiation
-"""mean_Hx(mesh, mur, fixed, u0, target) -- volume-weighted mean H_x over the target
-elements of the linear magnetostatic solution with relative permeability mur."""
-function mean_Hx(mesh, mur::Vector{Float64}, fixed::Vector{UInt8}, u0::Vector{Float64}, target::Vector{UInt8})
+struct AdjointStats
+    forward_iters::Int32
+    adjoint_iters::Int32
+    newton_iters::Int32
+    converged::Int32
+    forward_ms::Float64
+    adjoint_ms::Float64
+end
+
+"""mean_Hx(mesh, mur, fixed, u0, target; nl=nothing, precision=:mixed, rtol=1e-12) --
+volume-weighted mean H_x over the target elements (Magnetostatics/NewtonRaphson.jl:234-240)
+of the magnetostatic solution with relative permeability mur, and its gradient dJ/dmur
+from the GPU adjoint.  nl === nothing: linear problem; else the Newton problem with
+Froehlich elements nl[k] != 0."""
+function mean_Hx(mesh, mur::Vector{Float64}, fixed::Vector{UInt8}, u0::Vector{Float64}, target::Vector{UInt8};
+                 nl::Union{Nothing,Vector{UInt8}}=nothing, precision::Symbol=:mixed, rtol=1e-12)
     g = gpu(mesh)
     set_dirichlet!(g, fixed)
     J = Ref{Float64}(0.0)
     grad = zeros(g.nt)
-    check(ccall((:fg_adjoint_dJdmu, libpath()), Cint,
-                (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{UInt8}, Int32, Ref{Float64}, Ptr{Float64}),
-                g.h, mur, u0, target, 0, J, grad))
+    o = Ref(newton_opts(precision=precision))
+    s = Ref{AdjointStats}()
+    nlp = nl === nothing ? Ptr{UInt8}(C_NULL) : pointer(nl)
+    GC.@preserve nl begin
+        check(ccall((:fg_adjoint_dJdmu, libpath()), Cint,
+                    (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{UInt8}, Ptr{UInt8}, Ref{NewtonOpts}, Float64,
+                     Ref{Float64}, Ptr{Float64}, Ptr{Float64}, Ref{AdjointStats}),
+                    g.h, mur, u0, target, nlp, o, rtol, J, grad, C_NULL, s); allow_not_converged=true)
+    end
     return J[], grad
 end
 

@@ -204,6 +204,41 @@ fg_status fg_magnetostatics_linear(fg_mesh *m, const double *mu, const double *u
  * H and mu may be NULL. */
 fg_status fg_newton_magnetostatics(fg_mesh *m, const uint8_t *nl, const double *mu_lin, const double *u0,
                                    const fg_newton_opts *o, double *u, double *H, double *mu, fg_newton_stats *s);
+/* Backward-Euler heat conduction (Heat/heat3D.jl:50-90: T <- (M + dt A) \ (M T)) on
+ * P1 tetrahedra with heat capacity rho_c, per-element conductivity kappa (nt) and
+ * T = 0 on the Dirichlet nodes of fg_mesh_set_dirichlet:
+ * (rho_c M + dt K(kappa)) T_{n+1} = rho_c M T_n for nsteps steps, each solve started
+ * from T_n.  T (nv) holds the initial field and receives the last one; snapshots
+ * (may be NULL) receives T after every `every` steps (nsteps/every rows of nv).
+ * o->precision: FG_MIXED (FP32 operator and CG inside FP64 refinement) or FG_FP64;
+ * stats accumulate over the steps. */
+fg_status fg_heat_be(fg_mesh *m, const double *kappa, double rho_c, double dt, int32_t nsteps, double *T,
+                     int32_t every, double *snapshots, const fg_solve_opts *o, fg_solve_stats *s);
+
+typedef struct fg_adjoint_stats {
+  int32_t forward_iters;  /* CG iterations of the forward solve (all Newton steps) */
+  int32_t adjoint_iters;  /* CG iterations of the adjoint solve */
+  int32_t newton_iters;   /* 0 for the linear forward problem */
+  int32_t converged;      /* forward and adjoint both converged */
+  double forward_ms;      /* device time of the forward solve */
+  double adjoint_ms;      /* device time of J, the adjoint solve and the gradient */
+} fg_adjoint_stats;
+
+/* Differentiation of J = volume-weighted mean of H_x over the elements with
+ * target[k] != 0 (the volume average of Magnetostatics/NewtonRaphson.jl:234-240)
+ * with respect to the per-element relative permeability mur (mu = mu0 mur).
+ * Forward: linear magnetostatics (Magnetostatics/magneticField.jl:89-132) when
+ * nl == NULL, else the Newton solve of fg_newton_magnetostatics (Froehlich elements
+ * nl[k] != 0, the others mu0 mur[k]).  Adjoint: the symmetric operator (K(mu), or
+ * the converged Newton Jacobian K + At) solved for lambda with right-hand side
+ * dJ/du; grad[k] = dJ/dmur_k = -mu0 VE_k grad(lambda).grad(u).  Dirichlet nodes come
+ * from fg_mesh_set_dirichlet with values u0; o->precision selects FP32 solves with
+ * FP64 refinement (FG_MIXED) or FP64; rtol is the relative residual of the linear
+ * forward solve and of the adjoint solve.  u (nv, may be NULL) receives the forward
+ * potential.  No counterpart in the reference (which has no derivatives). */
+fg_status fg_adjoint_dJdmu(fg_mesh *m, const double *mur, const double *u0, const uint8_t *target,
+                           const uint8_t *nl, const fg_newton_opts *o, double rtol, double *J, double *grad,
+                           double *u, fg_adjoint_stats *s);
 /* H = -sum u_a grad(phi_a) per element (Magnetostatics/magneticField.jl:111-124). */
 fg_status fg_hfield(fg_mesh *m, const double *u, double *H);
 
