@@ -20,6 +20,8 @@ magnetostatics_linear           Magnetostatics/magneticField.jl:89-132         (
 newton_magnetostatics           Magnetostatics/NewtonRaphson.jl:109-214        (u, H, mu, stats)
 hfield(mesh, u)                 Magnetostatics/magneticField.jl:111-124        (3, nt) ndarray
 heat_be                         Heat/heat3D.jl:50-90                           (T, snapshots, stats)
+batch_magnetostatics_linear     magneticField.jl:89-132 on many meshes         (u list, iters, stats)
+magnetostatics_sweep            magneticField.jl:89-132 for many fields        (U nv x nfield, stats)
 adjoint_dJdmu                   (none: gradient of NewtonRaphson.jl:234-240)   (J, grad, u, stats)
 ==============================  =============================================  ==========================
 
@@ -41,7 +43,7 @@ __all__ = [
     "GPUMesh", "gpu_mesh", "stiffnessMatrix", "localStiffnessMatrix", "tangentialStiffnessMatrix", "massMatrix",
     "stiffnessMatrix2D", "massMatrix2D", "quadraticStiffnessMatrix", "quadraticMassMatrix",
     "quadraticStiffnessMatrix2D", "quadraticMassMatrix2D", "cg", "spmv", "magnetostatics_linear",
-    "newton_magnetostatics", "hfield", "heat_be", "adjoint_dJdmu", "solve_opts", "newton_opts", "MESH", "MU0", "box_tet_mesh", "box_tri_mesh",
+    "newton_magnetostatics", "hfield", "heat_be", "adjoint_dJdmu", "batch_magnetostatics_linear", "magnetostatics_sweep", "solve_opts", "newton_opts", "MESH", "MU0", "box_tet_mesh", "box_tri_mesh",
 ]
 
 
@@ -245,6 +247,41 @@ def heat_be(mesh: MESH, T0, kappa, rho_c=1.0, dt=1e-3, nsteps=100, every=10, pre
                             L.ptr(snaps) if nsnap else None, C.byref(o), C.byref(s))
     L.check(st, allow_not_converged=True)
     return T, snaps[:nsnap], L.stats_dict(s)
+
+
+def magnetostatics_sweep(mesh: MESH, mu, H0, rtol=1e-10, inner_rtol=1e-5, maxiter=1_000_000, check_every=16):
+    """Linear magnetostatics for many applied fields H0 (nfield x 3) at once (one
+    multi-right-hand-side CG, FP32 inner + FP64 refinement); returns (U nv x nfield, stats)."""
+    g = gpu_mesh(mesh)
+    H = _c(np.asarray(H0, dtype=np.float64).reshape(-1, 3), np.float64)   # 3 x nfield column-major
+    nf = H.shape[0]
+    U = np.zeros((nf, mesh.nv))                                             # column-major nv x nf
+    o = solve_opts(precision="mixed", rtol=rtol, inner_rtol=inner_rtol, maxiter=maxiter, check_every=check_every)
+    s = L.SolveStats()
+    st = L.lib().fg_magnetostatics_sweep(g.h, L.ptr(_c(mu, np.float64)), nf, L.ptr(H), C.byref(o), L.ptr(U),
+                                         C.byref(s))
+    L.check(st, allow_not_converged=True)
+    return U.T, L.stats_dict(s)
+
+
+def batch_magnetostatics_linear(meshes, mus, u_ins, rtol=1e-10, maxiter=1_000_000):
+    """Independent linear magnetostatic problems (one per mesh, Dirichlet rows from
+    each mesh) in one persistent GPU launch; returns (list of u, iterations, stats)."""
+    gs = [gpu_mesh(m) for m in meshes]
+    n = len(meshes)
+    mus_c = [_c(mu, np.float64) for mu in mus]
+    uin_c = [_c(u, np.float64) for u in u_ins]
+    outs = [np.zeros(m.nv) for m in meshes]
+    H = (C.c_void_p * n)(*[g.h.value for g in gs])
+    MU = (C.c_void_p * n)(*[a.ctypes.data for a in mus_c])
+    UI = (C.c_void_p * n)(*[a.ctypes.data for a in uin_c])
+    UO = (C.c_void_p * n)(*[a.ctypes.data for a in outs])
+    its = np.zeros(n, dtype=np.int32)
+    o = solve_opts(precision="fp64", rtol=rtol, maxiter=maxiter)
+    s = L.BatchStats()
+    st = L.lib().fg_batch_magnetostatics_linear(H, n, MU, UI, C.byref(o), UO, L.ptr(its), C.byref(s))
+    L.check(st, allow_not_converged=True)
+    return outs, its, L.stats_dict(s)
 
 
 def adjoint_dJdmu(mesh: MESH, mur, u0, target, nl=None, rtol=1e-12, **kw):

@@ -55,6 +55,11 @@ class AdjointStats(C.Structure):
                 ("converged", C.c_int32), ("forward_ms", C.c_double), ("adjoint_ms", C.c_double)]
 
 
+class BatchStats(C.Structure):
+    _fields_ = [("problems", C.c_int32), ("converged", C.c_int32), ("max_iterations", C.c_int32),
+                ("pad_", C.c_int32), ("total_iterations", C.c_int64), ("ms", C.c_double)]
+
+
 def stats_dict(s) -> dict:
     return {name: getattr(s, name) for name, _ in s._fields_ if name != "pad_"}
 
@@ -84,6 +89,8 @@ SIGNATURES = {
     "fg_newton_magnetostatics": [_vp, _vp, _vp, _vp, C.POINTER(NewtonOpts), _vp, _vp, _vp, C.POINTER(NewtonStats)],
     "fg_hfield": [_vp, _vp, _vp],
     "fg_heat_be": [_vp, _vp, _d, _d, _i32, _vp, _i32, _vp, C.POINTER(SolveOpts), C.POINTER(SolveStats)],
+    "fg_batch_magnetostatics_linear": [_vp, _i32, _vp, _vp, C.POINTER(SolveOpts), _vp, _vp, C.POINTER(BatchStats)],
+    "fg_magnetostatics_sweep": [_vp, _vp, _i32, _vp, C.POINTER(SolveOpts), _vp, C.POINTER(SolveStats)],
     "fg_adjoint_dJdmu": [_vp, _vp, _vp, _vp, _vp, C.POINTER(NewtonOpts), _d, C.POINTER(_d), _vp, _vp,
                          C.POINTER(AdjointStats)],
     "fg_scalar_potential_newton": [_vp, _i64, _vp, _i64, _i32, _vp, _vp, _vp, _vp, C.POINTER(NewtonOpts), _vp, _vp,

@@ -215,6 +215,37 @@ fg_status fg_newton_magnetostatics(fg_mesh *m, const uint8_t *nl, const double *
 fg_status fg_heat_be(fg_mesh *m, const double *kappa, double rho_c, double dt, int32_t nsteps, double *T,
                      int32_t every, double *snapshots, const fg_solve_opts *o, fg_solve_stats *s);
 
+/* A sweep of applied fields on one linear mesh (the hysteresis-loop use of
+ * Magnetostatics/magneticField.jl:89-132): for field c, K(mu) u_c = 0 on the free
+ * rows with u_c = -H0_c . x on the Dirichlet rows of fg_mesh_set_dirichlet, all
+ * fields solved together by one multi-right-hand-side Jacobi-PCG that reads the
+ * matrix once per iteration for every field (FP32 matrix and inner CG, FP64
+ * residual and solution by iterative refinement; o->precision must be FG_MIXED).
+ * mu: nt absolute permeabilities; H0: 3 x nfield; U (nv x nfield column-major, may
+ * be NULL) receives the potentials.  nfield <= 256; rows of at most 32 entries. */
+fg_status fg_magnetostatics_sweep(fg_mesh *m, const double *mu, int32_t nfield, const double *H0,
+                                  const fg_solve_opts *o, double *U, fg_solve_stats *s);
+
+typedef struct fg_batch_stats {
+  int32_t problems;
+  int32_t converged;       /* problems that reached rtol */
+  int32_t max_iterations;  /* largest CG iteration count of a problem */
+  int32_t pad_;
+  int64_t total_iterations;
+  double ms;               /* device time of the one persistent launch */
+} fg_batch_stats;
+
+/* count independent linear magnetostatic problems (Magnetostatics/magneticField.jl:89-132
+ * on each mesh: K(mu) u = 0 on free rows, u = u_in on the Dirichlet rows set by
+ * fg_mesh_set_dirichlet) solved by FP64 Jacobi-PCG in ONE persistent kernel launch,
+ * replayed from a CUDA graph: each problem runs on its own thread-block cluster.
+ * mu[k] (nt_k, absolute permeability), u_in[k] and u_out[k] (nv_k) are host arrays
+ * per mesh; iterations (count, may be NULL) receives each problem's CG iterations.
+ * All meshes on the current device; o->precision must be FG_FP64. */
+fg_status fg_batch_magnetostatics_linear(fg_mesh *const *meshes, int32_t count, const double *const *mu,
+                                         const double *const *u_in, const fg_solve_opts *o, double *const *u_out,
+                                         int32_t *iterations, fg_batch_stats *s);
+
 typedef struct fg_adjoint_stats {
   int32_t forward_iters;  /* CG iterations of the forward solve (all Newton steps) */
   int32_t adjoint_iters;  /* CG iterations of the adjoint solve */

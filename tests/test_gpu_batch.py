@@ -1,0 +1,48 @@
+"""Many independent linear magnetostatic problems in one persistent launch
+(fg_batch_magnetostatics_linear) against the oracle's per-mesh solve."""
+import numpy as np
+import pytest
+
+import femeko_gpu as fg
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def batch_case(count, lo, hi, seed=7):
+    rng = np.random.default_rng(seed)
+    meshes, mus, u0s = [], [], []
+    for k in range(count):
+        n = int(rng.integers(lo, hi + 1))
+        m = fg.box_tet_mesh(n, seed=100 + k)
+        meshes.append(m)
+        mus.append(rng.uniform(1, 1000, m.nt) * fg.MU0)
+        u0s.append(-m.p[0].copy())
+    return meshes, mus, u0s
+
+
+def test_batch_matches_single_solves():
+    meshes, mus, u0s = batch_case(12, 3, 9)
+    us, its, st = fg.batch_magnetostatics_linear(meshes, mus, u0s, rtol=1e-10)
+    assert st["problems"] == 12 and st["converged"] == 12
+    assert st["max_iterations"] == its.max() and st["total_iterations"] == its.sum()
+    for m, mu, u0, u, it in zip(meshes, mus, u0s, us, its):
+        uo, Ho, _ = O.linear_magnetostatics(m, u0, mu, cg_tol=1e-13)
+        assert it > 0
+        assert np.linalg.norm(u - uo) / np.linalg.norm(uo) < 1e-8
+        fx = m.dirichlet_mask().astype(bool)
+        assert np.array_equal(u[fx], u0[fx])
+
+
+def test_batch_sixty_four_uneven_meshes_twice():
+    """64 problems of uneven size; a second call on the same handles gives the same
+    answer (the launch and its graph are rebuilt per call)."""
+    meshes, mus, u0s = batch_case(64, 4, 12, seed=3)
+    us1, its1, st1 = fg.batch_magnetostatics_linear(meshes, mus, u0s, rtol=1e-9)
+    us2, its2, st2 = fg.batch_magnetostatics_linear(meshes, mus, u0s, rtol=1e-9)
+    assert st1["converged"] == 64 and np.array_equal(its1, its2)
+    for a, b in zip(us1, us2):
+        assert np.array_equal(a, b)
+    k = int(np.argmax([m.nv for m in meshes]))
+    uo, _, _ = O.linear_magnetostatics(meshes[k], u0s[k], mus[k], cg_tol=1e-12)
+    assert np.linalg.norm(us1[k] - uo) / np.linalg.norm(uo) < 1e-7
