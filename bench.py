@@ -242,14 +242,15 @@ def run_ours(args):
     lib.fg_mesh_layout(g.h, C.byref(nsell), C.byref(ninc), C.byref(nsl))
     fg.newton_magnetostatics(mesh, nl, mu_lin, u0, precision="mixed")   # leaves J32 on the handle
     chosen = C.c_int32()
-    variants_us = np.zeros(6)
-    L.check(lib.fg_autotune(g.h, L.FG_MIXED, C.byref(chosen), L.ptr(variants_us), 6))
+    variants_us = np.zeros(8)
+    L.check(lib.fg_autotune(g.h, L.FG_MIXED, C.byref(chosen), L.ptr(variants_us), 8))
     autotune = {"cg32_iteration_variants_us": [round(float(v), 2) for v in variants_us], "chosen": int(chosen.value),
-                "names": ["gather/256", "gather-hoist/256", "gather/128", "gather/512", "halo-smem",
-                          "halo-smem-pipelined"]}
-    ms_spmv = C.c_double()
+                "names": ["fused gather/256", "fused gather-hoist/256", "fused gather/128", "fused gather/512",
+                          "fused halo-smem", "fused halo-smem-pipelined", "split gather/256", "split halo-smem"]}
+    ms_spmv, ms_iter = C.c_double(), C.c_double()
     L.check(lib.fg_bench_kernel(g.h, 0, L.FG_MIXED, 200, C.byref(ms_spmv)))
-    kernels_us = {"cg32_iteration": ms_spmv.value * 1e3}
+    L.check(lib.fg_bench_kernel(g.h, 3, L.FG_MIXED, 200, C.byref(ms_iter)))
+    kernels_us = {"cg32_spmv": ms_spmv.value * 1e3, "cg32_iteration": ms_iter.value * 1e3}
     for name, which, prec in (("newton_assembly_f32", 2, L.FG_MIXED),):
         t = C.c_double()
         L.check(lib.fg_bench_kernel(g.h, which, prec, 20 if which == 2 else 200, C.byref(t)))
@@ -265,12 +266,19 @@ def run_ours(args):
         kernels_us[name] = t.value * 1e3
     fg.newton_magnetostatics(mesh, nl, mu_lin, u0, precision="mixed")
     n = mesh.nv
-    # one fused FP32 CG iteration: matrix value (4 B) + 16-bit column (2 B) per stored
-    # nonzero; per row the (r, w, s, dinv) state read and written (16 + 16 B) and
-    # p, x read and written (8 + 8 B).  Neighbour-state gathers are re-reads.
-    alg_bytes = g.nnz * 6 + 48 * n
+    v = int(chosen.value)
+    if v >= 6:
+        # split iteration, dominant kernel w = A u with its dots: FP32 value (4 B) and
+        # 16-bit column (2 B) per stored nonzero; per row u and r read, w written
+        # (12 B).  Neighbour gathers of u are re-reads.
+        alg_bytes = g.nnz * 6 + 12 * n
+        kname = "k_cg32s_spmv_halo" if v == 7 else "k_cg32s_spmv"
+    else:
+        # one fused iteration: matrix as above; per row the (r, w, s, dinv) state read
+        # and written (16 + 16 B) and p, x read and written (8 + 8 B)
+        alg_bytes = g.nnz * 6 + 48 * n
+        kname = {4: "k_cg32_iter_halo", 5: "k_cg32_iter_pipe"}.get(v, "k_cg32_iter")
     achieved = alg_bytes / (ms_spmv.value * 1e-3) / 1e9
-    kname = {4: "k_cg32_iter_halo", 5: "k_cg32_iter_pipe"}.get(int(chosen.value), "k_cg32_iter")
     roofline = {"bound": "hbm", "kernel": kname, "variant": autotune["names"][int(chosen.value)],
                 "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
@@ -352,6 +360,150 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------------
+# Secondary workloads (--case): the other configurations of the path, each printing
+# its own JSON line.  "cg-kernel" and "newton-kernels" are the small drivers the
+# profiles under profiles/ were captured with.
+
+def _line(metric, value, unit, higher, config, extra):
+    d = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "higher_is_better": higher,
+         "data": "synthetic", "config": config}
+    d.update(extra)
+    print(json.dumps(d))
+
+
+def case_cg_kernel(args):
+    """Forced FP32 CG kernel variant on K + M of the workload mesh, no graph:
+    one launch per iteration (the ncu capture target)."""
+    import femeko_gpu as fg
+    mesh, nl, mu_lin, u0 = workload(args.cells)
+    K = (fg.stiffnessMatrix(mesh) + fg.massMatrix(mesh)).tocsc()
+    b = np.random.default_rng(1).normal(size=mesh.nv)
+    x, st = fg.cg(K, b, reltol=1e-30, maxiter=args.iters, precision="mixed", spmv=args.variant, use_graph=False,
+                  return_stats=True)
+    _line("CG iteration time (FP32, forced variant)", 1e3 * st["ms"] / max(st["iterations"], 1), "us/iteration",
+          False, {"workload": f"K+M of the Kuhn-tet box, {args.cells}^3 cells", "variant": args.variant,
+                  "iterations": st["iterations"]}, {})
+
+
+def case_newton_kernels(args):
+    """One mixed and one FP64 Newton solve, then the per-launch time of the hot
+    kernels on each converged operator."""
+    import femeko_gpu as fg
+    import femeko_gpu._lib as L
+    mesh, nl, mu_lin, u0 = workload(args.cells)
+    g = fg.gpu_mesh(mesh)
+    lib = L.lib()
+    out = {}
+    for prec in ("mixed", "fp64"):
+        u, H, mu, st = fg.newton_magnetostatics(mesh, nl, mu_lin, u0, precision=prec)
+        P = L.FG_MIXED if prec == "mixed" else L.FG_FP64
+        for which, name in ((0, "cg_spmv"), (1, "cg_update"), (2, "newton_assembly")):
+            t = C.c_double()
+            L.check(lib.fg_bench_kernel(g.h, which, P, 5 if which < 2 else 2, C.byref(t)))
+            out[f"{prec}_{name}_us"] = t.value * 1e3
+    _line("Newton hot-kernel launch times", out["mixed_cg_spmv_us"], "us", False,
+          {"workload": f"nonlinear Froehlich-plate magnetostatics, Kuhn tets {args.cells}^3 cells"}, {"kernels": out})
+
+
+def case_heat(args):
+    """Backward-Euler heat, 64^3 cells: lognormal(0,1) conductivity, rho_c = 1,
+    dt = 1e-3, 100 steps, Gaussian bump of width 0.5 at a seeded interior point,
+    T = 0 on the boundary; mixed (FP32 CG + FP64 refinement) vs FP64, the mixed
+    snapshots compared with the FP64 ones every 10th step."""
+    import femeko_gpu as fg
+    from femeko_gpu.mesh import box_tet_mesh
+    cells = args.cells if args.cells != 96 else 64
+    mesh = box_tet_mesh(cells, seed=SEED)
+    rng = np.random.default_rng(SEED)
+    kappa = np.exp(rng.normal(size=mesh.nt))
+    x0 = rng.uniform(-2.5, 2.5, 3)
+    T0 = np.exp(-(((mesh.p - x0[:, None]) ** 2).sum(axis=0)) / 0.5 ** 2)
+    res = {}
+    for prec in ("fp64", "mixed"):
+        fg.heat_be(mesh, T0, kappa, nsteps=2, every=0, precision=prec)          # warm-up
+        T, snaps, st = fg.heat_be(mesh, T0, kappa, nsteps=100, every=10, precision=prec)
+        res[prec] = (snaps, st)
+    err = [float(np.linalg.norm(a - b) / np.linalg.norm(b)) for a, b in zip(res["mixed"][0], res["fp64"][0])]
+    ms_m, ms_d = res["mixed"][1]["ms"], res["fp64"][1]["ms"]
+    _line("heat BE steps/s (mixed FP32+FP64 refinement)", 100 / (ms_m * 1e-3), "steps/s", True,
+          {"workload": f"backward-Euler heat, Kuhn tets {cells}^3 cells, 100 steps", "tets": int(mesh.nt),
+           "nodes": int(mesh.nv)},
+          {"fp64_steps_per_s": 100 / (ms_d * 1e-3), "mixed_over_fp64": ms_d / ms_m,
+           "cg_iters": {"mixed": res["mixed"][1]["iterations"], "fp64": res["fp64"][1]["iterations"]},
+           "rel_err_mixed_vs_fp64_every_10th_step": err})
+
+
+def case_sweep(args):
+    """256 applied fields h (cos t, sin t, 0), h ~ U[-1e5, 1e5], t ~ U[0, pi], on the
+    48^3-cell linear plate mesh (mur 1000): one multi-field CG vs field-by-field."""
+    import femeko_gpu as fg
+    from femeko_gpu.mesh import box_tet_mesh
+    cells = args.cells if args.cells != 96 else 48
+    mesh = box_tet_mesh(cells, seed=SEED)
+    mu = np.where(mesh.elementID == 2, 1000.0, 1.0) * fg.MU0
+    rng = np.random.default_rng(SEED)
+    h, th = rng.uniform(-1e5, 1e5, 256), rng.uniform(0, np.pi, 256)
+    H0 = np.stack([h * np.cos(th), h * np.sin(th), np.zeros(256)], axis=1)
+    fg.magnetostatics_sweep(mesh, mu, H0[:32])                                   # warm-up
+    U, st = fg.magnetostatics_sweep(mesh, mu, H0)
+    singles = []
+    for c in range(8):                                                           # field-by-field sample
+        u0 = -(H0[c][:, None] * mesh.p).sum(axis=0)
+        _, _, s1 = fg.magnetostatics_linear(mesh, mu, u0, precision="mixed")
+        singles.append(s1["ms"])
+    per_single = float(np.median(singles))
+    _line("field-sweep solves/s (256 fields, one multi-field CG)", 256 / (st["ms"] * 1e-3), "solves/s", True,
+          {"workload": f"linear plate magnetostatics, Kuhn tets {cells}^3 cells, 256 fields", "tets": int(mesh.nt),
+           "nodes": int(mesh.nv)},
+          {"ms": st["ms"], "iterations": st["iterations"], "refinements": st["refinements"],
+           "single_field_solves_per_s": 1e3 / per_single, "speedup_vs_single_field": (256 / st["ms"]) / (1 / per_single)})
+
+
+def case_batch(args):
+    """64 independent linear problems, cells per side ~ U{8..40}, mur ~ U[1,1000] per
+    element, one persistent graph-captured launch."""
+    import femeko_gpu as fg
+    from femeko_gpu.mesh import box_tet_mesh
+    rng = np.random.default_rng(SEED)
+    ns = rng.integers(8, 41, 64)
+    meshes = [box_tet_mesh(int(n), seed=SEED + k) for k, n in enumerate(ns)]
+    mus = [rng.uniform(1, 1000, m.nt) * fg.MU0 for m in meshes]
+    u0s = [-m.p[0].copy() for m in meshes]
+    fg.batch_magnetostatics_linear(meshes, mus, u0s, rtol=1e-10)              # warm-up (assembly, handles)
+    us, its, st = fg.batch_magnetostatics_linear(meshes, mus, u0s, rtol=1e-10)
+    _line("batched independent solves/s (64 meshes, one persistent launch)", 64 / (st["ms"] * 1e-3), "solves/s",
+          True, {"workload": "64 linear problems, Kuhn tets 8..40 cells per side", "cells": [int(n) for n in ns],
+                 "total_nodes": int(sum(m.nv for m in meshes))},
+          {"ms": st["ms"], "max_iterations": st["max_iterations"], "total_iterations": st["total_iterations"],
+           "converged": st["converged"]})
+
+
+def case_adjoint(args):
+    """dJ/dmur for J = mean Hx over elements with centroid in |x| < 0.5 on the 64^3
+    linear mesh (mur ~ U[1,1000]): adjoint cost against the forward solve."""
+    import femeko_gpu as fg
+    from femeko_gpu.mesh import box_tet_mesh
+    cells = args.cells if args.cells != 96 else 64
+    mesh = box_tet_mesh(cells, seed=SEED)
+    rng = np.random.default_rng(SEED)
+    mur = rng.uniform(1, 1000, mesh.nt)
+    c = mesh.centroids()
+    target = (np.sqrt((c * c).sum(axis=0)) < 0.5).astype(np.uint8)
+    u0 = -mesh.p[0].copy()
+    fg.adjoint_dJdmu(mesh, mur, u0, target, precision="mixed", rtol=1e-10)     # warm-up
+    J, grad, u, st = fg.adjoint_dJdmu(mesh, mur, u0, target, precision="mixed", rtol=1e-10)
+    _line("adjoint dJ/dmur cost relative to the forward solve", st["adjoint_ms"] / st["forward_ms"], "x forward",
+          False, {"workload": f"linear magnetostatics, Kuhn tets {cells}^3 cells, mur ~ U[1,1000], |x| < 0.5 target",
+                  "tets": int(mesh.nt), "nodes": int(mesh.nv), "target_elements": int(target.sum())},
+          {"J": J, "forward_ms": st["forward_ms"], "adjoint_ms": st["adjoint_ms"],
+           "forward_iters": st["forward_iters"], "adjoint_iters": st["adjoint_iters"]})
+
+
+CASES = {"cg-kernel": case_cg_kernel, "newton-kernels": case_newton_kernels, "heat": case_heat,
+         "sweep": case_sweep, "batch": case_batch, "adjoint": case_adjoint}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -368,9 +520,17 @@ def main():
                     help="DRAM bytes per SpMV launch from an ncu capture (reported as roofline.traffic)")
     ap.add_argument("--ref-counts", type=int, nargs=3, default=[11, 39, 1324],
                     help="(newton iterations, line-search trials, CG iterations) of the solve; default: the FP64 GPU solve at 96^3")
+    ap.add_argument("--case", choices=sorted(CASES), default=None,
+                    help="run a secondary workload instead of the headline benchmark")
+    ap.add_argument("--variant", type=int, default=6, help="--case cg-kernel: forced CG kernel variant (1..6)")
+    ap.add_argument("--iters", type=int, default=200, help="--case cg-kernel: CG iterations")
     args = ap.parse_args()
     if args.fp64_steps is None:
         args.fp64_steps = args.steps
+    if args.case:
+        sys.path.insert(0, os.path.join(ROOT, "femeko.jl_gb300"))
+        CASES[args.case](args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

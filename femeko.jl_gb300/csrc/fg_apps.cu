@@ -23,16 +23,18 @@ extern "C" fg_status fg_scalar_potential_newton(const double *p, int64_t nv, con
 
 // Average device time (CUDA events on the handle's stream) of one launch of a hot
 // kernel on the operator currently held by the handle:
-//   which = 0: CG SpMV (q = A(z + beta p) and p.q) of the given precision;
-//   which = 1: CG vector update;
-//   which = 2: Newton element pass + row gather at the current potential.
+//   which = 0: CG SpMV with its dot products (w = A u; the whole iteration for the
+//              fused FP32 variants);
+//   which = 1: CG vector update (fused FP32 variants: the whole iteration);
+//   which = 2: Newton element pass + row gather at the current potential;
+//   which = 3: one whole CG iteration.
 fg_status fg_bench_cg_kernel(fg_mesh *m, int which, int precision, int reps, double *ms_per_launch);
 
 extern "C" fg_status fg_bench_kernel(fg_mesh *m, int32_t which, int32_t precision, int32_t reps,
                                      double *ms_per_launch) {
   return fg_guard([&]() -> fg_status {
     FG_REQUIRE(m && ms_per_launch && reps > 0, FG_BAD_ARG, "fg_bench_kernel: bad argument");
-    if (which == 0 || which == 1) return fg_bench_cg_kernel(m, which, precision, reps, ms_per_launch);
+    if (which == 0 || which == 1 || which == 3) return fg_bench_cg_kernel(m, which, precision, reps, ms_per_launch);
     FG_REQUIRE(which == 2, FG_BAD_ARG, "fg_bench_kernel: unknown kernel");
     FG_REQUIRE(m->v64[7] && m->mu, FG_BAD_ARG, "fg_bench_kernel: run a Newton solve on this handle first");
     if (!m->v64[11]) m->v64[11] = dev_alloc<double>(m, (size_t)m->nv);

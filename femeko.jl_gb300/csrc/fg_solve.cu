@@ -531,6 +531,144 @@ __global__ void __launch_bounds__(R) k_cg32_iter_pipe(PipeArgs a, const float4 *
   if (grid_finish<3>(part, partials, counter, tot) && ok) cgcg_scalars(tot, scal, ictl);
 }
 
+// FP32 Chronopoulos-Gear iteration split in two passes, as the FP64 one: a streaming
+// vector update (s = w + beta s, p = u + beta p, x += alpha p, r -= alpha s,
+// u = D^-1 r; four rows per thread) and w = A u with the three dot products.  The
+// SpMV then gathers 4-byte entries of u instead of 16-byte neighbour states.
+__global__ void __launch_bounds__(256) k_cg32s_vec(int64_t n4, float4 *__restrict__ r, const float4 *__restrict__ w,
+                                                   float4 *__restrict__ s, float4 *__restrict__ p,
+                                                   float4 *__restrict__ u, float4 *__restrict__ x,
+                                                   const float4 *__restrict__ dinv, const double *scal,
+                                                   const int *ictl) {
+  if (ictl[I_DONE]) return;
+  const float alpha = (float)scal[S_ALPHA], beta = (float)scal[S_BETA];
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n4) return;
+  const float4 ww = w[j], dd = dinv[j], uu = u[j];
+  float4 ss = s[j], pp = p[j], xx = x[j], rr = r[j];
+  ss.x = fmaf(beta, ss.x, ww.x); ss.y = fmaf(beta, ss.y, ww.y); ss.z = fmaf(beta, ss.z, ww.z); ss.w = fmaf(beta, ss.w, ww.w);
+  pp.x = fmaf(beta, pp.x, uu.x); pp.y = fmaf(beta, pp.y, uu.y); pp.z = fmaf(beta, pp.z, uu.z); pp.w = fmaf(beta, pp.w, uu.w);
+  xx.x = fmaf(alpha, pp.x, xx.x); xx.y = fmaf(alpha, pp.y, xx.y); xx.z = fmaf(alpha, pp.z, xx.z); xx.w = fmaf(alpha, pp.w, xx.w);
+  rr.x = fmaf(-alpha, ss.x, rr.x); rr.y = fmaf(-alpha, ss.y, rr.y); rr.z = fmaf(-alpha, ss.z, rr.z); rr.w = fmaf(-alpha, ss.w, rr.w);
+  s[j] = ss;
+  p[j] = pp;
+  x[j] = xx;
+  r[j] = rr;
+  u[j] = make_float4(dd.x * rr.x, dd.y * rr.y, dd.z * rr.z, dd.w * rr.w);
+}
+
+template <class CI>
+__global__ void __launch_bounds__(256) k_cg32s_spmv(int64_t n, const int *__restrict__ sl_ptr,
+                                                    const int *__restrict__ sl_len,
+                                                    const typename CI::T *__restrict__ col,
+                                                    const float *__restrict__ val, const float *__restrict__ u,
+                                                    const float *__restrict__ r, float *__restrict__ w, double *scal,
+                                                    int *ictl, double *partials, unsigned *counter) {
+  if (ictl[I_DONE]) return;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  Acc<float> dots[3];
+  if (i < n) {
+    const int s = (int)(i >> 5), lane = (int)(i & 31);
+    const int64_t base = (int64_t)sl_ptr[s] + lane * FG_GROUP;
+    const int G = sl_len[s];
+    const float4 *v4 = reinterpret_cast<const float4 *>(val + base);
+    const typename CI::T4 *c4 = reinterpret_cast<const typename CI::T4 *>(col + base);
+    float acc = 0.f;
+#pragma unroll 4
+    for (int g = 0; g < G; ++g) {
+      const float4 vv = __ldg(v4 + (int64_t)g * FG_SLICE);
+      const typename CI::T4 cc = ld_cols(c4 + (int64_t)g * FG_SLICE);
+      acc = fmaf(vv.x, __ldg(u + CI::col(cc.x, i)), acc);
+      acc = fmaf(vv.y, __ldg(u + CI::col(cc.y, i)), acc);
+      acc = fmaf(vv.z, __ldg(u + CI::col(cc.z, i)), acc);
+      acc = fmaf(vv.w, __ldg(u + CI::col(cc.w, i)), acc);
+    }
+    w[i] = acc;
+    const float ui = u[i], ri = r[i];
+    dots[0].add(ri * ui);
+    dots[1].add(acc * ui);
+    dots[2].add(ri * ri);
+  }
+  double part[3];
+  block_sum_acc<3>(dots, part);
+  double tot[3];
+  if (grid_finish<3>(part, partials, counter, tot)) cgcg_scalars(tot, scal, ictl);
+}
+
+// The split SpMV with halo staging of u (4 bytes per distinct neighbour).
+template <int R>
+__global__ void __launch_bounds__(R) k_cg32s_spmv_halo(int64_t n, const int *__restrict__ sl_ptr,
+                                                       const int *__restrict__ sl_len,
+                                                       const uint16_t *__restrict__ lcol,
+                                                       const float *__restrict__ val, const int *__restrict__ halo_col,
+                                                       const int *__restrict__ halo_len, int hcap,
+                                                       const float *__restrict__ u, const float *__restrict__ r,
+                                                       float *__restrict__ w, double *scal, int *ictl,
+                                                       double *partials, unsigned *counter) {
+  extern __shared__ float uhs[];
+  if (ictl[I_DONE]) return;
+  {
+    const int hl = halo_len[blockIdx.x];
+    const int *hc = halo_col + (int64_t)blockIdx.x * hcap;
+    for (int h = threadIdx.x; h < hl; h += R) uhs[h] = __ldg(u + __ldg(hc + h));
+  }
+  __syncthreads();
+  const int64_t i = (int64_t)blockIdx.x * R + threadIdx.x;
+  Acc<float> dots[3];
+  if (i < n) {
+    const int s = (int)(i >> 5), lane = (int)(i & 31);
+    const int64_t base = (int64_t)sl_ptr[s] + lane * FG_GROUP;
+    const int G = sl_len[s];
+    const float4 *v4 = reinterpret_cast<const float4 *>(val + base);
+    const ushort4 *c4 = reinterpret_cast<const ushort4 *>(lcol + base);
+    float acc = 0.f;
+#pragma unroll 4
+    for (int g = 0; g < G; ++g) {
+      const float4 vv = __ldg(v4 + (int64_t)g * FG_SLICE);
+      const ushort4 cc = __ldg(c4 + (int64_t)g * FG_SLICE);
+      acc = fmaf(vv.x, uhs[cc.x], acc);
+      acc = fmaf(vv.y, uhs[cc.y], acc);
+      acc = fmaf(vv.z, uhs[cc.z], acc);
+      acc = fmaf(vv.w, uhs[cc.w], acc);
+    }
+    w[i] = acc;
+    const float ui = u[i], ri = r[i];
+    dots[0].add(ri * ui);
+    dots[1].add(acc * ui);
+    dots[2].add(ri * ri);
+  }
+  double part[3];
+  block_sum_acc<3>(dots, part);
+  double tot[3];
+  if (grid_finish<3>(part, partials, counter, tot)) cgcg_scalars(tot, scal, ictl);
+}
+
+// r = scale * rin, u = D^-1 r, s = p = x = 0 for the split FP32 iteration.
+__global__ void k_cg32s_init(int64_t n, int64_t np, const double *__restrict__ rin, double scale,
+                             const float *__restrict__ dinv, float *__restrict__ r, float *__restrict__ u,
+                             float *__restrict__ s, float *__restrict__ p, float *__restrict__ x, double tol2_rel,
+                             int maxit, double *scal, int *ictl) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < np; i += stride) {
+    const float ri = (i < n) ? (float)(scale * rin[i]) : 0.f;
+    r[i] = ri;
+    u[i] = dinv[i] * ri;
+    s[i] = 0.f;
+    p[i] = 0.f;
+    x[i] = 0.f;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    scal[S_TOL2] = tol2_rel;
+    scal[S_ALPHA] = 0.0;
+    scal[S_BETA] = 0.0;
+    ictl[I_ITERS] = -1;
+    ictl[I_MAXIT] = maxit;
+    ictl[I_STATUS] = 0;
+    ictl[I_FAULT] = 0;
+    ictl[I_DONE] = 0;
+  }
+}
+
 // r0 = scale * rin, state (r0, 0, 0, dinv) in both buffers, p = x = 0.  The threshold
 // tol2_rel becomes absolute (times r0.r0) in the first iteration.
 __global__ void k_cg32_init(int64_t n, int64_t np, const double *__restrict__ rin, double scale,
@@ -637,9 +775,20 @@ __global__ void __launch_bounds__(R) k_cg64_spmv_halo(int64_t n, const int *__re
   extern __shared__ double ud[];
   if (ictl[I_DONE]) return;
   {
+    constexpr int HB = 8;  // a batch of indices, then their values: HB independent gathers in flight
     const int hl = halo_len[blockIdx.x];
     const int *hc = halo_col + (int64_t)blockIdx.x * hcap;
-    for (int h = threadIdx.x; h < hl; h += R) ud[h] = __ldg(u + __ldg(hc + h));
+    for (int h0 = threadIdx.x; h0 < hl; h0 += HB * R) {
+      int idx[HB];
+#pragma unroll
+      for (int k = 0; k < HB; ++k) idx[k] = (h0 + k * R < hl) ? __ldg(hc + h0 + k * R) : -1;
+      double v[HB];
+#pragma unroll
+      for (int k = 0; k < HB; ++k) v[k] = (idx[k] >= 0) ? __ldg(u + idx[k]) : 0.0;
+#pragma unroll
+      for (int k = 0; k < HB; ++k)
+        if (idx[k] >= 0) ud[h0 + k * R] = v[k];
+    }
   }
   __syncthreads();
   const int64_t i = (int64_t)blockIdx.x * R + threadIdx.x;
@@ -801,10 +950,12 @@ void fg_spmv64_dev(fg_mesh *m, const double *x, double *y) { spmv64_launch(m, x,
 // CG vectors, padded to whole slices and zeroed once (pads stay zero).
 // FP32: v32[0] x, v32[1] p, v32[2] / v32[3] the two (r, w, s, dinv) state buffers.
 // FP64: v64[0] x, v64[1] r, v64[2] u, v64[3] s, v64[4] p, v64[12] w.
+// FP32 CG vectors: [0] x, [1] p, [2] [3] float4 states of the fused iteration;
+// the split iteration uses [4] r, [5] w, [6] s, [7] u.
 static void ensure_cg32(fg_mesh *m) {
-  for (int j = 0; j < 4; ++j)
+  for (int j = 0; j < 8; ++j)
     if (!m->v32[j]) {
-      size_t len = (size_t)m->nvp * (j >= 2 ? 4 : 1);
+      size_t len = (size_t)m->nvp * ((j == 2 || j == 3) ? 4 : 1);
       m->v32[j] = dev_alloc<float>(m, len);
       FG_CUDA_TRY(cudaMemsetAsync(m->v32[j], 0, sizeof(float) * len, m->stream));
     }
@@ -819,7 +970,10 @@ static void ensure_cg64(fg_mesh *m) {
 }
 
 // FP32 iteration variants (block size x load scheduling) for the autotuner.
-constexpr int FG_N_SPMV32 = 6;   // 0-3 direct gathers, 4 halo staging, 5 pipelined halo staging
+// 0-3 fused iteration with direct gathers, 4 fused with halo staging, 5 fused and
+// pipelined, 6 split (vector pass + SpMV) with direct gathers, 7 split with halo staging
+constexpr int FG_N_SPMV32 = 8;
+static inline bool split32(int v) { return v >= 6; }
 constexpr int FG_N_SPMV64 = 2;   // 0 direct gathers, 1 halo staging
 
 template <class CI>
@@ -924,7 +1078,42 @@ static void pipe_launch32(fg_mesh *m, const float4 *in, float4 *out) {
   }
 }
 
+template <int R>
+struct Spmv32sHalo {
+  static constexpr auto fn = k_cg32s_spmv_halo<R>;
+};
+
+// w = A u and the dots of the split FP32 iteration
+static void launch_spmv32s(fg_mesh *m, int v) {
+  if (v == 7 && m->halo_col)
+    halo_launch<Spmv32sHalo>(m, sizeof(float), m->nv, (const int *)m->sl_ptr, (const int *)m->sl_len,
+                             (const uint16_t *)m->sl_lcol, (const float *)m->val32, (const int *)m->halo_col,
+                             (const int *)m->halo_len, m->hcap, (const float *)m->v32[7], (const float *)m->v32[4],
+                             m->v32[5], m->scal, m->ictl, m->red.partials, m->red.counter);
+  else if (m->use_dcol)
+    k_cg32s_spmv<ColRel><<<grid_for(m->nv, 256), 256, 0, m->stream>>>(
+        m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl,
+        m->red.partials, m->red.counter);
+  else
+    k_cg32s_spmv<ColAbs><<<grid_for(m->nv, 256), 256, 0, m->stream>>>(
+        m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl,
+        m->red.partials, m->red.counter);
+}
+
+static void launch_vec32s(fg_mesh *m) {
+  k_cg32s_vec<<<grid_for(m->nvp / 4, 256), 256, 0, m->stream>>>(
+      m->nvp / 4, reinterpret_cast<float4 *>(m->v32[4]), reinterpret_cast<const float4 *>(m->v32[5]),
+      reinterpret_cast<float4 *>(m->v32[6]), reinterpret_cast<float4 *>(m->v32[1]),
+      reinterpret_cast<float4 *>(m->v32[7]), reinterpret_cast<float4 *>(m->v32[0]),
+      reinterpret_cast<const float4 *>(m->dinv32), m->scal, m->ictl);
+}
+
 static void launch_iter32(fg_mesh *m, int v, bool from_first_buffer) {
+  if (split32(v)) {
+    launch_vec32s(m);
+    launch_spmv32s(m, v);
+    return;
+  }
   const float4 *in = reinterpret_cast<const float4 *>(from_first_buffer ? m->v32[2] : m->v32[3]);
   float4 *out = reinterpret_cast<float4 *>(from_first_buffer ? m->v32[3] : m->v32[2]);
   if (v == 5 && pipe_available(m))
@@ -966,7 +1155,11 @@ static void launch_vec64(fg_mesh *m) {
 // buffer 0 -> 1, so the iteration blocks start reading buffer 1.
 static void start_cg(fg_mesh *m, bool mixed, const double *r64, double scale, double tol2_rel, int maxit) {
   const unsigned g = red_grid(m->nvp);
-  if (mixed) {
+  if (mixed && split32(m->spmv_variant32)) {
+    k_cg32s_init<<<g, 256, 0, m->stream>>>(m->nv, m->nvp, r64, scale, m->dinv32, m->v32[4], m->v32[7], m->v32[6],
+                                           m->v32[1], m->v32[0], tol2_rel, maxit, m->scal, m->ictl);
+    launch_spmv32s(m, m->spmv_variant32);
+  } else if (mixed) {
     k_cg32_init<<<g, 256, 0, m->stream>>>(m->nv, m->nvp, r64, scale, m->dinv32,
                                           reinterpret_cast<float4 *>(m->v32[2]), reinterpret_cast<float4 *>(m->v32[3]),
                                           m->v32[1], m->v32[0], tol2_rel, maxit, m->scal, m->ictl);
@@ -984,7 +1177,7 @@ static void start_cg(fg_mesh *m, bool mixed, const double *r64, double scale, do
 static int run_cg(fg_mesh *m, bool mixed, const fg_solve_opts &o, int *status) {
   int block = o.check_every > 0 ? o.check_every : 32;
   if (block & 1) ++block;
-  const int per_iter = mixed ? 1 : 2;
+  const int per_iter = (mixed && !split32(m->spmv_variant32)) ? 1 : 2;
   GraphCache &gc = m->graph[mixed ? 1 : 0];
   const void *key[5] = {mixed ? (const void *)m->val32 : (const void *)m->val64,
                         mixed ? (const void *)(intptr_t)(m->spmv_variant32 + 1) : (const void *)m->v64[0],
@@ -1043,7 +1236,7 @@ static int inner_solve(fg_mesh *m, bool mixed, const double *r64, double rn, dou
       // a forced variant that this operator cannot run (no halo lists, stages too
       // large for shared memory) falls back to the plain gather kernel
       const int v = o.spmv - 1;
-      const bool avail = v < 4 || (v == 4 && m->halo_col) || (v == 5 && pipe_available(m));
+      const bool avail = v < 4 || v == 6 || ((v == 4 || v == 7) && m->halo_col) || (v == 5 && pipe_available(m));
       m->spmv_variant32 = avail ? v : 0;
     } else if (!m->tuned32) {
       fg_autotune_spmv32(m, 20, nullptr, nullptr);
@@ -1287,11 +1480,15 @@ fg_status fg_bench_cg_kernel(fg_mesh *m, int which, int precision, int reps, dou
   const bool mixed = precision == FG_MIXED;
   FG_REQUIRE(mixed ? m->val32 != nullptr : m->val64 != nullptr, FG_BAD_ARG, "operator not assembled");
   timing_state(m, mixed);
+  const int v = m->spmv_variant32;
   auto body = [&](int n) {
     for (int r = 0; r < n; ++r) {
-      if (mixed) launch_iter32(m, m->spmv_variant32, (r & 1) == 0 ? false : true);
+      if (mixed && (!split32(v) || which == 3)) launch_iter32(m, v, (r & 1) != 0);
+      else if (mixed && which == 0) launch_spmv32s(m, v);
+      else if (mixed) launch_vec32s(m);
       else if (which == 0) launch_spmv64cg(m);
-      else launch_vec64(m);
+      else if (which == 1) launch_vec64(m);
+      else { launch_vec64(m); launch_spmv64cg(m); }
     }
     FG_LAUNCHED(n);
   };
@@ -1316,7 +1513,7 @@ fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_v
   int best = 0;
   double best_us = 1e30;
   for (int v = 0; v < FG_N_SPMV32; ++v) {
-    if ((v == 4 && !m->halo_col) || (v == 5 && !pipe_available(m))) {  // not available for this operator
+    if (((v == 4 || v == 7) && !m->halo_col) || (v == 5 && !pipe_available(m))) {  // not available here
       if (us_per_variant) us_per_variant[v] = 0.0;
       continue;
     }

@@ -52,10 +52,13 @@ enum {
                           of |F(u + a du)|^2, kept in [0.1, 0.5] of the last step */
 };
 /* FP32 CG iteration kernel: FG_SPMV_AUTO lets the autotuner time the variants on
- * the first mixed solve of a handle and keep the fastest; k = 1..5 forces variant
- * k-1 (1: 4x-unrolled gather loop, 256 threads; 2: all row loads issued first, 256
- * threads; 3: loop, 128 threads; 4: loop, 512 threads; 5: halo staging, the
- * neighbour entries of a block of rows gathered once into shared memory). */
+ * the first mixed solve of a handle and keep the fastest; k = 1..8 forces variant
+ * k-1.  One fused kernel per iteration: 1: 4x-unrolled gather loop, 256 threads;
+ * 2: all row loads issued first, 256 threads; 3: loop, 128 threads; 4: loop, 512
+ * threads; 5: halo staging (the neighbour entries of a block of rows gathered once
+ * into shared memory); 6: halo staging, persistent and software-pipelined (bulk
+ * copies and asynchronous gathers of the next row blocks).  Two kernels per
+ * iteration (vector pass + SpMV): 7: direct gathers; 8: halo staging. */
 enum { FG_SPMV_AUTO = 0 };
 
 typedef struct fg_mesh fg_mesh;
@@ -67,7 +70,7 @@ typedef struct fg_solve_opts {
   double inner_rtol;   /* mixed: FP32 PCG target per refinement step */
   int32_t check_every; /* iterations per graph launch between convergence checks (even) */
   int32_t use_graph;   /* 1: replay each block of iterations as a CUDA graph */
-  int32_t spmv;        /* FG_SPMV_AUTO or a forced variant 1..5 */
+  int32_t spmv;        /* FG_SPMV_AUTO or a forced variant 1..8 */
   int32_t reserved_;
 } fg_solve_opts;
 
@@ -287,8 +290,10 @@ fg_status fg_scalar_potential_newton(const double *p, int64_t nv, const int32_t 
 /* Kernel launches issued by this library so far (graph replays count every node). */
 int64_t fg_kernel_launches(void);
 /* Average device time of one launch of a hot kernel on the handle's current
- * operator: which = 0 CG SpMV, 1 CG vector update, 2 Newton element pass + row
- * gather.  No reference counterpart (used for roofline reporting). */
+ * operator: which = 0 CG SpMV with its dot products (for the fused FP32 iteration
+ * variants: the whole iteration), 1 CG vector update, 2 Newton element pass + row
+ * gather, 3 one whole CG iteration.  No reference counterpart (used for roofline
+ * reporting). */
 fg_status fg_bench_kernel(fg_mesh *m, int32_t which, int32_t precision, int32_t reps, double *ms_per_launch);
 /* Autotuner: times the CG kernel variants of one precision on the handle's current
  * operator (FG_MIXED: the 5 FP32 iteration variants; FG_FP64: direct gathers or halo
