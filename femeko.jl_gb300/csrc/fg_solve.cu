@@ -123,48 +123,58 @@ __device__ __forceinline__ void block_sum_acc(const Acc<float> (&a)[N], double (
   block_sum_ff<N>(v, out, shf);
 }
 
-// Block partials -> the last block to arrive sums them.  Returns true in thread 0 of
-// the last block, with the totals in tot.  The whole last block loads the partials
-// (independent loads), then a fixed-shape tree: the order of the sum depends only on
-// the grid size, so results are reproducible.
-// Arrival is counted in two levels so that no single counter takes one atomic per
-// block: block b arrives on counter[1 + b % 64]; the last block of each of those
-// groups arrives on counter[0]; the last of those finishes the sum and resets all
-// counters.  (Each arrival follows a __threadfence, so the finishing block sees every
-// partial.)
+// Block partials -> one total, in two parallel levels so that no single block reads
+// every partial.  Block b writes its partial and arrives on counter[1 + b % 64]; the
+// last block of each of those groups sums the group's partials (one per thread) and
+// arrives on counter[0]; the last group finisher sums the group totals.  Each sum is a
+// fixed-shape tree over a fixed index order, so results do not depend on scheduling.
+// Group totals sit right after the block partials (gridDim.x * N doubles).  Returns
+// true in thread 0 of the finishing block, with the totals in tot.
 constexpr int FG_ARRIVE_GROUPS = 64;
 
 template <int N>
 __device__ __forceinline__ bool grid_finish(const double (&v)[N], double *partials, unsigned *counter,
                                             double (&tot)[N]) {
-  __shared__ bool s_last;
+  __shared__ int s_role;
+  __shared__ double shg[N][32], shf[N][32];
+  const unsigned G = gridDim.x;
+  const unsigned grp = blockIdx.x % FG_ARRIVE_GROUPS;
+  const unsigned ngroups = G < FG_ARRIVE_GROUPS ? G : FG_ARRIVE_GROUPS;
+  const unsigned gsize = (G - grp + FG_ARRIVE_GROUPS - 1) / FG_ARRIVE_GROUPS;
+  double *gpart = partials + (size_t)G * N;
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int j = 0; j < N; ++j) partials[(size_t)blockIdx.x * N + j] = v[j];
     __threadfence();
-    const unsigned G = gridDim.x;
-    const unsigned grp = blockIdx.x % FG_ARRIVE_GROUPS;
-    const unsigned ngroups = G < FG_ARRIVE_GROUPS ? G : FG_ARRIVE_GROUPS;
-    const unsigned gsize = (G - grp + FG_ARRIVE_GROUPS - 1) / FG_ARRIVE_GROUPS;
-    bool last = false;
-    if (atomicAdd(counter + 1 + grp, 1u) == gsize - 1) {
-      __threadfence();
-      last = (atomicAdd(counter, 1u) == ngroups - 1);
-    }
-    s_last = last;
+    s_role = (atomicAdd(counter + 1 + grp, 1u) == gsize - 1) ? 1 : 0;
   }
   __syncthreads();
-  if (!s_last) return false;
+  if (s_role == 0) return false;
   __threadfence();
-  if (threadIdx.x <= FG_ARRIVE_GROUPS) counter[threadIdx.x] = 0u;
   double acc[N];
 #pragma unroll
   for (int j = 0; j < N; ++j) acc[j] = 0.0;
-  for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+  for (unsigned k = threadIdx.x; k < gsize; k += blockDim.x)
 #pragma unroll
-    for (int j = 0; j < N; ++j) acc[j] += __ldcg(partials + (size_t)b * N + j);
-  __shared__ double shfin[N][32];
-  block_sum<N>(acc, shfin);
+    for (int j = 0; j < N; ++j) acc[j] += __ldcg(partials + (size_t)(grp + k * FG_ARRIVE_GROUPS) * N + j);
+  block_sum<N>(acc, shg);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int j = 0; j < N; ++j) gpart[(size_t)grp * N + j] = acc[j];
+    counter[1 + grp] = 0u;  // every member of the group has arrived
+    __threadfence();
+    s_role = (atomicAdd(counter, 1u) == ngroups - 1) ? 2 : 0;
+  }
+  __syncthreads();
+  if (s_role != 2) return false;
+  __threadfence();
+#pragma unroll
+  for (int j = 0; j < N; ++j) acc[j] = 0.0;
+  for (unsigned g = threadIdx.x; g < ngroups; g += blockDim.x)
+#pragma unroll
+    for (int j = 0; j < N; ++j) acc[j] += __ldcg(gpart + (size_t)g * N + j);
+  block_sum<N>(acc, shf);
+  if (threadIdx.x == 0) counter[0] = 0u;
 #pragma unroll
   for (int j = 0; j < N; ++j) tot[j] = acc[j];
   return threadIdx.x == 0;
