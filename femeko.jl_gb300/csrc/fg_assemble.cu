@@ -19,6 +19,8 @@
 //   P2 mass           src/FEM3D.jl:494-561, src/FEM2D.jl:163-229 (Gauss rules below)
 #include <type_traits>
 
+#include <algorithm>
+
 #include "fg_common.cuh"
 
 // ------------------------------------------------------------------ helpers
@@ -433,6 +435,116 @@ __global__ void __launch_bounds__(128) k_elem_newton(int64_t nt, const double *_
   }
 }
 
+// ---------------------------------------------------------------- nonlinear subset
+// Newton on a mesh whose elements are mostly linear: the linear elements' part of the
+// operator does not change between Newton iterations, so it is assembled once per
+// solve and only the nonlinear (Froehlich) elements are re-evaluated.  These kernels
+// work on the list of nonlinear elements.
+
+// For nonlinear element e (mesh element k = list[e]) and local nodes a, b: the SELL
+// position of the entry (t[a], t[b]) and the row t[a].
+__global__ void k_nl_map(int n_nl, const int *__restrict__ list, int64_t nt, const int *__restrict__ t,
+                         const int *__restrict__ recpos, const uint8_t *__restrict__ in_slot,
+                         const int *__restrict__ sl_ptr, int *__restrict__ pos_out, int *__restrict__ row_out) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_nl) return;
+  const int64_t k = list[e];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const int row = t[(int64_t)a * nt + k];
+    const int64_t ip = recpos[(int64_t)a * nt + k];
+    row_out[4 * e + a] = row;
+#pragma unroll
+    for (int b = 0; b < 4; ++b)
+      pos_out[16 * e + 4 * a + b] = (int)sell_pos(sl_ptr[row / FG_SLICE], row % FG_SLICE, in_slot[ip * 4 + b]);
+  }
+}
+
+// The Froehlich elements of k_elem_newton: mu, dmu, the local residual VE mu G d
+// (re, 4 per element) and, when ke != null, the local Jacobian VE mu G + ct w w^T
+// (16 per element), all FP64.
+__global__ void __launch_bounds__(128) k_elem_newton_nl(int n_nl, const int *__restrict__ list, int64_t nt,
+                                                        const double *__restrict__ geo, const int *__restrict__ t,
+                                                        const double *__restrict__ u, double Ms, double Hk,
+                                                        double *__restrict__ mu_out, double *__restrict__ dmu_out,
+                                                        double *__restrict__ re, double *__restrict__ ke, int tangent,
+                                                        int *flags) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_nl) return;
+  const int64_t k = list[e];
+  double G[10];
+#pragma unroll
+  for (int c = 0; c < 10; ++c) G[c] = geo[(int64_t)(13 + c) * nt + k];
+  const double VE = geo[12 * nt + k];
+  double uu[4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) uu[a] = u[t[(int64_t)a * nt + k]];
+  const double d1 = uu[1] - uu[0], d2 = uu[2] - uu[0], d3 = uu[3] - uu[0];
+  double w[4];
+  w[0] = G[1] * d1 + G[2] * d2 + G[3] * d3;
+  w[1] = G[4] * d1 + G[5] * d2 + G[6] * d3;
+  w[2] = G[5] * d1 + G[7] * d2 + G[8] * d3;
+  w[3] = G[6] * d1 + G[8] * d2 + G[9] * d3;
+  const double h2 = fmax(d1 * w[1] + d2 * w[2] + d3 * w[3], 0.0);
+  const double ih = rsqrt_nr(h2);
+  const double h = h2 * ih;
+  const double inv = rcp_nr(Hk + h);
+  const double mu = FG_MU0 * fma(Ms, inv, 1.0);
+  const double dmu = -FG_MU0 * Ms * inv * inv;
+  if (!isfinite(mu) || !isfinite(dmu)) atomicOr(flags, FLAG_NAN);
+  mu_out[k] = mu;
+  dmu_out[k] = dmu;
+  const double vm = VE * mu;
+#pragma unroll
+  for (int a = 0; a < 4; ++a) re[4 * e + a] = vm * w[a];
+  if (ke == nullptr) return;
+  const double ct = tangent ? VE * dmu * ih : 0.0;
+  const int idx[4][4] = {{0, 1, 2, 3}, {1, 4, 5, 6}, {2, 5, 7, 8}, {3, 6, 8, 9}};
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) ke[16 * e + 4 * a + b] = fma(ct * w[a], w[b], vm * G[idx[a][b]]);
+}
+
+// y[row] += the nonlinear elements' residual records of the row, in a fixed order
+// (rows listed once; Dirichlet rows untouched).
+__global__ void k_nl_rows(int n_rows, const int *__restrict__ rows, const int *__restrict__ ptr,
+                          const int *__restrict__ src, const double *__restrict__ re,
+                          const uint8_t *__restrict__ fixed, double *__restrict__ y) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_rows) return;
+  const int i = rows[r];
+  if (fixed && fixed[i]) return;
+  double s = 0.0;
+  for (int q = ptr[r]; q < ptr[r + 1]; ++q) s += re[src[q]];
+  y[i] += s;
+}
+
+// val[pos] = lin[pos] + the nonlinear elements' entries at that position (fixed
+// order); on the diagonal also the Jacobi inverse.  code >= 0: the row of an
+// off-diagonal slot; code < 0: ~row of a diagonal slot.  Dirichlet rows keep their
+// identity rows.
+template <typename T>
+__global__ void k_nl_slots(int n_slots, const int *__restrict__ pos, const int *__restrict__ ptr,
+                           const int *__restrict__ src, const int *__restrict__ code, const double *__restrict__ lin,
+                           const double *__restrict__ ke, const uint8_t *__restrict__ fixed, T *__restrict__ val,
+                           T *__restrict__ dinv) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n_slots) return;
+  const int c = code[q];
+  const int row = c >= 0 ? c : ~c;
+  if (fixed && fixed[row]) return;
+  const int p = pos[q];
+  double v = lin[p];
+  for (int j = ptr[q]; j < ptr[q + 1]; ++j) v += ke[src[j]];
+  val[p] = (T)v;
+  if (c < 0) dinv[row] = (T)(v != 0.0 ? 1.0 / v : 0.0);
+}
+template __global__ void k_nl_slots<float>(int, const int *, const int *, const int *, const int *, const double *,
+                                           const double *, const uint8_t *, float *, float *);
+template __global__ void k_nl_slots<double>(int, const int *, const int *, const int *, const int *, const double *,
+                                            const double *, const uint8_t *, double *, double *);
+
 // Energy density integral of H dB times VE (src/magneticProperties.jl:252-309, FEMM
 // style) in closed form: linear elements mu |H|^2 / 2, Froehlich elements
 // mu0 [|H|^2/2 + Ms Hk (ln(1 + |H|/Hk) + Hk/(Hk + |H|) - 1)].
@@ -762,6 +874,167 @@ void fg_newton_assemble(fg_mesh *m, const double *d_u, double Ms, double Hk, boo
     FG_LAUNCHED(1);
     launch_row<4, double, double>(m, rec, m->rec_r, 1, m->val64, nullptr, nullptr, m->dinv64, nullptr, d_F, -1.0, 1);
   }
+}
+
+__global__ void k_negate64(int64_t n, double *__restrict__ x) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = -x[i];
+}
+
+__global__ void k_linear_coef(int64_t nt, const double *__restrict__ mu_lin, const uint8_t *__restrict__ nl,
+                              double *__restrict__ coef, double *__restrict__ mu, double *__restrict__ dmu) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt) return;
+  coef[k] = nl[k] ? 0.0 : mu_lin[k];
+  mu[k] = mu_lin[k];
+  dmu[k] = 0.0;
+}
+
+void fg_nl_setup(fg_mesh *m, const uint8_t *nl_host, bool mixed) {
+  FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "Newton magnetostatics needs P1 tetrahedra");
+  fg_ensure_records(m);
+  const int64_t nt = m->nt;
+  std::vector<int> list;
+  for (int64_t k = 0; k < nt; ++k)
+    if (nl_host[k]) list.push_back((int)k);
+  if (!m->nl_maps_valid || list != m->nl_list_host) {
+    const int n = (int)list.size();
+    if (n > m->nl_cap) {
+      const int cap = std::max(n, 64);
+      m->nl_elems = dev_alloc<int>(m, (size_t)cap);
+      m->nl_re = dev_alloc<double>(m, 4 * (size_t)cap);
+      m->nl_ke = dev_alloc<double>(m, 16 * (size_t)cap);
+      m->nl_slot_pos = dev_alloc<int>(m, 16 * (size_t)cap);
+      m->nl_slot_ptr = dev_alloc<int>(m, 16 * (size_t)cap + 1);
+      m->nl_slot_src = dev_alloc<int>(m, 16 * (size_t)cap);
+      m->nl_slot_code = dev_alloc<int>(m, 16 * (size_t)cap);
+      m->nl_rows = dev_alloc<int>(m, 4 * (size_t)cap);
+      m->nl_row_ptr = dev_alloc<int>(m, 4 * (size_t)cap + 1);
+      m->nl_row_src = dev_alloc<int>(m, 4 * (size_t)cap);
+      m->nl_cap = cap;
+    }
+    m->n_nl = n;
+    m->n_nl_slots = m->n_nl_rows = 0;
+    if (n > 0) {
+      FG_CUDA_TRY(cudaMemcpyAsync(m->nl_elems, list.data(), sizeof(int) * n, cudaMemcpyHostToDevice, m->stream));
+      // positions and rows into the (not yet used) CSR buffers, then grouped on the host
+      k_nl_map<<<grid_for(n, 128), 128, 0, m->stream>>>(n, m->nl_elems, nt, m->t, m->recpos, m->in_slot, m->sl_ptr,
+                                                         m->nl_slot_src, m->nl_row_src);
+      FG_CUDA_TRY(cudaGetLastError());
+      FG_LAUNCHED(1);
+      std::vector<int> pos(16 * (size_t)n), rows(4 * (size_t)n);
+      FG_CUDA_TRY(cudaMemcpyAsync(pos.data(), m->nl_slot_src, sizeof(int) * pos.size(), cudaMemcpyDeviceToHost,
+                                  m->stream));
+      FG_CUDA_TRY(cudaMemcpyAsync(rows.data(), m->nl_row_src, sizeof(int) * rows.size(), cudaMemcpyDeviceToHost,
+                                  m->stream));
+      fg_sync(m);
+      // slots: sources (e, a, b) grouped by position, in source order within a position
+      std::vector<int> ord(pos.size());
+      for (size_t q = 0; q < ord.size(); ++q) ord[q] = (int)q;
+      std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return pos[x] < pos[y]; });
+      std::vector<int> spos, sptr, scode, ssrc(ord.size());
+      for (size_t q = 0; q < ord.size(); ++q) {
+        const int src = ord[q];
+        ssrc[q] = src;
+        if (q == 0 || pos[src] != pos[ord[q - 1]]) {
+          const int e = src / 16, a = (src / 4) % 4, b = src % 4;
+          const int row = rows[4 * e + a];
+          spos.push_back(pos[src]);
+          sptr.push_back((int)q);
+          scode.push_back(a == b ? ~row : row);
+        }
+      }
+      sptr.push_back((int)ord.size());
+      // rows: sources (e, a) grouped by row
+      std::vector<int> rord(rows.size());
+      for (size_t q = 0; q < rord.size(); ++q) rord[q] = (int)q;
+      std::stable_sort(rord.begin(), rord.end(), [&](int x, int y) { return rows[x] < rows[y]; });
+      std::vector<int> rlist, rptr;
+      for (size_t q = 0; q < rord.size(); ++q)
+        if (q == 0 || rows[rord[q]] != rows[rord[q - 1]]) {
+          rlist.push_back(rows[rord[q]]);
+          rptr.push_back((int)q);
+        }
+      rptr.push_back((int)rord.size());
+      m->n_nl_slots = (int)spos.size();
+      m->n_nl_rows = (int)rlist.size();
+      auto up = [&](int *dst, const std::vector<int> &v) {
+        FG_CUDA_TRY(cudaMemcpyAsync(dst, v.data(), sizeof(int) * v.size(), cudaMemcpyHostToDevice, m->stream));
+      };
+      up(m->nl_slot_pos, spos);
+      up(m->nl_slot_ptr, sptr);
+      up(m->nl_slot_code, scode);
+      up(m->nl_slot_src, ssrc);
+      up(m->nl_rows, rlist);
+      up(m->nl_row_ptr, rptr);
+      up(m->nl_row_src, rord);
+      fg_sync(m);
+    }
+    m->nl_list_host = list;
+    m->nl_maps_valid = true;
+  }
+  // the linear elements' operator (nonlinear elements contribute 0), Dirichlet rows
+  // applied; element state starts at the linear values
+  double *coef = m->objbuf ? m->objbuf : (m->objbuf = dev_alloc<double>(m, 2 * (size_t)nt));
+  k_linear_coef<<<grid_for(nt, 256), 256, 0, m->stream>>>(nt, m->mu_lin, m->nl, coef, m->mu, m->dmu);
+  FG_LAUNCHED(1);
+  fg_assemble_operator(m, ASM_STIFF, coef, nullptr, nullptr, 0.0, 0.0, 0, OUT_SELL, true, mixed, true);
+  if (!m->vlin64) m->vlin64 = dev_alloc<double>(m, (size_t)m->nsell);
+  if (!m->dlin64) m->dlin64 = dev_alloc<double>(m, (size_t)m->nvp);
+  FG_CUDA_TRY(cudaMemcpyAsync(m->vlin64, m->val64, sizeof(double) * (size_t)m->nsell, cudaMemcpyDeviceToDevice,
+                              m->stream));
+  FG_CUDA_TRY(cudaMemcpyAsync(m->dlin64, m->dinv64, sizeof(double) * (size_t)m->nvp, cudaMemcpyDeviceToDevice,
+                              m->stream));
+  if (mixed) {
+    if (!m->vlin32) m->vlin32 = dev_alloc<float>(m, (size_t)m->nsell);
+    if (!m->dlin32) m->dlin32 = dev_alloc<float>(m, (size_t)m->nvp);
+    FG_CUDA_TRY(cudaMemcpyAsync(m->vlin32, m->val32, sizeof(float) * (size_t)m->nsell, cudaMemcpyDeviceToDevice,
+                                m->stream));
+    FG_CUDA_TRY(cudaMemcpyAsync(m->dlin32, m->dinv32, sizeof(float) * (size_t)m->nvp, cudaMemcpyDeviceToDevice,
+                                m->stream));
+  }
+}
+
+void fg_newton_assemble_split(fg_mesh *m, const double *d_u, double Ms, double Hk, bool mixed, double *d_F,
+                              bool want_jacobian, bool tangent) {
+  FG_REQUIRE(m->vlin64 != nullptr && m->nl_maps_valid, FG_BAD_ARG, "Newton split: no linear operator");
+  const int n = m->n_nl;
+  const uint8_t *fx = m->has_fixed ? m->fixed : nullptr;
+  // F = -(K_lin u + the nonlinear elements' K_e(mu(u)) u_e), Dirichlet rows 0
+  fg_spmv64_vals(m, m->vlin64, d_u, d_F);
+  if (n > 0) {
+    k_elem_newton_nl<<<grid_for(n, 128), 128, 0, m->stream>>>(n, m->nl_elems, m->nt, m->geo, m->t, d_u, Ms, Hk,
+                                                              m->mu, m->dmu, m->nl_re,
+                                                              want_jacobian ? m->nl_ke : nullptr, tangent ? 1 : 0,
+                                                              m->flags);
+    k_nl_rows<<<grid_for(m->n_nl_rows, 128), 128, 0, m->stream>>>(m->n_nl_rows, m->nl_rows, m->nl_row_ptr,
+                                                                  m->nl_row_src, m->nl_re, fx, d_F);
+    FG_LAUNCHED(2);
+  }
+  k_negate64<<<grid_for(m->nv, 256), 256, 0, m->stream>>>(m->nv, d_F);
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(1);
+  if (!want_jacobian) return;
+  const unsigned gs = grid_for(std::max(m->n_nl_slots, 1), 128);
+  if (mixed) {
+    FG_CUDA_TRY(cudaMemcpyAsync(m->val32, m->vlin32, sizeof(float) * (size_t)m->nsell, cudaMemcpyDeviceToDevice,
+                                m->stream));
+    FG_CUDA_TRY(cudaMemcpyAsync(m->dinv32, m->dlin32, sizeof(float) * (size_t)m->nvp, cudaMemcpyDeviceToDevice,
+                                m->stream));
+    if (n > 0)
+      k_nl_slots<float><<<gs, 128, 0, m->stream>>>(m->n_nl_slots, m->nl_slot_pos, m->nl_slot_ptr, m->nl_slot_src,
+                                                   m->nl_slot_code, m->vlin64, m->nl_ke, fx, m->val32, m->dinv32);
+  } else {
+    FG_CUDA_TRY(cudaMemcpyAsync(m->val64, m->vlin64, sizeof(double) * (size_t)m->nsell, cudaMemcpyDeviceToDevice,
+                                m->stream));
+    FG_CUDA_TRY(cudaMemcpyAsync(m->dinv64, m->dlin64, sizeof(double) * (size_t)m->nvp, cudaMemcpyDeviceToDevice,
+                                m->stream));
+    if (n > 0)
+      k_nl_slots<double><<<gs, 128, 0, m->stream>>>(m->n_nl_slots, m->nl_slot_pos, m->nl_slot_ptr, m->nl_slot_src,
+                                                    m->nl_slot_code, m->vlin64, m->nl_ke, fx, m->val64, m->dinv64);
+  }
+  FG_CUDA_TRY(cudaGetLastError());
+  if (n > 0) FG_LAUNCHED(1);
 }
 
 void fg_apply_operator_vec(fg_mesh *m, int kind, const double *d_coef, double c_mass, double c_stiff,

@@ -172,6 +172,17 @@ struct fg_mesh {
   double *mu = nullptr, *dmu = nullptr, *H = nullptr, *wdens = nullptr;
   double *mu_lin = nullptr;
   uint8_t *nl = nullptr;
+  // Newton with a few nonlinear elements: the linear elements' operator (with the
+  // Dirichlet rows) assembled once per solve, and the maps of the nonlinear ones
+  double *vlin64 = nullptr, *dlin64 = nullptr;  // SELL values / Jacobi inverses
+  float *vlin32 = nullptr, *dlin32 = nullptr;
+  int n_nl = 0, nl_cap = 0, n_nl_slots = 0, n_nl_rows = 0;
+  int *nl_elems = nullptr;                       // nonlinear element indices
+  int *nl_slot_pos = nullptr, *nl_slot_ptr = nullptr, *nl_slot_src = nullptr, *nl_slot_code = nullptr;
+  int *nl_rows = nullptr, *nl_row_ptr = nullptr, *nl_row_src = nullptr;
+  double *nl_re = nullptr, *nl_ke = nullptr;     // 4 / 16 per nonlinear element
+  std::vector<int> nl_list_host;                 // the list the maps were built for
+  bool nl_maps_valid = false;
   uint8_t *target = nullptr;  // nt objective mask (adjoint)
   double *objbuf = nullptr;   // 2 x nt objective scratch (adjoint)
 
@@ -228,6 +239,15 @@ void fg_ensure_records(fg_mesh *m);
 // Jacobian K + At in the operator (FP32 when mixed) with its Jacobi diagonal.
 void fg_newton_assemble(fg_mesh *m, const double *d_u, double Ms, double Hk, bool mixed, double *d_F,
                         bool want_jacobian = true, bool tangent = true);
+// Newton on the linear/nonlinear split: fg_nl_setup (once per solve, after mu_lin and
+// nl are on the device; nl_host is the same mask on the host) assembles the linear
+// elements' operator and the nonlinear elements' maps; fg_newton_assemble_split then
+// has the contract of fg_newton_assemble.
+void fg_nl_setup(fg_mesh *m, const uint8_t *nl_host, bool mixed);
+void fg_newton_assemble_split(fg_mesh *m, const double *d_u, double Ms, double Hk, bool mixed, double *d_F,
+                              bool want_jacobian, bool tangent);
+// y = vals x on the handle's pattern (FP64), Dirichlet rows 0.
+void fg_spmv64_vals(fg_mesh *m, const double *vals, const double *x, double *y);
 void fg_apply_operator_vec(fg_mesh *m, int kind, const double *d_coef, double c_mass, double c_stiff,
                            const double *d_x, double *d_y, bool zero_fixed);
 void fg_hfield_dev(fg_mesh *m, const double *d_u, double *d_H);

@@ -3,8 +3,11 @@
 // Femeko_jl_C++/Magnetostatics/magnetostatics.cpp:49-95) and the Newton-Raphson
 // iteration of Magnetostatics/NewtonRaphson.jl:109-214, both with Dirichlet rows.
 //
-// Newton step: the element pass computes H, mu, dmu, the residual F = -K(mu(u)) u and
-// the Jacobian K(mu) + At(H, dmu) in one launch; the row pass sums them.  The inner
+// Newton step: the residual F = -K(mu(u)) u and the Jacobian K(mu) + At(H, dmu).  The
+// linear elements' part of K is assembled once per solve (mu fixed there); each
+// residual is that operator's FP64 SpMV plus the nonlinear (Froehlich) elements
+// re-evaluated and summed into their rows, and each Jacobian is a copy of the linear
+// operator with the nonlinear elements' entries added at their slots.  The inner
 // increment solve J du = F runs to a relative residual inner_rtol in FP32 (mixed)
 // or FP64; F is always FP64, so the Newton loop is the iterative refinement.
 // Step control follows src/FEM3D.jl:123-152 (alpha = 1, 0.9, 0.81, ... while the
@@ -63,7 +66,8 @@ static void ensure_element_state(fg_mesh *m) {
 
 // Device-resident Newton solve; u (device) holds the initial guess and receives the
 // solution.  Element state (H, mu, dmu) is left at the solution.
-static int newton_dev(fg_mesh *m, double *d_u, const fg_newton_opts &o, fg_newton_stats *st) {
+static int newton_dev(fg_mesh *m, double *d_u, const uint8_t *nl_host, const fg_newton_opts &o,
+                      fg_newton_stats *st) {
   const bool mixed = o.precision == FG_MIXED;
   double *d_du = vec64(m, 8), *d_F = vec64(m, 9), *d_ut = vec64(m, 10), *d_Ft = vec64(m, 11);
   fg_solve_opts so;
@@ -80,7 +84,10 @@ static int newton_dev(fg_mesh *m, double *d_u, const fg_newton_opts &o, fg_newto
   FG_CUDA_TRY(cudaEventCreate(&e1));
   FG_CUDA_TRY(cudaEventRecord(e0, m->stream));
 
-  fg_newton_assemble(m, d_u, o.Ms, o.Hk, mixed, d_F, true, o.picard_steps <= 0);
+  // the linear elements' operator once; each residual / Jacobian below re-evaluates
+  // only the nonlinear elements on top of it
+  fg_nl_setup(m, nl_host, mixed);
+  fg_newton_assemble_split(m, d_u, o.Ms, o.Hk, mixed, d_F, true, o.picard_steps <= 0);
   fg_check_flags(m, "fg_newton_magnetostatics");
   double rF = fg_norm2_dev(m, d_F, nv, true);
   int it = 0, cg_total = 0, trials = 0, converged = 0, status = 0;
@@ -118,7 +125,7 @@ static int newton_dev(fg_mesh *m, double *d_u, const fg_newton_opts &o, fg_newto
       for (;;) {
         k_axpby64<<<g, 256, 0, m->stream>>>(nv, 1.0, d_u, alpha, d_du, d_ut);
         FG_LAUNCHED(1);
-        fg_newton_assemble(m, d_ut, o.Ms, o.Hk, mixed, d_Ft, trial_jacobian, next_tangent);
+        fg_newton_assemble_split(m, d_ut, o.Ms, o.Hk, mixed, d_Ft, trial_jacobian, next_tangent);
         rt = fg_norm2_dev(m, d_Ft, nv, true);
         ++trials;
         if (o.line_search == FG_LS_NONE || !(rt > rF && alpha > o.min_step)) break;
@@ -135,7 +142,7 @@ static int newton_dev(fg_mesh *m, double *d_u, const fg_newton_opts &o, fg_newto
       }
       if (alpha < o.min_step) {
         // no decrease: keep u (src/FEM3D.jl:144-147) and restore the state at u
-        fg_newton_assemble(m, d_u, o.Ms, o.Hk, mixed, d_F, true, it > o.picard_steps);
+        fg_newton_assemble_split(m, d_u, o.Ms, o.Hk, mixed, d_F, true, it > o.picard_steps);
         status = 1;
         alpha = 0.0;
         break;
@@ -162,7 +169,7 @@ static int newton_dev(fg_mesh *m, double *d_u, const fg_newton_opts &o, fg_newto
       if (alpha < o.min_step) { status = 1; alpha = 0.0; break; }
       k_axpby64<<<g, 256, 0, m->stream>>>(nv, 1.0, d_u, alpha, d_du, d_u);
       FG_LAUNCHED(1);
-      fg_newton_assemble(m, d_u, o.Ms, o.Hk, mixed, d_F, true, next_tangent);
+      fg_newton_assemble_split(m, d_u, o.Ms, o.Hk, mixed, d_F, true, next_tangent);
       rF = fg_norm2_dev(m, d_F, nv, true);
     }
     fg_check_flags(m, "fg_newton_magnetostatics");
@@ -171,7 +178,7 @@ static int newton_dev(fg_mesh *m, double *d_u, const fg_newton_opts &o, fg_newto
     ratio = (un > 0.0) ? dn / un : dn;
     if (!std::isfinite(ratio)) throw FgError{FG_NAN, "Newton update is not finite"};
     if (ratio <= o.tol_update) { converged = 1; break; }
-    if (need_jacobian) fg_newton_assemble(m, d_u, o.Ms, o.Hk, mixed, d_F, true, next_tangent);
+    if (need_jacobian) fg_newton_assemble_split(m, d_u, o.Ms, o.Hk, mixed, d_F, true, next_tangent);
   }
   fg_energy_dev(m, d_u, o.Ms, o.Hk);
   double energy = fg_dot_dev(m, m->wdens, nullptr, m->nt, false);
@@ -212,7 +219,7 @@ extern "C" fg_status fg_newton_magnetostatics(fg_mesh *m, const uint8_t *nl, con
     upload(m, m->mu_lin, mu_lin, sizeof(double) * (size_t)m->nt);
     double *d_u = vec64(m, 7);
     upload(m, d_u, u0, sizeof(double) * (size_t)m->nv);
-    int rc = newton_dev(m, d_u, opts, s);
+    int rc = newton_dev(m, d_u, nl, opts, s);
     download(m, u, d_u, sizeof(double) * (size_t)m->nv);
     if (H) {
       fg_hfield_dev(m, d_u, m->H);
@@ -303,7 +310,7 @@ extern "C" fg_status fg_adjoint_dJdmu(fg_mesh *m, const double *mur, const doubl
     } else {
       upload(m, m->nl, nl, (size_t)nt);
       fg_newton_stats ns{};
-      converged = newton_dev(m, d_u, opts, &ns) == 0;
+      converged = newton_dev(m, d_u, nl, opts, &ns) == 0;
       fwd_iters = ns.cg_iters;
       newton_iters = ns.newton_iters;
       // the Jacobian at the converged state: FP64 for the refinement residual, FP32

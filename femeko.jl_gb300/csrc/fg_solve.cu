@@ -957,11 +957,22 @@ static void spmv64_launch(fg_mesh *m, const double *x, const double *b, double *
 
 void fg_spmv64_dev(fg_mesh *m, const double *x, double *y) { spmv64_launch(m, x, nullptr, y, nullptr, -1); }
 
+void fg_spmv64_vals(fg_mesh *m, const double *vals, const double *x, double *y) {
+  const uint8_t *fx = m->has_fixed ? m->fixed : nullptr;
+  if (m->use_dcol)
+    k_spmv64<ColRel><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, vals, x, nullptr, y,
+                                                         fx, -1, m->scal, m->red.partials, m->red.counter);
+  else
+    k_spmv64<ColAbs><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col, vals, x, nullptr, y,
+                                                         fx, -1, m->scal, m->red.partials, m->red.counter);
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(1);
+}
+
 // CG vectors, padded to whole slices and zeroed once (pads stay zero).
-// FP32: v32[0] x, v32[1] p, v32[2] / v32[3] the two (r, w, s, dinv) state buffers.
+// FP32: v32[0] x, v32[1] p, v32[2] / v32[3] the two (r, w, s, dinv) state buffers of
+// the fused iteration; the split iteration uses v32[4] r, [5] w, [6] s, [7] u.
 // FP64: v64[0] x, v64[1] r, v64[2] u, v64[3] s, v64[4] p, v64[12] w.
-// FP32 CG vectors: [0] x, [1] p, [2] [3] float4 states of the fused iteration;
-// the split iteration uses [4] r, [5] w, [6] s, [7] u.
 static void ensure_cg32(fg_mesh *m) {
   for (int j = 0; j < 8; ++j)
     if (!m->v32[j]) {
