@@ -251,9 +251,10 @@ def run_ours(args):
     L.check(lib.fg_bench_kernel(g.h, 0, L.FG_MIXED, 200, C.byref(ms_spmv)))
     L.check(lib.fg_bench_kernel(g.h, 3, L.FG_MIXED, 200, C.byref(ms_iter)))
     kernels_us = {"cg32_spmv": ms_spmv.value * 1e3, "cg32_iteration": ms_iter.value * 1e3}
-    for name, which, prec in (("newton_assembly_f32", 2, L.FG_MIXED),):
+    for name, which in (("newton_element_pass_all_f32", 2), ("newton_residual_split", 4),
+                        ("newton_residual_jacobian_split_f32", 5)):
         t = C.c_double()
-        L.check(lib.fg_bench_kernel(g.h, which, prec, 20 if which == 2 else 200, C.byref(t)))
+        L.check(lib.fg_bench_kernel(g.h, which, L.FG_MIXED, 20, C.byref(t)))
         kernels_us[name] = t.value * 1e3
     fg.newton_magnetostatics(mesh, nl, mu_lin, u0, precision="fp64")   # leaves J64 on the handle
     ch64, us64 = C.c_int32(), np.zeros(2)
@@ -398,9 +399,10 @@ def case_newton_kernels(args):
     for prec in ("mixed", "fp64"):
         u, H, mu, st = fg.newton_magnetostatics(mesh, nl, mu_lin, u0, precision=prec)
         P = L.FG_MIXED if prec == "mixed" else L.FG_FP64
-        for which, name in ((0, "cg_spmv"), (1, "cg_update"), (2, "newton_assembly")):
+        for which, name in ((0, "cg_spmv"), (1, "cg_update"), (2, "newton_element_pass_all"),
+                            (4, "newton_residual_split"), (5, "newton_residual_jacobian_split")):
             t = C.c_double()
-            L.check(lib.fg_bench_kernel(g.h, which, P, 5 if which < 2 else 2, C.byref(t)))
+            L.check(lib.fg_bench_kernel(g.h, which, P, 5 if which < 2 else 3, C.byref(t)))
             out[f"{prec}_{name}_us"] = t.value * 1e3
     _line("Newton hot-kernel launch times", out["mixed_cg_spmv_us"], "us", False,
           {"workload": f"nonlinear Froehlich-plate magnetostatics, Kuhn tets {args.cells}^3 cells"}, {"kernels": out})

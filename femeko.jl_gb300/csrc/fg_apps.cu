@@ -26,8 +26,12 @@ extern "C" fg_status fg_scalar_potential_newton(const double *p, int64_t nv, con
 //   which = 0: CG SpMV with its dot products (w = A u; the whole iteration for the
 //              fused FP32 variants);
 //   which = 1: CG vector update (fused FP32 variants: the whole iteration);
-//   which = 2: Newton element pass + row gather at the current potential;
-//   which = 3: one whole CG iteration.
+//   which = 2: Newton element pass + row gather over all elements at the current
+//              potential (residual and Jacobian);
+//   which = 3: one whole CG iteration;
+//   which = 4: Newton residual on the linear/nonlinear split (FP64 SpMV of the
+//              linear elements' operator + the nonlinear elements);
+//   which = 5: the same with the Jacobian.
 fg_status fg_bench_cg_kernel(fg_mesh *m, int which, int precision, int reps, double *ms_per_launch);
 
 extern "C" fg_status fg_bench_kernel(fg_mesh *m, int32_t which, int32_t precision, int32_t reps,
@@ -35,12 +39,18 @@ extern "C" fg_status fg_bench_kernel(fg_mesh *m, int32_t which, int32_t precisio
   return fg_guard([&]() -> fg_status {
     FG_REQUIRE(m && ms_per_launch && reps > 0, FG_BAD_ARG, "fg_bench_kernel: bad argument");
     if (which == 0 || which == 1 || which == 3) return fg_bench_cg_kernel(m, which, precision, reps, ms_per_launch);
-    FG_REQUIRE(which == 2, FG_BAD_ARG, "fg_bench_kernel: unknown kernel");
+    FG_REQUIRE(which == 2 || which == 4 || which == 5, FG_BAD_ARG, "fg_bench_kernel: unknown kernel");
     FG_REQUIRE(m->v64[7] && m->mu, FG_BAD_ARG, "fg_bench_kernel: run a Newton solve on this handle first");
+    FG_REQUIRE(which == 2 || m->nl_maps_valid, FG_BAD_ARG, "fg_bench_kernel: run a Newton solve on this handle first");
     if (!m->v64[11]) m->v64[11] = dev_alloc<double>(m, (size_t)m->nv);
-    fg_newton_assemble(m, m->v64[7], 1.2e6, 500.0, precision == FG_MIXED, m->v64[11]);
+    const bool mixed = precision == FG_MIXED;
+    auto once = [&]() {
+      if (which == 2) fg_newton_assemble(m, m->v64[7], 1.2e6, 500.0, mixed, m->v64[11]);
+      else fg_newton_assemble_split(m, m->v64[7], 1.2e6, 500.0, mixed, m->v64[11], which == 5, true);
+    };
+    once();
     FG_CUDA_TRY(cudaEventRecord(m->ev0, m->stream));
-    for (int r = 0; r < reps; ++r) fg_newton_assemble(m, m->v64[7], 1.2e6, 500.0, precision == FG_MIXED, m->v64[11]);
+    for (int r = 0; r < reps; ++r) once();
     FG_CUDA_TRY(cudaEventRecord(m->ev1, m->stream));
     fg_sync(m);
     float ms = 0.f;

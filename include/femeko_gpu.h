@@ -292,8 +292,9 @@ int64_t fg_kernel_launches(void);
 /* Average device time of one launch of a hot kernel on the handle's current
  * operator: which = 0 CG SpMV with its dot products (for the fused FP32 iteration
  * variants: the whole iteration), 1 CG vector update, 2 Newton element pass + row
- * gather, 3 one whole CG iteration.  No reference counterpart (used for roofline
- * reporting). */
+ * gather over all elements, 3 one whole CG iteration, 4 Newton residual on the
+ * linear/nonlinear split, 5 the same with the Jacobian (4, 5: after a Newton solve).
+ * No reference counterpart (used for roofline reporting). */
 fg_status fg_bench_kernel(fg_mesh *m, int32_t which, int32_t precision, int32_t reps, double *ms_per_launch);
 /* Autotuner: times the CG kernel variants of one precision on the handle's current
  * operator (FG_MIXED: the 5 FP32 iteration variants; FG_FP64: direct gathers or halo
