@@ -200,6 +200,41 @@ function cg(A::SparseMatrixCSC{Float64,Int64}, b::Vector{Float64}; reltol=sqrt(e
     return x
 end
 
+"""heat_be(mesh, T, kappa, fixed; rho_c=1.0, dt=1e-3, nsteps=100, every=10, precision=:mixed)
+-- the backward-Euler loop of Heat/heat3D.jl:83-89 with T = 0 on the `fixed` nodes.
+Returns (T after nsteps, snapshots nv x (nsteps ÷ every), stats)."""
+function heat_be(mesh, T0::Vector{Float64}, kappa::Vector{Float64}, fixed::Vector{UInt8}; rho_c=1.0, dt=1e-3,
+                 nsteps::Integer=100, every::Integer=10, precision::Symbol=:mixed, rtol=1e-10)
+    g = gpu(mesh)
+    set_dirichlet!(g, fixed)
+    T = copy(T0)
+    snaps = zeros(g.nv, every > 0 ? nsteps ÷ every : 0)
+    o = Ref(solve_opts(precision=precision, rtol=rtol))
+    s = Ref{SolveStats}()
+    st = ccall((:fg_heat_be, libpath()), Cint,
+               (Ptr{Cvoid}, Ptr{Float64}, Float64, Float64, Int32, Ptr{Float64}, Int32, Ptr{Float64},
+                Ref{SolveOpts}, Ref{SolveStats}),
+               g.h, kappa, rho_c, dt, nsteps, T, every, isempty(snaps) ? C_NULL : snaps, o, s)
+    check(st; allow_not_converged=true)
+    return T, snaps, s[]
+end
+
+"""magnetostatics_sweep(mesh, mu, H0, fixed) -- potentials for every applied field
+(columns of H0, 3 x nfield, nfield <= 256) of the linear problem
+Magnetostatics/magneticField.jl:89-132, solved together; returns U (nv x nfield)."""
+function magnetostatics_sweep(mesh, mu::Vector{Float64}, H0::Matrix{Float64}, fixed::Vector{UInt8}; rtol=1e-10)
+    g = gpu(mesh)
+    set_dirichlet!(g, fixed)
+    U = zeros(g.nv, size(H0, 2))
+    o = Ref(solve_opts(precision=:mixed, rtol=rtol))
+    s = Ref{SolveStats}()
+    st = ccall((:fg_magnetostatics_sweep, libpath()), Cint,
+               (Ptr{Cvoid}, Ptr{Float64}, Int32, Ptr{Float64}, Ref{SolveOpts}, Ptr{Float64}, Ref{SolveStats}),
+               g.h, mu, size(H0, 2), H0, o, U, s)
+    check(st; allow_not_converged=true)
+    return U
+end
+
 """Newton-Raphson magnetostatics (Magnetostatics/NewtonRaphson.jl:109-214) with
 Dirichlet nodes `fixed` holding u0.  Returns (u, Hfield 3 x nt, mu, stats)."""
 function newton_magnetostatics(mesh, fixed::Vector{UInt8}, nl::Vector{UInt8}, mu_lin::Vector{Float64},
