@@ -190,6 +190,10 @@ def run_ours(args):
     t0 = time.time()
     g = fg.gpu_mesh(mesh)
     t_setup = time.time() - t0
+    if args.cg_variant:
+        L.check(lib.fg_set_cg_variant(g.h, L.FG_MIXED, args.cg_variant))
+    if args.cg64_variant:
+        L.check(lib.fg_set_cg_variant(g.h, L.FG_FP64, args.cg64_variant))
 
     def solve(precision):
         u, H, mu, st = fg.newton_magnetostatics(mesh, nl, mu_lin, u0, precision=precision)
@@ -242,11 +246,12 @@ def run_ours(args):
     lib.fg_mesh_layout(g.h, C.byref(nsell), C.byref(ninc), C.byref(nsl))
     fg.newton_magnetostatics(mesh, nl, mu_lin, u0, precision="mixed")   # leaves J32 on the handle
     chosen = C.c_int32()
-    variants_us = np.zeros(8)
-    L.check(lib.fg_autotune(g.h, L.FG_MIXED, C.byref(chosen), L.ptr(variants_us), 8))
+    variants_us = np.zeros(9)
+    L.check(lib.fg_autotune(g.h, L.FG_MIXED, C.byref(chosen), L.ptr(variants_us), 9))
     autotune = {"cg32_iteration_variants_us": [round(float(v), 2) for v in variants_us], "chosen": int(chosen.value),
                 "names": ["fused gather/256", "fused gather-hoist/256", "fused gather/128", "fused gather/512",
-                          "fused halo-smem", "fused halo-smem-pipelined", "split gather/256", "split halo-smem"]}
+                          "fused halo-smem", "fused halo-smem-pipelined", "split gather/256", "split halo-smem",
+                          "split gather 2 rows/thread"]}
     ms_spmv, ms_iter = C.c_double(), C.c_double()
     L.check(lib.fg_bench_kernel(g.h, 0, L.FG_MIXED, 200, C.byref(ms_spmv)))
     L.check(lib.fg_bench_kernel(g.h, 3, L.FG_MIXED, 200, C.byref(ms_iter)))
@@ -273,7 +278,7 @@ def run_ours(args):
         # 16-bit column (2 B) per stored nonzero; per row u and r read, w written
         # (12 B).  Neighbour gathers of u are re-reads.
         alg_bytes = g.nnz * 6 + 12 * n
-        kname = "k_cg32s_spmv_halo" if v == 7 else "k_cg32s_spmv"
+        kname = {7: "k_cg32s_spmv_halo", 8: "k_cg32s_spmv2"}.get(v, "k_cg32s_spmv")
     else:
         # one fused iteration: matrix as above; per row the (r, w, s, dinv) state read
         # and written (16 + 16 B) and p, x read and written (8 + 8 B)
@@ -350,7 +355,7 @@ def run_ours(args):
             "accuracy_vs_fp64_gpu": {"H_rel": herr, "u_rel": uerr, "energy_rel": werr},
             "newton_iters": sm["newton_iters"], "cg_iters": sm["cg_iters"], "trials": sm["trials"],
             "roofline": roofline, "kernels_us": kernels_us, "autotune": autotune, "cpu_baseline": cpu, "e2e": e2e,
-            "gpu_launches": int(launches),
+            "gpu_launches": int(launches), "cg_variant_fixed": {"mixed": args.cg_variant, "fp64": args.cg64_variant},
             "clocks": res["mixed"]["clocks"], "clocks_fp64": res["fp64"]["clocks"],
             "setup_s": {"mesh_generate": t_gen, "mesh_create_pattern": t_setup},
             "wall_s": {"mixed": res["mixed"]["wall"], "fp64": res["fp64"]["wall"]}}
@@ -522,6 +527,9 @@ def main():
                     help="DRAM bytes per SpMV launch from an ncu capture (reported as roofline.traffic)")
     ap.add_argument("--ref-counts", type=int, nargs=3, default=[11, 39, 1324],
                     help="(newton iterations, line-search trials, CG iterations) of the solve; default: the FP64 GPU solve at 96^3")
+    ap.add_argument("--cg-variant", type=int, default=0,
+                    help="fix the FP32 CG kernel variant (1..9; 0: autotuned), e.g. for profiling runs")
+    ap.add_argument("--cg64-variant", type=int, default=0, help="fix the FP64 CG SpMV variant (1..2; 0: autotuned)")
     ap.add_argument("--case", choices=sorted(CASES), default=None,
                     help="run a secondary workload instead of the headline benchmark")
     ap.add_argument("--variant", type=int, default=6, help="--case cg-kernel: forced CG kernel variant (1..6)")

@@ -605,6 +605,93 @@ __global__ void __launch_bounds__(256) k_cg32s_spmv(int64_t n, const int *__rest
   if (grid_finish<3>(part, partials, counter, tot)) cgcg_scalars(tot, scal, ictl);
 }
 
+// The split SpMV with two rows per thread (rows i and i + 256 of a 512-row block)
+// and every load of both rows issued before the first use: the row metadata and the
+// done flag together, then all values and columns, then all gathers.  Twice the
+// memory-level parallelism per thread of k_cg32s_spmv.
+template <class CI>
+__global__ void __launch_bounds__(256) k_cg32s_spmv2(int64_t n, const int *__restrict__ sl_ptr,
+                                                     const int *__restrict__ sl_len,
+                                                     const typename CI::T *__restrict__ col,
+                                                     const float *__restrict__ val, const float *__restrict__ u,
+                                                     const float *__restrict__ r, float *__restrict__ w, double *scal,
+                                                     int *ictl, double *partials, unsigned *counter) {
+  int64_t row[2];
+  row[0] = (int64_t)blockIdx.x * 512 + threadIdx.x;
+  row[1] = row[0] + 256;
+  int G[2] = {0, 0};
+  int64_t base[2] = {0, 0};
+  float ui[2] = {0.f, 0.f}, ri[2] = {0.f, 0.f};
+#pragma unroll
+  for (int k = 0; k < 2; ++k)
+    if (row[k] < n) {
+      const int s = (int)(row[k] >> 5);
+      base[k] = (int64_t)__ldg(sl_ptr + s) + (int)(row[k] & 31) * FG_GROUP;
+      G[k] = __ldg(sl_len + s);
+      ui[k] = __ldg(u + row[k]);
+      ri[k] = __ldg(r + row[k]);
+    }
+  if (ictl[I_DONE]) return;
+  float acc[2] = {0.f, 0.f};
+  if (G[0] <= 4 && G[1] <= 4) {
+    float4 vv[2][4];
+    typename CI::T4 cc[2][4];
+#pragma unroll
+    for (int k = 0; k < 2; ++k)
+#pragma unroll
+      for (int g = 0; g < 4; ++g)
+        if (g < G[k]) {
+          vv[k][g] = __ldg(reinterpret_cast<const float4 *>(val + base[k]) + (int64_t)g * FG_SLICE);
+          cc[k][g] = ld_cols(reinterpret_cast<const typename CI::T4 *>(col + base[k]) + (int64_t)g * FG_SLICE);
+        }
+    float uu[2][4][4];
+#pragma unroll
+    for (int k = 0; k < 2; ++k)
+#pragma unroll
+      for (int g = 0; g < 4; ++g)
+        if (g < G[k]) {
+          uu[k][g][0] = __ldg(u + CI::col(cc[k][g].x, row[k]));
+          uu[k][g][1] = __ldg(u + CI::col(cc[k][g].y, row[k]));
+          uu[k][g][2] = __ldg(u + CI::col(cc[k][g].z, row[k]));
+          uu[k][g][3] = __ldg(u + CI::col(cc[k][g].w, row[k]));
+        }
+#pragma unroll
+    for (int k = 0; k < 2; ++k)
+#pragma unroll
+      for (int g = 0; g < 4; ++g)
+        if (g < G[k]) {
+          acc[k] = fmaf(vv[k][g].x, uu[k][g][0], acc[k]);
+          acc[k] = fmaf(vv[k][g].y, uu[k][g][1], acc[k]);
+          acc[k] = fmaf(vv[k][g].z, uu[k][g][2], acc[k]);
+          acc[k] = fmaf(vv[k][g].w, uu[k][g][3], acc[k]);
+        }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 2; ++k)
+      for (int g = 0; g < G[k]; ++g) {
+        const float4 vv = __ldg(reinterpret_cast<const float4 *>(val + base[k]) + (int64_t)g * FG_SLICE);
+        const typename CI::T4 cc = ld_cols(reinterpret_cast<const typename CI::T4 *>(col + base[k]) + (int64_t)g * FG_SLICE);
+        acc[k] = fmaf(vv.x, __ldg(u + CI::col(cc.x, row[k])), acc[k]);
+        acc[k] = fmaf(vv.y, __ldg(u + CI::col(cc.y, row[k])), acc[k]);
+        acc[k] = fmaf(vv.z, __ldg(u + CI::col(cc.z, row[k])), acc[k]);
+        acc[k] = fmaf(vv.w, __ldg(u + CI::col(cc.w, row[k])), acc[k]);
+      }
+  }
+  Acc<float> dots[3];
+#pragma unroll
+  for (int k = 0; k < 2; ++k)
+    if (row[k] < n) {
+      w[row[k]] = acc[k];
+      dots[0].add(ri[k] * ui[k]);
+      dots[1].add(acc[k] * ui[k]);
+      dots[2].add(ri[k] * ri[k]);
+    }
+  double part[3];
+  block_sum_acc<3>(dots, part);
+  double tot[3];
+  if (grid_finish<3>(part, partials, counter, tot)) cgcg_scalars(tot, scal, ictl);
+}
+
 // The split SpMV with halo staging of u (4 bytes per distinct neighbour).
 template <int R>
 __global__ void __launch_bounds__(R) k_cg32s_spmv_halo(int64_t n, const int *__restrict__ sl_ptr,
@@ -992,8 +1079,9 @@ static void ensure_cg64(fg_mesh *m) {
 
 // FP32 iteration variants (block size x load scheduling) for the autotuner.
 // 0-3 fused iteration with direct gathers, 4 fused with halo staging, 5 fused and
-// pipelined, 6 split (vector pass + SpMV) with direct gathers, 7 split with halo staging
-constexpr int FG_N_SPMV32 = 8;
+// pipelined, 6 split (vector pass + SpMV) with direct gathers, 7 split with halo
+// staging, 8 split with two rows per thread
+constexpr int FG_N_SPMV32 = 9;
 static inline bool split32(int v) { return v >= 6; }
 constexpr int FG_N_SPMV64 = 2;   // 0 direct gathers, 1 halo staging
 
@@ -1106,7 +1194,16 @@ struct Spmv32sHalo {
 
 // w = A u and the dots of the split FP32 iteration
 static void launch_spmv32s(fg_mesh *m, int v) {
-  if (v == 7 && m->halo_col)
+  if (v == 8) {
+    if (m->use_dcol)
+      k_cg32s_spmv2<ColRel><<<grid_for(m->nv, 512), 256, 0, m->stream>>>(
+          m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl,
+          m->red.partials, m->red.counter);
+    else
+      k_cg32s_spmv2<ColAbs><<<grid_for(m->nv, 512), 256, 0, m->stream>>>(
+          m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl,
+          m->red.partials, m->red.counter);
+  } else if (v == 7 && m->halo_col)
     halo_launch<Spmv32sHalo>(m, sizeof(float), m->nv, (const int *)m->sl_ptr, (const int *)m->sl_len,
                              (const uint16_t *)m->sl_lcol, (const float *)m->val32, (const int *)m->halo_col,
                              (const int *)m->halo_len, m->hcap, (const float *)m->v32[7], (const float *)m->v32[4],
@@ -1257,7 +1354,8 @@ static int inner_solve(fg_mesh *m, bool mixed, const double *r64, double rn, dou
       // a forced variant that this operator cannot run (no halo lists, stages too
       // large for shared memory) falls back to the plain gather kernel
       const int v = o.spmv - 1;
-      const bool avail = v < 4 || v == 6 || ((v == 4 || v == 7) && m->halo_col) || (v == 5 && pipe_available(m));
+      const bool avail = v < 4 || v == 6 || v == 8 || ((v == 4 || v == 7) && m->halo_col) ||
+                         (v == 5 && pipe_available(m));
       m->spmv_variant32 = avail ? v : 0;
     } else if (!m->tuned32) {
       fg_autotune_spmv32(m, 20, nullptr, nullptr);
@@ -1592,11 +1690,34 @@ fg_status fg_autotune_spmv64(fg_mesh *m, int reps, int *chosen, double *us_per_v
   return FG_OK;
 }
 
+extern "C" fg_status fg_set_cg_variant(fg_mesh *m, int32_t precision, int32_t variant) {
+  return fg_guard([&]() -> fg_status {
+    FG_REQUIRE(m != nullptr, FG_BAD_ARG, "fg_set_cg_variant: null handle");
+    if (precision == FG_MIXED) {
+      FG_REQUIRE(variant >= 0 && variant <= FG_N_SPMV32, FG_BAD_ARG, "fg_set_cg_variant: no such variant");
+      if (variant == 0) { m->tuned32 = false; return FG_OK; }
+      const int v = variant - 1;
+      const bool avail = v < 4 || v == 6 || v == 8 || ((v == 4 || v == 7) && m->halo_col) ||
+                         (v == 5 && pipe_available(m));
+      FG_REQUIRE(avail, FG_UNSUPPORTED, "fg_set_cg_variant: variant not available for this operator");
+      m->spmv_variant32 = v;
+      m->tuned32 = true;
+    } else {
+      FG_REQUIRE(variant >= 0 && variant <= FG_N_SPMV64, FG_BAD_ARG, "fg_set_cg_variant: no such variant");
+      if (variant == 0) { m->tuned64 = false; return FG_OK; }
+      FG_REQUIRE(variant == 1 || m->halo_col, FG_UNSUPPORTED, "fg_set_cg_variant: variant not available");
+      m->spmv_variant64 = variant - 1;
+      m->tuned64 = true;
+    }
+    return FG_OK;
+  });
+}
+
 extern "C" fg_status fg_autotune(fg_mesh *m, int32_t precision, int32_t *variant, double *us_per_variant,
                                  int32_t n_slots) {
   return fg_guard([&]() -> fg_status {
     FG_REQUIRE(m != nullptr, FG_BAD_ARG, "fg_autotune: null handle");
-    double us[8] = {0};
+    double us[16] = {0};
     int chosen = 0, nv = 0;
     fg_status st;
     if (precision == FG_MIXED) {
