@@ -251,7 +251,7 @@ def run_ours(args):
     autotune = {"cg32_iteration_variants_us": [round(float(v), 2) for v in variants_us], "chosen": int(chosen.value),
                 "names": ["fused gather/256", "fused gather-hoist/256", "fused gather/128", "fused gather/512",
                           "fused halo-smem", "fused halo-smem-pipelined", "split gather/256", "split halo-smem",
-                          "split gather 2 rows/thread"]}
+                          "split gather persistent"]}
     ms_spmv, ms_iter = C.c_double(), C.c_double()
     L.check(lib.fg_bench_kernel(g.h, 0, L.FG_MIXED, 200, C.byref(ms_spmv)))
     L.check(lib.fg_bench_kernel(g.h, 3, L.FG_MIXED, 200, C.byref(ms_iter)))
@@ -278,7 +278,7 @@ def run_ours(args):
         # 16-bit column (2 B) per stored nonzero; per row u and r read, w written
         # (12 B).  Neighbour gathers of u are re-reads.
         alg_bytes = g.nnz * 6 + 12 * n
-        kname = {7: "k_cg32s_spmv_halo", 8: "k_cg32s_spmv2"}.get(v, "k_cg32s_spmv")
+        kname = "k_cg32s_spmv_halo" if v == 7 else "k_cg32s_spmv"
     else:
         # one fused iteration: matrix as above; per row the (r, w, s, dinv) state read
         # and written (16 + 16 B) and p, x read and written (8 + 8 B)

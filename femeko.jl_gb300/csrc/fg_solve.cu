@@ -132,6 +132,15 @@ __device__ __forceinline__ void block_sum_acc(const Acc<float> (&a)[N], double (
 // true in thread 0 of the finishing block, with the totals in tot.
 constexpr int FG_ARRIVE_GROUPS = 64;
 
+// Arrival: an atomic add with release (the partials written before it are visible to
+// whoever acquires the counter later) and acquire semantics at GPU scope; lighter
+// than a full fence followed by a relaxed add.
+__device__ __forceinline__ unsigned atom_add_acq_rel(unsigned *p, unsigned v) {
+  unsigned old;
+  asm volatile("atom.acq_rel.gpu.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+
 template <int N>
 __device__ __forceinline__ bool grid_finish(const double (&v)[N], double *partials, unsigned *counter,
                                             double (&tot)[N]) {
@@ -145,8 +154,7 @@ __device__ __forceinline__ bool grid_finish(const double (&v)[N], double *partia
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int j = 0; j < N; ++j) partials[(size_t)blockIdx.x * N + j] = v[j];
-    __threadfence();
-    s_role = (atomicAdd(counter + 1 + grp, 1u) == gsize - 1) ? 1 : 0;
+    s_role = (atom_add_acq_rel(counter + 1 + grp, 1u) == gsize - 1) ? 1 : 0;
   }
   __syncthreads();
   if (s_role == 0) return false;
@@ -162,8 +170,7 @@ __device__ __forceinline__ bool grid_finish(const double (&v)[N], double *partia
 #pragma unroll
     for (int j = 0; j < N; ++j) gpart[(size_t)grp * N + j] = acc[j];
     counter[1 + grp] = 0u;  // every member of the group has arrived
-    __threadfence();
-    s_role = (atomicAdd(counter, 1u) == ngroups - 1) ? 2 : 0;
+    s_role = (atom_add_acq_rel(counter, 1u) == ngroups - 1) ? 2 : 0;
   }
   __syncthreads();
   if (s_role != 2) return false;
@@ -550,12 +557,15 @@ __global__ void __launch_bounds__(256) k_cg32s_vec(int64_t n4, float4 *__restric
                                                    float4 *__restrict__ u, float4 *__restrict__ x,
                                                    const float4 *__restrict__ dinv, const double *scal,
                                                    const int *ictl) {
-  if (ictl[I_DONE]) return;
-  const float alpha = (float)scal[S_ALPHA], beta = (float)scal[S_BETA];
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n4) return;
+  // the flag, the scalars and the vectors are loaded together
+  const int done = ictl[I_DONE];
+  const double alpha_d = scal[S_ALPHA], beta_d = scal[S_BETA];
   const float4 ww = w[j], dd = dinv[j], uu = u[j];
   float4 ss = s[j], pp = p[j], xx = x[j], rr = r[j];
+  if (done) return;
+  const float alpha = (float)alpha_d, beta = (float)beta_d;
   ss.x = fmaf(beta, ss.x, ww.x); ss.y = fmaf(beta, ss.y, ww.y); ss.z = fmaf(beta, ss.z, ww.z); ss.w = fmaf(beta, ss.w, ww.w);
   pp.x = fmaf(beta, pp.x, uu.x); pp.y = fmaf(beta, pp.y, uu.y); pp.z = fmaf(beta, pp.z, uu.z); pp.w = fmaf(beta, pp.w, uu.w);
   xx.x = fmaf(alpha, pp.x, xx.x); xx.y = fmaf(alpha, pp.y, xx.y); xx.z = fmaf(alpha, pp.z, xx.z); xx.w = fmaf(alpha, pp.w, xx.w);
@@ -567,20 +577,35 @@ __global__ void __launch_bounds__(256) k_cg32s_vec(int64_t n4, float4 *__restric
   u[j] = make_float4(dd.x * rr.x, dd.y * rr.y, dd.z * rr.z, dd.w * rr.w);
 }
 
-template <class CI>
+// PERSIST: a grid of at most the resident blocks walks the 256-row blocks with a
+// grid stride, so each block reduces and arrives once for several row blocks.
+template <class CI, bool PERSIST>
 __global__ void __launch_bounds__(256) k_cg32s_spmv(int64_t n, const int *__restrict__ sl_ptr,
                                                     const int *__restrict__ sl_len,
                                                     const typename CI::T *__restrict__ col,
                                                     const float *__restrict__ val, const float *__restrict__ u,
                                                     const float *__restrict__ r, float *__restrict__ w, double *scal,
                                                     int *ictl, double *partials, unsigned *counter) {
-  if (ictl[I_DONE]) return;
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  // the done flag is loaded together with the first row's metadata: its latency
+  // overlaps theirs instead of preceding them
+  const int done = ictl[I_DONE];
   Acc<float> dots[3];
+  const int64_t nrb = (n + 255) / 256;
+  bool first_block = true;
+  for (int64_t rb = blockIdx.x; rb < (PERSIST ? nrb : (int64_t)blockIdx.x + 1); rb += gridDim.x) {
+  const int64_t i = rb * 256 + threadIdx.x;
+  int G = 0;
+  int64_t base = 0;
   if (i < n) {
     const int s = (int)(i >> 5), lane = (int)(i & 31);
-    const int64_t base = (int64_t)sl_ptr[s] + lane * FG_GROUP;
-    const int G = sl_len[s];
+    base = (int64_t)sl_ptr[s] + lane * FG_GROUP;
+    G = sl_len[s];
+  }
+  if (first_block) {
+    if (done) return;
+    first_block = false;
+  }
+  if (i < n) {
     const float4 *v4 = reinterpret_cast<const float4 *>(val + base);
     const typename CI::T4 *c4 = reinterpret_cast<const typename CI::T4 *>(col + base);
     float acc = 0.f;
@@ -599,93 +624,7 @@ __global__ void __launch_bounds__(256) k_cg32s_spmv(int64_t n, const int *__rest
     dots[1].add(acc * ui);
     dots[2].add(ri * ri);
   }
-  double part[3];
-  block_sum_acc<3>(dots, part);
-  double tot[3];
-  if (grid_finish<3>(part, partials, counter, tot)) cgcg_scalars(tot, scal, ictl);
-}
-
-// The split SpMV with two rows per thread (rows i and i + 256 of a 512-row block)
-// and every load of both rows issued before the first use: the row metadata and the
-// done flag together, then all values and columns, then all gathers.  Twice the
-// memory-level parallelism per thread of k_cg32s_spmv.
-template <class CI>
-__global__ void __launch_bounds__(256) k_cg32s_spmv2(int64_t n, const int *__restrict__ sl_ptr,
-                                                     const int *__restrict__ sl_len,
-                                                     const typename CI::T *__restrict__ col,
-                                                     const float *__restrict__ val, const float *__restrict__ u,
-                                                     const float *__restrict__ r, float *__restrict__ w, double *scal,
-                                                     int *ictl, double *partials, unsigned *counter) {
-  int64_t row[2];
-  row[0] = (int64_t)blockIdx.x * 512 + threadIdx.x;
-  row[1] = row[0] + 256;
-  int G[2] = {0, 0};
-  int64_t base[2] = {0, 0};
-  float ui[2] = {0.f, 0.f}, ri[2] = {0.f, 0.f};
-#pragma unroll
-  for (int k = 0; k < 2; ++k)
-    if (row[k] < n) {
-      const int s = (int)(row[k] >> 5);
-      base[k] = (int64_t)__ldg(sl_ptr + s) + (int)(row[k] & 31) * FG_GROUP;
-      G[k] = __ldg(sl_len + s);
-      ui[k] = __ldg(u + row[k]);
-      ri[k] = __ldg(r + row[k]);
-    }
-  if (ictl[I_DONE]) return;
-  float acc[2] = {0.f, 0.f};
-  if (G[0] <= 4 && G[1] <= 4) {
-    float4 vv[2][4];
-    typename CI::T4 cc[2][4];
-#pragma unroll
-    for (int k = 0; k < 2; ++k)
-#pragma unroll
-      for (int g = 0; g < 4; ++g)
-        if (g < G[k]) {
-          vv[k][g] = __ldg(reinterpret_cast<const float4 *>(val + base[k]) + (int64_t)g * FG_SLICE);
-          cc[k][g] = ld_cols(reinterpret_cast<const typename CI::T4 *>(col + base[k]) + (int64_t)g * FG_SLICE);
-        }
-    float uu[2][4][4];
-#pragma unroll
-    for (int k = 0; k < 2; ++k)
-#pragma unroll
-      for (int g = 0; g < 4; ++g)
-        if (g < G[k]) {
-          uu[k][g][0] = __ldg(u + CI::col(cc[k][g].x, row[k]));
-          uu[k][g][1] = __ldg(u + CI::col(cc[k][g].y, row[k]));
-          uu[k][g][2] = __ldg(u + CI::col(cc[k][g].z, row[k]));
-          uu[k][g][3] = __ldg(u + CI::col(cc[k][g].w, row[k]));
-        }
-#pragma unroll
-    for (int k = 0; k < 2; ++k)
-#pragma unroll
-      for (int g = 0; g < 4; ++g)
-        if (g < G[k]) {
-          acc[k] = fmaf(vv[k][g].x, uu[k][g][0], acc[k]);
-          acc[k] = fmaf(vv[k][g].y, uu[k][g][1], acc[k]);
-          acc[k] = fmaf(vv[k][g].z, uu[k][g][2], acc[k]);
-          acc[k] = fmaf(vv[k][g].w, uu[k][g][3], acc[k]);
-        }
-  } else {
-#pragma unroll
-    for (int k = 0; k < 2; ++k)
-      for (int g = 0; g < G[k]; ++g) {
-        const float4 vv = __ldg(reinterpret_cast<const float4 *>(val + base[k]) + (int64_t)g * FG_SLICE);
-        const typename CI::T4 cc = ld_cols(reinterpret_cast<const typename CI::T4 *>(col + base[k]) + (int64_t)g * FG_SLICE);
-        acc[k] = fmaf(vv.x, __ldg(u + CI::col(cc.x, row[k])), acc[k]);
-        acc[k] = fmaf(vv.y, __ldg(u + CI::col(cc.y, row[k])), acc[k]);
-        acc[k] = fmaf(vv.z, __ldg(u + CI::col(cc.z, row[k])), acc[k]);
-        acc[k] = fmaf(vv.w, __ldg(u + CI::col(cc.w, row[k])), acc[k]);
-      }
   }
-  Acc<float> dots[3];
-#pragma unroll
-  for (int k = 0; k < 2; ++k)
-    if (row[k] < n) {
-      w[row[k]] = acc[k];
-      dots[0].add(ri[k] * ui[k]);
-      dots[1].add(acc[k] * ui[k]);
-      dots[2].add(ri[k] * ri[k]);
-    }
   double part[3];
   block_sum_acc<3>(dots, part);
   double tot[3];
@@ -1080,7 +1019,7 @@ static void ensure_cg64(fg_mesh *m) {
 // FP32 iteration variants (block size x load scheduling) for the autotuner.
 // 0-3 fused iteration with direct gathers, 4 fused with halo staging, 5 fused and
 // pipelined, 6 split (vector pass + SpMV) with direct gathers, 7 split with halo
-// staging, 8 split with two rows per thread
+// staging, 8 split with direct gathers in a persistent grid
 constexpr int FG_N_SPMV32 = 9;
 static inline bool split32(int v) { return v >= 6; }
 constexpr int FG_N_SPMV64 = 2;   // 0 direct gathers, 1 halo staging
@@ -1195,25 +1134,27 @@ struct Spmv32sHalo {
 // w = A u and the dots of the split FP32 iteration
 static void launch_spmv32s(fg_mesh *m, int v) {
   if (v == 8) {
+    // persistent: at most 8 resident 256-thread blocks per SM
+    const unsigned g = std::min<unsigned>(grid_for(m->nv, 256), 8u * (unsigned)std::max(m->sm_count, 1));
     if (m->use_dcol)
-      k_cg32s_spmv2<ColRel><<<grid_for(m->nv, 512), 256, 0, m->stream>>>(
-          m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl,
-          m->red.partials, m->red.counter);
+      k_cg32s_spmv<ColRel, true><<<g, 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, m->val32,
+                                                           m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl,
+                                                           m->red.partials, m->red.counter);
     else
-      k_cg32s_spmv2<ColAbs><<<grid_for(m->nv, 512), 256, 0, m->stream>>>(
-          m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl,
-          m->red.partials, m->red.counter);
+      k_cg32s_spmv<ColAbs, true><<<g, 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val32,
+                                                           m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl,
+                                                           m->red.partials, m->red.counter);
   } else if (v == 7 && m->halo_col)
     halo_launch<Spmv32sHalo>(m, sizeof(float), m->nv, (const int *)m->sl_ptr, (const int *)m->sl_len,
                              (const uint16_t *)m->sl_lcol, (const float *)m->val32, (const int *)m->halo_col,
                              (const int *)m->halo_len, m->hcap, (const float *)m->v32[7], (const float *)m->v32[4],
                              m->v32[5], m->scal, m->ictl, m->red.partials, m->red.counter);
   else if (m->use_dcol)
-    k_cg32s_spmv<ColRel><<<grid_for(m->nv, 256), 256, 0, m->stream>>>(
+    k_cg32s_spmv<ColRel, false><<<grid_for(m->nv, 256), 256, 0, m->stream>>>(
         m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl,
         m->red.partials, m->red.counter);
   else
-    k_cg32s_spmv<ColAbs><<<grid_for(m->nv, 256), 256, 0, m->stream>>>(
+    k_cg32s_spmv<ColAbs, false><<<grid_for(m->nv, 256), 256, 0, m->stream>>>(
         m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl,
         m->red.partials, m->red.counter);
 }

@@ -59,7 +59,7 @@ enum {
  * into shared memory); 6: halo staging, persistent and software-pipelined (bulk
  * copies and asynchronous gathers of the next row blocks).  Two kernels per
  * iteration (vector pass + SpMV): 7: direct gathers; 8: halo staging; 9: direct
- * gathers, two rows per thread with every load issued first. */
+ * gathers in a persistent grid (each block walks several row blocks). */
 enum { FG_SPMV_AUTO = 0 };
 
 typedef struct fg_mesh fg_mesh;
