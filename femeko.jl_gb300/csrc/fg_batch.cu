@@ -17,8 +17,9 @@
 
 namespace cgrp = cooperative_groups;
 
-constexpr int FG_BATCH_CL = 8;        // CTAs per problem (portable cluster size)
-constexpr int FG_BATCH_THREADS = 512;
+// CTAs per problem: 16 (a non-portable cluster size) where the device places such
+// clusters, else 8 (the portable size)
+constexpr int FG_BATCH_THREADS = 1024;
 
 struct BatchProb {
   int64_t n;
@@ -37,6 +38,7 @@ struct BatchProb {
 // Block sum of two values, then the cluster-wide sum of the CTAs' block sums (read
 // from every CTA's shared slot in rank order).  slot alternates between calls so a
 // slot is rewritten only after the next cluster barrier.
+template <int CL>
 __device__ __forceinline__ void cluster_sum2(cgrp::cluster_group &cl, double a, double b, double (*slot)[2],
                                              int which, double &ta, double &tb) {
   __shared__ double wsum[2][FG_BATCH_THREADS / 32];
@@ -57,7 +59,7 @@ __device__ __forceinline__ void cluster_sum2(cgrp::cluster_group &cl, double a, 
   __threadfence();
   cl.sync();
   double sa = 0.0, sb = 0.0;
-  for (int rank = 0; rank < FG_BATCH_CL; ++rank) {
+  for (int rank = 0; rank < CL; ++rank) {
     const double *remote = cl.map_shared_rank(&slot[which][0], rank);
     sa += remote[0];
     sb += remote[1];
@@ -66,11 +68,12 @@ __device__ __forceinline__ void cluster_sum2(cgrp::cluster_group &cl, double a, 
   tb = sb;
 }
 
-__global__ void __launch_bounds__(FG_BATCH_THREADS) k_batch_pcg64(const BatchProb *__restrict__ probs) {
+template <int CL>
+__global__ void __launch_bounds__(FG_BATCH_THREADS, 1) k_batch_pcg64(const BatchProb *__restrict__ probs) {
   cgrp::cluster_group cl = cgrp::this_cluster();
   __shared__ double slot[2][2];
   const int rank = (int)cl.block_rank();
-  const BatchProb *pp = probs + blockIdx.x / FG_BATCH_CL;
+  const BatchProb *pp = probs + blockIdx.x / CL;
   const int64_t n = pp->n;
   const int nslices = pp->nslices;
   const int *__restrict__ sl_ptr = pp->sl_ptr;
@@ -82,7 +85,7 @@ __global__ void __launch_bounds__(FG_BATCH_THREADS) k_batch_pcg64(const BatchPro
   double *x = pp->x, *r = pp->r, *z = pp->z, *q = pp->q;
   double *pold = pp->p0, *pnew = pp->p1;
   // this CTA's rows: a contiguous run of whole slices
-  const int per = (nslices + FG_BATCH_CL - 1) / FG_BATCH_CL;
+  const int per = (nslices + CL - 1) / CL;
   const int s0 = min(rank * per, nslices), s1 = min(s0 + per, nslices);
   const int64_t i0 = (int64_t)s0 * FG_SLICE, i1 = min((int64_t)s1 * FG_SLICE, n);
   // r = -A x on free rows (the right-hand side is 0), z = D^-1 r, p = 0
@@ -111,7 +114,7 @@ __global__ void __launch_bounds__(FG_BATCH_THREADS) k_batch_pcg64(const BatchPro
   }
   int which = 0;
   double rz, rr;
-  cluster_sum2(cl, prz, prr, slot, which, rz, rr);
+  cluster_sum2<CL>(cl, prz, prr, slot, which, rz, rr);
   which ^= 1;
   const double rr0 = rr, tol2 = pp->tol2_rel * rr0;
   const int maxit = pp->maxit;
@@ -143,7 +146,7 @@ __global__ void __launch_bounds__(FG_BATCH_THREADS) k_batch_pcg64(const BatchPro
       ppq += pi * qi;
     }
     double pq, unused;
-    cluster_sum2(cl, ppq, 0.0, slot, which, pq, unused);
+    cluster_sum2<CL>(cl, ppq, 0.0, slot, which, pq, unused);
     which ^= 1;
     if (!(pq > 0.0) || !isfinite(pq)) { status = (pq == 0.0) ? 0 : 2; break; }
     const double alpha = rz / pq;
@@ -160,7 +163,7 @@ __global__ void __launch_bounds__(FG_BATCH_THREADS) k_batch_pcg64(const BatchPro
       prr += ri * ri;
     }
     double rzn;
-    cluster_sum2(cl, prz, prr, slot, which, rzn, rr);
+    cluster_sum2<CL>(cl, prz, prr, slot, which, rzn, rr);
     which ^= 1;
     ++it;
     if (!isfinite(rr)) { status = 2; break; }
@@ -234,6 +237,7 @@ extern "C" fg_status fg_batch_magnetostatics_linear(fg_mesh *const *meshes, int3
     int *d_out = nullptr;
     BatchProb *d_probs = nullptr;
     double *d_rel = nullptr;
+    int cluster_size = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -260,24 +264,36 @@ extern "C" fg_status fg_batch_magnetostatics_linear(fg_mesh *const *meshes, int3
       cudaStream_t st = m0->stream;
       FG_CUDA_TRY(cudaMemcpyAsync(d_probs, sorted.data(), sizeof(BatchProb) * count, cudaMemcpyHostToDevice, st));
       cudaLaunchConfig_t cfg = {};
-      cfg.gridDim = dim3((unsigned)(count * FG_BATCH_CL));
       cfg.blockDim = dim3(FG_BATCH_THREADS);
       cfg.dynamicSmemBytes = 0;
       cfg.stream = st;
       cudaLaunchAttribute attr[1];
       attr[0].id = cudaLaunchAttributeClusterDimension;
-      attr[0].val.clusterDim.x = FG_BATCH_CL;
       attr[0].val.clusterDim.y = 1;
       attr[0].val.clusterDim.z = 1;
       cfg.attrs = attr;
       cfg.numAttrs = 1;
-      int fit = 0;
-      FG_CUDA_TRY(cudaOccupancyMaxActiveClusters(&fit, k_batch_pcg64, &cfg));
+      // clusters of 16 where the device places them, else 8
+      int cl = 16, fit = 0;
+      if (cudaFuncSetAttribute(k_batch_pcg64<16>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+        cfg.gridDim = dim3((unsigned)(count * 16));
+        attr[0].val.clusterDim.x = 16;
+        if (cudaOccupancyMaxActiveClusters(&fit, k_batch_pcg64<16>, &cfg) != cudaSuccess) fit = 0;
+      }
+      cudaGetLastError();
+      if (fit <= 0) {
+        cl = 8;
+        cfg.gridDim = dim3((unsigned)(count * 8));
+        attr[0].val.clusterDim.x = 8;
+        FG_CUDA_TRY(cudaOccupancyMaxActiveClusters(&fit, k_batch_pcg64<8>, &cfg));
+      }
       FG_REQUIRE(fit > 0, FG_UNSUPPORTED, "fg_batch_magnetostatics_linear: the device cannot place one cluster");
+      cluster_size = cl;
       FG_CUDA_TRY(cudaEventCreate(&e0));
       FG_CUDA_TRY(cudaEventCreate(&e1));
       FG_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-      cudaError_t le = cudaLaunchKernelEx(&cfg, k_batch_pcg64, (const BatchProb *)d_probs);
+      cudaError_t le = (cl == 16) ? cudaLaunchKernelEx(&cfg, k_batch_pcg64<16>, (const BatchProb *)d_probs)
+                                  : cudaLaunchKernelEx(&cfg, k_batch_pcg64<8>, (const BatchProb *)d_probs);
       cudaError_t ce = cudaStreamEndCapture(st, &graph);
       FG_CUDA_TRY(le);
       FG_CUDA_TRY(ce);
@@ -311,7 +327,7 @@ extern "C" fg_status fg_batch_magnetostatics_linear(fg_mesh *const *meshes, int3
         s->problems = count;
         s->converged = conv;
         s->max_iterations = maxit;
-        s->pad_ = 0;
+        s->cluster_ctas = cluster_size;
         s->total_iterations = tot;
         s->ms = ms;
       }

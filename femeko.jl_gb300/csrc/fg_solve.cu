@@ -548,6 +548,14 @@ __global__ void __launch_bounds__(R) k_cg32_iter_pipe(PipeArgs a, const float4 *
   if (grid_finish<3>(part, partials, counter, tot) && ok) cgcg_scalars(tot, scal, ictl);
 }
 
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialisation may start while the previous kernel in the stream finishes;
+// griddep_wait() returns once that kernel has completed and its writes are visible,
+// griddep_release() lets the next kernel start launching.  Both are no-ops for a
+// kernel launched without the attribute.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // FP32 Chronopoulos-Gear iteration split in two passes, as the FP64 one: a streaming
 // vector update (s = w + beta s, p = u + beta p, x += alpha p, r -= alpha s,
 // u = D^-1 r; four rows per thread) and w = A u with the three dot products.  The
@@ -557,6 +565,8 @@ __global__ void __launch_bounds__(256) k_cg32s_vec(int64_t n4, float4 *__restric
                                                    float4 *__restrict__ u, float4 *__restrict__ x,
                                                    const float4 *__restrict__ dinv, const double *scal,
                                                    const int *ictl) {
+  griddep_wait();
+  griddep_release();
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n4) return;
   // the flag, the scalars and the vectors are loaded together
@@ -586,6 +596,8 @@ __global__ void __launch_bounds__(256) k_cg32s_spmv(int64_t n, const int *__rest
                                                     const float *__restrict__ val, const float *__restrict__ u,
                                                     const float *__restrict__ r, float *__restrict__ w, double *scal,
                                                     int *ictl, double *partials, unsigned *counter) {
+  griddep_wait();
+  griddep_release();
   // the done flag is loaded together with the first row's metadata: its latency
   // overlaps theirs instead of preceding them
   const int done = ictl[I_DONE];
@@ -642,6 +654,8 @@ __global__ void __launch_bounds__(R) k_cg32s_spmv_halo(int64_t n, const int *__r
                                                        float *__restrict__ w, double *scal, int *ictl,
                                                        double *partials, unsigned *counter) {
   extern __shared__ float uhs[];
+  griddep_wait();
+  griddep_release();
   if (ictl[I_DONE]) return;
   {
     const int hl = halo_len[blockIdx.x];
@@ -1132,39 +1146,55 @@ struct Spmv32sHalo {
 };
 
 // w = A u and the dots of the split FP32 iteration
+// Launch with programmatic stream serialisation (the kernel waits for its
+// predecessor with griddep_wait, so its launch overlaps the predecessor's tail).
+template <typename... KArgs, typename... Args>
+static void pdl_launch(void (*kern)(KArgs...), unsigned grid, unsigned block, size_t smem, cudaStream_t st,
+                       Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  FG_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...));
+}
+
 static void launch_spmv32s(fg_mesh *m, int v) {
   if (v == 8) {
     // persistent: at most 8 resident 256-thread blocks per SM
     const unsigned g = std::min<unsigned>(grid_for(m->nv, 256), 8u * (unsigned)std::max(m->sm_count, 1));
     if (m->use_dcol)
-      k_cg32s_spmv<ColRel, true><<<g, 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, m->val32,
-                                                           m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl,
-                                                           m->red.partials, m->red.counter);
+      pdl_launch(k_cg32s_spmv<ColRel, true>, g, 256, 0, m->stream, m->nv, m->sl_ptr, m->sl_len, m->sl_dcol,
+                 m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl, m->red.partials, m->red.counter);
     else
-      k_cg32s_spmv<ColAbs, true><<<g, 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val32,
-                                                           m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl,
-                                                           m->red.partials, m->red.counter);
+      pdl_launch(k_cg32s_spmv<ColAbs, true>, g, 256, 0, m->stream, m->nv, m->sl_ptr, m->sl_len, m->sl_col,
+                 m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl, m->red.partials, m->red.counter);
   } else if (v == 7 && m->halo_col)
     halo_launch<Spmv32sHalo>(m, sizeof(float), m->nv, (const int *)m->sl_ptr, (const int *)m->sl_len,
                              (const uint16_t *)m->sl_lcol, (const float *)m->val32, (const int *)m->halo_col,
                              (const int *)m->halo_len, m->hcap, (const float *)m->v32[7], (const float *)m->v32[4],
                              m->v32[5], m->scal, m->ictl, m->red.partials, m->red.counter);
   else if (m->use_dcol)
-    k_cg32s_spmv<ColRel, false><<<grid_for(m->nv, 256), 256, 0, m->stream>>>(
-        m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl,
-        m->red.partials, m->red.counter);
+    pdl_launch(k_cg32s_spmv<ColRel, false>, grid_for(m->nv, 256), 256, 0, m->stream, m->nv, m->sl_ptr, m->sl_len,
+               m->sl_dcol, m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl, m->red.partials,
+               m->red.counter);
   else
-    k_cg32s_spmv<ColAbs, false><<<grid_for(m->nv, 256), 256, 0, m->stream>>>(
-        m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl,
-        m->red.partials, m->red.counter);
+    pdl_launch(k_cg32s_spmv<ColAbs, false>, grid_for(m->nv, 256), 256, 0, m->stream, m->nv, m->sl_ptr, m->sl_len,
+               m->sl_col, m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl, m->red.partials,
+               m->red.counter);
 }
 
 static void launch_vec32s(fg_mesh *m) {
-  k_cg32s_vec<<<grid_for(m->nvp / 4, 256), 256, 0, m->stream>>>(
-      m->nvp / 4, reinterpret_cast<float4 *>(m->v32[4]), reinterpret_cast<const float4 *>(m->v32[5]),
-      reinterpret_cast<float4 *>(m->v32[6]), reinterpret_cast<float4 *>(m->v32[1]),
-      reinterpret_cast<float4 *>(m->v32[7]), reinterpret_cast<float4 *>(m->v32[0]),
-      reinterpret_cast<const float4 *>(m->dinv32), m->scal, m->ictl);
+  pdl_launch(k_cg32s_vec, grid_for(m->nvp / 4, 256), 256, 0, m->stream, m->nvp / 4,
+             reinterpret_cast<float4 *>(m->v32[4]), reinterpret_cast<const float4 *>(m->v32[5]),
+             reinterpret_cast<float4 *>(m->v32[6]), reinterpret_cast<float4 *>(m->v32[1]),
+             reinterpret_cast<float4 *>(m->v32[7]), reinterpret_cast<float4 *>(m->v32[0]),
+             reinterpret_cast<const float4 *>(m->dinv32), (const double *)m->scal, (const int *)m->ictl);
 }
 
 static void launch_iter32(fg_mesh *m, int v, bool from_first_buffer) {

@@ -97,8 +97,16 @@ __global__ void k_sw_fieldsum(const double *__restrict__ partials, int nblocks, 
   __shared__ double sh[8][33];
   const int c = blockIdx.x * 32 + (threadIdx.x & 31), part = threadIdx.x >> 5;
   double t = 0.0;
-  if (c < NR)
-    for (int b = part; b < nblocks; b += 8) t += partials[(int64_t)b * NR + c];
+  if (c < NR) {
+    // four independent partial sums per thread keep four loads in flight
+    double t4[4] = {0.0, 0.0, 0.0, 0.0};
+    int b = part;
+    for (; b + 24 < nblocks; b += 32)
+#pragma unroll
+      for (int k = 0; k < 4; ++k) t4[k] += partials[(int64_t)(b + 8 * k) * NR + c];
+    for (; b < nblocks; b += 8) t4[0] += partials[(int64_t)b * NR + c];
+    t = (t4[0] + t4[1]) + (t4[2] + t4[3]);
+  }
   sh[part][threadIdx.x & 31] = t;
   __syncthreads();
   if (part == 0 && c < NR) {
@@ -325,7 +333,7 @@ static fg_status sweep_impl(fg_mesh *m, int nfield, const double *H0, const fg_s
     }
   } release{tmp};
   cudaStream_t st = m->stream;
-  const int nblocks = std::max(1, std::min<int>(m->sm_count * 8, (int)((n + SW_WARPS - 1) / SW_WARPS)));
+  const int nblocks = std::max(1, std::min<int>(m->sm_count * 4, (int)((n + SW_WARPS - 1) / SW_WARPS)));
   double *X = (double *)alloc(sizeof(double) * blk), *R = (double *)alloc(sizeof(double) * blk);
   float *r = (float *)alloc(sizeof(float) * blk), *p0 = (float *)alloc(sizeof(float) * blk);
   float *p1 = (float *)alloc(sizeof(float) * blk), *q = (float *)alloc(sizeof(float) * blk);

@@ -234,7 +234,7 @@ typedef struct fg_batch_stats {
   int32_t problems;
   int32_t converged;       /* problems that reached rtol */
   int32_t max_iterations;  /* largest CG iteration count of a problem */
-  int32_t pad_;
+  int32_t cluster_ctas;    /* CTAs per problem (thread-block cluster size) */
   int64_t total_iterations;
   double ms;               /* device time of the one persistent launch */
 } fg_batch_stats;
