@@ -17,9 +17,9 @@
 
 namespace cgrp = cooperative_groups;
 
-// CTAs per problem: 16 (a non-portable cluster size) where the device places such
-// clusters, else 8 (the portable size)
-constexpr int FG_BATCH_THREADS = 1024;
+// CTAs per problem: the portable cluster size 8 (16-CTA clusters of 1024 threads
+// measured 2x slower on the 64-mesh batch: 64 registers per thread spill)
+constexpr int FG_BATCH_THREADS = 512;
 
 struct BatchProb {
   int64_t n;
@@ -69,7 +69,7 @@ __device__ __forceinline__ void cluster_sum2(cgrp::cluster_group &cl, double a, 
 }
 
 template <int CL>
-__global__ void __launch_bounds__(FG_BATCH_THREADS, 1) k_batch_pcg64(const BatchProb *__restrict__ probs) {
+__global__ void __launch_bounds__(FG_BATCH_THREADS) k_batch_pcg64(const BatchProb *__restrict__ probs) {
   cgrp::cluster_group cl = cgrp::this_cluster();
   __shared__ double slot[2][2];
   const int rank = (int)cl.block_rank();
@@ -273,27 +273,17 @@ extern "C" fg_status fg_batch_magnetostatics_linear(fg_mesh *const *meshes, int3
       attr[0].val.clusterDim.z = 1;
       cfg.attrs = attr;
       cfg.numAttrs = 1;
-      // clusters of 16 where the device places them, else 8
-      int cl = 16, fit = 0;
-      if (cudaFuncSetAttribute(k_batch_pcg64<16>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
-        cfg.gridDim = dim3((unsigned)(count * 16));
-        attr[0].val.clusterDim.x = 16;
-        if (cudaOccupancyMaxActiveClusters(&fit, k_batch_pcg64<16>, &cfg) != cudaSuccess) fit = 0;
-      }
-      cudaGetLastError();
-      if (fit <= 0) {
-        cl = 8;
-        cfg.gridDim = dim3((unsigned)(count * 8));
-        attr[0].val.clusterDim.x = 8;
-        FG_CUDA_TRY(cudaOccupancyMaxActiveClusters(&fit, k_batch_pcg64<8>, &cfg));
-      }
+      const int cl = 8;
+      int fit = 0;
+      cfg.gridDim = dim3((unsigned)(count * cl));
+      attr[0].val.clusterDim.x = cl;
+      FG_CUDA_TRY(cudaOccupancyMaxActiveClusters(&fit, k_batch_pcg64<8>, &cfg));
       FG_REQUIRE(fit > 0, FG_UNSUPPORTED, "fg_batch_magnetostatics_linear: the device cannot place one cluster");
       cluster_size = cl;
       FG_CUDA_TRY(cudaEventCreate(&e0));
       FG_CUDA_TRY(cudaEventCreate(&e1));
       FG_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-      cudaError_t le = (cl == 16) ? cudaLaunchKernelEx(&cfg, k_batch_pcg64<16>, (const BatchProb *)d_probs)
-                                  : cudaLaunchKernelEx(&cfg, k_batch_pcg64<8>, (const BatchProb *)d_probs);
+      cudaError_t le = cudaLaunchKernelEx(&cfg, k_batch_pcg64<8>, (const BatchProb *)d_probs);
       cudaError_t ce = cudaStreamEndCapture(st, &graph);
       FG_CUDA_TRY(le);
       FG_CUDA_TRY(ce);

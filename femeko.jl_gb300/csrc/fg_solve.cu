@@ -1033,8 +1033,9 @@ static void ensure_cg64(fg_mesh *m) {
 // FP32 iteration variants (block size x load scheduling) for the autotuner.
 // 0-3 fused iteration with direct gathers, 4 fused with halo staging, 5 fused and
 // pipelined, 6 split (vector pass + SpMV) with direct gathers, 7 split with halo
-// staging, 8 split with direct gathers in a persistent grid
-constexpr int FG_N_SPMV32 = 9;
+// staging, 8 split with direct gathers in a persistent grid, 9 the same launched with
+// programmatic dependent launch
+constexpr int FG_N_SPMV32 = 10;
 static inline bool split32(int v) { return v >= 6; }
 constexpr int FG_N_SPMV64 = 2;   // 0 direct gathers, 1 halo staging
 
@@ -1149,8 +1150,8 @@ struct Spmv32sHalo {
 // Launch with programmatic stream serialisation (the kernel waits for its
 // predecessor with griddep_wait, so its launch overlaps the predecessor's tail).
 template <typename... KArgs, typename... Args>
-static void pdl_launch(void (*kern)(KArgs...), unsigned grid, unsigned block, size_t smem, cudaStream_t st,
-                       Args... args) {
+static void pdl_launch(bool pdl, void (*kern)(KArgs...), unsigned grid, unsigned block, size_t smem,
+                       cudaStream_t st, Args... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(block);
@@ -1160,19 +1161,20 @@ static void pdl_launch(void (*kern)(KArgs...), unsigned grid, unsigned block, si
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = pdl ? 1 : 0;
   FG_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...));
 }
 
 static void launch_spmv32s(fg_mesh *m, int v) {
-  if (v == 8) {
+  const bool pdl = (v == 9);
+  if (v == 8 || v == 9) {
     // persistent: at most 8 resident 256-thread blocks per SM
     const unsigned g = std::min<unsigned>(grid_for(m->nv, 256), 8u * (unsigned)std::max(m->sm_count, 1));
     if (m->use_dcol)
-      pdl_launch(k_cg32s_spmv<ColRel, true>, g, 256, 0, m->stream, m->nv, m->sl_ptr, m->sl_len, m->sl_dcol,
+      pdl_launch(pdl, k_cg32s_spmv<ColRel, true>, g, 256, 0, m->stream, m->nv, m->sl_ptr, m->sl_len, m->sl_dcol,
                  m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl, m->red.partials, m->red.counter);
     else
-      pdl_launch(k_cg32s_spmv<ColAbs, true>, g, 256, 0, m->stream, m->nv, m->sl_ptr, m->sl_len, m->sl_col,
+      pdl_launch(pdl, k_cg32s_spmv<ColAbs, true>, g, 256, 0, m->stream, m->nv, m->sl_ptr, m->sl_len, m->sl_col,
                  m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl, m->red.partials, m->red.counter);
   } else if (v == 7 && m->halo_col)
     halo_launch<Spmv32sHalo>(m, sizeof(float), m->nv, (const int *)m->sl_ptr, (const int *)m->sl_len,
@@ -1180,17 +1182,17 @@ static void launch_spmv32s(fg_mesh *m, int v) {
                              (const int *)m->halo_len, m->hcap, (const float *)m->v32[7], (const float *)m->v32[4],
                              m->v32[5], m->scal, m->ictl, m->red.partials, m->red.counter);
   else if (m->use_dcol)
-    pdl_launch(k_cg32s_spmv<ColRel, false>, grid_for(m->nv, 256), 256, 0, m->stream, m->nv, m->sl_ptr, m->sl_len,
-               m->sl_dcol, m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl, m->red.partials,
+    pdl_launch(false, k_cg32s_spmv<ColRel, false>, grid_for(m->nv, 256), 256, 0, m->stream, m->nv, m->sl_ptr,
+               m->sl_len, m->sl_dcol, m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl, m->red.partials,
                m->red.counter);
   else
-    pdl_launch(k_cg32s_spmv<ColAbs, false>, grid_for(m->nv, 256), 256, 0, m->stream, m->nv, m->sl_ptr, m->sl_len,
-               m->sl_col, m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl, m->red.partials,
+    pdl_launch(false, k_cg32s_spmv<ColAbs, false>, grid_for(m->nv, 256), 256, 0, m->stream, m->nv, m->sl_ptr,
+               m->sl_len, m->sl_col, m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl, m->red.partials,
                m->red.counter);
 }
 
-static void launch_vec32s(fg_mesh *m) {
-  pdl_launch(k_cg32s_vec, grid_for(m->nvp / 4, 256), 256, 0, m->stream, m->nvp / 4,
+static void launch_vec32s(fg_mesh *m, bool pdl) {
+  pdl_launch(pdl, k_cg32s_vec, grid_for(m->nvp / 4, 256), 256, 0, m->stream, m->nvp / 4,
              reinterpret_cast<float4 *>(m->v32[4]), reinterpret_cast<const float4 *>(m->v32[5]),
              reinterpret_cast<float4 *>(m->v32[6]), reinterpret_cast<float4 *>(m->v32[1]),
              reinterpret_cast<float4 *>(m->v32[7]), reinterpret_cast<float4 *>(m->v32[0]),
@@ -1199,7 +1201,7 @@ static void launch_vec32s(fg_mesh *m) {
 
 static void launch_iter32(fg_mesh *m, int v, bool from_first_buffer) {
   if (split32(v)) {
-    launch_vec32s(m);
+    launch_vec32s(m, v == 9);
     launch_spmv32s(m, v);
     return;
   }
@@ -1325,7 +1327,7 @@ static int inner_solve(fg_mesh *m, bool mixed, const double *r64, double rn, dou
       // a forced variant that this operator cannot run (no halo lists, stages too
       // large for shared memory) falls back to the plain gather kernel
       const int v = o.spmv - 1;
-      const bool avail = v < 4 || v == 6 || v == 8 || ((v == 4 || v == 7) && m->halo_col) ||
+      const bool avail = v < 4 || v == 6 || v == 8 || v == 9 || ((v == 4 || v == 7) && m->halo_col) ||
                          (v == 5 && pipe_available(m));
       m->spmv_variant32 = avail ? v : 0;
     } else if (!m->tuned32) {
@@ -1575,7 +1577,7 @@ fg_status fg_bench_cg_kernel(fg_mesh *m, int which, int precision, int reps, dou
     for (int r = 0; r < n; ++r) {
       if (mixed && (!split32(v) || which == 3)) launch_iter32(m, v, (r & 1) != 0);
       else if (mixed && which == 0) launch_spmv32s(m, v);
-      else if (mixed) launch_vec32s(m);
+      else if (mixed) launch_vec32s(m, v == 9);
       else if (which == 0) launch_spmv64cg(m);
       else if (which == 1) launch_vec64(m);
       else { launch_vec64(m); launch_spmv64cg(m); }
@@ -1610,14 +1612,25 @@ fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_v
     m->spmv_variant32 = v;
     timing_state(m, true);
     for (int r = 0; r < 2; ++r) launch_iter32(m, v, r == 1);
-    FG_CUDA_TRY(cudaEventRecord(m->ev0, m->stream));
+    // timed as the solver runs them: a CUDA graph of reps iterations, replayed
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    FG_CUDA_TRY(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
     for (int r = 0; r < reps; ++r) launch_iter32(m, v, r & 1);
-    FG_CUDA_TRY(cudaEventRecord(m->ev1, m->stream));
-    FG_CUDA_TRY(cudaGetLastError());
-    FG_LAUNCHED(reps + 2);
-    fg_sync(m);
+    FG_CUDA_TRY(cudaStreamEndCapture(m->stream, &graph));
+    cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    FG_CUDA_TRY(ie);
     float ms = 0.f;
-    FG_CUDA_TRY(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
+    cudaError_t le = cudaGraphLaunch(exec, m->stream);
+    if (le == cudaSuccess) le = cudaEventRecord(m->ev0, m->stream);
+    if (le == cudaSuccess) le = cudaGraphLaunch(exec, m->stream);
+    if (le == cudaSuccess) le = cudaEventRecord(m->ev1, m->stream);
+    if (le == cudaSuccess) le = cudaStreamSynchronize(m->stream);
+    if (le == cudaSuccess) le = cudaEventElapsedTime(&ms, m->ev0, m->ev1);
+    cudaGraphExecDestroy(exec);
+    FG_CUDA_TRY(le);
+    FG_LAUNCHED(2LL * reps * (split32(v) ? 2 : 1) + 2);
     const double us = 1e3 * ms / reps;
     if (us_per_variant) us_per_variant[v] = us;
     if (us < best_us) { best_us = us; best = v; }
@@ -1668,7 +1681,7 @@ extern "C" fg_status fg_set_cg_variant(fg_mesh *m, int32_t precision, int32_t va
       FG_REQUIRE(variant >= 0 && variant <= FG_N_SPMV32, FG_BAD_ARG, "fg_set_cg_variant: no such variant");
       if (variant == 0) { m->tuned32 = false; return FG_OK; }
       const int v = variant - 1;
-      const bool avail = v < 4 || v == 6 || v == 8 || ((v == 4 || v == 7) && m->halo_col) ||
+      const bool avail = v < 4 || v == 6 || v == 8 || v == 9 || ((v == 4 || v == 7) && m->halo_col) ||
                          (v == 5 && pipe_available(m));
       FG_REQUIRE(avail, FG_UNSUPPORTED, "fg_set_cg_variant: variant not available for this operator");
       m->spmv_variant32 = v;

@@ -333,7 +333,7 @@ static fg_status sweep_impl(fg_mesh *m, int nfield, const double *H0, const fg_s
     }
   } release{tmp};
   cudaStream_t st = m->stream;
-  const int nblocks = std::max(1, std::min<int>(m->sm_count * 4, (int)((n + SW_WARPS - 1) / SW_WARPS)));
+  const int nblocks = std::max(1, std::min<int>(m->sm_count * 8, (int)((n + SW_WARPS - 1) / SW_WARPS)));
   double *X = (double *)alloc(sizeof(double) * blk), *R = (double *)alloc(sizeof(double) * blk);
   float *r = (float *)alloc(sizeof(float) * blk), *p0 = (float *)alloc(sizeof(float) * blk);
   float *p1 = (float *)alloc(sizeof(float) * blk), *q = (float *)alloc(sizeof(float) * blk);

@@ -52,14 +52,16 @@ enum {
                           of |F(u + a du)|^2, kept in [0.1, 0.5] of the last step */
 };
 /* FP32 CG iteration kernel: FG_SPMV_AUTO lets the autotuner time the variants on
- * the first mixed solve of a handle and keep the fastest; k = 1..9 forces variant
+ * the first mixed solve of a handle and keep the fastest; k = 1..10 forces variant
  * k-1.  One fused kernel per iteration: 1: 4x-unrolled gather loop, 256 threads;
  * 2: all row loads issued first, 256 threads; 3: loop, 128 threads; 4: loop, 512
  * threads; 5: halo staging (the neighbour entries of a block of rows gathered once
  * into shared memory); 6: halo staging, persistent and software-pipelined (bulk
  * copies and asynchronous gathers of the next row blocks).  Two kernels per
  * iteration (vector pass + SpMV): 7: direct gathers; 8: halo staging; 9: direct
- * gathers in a persistent grid (each block walks several row blocks). */
+ * gathers in a persistent grid (each block walks several row blocks); 10: 9 with
+ * programmatic dependent launch between the two kernels.  The autotuner times each
+ * variant as a replayed CUDA graph of iterations, the way the solver runs them. */
 enum { FG_SPMV_AUTO = 0 };
 
 typedef struct fg_mesh fg_mesh;
@@ -71,7 +73,7 @@ typedef struct fg_solve_opts {
   double inner_rtol;   /* mixed: FP32 PCG target per refinement step */
   int32_t check_every; /* iterations per graph launch between convergence checks (even) */
   int32_t use_graph;   /* 1: replay each block of iterations as a CUDA graph */
-  int32_t spmv;        /* FG_SPMV_AUTO or a forced variant 1..9 */
+  int32_t spmv;        /* FG_SPMV_AUTO or a forced variant 1..10 */
   int32_t reserved_;
 } fg_solve_opts;
 
@@ -304,7 +306,7 @@ fg_status fg_bench_kernel(fg_mesh *m, int32_t which, int32_t precision, int32_t 
  * be NULL) the measured microseconds per launch.  No reference counterpart. */
 fg_status fg_autotune(fg_mesh *m, int32_t precision, int32_t *variant, double *us_per_variant, int32_t n_slots);
 /* Fixes the CG kernel variant of one precision for the handle (the numbering of
- * fg_solve_opts.spmv: FG_MIXED 1..9, FG_FP64 1..2), or 0 to let the autotuner choose
+ * fg_solve_opts.spmv: FG_MIXED 1..10, FG_FP64 1..2), or 0 to let the autotuner choose
  * again at the next solve.  No reference counterpart (profiling and tuning control). */
 fg_status fg_set_cg_variant(fg_mesh *m, int32_t precision, int32_t variant);
 /* Padded sizes of the device layouts: SELL-32 matrix entries, incidence records, slices. */
