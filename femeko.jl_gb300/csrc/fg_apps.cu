@@ -1,6 +1,8 @@
 // One-shot entry points shaped like the reference's ccall boundary, and kernel
 // timing used by the benchmark's roofline report.
+#include <algorithm>
 #include <cmath>
+#include <vector>
 
 #include "fg_common.cuh"
 
@@ -66,6 +68,122 @@ extern "C" fg_status fg_mesh_layout(const fg_mesh *m, int64_t *nsell, int64_t *n
     if (nsell) *nsell = m->nsell;
     if (ninc) *ninc = m->ninc;
     if (nslices) *nslices = m->nslices;
+    return FG_OK;
+  });
+}
+
+// ------------------------------------------------------------------ right-hand sides
+// src/FEM3D.jl:274-281 lagrange: C_i = sum over the elements of node i of VE/4, as
+// vector records summed per row in a fixed order.
+__global__ void k_lagrange_tet4(int64_t nt, const double *__restrict__ geo, const int *__restrict__ recpos,
+                                double *__restrict__ rec_r) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt) return;
+  const double q = 0.25 * geo[12 * nt + k];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) rec_r[recpos[(int64_t)a * nt + k]] = q;
+}
+
+extern "C" fg_status fg_lagrange(fg_mesh *m, double *C) {
+  return fg_guard([&]() -> fg_status {
+    FG_REQUIRE(m && C, FG_BAD_ARG, "fg_lagrange: null pointer");
+    FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "fg_lagrange: P1 tetrahedra only");
+    fg_ensure_records(m);
+    k_lagrange_tet4<<<grid_for(m->nt, 256), 256, 0, m->stream>>>(m->nt, m->geo, m->recpos, m->rec_r);
+    FG_CUDA_TRY(cudaGetLastError());
+    FG_LAUNCHED(1);
+    if (!m->v64[15]) m->v64[15] = dev_alloc<double>(m, (size_t)m->nvp);
+    fg_vector_gather(m, m->v64[15]);
+    FG_CUDA_TRY(cudaMemcpyAsync(C, m->v64[15], sizeof(double) * (size_t)m->nv, cudaMemcpyDeviceToHost, m->stream));
+    fg_sync(m);
+    return FG_OK;
+  });
+}
+
+// src/FEM3D.jl:284-297 BoundaryIntegral: RHS[face nodes] += (n . F) AE / 3 over the
+// boundary faces whose id is in shell_id.  Per face value, then per node the sum
+// over its faces in face order (a node -> face list built on the host).
+__global__ void k_face_flux(int64_t ns, const int *__restrict__ sT, const double *__restrict__ normal,
+                            const double *__restrict__ AE, double F0, double F1, double F2,
+                            const int *__restrict__ shell, int nshell, double *__restrict__ v) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= ns) return;
+  const int id = sT[4 * s + 3];
+  bool hit = false;
+  for (int q = 0; q < nshell; ++q) hit |= (id == shell[q]);
+  v[s] = hit ? (normal[3 * s] * F0 + normal[3 * s + 1] * F1 + normal[3 * s + 2] * F2) * AE[s] / 3.0 : 0.0;
+}
+
+__global__ void k_node_faces(int64_t nv, const int *__restrict__ ptr, const int *__restrict__ face,
+                             const double *__restrict__ v, double *__restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nv) return;
+  double acc = 0.0;
+  for (int q = ptr[i]; q < ptr[i + 1]; ++q) acc += v[face[q]];
+  out[i] = acc;
+}
+
+extern "C" fg_status fg_boundary_integral(fg_mesh *m, const int32_t *surfaceT, int64_t ns, int32_t index_base,
+                                          const double *normal, const double *AE, const double *F,
+                                          const int32_t *shell_id, int32_t nshell, double *RHS) {
+  return fg_guard([&]() -> fg_status {
+    FG_REQUIRE(m && RHS && F && (ns == 0 || (surfaceT && normal && AE)), FG_BAD_ARG,
+               "fg_boundary_integral: null pointer");
+    FG_REQUIRE(ns >= 0 && nshell >= 0 && (nshell == 0 || shell_id), FG_BAD_ARG, "fg_boundary_integral: bad sizes");
+    FG_REQUIRE(index_base == 0 || index_base == 1, FG_BAD_ARG, "fg_boundary_integral: index_base must be 0 or 1");
+    const int64_t nv = m->nv;
+    // node -> faces (face order), 0-based copy of the faces
+    std::vector<int> st((size_t)4 * ns), cnt((size_t)nv + 1, 0);
+    for (int64_t s = 0; s < ns; ++s) {
+      for (int a = 0; a < 3; ++a) {
+        const int64_t node = (int64_t)surfaceT[4 * s + a] - index_base;
+        FG_REQUIRE(node >= 0 && node < nv, FG_BAD_MESH, "fg_boundary_integral: face node out of range");
+        st[4 * s + a] = (int)node;
+        ++cnt[node + 1];
+      }
+      st[4 * s + 3] = surfaceT[4 * s + 3];
+    }
+    for (int64_t i = 0; i < nv; ++i) cnt[i + 1] += cnt[i];
+    std::vector<int> face((size_t)3 * ns), fill(cnt.begin(), cnt.end() - 1);
+    for (int64_t s = 0; s < ns; ++s)
+      for (int a = 0; a < 3; ++a) face[fill[st[4 * s + a]]++] = (int)s;
+    // device work space for this call
+    std::vector<void *> tmp;
+    struct Free {
+      std::vector<void *> &v;
+      ~Free() {
+        for (void *p : v) cudaFree(p);
+      }
+    } release{tmp};
+    auto dmalloc = [&](size_t bytes) {
+      void *p = nullptr;
+      FG_CUDA_TRY(cudaMalloc(&p, std::max<size_t>(bytes, 16)));
+      tmp.push_back(p);
+      return p;
+    };
+    int *d_st = (int *)dmalloc(sizeof(int) * st.size()), *d_ptr = (int *)dmalloc(sizeof(int) * cnt.size());
+    int *d_face = (int *)dmalloc(sizeof(int) * face.size()), *d_shell = (int *)dmalloc(sizeof(int) * (nshell + 1));
+    double *d_n = (double *)dmalloc(sizeof(double) * 3 * ns), *d_ae = (double *)dmalloc(sizeof(double) * ns);
+    double *d_v = (double *)dmalloc(sizeof(double) * ns), *d_out = (double *)dmalloc(sizeof(double) * nv);
+    auto up = [&](void *dst, const void *src, size_t bytes) {
+      if (bytes) FG_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, m->stream));
+    };
+    up(d_st, st.data(), sizeof(int) * st.size());
+    up(d_ptr, cnt.data(), sizeof(int) * cnt.size());
+    up(d_face, face.data(), sizeof(int) * face.size());
+    up(d_shell, shell_id, sizeof(int) * nshell);
+    up(d_n, normal, sizeof(double) * 3 * ns);
+    up(d_ae, AE, sizeof(double) * ns);
+    if (ns > 0) {
+      k_face_flux<<<grid_for(ns, 256), 256, 0, m->stream>>>(ns, d_st, d_n, d_ae, F[0], F[1], F[2], d_shell, nshell,
+                                                            d_v);
+      FG_LAUNCHED(1);
+    }
+    k_node_faces<<<grid_for(nv, 256), 256, 0, m->stream>>>(nv, d_ptr, d_face, d_v, d_out);
+    FG_LAUNCHED(1);
+    FG_CUDA_TRY(cudaGetLastError());
+    FG_CUDA_TRY(cudaMemcpyAsync(RHS, d_out, sizeof(double) * nv, cudaMemcpyDeviceToHost, m->stream));
+    fg_sync(m);
     return FG_OK;
   });
 }

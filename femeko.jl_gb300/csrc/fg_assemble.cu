@@ -1063,6 +1063,11 @@ void fg_hfield_dev(fg_mesh *m, const double *d_u, double *d_H) {
   FG_LAUNCHED(1);
 }
 
+void fg_vector_gather(fg_mesh *m, double *d_out) {
+  FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "vector gather: P1 tetrahedra only");
+  launch_row<4, double, double>(m, nullptr, m->rec_r, 0, nullptr, nullptr, nullptr, nullptr, nullptr, d_out, 1.0, 0);
+}
+
 void fg_objective_parts_dev(fg_mesh *m, const double *d_u, const uint8_t *d_target, double *d_a, double *d_v) {
   FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "objective needs P1 tetrahedra");
   k_objective_tet4<<<grid_for(m->nt, 256), 256, 0, m->stream>>>(m->nt, m->geo, m->t, d_u, d_target, d_a, d_v);

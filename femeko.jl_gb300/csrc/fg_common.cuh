@@ -246,6 +246,8 @@ void fg_newton_assemble(fg_mesh *m, const double *d_u, double Ms, double Hk, boo
 void fg_nl_setup(fg_mesh *m, const uint8_t *nl_host, bool mixed);
 void fg_newton_assemble_split(fg_mesh *m, const double *d_u, double Ms, double Hk, bool mixed, double *d_F,
                               bool want_jacobian, bool tangent);
+// d_out[i] = sum of the vector records of row i (P1 tetrahedra), no Dirichlet masking.
+void fg_vector_gather(fg_mesh *m, double *d_out);
 // y = vals x on the handle's pattern (FP64), Dirichlet rows 0.
 void fg_spmv64_vals(fg_mesh *m, const double *vals, const double *x, double *y);
 void fg_apply_operator_vec(fg_mesh *m, int kind, const double *d_coef, double c_mass, double c_stiff,

@@ -15,6 +15,8 @@ quadraticStiffnessMatrix        src/FEM3D.jl:378-395                           s
 quadraticMassMatrix             src/FEM3D.jl:494-561                           scipy CSC
 quadraticStiffnessMatrix2D      src/FEM2D.jl:117-137                           scipy CSC
 quadraticMassMatrix2D           src/FEM2D.jl:163-229                           scipy CSC
+lagrange(mesh)                  src/FEM3D.jl:274-281                           ndarray (nv)
+BoundaryIntegral(mesh, F)       src/FEM3D.jl:284-297                           ndarray (nv)
 cg(A, b)                        IterativeSolvers.cg (e.g. run.jl:141)          ndarray
 magnetostatics_linear           Magnetostatics/magneticField.jl:89-132         (u, H, stats)
 newton_magnetostatics           Magnetostatics/NewtonRaphson.jl:109-214        (u, H, mu, stats)
@@ -40,7 +42,7 @@ from . import _lib as L
 from .mesh import MESH, MU0, box_tet_mesh, box_tri_mesh  # noqa: F401
 
 __all__ = [
-    "GPUMesh", "gpu_mesh", "stiffnessMatrix", "localStiffnessMatrix", "tangentialStiffnessMatrix", "massMatrix",
+    "GPUMesh", "gpu_mesh", "lagrange", "BoundaryIntegral", "stiffnessMatrix", "localStiffnessMatrix", "tangentialStiffnessMatrix", "massMatrix",
     "stiffnessMatrix2D", "massMatrix2D", "quadraticStiffnessMatrix", "quadraticMassMatrix",
     "quadraticStiffnessMatrix2D", "quadraticMassMatrix2D", "cg", "spmv", "magnetostatics_linear",
     "newton_magnetostatics", "hfield", "heat_be", "adjoint_dJdmu", "batch_magnetostatics_linear", "magnetostatics_sweep", "solve_opts", "newton_opts", "MESH", "MU0", "box_tet_mesh", "box_tri_mesh",
@@ -149,6 +151,26 @@ def localStiffnessMatrix(mesh: MESH, f=None):
     Ak = np.zeros(16 * mesh.nt)
     L.check(L.lib().fg_local_stiffness(g.h, L.ptr(fv), L.ptr(Ak)))
     return Ak.reshape(mesh.nt, 16).T
+
+
+def lagrange(mesh: MESH):
+    """Lagrange-multiplier row C_i = sum over the elements of node i of VE/4 (src/FEM3D.jl:274-281)."""
+    g = gpu_mesh(mesh)
+    C_ = np.zeros(mesh.nv)
+    L.check(L.lib().fg_lagrange(g.h, L.ptr(C_)))
+    return C_
+
+
+def BoundaryIntegral(mesh: MESH, F, shell_id=(1,)):
+    """Neumann right-hand side (n . F) AE / 3 on the faces of the given boundary ids (src/FEM3D.jl:284-297)."""
+    g = gpu_mesh(mesh)
+    sT = _c(mesh.surfaceT.T, np.int32)
+    RHS = np.zeros(mesh.nv)
+    sh = _c(shell_id, np.int32)
+    L.check(L.lib().fg_boundary_integral(g.h, L.ptr(sT), mesh.ns, 0, L.ptr(_c(mesh.normal.T, np.float64)),
+                                         L.ptr(_c(mesh.AE, np.float64)), L.ptr(_c(F, np.float64)), L.ptr(sh),
+                                         len(sh), L.ptr(RHS)))
+    return RHS
 
 
 def solve_opts(precision="fp64", rtol=1e-10, maxiter=1_000_000, inner_rtol=1e-5, check_every=32, use_graph=True,

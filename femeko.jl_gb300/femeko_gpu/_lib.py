@@ -82,6 +82,8 @@ SIGNATURES = {
     "fg_mass": [_vp, _vp, _i32, _vp],
     "fg_tangent": [_vp, _vp, _vp, _vp],
     "fg_local_stiffness": [_vp, _vp, _vp],
+    "fg_lagrange": [_vp, _vp],
+    "fg_boundary_integral": [_vp, _vp, _i64, _i32, _vp, _vp, _vp, _vp, _i32, _vp],
     "fg_cg_csc": [_i64, _vp, _vp, _vp, _i32, _vp, _vp, C.POINTER(SolveOpts), C.POINTER(SolveStats)],
     "fg_spmv_csc": [_i64, _vp, _vp, _vp, _i32, _vp, _vp],
     "fg_cg_csc_noalloc": [_i64, _vp, _vp, _vp, _i32, _vp, _vp, C.POINTER(SolveOpts), _vp, C.POINTER(SolveStats)],

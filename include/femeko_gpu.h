@@ -166,6 +166,17 @@ fg_status fg_tangent(fg_mesh *m, const double *H, const double *dmu, double *nzv
  * element matrix in column-major order). */
 fg_status fg_local_stiffness(fg_mesh *m, const double *f, double *Ak);
 
+/* ------------------------------------------------------------ right-hand sides */
+/* src/FEM3D.jl:274-281 lagrange: C (nv) with C_i = sum of VE/4 over the P1
+ * tetrahedra of node i (the Lagrange-multiplier row). */
+fg_status fg_lagrange(fg_mesh *m, double *C);
+/* src/FEM3D.jl:284-297 BoundaryIntegral: RHS (nv) with RHS[face nodes] += (n . F) AE/3
+ * over the boundary faces whose id (row 4 of surfaceT, 4 x ns) is one of shell_id
+ * (nshell ids); normal 3 x ns, AE ns, F 3; face nodes carry index_base. */
+fg_status fg_boundary_integral(fg_mesh *m, const int32_t *surfaceT, int64_t ns, int32_t index_base,
+                               const double *normal, const double *AE, const double *F, const int32_t *shell_id,
+                               int32_t nshell, double *RHS);
+
 /* ------------------------------------------------------------------- solvers */
 /* Drop-in for IterativeSolvers.cg(A, b) (Magnetostatics/2DmagneticField.jl:139,
  * Micromagnetics/LL.jl:185, Femeko_jl_C++/Magnetostatics/run.jl:141) and Eigen's

@@ -216,6 +216,15 @@ def test_autotune_and_forced_variants_agree():
     assert us[chosen.value] == us.min()
 
 
+def test_lagrange_and_boundary_integral(tet):
+    """src/FEM3D.jl:274-297 right-hand sides vs the oracle (FP64, same sums)."""
+    assert rel(fg.lagrange(tet), O.lagrange(tet)) < 1e-14
+    F = np.array([1.0, -2.0, 0.5])
+    assert rel(fg.BoundaryIntegral(tet, F), O.BoundaryIntegral(tet, F)) < 1e-14
+    # a boundary id that no face carries gives zero
+    assert np.abs(fg.BoundaryIntegral(tet, F, shell_id=(7,))).max() == 0.0
+
+
 def test_hfield(tet):
     u = np.random.default_rng(10).normal(size=tet.nv)
     assert rel(fg.hfield(tet, u), O.hfield(tet, u)) < 1e-12
