@@ -30,6 +30,9 @@
 // the Newton loop itself is that refinement.
 #include <algorithm>
 #include <cmath>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "fg_async.cuh"
@@ -1316,6 +1319,32 @@ static int run_cg(fg_mesh *m, bool mixed, const fg_solve_opts &o, int *status) {
 fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_variant);
 fg_status fg_autotune_spmv64(fg_mesh *m, int reps, int *chosen, double *us_per_variant);
 
+// Process-wide memory of the autotuner's choices, keyed by the device and the shape
+// of the operator (rows, padded entries, longest row, halo rows per block, column
+// format): a new handle for a mesh of the same structure (the one-shot entry points
+// create one per call) reuses the choice instead of timing the variants again.
+namespace {
+std::mutex g_tune_lock;
+std::map<std::tuple<int, int64_t, int64_t, int, int, int, bool>, int> g_tune;
+std::tuple<int, int64_t, int64_t, int, int, int, bool> tune_key(const fg_mesh *m, bool mixed) {
+  return std::make_tuple(m->device, m->nv, m->nsell, m->maxrow4, m->hrows, (int)m->use_dcol, mixed);
+}
+}  // namespace
+
+static bool tune_cache_get(fg_mesh *m, bool mixed) {
+  std::lock_guard<std::mutex> g(g_tune_lock);
+  auto it = g_tune.find(tune_key(m, mixed));
+  if (it == g_tune.end()) return false;
+  if (mixed) { m->spmv_variant32 = it->second; m->tuned32 = true; }
+  else { m->spmv_variant64 = it->second; m->tuned64 = true; }
+  return true;
+}
+
+static void tune_cache_put(fg_mesh *m, bool mixed) {
+  std::lock_guard<std::mutex> g(g_tune_lock);
+  g_tune[tune_key(m, mixed)] = mixed ? m->spmv_variant32 : m->spmv_variant64;
+}
+
 // Inner solve of A d = scale * r64 from d = 0 to relative residual `inner`, then
 // x += d / scale.  Returns iterations; *ist = 0 converged, 1 cap, 2 non-finite.
 static int inner_solve(fg_mesh *m, bool mixed, const double *r64, double rn, double inner, int maxit,
@@ -1330,15 +1359,19 @@ static int inner_solve(fg_mesh *m, bool mixed, const double *r64, double rn, dou
       const bool avail = v < 4 || v == 6 || v == 8 || v == 9 || ((v == 4 || v == 7) && m->halo_col) ||
                          (v == 5 && pipe_available(m));
       m->spmv_variant32 = avail ? v : 0;
-    } else if (!m->tuned32) {
+    } else if (!m->tuned32 && !tune_cache_get(m, true)) {
       fg_autotune_spmv32(m, 20, nullptr, nullptr);
+      tune_cache_put(m, true);
     }
     start_cg(m, true, r64, 1.0 / rn, inner * inner, maxit);
     its = run_cg(m, true, o, ist);
     k_axpy_to64<float><<<red_grid(m->nv), 256, 0, m->stream>>>(m->nv, rn, m->v32[0], d_x);
   } else {
     ensure_cg64(m);
-    if (!m->tuned64) fg_autotune_spmv64(m, 20, nullptr, nullptr);
+    if (!m->tuned64 && !tune_cache_get(m, false)) {
+      fg_autotune_spmv64(m, 20, nullptr, nullptr);
+      tune_cache_put(m, false);
+    }
     start_cg(m, false, r64, 1.0 / rn, inner * inner, maxit);
     its = run_cg(m, false, o, ist);
     k_axpy_to64<double><<<red_grid(m->nv), 256, 0, m->stream>>>(m->nv, rn, m->v64[0], d_x);
@@ -1711,6 +1744,7 @@ extern "C" fg_status fg_autotune(fg_mesh *m, int32_t precision, int32_t *variant
       st = fg_autotune_spmv64(m, 50, &chosen, us);
       nv = FG_N_SPMV64;
     }
+    tune_cache_put(m, precision == FG_MIXED);
     if (variant) *variant = chosen;
     if (us_per_variant)
       for (int v = 0; v < nv && v < n_slots; ++v) us_per_variant[v] = us[v];

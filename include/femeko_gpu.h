@@ -317,8 +317,11 @@ fg_status fg_bench_kernel(fg_mesh *m, int32_t which, int32_t precision, int32_t 
  * be NULL) the measured microseconds per launch.  No reference counterpart. */
 fg_status fg_autotune(fg_mesh *m, int32_t precision, int32_t *variant, double *us_per_variant, int32_t n_slots);
 /* Fixes the CG kernel variant of one precision for the handle (the numbering of
- * fg_solve_opts.spmv: FG_MIXED 1..10, FG_FP64 1..2), or 0 to let the autotuner choose
- * again at the next solve.  No reference counterpart (profiling and tuning control). */
+ * fg_solve_opts.spmv: FG_MIXED 1..10, FG_FP64 1..2), or 0 to return to the
+ * autotuner's choice at the next solve.  The autotuner's choices are remembered per
+ * process for each operator shape (device, rows, padded entries, longest row), so a
+ * new handle for a mesh of the same structure does not time the variants again.
+ * No reference counterpart (profiling and tuning control). */
 fg_status fg_set_cg_variant(fg_mesh *m, int32_t precision, int32_t variant);
 /* Padded sizes of the device layouts: SELL-32 matrix entries, incidence records, slices. */
 fg_status fg_mesh_layout(const fg_mesh *m, int64_t *nsell, int64_t *ninc, int32_t *nslices);
