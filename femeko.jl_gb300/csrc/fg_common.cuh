@@ -182,6 +182,8 @@ struct fg_mesh {
   int *nl_rows = nullptr, *nl_row_ptr = nullptr, *nl_row_src = nullptr;
   double *nl_re = nullptr, *nl_ke = nullptr;     // 4 / 16 per nonlinear element
   std::vector<int> nl_list_host;                 // the list the maps were built for
+  std::vector<uint8_t> nl_host;                  // nonlinear mask of the current Newton inputs
+  double *u0dev = nullptr;                       // Dirichlet values / initial guess of the Newton inputs
   bool nl_maps_valid = false;
   uint8_t *target = nullptr;  // nt objective mask (adjoint)
   double *objbuf = nullptr;   // 2 x nt objective scratch (adjoint)

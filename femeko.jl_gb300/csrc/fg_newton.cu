@@ -203,31 +203,79 @@ static int newton_dev(fg_mesh *m, double *d_u, const uint8_t *nl_host, const fg_
   return converged ? 0 : 1;
 }
 
+static fg_newton_opts checked_opts(const fg_newton_opts *o) {
+  fg_newton_opts opts;
+  fg_newton_opts_default(&opts);
+  if (o) opts = *o;
+  FG_REQUIRE(opts.Hk > 0.0 && opts.tol_update > 0.0 && opts.maxit > 0, FG_BAD_ARG,
+             "fg_newton_magnetostatics: bad options");
+  return opts;
+}
+
+static void set_inputs(fg_mesh *m, const uint8_t *nl, const double *mu_lin, const double *u0) {
+  FG_REQUIRE(m && nl && mu_lin && u0, FG_BAD_ARG, "fg_newton_magnetostatics: null pointer");
+  FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "fg_newton_magnetostatics: P1 tetrahedra only");
+  ensure_element_state(m);
+  upload(m, m->nl, nl, (size_t)m->nt);
+  upload(m, m->mu_lin, mu_lin, sizeof(double) * (size_t)m->nt);
+  if (!m->u0dev) m->u0dev = dev_alloc<double>(m, (size_t)m->nv);
+  upload(m, m->u0dev, u0, sizeof(double) * (size_t)m->nv);
+  m->nl_host.assign(nl, nl + m->nt);
+}
+
+// Newton solve from the inputs held on the device; u, H and mu stay on the device.
+static int solve_resident(fg_mesh *m, const fg_newton_opts &opts, fg_newton_stats *s) {
+  FG_REQUIRE(m->nl_host.size() == (size_t)m->nt, FG_BAD_ARG, "fg_newton_solve_resident: no inputs set");
+  double *d_u = vec64(m, 7);
+  FG_CUDA_TRY(cudaMemcpyAsync(d_u, m->u0dev, sizeof(double) * (size_t)m->nv, cudaMemcpyDeviceToDevice,
+                              m->stream));
+  const int rc = newton_dev(m, d_u, m->nl_host.data(), opts, s);
+  fg_hfield_dev(m, d_u, m->H);
+  fg_sync(m);
+  return rc;
+}
+
+static void get_outputs(fg_mesh *m, double *u, double *H, double *mu) {
+  if (u) download(m, u, m->v64[7], sizeof(double) * (size_t)m->nv);
+  if (H) download(m, H, m->H, sizeof(double) * 3 * (size_t)m->nt);
+  if (mu) download(m, mu, m->mu, sizeof(double) * (size_t)m->nt);
+  fg_sync(m);
+}
+
 extern "C" fg_status fg_newton_magnetostatics(fg_mesh *m, const uint8_t *nl, const double *mu_lin, const double *u0,
                                               const fg_newton_opts *o, double *u, double *H, double *mu,
                                               fg_newton_stats *s) {
   return fg_guard([&]() -> fg_status {
-    FG_REQUIRE(m && nl && mu_lin && u0 && u, FG_BAD_ARG, "fg_newton_magnetostatics: null pointer");
-    FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "fg_newton_magnetostatics: P1 tetrahedra only");
-    fg_newton_opts opts;
-    fg_newton_opts_default(&opts);
-    if (o) opts = *o;
-    FG_REQUIRE(opts.Hk > 0.0 && opts.tol_update > 0.0 && opts.maxit > 0, FG_BAD_ARG,
-               "fg_newton_magnetostatics: bad options");
-    ensure_element_state(m);
-    upload(m, m->nl, nl, (size_t)m->nt);
-    upload(m, m->mu_lin, mu_lin, sizeof(double) * (size_t)m->nt);
-    double *d_u = vec64(m, 7);
-    upload(m, d_u, u0, sizeof(double) * (size_t)m->nv);
-    int rc = newton_dev(m, d_u, nl, opts, s);
-    download(m, u, d_u, sizeof(double) * (size_t)m->nv);
-    if (H) {
-      fg_hfield_dev(m, d_u, m->H);
-      download(m, H, m->H, sizeof(double) * 3 * (size_t)m->nt);
-    }
-    if (mu) download(m, mu, m->mu, sizeof(double) * (size_t)m->nt);
-    fg_sync(m);
+    FG_REQUIRE(u != nullptr, FG_BAD_ARG, "fg_newton_magnetostatics: null pointer");
+    const fg_newton_opts opts = checked_opts(o);
+    set_inputs(m, nl, mu_lin, u0);
+    const int rc = solve_resident(m, opts, s);
+    get_outputs(m, u, H, mu);
     return rc == 0 ? FG_OK : FG_NOT_CONVERGED;
+  });
+}
+
+extern "C" fg_status fg_newton_set_inputs(fg_mesh *m, const uint8_t *nl, const double *mu_lin, const double *u0) {
+  return fg_guard([&]() -> fg_status {
+    set_inputs(m, nl, mu_lin, u0);
+    fg_sync(m);
+    return FG_OK;
+  });
+}
+
+extern "C" fg_status fg_newton_solve_resident(fg_mesh *m, const fg_newton_opts *o, fg_newton_stats *s) {
+  return fg_guard([&]() -> fg_status {
+    FG_REQUIRE(m != nullptr, FG_BAD_ARG, "fg_newton_solve_resident: null handle");
+    const fg_newton_opts opts = checked_opts(o);
+    return solve_resident(m, opts, s) == 0 ? FG_OK : FG_NOT_CONVERGED;
+  });
+}
+
+extern "C" fg_status fg_newton_get_outputs(fg_mesh *m, double *u, double *H, double *mu) {
+  return fg_guard([&]() -> fg_status {
+    FG_REQUIRE(m != nullptr && m->v64[7] && m->H && m->mu, FG_BAD_ARG, "fg_newton_get_outputs: nothing solved");
+    get_outputs(m, u, H, mu);
+    return FG_OK;
   });
 }
 
@@ -310,6 +358,7 @@ extern "C" fg_status fg_adjoint_dJdmu(fg_mesh *m, const double *mur, const doubl
     } else {
       upload(m, m->nl, nl, (size_t)nt);
       fg_newton_stats ns{};
+      m->nl_host.assign(nl, nl + nt);
       converged = newton_dev(m, d_u, nl, opts, &ns) == 0;
       fwd_iters = ns.cg_iters;
       newton_iters = ns.newton_iters;

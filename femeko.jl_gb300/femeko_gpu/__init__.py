@@ -45,7 +45,7 @@ __all__ = [
     "GPUMesh", "gpu_mesh", "lagrange", "BoundaryIntegral", "stiffnessMatrix", "localStiffnessMatrix", "tangentialStiffnessMatrix", "massMatrix",
     "stiffnessMatrix2D", "massMatrix2D", "quadraticStiffnessMatrix", "quadraticMassMatrix",
     "quadraticStiffnessMatrix2D", "quadraticMassMatrix2D", "cg", "spmv", "magnetostatics_linear",
-    "newton_magnetostatics", "hfield", "heat_be", "adjoint_dJdmu", "batch_magnetostatics_linear", "magnetostatics_sweep", "solve_opts", "newton_opts", "MESH", "MU0", "box_tet_mesh", "box_tri_mesh",
+    "newton_magnetostatics", "ResidentNewton", "hfield", "heat_be", "adjoint_dJdmu", "batch_magnetostatics_linear", "magnetostatics_sweep", "solve_opts", "newton_opts", "MESH", "MU0", "box_tet_mesh", "box_tri_mesh",
 ]
 
 
@@ -322,6 +322,29 @@ def adjoint_dJdmu(mesh: MESH, mur, u0, target, nl=None, rtol=1e-12, **kw):
                                   L.ptr(u), C.byref(s))
     L.check(st, allow_not_converged=True)
     return J.value, grad, u, L.stats_dict(s)
+
+
+class ResidentNewton:
+    """Newton magnetostatics kept on the device: inputs uploaded once, each solve()
+    runs from them and leaves u, H, mu on the GPU until outputs() downloads them."""
+
+    def __init__(self, mesh: MESH, nl, mu_lin, u0):
+        self.mesh = mesh
+        self.g = gpu_mesh(mesh)
+        self._in = (_c(nl, np.uint8), _c(mu_lin, np.float64), _c(u0, np.float64))
+        L.check(L.lib().fg_newton_set_inputs(self.g.h, *(L.ptr(a) for a in self._in)))
+
+    def solve(self, **kw):
+        o = newton_opts(**kw)
+        s = L.NewtonStats()
+        L.check(L.lib().fg_newton_solve_resident(self.g.h, C.byref(o), C.byref(s)), allow_not_converged=True)
+        return L.stats_dict(s)
+
+    def outputs(self):
+        m = self.mesh
+        u, H, mu = np.zeros(m.nv), np.zeros(3 * m.nt), np.zeros(m.nt)
+        L.check(L.lib().fg_newton_get_outputs(self.g.h, L.ptr(u), L.ptr(H), L.ptr(mu)))
+        return u, H.reshape(m.nt, 3).T, mu
 
 
 def hfield(mesh: MESH, u):

@@ -287,6 +287,13 @@ typedef struct fg_adjoint_stats {
 fg_status fg_adjoint_dJdmu(fg_mesh *m, const double *mur, const double *u0, const uint8_t *target,
                            const uint8_t *nl, const fg_newton_opts *o, double rtol, double *J, double *grad,
                            double *u, fg_adjoint_stats *s);
+/* The same solve in three steps, for callers that keep the problem on the device
+ * and solve it repeatedly: fg_newton_set_inputs uploads nl, mu_lin and u0 once;
+ * fg_newton_solve_resident runs the Newton solve from them and leaves u, H and mu
+ * on the device; fg_newton_get_outputs downloads them (each may be NULL). */
+fg_status fg_newton_set_inputs(fg_mesh *m, const uint8_t *nl, const double *mu_lin, const double *u0);
+fg_status fg_newton_solve_resident(fg_mesh *m, const fg_newton_opts *o, fg_newton_stats *s);
+fg_status fg_newton_get_outputs(fg_mesh *m, double *u, double *H, double *mu);
 /* H = -sum u_a grad(phi_a) per element (Magnetostatics/magneticField.jl:111-124). */
 fg_status fg_hfield(fg_mesh *m, const double *u, double *H);
 

@@ -145,6 +145,18 @@ def test_newton(precision):
     assert np.abs(mug - muo).max() / muo.max() < 1e-8
 
 
+def test_resident_newton_same_as_one_call():
+    """set inputs once / solve on the device / get outputs == the one-call entry point."""
+    m, nl, mu_lin, u0 = newton_case()
+    ug, Hg, mug, st = fg.newton_magnetostatics(m, nl, mu_lin, u0, precision="mixed")
+    r = fg.ResidentNewton(m, nl, mu_lin, u0)
+    for _ in range(2):   # repeated solves start from the stored inputs
+        s2 = r.solve(precision="mixed")
+        u2, H2, mu2 = r.outputs()
+        assert s2["newton_iters"] == st["newton_iters"] and s2["cg_iters"] == st["cg_iters"]
+        assert np.array_equal(u2, ug) and np.array_equal(H2, Hg) and np.array_equal(mu2, mug)
+
+
 def test_newton_reference_line_search_same_iterates():
     """The reference lineSearch (frozen secant, src/FEM3D.jl:123-152) converges only
     linearly; with tight inner solves the GPU follows the oracle's iterates."""
