@@ -200,6 +200,28 @@ function cg(A::SparseMatrixCSC{Float64,Int64}, b::Vector{Float64}; reltol=sqrt(e
     return x
 end
 
+"""lagrange(mesh) -- the Lagrange-multiplier row of src/FEM3D.jl:274-281."""
+function lagrange(mesh)
+    g = gpu(mesh)
+    C = zeros(g.nv)
+    check(ccall((:fg_lagrange, libpath()), Cint, (Ptr{Cvoid}, Ptr{Float64}), g.h, C))
+    return C
+end
+
+"""BoundaryIntegral(mesh, F, shell_id) -- Neumann right-hand side of src/FEM3D.jl:284-297
+(mesh.surfaceT is 4 x ns, 1-based, boundary id in row 4)."""
+function BoundaryIntegral(mesh, F::Vector{Float64}, shell_id)
+    g = gpu(mesh)
+    RHS = zeros(g.nv)
+    ids = Int32.(collect(shell_id))
+    check(ccall((:fg_boundary_integral, libpath()), Cint,
+                (Ptr{Cvoid}, Ptr{Int32}, Int64, Int32, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Int32}, Int32,
+                 Ptr{Float64}),
+                g.h, Int32.(mesh.surfaceT), size(mesh.surfaceT, 2), 1, mesh.normal, mesh.AE, F, ids, length(ids),
+                RHS))
+    return RHS
+end
+
 """heat_be(mesh, T, kappa, fixed; rho_c=1.0, dt=1e-3, nsteps=100, every=10, precision=:mixed)
 -- the backward-Euler loop of Heat/heat3D.jl:83-89 with T = 0 on the `fixed` nodes.
 Returns (T after nsteps, snapshots nv x (nsteps ÷ every), stats)."""
