@@ -201,6 +201,8 @@ struct fg_mesh {
   int *hint = nullptr;        // pinned host ints (16)
 
   GraphCache graph[4];
+  int64_t l2_win_bytes = 0;  // L2 access-policy window on val32 (0: not set up, -1: unavailable)
+  float l2_hit_ratio = 0.f;
   int spmv_variant32 = 0;     // FP32 CG iteration variant chosen by the autotuner
   int spmv_variant64 = 0;     // FP64 CG SpMV variant chosen by the autotuner
   bool tuned32 = false, tuned64 = false;
@@ -225,6 +227,8 @@ void fg_count_launch(long long n);
 #define FG_LAUNCHED(n) fg_count_launch(n)
 
 void fg_check_flags(fg_mesh *m, const char *where);
+// Releases the handle's share of the persisting-L2 set-aside (fg_solve.cu).
+void fg_release_l2(fg_mesh *m);
 void fg_sync(fg_mesh *m);
 // Builds the halo lists and local column indices (needs sl_ptr/sl_len/sl_col, maxrow4).
 void fg_build_halo(fg_mesh *m);

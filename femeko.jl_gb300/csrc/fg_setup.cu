@@ -616,6 +616,7 @@ extern "C" fg_status fg_mesh_destroy(fg_mesh *m) {
   return fg_guard([&]() -> fg_status {
     if (!m) return FG_OK;
     cudaStreamSynchronize(m->stream);
+    fg_release_l2(m);
     free_mesh(m);
     return FG_OK;
   });

@@ -1037,8 +1037,8 @@ static void ensure_cg64(fg_mesh *m) {
 // 0-3 fused iteration with direct gathers, 4 fused with halo staging, 5 fused and
 // pipelined, 6 split (vector pass + SpMV) with direct gathers, 7 split with halo
 // staging, 8 split with direct gathers in a persistent grid, 9 the same launched with
-// programmatic dependent launch
-constexpr int FG_N_SPMV32 = 10;
+// programmatic dependent launch, 10 the same with the matrix values held in L2
+constexpr int FG_N_SPMV32 = 11;
 static inline bool split32(int v) { return v >= 6; }
 constexpr int FG_N_SPMV64 = 2;   // 0 direct gathers, 1 halo staging
 
@@ -1168,9 +1168,84 @@ static void pdl_launch(bool pdl, void (*kern)(KArgs...), unsigned grid, unsigned
   FG_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...));
 }
 
+// L2 residency of the FP32 matrix values (variant 10): an access-policy window on
+// the SpMV launches marks the values persisting in a set-aside part of L2, so that
+// the ~100 iterations of an inner solve read them from L2 instead of HBM.  The
+// set-aside is a limit of this process's context, sized once per device to the
+// largest operator seen and released when the last handle using it is destroyed.
+namespace {
+std::mutex g_l2_lock;
+size_t g_l2_setaside[64] = {0};
+int g_l2_users[64] = {0};
+}  // namespace
+
+static bool prepare_l2(fg_mesh *m) {
+  if (m->l2_win_bytes > 0) return true;
+  if (m->l2_win_bytes < 0 || !m->val32 || m->device < 0 || m->device >= 64) return false;
+  int max_persist = 0, max_win = 0;
+  if (cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, m->device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&max_win, cudaDevAttrMaxAccessPolicyWindowSize, m->device) != cudaSuccess ||
+      max_persist <= 0 || max_win <= 0) {
+    cudaGetLastError();
+    m->l2_win_bytes = -1;
+    return false;
+  }
+  const size_t want = sizeof(float) * (size_t)m->nsell;
+  std::lock_guard<std::mutex> g(g_l2_lock);
+  const size_t setaside = std::min(want, (size_t)max_persist);
+  if (setaside > g_l2_setaside[m->device]) {
+    FG_CUDA_TRY(cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, setaside));
+    g_l2_setaside[m->device] = setaside;
+  }
+  ++g_l2_users[m->device];
+  m->l2_win_bytes = (int64_t)std::min(want, (size_t)max_win);
+  m->l2_hit_ratio = (float)std::min(1.0, (double)g_l2_setaside[m->device] / (double)m->l2_win_bytes);
+  return true;
+}
+
+void fg_release_l2(fg_mesh *m) {
+  if (m->l2_win_bytes <= 0) return;
+  std::lock_guard<std::mutex> g(g_l2_lock);
+  cudaCtxResetPersistingL2Cache();
+  if (--g_l2_users[m->device] == 0) {
+    cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
+    g_l2_setaside[m->device] = 0;
+  }
+  cudaGetLastError();
+  m->l2_win_bytes = 0;
+}
+
+template <typename... KArgs, typename... Args>
+static void l2_launch(fg_mesh *m, void (*kern)(KArgs...), unsigned grid, unsigned block, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.stream = m->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeAccessPolicyWindow;
+  attr[0].val.accessPolicyWindow.base_ptr = (void *)m->val32;
+  attr[0].val.accessPolicyWindow.num_bytes = (size_t)m->l2_win_bytes;
+  attr[0].val.accessPolicyWindow.hitRatio = m->l2_hit_ratio;
+  attr[0].val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+  attr[0].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  FG_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...));
+}
+
 static void launch_spmv32s(fg_mesh *m, int v) {
   const bool pdl = (v == 9);
-  if (v == 8 || v == 9) {
+  if (v == 10 && m->l2_win_bytes > 0) {
+    const unsigned g = std::min<unsigned>(grid_for(m->nv, 256), 8u * (unsigned)std::max(m->sm_count, 1));
+    if (m->use_dcol)
+      l2_launch(m, k_cg32s_spmv<ColRel, true>, g, 256, m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, m->val32,
+                m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl, m->red.partials, m->red.counter);
+    else
+      l2_launch(m, k_cg32s_spmv<ColAbs, true>, g, 256, m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val32,
+                m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl, m->red.partials, m->red.counter);
+    return;
+  }
+  if (v == 8 || v == 9 || v == 10) {
     // persistent: at most 8 resident 256-thread blocks per SM
     const unsigned g = std::min<unsigned>(grid_for(m->nv, 256), 8u * (unsigned)std::max(m->sm_count, 1));
     if (m->use_dcol)
@@ -1356,13 +1431,14 @@ static int inner_solve(fg_mesh *m, bool mixed, const double *r64, double rn, dou
       // a forced variant that this operator cannot run (no halo lists, stages too
       // large for shared memory) falls back to the plain gather kernel
       const int v = o.spmv - 1;
-      const bool avail = v < 4 || v == 6 || v == 8 || v == 9 || ((v == 4 || v == 7) && m->halo_col) ||
-                         (v == 5 && pipe_available(m));
+      const bool avail = v < 4 || v == 6 || v == 8 || v == 9 || (v == 10 && prepare_l2(m)) ||
+                         ((v == 4 || v == 7) && m->halo_col) || (v == 5 && pipe_available(m));
       m->spmv_variant32 = avail ? v : 0;
     } else if (!m->tuned32 && !tune_cache_get(m, true)) {
       fg_autotune_spmv32(m, 20, nullptr, nullptr);
       tune_cache_put(m, true);
     }
+    if (m->spmv_variant32 == 10 && !prepare_l2(m)) m->spmv_variant32 = 8;
     start_cg(m, true, r64, 1.0 / rn, inner * inner, maxit);
     its = run_cg(m, true, o, ist);
     k_axpy_to64<float><<<red_grid(m->nv), 256, 0, m->stream>>>(m->nv, rn, m->v32[0], d_x);
@@ -1638,7 +1714,8 @@ fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_v
   int best = 0;
   double best_us = 1e30;
   for (int v = 0; v < FG_N_SPMV32; ++v) {
-    if (((v == 4 || v == 7) && !m->halo_col) || (v == 5 && !pipe_available(m))) {  // not available here
+    if (((v == 4 || v == 7) && !m->halo_col) || (v == 5 && !pipe_available(m)) ||
+        (v == 10 && !prepare_l2(m))) {  // not available here
       if (us_per_variant) us_per_variant[v] = 0.0;
       continue;
     }
@@ -1714,8 +1791,8 @@ extern "C" fg_status fg_set_cg_variant(fg_mesh *m, int32_t precision, int32_t va
       FG_REQUIRE(variant >= 0 && variant <= FG_N_SPMV32, FG_BAD_ARG, "fg_set_cg_variant: no such variant");
       if (variant == 0) { m->tuned32 = false; return FG_OK; }
       const int v = variant - 1;
-      const bool avail = v < 4 || v == 6 || v == 8 || v == 9 || ((v == 4 || v == 7) && m->halo_col) ||
-                         (v == 5 && pipe_available(m));
+      const bool avail = v < 4 || v == 6 || v == 8 || v == 9 || (v == 10 && prepare_l2(m)) ||
+                         ((v == 4 || v == 7) && m->halo_col) || (v == 5 && pipe_available(m));
       FG_REQUIRE(avail, FG_UNSUPPORTED, "fg_set_cg_variant: variant not available for this operator");
       m->spmv_variant32 = v;
       m->tuned32 = true;
