@@ -587,6 +587,56 @@ __global__ void k_objective_tet4(int64_t nt, const double *__restrict__ geo, con
   v_out[k] = v;
 }
 
+// Demagnetising-field load vector of Micromagnetics/LL.jl:169-181: for an inside
+// element, VE (grad phi_a . f) with f the mean of the nodal magnetisation M (3 x nv,
+// M[3 i + c]); outside elements write 0.
+__global__ void k_demag_rhs_tet4(int64_t nt, const double *__restrict__ geo, const int *__restrict__ t,
+                                 const uint8_t *__restrict__ inside, const double *__restrict__ M,
+                                 const int *__restrict__ recpos, double *__restrict__ rec_r) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt) return;
+  double f[3] = {0.0, 0.0, 0.0};
+  const bool in = inside[k] != 0;
+  if (in)
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      const int node = t[(int64_t)a * nt + k];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) f[c] += 0.25 * M[3 * (int64_t)node + c];
+    }
+  const double VE = geo[12 * nt + k];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    double v = 0.0;
+    if (in)
+      v = VE * (geo[(int64_t)(3 * a) * nt + k] * f[0] + geo[(int64_t)(3 * a + 1) * nt + k] * f[1] +
+                geo[(int64_t)(3 * a + 2) * nt + k] * f[2]);
+    rec_r[recpos[(int64_t)a * nt + k]] = v;
+  }
+}
+
+// VE x_k on the 4 records of every inside element (x = component c of H (3 x nt), or
+// 1 when H is null: the node volumes); outside elements write 0.
+__global__ void k_inside_weighted_tet4(int64_t nt, const double *__restrict__ geo, const uint8_t *__restrict__ inside,
+                                       const double *__restrict__ H, int c, const int *__restrict__ recpos,
+                                       double *__restrict__ rec_r) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt) return;
+  const double v = inside[k] ? geo[12 * nt + k] * (H ? H[3 * k + c] : 1.0) : 0.0;
+#pragma unroll
+  for (int a = 0; a < 4; ++a) rec_r[recpos[(int64_t)a * nt + k]] = v;
+}
+
+__global__ void k_nodal_average(int64_t nv, const double *__restrict__ sx, const double *__restrict__ sy,
+                                const double *__restrict__ sz, const double *__restrict__ vol, double *__restrict__ Hn) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nv) return;
+  // plain division, 0/0 = NaN on nodes without an inside element (as the reference)
+  Hn[3 * i] = sx[i] / vol[i];
+  Hn[3 * i + 1] = sy[i] / vol[i];
+  Hn[3 * i + 2] = sz[i] / vol[i];
+}
+
 // dJ/du_a = -sum_{T owns a} VE dphi_a/dx / vol as vector records (every element writes
 // its 4 records; zero outside the target).
 __global__ void k_objective_rhs_tet4(int64_t nt, const double *__restrict__ geo,
@@ -831,6 +881,7 @@ static void launch_elem(fg_mesh *m, int kind, const double *d_f, const double *d
 void fg_assemble_operator(fg_mesh *m, int kind, const double *d_f, const double *d_H, const double *d_dmu,
                           double c_mass, double c_stiff, int full_phi, int layout, bool want64, bool want32,
                           bool apply_bc) {
+  if (layout != OUT_CSR) m->op_tag = 0;
   launch_elem(m, kind, d_f, d_H, d_dmu, c_mass, c_stiff, full_phi);
   const double *rec = static_cast<const double *>(m->rec);
   if (layout == OUT_CSR) {
@@ -847,6 +898,7 @@ void fg_newton_assemble(fg_mesh *m, const double *d_u, double Ms, double Hk, boo
                         bool want_jacobian, bool tangent) {
   const int tg = tangent ? 1 : 0;
   FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "Newton magnetostatics needs P1 tetrahedra");
+  if (want_jacobian) m->op_tag = 0;
   fg_ensure_records(m);
   ensure_operator(m, !mixed, mixed);
   unsigned g = grid_for(m->nt, 128);
@@ -1015,6 +1067,7 @@ void fg_newton_assemble_split(fg_mesh *m, const double *d_u, double Ms, double H
   FG_CUDA_TRY(cudaGetLastError());
   FG_LAUNCHED(1);
   if (!want_jacobian) return;
+  m->op_tag = 0;
   const unsigned gs = grid_for(std::max(m->n_nl_slots, 1), 128);
   if (mixed) {
     FG_CUDA_TRY(cudaMemcpyAsync(m->val32, m->vlin32, sizeof(float) * (size_t)m->nsell, cudaMemcpyDeviceToDevice,
@@ -1059,6 +1112,35 @@ void fg_energy_dev(fg_mesh *m, const double *d_u, double Ms, double Hk) {
 void fg_hfield_dev(fg_mesh *m, const double *d_u, double *d_H) {
   FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "H field needs P1 tetrahedra");
   k_hfield_tet4<<<grid_for(m->nt, 256), 256, 0, m->stream>>>(m->nt, m->geo, m->t, d_u, d_H);
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(1);
+}
+
+void fg_demag_rhs_dev(fg_mesh *m, const uint8_t *d_inside, const double *d_M, double *d_b) {
+  FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "demagnetising field: P1 tetrahedra only");
+  fg_ensure_records(m);
+  k_demag_rhs_tet4<<<grid_for(m->nt, 256), 256, 0, m->stream>>>(m->nt, m->geo, m->t, d_inside, d_M, m->recpos,
+                                                                 m->rec_r);
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(1);
+  launch_row<4, double, double>(m, nullptr, m->rec_r, 0, nullptr, nullptr, nullptr, nullptr, nullptr, d_b, 1.0, 1);
+}
+
+// Nodal field: sum over the inside elements of VE H_k at each node over the node volume.
+void fg_nodal_average_dev(fg_mesh *m, const uint8_t *d_inside, const double *d_H, double *d_work, double *d_Hn) {
+  fg_ensure_records(m);
+  const int64_t nv = m->nv;
+  for (int c = 0; c < 4; ++c) {
+    k_inside_weighted_tet4<<<grid_for(m->nt, 256), 256, 0, m->stream>>>(m->nt, m->geo, d_inside,
+                                                                       c < 3 ? d_H : nullptr, c % 3, m->recpos,
+                                                                       m->rec_r);
+    FG_CUDA_TRY(cudaGetLastError());
+    FG_LAUNCHED(1);
+    launch_row<4, double, double>(m, nullptr, m->rec_r, 0, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                  d_work + c * nv, 1.0, 0);
+  }
+  k_nodal_average<<<grid_for(nv, 256), 256, 0, m->stream>>>(nv, d_work, d_work + nv, d_work + 2 * nv,
+                                                            d_work + 3 * nv, d_Hn);
   FG_CUDA_TRY(cudaGetLastError());
   FG_LAUNCHED(1);
 }

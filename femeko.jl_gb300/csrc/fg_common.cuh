@@ -201,6 +201,10 @@ struct fg_mesh {
   int *hint = nullptr;        // pinned host ints (16)
 
   GraphCache graph[4];
+  int op_tag = 0;            // what val64/val32 hold when a caller reuses them (0: unknown)
+  uint8_t *inside = nullptr; // nt mask of the magnetic body (demagnetising field)
+  double *nodal_in = nullptr;// 3 x nv nodal magnetisation (demagnetising field)
+  double *nodal_work = nullptr; // 7 x nv: nodal sums, volumes and the nodal field
   int64_t l2_win_bytes = 0;  // L2 access-policy window on val32 (0: not set up, -1: unavailable)
   float l2_hit_ratio = 0.f;
   int spmv_variant32 = 0;     // FP32 CG iteration variant chosen by the autotuner
@@ -254,6 +258,10 @@ void fg_newton_assemble_split(fg_mesh *m, const double *d_u, double Ms, double H
                               bool want_jacobian, bool tangent);
 // d_out[i] = sum of the vector records of row i (P1 tetrahedra), no Dirichlet masking.
 void fg_vector_gather(fg_mesh *m, double *d_out);
+// Demagnetising field (Micromagnetics/LL.jl:162-211): load vector of the inside
+// elements from the nodal magnetisation, and the nodal volume average of H.
+void fg_demag_rhs_dev(fg_mesh *m, const uint8_t *d_inside, const double *d_M, double *d_b);
+void fg_nodal_average_dev(fg_mesh *m, const uint8_t *d_inside, const double *d_H, double *d_work, double *d_Hn);
 // y = vals x on the handle's pattern (FP64), Dirichlet rows 0.
 void fg_spmv64_vals(fg_mesh *m, const double *vals, const double *x, double *y);
 void fg_apply_operator_vec(fg_mesh *m, int kind, const double *d_coef, double c_mass, double c_stiff,

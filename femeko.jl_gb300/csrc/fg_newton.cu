@@ -402,6 +402,49 @@ extern "C" fg_status fg_adjoint_dJdmu(fg_mesh *m, const double *mur, const doubl
   });
 }
 
+// Demagnetising field of Micromagnetics/LL.jl:162-211 (magnetostaticField): the
+// stiffness operator of the whole mesh (assembled once and kept while nothing else
+// is assembled on the handle: the reference builds A once and calls cg every
+// Landau-Lifshitz step), the load vector of the inside elements from the nodal
+// magnetisation, the CG solve from zero, H = -grad u and its nodal volume average.
+enum { OP_DEMAG64 = 1, OP_DEMAG_MIXED = 2 };
+
+extern "C" fg_status fg_demag_field(fg_mesh *m, const uint8_t *inside, const double *M, const fg_solve_opts *o,
+                                    double *Hn, double *u, fg_solve_stats *s) {
+  return fg_guard([&]() -> fg_status {
+    FG_REQUIRE(m && inside && M && Hn, FG_BAD_ARG, "fg_demag_field: null pointer");
+    FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "fg_demag_field: P1 tetrahedra only");
+    fg_solve_opts opts;
+    fg_solve_opts_default(&opts);
+    if (o) opts = *o;
+    const bool mixed = opts.precision == FG_MIXED;
+    const int64_t nv = m->nv, nt = m->nt;
+    ensure_element_state(m);
+    if (!m->inside) m->inside = dev_alloc<uint8_t>(m, (size_t)nt);
+    if (!m->nodal_in) m->nodal_in = dev_alloc<double>(m, 3 * (size_t)nv);
+    upload(m, m->inside, inside, (size_t)nt);
+    upload(m, m->nodal_in, M, sizeof(double) * 3 * (size_t)nv);
+    const int want = mixed ? OP_DEMAG_MIXED : OP_DEMAG64;
+    if (m->op_tag != want && m->op_tag != OP_DEMAG_MIXED) {
+      fg_assemble_operator(m, ASM_STIFF, nullptr, nullptr, nullptr, 0.0, 0.0, 0, OUT_SELL, true, mixed, true);
+      m->op_tag = want;
+    }
+    double *d_b = vec64(m, 9), *d_u = vec64(m, 7);
+    fg_demag_rhs_dev(m, m->inside, m->nodal_in, d_b);
+    FG_CUDA_TRY(cudaMemsetAsync(d_u, 0, sizeof(double) * (size_t)nv, m->stream));
+    fg_solve_stats st{};
+    const int rc = fg_pcg_solve(m, d_b, d_u, opts, &st, false);
+    fg_hfield_dev(m, d_u, m->H);
+    if (!m->nodal_work) m->nodal_work = dev_alloc<double>(m, 7 * (size_t)nv);  // 4 sums + 3 x nv field
+    fg_nodal_average_dev(m, m->inside, m->H, m->nodal_work, m->nodal_work + 4 * nv);
+    download(m, Hn, m->nodal_work + 4 * nv, sizeof(double) * 3 * (size_t)nv);
+    if (u) download(m, u, d_u, sizeof(double) * (size_t)nv);
+    fg_sync(m);
+    if (s) *s = st;
+    return rc == 0 ? FG_OK : FG_NOT_CONVERGED;
+  });
+}
+
 extern "C" fg_status fg_hfield(fg_mesh *m, const double *u, double *H) {
   return fg_guard([&]() -> fg_status {
     FG_REQUIRE(m && u && H, FG_BAD_ARG, "fg_hfield: null pointer");

@@ -22,6 +22,7 @@ magnetostatics_linear           Magnetostatics/magneticField.jl:89-132         (
 newton_magnetostatics           Magnetostatics/NewtonRaphson.jl:109-214        (u, H, mu, stats)
 hfield(mesh, u)                 Magnetostatics/magneticField.jl:111-124        (3, nt) ndarray
 heat_be                         Heat/heat3D.jl:50-90                           (T, snapshots, stats)
+magnetostaticField              Micromagnetics/LL.jl:162-211                   (Hn 3 x nv, u, stats)
 batch_magnetostatics_linear     magneticField.jl:89-132 on many meshes         (u list, iters, stats)
 magnetostatics_sweep            magneticField.jl:89-132 for many fields        (U nv x nfield, stats)
 adjoint_dJdmu                   (none: gradient of NewtonRaphson.jl:234-240)   (J, grad, u, stats)
@@ -45,7 +46,7 @@ __all__ = [
     "GPUMesh", "gpu_mesh", "lagrange", "BoundaryIntegral", "stiffnessMatrix", "localStiffnessMatrix", "tangentialStiffnessMatrix", "massMatrix",
     "stiffnessMatrix2D", "massMatrix2D", "quadraticStiffnessMatrix", "quadraticMassMatrix",
     "quadraticStiffnessMatrix2D", "quadraticMassMatrix2D", "cg", "spmv", "magnetostatics_linear",
-    "newton_magnetostatics", "ResidentNewton", "hfield", "heat_be", "adjoint_dJdmu", "batch_magnetostatics_linear", "magnetostatics_sweep", "solve_opts", "newton_opts", "MESH", "MU0", "box_tet_mesh", "box_tri_mesh",
+    "newton_magnetostatics", "ResidentNewton", "hfield", "heat_be", "adjoint_dJdmu", "magnetostaticField", "batch_magnetostatics_linear", "magnetostatics_sweep", "solve_opts", "newton_opts", "MESH", "MU0", "box_tet_mesh", "box_tri_mesh",
 ]
 
 
@@ -322,6 +323,20 @@ def adjoint_dJdmu(mesh: MESH, mur, u0, target, nl=None, rtol=1e-12, **kw):
                                   L.ptr(u), C.byref(s))
     L.check(st, allow_not_converged=True)
     return J.value, grad, u, L.stats_dict(s)
+
+
+def magnetostaticField(mesh: MESH, M, inside, precision="fp64", rtol=1e-10, **kw):
+    """Demagnetising field on the nodes (Micromagnetics/LL.jl:162-211); M is 3 x nv,
+    inside the nt mask of the magnetic body.  Returns (Hn 3 x nv, u, stats)."""
+    g = gpu_mesh(mesh)
+    Hn = np.zeros(3 * mesh.nv)
+    u = np.zeros(mesh.nv)
+    o = solve_opts(precision=precision, rtol=rtol, **kw)
+    s = L.SolveStats()
+    st = L.lib().fg_demag_field(g.h, L.ptr(_c(inside, np.uint8)), L.ptr(_c(np.asarray(M).T, np.float64)),
+                                C.byref(o), L.ptr(Hn), L.ptr(u), C.byref(s))
+    L.check(st, allow_not_converged=True)
+    return Hn.reshape(mesh.nv, 3).T, u, L.stats_dict(s)
 
 
 class ResidentNewton:

@@ -90,6 +90,7 @@ SIGNATURES = {
     "fg_magnetostatics_linear": [_vp, _vp, _vp, C.POINTER(SolveOpts), _vp, _vp, C.POINTER(SolveStats)],
     "fg_newton_magnetostatics": [_vp, _vp, _vp, _vp, C.POINTER(NewtonOpts), _vp, _vp, _vp, C.POINTER(NewtonStats)],
     "fg_hfield": [_vp, _vp, _vp],
+    "fg_demag_field": [_vp, _vp, _vp, C.POINTER(SolveOpts), _vp, _vp, C.POINTER(SolveStats)],
     "fg_newton_set_inputs": [_vp, _vp, _vp, _vp],
     "fg_newton_solve_resident": [_vp, C.POINTER(NewtonOpts), C.POINTER(NewtonStats)],
     "fg_newton_get_outputs": [_vp, _vp, _vp, _vp],

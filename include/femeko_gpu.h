@@ -296,6 +296,16 @@ fg_status fg_adjoint_dJdmu(fg_mesh *m, const double *mur, const double *u0, cons
 fg_status fg_newton_set_inputs(fg_mesh *m, const uint8_t *nl, const double *mu_lin, const double *u0);
 fg_status fg_newton_solve_resident(fg_mesh *m, const fg_newton_opts *o, fg_newton_stats *s);
 fg_status fg_newton_get_outputs(fg_mesh *m, double *u, double *H, double *mu);
+/* Demagnetising field of Micromagnetics/LL.jl:162-211 (magnetostaticField), the
+ * Poisson solve of every Landau-Lifshitz step: RHS_i = sum over the inside elements
+ * (inside[k] != 0) of VE (grad phi_i . mean nodal M), u = PCG(A, RHS) from zero with
+ * A the stiffness matrix (assembled on the first call and kept for the next ones;
+ * Dirichlet rows of fg_mesh_set_dirichlet apply if set, the reference has none),
+ * H = -grad u per element, and Hn (3 x nv) its volume-weighted nodal average over
+ * the inside elements (NaN on nodes with no inside element, as the reference's
+ * division by a zero node volume).  M is 3 x nv; u (nv) may be NULL. */
+fg_status fg_demag_field(fg_mesh *m, const uint8_t *inside, const double *M, const fg_solve_opts *o, double *Hn,
+                         double *u, fg_solve_stats *s);
 /* H = -sum u_a grad(phi_a) per element (Magnetostatics/magneticField.jl:111-124). */
 fg_status fg_hfield(fg_mesh *m, const double *u, double *H);
 

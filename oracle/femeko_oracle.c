@@ -956,3 +956,51 @@ int or_adjoint(const double *p, const int *t, int nv, long nt, const double *VE,
   free(cp); free(ri); free(Av); free(g);
   return it < 0 ? 1 : 0;
 }
+
+/* Demagnetising field of Micromagnetics/LL.jl:162-211 (magnetostaticField): load
+ * vector RHS_i = sum over the inside elements of VE (grad phi_i . mean nodal M),
+ * u = PCG(A, RHS) with A the stiffness matrix of the whole mesh (no Dirichlet rows;
+ * the Neumann problem is consistent), H_k = -grad u per element, and the nodal field
+ * sum over the inside elements of VE H_k divided by the node volumes (the sum of VE
+ * of the inside elements of the node; 0/0 where a node has none, as the reference).
+ * M is 3 x nv (M[3*i + c]); Hn is 3 x nv. */
+int or_demag_field(const double *p, const int *t, int nv, long nt, const double *VE, const unsigned char *inside,
+                   const double *M, double cg_tol, int cg_maxit, double *u, double *Hn, int *iters) {
+  long *cp = (long *)malloc(sizeof(long) * ((size_t)nv + 1));
+  int *ri = (int *)malloc(sizeof(int) * 16 * (size_t)nt);
+  double *Av = (double *)malloc(sizeof(double) * 16 * (size_t)nt);
+  or_stiffness(p, t, nv, nt, VE, NULL, 0, cp, ri, Av);
+  double *rhs = (double *)calloc((size_t)nv, sizeof(double));
+  double *vol = (double *)calloc((size_t)nv, sizeof(double));
+  for (long k = 0; k < nt; ++k) {
+    if (!inside[k]) continue;
+    const int *nds = t + 4 * k;
+    double f[3] = {0, 0, 0};
+    for (int a = 0; a < 4; ++a)
+      for (int c = 0; c < 3; ++c) f[c] += M[3 * nds[a] + c] / 4.0;
+    for (int a = 0; a < 4; ++a) {
+      double r[4];
+      or_abcd(p, nds, nds[a], r);
+      rhs[nds[a]] += VE[k] * (r[1] * f[0] + r[2] * f[1] + r[3] * f[2]);
+    }
+  }
+  for (int i = 0; i < nv; ++i) u[i] = 0.0;
+  double rr;
+  int it = or_pcg(nv, cp, ri, Av, rhs, u, NULL, cg_tol, cg_maxit, &rr);
+  if (iters) *iters = it;
+  double *H = (double *)malloc(sizeof(double) * 3 * (size_t)nt);
+  or_hfield(p, t, nt, u, 0, H);
+  for (int i = 0; i < 3 * nv; ++i) Hn[i] = 0.0;
+  for (long k = 0; k < nt; ++k) {
+    if (!inside[k]) continue;
+    const int *nds = t + 4 * k;
+    for (int a = 0; a < 4; ++a) {
+      vol[nds[a]] += VE[k];
+      for (int c = 0; c < 3; ++c) Hn[3 * nds[a] + c] += VE[k] * H[3 * k + c];
+    }
+  }
+  for (int i = 0; i < nv; ++i)
+    for (int c = 0; c < 3; ++c) Hn[3 * i + c] /= vol[i];
+  free(cp); free(ri); free(Av); free(rhs); free(vol); free(H);
+  return it < 0 ? 1 : 0;
+}

@@ -74,6 +74,9 @@ def lib():
         L.or_p2_mass2d.restype = C.c_long
         L.or_p2_mass2d.argtypes = [_dp, _ip, C.c_int, C.c_long, _dp] + csc_out
         L.or_lagrange.argtypes = [_ip, C.c_int, C.c_long, _dp, _dp]
+        L.or_demag_field.argtypes = [_dp, _ip, C.c_int, C.c_long, _dp, _bp, _dp, C.c_double, C.c_int, _dp, _dp,
+                                     C.POINTER(C.c_int)]
+        L.or_demag_field.restype = C.c_int
         L.or_boundary_integral.argtypes = [_ip, C.c_long, C.c_int, _dp, _dp, _dp, _ip, C.c_int, _dp]
         L.or_spmv.argtypes = [C.c_int, _lp, _ip, _dp, _dp, _dp]
         L.or_pcg.restype = C.c_int
@@ -333,6 +336,18 @@ def adjoint(mesh, target, mu, u, H=None, dmu=None, cg_tol=1e-12, cg_maxit=200000
     lib().or_adjoint(p, t, mesh.nv, mesh.nt, _c(mesh.VE, np.float64), mesh.dirichlet_mask(), _c(target, np.uint8),
                      _c(mu, np.float64), _ptr(Hc), _ptr(dc), _c(u, np.float64), cg_tol, cg_maxit, lam, grad)
     return grad, lam
+
+
+def magnetostaticField(mesh, M, inside, cg_tol=1e-12, cg_maxit=200000):
+    """Demagnetising field on the nodes (Micromagnetics/LL.jl:162-211); M is 3 x nv.
+    Returns (Hn 3 x nv, u, CG iterations)."""
+    p, t = _pt(mesh)
+    u = np.zeros(mesh.nv)
+    Hn = np.zeros(3 * mesh.nv)
+    it = C.c_int()
+    lib().or_demag_field(p, t, mesh.nv, mesh.nt, _c(mesh.VE, np.float64), _c(inside, np.uint8),
+                         _c(np.asarray(M).T, np.float64), cg_tol, cg_maxit, u, Hn, C.byref(it))
+    return Hn.reshape(mesh.nv, 3).T, u, it.value
 
 
 def newton_sample(mesh, u, nl, mu_lin, Ms, Hk, cg_iters):

@@ -243,3 +243,38 @@ def test_triangle_mesh_properties():
     u = 2 * m2.p[0] - 3 * m2.p[1]
     free = m2.dirichlet_mask() == 0
     assert np.abs((O.quadraticStiffnessMatrix2D(m2) @ u)[free]).max() < 1e-10
+
+
+def test_demag_field_matches_direct_solve():
+    """Micromagnetics/LL.jl:162-211 restated: PCG on the singular Neumann problem vs a
+    direct solve with one node pinned (H does not see the constant)."""
+    import scipy.sparse.linalg as spla
+    m = box_tet_mesh(8, seed=3)
+    rng = np.random.default_rng(0)
+    M = rng.normal(size=(3, m.nv))
+    M /= np.linalg.norm(M, axis=0)
+    c = m.centroids()
+    inside = (np.sqrt((c * c).sum(0)) < 3.0).astype(np.uint8)
+    Hn, u, it = O.magnetostaticField(m, M, inside)
+    K = O.stiffnessMatrix(m).tocsr()
+    rhs = np.zeros(m.nv)
+    for k in np.flatnonzero(inside):
+        nds = m.t[:, k]
+        f = M[:, nds].mean(axis=1)
+        for a in range(4):
+            r = O.abcd(m, k, a)
+            rhs[nds[a]] += m.VE[k] * (r[1] * f[0] + r[2] * f[1] + r[3] * f[2])
+    assert abs(rhs.sum()) < 1e-12
+    ud = np.zeros(m.nv)
+    ud[1:] = spla.spsolve(K[1:, 1:].tocsc(), rhs[1:])
+    Hd = O.hfield(m, ud)
+    Hnd, vol = np.zeros((3, m.nv)), np.zeros(m.nv)
+    for k in np.flatnonzero(inside):
+        for a in range(4):
+            vol[m.t[a, k]] += m.VE[k]
+            Hnd[:, m.t[a, k]] += m.VE[k] * Hd[:, k]
+    with np.errstate(invalid="ignore", divide="ignore"):
+        Hnd /= vol
+    ok = np.isfinite(Hnd[0])
+    assert np.array_equal(np.isfinite(Hn), np.isfinite(Hnd))
+    assert np.linalg.norm(Hn[:, ok] - Hnd[:, ok]) / np.linalg.norm(Hnd[:, ok]) < 1e-10
