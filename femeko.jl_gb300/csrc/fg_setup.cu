@@ -634,6 +634,7 @@ extern "C" fg_status fg_mesh_nnz(const fg_mesh *m, int64_t *nnz, int32_t *max_ro
 extern "C" fg_status fg_mesh_set_dirichlet(fg_mesh *m, const uint8_t *fixed) {
   return fg_guard([&]() -> fg_status {
     FG_REQUIRE(m != nullptr, FG_BAD_ARG, "fg_mesh_set_dirichlet: null handle");
+    m->op_tag = 0;  // an operator kept on the handle has the old Dirichlet rows
     if (!m->fixed) m->fixed = dev_alloc<uint8_t>(m, (size_t)m->nv);
     if (fixed) {
       FG_CUDA_TRY(cudaMemcpyAsync(m->fixed, fixed, (size_t)m->nv, cudaMemcpyHostToDevice, m->stream));

@@ -327,8 +327,15 @@ def adjoint_dJdmu(mesh: MESH, mur, u0, target, nl=None, rtol=1e-12, **kw):
 
 def magnetostaticField(mesh: MESH, M, inside, precision="fp64", rtol=1e-10, **kw):
     """Demagnetising field on the nodes (Micromagnetics/LL.jl:162-211); M is 3 x nv,
-    inside the nt mask of the magnetic body.  Returns (Hn 3 x nv, u, stats)."""
-    g = gpu_mesh(mesh)
+    inside the nt mask of the magnetic body.  Like the reference, the Poisson problem
+    has no Dirichlet rows.
+    Returns (Hn 3 x nv, u, stats)."""
+    # a handle of its own without Dirichlet rows, kept on the mesh so that the
+    # operator stays assembled from one micromagnetic step to the next
+    g = getattr(mesh, "_gpu_demag", None)
+    if g is None or g.h is None:
+        g = GPUMesh(mesh, dirichlet=False)
+        object.__setattr__(mesh, "_gpu_demag", g)
     Hn = np.zeros(3 * mesh.nv)
     u = np.zeros(mesh.nv)
     o = solve_opts(precision=precision, rtol=rtol, **kw)

@@ -222,6 +222,22 @@ function BoundaryIntegral(mesh, F::Vector{Float64}, shell_id)
     return RHS
 end
 
+"""magnetostaticField(mesh, M, inside; precision=:fp64, rtol=1e-10) -- the demagnetising
+field on the nodes of Micromagnetics/LL.jl:162-211 (M is 3 x nv, inside an nt UInt8
+mask of the magnetic body).  The stiffness operator stays on the device between
+calls, as the reference's A between Landau-Lifshitz steps."""
+function magnetostaticField(mesh, M::Matrix{Float64}, inside::Vector{UInt8}; precision::Symbol=:fp64, rtol=1e-10)
+    g = gpu(mesh)
+    Hn = zeros(3, g.nv)
+    o = Ref(solve_opts(precision=precision, rtol=rtol))
+    s = Ref{SolveStats}()
+    st = ccall((:fg_demag_field, libpath()), Cint,
+               (Ptr{Cvoid}, Ptr{UInt8}, Ptr{Float64}, Ref{SolveOpts}, Ptr{Float64}, Ptr{Float64}, Ref{SolveStats}),
+               g.h, inside, M, o, Hn, C_NULL, s)
+    check(st; allow_not_converged=true)
+    return Hn
+end
+
 """heat_be(mesh, T, kappa, fixed; rho_c=1.0, dt=1e-3, nsteps=100, every=10, precision=:mixed)
 -- the backward-Euler loop of Heat/heat3D.jl:83-89 with T = 0 on the `fixed` nodes.
 Returns (T after nsteps, snapshots nv x (nsteps ÷ every), stats)."""
