@@ -1037,8 +1037,9 @@ static void ensure_cg64(fg_mesh *m) {
 // 0-3 fused iteration with direct gathers, 4 fused with halo staging, 5 fused and
 // pipelined, 6 split (vector pass + SpMV) with direct gathers, 7 split with halo
 // staging, 8 split with direct gathers in a persistent grid, 9 the same launched with
-// programmatic dependent launch, 10 the same with the matrix values held in L2
-constexpr int FG_N_SPMV32 = 11;
+// programmatic dependent launch, 10 the same with the matrix values held in L2,
+// 11 and 12 persistent grids of 4 and 2 blocks per SM
+constexpr int FG_N_SPMV32 = 13;
 static inline bool split32(int v) { return v >= 6; }
 constexpr int FG_N_SPMV64 = 2;   // 0 direct gathers, 1 halo staging
 
@@ -1245,9 +1246,11 @@ static void launch_spmv32s(fg_mesh *m, int v) {
                 m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl, m->red.partials, m->red.counter);
     return;
   }
-  if (v == 8 || v == 9 || v == 10) {
-    // persistent: at most 8 resident 256-thread blocks per SM
-    const unsigned g = std::min<unsigned>(grid_for(m->nv, 256), 8u * (unsigned)std::max(m->sm_count, 1));
+  if (v == 8 || v == 9 || v == 10 || v == 11 || v == 12) {
+    // persistent: at most 8 (variants 8-10), 4 (11) or 2 (12) 256-thread blocks per SM;
+    // fewer blocks walk more row blocks each and reduce once for all of them
+    const unsigned per_sm = (v == 11) ? 4u : (v == 12) ? 2u : 8u;
+    const unsigned g = std::min<unsigned>(grid_for(m->nv, 256), per_sm * (unsigned)std::max(m->sm_count, 1));
     if (m->use_dcol)
       pdl_launch(pdl, k_cg32s_spmv<ColRel, true>, g, 256, 0, m->stream, m->nv, m->sl_ptr, m->sl_len, m->sl_dcol,
                  m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl, m->red.partials, m->red.counter);
@@ -1431,7 +1434,7 @@ static int inner_solve(fg_mesh *m, bool mixed, const double *r64, double rn, dou
       // a forced variant that this operator cannot run (no halo lists, stages too
       // large for shared memory) falls back to the plain gather kernel
       const int v = o.spmv - 1;
-      const bool avail = v < 4 || v == 6 || v == 8 || v == 9 || (v == 10 && prepare_l2(m)) ||
+      const bool avail = v < 4 || v == 6 || v == 8 || v == 9 || v == 11 || v == 12 || (v == 10 && prepare_l2(m)) ||
                          ((v == 4 || v == 7) && m->halo_col) || (v == 5 && pipe_available(m));
       m->spmv_variant32 = avail ? v : 0;
     } else if (!m->tuned32 && !tune_cache_get(m, true)) {
@@ -1791,7 +1794,7 @@ extern "C" fg_status fg_set_cg_variant(fg_mesh *m, int32_t precision, int32_t va
       FG_REQUIRE(variant >= 0 && variant <= FG_N_SPMV32, FG_BAD_ARG, "fg_set_cg_variant: no such variant");
       if (variant == 0) { m->tuned32 = false; return FG_OK; }
       const int v = variant - 1;
-      const bool avail = v < 4 || v == 6 || v == 8 || v == 9 || (v == 10 && prepare_l2(m)) ||
+      const bool avail = v < 4 || v == 6 || v == 8 || v == 9 || v == 11 || v == 12 || (v == 10 && prepare_l2(m)) ||
                          ((v == 4 || v == 7) && m->halo_col) || (v == 5 && pipe_available(m));
       FG_REQUIRE(avail, FG_UNSUPPORTED, "fg_set_cg_variant: variant not available for this operator");
       m->spmv_variant32 = v;
