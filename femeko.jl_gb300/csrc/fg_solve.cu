@@ -776,7 +776,9 @@ __global__ void __launch_bounds__(256) k_cg64_vec(int64_t n2, double2 *__restric
 
 // w = A u with gamma = r.u, delta = w.u and r.r reduced; the last block sets the
 // next alpha, beta and the stopping test.
-template <class CI>
+// PERSIST: a grid of a few blocks per SM walks the 256-row blocks (one reduction per
+// block for all of its rows, as in k_cg32s_spmv).
+template <class CI, bool PERSIST>
 __global__ void __launch_bounds__(256) k_cg64_spmv(int64_t n, const int *__restrict__ sl_ptr,
                                                    const int *__restrict__ sl_len,
                                                    const typename CI::T *__restrict__ col,
@@ -784,8 +786,10 @@ __global__ void __launch_bounds__(256) k_cg64_spmv(int64_t n, const int *__restr
                                                    const double *__restrict__ r, double *__restrict__ w,
                                                    double *scal, int *ictl, double *partials, unsigned *counter) {
   if (ictl[I_DONE]) return;
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double d3[3] = {0.0, 0.0, 0.0};
+  const int64_t nrb = (n + 255) / 256;
+  for (int64_t rb = blockIdx.x; rb < (PERSIST ? nrb : (int64_t)blockIdx.x + 1); rb += gridDim.x) {
+  const int64_t i = rb * 256 + threadIdx.x;
   if (i < n) {
     const int s = (int)(i >> 5), lane = (int)(i & 31);
     const int64_t base = (int64_t)sl_ptr[s] + lane * FG_GROUP;
@@ -805,9 +809,10 @@ __global__ void __launch_bounds__(256) k_cg64_spmv(int64_t n, const int *__restr
     }
     w[i] = acc;
     const double ui = u[i], ri = r[i];
-    d3[0] = ri * ui;
-    d3[1] = acc * ui;
-    d3[2] = ri * ri;
+    d3[0] = fma(ri, ui, d3[0]);
+    d3[1] = fma(acc, ui, d3[1]);
+    d3[2] = fma(ri, ri, d3[2]);
+  }
   }
   __shared__ double shd[3][32];
   block_sum<3>(d3, shd);
@@ -1038,10 +1043,10 @@ static void ensure_cg64(fg_mesh *m) {
 // pipelined, 6 split (vector pass + SpMV) with direct gathers, 7 split with halo
 // staging, 8 split with direct gathers in a persistent grid, 9 the same launched with
 // programmatic dependent launch, 10 the same with the matrix values held in L2,
-// 11 and 12 persistent grids of 4 and 2 blocks per SM
-constexpr int FG_N_SPMV32 = 13;
+// 11-14 persistent grids of 4, 3, 5 and 6 blocks per SM
+constexpr int FG_N_SPMV32 = 15;
 static inline bool split32(int v) { return v >= 6; }
-constexpr int FG_N_SPMV64 = 2;   // 0 direct gathers, 1 halo staging
+constexpr int FG_N_SPMV64 = 4;   // 0 direct gathers, 1 halo staging, 2/3 persistent with 4/8 blocks per SM
 
 template <class CI>
 static void iter32_variant(fg_mesh *m, int v, const typename CI::T *col, const float4 *in, float4 *out) {
@@ -1246,10 +1251,12 @@ static void launch_spmv32s(fg_mesh *m, int v) {
                 m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl, m->red.partials, m->red.counter);
     return;
   }
-  if (v == 8 || v == 9 || v == 10 || v == 11 || v == 12) {
-    // persistent: at most 8 (variants 8-10), 4 (11) or 2 (12) 256-thread blocks per SM;
-    // fewer blocks walk more row blocks each and reduce once for all of them
-    const unsigned per_sm = (v == 11) ? 4u : (v == 12) ? 2u : 8u;
+  if (v >= 8) {
+    // persistent: 8 (variants 8-10), 4 (11), 3 (12), 5 (13) or 6 (14) resident
+    // 256-thread blocks per SM; fewer blocks walk more row blocks each and reduce
+    // once for all of them
+    static const unsigned kPerSm[15] = {0, 0, 0, 0, 0, 0, 0, 0, 8, 8, 8, 4, 3, 5, 6};
+    const unsigned per_sm = kPerSm[v];
     const unsigned g = std::min<unsigned>(grid_for(m->nv, 256), per_sm * (unsigned)std::max(m->sm_count, 1));
     if (m->use_dcol)
       pdl_launch(pdl, k_cg32s_spmv<ColRel, true>, g, 256, 0, m->stream, m->nv, m->sl_ptr, m->sl_len, m->sl_dcol,
@@ -1300,17 +1307,28 @@ static void launch_iter32(fg_mesh *m, int v, bool from_first_buffer) {
 }
 
 static void launch_spmv64cg(fg_mesh *m) {
-  if (m->spmv_variant64 == 1)
+  if (m->spmv_variant64 == 2 || m->spmv_variant64 == 3) {
+    const unsigned per_sm = (m->spmv_variant64 == 2) ? 4u : 8u;
+    const unsigned g = std::min<unsigned>(grid_for(m->nv, 256), per_sm * (unsigned)std::max(m->sm_count, 1));
+    if (m->use_dcol)
+      k_cg64_spmv<ColRel, true><<<g, 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, m->val64,
+                                                           m->v64[2], m->v64[1], m->v64[12], m->scal, m->ictl,
+                                                           m->red.partials, m->red.counter);
+    else
+      k_cg64_spmv<ColAbs, true><<<g, 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val64,
+                                                           m->v64[2], m->v64[1], m->v64[12], m->scal, m->ictl,
+                                                           m->red.partials, m->red.counter);
+  } else if (m->spmv_variant64 == 1)
     halo_launch<Spmv64Halo>(m, sizeof(double), m->nv, (const int *)m->sl_ptr, (const int *)m->sl_len,
                             (const uint16_t *)m->sl_lcol, (const double *)m->val64, (const int *)m->halo_col,
                             (const int *)m->halo_len, m->hcap, (const double *)m->v64[2], (const double *)m->v64[1],
                             m->v64[12], m->scal, m->ictl, m->red.partials, m->red.counter);
   else if (m->use_dcol)
-    k_cg64_spmv<ColRel><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, m->val64,
+    k_cg64_spmv<ColRel, false><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, m->val64,
                                                             m->v64[2], m->v64[1], m->v64[12], m->scal, m->ictl,
                                                             m->red.partials, m->red.counter);
   else
-    k_cg64_spmv<ColAbs><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val64,
+    k_cg64_spmv<ColAbs, false><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val64,
                                                             m->v64[2], m->v64[1], m->v64[12], m->scal, m->ictl,
                                                             m->red.partials, m->red.counter);
 }
@@ -1434,7 +1452,7 @@ static int inner_solve(fg_mesh *m, bool mixed, const double *r64, double rn, dou
       // a forced variant that this operator cannot run (no halo lists, stages too
       // large for shared memory) falls back to the plain gather kernel
       const int v = o.spmv - 1;
-      const bool avail = v < 4 || v == 6 || v == 8 || v == 9 || v == 11 || v == 12 || (v == 10 && prepare_l2(m)) ||
+      const bool avail = v < 4 || v == 6 || v == 8 || v == 9 || v >= 11 || (v == 10 && prepare_l2(m)) ||
                          ((v == 4 || v == 7) && m->halo_col) || (v == 5 && pipe_available(m));
       m->spmv_variant32 = avail ? v : 0;
     } else if (!m->tuned32 && !tune_cache_get(m, true)) {
@@ -1754,7 +1772,8 @@ fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_v
   return FG_OK;
 }
 
-// The same for the FP64 SpMV (direct gathers or halo staging).
+// The same for the FP64 iteration (SpMV with direct gathers, halo staging, or a
+// persistent grid of 4 or 8 blocks per SM), timed per whole iteration.
 fg_status fg_autotune_spmv64(fg_mesh *m, int reps, int *chosen, double *us_per_variant) {
   FG_REQUIRE(m->val64 != nullptr, FG_BAD_ARG, "autotune: no FP64 operator assembled");
   reps = std::max(2, reps);
@@ -1767,15 +1786,27 @@ fg_status fg_autotune_spmv64(fg_mesh *m, int reps, int *chosen, double *us_per_v
     }
     m->spmv_variant64 = v;
     timing_state(m, false);
+    launch_vec64(m);
     launch_spmv64cg(m);
-    FG_CUDA_TRY(cudaEventRecord(m->ev0, m->stream));
-    for (int r = 0; r < reps; ++r) launch_spmv64cg(m);
-    FG_CUDA_TRY(cudaEventRecord(m->ev1, m->stream));
-    FG_CUDA_TRY(cudaGetLastError());
-    FG_LAUNCHED(reps + 1);
-    fg_sync(m);
+    // timed as the solver runs them: a CUDA graph of reps whole iterations, replayed
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    FG_CUDA_TRY(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
+    for (int r = 0; r < reps; ++r) { launch_vec64(m); launch_spmv64cg(m); }
+    FG_CUDA_TRY(cudaStreamEndCapture(m->stream, &graph));
+    cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    FG_CUDA_TRY(ie);
     float ms = 0.f;
-    FG_CUDA_TRY(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
+    cudaError_t le = cudaGraphLaunch(exec, m->stream);
+    if (le == cudaSuccess) le = cudaEventRecord(m->ev0, m->stream);
+    if (le == cudaSuccess) le = cudaGraphLaunch(exec, m->stream);
+    if (le == cudaSuccess) le = cudaEventRecord(m->ev1, m->stream);
+    if (le == cudaSuccess) le = cudaStreamSynchronize(m->stream);
+    if (le == cudaSuccess) le = cudaEventElapsedTime(&ms, m->ev0, m->ev1);
+    cudaGraphExecDestroy(exec);
+    FG_CUDA_TRY(le);
+    FG_LAUNCHED(4LL * reps + 2);
     const double us = 1e3 * ms / reps;
     if (us_per_variant) us_per_variant[v] = us;
     if (us < best_us) { best_us = us; best = v; }
@@ -1794,7 +1825,7 @@ extern "C" fg_status fg_set_cg_variant(fg_mesh *m, int32_t precision, int32_t va
       FG_REQUIRE(variant >= 0 && variant <= FG_N_SPMV32, FG_BAD_ARG, "fg_set_cg_variant: no such variant");
       if (variant == 0) { m->tuned32 = false; return FG_OK; }
       const int v = variant - 1;
-      const bool avail = v < 4 || v == 6 || v == 8 || v == 9 || v == 11 || v == 12 || (v == 10 && prepare_l2(m)) ||
+      const bool avail = v < 4 || v == 6 || v == 8 || v == 9 || v >= 11 || (v == 10 && prepare_l2(m)) ||
                          ((v == 4 || v == 7) && m->halo_col) || (v == 5 && pipe_available(m));
       FG_REQUIRE(avail, FG_UNSUPPORTED, "fg_set_cg_variant: variant not available for this operator");
       m->spmv_variant32 = v;
@@ -1802,7 +1833,7 @@ extern "C" fg_status fg_set_cg_variant(fg_mesh *m, int32_t precision, int32_t va
     } else {
       FG_REQUIRE(variant >= 0 && variant <= FG_N_SPMV64, FG_BAD_ARG, "fg_set_cg_variant: no such variant");
       if (variant == 0) { m->tuned64 = false; return FG_OK; }
-      FG_REQUIRE(variant == 1 || m->halo_col, FG_UNSUPPORTED, "fg_set_cg_variant: variant not available");
+      FG_REQUIRE(variant != 2 || m->halo_col, FG_UNSUPPORTED, "fg_set_cg_variant: variant not available");
       m->spmv_variant64 = variant - 1;
       m->tuned64 = true;
     }
