@@ -1043,8 +1043,8 @@ static void ensure_cg64(fg_mesh *m) {
 // pipelined, 6 split (vector pass + SpMV) with direct gathers, 7 split with halo
 // staging, 8 split with direct gathers in a persistent grid, 9 the same launched with
 // programmatic dependent launch, 10 the same with the matrix values held in L2,
-// 11-14 persistent grids of 4, 3, 5 and 6 blocks per SM
-constexpr int FG_N_SPMV32 = 15;
+// 11-15 persistent grids of 4, 3, 5, 6 and 7 blocks per SM
+constexpr int FG_N_SPMV32 = 16;
 static inline bool split32(int v) { return v >= 6; }
 constexpr int FG_N_SPMV64 = 4;   // 0 direct gathers, 1 halo staging, 2/3 persistent with 4/8 blocks per SM
 
@@ -1252,10 +1252,10 @@ static void launch_spmv32s(fg_mesh *m, int v) {
     return;
   }
   if (v >= 8) {
-    // persistent: 8 (variants 8-10), 4 (11), 3 (12), 5 (13) or 6 (14) resident
-    // 256-thread blocks per SM; fewer blocks walk more row blocks each and reduce
-    // once for all of them
-    static const unsigned kPerSm[15] = {0, 0, 0, 0, 0, 0, 0, 0, 8, 8, 8, 4, 3, 5, 6};
+    // persistent: 8 (variants 8-10), 4 (11), 3 (12), 5 (13), 6 (14) or 7 (15)
+    // resident 256-thread blocks per SM; fewer blocks walk more row blocks each and
+    // reduce once for all of them
+    static const unsigned kPerSm[16] = {0, 0, 0, 0, 0, 0, 0, 0, 8, 8, 8, 4, 3, 5, 6, 7};
     const unsigned per_sm = kPerSm[v];
     const unsigned g = std::min<unsigned>(grid_for(m->nv, 256), per_sm * (unsigned)std::max(m->sm_count, 1));
     if (m->use_dcol)
@@ -1845,7 +1845,7 @@ extern "C" fg_status fg_autotune(fg_mesh *m, int32_t precision, int32_t *variant
                                  int32_t n_slots) {
   return fg_guard([&]() -> fg_status {
     FG_REQUIRE(m != nullptr, FG_BAD_ARG, "fg_autotune: null handle");
-    double us[16] = {0};
+    double us[32] = {0};
     int chosen = 0, nv = 0;
     fg_status st;
     if (precision == FG_MIXED) {
