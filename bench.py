@@ -251,15 +251,16 @@ def run_ours(args):
     lib.fg_mesh_layout(g.h, C.byref(nsell), C.byref(ninc), C.byref(nsl))
     fg.newton_magnetostatics(mesh, nl, mu_lin, u0, precision="mixed")   # leaves J32 on the handle
     chosen = C.c_int32()
-    variants_us = np.zeros(16)
-    L.check(lib.fg_autotune(g.h, L.FG_MIXED, C.byref(chosen), L.ptr(variants_us), 16))
+    variants_us = np.zeros(17)
+    L.check(lib.fg_autotune(g.h, L.FG_MIXED, C.byref(chosen), L.ptr(variants_us), 17))
     autotune = {"cg32_iteration_variants_us": [round(float(v), 2) for v in variants_us], "chosen": int(chosen.value),
                 "names": ["fused gather/256", "fused gather-hoist/256", "fused gather/128", "fused gather/512",
                           "fused halo-smem", "fused halo-smem-pipelined", "split gather/256", "split halo-smem",
                           "split gather persistent", "split gather persistent, programmatic launch",
                           "split gather persistent, values in L2", "split gather persistent 4/SM",
                           "split gather persistent 3/SM", "split gather persistent 5/SM",
-                          "split gather persistent 6/SM", "split gather persistent 7/SM"]}
+                          "split gather persistent 6/SM", "split gather persistent 7/SM",
+                          "split, Jacobi-scaled system, persistent 6/SM"]}
     ms_spmv, ms_iter = C.c_double(), C.c_double()
     L.check(lib.fg_bench_kernel(g.h, 0, L.FG_MIXED, 200, C.byref(ms_spmv)))
     L.check(lib.fg_bench_kernel(g.h, 3, L.FG_MIXED, 200, C.byref(ms_iter)))
@@ -281,7 +282,12 @@ def run_ours(args):
     fg.newton_magnetostatics(mesh, nl, mu_lin, u0, precision="mixed")
     n = mesh.nv
     v = int(chosen.value)
-    if v >= 6:
+    if v == 16:
+        # scaled system: w = A' r with its dots; value + 16-bit column per stored
+        # nonzero, r read and w written per row (8 B)
+        alg_bytes = g.nnz * 6 + 8 * n
+        kname = "k_cg32s_spmv"
+    elif v >= 6:
         # split iteration, dominant kernel w = A u with its dots: FP32 value (4 B) and
         # 16-bit column (2 B) per stored nonzero; per row u and r read, w written
         # (12 B).  Neighbour gathers of u are re-reads.
@@ -536,7 +542,7 @@ def main():
     ap.add_argument("--ref-counts", type=int, nargs=3, default=[11, 39, 1324],
                     help="(newton iterations, line-search trials, CG iterations) of the solve; default: the FP64 GPU solve at 96^3")
     ap.add_argument("--cg-variant", type=int, default=0,
-                    help="fix the FP32 CG kernel variant (1..16; 0: autotuned), e.g. for profiling runs")
+                    help="fix the FP32 CG kernel variant (1..17; 0: autotuned), e.g. for profiling runs")
     ap.add_argument("--cg64-variant", type=int, default=0, help="fix the FP64 CG SpMV variant (1..4; 0: autotuned)")
     ap.add_argument("--case", choices=sorted(CASES), default=None,
                     help="run a secondary workload instead of the headline benchmark")

@@ -881,7 +881,7 @@ static void launch_elem(fg_mesh *m, int kind, const double *d_f, const double *d
 void fg_assemble_operator(fg_mesh *m, int kind, const double *d_f, const double *d_H, const double *d_dmu,
                           double c_mass, double c_stiff, int full_phi, int layout, bool want64, bool want32,
                           bool apply_bc) {
-  if (layout != OUT_CSR) m->op_tag = 0;
+  if (layout != OUT_CSR) { m->op_tag = 0; ++m->op_version; }
   launch_elem(m, kind, d_f, d_H, d_dmu, c_mass, c_stiff, full_phi);
   const double *rec = static_cast<const double *>(m->rec);
   if (layout == OUT_CSR) {
@@ -898,7 +898,7 @@ void fg_newton_assemble(fg_mesh *m, const double *d_u, double Ms, double Hk, boo
                         bool want_jacobian, bool tangent) {
   const int tg = tangent ? 1 : 0;
   FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "Newton magnetostatics needs P1 tetrahedra");
-  if (want_jacobian) m->op_tag = 0;
+  if (want_jacobian) { m->op_tag = 0; ++m->op_version; }
   fg_ensure_records(m);
   ensure_operator(m, !mixed, mixed);
   unsigned g = grid_for(m->nt, 128);
@@ -1068,6 +1068,7 @@ void fg_newton_assemble_split(fg_mesh *m, const double *d_u, double Ms, double H
   FG_LAUNCHED(1);
   if (!want_jacobian) return;
   m->op_tag = 0;
+  ++m->op_version;
   const unsigned gs = grid_for(std::max(m->n_nl_slots, 1), 128);
   if (mixed) {
     FG_CUDA_TRY(cudaMemcpyAsync(m->val32, m->vlin32, sizeof(float) * (size_t)m->nsell, cudaMemcpyDeviceToDevice,

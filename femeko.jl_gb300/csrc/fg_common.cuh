@@ -202,6 +202,10 @@ struct fg_mesh {
 
   GraphCache graph[4];
   int op_tag = 0;            // what val64/val32 hold when a caller reuses them (0: unknown)
+  int64_t op_version = 0;    // incremented whenever val64/val32 are rewritten
+  // symmetrically Jacobi-scaled FP32 operator D^-1/2 A D^-1/2 (the scaled CG variant)
+  float *val32s = nullptr, *sdiag32 = nullptr;
+  int64_t val32s_version = -1;
   uint8_t *inside = nullptr; // nt mask of the magnetic body (demagnetising field)
   double *nodal_in = nullptr;// 3 x nv nodal magnetisation (demagnetising field)
   double *nodal_work = nullptr; // 7 x nv: nodal sums, volumes and the nodal field

@@ -696,6 +696,84 @@ __global__ void __launch_bounds__(R) k_cg32s_spmv_halo(int64_t n, const int *__r
   if (grid_finish<3>(part, partials, counter, tot)) cgcg_scalars(tot, scal, ictl);
 }
 
+// Jacobi-PCG as plain CG on the symmetrically scaled system (the scaled split
+// variant): A' = S A S with S = D^-1/2 (sdiag = sqrt of the Jacobi inverse, 0 on
+// Dirichlet rows), b' = S b, x = S y.  The iterates are those of Jacobi-PCG; the
+// preconditioned residual u = r' needs no vector of its own, and the stopping test
+// measures |r'| = |S r| (the preconditioned residual norm).
+__global__ void k_sdiag32(int64_t np, const float *__restrict__ dinv, float *__restrict__ sdiag) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < np) sdiag[i] = sqrtf(dinv[i]);
+}
+
+template <class CI>
+__global__ void k_scale_op32(int64_t n, const int *__restrict__ sl_ptr, const int *__restrict__ sl_len,
+                             const typename CI::T *__restrict__ col, const float *__restrict__ val,
+                             const float *__restrict__ sdiag, float *__restrict__ vals) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int s = (int)(i >> 5), lane = (int)(i & 31);
+  const float si = sdiag[i];
+  const int L = FG_GROUP * sl_len[s];
+  for (int q = 0; q < L; ++q) {
+    const int64_t e = sell_pos(sl_ptr[s], lane, q);
+    vals[e] = val[e] * si * sdiag[CI::col(col[e], i)];
+  }
+}
+
+// r' = S (scale rin), s = p = y = 0.
+__global__ void k_cg32ss_init(int64_t n, int64_t np, const double *__restrict__ rin, double scale,
+                              const float *__restrict__ sdiag, float *__restrict__ r, float *__restrict__ s,
+                              float *__restrict__ p, float *__restrict__ y, double tol2_rel, int maxit, double *scal,
+                              int *ictl) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < np; i += stride) {
+    r[i] = (i < n) ? (float)(scale * rin[i]) * sdiag[i] : 0.f;
+    s[i] = 0.f;
+    p[i] = 0.f;
+    y[i] = 0.f;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    scal[S_TOL2] = tol2_rel;
+    scal[S_ALPHA] = 0.0;
+    scal[S_BETA] = 0.0;
+    ictl[I_ITERS] = -1;
+    ictl[I_MAXIT] = maxit;
+    ictl[I_STATUS] = 0;
+    ictl[I_FAULT] = 0;
+    ictl[I_DONE] = 0;
+  }
+}
+
+// s = w + beta s, p = r + beta p, y += alpha p, r -= alpha s (four rows per thread).
+__global__ void __launch_bounds__(256) k_cg32ss_vec(int64_t n4, float4 *__restrict__ r, const float4 *__restrict__ w,
+                                                    float4 *__restrict__ s, float4 *__restrict__ p,
+                                                    float4 *__restrict__ y, const double *scal, const int *ictl) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n4) return;
+  const int done = ictl[I_DONE];
+  const double alpha_d = scal[S_ALPHA], beta_d = scal[S_BETA];
+  const float4 ww = w[j];
+  float4 ss = s[j], pp = p[j], yy = y[j], rr = r[j];
+  if (done) return;
+  const float alpha = (float)alpha_d, beta = (float)beta_d;
+  ss.x = fmaf(beta, ss.x, ww.x); ss.y = fmaf(beta, ss.y, ww.y); ss.z = fmaf(beta, ss.z, ww.z); ss.w = fmaf(beta, ss.w, ww.w);
+  pp.x = fmaf(beta, pp.x, rr.x); pp.y = fmaf(beta, pp.y, rr.y); pp.z = fmaf(beta, pp.z, rr.z); pp.w = fmaf(beta, pp.w, rr.w);
+  yy.x = fmaf(alpha, pp.x, yy.x); yy.y = fmaf(alpha, pp.y, yy.y); yy.z = fmaf(alpha, pp.z, yy.z); yy.w = fmaf(alpha, pp.w, yy.w);
+  rr.x = fmaf(-alpha, ss.x, rr.x); rr.y = fmaf(-alpha, ss.y, rr.y); rr.z = fmaf(-alpha, ss.z, rr.z); rr.w = fmaf(-alpha, ss.w, rr.w);
+  s[j] = ss;
+  p[j] = pp;
+  y[j] = yy;
+  r[j] = rr;
+}
+
+// x += scale * S y (the solution of the unscaled system).
+__global__ void k_axpy_scaled_to64(int64_t n, double scale, const float *__restrict__ sdiag,
+                                   const float *__restrict__ y, double *__restrict__ x) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] += scale * (double)(sdiag[i] * y[i]);
+}
+
 // r = scale * rin, u = D^-1 r, s = p = x = 0 for the split FP32 iteration.
 __global__ void k_cg32s_init(int64_t n, int64_t np, const double *__restrict__ rin, double scale,
                              const float *__restrict__ dinv, float *__restrict__ r, float *__restrict__ u,
@@ -1043,8 +1121,9 @@ static void ensure_cg64(fg_mesh *m) {
 // pipelined, 6 split (vector pass + SpMV) with direct gathers, 7 split with halo
 // staging, 8 split with direct gathers in a persistent grid, 9 the same launched with
 // programmatic dependent launch, 10 the same with the matrix values held in L2,
-// 11-15 persistent grids of 4, 3, 5, 6 and 7 blocks per SM
-constexpr int FG_N_SPMV32 = 16;
+// 11-15 persistent grids of 4, 3, 5, 6 and 7 blocks per SM, 16 CG on the
+// symmetrically Jacobi-scaled system with the SpMV of variant 14
+constexpr int FG_N_SPMV32 = 17;
 static inline bool split32(int v) { return v >= 6; }
 constexpr int FG_N_SPMV64 = 4;   // 0 direct gathers, 1 halo staging, 2/3 persistent with 4/8 blocks per SM
 
@@ -1239,8 +1318,41 @@ static void l2_launch(fg_mesh *m, void (*kern)(KArgs...), unsigned grid, unsigne
   FG_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...));
 }
 
+// The scaled operator of variant 16, rebuilt when the operator changed.
+static void ensure_scaled(fg_mesh *m) {
+  if (!m->val32s) m->val32s = dev_alloc<float>(m, (size_t)m->nsell);
+  if (!m->sdiag32) {
+    m->sdiag32 = dev_alloc<float>(m, (size_t)m->nvp);
+    FG_CUDA_TRY(cudaMemsetAsync(m->sdiag32, 0, sizeof(float) * (size_t)m->nvp, m->stream));
+  }
+  if (m->val32s_version == m->op_version) return;
+  k_sdiag32<<<grid_for(m->nvp, 256), 256, 0, m->stream>>>(m->nvp, m->dinv32, m->sdiag32);
+  if (m->use_dcol)
+    k_scale_op32<ColRel><<<grid_for(m->nv, 256), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_dcol,
+                                                                      m->val32, m->sdiag32, m->val32s);
+  else
+    k_scale_op32<ColAbs><<<grid_for(m->nv, 256), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col,
+                                                                      m->val32, m->sdiag32, m->val32s);
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(2);
+  m->val32s_version = m->op_version;
+}
+
 static void launch_spmv32s(fg_mesh *m, int v) {
   const bool pdl = (v == 9);
+  if (v == 16) {
+    // w = A' r' with the dots r'.r', w.r', r'.r' (u = r' on the scaled system)
+    const unsigned g = std::min<unsigned>(grid_for(m->nv, 256), 6u * (unsigned)std::max(m->sm_count, 1));
+    if (m->use_dcol)
+      k_cg32s_spmv<ColRel, true><<<g, 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, m->val32s,
+                                                           m->v32[4], m->v32[4], m->v32[5], m->scal, m->ictl,
+                                                           m->red.partials, m->red.counter);
+    else
+      k_cg32s_spmv<ColAbs, true><<<g, 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val32s,
+                                                           m->v32[4], m->v32[4], m->v32[5], m->scal, m->ictl,
+                                                           m->red.partials, m->red.counter);
+    return;
+  }
   if (v == 10 && m->l2_win_bytes > 0) {
     const unsigned g = std::min<unsigned>(grid_for(m->nv, 256), 8u * (unsigned)std::max(m->sm_count, 1));
     if (m->use_dcol)
@@ -1279,7 +1391,15 @@ static void launch_spmv32s(fg_mesh *m, int v) {
                m->red.counter);
 }
 
-static void launch_vec32s(fg_mesh *m, bool pdl) {
+static void launch_vec32s(fg_mesh *m, int v) {
+  if (v == 16) {
+    k_cg32ss_vec<<<grid_for(m->nvp / 4, 256), 256, 0, m->stream>>>(
+        m->nvp / 4, reinterpret_cast<float4 *>(m->v32[4]), reinterpret_cast<const float4 *>(m->v32[5]),
+        reinterpret_cast<float4 *>(m->v32[6]), reinterpret_cast<float4 *>(m->v32[1]),
+        reinterpret_cast<float4 *>(m->v32[0]), m->scal, m->ictl);
+    return;
+  }
+  const bool pdl = (v == 9);
   pdl_launch(pdl, k_cg32s_vec, grid_for(m->nvp / 4, 256), 256, 0, m->stream, m->nvp / 4,
              reinterpret_cast<float4 *>(m->v32[4]), reinterpret_cast<const float4 *>(m->v32[5]),
              reinterpret_cast<float4 *>(m->v32[6]), reinterpret_cast<float4 *>(m->v32[1]),
@@ -1289,7 +1409,7 @@ static void launch_vec32s(fg_mesh *m, bool pdl) {
 
 static void launch_iter32(fg_mesh *m, int v, bool from_first_buffer) {
   if (split32(v)) {
-    launch_vec32s(m, v == 9);
+    launch_vec32s(m, v);
     launch_spmv32s(m, v);
     return;
   }
@@ -1345,7 +1465,12 @@ static void launch_vec64(fg_mesh *m) {
 // buffer 0 -> 1, so the iteration blocks start reading buffer 1.
 static void start_cg(fg_mesh *m, bool mixed, const double *r64, double scale, double tol2_rel, int maxit) {
   const unsigned g = red_grid(m->nvp);
-  if (mixed && split32(m->spmv_variant32)) {
+  if (mixed && m->spmv_variant32 == 16) {
+    ensure_scaled(m);
+    k_cg32ss_init<<<g, 256, 0, m->stream>>>(m->nv, m->nvp, r64, scale, m->sdiag32, m->v32[4], m->v32[6], m->v32[1],
+                                            m->v32[0], tol2_rel, maxit, m->scal, m->ictl);
+    launch_spmv32s(m, 16);
+  } else if (mixed && split32(m->spmv_variant32)) {
     k_cg32s_init<<<g, 256, 0, m->stream>>>(m->nv, m->nvp, r64, scale, m->dinv32, m->v32[4], m->v32[7], m->v32[6],
                                            m->v32[1], m->v32[0], tol2_rel, maxit, m->scal, m->ictl);
     launch_spmv32s(m, m->spmv_variant32);
@@ -1462,7 +1587,10 @@ static int inner_solve(fg_mesh *m, bool mixed, const double *r64, double rn, dou
     if (m->spmv_variant32 == 10 && !prepare_l2(m)) m->spmv_variant32 = 8;
     start_cg(m, true, r64, 1.0 / rn, inner * inner, maxit);
     its = run_cg(m, true, o, ist);
-    k_axpy_to64<float><<<red_grid(m->nv), 256, 0, m->stream>>>(m->nv, rn, m->v32[0], d_x);
+    if (m->spmv_variant32 == 16)
+      k_axpy_scaled_to64<<<grid_for(m->nv, 256), 256, 0, m->stream>>>(m->nv, rn, m->sdiag32, m->v32[0], d_x);
+    else
+      k_axpy_to64<float><<<red_grid(m->nv), 256, 0, m->stream>>>(m->nv, rn, m->v32[0], d_x);
   } else {
     ensure_cg64(m);
     if (!m->tuned64 && !tune_cache_get(m, false)) {
@@ -1707,7 +1835,7 @@ fg_status fg_bench_cg_kernel(fg_mesh *m, int which, int precision, int reps, dou
     for (int r = 0; r < n; ++r) {
       if (mixed && (!split32(v) || which == 3)) launch_iter32(m, v, (r & 1) != 0);
       else if (mixed && which == 0) launch_spmv32s(m, v);
-      else if (mixed) launch_vec32s(m, v == 9);
+      else if (mixed) launch_vec32s(m, v);
       else if (which == 0) launch_spmv64cg(m);
       else if (which == 1) launch_vec64(m);
       else { launch_vec64(m); launch_spmv64cg(m); }

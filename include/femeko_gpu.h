@@ -52,7 +52,7 @@ enum {
                           of |F(u + a du)|^2, kept in [0.1, 0.5] of the last step */
 };
 /* FP32 CG iteration kernel: FG_SPMV_AUTO lets the autotuner time the variants on
- * the first mixed solve of a handle and keep the fastest; k = 1..16 forces variant
+ * the first mixed solve of a handle and keep the fastest; k = 1..17 forces variant
  * k-1.  One fused kernel per iteration: 1: 4x-unrolled gather loop, 256 threads;
  * 2: all row loads issued first, 256 threads; 3: loop, 128 threads; 4: loop, 512
  * threads; 5: halo staging (the neighbour entries of a block of rows gathered once
@@ -63,7 +63,9 @@ enum {
  * programmatic dependent launch between the two kernels; 11: 9 with the matrix
  * values kept in a persisting-L2 window (the process's context sets aside L2 for
  * them while a handle uses this variant); 12-16: 9 with 4, 3, 5, 6 and 7 blocks per
- * SM.
+ * SM; 17: plain CG on the symmetrically Jacobi-scaled system D^-1/2 A D^-1/2 (the
+ * same iterates as Jacobi-PCG, no preconditioned-residual vector, stopping test on
+ * the preconditioned residual norm) with the SpMV of 15.
  * The autotuner times each variant as a replayed CUDA graph of iterations, the way
  * the solver runs them. */
 enum { FG_SPMV_AUTO = 0 };
@@ -77,7 +79,7 @@ typedef struct fg_solve_opts {
   double inner_rtol;   /* mixed: FP32 PCG target per refinement step */
   int32_t check_every; /* iterations per graph launch between convergence checks (even) */
   int32_t use_graph;   /* 1: replay each block of iterations as a CUDA graph */
-  int32_t spmv;        /* FG_SPMV_AUTO or a forced variant 1..16 */
+  int32_t spmv;        /* FG_SPMV_AUTO or a forced variant 1..17 */
   int32_t reserved_;
 } fg_solve_opts;
 
@@ -339,7 +341,7 @@ fg_status fg_bench_kernel(fg_mesh *m, int32_t which, int32_t precision, int32_t 
  * be NULL) the measured microseconds per launch.  No reference counterpart. */
 fg_status fg_autotune(fg_mesh *m, int32_t precision, int32_t *variant, double *us_per_variant, int32_t n_slots);
 /* Fixes the CG kernel variant of one precision for the handle (the numbering of
- * fg_solve_opts.spmv: FG_MIXED 1..16, FG_FP64 1..4), or 0 to return to the
+ * fg_solve_opts.spmv: FG_MIXED 1..17, FG_FP64 1..4), or 0 to return to the
  * autotuner's choice at the next solve.  The autotuner's choices are remembered per
  * process for each operator shape (device, rows, padded entries, longest row), so a
  * new handle for a mesh of the same structure does not time the variants again.
