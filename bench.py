@@ -200,7 +200,7 @@ def run_ours(args):
     resident = fg.ResidentNewton(mesh, nl, mu_lin, u0)
 
     def solve(precision):
-        st = resident.solve(precision=precision)
+        st = resident.solve(precision=precision, check_every=args.check_every, use_graph=args.graph_mode)
         if not st["converged"]:
             raise RuntimeError(f"Newton did not converge: {st}")
         return st
@@ -251,8 +251,8 @@ def run_ours(args):
     lib.fg_mesh_layout(g.h, C.byref(nsell), C.byref(ninc), C.byref(nsl))
     fg.newton_magnetostatics(mesh, nl, mu_lin, u0, precision="mixed")   # leaves J32 on the handle
     chosen = C.c_int32()
-    variants_us = np.zeros(17)
-    L.check(lib.fg_autotune(g.h, L.FG_MIXED, C.byref(chosen), L.ptr(variants_us), 17))
+    variants_us = np.zeros(20)
+    L.check(lib.fg_autotune(g.h, L.FG_MIXED, C.byref(chosen), L.ptr(variants_us), 20))
     autotune = {"cg32_iteration_variants_us": [round(float(v), 2) for v in variants_us], "chosen": int(chosen.value),
                 "names": ["fused gather/256", "fused gather-hoist/256", "fused gather/128", "fused gather/512",
                           "fused halo-smem", "fused halo-smem-pipelined", "split gather/256", "split halo-smem",
@@ -260,7 +260,9 @@ def run_ours(args):
                           "split gather persistent, values in L2", "split gather persistent 4/SM",
                           "split gather persistent 3/SM", "split gather persistent 5/SM",
                           "split gather persistent 6/SM", "split gather persistent 7/SM",
-                          "split, Jacobi-scaled system, persistent 6/SM"]}
+                          "split, Jacobi-scaled system, persistent 6/SM",
+                          "split, bulk-staged entries, persistent 4/SM", "split, bulk-staged entries, persistent 3/SM",
+                          "split, bulk-staged entries, persistent 2/SM"]}
     ms_spmv, ms_iter = C.c_double(), C.c_double()
     L.check(lib.fg_bench_kernel(g.h, 0, L.FG_MIXED, 200, C.byref(ms_spmv)))
     L.check(lib.fg_bench_kernel(g.h, 3, L.FG_MIXED, 200, C.byref(ms_iter)))
@@ -292,7 +294,7 @@ def run_ours(args):
         # 16-bit column (2 B) per stored nonzero; per row u and r read, w written
         # (12 B).  Neighbour gathers of u are re-reads.
         alg_bytes = g.nnz * 6 + 12 * n
-        kname = "k_cg32s_spmv_halo" if v == 7 else "k_cg32s_spmv"
+        kname = "k_cg32s_spmv_halo" if v == 7 else ("k_cg32s_spmv_bulk" if v >= 17 else "k_cg32s_spmv")
     else:
         # one fused iteration: matrix as above; per row the (r, w, s, dinv) state read
         # and written (16 + 16 B) and p, x read and written (8 + 8 B)
@@ -359,17 +361,27 @@ def run_ours(args):
                           f"(newton, trials, cg) = {counts} to {est:.1f} s per solve")}
 
     sm = res["mixed"]["stats"]
+
+    def phases(st):
+        # one solve (the last timed one): set-up (linear elements' operator, first
+        # residual), inner CG solves, the rest (residuals, line search, Jacobians)
+        return {"setup": round(st["setup_ms"], 3), "cg": round(st["cg_ms"], 3),
+                "newton_rest": round(st["ms"] - st["setup_ms"] - st["cg_ms"], 3)}
+
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * res["mixed"]["sec"] / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 operator/CG, f64 residual/update",
             "data": "synthetic", "config": config(args.cells, mesh),
             "fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": 1000.0 * res["fp64"]["sec"] / args.fp64_steps,
-                     "newton_iters": res["fp64"]["stats"]["newton_iters"], "cg_iters": res["fp64"]["stats"]["cg_iters"]},
+                     "newton_iters": res["fp64"]["stats"]["newton_iters"], "cg_iters": res["fp64"]["stats"]["cg_iters"],
+                     "phases_ms": phases(res["fp64"]["stats"])},
+            "phases_ms": phases(sm),
             "mixed_over_fp64": value / fp64_value,
             "accuracy_vs_fp64_gpu": {"H_rel": herr, "u_rel": uerr, "energy_rel": werr},
             "newton_iters": sm["newton_iters"], "cg_iters": sm["cg_iters"], "trials": sm["trials"],
             "roofline": roofline, "kernels_us": kernels_us, "autotune": autotune, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(launches), "cg_variant_fixed": {"mixed": args.cg_variant, "fp64": args.cg64_variant},
+            "cg_loop": {"check_every": args.check_every, "graph_mode": args.graph_mode},
             "clocks": res["mixed"]["clocks"], "clocks_fp64": res["fp64"]["clocks"],
             "setup_s": {"mesh_generate": t_gen, "mesh_create_pattern": t_setup},
             "wall_s": {"mixed": res["mixed"]["wall"], "fp64": res["fp64"]["wall"]}}
@@ -541,8 +553,12 @@ def main():
                     help="DRAM bytes per SpMV launch from an ncu capture (reported as roofline.traffic)")
     ap.add_argument("--ref-counts", type=int, nargs=3, default=[11, 39, 1324],
                     help="(newton iterations, line-search trials, CG iterations) of the solve; default: the FP64 GPU solve at 96^3")
+    ap.add_argument("--check-every", type=int, default=32,
+                    help="CG iterations between convergence tests (the body of the solve's graph loop)")
+    ap.add_argument("--graph-mode", type=int, default=1, choices=[0, 1, 2],
+                    help="1: whole CG in one graph launch (device-side loop); 2: host-checked graph blocks; 0: no graph")
     ap.add_argument("--cg-variant", type=int, default=0,
-                    help="fix the FP32 CG kernel variant (1..17; 0: autotuned), e.g. for profiling runs")
+                    help="fix the FP32 CG kernel variant (1..20; 0: autotuned), e.g. for profiling runs")
     ap.add_argument("--cg64-variant", type=int, default=0, help="fix the FP64 CG SpMV variant (1..4; 0: autotuned)")
     ap.add_argument("--case", choices=sorted(CASES), default=None,
                     help="run a secondary workload instead of the headline benchmark")

@@ -20,6 +20,7 @@
 #include <type_traits>
 
 #include <algorithm>
+#include <cstring>
 
 #include "fg_common.cuh"
 
@@ -942,12 +943,29 @@ __global__ void k_linear_coef(int64_t nt, const double *__restrict__ mu_lin, con
   dmu[k] = 0.0;
 }
 
-void fg_nl_setup(fg_mesh *m, const uint8_t *nl_host, bool mixed) {
-  FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "Newton magnetostatics needs P1 tetrahedra");
-  fg_ensure_records(m);
+void fg_set_nl_host(fg_mesh *m, const uint8_t *nl) {
+  const size_t nt = (size_t)m->nt;
+  if (m->nl_host.size() == nt && std::memcmp(m->nl_host.data(), nl, nt) == 0) return;
+  m->nl_host.assign(nl, nl + nt);
+  m->nl_list_current = false;
+}
+
+// The nonlinear element list of a mask and, when it differs from the list the maps
+// were built for, the slot and row maps of the split residual / Jacobian.
+static void nl_maps(fg_mesh *m, const uint8_t *nl_host) {
   const int64_t nt = m->nt;
+  // eight mask bytes per test: a sparse mask (a few nonlinear parts in a large
+  // mesh) is scanned at memory speed
   std::vector<int> list;
-  for (int64_t k = 0; k < nt; ++k)
+  int64_t k = 0;
+  for (; k + 8 <= nt; k += 8) {
+    uint64_t word;
+    std::memcpy(&word, nl_host + k, sizeof(word));
+    if (!word) continue;
+    for (int b = 0; b < 8; ++b)
+      if (nl_host[k + b]) list.push_back((int)(k + b));
+  }
+  for (; k < nt; ++k)
     if (nl_host[k]) list.push_back((int)k);
   if (!m->nl_maps_valid || list != m->nl_list_host) {
     const int n = (int)list.size();
@@ -1024,6 +1042,20 @@ void fg_nl_setup(fg_mesh *m, const uint8_t *nl_host, bool mixed) {
     }
     m->nl_list_host = list;
     m->nl_maps_valid = true;
+  }
+}
+
+void fg_nl_setup(fg_mesh *m, const uint8_t *nl_host, bool mixed) {
+  FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "Newton magnetostatics needs P1 tetrahedra");
+  fg_ensure_records(m);
+  const int64_t nt = m->nt;
+  // the mask of the handle's inputs, unchanged since its list was built, needs no
+  // scan (a scan of millions of elements takes milliseconds on the host, with the
+  // device idle)
+  const bool own = (nl_host == m->nl_host.data());
+  if (!(own && m->nl_list_current && m->nl_maps_valid)) {
+    nl_maps(m, nl_host);
+    if (own) m->nl_list_current = true;
   }
   // the linear elements' operator (nonlinear elements contribute 0), Dirichlet rows
   // applied; element state starts at the linear values

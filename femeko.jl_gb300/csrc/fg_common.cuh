@@ -82,8 +82,9 @@ enum {
   S_NSCAL = 16
 };
 // CG control words; I_FAULT is set by a kernel whose asynchronous copy did not
-// complete within its bounded wait (the solve stops and reports an error).
-enum { I_DONE = 0, I_ITERS, I_MAXIT, I_STATUS, I_FAULT, I_NINT = 8 };
+// complete within its bounded wait (the solve stops and reports an error); I_BODIES
+// counts the bodies run by a whole-solve loop graph.
+enum { I_DONE = 0, I_ITERS, I_MAXIT, I_STATUS, I_FAULT, I_BODIES, I_NINT = 8 };
 
 // Reduction workspace: per-block partials and an arrival counter for the
 // "last block finishes the sum" pattern (the sum runs in block order, so results
@@ -93,11 +94,13 @@ struct RedWs {
   unsigned int *counter;
 };
 
-// A block of CG iterations captured as a CUDA graph.
+// A block of CG iterations captured as a CUDA graph; `loop`: the graph is a WHILE
+// conditional node around that block, run until the device's done flag is set.
 struct GraphCache {
   cudaGraphExec_t exec = nullptr;
   const void *key[8] = {nullptr};
   int iters = 0;
+  bool loop = false;
 };
 
 struct fg_mesh {
@@ -140,6 +143,8 @@ struct fg_mesh {
   // (sl_lcol), so a CTA gathers each needed vector entry once into shared memory.
   int hrows = 0, hcap = 0, hmax = 0, nhblocks = 0;
   int tmax = 0;       // most matrix entries (padded slots) of one row block
+  int tmax256 = 0;    // most matrix entries (padded slots) of one 256-row block
+  int bulk_fit = -1;  // resident CTAs per SM of the bulk-staged SpMV (-1: not sized yet)
   int pipe_grid = 0;  // CTAs of the persistent pipelined iteration (0: not sized yet, -1: does not fit)
   int *halo_col = nullptr, *halo_len = nullptr;
   uint16_t *sl_lcol = nullptr;
@@ -185,6 +190,7 @@ struct fg_mesh {
   std::vector<uint8_t> nl_host;                  // nonlinear mask of the current Newton inputs
   double *u0dev = nullptr;                       // Dirichlet values / initial guess of the Newton inputs
   bool nl_maps_valid = false;
+  bool nl_list_current = false;                  // nl_list_host was built from nl_host as it is now
   uint8_t *target = nullptr;  // nt objective mask (adjoint)
   double *objbuf = nullptr;   // 2 x nt objective scratch (adjoint)
 
@@ -258,6 +264,9 @@ void fg_newton_assemble(fg_mesh *m, const double *d_u, double Ms, double Hk, boo
 // elements' operator and the nonlinear elements' maps; fg_newton_assemble_split then
 // has the contract of fg_newton_assemble.
 void fg_nl_setup(fg_mesh *m, const uint8_t *nl_host, bool mixed);
+// Stores the nonlinear mask of new Newton inputs in m->nl_host; the element list
+// built from it is kept when the mask did not change.
+void fg_set_nl_host(fg_mesh *m, const uint8_t *nl);
 void fg_newton_assemble_split(fg_mesh *m, const double *d_u, double Ms, double Hk, bool mixed, double *d_F,
                               bool want_jacobian, bool tangent);
 // d_out[i] = sum of the vector records of row i (P1 tetrahedra), no Dirichlet masking.
@@ -284,8 +293,14 @@ void fg_adjoint_grad_dev(fg_mesh *m, const double *d_lam, const double *d_u, dou
 // solve (fg_solve.cu)
 double fg_norm2_dev(fg_mesh *m, const double *x, int64_t n, bool mask_fixed);
 double fg_dot_dev(fg_mesh *m, const double *x, const double *y, int64_t n, bool mask_fixed);
+// Enqueues x.y into scal[slot] (slots 10-15 are free for callers) without waiting.
+void fg_dot_enqueue(fg_mesh *m, const double *x, const double *y, int64_t n, bool mask_fixed, int slot);
+// Throws the error that a device flag word h reports (no-op for 0).
+void fg_raise_flags(fg_mesh *m, int h, const char *where);
 // Solves A x = b (A = the handle's operator, SELL layout) on free rows.  b, x are FP64
 // device vectors; x holds the initial guess.  Returns iterations; stats filled.
+// newton_inner: one inner solve from x = 0 (no FP64 refinement), not timed; b_norm,
+// when >= 0, is |b| on the free rows, already known to the caller.
 int fg_pcg_solve(fg_mesh *m, const double *d_b, double *d_x, const fg_solve_opts &o, fg_solve_stats *st,
-                 bool newton_inner);
+                 bool newton_inner, double b_norm = -1.0);
 void fg_spmv64_dev(fg_mesh *m, const double *x, double *y);

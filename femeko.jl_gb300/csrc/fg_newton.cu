@@ -79,17 +79,25 @@ static int newton_dev(fg_mesh *m, double *d_u, const uint8_t *nl_host, const fg_
   so.use_graph = o.use_graph;
   const int64_t nv = m->nv;
   const unsigned g = grid_for(nv, 256);
-  cudaEvent_t e0, e1;
+  // e0/e1 bracket the solve, e0/es the set-up, ec0/ec1 each inner solve (read after
+  // the next host wait, so that timing adds none)
+  cudaEvent_t e0, e1, es, ec0, ec1;
   FG_CUDA_TRY(cudaEventCreate(&e0));
   FG_CUDA_TRY(cudaEventCreate(&e1));
+  FG_CUDA_TRY(cudaEventCreate(&es));
+  FG_CUDA_TRY(cudaEventCreate(&ec0));
+  FG_CUDA_TRY(cudaEventCreate(&ec1));
   FG_CUDA_TRY(cudaEventRecord(e0, m->stream));
 
   // the linear elements' operator once; each residual / Jacobian below re-evaluates
   // only the nonlinear elements on top of it
   fg_nl_setup(m, nl_host, mixed);
   fg_newton_assemble_split(m, d_u, o.Ms, o.Hk, mixed, d_F, true, o.picard_steps <= 0);
+  FG_CUDA_TRY(cudaEventRecord(es, m->stream));
   fg_check_flags(m, "fg_newton_magnetostatics");
   double rF = fg_norm2_dev(m, d_F, nv, true);
+  float setup_ms = 0.f, cg_ms = 0.f;
+  cudaEventElapsedTime(&setup_ms, e0, es);
   int it = 0, cg_total = 0, trials = 0, converged = 0, status = 0;
   double ratio = 0.0, alpha = 0.0;
   double eta = (o.forcing == FG_FORCING_EW) ? o.eta_max : o.inner_rtol, rF_prev = -1.0;
@@ -111,7 +119,9 @@ static int newton_dev(fg_mesh *m, double *d_u, const uint8_t *nl_host, const fg_
     const bool next_tangent = (it >= o.picard_steps);
     FG_CUDA_TRY(cudaMemsetAsync(d_du, 0, sizeof(double) * (size_t)nv, m->stream));
     fg_solve_stats cst{};
-    fg_pcg_solve(m, d_F, d_du, so, &cst, true);
+    FG_CUDA_TRY(cudaEventRecord(ec0, m->stream));
+    fg_pcg_solve(m, d_F, d_du, so, &cst, true, rF);
+    FG_CUDA_TRY(cudaEventRecord(ec1, m->stream));
     cg_total += cst.iterations;
     alpha = 1.0;
     bool need_jacobian = false;
@@ -172,9 +182,19 @@ static int newton_dev(fg_mesh *m, double *d_u, const uint8_t *nl_host, const fg_
       fg_newton_assemble_split(m, d_u, o.Ms, o.Hk, mixed, d_F, true, next_tangent);
       rF = fg_norm2_dev(m, d_F, nv, true);
     }
-    fg_check_flags(m, "fg_newton_magnetostatics");
-    double dn = alpha * fg_norm2_dev(m, d_du, nv, false);
-    double un = fg_norm2_dev(m, d_u, nv, false);
+    // |du|, |u| and the device error flags in one round trip
+    fg_dot_enqueue(m, d_du, d_du, nv, false, 10);
+    fg_dot_enqueue(m, d_u, d_u, nv, false, 11);
+    FG_CUDA_TRY(cudaMemcpyAsync(m->hbuf, m->scal + 10, 2 * sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+    FG_CUDA_TRY(cudaMemcpyAsync(m->hint + 8, m->flags, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
+    fg_sync(m);
+    fg_raise_flags(m, m->hint[8], "fg_newton_magnetostatics");
+    {
+      float t = 0.f;
+      if (cudaEventElapsedTime(&t, ec0, ec1) == cudaSuccess) cg_ms += t;
+    }
+    double dn = alpha * std::sqrt(m->hbuf[0]);
+    double un = std::sqrt(m->hbuf[1]);
     ratio = (un > 0.0) ? dn / un : dn;
     if (!std::isfinite(ratio)) throw FgError{FG_NAN, "Newton update is not finite"};
     if (ratio <= o.tol_update) { converged = 1; break; }
@@ -188,6 +208,9 @@ static int newton_dev(fg_mesh *m, double *d_u, const uint8_t *nl_host, const fg_
   cudaEventElapsedTime(&ms, e0, e1);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  cudaEventDestroy(es);
+  cudaEventDestroy(ec0);
+  cudaEventDestroy(ec1);
   if (st) {
     st->newton_iters = std::min(it, o.maxit);
     st->cg_iters = cg_total;
@@ -198,6 +221,8 @@ static int newton_dev(fg_mesh *m, double *d_u, const uint8_t *nl_host, const fg_
     st->alpha = alpha;
     st->energy = energy;
     st->ms = ms;
+    st->setup_ms = setup_ms;
+    st->cg_ms = cg_ms;
   }
   (void)status;
   return converged ? 0 : 1;
@@ -220,7 +245,7 @@ static void set_inputs(fg_mesh *m, const uint8_t *nl, const double *mu_lin, cons
   upload(m, m->mu_lin, mu_lin, sizeof(double) * (size_t)m->nt);
   if (!m->u0dev) m->u0dev = dev_alloc<double>(m, (size_t)m->nv);
   upload(m, m->u0dev, u0, sizeof(double) * (size_t)m->nv);
-  m->nl_host.assign(nl, nl + m->nt);
+  fg_set_nl_host(m, nl);
 }
 
 // Newton solve from the inputs held on the device; u, H and mu stay on the device.
@@ -358,8 +383,8 @@ extern "C" fg_status fg_adjoint_dJdmu(fg_mesh *m, const double *mur, const doubl
     } else {
       upload(m, m->nl, nl, (size_t)nt);
       fg_newton_stats ns{};
-      m->nl_host.assign(nl, nl + nt);
-      converged = newton_dev(m, d_u, nl, opts, &ns) == 0;
+      fg_set_nl_host(m, nl);
+      converged = newton_dev(m, d_u, m->nl_host.data(), opts, &ns) == 0;
       fwd_iters = ns.cg_iters;
       newton_iters = ns.newton_iters;
       // the Jacobian at the converged state: FP64 for the refinement residual, FP32

@@ -55,6 +55,10 @@ void fg_check_flags(fg_mesh *m, const char *where) {
   int h = 0;
   FG_CUDA_TRY(cudaMemcpyAsync(&h, m->flags, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
   fg_sync(m);
+  fg_raise_flags(m, h, where);
+}
+
+void fg_raise_flags(fg_mesh *m, int h, const char *where) {
   if (!h) return;
   FG_CUDA_TRY(cudaMemsetAsync(m->flags, 0, sizeof(int), m->stream));
   std::string w(where);
@@ -541,6 +545,10 @@ extern "C" fg_status fg_mesh_create(const double *p, int64_t nv, const int32_t *
     }
     hsl_ptr[m->nslices] = (int)acc;
     hin_ptr[m->nslices] = (int)acc2;
+    // largest 256-row block in padded entries (the bulk-staged SpMV stages one)
+    m->tmax256 = 0;
+    for (int s0 = 0; s0 < m->nslices; s0 += 256 / FG_SLICE)
+      m->tmax256 = std::max(m->tmax256, hsl_ptr[std::min(s0 + 256 / FG_SLICE, m->nslices)] - hsl_ptr[s0]);
     m->nsell = acc;
     m->ninc = acc2;
 

@@ -696,6 +696,120 @@ __global__ void __launch_bounds__(R) k_cg32s_spmv_halo(int64_t n, const int *__r
   if (grid_finish<3>(part, partials, counter, tot)) cgcg_scalars(tot, scal, ictl);
 }
 
+// The split SpMV with the matrix entries staged by the bulk-copy engine: a persistent
+// grid whose blocks walk their 256-row blocks; while a block computes one, the values
+// and column offsets of its next one (two contiguous ranges of the SELL layout) are
+// in flight into the other shared-memory stage (cp.async.bulk completing on an
+// mbarrier).  Threads read their row's entries from shared memory and gather u from
+// global memory.  cap: the most padded entries of one 256-row block.  A stage that
+// does not arrive within the bounded wait stops the CG with I_FAULT set.
+template <class CI>
+__global__ void __launch_bounds__(256) k_cg32s_spmv_bulk(int64_t n, int nslices, int cap,
+                                                         const int *__restrict__ sl_ptr,
+                                                         const int *__restrict__ sl_len,
+                                                         const typename CI::T *__restrict__ col,
+                                                         const float *__restrict__ val, const float *__restrict__ u,
+                                                         const float *__restrict__ r, float *__restrict__ w,
+                                                         double *scal, int *ictl, double *partials,
+                                                         unsigned *counter) {
+  using T = typename CI::T;
+  using T4 = typename CI::T4;
+  extern __shared__ __align__(128) unsigned char sm_bulk[];
+  __shared__ __align__(8) uint64_t bar[2];
+  if (ictl[I_DONE]) return;
+  const int tid = threadIdx.x;
+  const size_t o_col = pipe_align((size_t)cap * 4);
+  const size_t stage = o_col + pipe_align((size_t)cap * sizeof(T));
+  const int64_t nrb = (n + 255) / 256;
+  const int K = (int)((nrb - (int64_t)blockIdx.x + gridDim.x - 1) / gridDim.x);
+  auto rowblock = [&](int k) { return (int64_t)blockIdx.x + (int64_t)k * gridDim.x; };
+  // thread 0: the values and columns of the k-th row block of this CTA into stage st
+  auto issue = [&](int k, int st) {
+    const int s0 = (int)(rowblock(k) * (256 / FG_SLICE)), s1 = min(s0 + 256 / FG_SLICE, nslices);
+    const int e0 = sl_ptr[s0], e1 = sl_ptr[s1];
+    const uint32_t vb = (uint32_t)(e1 - e0) * 4u, cb = (uint32_t)(e1 - e0) * (uint32_t)sizeof(T);
+    fence_proxy_async_smem();
+    mbar_arrive_expect_tx(&bar[st], vb + cb);
+    bulk_g2s(sm_bulk + st * stage, val + e0, vb, &bar[st]);
+    bulk_g2s(sm_bulk + st * stage + o_col, col + e0, cb, &bar[st]);
+  };
+  uint32_t inflight = 0u;  // bit st: a copy into stage st not yet waited for
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_proxy_async_smem();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    issue(0, 0);
+    if (K > 1) issue(1, 1);
+  }
+  inflight = (K > 1) ? 3u : 1u;
+  uint32_t phase = 0u;  // bit st: parity of stage st's next phase
+  bool ok = true;
+  Acc<float> dots[3];
+  for (int k = 0; k < K; ++k) {
+    const int st = k & 1;
+    const int64_t rb = rowblock(k);
+    const int64_t i = rb * 256 + tid;
+    const bool row = i < n;
+    int G = 0, base = 0;
+    float ui = 0.f, ri = 0.f;
+    if (row) {
+      // own row's metadata and vector entries, issued before the wait
+      const int s = (int)(i >> 5);
+      G = sl_len[s];
+      base = sl_ptr[s] - sl_ptr[rb * (256 / FG_SLICE)] + (tid & 31) * FG_GROUP;
+      ui = u[i];
+      ri = r[i];
+    }
+    const bool got = mbar_wait(&bar[st], (phase >> st) & 1u);
+    if (got) {
+      phase ^= 1u << st;
+      inflight &= ~(1u << st);
+    }
+    if (__syncthreads_or(!got)) { ok = false; break; }
+    if (row) {
+      const float *v = reinterpret_cast<const float *>(sm_bulk + st * stage);
+      const T *c = reinterpret_cast<const T *>(sm_bulk + st * stage + o_col);
+      float acc = 0.f;
+#pragma unroll 4
+      for (int g = 0; g < G; ++g) {
+        const float4 vv = *reinterpret_cast<const float4 *>(v + base + g * FG_SLICE * FG_GROUP);
+        const T4 cc = *reinterpret_cast<const T4 *>(c + base + g * FG_SLICE * FG_GROUP);
+        acc = fmaf(vv.x, __ldg(u + CI::col(cc.x, i)), acc);
+        acc = fmaf(vv.y, __ldg(u + CI::col(cc.y, i)), acc);
+        acc = fmaf(vv.z, __ldg(u + CI::col(cc.z, i)), acc);
+        acc = fmaf(vv.w, __ldg(u + CI::col(cc.w, i)), acc);
+      }
+      w[i] = acc;
+      dots[0].add(ri * ui);
+      dots[1].add(acc * ui);
+      dots[2].add(ri * ri);
+    }
+    // every thread is done with stage st: refill it with the row block after next
+    __syncthreads();
+    if (k + 2 < K) {
+      if (tid == 0) issue(k + 2, st);
+      inflight |= 1u << st;
+    }
+  }
+  if (!ok) {
+    // a stage did not arrive: wait (bounded) for the copies in flight, stop the CG
+    if (tid == 0) {
+      for (int st = 0; st < 2; ++st)
+        if (inflight & (1u << st)) mbar_wait(&bar[st], (phase >> st) & 1u, 1 << 20);
+      atomicExch(ictl + I_FAULT, 1);
+      atomicExch(ictl + I_DONE, 1);
+    }
+    __syncthreads();
+  }
+  double part[3];
+  block_sum_acc<3>(dots, part);
+  double tot[3];
+  if (grid_finish<3>(part, partials, counter, tot) && ok) cgcg_scalars(tot, scal, ictl);
+}
+
 // Jacobi-PCG as plain CG on the symmetrically scaled system (the scaled split
 // variant): A' = S A S with S = D^-1/2 (sdiag = sqrt of the Jacobi inverse, 0 on
 // Dirichlet rows), b' = S b, x = S y.  The iterates are those of Jacobi-PCG; the
@@ -742,6 +856,7 @@ __global__ void k_cg32ss_init(int64_t n, int64_t np, const double *__restrict__ 
     ictl[I_STATUS] = 0;
     ictl[I_FAULT] = 0;
     ictl[I_DONE] = 0;
+    ictl[I_BODIES] = 0;
   }
 }
 
@@ -797,6 +912,7 @@ __global__ void k_cg32s_init(int64_t n, int64_t np, const double *__restrict__ r
     ictl[I_STATUS] = 0;
     ictl[I_FAULT] = 0;
     ictl[I_DONE] = 0;
+    ictl[I_BODIES] = 0;
   }
 }
 
@@ -824,6 +940,7 @@ __global__ void k_cg32_init(int64_t n, int64_t np, const double *__restrict__ ri
     ictl[I_STATUS] = 0;
     ictl[I_FAULT] = 0;
     ictl[I_DONE] = 0;
+    ictl[I_BODIES] = 0;
   }
 }
 
@@ -981,6 +1098,7 @@ __global__ void k_cg64_init(int64_t n, int64_t np, const double *__restrict__ ri
     ictl[I_STATUS] = 0;
     ictl[I_FAULT] = 0;
     ictl[I_DONE] = 0;
+    ictl[I_BODIES] = 0;
   }
 }
 
@@ -1054,12 +1172,16 @@ static unsigned red_grid(int64_t n) {
 }
 static unsigned row_grid(const fg_mesh *m) { return grid_for(m->nv, 256); }
 
-double fg_dot_dev(fg_mesh *m, const double *x, const double *y, int64_t n, bool mask_fixed) {
-  const int slot = 8;
+void fg_dot_enqueue(fg_mesh *m, const double *x, const double *y, int64_t n, bool mask_fixed, int slot) {
   k_dot64<<<red_grid(n), 256, 0, m->stream>>>(n, x, y, (mask_fixed && m->has_fixed) ? m->fixed : nullptr, slot,
                                               m->scal, m->red.partials, m->red.counter);
   FG_CUDA_TRY(cudaGetLastError());
   FG_LAUNCHED(1);
+}
+
+double fg_dot_dev(fg_mesh *m, const double *x, const double *y, int64_t n, bool mask_fixed) {
+  const int slot = 8;
+  fg_dot_enqueue(m, x, y, n, mask_fixed, slot);
   FG_CUDA_TRY(cudaMemcpyAsync(m->hbuf, m->scal + slot, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
   fg_sync(m);
   return m->hbuf[0];
@@ -1123,7 +1245,7 @@ static void ensure_cg64(fg_mesh *m) {
 // programmatic dependent launch, 10 the same with the matrix values held in L2,
 // 11-15 persistent grids of 4, 3, 5, 6 and 7 blocks per SM, 16 CG on the
 // symmetrically Jacobi-scaled system with the SpMV of variant 14
-constexpr int FG_N_SPMV32 = 17;
+constexpr int FG_N_SPMV32 = 20;
 static inline bool split32(int v) { return v >= 6; }
 constexpr int FG_N_SPMV64 = 4;   // 0 direct gathers, 1 halo staging, 2/3 persistent with 4/8 blocks per SM
 
@@ -1338,6 +1460,67 @@ static void ensure_scaled(fg_mesh *m) {
   m->val32s_version = m->op_version;
 }
 
+// Shared memory of the bulk-staged SpMV: two stages of the largest 256-row block.
+static size_t bulk_smem(const fg_mesh *m) {
+  const size_t cb = m->use_dcol ? sizeof(int16_t) : sizeof(int);
+  return 2 * (pipe_align((size_t)m->tmax256 * 4) + pipe_align((size_t)m->tmax256 * cb));
+}
+
+// Blocks per SM of the bulk-staged variants 17, 18, 19 (4, 3, 2 wanted), or 0 where
+// two stages do not fit; sized once per handle.  The kernels may take up to the
+// device's opt-in shared memory (set once per process).
+static int bulk_per_sm(fg_mesh *m, int v) {
+  static const int kWant[3] = {4, 3, 2};
+  if (m->bulk_fit < 0) {
+    static std::once_flag attr_once;
+    static int dyn_max = 0;  // opt-in shared memory less the kernels' static shared memory
+    std::call_once(attr_once, [&]() {
+      int dev_max = 0;
+      cudaFuncAttributes fa[2];
+      if (cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, m->device) != cudaSuccess ||
+          cudaFuncGetAttributes(&fa[0], k_cg32s_spmv_bulk<ColRel>) != cudaSuccess ||
+          cudaFuncGetAttributes(&fa[1], k_cg32s_spmv_bulk<ColAbs>) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+      }
+      const int d = dev_max - (int)std::max(fa[0].sharedSizeBytes, fa[1].sharedSizeBytes);
+      if (cudaFuncSetAttribute(k_cg32s_spmv_bulk<ColRel>, cudaFuncAttributeMaxDynamicSharedMemorySize, d) !=
+              cudaSuccess ||
+          cudaFuncSetAttribute(k_cg32s_spmv_bulk<ColAbs>, cudaFuncAttributeMaxDynamicSharedMemorySize, d) !=
+              cudaSuccess) {
+        cudaGetLastError();
+        return;
+      }
+      dyn_max = d;
+    });
+    const size_t smem = bulk_smem(m);
+    int per_sm = 0;
+    if (m->tmax256 > 0 && smem <= (size_t)dyn_max) {
+      if (m->use_dcol)
+        FG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg32s_spmv_bulk<ColRel>, 256, smem));
+      else
+        FG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg32s_spmv_bulk<ColAbs>, 256, smem));
+    }
+    m->bulk_fit = per_sm;
+  }
+  return std::min(m->bulk_fit, kWant[v - 17]);
+}
+
+static void bulk_launch32(fg_mesh *m, int v) {
+  const int per_sm = bulk_per_sm(m, v);
+  FG_REQUIRE(per_sm > 0, FG_UNSUPPORTED, "bulk-staged SpMV: row blocks too large for shared memory");
+  const unsigned g = std::min<unsigned>(grid_for(m->nv, 256), (unsigned)per_sm * (unsigned)std::max(m->sm_count, 1));
+  const size_t smem = bulk_smem(m);
+  if (m->use_dcol)
+    k_cg32s_spmv_bulk<ColRel><<<g, 256, smem, m->stream>>>(m->nv, m->nslices, m->tmax256, m->sl_ptr, m->sl_len,
+                                                           m->sl_dcol, m->val32, m->v32[7], m->v32[4], m->v32[5],
+                                                           m->scal, m->ictl, m->red.partials, m->red.counter);
+  else
+    k_cg32s_spmv_bulk<ColAbs><<<g, 256, smem, m->stream>>>(m->nv, m->nslices, m->tmax256, m->sl_ptr, m->sl_len,
+                                                           m->sl_col, m->val32, m->v32[7], m->v32[4], m->v32[5],
+                                                           m->scal, m->ictl, m->red.partials, m->red.counter);
+}
+
 static void launch_spmv32s(fg_mesh *m, int v) {
   const bool pdl = (v == 9);
   if (v == 16) {
@@ -1363,7 +1546,9 @@ static void launch_spmv32s(fg_mesh *m, int v) {
                 m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl, m->red.partials, m->red.counter);
     return;
   }
-  if (v >= 8) {
+  if (v >= 17) {
+    bulk_launch32(m, v);
+  } else if (v >= 8) {
     // persistent: 8 (variants 8-10), 4 (11), 3 (12), 5 (13), 6 (14) or 7 (15)
     // resident 256-thread blocks per SM; fewer blocks walk more row blocks each and
     // reduce once for all of them
@@ -1488,50 +1673,130 @@ static void start_cg(fg_mesh *m, bool mixed, const double *r64, double scale, do
   FG_LAUNCHED(2);
 }
 
+// Closes each body of the whole-solve loop graph: the WHILE node runs the body again
+// while the CG is not done, and never more than max_it / body + 2 times (a bound that
+// holds even if no iteration of a body counted).
+__global__ void k_cg_continue(cudaGraphConditionalHandle h, int *ictl, int body) {
+  if (threadIdx.x != 0) return;
+  const int b = ictl[I_BODIES] + 1;
+  ictl[I_BODIES] = b;
+  const bool more = ictl[I_DONE] == 0 && b < ictl[I_MAXIT] / body + 2;
+  cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+
+// Captures `enqueue` (one body of iterations) into a graph: a plain block of
+// iterations, or a WHILE conditional node around the body and k_cg_continue, so that
+// one launch runs the solve to its end without host round trips.  Returns false,
+// with the stream out of capture and the error cleared, when the loop graph cannot
+// be built (the caller then replays plain blocks).
+template <class F>
+static bool capture_iterations(fg_mesh *m, GraphCache &gc, int body, bool loop, F &&enqueue) {
+  cudaGraph_t graph = nullptr, target = nullptr;
+  cudaGraphConditionalHandle h = 0;
+  if (loop) {
+    if (cudaGraphCreate(&graph, 0) != cudaSuccess ||
+        cudaGraphConditionalHandleCreate(&h, graph, 1u, cudaGraphCondAssignDefault) != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      cudaGetLastError();
+      return false;
+    }
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np) != cudaSuccess) {
+      cudaGraphDestroy(graph);
+      cudaGetLastError();
+      return false;
+    }
+    target = np.conditional.phGraph_out[0];
+    FG_CUDA_TRY(cudaStreamBeginCaptureToGraph(m->stream, target, nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeThreadLocal));
+  } else {
+    FG_CUDA_TRY(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
+  }
+  bool ok = true;
+  try {
+    enqueue();
+    if (loop) k_cg_continue<<<1, 32, 0, m->stream>>>(h, m->ictl, body);
+    ok = cudaGetLastError() == cudaSuccess;
+  } catch (const FgError &) {
+    ok = false;
+  }
+  cudaGraph_t captured = nullptr;
+  ok = (cudaStreamEndCapture(m->stream, &captured) == cudaSuccess) && ok;
+  if (!loop) graph = captured;
+  if (ok) ok = cudaGraphInstantiate(&gc.exec, graph, 0) == cudaSuccess;
+  if (graph) cudaGraphDestroy(graph);
+  if (!ok) {
+    gc.exec = nullptr;
+    cudaGetLastError();
+    FG_REQUIRE(loop, FG_CUDA, "CG graph capture failed");
+  }
+  return ok;
+}
+
 // Runs CG iterations until the device sets "done".  Returns the iteration count.
+// use_graph 1: one launch of a WHILE-node graph (bodies of check_every iterations)
+// runs the whole solve; where that graph cannot be built (launch attributes the
+// conditional body does not take), and with use_graph 2, blocks of check_every
+// iterations are replayed with a host check of the done flag between them.
 static int run_cg(fg_mesh *m, bool mixed, const fg_solve_opts &o, int *status) {
   int block = o.check_every > 0 ? o.check_every : 32;
   if (block & 1) ++block;
   const int per_iter = (mixed && !split32(m->spmv_variant32)) ? 1 : 2;
   GraphCache &gc = m->graph[mixed ? 1 : 0];
+  const bool use_graph = o.use_graph != 0;
+  // PDL and L2-window launches keep the host-checked blocks
+  const bool want_loop = o.use_graph == 1 && !(mixed && (m->spmv_variant32 == 9 || m->spmv_variant32 == 10));
+  const int body = block;
   const void *key[5] = {mixed ? (const void *)m->val32 : (const void *)m->val64,
                         mixed ? (const void *)(intptr_t)(m->spmv_variant32 + 1) : (const void *)m->v64[0],
-                        (const void *)(intptr_t)block, (const void *)(intptr_t)m->use_dcol,
+                        (const void *)(intptr_t)body, (const void *)(intptr_t)m->use_dcol,
                         (const void *)(intptr_t)(mixed ? 0 : m->spmv_variant64 + 1)};
-  const bool use_graph = o.use_graph != 0;
-  auto enqueue_block = [&]() {
-    for (int it = 0; it < block; ++it) {
+  auto enqueue_block = [&](int n) {
+    for (int it = 0; it < n; ++it) {
       if (mixed) launch_iter32(m, m->spmv_variant32, (it & 1) != 0);
       else { launch_vec64(m); launch_spmv64cg(m); }
     }
   };
+  bool loop = false;
   if (use_graph) {
-    bool match = gc.exec && gc.iters == block;
+    bool match = gc.exec && gc.iters == body && gc.loop == want_loop;
     for (int j = 0; j < 5 && match; ++j) match = (gc.key[j] == key[j]);
     if (!match) {
       if (gc.exec) { cudaGraphExecDestroy(gc.exec); gc.exec = nullptr; }
-      cudaGraph_t graph;
-      FG_CUDA_TRY(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
-      enqueue_block();
-      FG_CUDA_TRY(cudaStreamEndCapture(m->stream, &graph));
-      FG_CUDA_TRY(cudaGraphInstantiate(&gc.exec, graph, 0));
-      cudaGraphDestroy(graph);
-      gc.iters = block;
+      gc.loop = want_loop && capture_iterations(m, gc, body, true, [&]() { enqueue_block(body); });
+      if (!gc.loop) capture_iterations(m, gc, block, false, [&]() { enqueue_block(block); });
+      gc.iters = gc.loop ? body : block;
       for (int j = 0; j < 5; ++j) gc.key[j] = key[j];
+      if (!gc.loop) gc.key[2] = (const void *)(intptr_t)-1;  // a plain block: rebuilt for a new request
     }
+    loop = gc.loop;
   }
+  // the whole solve in one launch (bodies of an even number of iterations keep the
+  // fused variants' state buffers in step); launches are counted from the bodies run
+  if (loop) FG_CUDA_TRY(cudaGraphLaunch(gc.exec, m->stream));
+  int bodies = 0;
   for (;;) {
-    FG_CUDA_TRY(cudaMemcpyAsync(m->hint, m->ictl, sizeof(int) * 5, cudaMemcpyDeviceToHost, m->stream));
+    FG_CUDA_TRY(cudaMemcpyAsync(m->hint, m->ictl, sizeof(int) * (I_BODIES + 1), cudaMemcpyDeviceToHost,
+                                m->stream));
     fg_sync(m);
+    if (loop) {
+      FG_LAUNCHED((long long)(m->hint[I_BODIES] - bodies) * (per_iter * body + 1));
+      bodies = m->hint[I_BODIES];
+    }
     FG_REQUIRE(m->hint[I_FAULT] == 0, FG_CUDA, "CG kernel: an asynchronous shared-memory copy did not complete");
     if (m->hint[I_DONE]) break;
     if (use_graph) {
       FG_CUDA_TRY(cudaGraphLaunch(gc.exec, m->stream));
     } else {
-      enqueue_block();
+      enqueue_block(block);
       FG_CUDA_TRY(cudaGetLastError());
     }
-    FG_LAUNCHED((long long)per_iter * block);
+    if (!loop) FG_LAUNCHED((long long)per_iter * block);
   }
   if (status) *status = m->hint[I_STATUS];
   return std::max(m->hint[I_ITERS], 0);
@@ -1577,7 +1842,8 @@ static int inner_solve(fg_mesh *m, bool mixed, const double *r64, double rn, dou
       // a forced variant that this operator cannot run (no halo lists, stages too
       // large for shared memory) falls back to the plain gather kernel
       const int v = o.spmv - 1;
-      const bool avail = v < 4 || v == 6 || v == 8 || v == 9 || v >= 11 || (v == 10 && prepare_l2(m)) ||
+      const bool avail = v < 4 || v == 6 || v == 8 || v == 9 || (v >= 11 && v < 17) ||
+                         (v >= 17 && bulk_per_sm(m, v) > 0) || (v == 10 && prepare_l2(m)) ||
                          ((v == 4 || v == 7) && m->halo_col) || (v == 5 && pipe_available(m));
       m->spmv_variant32 = avail ? v : 0;
     } else if (!m->tuned32 && !tune_cache_get(m, true)) {
@@ -1607,7 +1873,7 @@ static int inner_solve(fg_mesh *m, bool mixed, const double *r64, double rn, dou
 }
 
 int fg_pcg_solve(fg_mesh *m, const double *d_b, double *d_x, const fg_solve_opts &o, fg_solve_stats *st,
-                 bool newton_inner) {
+                 bool newton_inner, double b_norm) {
   const bool mixed = o.precision == FG_MIXED;
   FG_REQUIRE(mixed ? m->val32 != nullptr : m->val64 != nullptr, FG_BAD_ARG, "operator not assembled");
   if (!m->v64[6]) m->v64[6] = dev_alloc<double>(m, (size_t)m->nvp);
@@ -1621,7 +1887,7 @@ int fg_pcg_solve(fg_mesh *m, const double *d_b, double *d_x, const fg_solve_opts
     if (newton_inner) {
       // x = 0, residual = b
       FG_CUDA_TRY(cudaMemcpyAsync(r64, d_b, sizeof(double) * (size_t)m->nv, cudaMemcpyDeviceToDevice, m->stream));
-      rn = fg_norm2_dev(m, r64, m->nv, true);
+      rn = (b_norm >= 0.0) ? b_norm : fg_norm2_dev(m, r64, m->nv, true);
     } else {
       FG_REQUIRE(m->val64 != nullptr, FG_BAD_ARG, "refinement needs the FP64 operator");
       spmv64_launch(m, d_x, d_b, r64, fx, 9);
@@ -1643,11 +1909,15 @@ int fg_pcg_solve(fg_mesh *m, const double *d_b, double *d_x, const fg_solve_opts
     if (ist == 2) { status = 2; break; }
     if (newton_inner) { status = ist; break; }
   }
-  FG_CUDA_TRY(cudaEventRecord(m->ev1, m->stream));
-  fg_sync(m);
+  // a Newton step continues on the stream: its solve is not timed (no wait here)
+  const bool timed = !newton_inner;
+  if (timed) {
+    FG_CUDA_TRY(cudaEventRecord(m->ev1, m->stream));
+    fg_sync(m);
+  }
   if (st) {
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, m->ev0, m->ev1);
+    if (timed) cudaEventElapsedTime(&ms, m->ev0, m->ev1);
     st->iterations = total;
     st->refinements = refinements;
     st->converged = (status == 0);
@@ -1864,7 +2134,7 @@ fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_v
   double best_us = 1e30;
   for (int v = 0; v < FG_N_SPMV32; ++v) {
     if (((v == 4 || v == 7) && !m->halo_col) || (v == 5 && !pipe_available(m)) ||
-        (v == 10 && !prepare_l2(m))) {  // not available here
+        (v == 10 && !prepare_l2(m)) || (v >= 17 && bulk_per_sm(m, v) == 0)) {  // not available here
       if (us_per_variant) us_per_variant[v] = 0.0;
       continue;
     }
@@ -1953,7 +2223,8 @@ extern "C" fg_status fg_set_cg_variant(fg_mesh *m, int32_t precision, int32_t va
       FG_REQUIRE(variant >= 0 && variant <= FG_N_SPMV32, FG_BAD_ARG, "fg_set_cg_variant: no such variant");
       if (variant == 0) { m->tuned32 = false; return FG_OK; }
       const int v = variant - 1;
-      const bool avail = v < 4 || v == 6 || v == 8 || v == 9 || v >= 11 || (v == 10 && prepare_l2(m)) ||
+      const bool avail = v < 4 || v == 6 || v == 8 || v == 9 || (v >= 11 && v < 17) ||
+                         (v >= 17 && bulk_per_sm(m, v) > 0) || (v == 10 && prepare_l2(m)) ||
                          ((v == 4 || v == 7) && m->halo_col) || (v == 5 && pipe_available(m));
       FG_REQUIRE(avail, FG_UNSUPPORTED, "fg_set_cg_variant: variant not available for this operator");
       m->spmv_variant32 = v;

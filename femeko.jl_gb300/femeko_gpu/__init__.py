@@ -176,7 +176,7 @@ def BoundaryIntegral(mesh: MESH, F, shell_id=(1,)):
 
 def solve_opts(precision="fp64", rtol=1e-10, maxiter=1_000_000, inner_rtol=1e-5, check_every=32, use_graph=True,
                spmv=0):
-    """Linear-solve options; spmv = 0 autotunes the FP32 CG iteration kernel, 1..5 forces a variant."""
+    """Linear-solve options; spmv = 0 autotunes the FP32 CG iteration kernel, 1..20 forces a variant."""
     o = L.SolveOpts()
     L.lib().fg_solve_opts_default(C.byref(o))
     o.precision = L.FG_MIXED if precision == "mixed" else L.FG_FP64
@@ -200,7 +200,7 @@ def newton_opts(precision="mixed", tol_update=1e-8, maxit=100, inner_rtol=1e-4, 
     o.tol_update, o.maxit, o.inner_rtol, o.cg_maxiter = tol_update, maxit, inner_rtol, cg_maxiter
     o.line_search = {"none": L.FG_LS_NONE, "reference": L.FG_LS_REFERENCE, "residual": L.FG_LS_RESIDUAL,
                      "quadratic": L.FG_LS_QUADRATIC}[line_search]
-    o.min_step, o.Ms, o.Hk, o.check_every, o.use_graph = min_step, Ms, Hk, check_every, int(use_graph)
+    o.min_step, o.Ms, o.Hk, o.check_every, o.use_graph = min_step, Ms, Hk, check_every, int(use_graph)   # 2: host-checked blocks
     return o
 
 

@@ -47,7 +47,8 @@ class NewtonOpts(C.Structure):
 class NewtonStats(C.Structure):
     _fields_ = [("newton_iters", C.c_int32), ("cg_iters", C.c_int32), ("converged", C.c_int32),
                 ("trials", C.c_int32), ("update_ratio", C.c_double), ("residual", C.c_double),
-                ("alpha", C.c_double), ("energy", C.c_double), ("ms", C.c_double)]
+                ("alpha", C.c_double), ("energy", C.c_double), ("ms", C.c_double), ("setup_ms", C.c_double),
+                ("cg_ms", C.c_double)]
 
 
 class AdjointStats(C.Structure):

@@ -78,6 +78,8 @@ struct NewtonStats
     alpha::Float64
     energy::Float64
     ms::Float64
+    setup_ms::Float64
+    cg_ms::Float64
 end
 
 const FG_OK = Cint(0)

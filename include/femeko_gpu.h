@@ -52,7 +52,7 @@ enum {
                           of |F(u + a du)|^2, kept in [0.1, 0.5] of the last step */
 };
 /* FP32 CG iteration kernel: FG_SPMV_AUTO lets the autotuner time the variants on
- * the first mixed solve of a handle and keep the fastest; k = 1..17 forces variant
+ * the first mixed solve of a handle and keep the fastest; k = 1..20 forces variant
  * k-1.  One fused kernel per iteration: 1: 4x-unrolled gather loop, 256 threads;
  * 2: all row loads issued first, 256 threads; 3: loop, 128 threads; 4: loop, 512
  * threads; 5: halo staging (the neighbour entries of a block of rows gathered once
@@ -65,7 +65,10 @@ enum {
  * them while a handle uses this variant); 12-16: 9 with 4, 3, 5, 6 and 7 blocks per
  * SM; 17: plain CG on the symmetrically Jacobi-scaled system D^-1/2 A D^-1/2 (the
  * same iterates as Jacobi-PCG, no preconditioned-residual vector, stopping test on
- * the preconditioned residual norm) with the SpMV of 15.
+ * the preconditioned residual norm) with the SpMV of 15; 18-20: 9 with 4, 3 and 2
+ * blocks per SM and the matrix entries of each block's next 256 rows copied into a
+ * second shared-memory stage by the bulk-copy engine while it computes the current
+ * ones (available where two stages fit in shared memory).
  * The autotuner times each variant as a replayed CUDA graph of iterations, the way
  * the solver runs them. */
 enum { FG_SPMV_AUTO = 0 };
@@ -77,9 +80,11 @@ typedef struct fg_solve_opts {
   double rtol;         /* FP64 relative residual target ||b - A x|| <= rtol ||b|| */
   int32_t maxiter;     /* cap on CG iterations (inner iterations in total) */
   double inner_rtol;   /* mixed: FP32 PCG target per refinement step */
-  int32_t check_every; /* iterations per graph launch between convergence checks (even) */
-  int32_t use_graph;   /* 1: replay each block of iterations as a CUDA graph */
-  int32_t spmv;        /* FG_SPMV_AUTO or a forced variant 1..17 */
+  int32_t check_every; /* iterations between convergence checks (even) */
+  int32_t use_graph;   /* 1: the whole CG as one CUDA graph launch (a WHILE node around
+                          check_every iterations, the test on the device); 2: a graph of
+                          check_every iterations per launch, tested on the host; 0: no graph */
+  int32_t spmv;        /* FG_SPMV_AUTO or a forced variant 1..20 */
   int32_t reserved_;
 } fg_solve_opts;
 
@@ -124,6 +129,8 @@ typedef struct fg_newton_stats {
   double alpha;        /* last accepted step */
   double energy;       /* integral of H dB (src/magneticProperties.jl:252-309, closed form) */
   double ms;           /* device time of the solve */
+  double setup_ms;     /* of which: the linear elements' operator and the first residual */
+  double cg_ms;        /* of which: the inner CG solves */
 } fg_newton_stats;
 
 /* Defaults matching the reference behaviour / the published path settings. */
@@ -341,7 +348,7 @@ fg_status fg_bench_kernel(fg_mesh *m, int32_t which, int32_t precision, int32_t 
  * be NULL) the measured microseconds per launch.  No reference counterpart. */
 fg_status fg_autotune(fg_mesh *m, int32_t precision, int32_t *variant, double *us_per_variant, int32_t n_slots);
 /* Fixes the CG kernel variant of one precision for the handle (the numbering of
- * fg_solve_opts.spmv: FG_MIXED 1..17, FG_FP64 1..4), or 0 to return to the
+ * fg_solve_opts.spmv: FG_MIXED 1..20, FG_FP64 1..4), or 0 to return to the
  * autotuner's choice at the next solve.  The autotuner's choices are remembered per
  * process for each operator shape (device, rows, padded entries, longest row), so a
  * new handle for a mesh of the same structure does not time the variants again.
