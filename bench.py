@@ -245,6 +245,11 @@ def run_ours(args):
     value = ws * args.steps / res["mixed"]["sec"]
     fp64_value = ws * args.fp64_steps / res["fp64"]["sec"]
 
+    # the CG variants the timed solves ran (autotuned at the first solve of the handle)
+    used32, used64 = C.c_int32(), C.c_int32()
+    L.check(lib.fg_get_cg_variant(g.h, L.FG_MIXED, C.byref(used32)))
+    L.check(lib.fg_get_cg_variant(g.h, L.FG_FP64, C.byref(used64)))
+
     # roofline: dominant kernel = the FP32 CG SpMV on the converged tangent operator
     peak, peak_kind = measured_peaks()
     nsell, ninc, nsl = C.c_int64(), C.c_int64(), C.c_int32()
@@ -252,17 +257,23 @@ def run_ours(args):
     fg.newton_magnetostatics(mesh, nl, mu_lin, u0, precision="mixed")   # leaves J32 on the handle
     chosen = C.c_int32()
     variants_us = np.zeros(20)
+    # the table of every variant on the converged operator (a second timing); the
+    # per-kernel figures below are for the variant the timed solves used
     L.check(lib.fg_autotune(g.h, L.FG_MIXED, C.byref(chosen), L.ptr(variants_us), 20))
-    autotune = {"cg32_iteration_variants_us": [round(float(v), 2) for v in variants_us], "chosen": int(chosen.value),
+    L.check(lib.fg_set_cg_variant(g.h, L.FG_MIXED, used32.value))
+    autotune = {"cg32_iteration_variants_us": [round(float(v), 2) for v in variants_us],
+                "chosen_on_converged_operator": int(chosen.value), "used_by_timed_solves": int(used32.value) - 1,
+                "used64_by_timed_solves": int(used64.value) - 1,
                 "names": ["fused gather/256", "fused gather-hoist/256", "fused gather/128", "fused gather/512",
                           "fused halo-smem", "fused halo-smem-pipelined", "split gather/256", "split halo-smem",
                           "split gather persistent", "split gather persistent, programmatic launch",
-                          "split gather persistent, values in L2", "split gather persistent 4/SM",
+                          "split gather persistent 6/SM, values in L2 window", "split gather persistent 4/SM",
                           "split gather persistent 3/SM", "split gather persistent 5/SM",
                           "split gather persistent 6/SM", "split gather persistent 7/SM",
                           "split, Jacobi-scaled system, persistent 6/SM",
                           "split, bulk-staged entries, persistent 4/SM", "split, bulk-staged entries, persistent 3/SM",
-                          "split, bulk-staged entries, persistent 2/SM"]}
+                          "split, bulk-staged entries, persistent 2/SM",
+                          "split, Jacobi-scaled system, persistent 6/SM, values in L2 window"]}
     ms_spmv, ms_iter = C.c_double(), C.c_double()
     L.check(lib.fg_bench_kernel(g.h, 0, L.FG_MIXED, 200, C.byref(ms_spmv)))
     L.check(lib.fg_bench_kernel(g.h, 3, L.FG_MIXED, 200, C.byref(ms_iter)))
@@ -275,33 +286,35 @@ def run_ours(args):
     fg.newton_magnetostatics(mesh, nl, mu_lin, u0, precision="fp64")   # leaves J64 on the handle
     ch64, us64 = C.c_int32(), np.zeros(4)
     L.check(lib.fg_autotune(g.h, L.FG_FP64, C.byref(ch64), L.ptr(us64), 4))
+    L.check(lib.fg_set_cg_variant(g.h, L.FG_FP64, used64.value))
     autotune["cg64_spmv_variants_us"] = [round(float(v), 2) for v in us64]
-    autotune["chosen64"] = int(ch64.value)
+    autotune["chosen64_on_converged_operator"] = int(ch64.value)
     for name, which in (("cg64_spmv", 0), ("cg64_update", 1)):
         t = C.c_double()
         L.check(lib.fg_bench_kernel(g.h, which, L.FG_FP64, 200, C.byref(t)))
         kernels_us[name] = t.value * 1e3
     fg.newton_magnetostatics(mesh, nl, mu_lin, u0, precision="mixed")
     n = mesh.nv
-    v = int(chosen.value)
-    if v == 16:
+    v = int(used32.value) - 1
+    if v in (16, 20):
         # scaled system: w = A' r with its dots; value + 16-bit column per stored
-        # nonzero, r read and w written per row (8 B)
-        alg_bytes = g.nnz * 6 + 8 * n
+        # nonzero, r and the diagonal read and w written per row (12 B)
+        alg_bytes = g.nnz * 6 + 12 * n
         kname = "k_cg32s_spmv"
     elif v >= 6:
         # split iteration, dominant kernel w = A u with its dots: FP32 value (4 B) and
         # 16-bit column (2 B) per stored nonzero; per row u and r read, w written
         # (12 B).  Neighbour gathers of u are re-reads.
         alg_bytes = g.nnz * 6 + 12 * n
-        kname = "k_cg32s_spmv_halo" if v == 7 else ("k_cg32s_spmv_bulk" if v >= 17 else "k_cg32s_spmv")
+        kname = {7: "k_cg32s_spmv_halo", 17: "k_cg32s_spmv_bulk", 18: "k_cg32s_spmv_bulk",
+                 19: "k_cg32s_spmv_bulk"}.get(v, "k_cg32s_spmv")
     else:
         # one fused iteration: matrix as above; per row the (r, w, s, dinv) state read
         # and written (16 + 16 B) and p, x read and written (8 + 8 B)
         alg_bytes = g.nnz * 6 + 48 * n
         kname = {4: "k_cg32_iter_halo", 5: "k_cg32_iter_pipe"}.get(v, "k_cg32_iter")
     achieved = alg_bytes / (ms_spmv.value * 1e-3) / 1e9
-    roofline = {"bound": "hbm", "kernel": kname, "variant": autotune["names"][int(chosen.value)],
+    roofline = {"bound": "hbm", "kernel": kname, "variant": autotune["names"][v],
                 "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                 "traffic": args.spmv_traffic, "algorithmic_bytes": alg_bytes, "us_per_launch": ms_spmv.value * 1e3}
@@ -416,6 +429,26 @@ def case_cg_kernel(args):
     _line("CG iteration time (FP32, forced variant)", 1e3 * st["ms"] / max(st["iterations"], 1), "us/iteration",
           False, {"workload": f"K+M of the Kuhn-tet box, {args.cells}^3 cells", "variant": args.variant,
                   "iterations": st["iterations"]}, {})
+
+
+def case_cg_loop(args):
+    """Forced FP32 CG kernel variant on K + M of the workload mesh run as the solver
+    runs it (the whole solve in one graph launch): time per iteration including the
+    loop's own costs, next to the autotuner's replayed-graph time."""
+    import femeko_gpu as fg
+    mesh, nl, mu_lin, u0 = workload(args.cells)
+    K = (fg.stiffnessMatrix(mesh) + fg.massMatrix(mesh)).tocsc()
+    b = np.random.default_rng(1).normal(size=mesh.nv) if args.rhs == "random" else np.ones(mesh.nv)
+    out = {}
+    for rep in range(2):   # the first run builds the handle and the graphs
+        x, st = fg.cg(K, b, reltol=1e-30, maxiter=args.iters, precision="mixed", spmv=args.variant,
+                      inner_rtol=1e-30, use_graph=args.graph_mode, check_every=args.check_every,
+                      return_stats=True)
+        out = {"us_per_iteration": 1e3 * st["ms"] / max(st["iterations"], 1), "iterations": st["iterations"]}
+    _line("CG iteration time in the solve loop (FP32, forced variant)", out["us_per_iteration"], "us/iteration",
+          False, {"workload": f"K+M of the Kuhn-tet box, {args.cells}^3 cells", "variant": args.variant,
+                  "iterations": out["iterations"], "graph_mode": args.graph_mode, "check_every": args.check_every,
+                  "rhs": args.rhs}, {})
 
 
 def case_newton_kernels(args):
@@ -533,7 +566,7 @@ def case_adjoint(args):
            "forward_iters": st["forward_iters"], "adjoint_iters": st["adjoint_iters"]})
 
 
-CASES = {"cg-kernel": case_cg_kernel, "newton-kernels": case_newton_kernels, "heat": case_heat,
+CASES = {"cg-kernel": case_cg_kernel, "cg-loop": case_cg_loop, "newton-kernels": case_newton_kernels, "heat": case_heat,
          "sweep": case_sweep, "batch": case_batch, "adjoint": case_adjoint}
 
 
@@ -558,12 +591,13 @@ def main():
     ap.add_argument("--graph-mode", type=int, default=1, choices=[0, 1, 2],
                     help="1: whole CG in one graph launch (device-side loop); 2: host-checked graph blocks; 0: no graph")
     ap.add_argument("--cg-variant", type=int, default=0,
-                    help="fix the FP32 CG kernel variant (1..20; 0: autotuned), e.g. for profiling runs")
+                    help="fix the FP32 CG kernel variant (1..21; 0: autotuned), e.g. for profiling runs")
     ap.add_argument("--cg64-variant", type=int, default=0, help="fix the FP64 CG SpMV variant (1..4; 0: autotuned)")
     ap.add_argument("--case", choices=sorted(CASES), default=None,
                     help="run a secondary workload instead of the headline benchmark")
     ap.add_argument("--variant", type=int, default=6, help="--case cg-kernel: forced CG kernel variant (1..6)")
     ap.add_argument("--iters", type=int, default=200, help="--case cg-kernel: CG iterations")
+    ap.add_argument("--rhs", choices=["random", "ones"], default="random", help="--case cg-loop: right-hand side")
     args = ap.parse_args()
     if args.fp64_steps is None:
         args.fp64_steps = args.steps

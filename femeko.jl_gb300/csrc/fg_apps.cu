@@ -40,7 +40,8 @@ extern "C" fg_status fg_bench_kernel(fg_mesh *m, int32_t which, int32_t precisio
                                      double *ms_per_launch) {
   return fg_guard([&]() -> fg_status {
     FG_REQUIRE(m && ms_per_launch && reps > 0, FG_BAD_ARG, "fg_bench_kernel: bad argument");
-    if (which == 0 || which == 1 || which == 3) return fg_bench_cg_kernel(m, which, precision, reps, ms_per_launch);
+    if (which == 0 || which == 1 || which == 3 || which == 6)
+      return fg_bench_cg_kernel(m, which, precision, reps, ms_per_launch);
     FG_REQUIRE(which == 2 || which == 4 || which == 5, FG_BAD_ARG, "fg_bench_kernel: unknown kernel");
     FG_REQUIRE(m->v64[7] && m->mu, FG_BAD_ARG, "fg_bench_kernel: run a Newton solve on this handle first");
     FG_REQUIRE(which == 2 || m->nl_maps_valid, FG_BAD_ARG, "fg_bench_kernel: run a Newton solve on this handle first");

@@ -209,8 +209,9 @@ struct fg_mesh {
   GraphCache graph[4];
   int op_tag = 0;            // what val64/val32 hold when a caller reuses them (0: unknown)
   int64_t op_version = 0;    // incremented whenever val64/val32 are rewritten
-  // symmetrically Jacobi-scaled FP32 operator D^-1/2 A D^-1/2 (the scaled CG variant)
-  float *val32s = nullptr, *sdiag32 = nullptr;
+  // symmetrically Jacobi-scaled FP32 operator D^-1/2 A D^-1/2 (the scaled CG variant),
+  // D^-1/2 and D (the weights of the residual norm) per row
+  float *val32s = nullptr, *sdiag32 = nullptr, *diag32 = nullptr;
   int64_t val32s_version = -1;
   uint8_t *inside = nullptr; // nt mask of the magnetic body (demagnetising field)
   double *nodal_in = nullptr;// 3 x nv nodal magnetisation (demagnetising field)
@@ -232,6 +233,7 @@ static inline T *dev_alloc(fg_mesh *m, size_t count) {
   if (m) m->extra.push_back(ptr);
   return static_cast<T *>(ptr);
 }
+
 
 static inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
 

@@ -597,8 +597,9 @@ __global__ void __launch_bounds__(256) k_cg32s_spmv(int64_t n, const int *__rest
                                                     const int *__restrict__ sl_len,
                                                     const typename CI::T *__restrict__ col,
                                                     const float *__restrict__ val, const float *__restrict__ u,
-                                                    const float *__restrict__ r, float *__restrict__ w, double *scal,
-                                                    int *ictl, double *partials, unsigned *counter) {
+                                                    const float *__restrict__ r, const float *__restrict__ rw,
+                                                    float *__restrict__ w, double *scal, int *ictl,
+                                                    double *partials, unsigned *counter) {
   griddep_wait();
   griddep_release();
   // the done flag is loaded together with the first row's metadata: its latency
@@ -637,7 +638,8 @@ __global__ void __launch_bounds__(256) k_cg32s_spmv(int64_t n, const int *__rest
     const float ui = u[i], ri = r[i];
     dots[0].add(ri * ui);
     dots[1].add(acc * ui);
-    dots[2].add(ri * ri);
+    // rw (the scaled system): r.r of the unscaled residual, sum of D_ii r'_i^2
+    dots[2].add(rw ? ri * ri * __ldg(rw + i) : ri * ri);
   }
   }
   double part[3];
@@ -814,10 +816,15 @@ __global__ void __launch_bounds__(256) k_cg32s_spmv_bulk(int64_t n, int nslices,
 // variant): A' = S A S with S = D^-1/2 (sdiag = sqrt of the Jacobi inverse, 0 on
 // Dirichlet rows), b' = S b, x = S y.  The iterates are those of Jacobi-PCG; the
 // preconditioned residual u = r' needs no vector of its own, and the stopping test
-// measures |r'| = |S r| (the preconditioned residual norm).
-__global__ void k_sdiag32(int64_t np, const float *__restrict__ dinv, float *__restrict__ sdiag) {
+// measures the unscaled residual |r| = |S^-1 r'| (r.r = sum D_ii r'_i^2), as
+// Jacobi-PCG does.
+__global__ void k_sdiag32(int64_t np, const float *__restrict__ dinv, float *__restrict__ sdiag,
+                          float *__restrict__ diag) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < np) sdiag[i] = sqrtf(dinv[i]);
+  if (i >= np) return;
+  const float d = dinv[i];
+  sdiag[i] = sqrtf(d);
+  diag[i] = (d > 0.f) ? 1.f / d : 0.f;  // D_ii, the weight of r'_i^2 in the unscaled r.r
 }
 
 template <class CI>
@@ -1245,7 +1252,7 @@ static void ensure_cg64(fg_mesh *m) {
 // programmatic dependent launch, 10 the same with the matrix values held in L2,
 // 11-15 persistent grids of 4, 3, 5, 6 and 7 blocks per SM, 16 CG on the
 // symmetrically Jacobi-scaled system with the SpMV of variant 14
-constexpr int FG_N_SPMV32 = 20;
+constexpr int FG_N_SPMV32 = 21;
 static inline bool split32(int v) { return v >= 6; }
 constexpr int FG_N_SPMV64 = 4;   // 0 direct gathers, 1 halo staging, 2/3 persistent with 4/8 blocks per SM
 
@@ -1397,6 +1404,8 @@ static bool prepare_l2(fg_mesh *m) {
     m->l2_win_bytes = -1;
     return false;
   }
+  // the values only: a set-aside for values and columns (81 MB of the 135 MB L2 at
+  // 96^3) left too little L2 for everything else and was slower
   const size_t want = sizeof(float) * (size_t)m->nsell;
   std::lock_guard<std::mutex> g(g_l2_lock);
   const size_t setaside = std::min(want, (size_t)max_persist);
@@ -1408,6 +1417,15 @@ static bool prepare_l2(fg_mesh *m) {
   m->l2_win_bytes = (int64_t)std::min(want, (size_t)max_win);
   m->l2_hit_ratio = (float)std::min(1.0, (double)g_l2_setaside[m->device] / (double)m->l2_win_bytes);
   return true;
+}
+
+// Returns every line the process's context holds as persisting to normal, so that
+// a timing does not profit from lines an earlier variant's L2 window left behind.
+static void reset_persisting_l2(fg_mesh *m) {
+  std::lock_guard<std::mutex> g(g_l2_lock);
+  if (m->device < 0 || m->device >= 64 || g_l2_setaside[m->device] == 0) return;
+  cudaCtxResetPersistingL2Cache();
+  cudaGetLastError();
 }
 
 void fg_release_l2(fg_mesh *m) {
@@ -1422,15 +1440,17 @@ void fg_release_l2(fg_mesh *m) {
   m->l2_win_bytes = 0;
 }
 
+// A launch whose accesses to the window [win, win + l2_win_bytes) persist in L2.
 template <typename... KArgs, typename... Args>
-static void l2_launch(fg_mesh *m, void (*kern)(KArgs...), unsigned grid, unsigned block, Args... args) {
+static void l2_launch(fg_mesh *m, const float *win, void (*kern)(KArgs...), unsigned grid, unsigned block,
+                      Args... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(block);
   cfg.stream = m->stream;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeAccessPolicyWindow;
-  attr[0].val.accessPolicyWindow.base_ptr = (void *)m->val32;
+  attr[0].val.accessPolicyWindow.base_ptr = (void *)win;
   attr[0].val.accessPolicyWindow.num_bytes = (size_t)m->l2_win_bytes;
   attr[0].val.accessPolicyWindow.hitRatio = m->l2_hit_ratio;
   attr[0].val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
@@ -1445,10 +1465,12 @@ static void ensure_scaled(fg_mesh *m) {
   if (!m->val32s) m->val32s = dev_alloc<float>(m, (size_t)m->nsell);
   if (!m->sdiag32) {
     m->sdiag32 = dev_alloc<float>(m, (size_t)m->nvp);
+    m->diag32 = dev_alloc<float>(m, (size_t)m->nvp);
     FG_CUDA_TRY(cudaMemsetAsync(m->sdiag32, 0, sizeof(float) * (size_t)m->nvp, m->stream));
+    FG_CUDA_TRY(cudaMemsetAsync(m->diag32, 0, sizeof(float) * (size_t)m->nvp, m->stream));
   }
   if (m->val32s_version == m->op_version) return;
-  k_sdiag32<<<grid_for(m->nvp, 256), 256, 0, m->stream>>>(m->nvp, m->dinv32, m->sdiag32);
+  k_sdiag32<<<grid_for(m->nvp, 256), 256, 0, m->stream>>>(m->nvp, m->dinv32, m->sdiag32, m->diag32);
   if (m->use_dcol)
     k_scale_op32<ColRel><<<grid_for(m->nv, 256), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_dcol,
                                                                       m->val32, m->sdiag32, m->val32s);
@@ -1523,27 +1545,44 @@ static void bulk_launch32(fg_mesh *m, int v) {
 
 static void launch_spmv32s(fg_mesh *m, int v) {
   const bool pdl = (v == 9);
-  if (v == 16) {
-    // w = A' r' with the dots r'.r', w.r', r'.r' (u = r' on the scaled system)
+  if (v == 20 && m->l2_win_bytes > 0) {
+    // the scaled system (16) with its values in the L2 window
+    const unsigned g = std::min<unsigned>(grid_for(m->nv, 256), 6u * (unsigned)std::max(m->sm_count, 1));
+    if (m->use_dcol)
+      l2_launch(m, m->val32s, k_cg32s_spmv<ColRel, true>, g, 256, m->nv, m->sl_ptr, m->sl_len, m->sl_dcol,
+                m->val32s, m->v32[4], m->v32[4], m->diag32, m->v32[5], m->scal, m->ictl, m->red.partials,
+                m->red.counter);
+    else
+      l2_launch(m, m->val32s, k_cg32s_spmv<ColAbs, true>, g, 256, m->nv, m->sl_ptr, m->sl_len, m->sl_col,
+                m->val32s, m->v32[4], m->v32[4], m->diag32, m->v32[5], m->scal, m->ictl, m->red.partials,
+                m->red.counter);
+    return;
+  }
+  if (v == 16 || v == 20) {
+    // w = A' r' with the dots r'.r', w.r' and r.r = sum D_ii r'_i^2 (u = r' on the scaled
+    // system; the stopping test is on the unscaled residual, as in Jacobi-PCG)
     const unsigned g = std::min<unsigned>(grid_for(m->nv, 256), 6u * (unsigned)std::max(m->sm_count, 1));
     if (m->use_dcol)
       k_cg32s_spmv<ColRel, true><<<g, 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, m->val32s,
-                                                           m->v32[4], m->v32[4], m->v32[5], m->scal, m->ictl,
-                                                           m->red.partials, m->red.counter);
+                                                           m->v32[4], m->v32[4], m->diag32, m->v32[5], m->scal,
+                                                           m->ictl, m->red.partials, m->red.counter);
     else
       k_cg32s_spmv<ColAbs, true><<<g, 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val32s,
-                                                           m->v32[4], m->v32[4], m->v32[5], m->scal, m->ictl,
-                                                           m->red.partials, m->red.counter);
+                                                           m->v32[4], m->v32[4], m->diag32, m->v32[5], m->scal,
+                                                           m->ictl, m->red.partials, m->red.counter);
     return;
   }
   if (v == 10 && m->l2_win_bytes > 0) {
-    const unsigned g = std::min<unsigned>(grid_for(m->nv, 256), 8u * (unsigned)std::max(m->sm_count, 1));
+    // the persistent grid of 14 (6 blocks per SM) with the values in the L2 window
+    const unsigned g = std::min<unsigned>(grid_for(m->nv, 256), 6u * (unsigned)std::max(m->sm_count, 1));
     if (m->use_dcol)
-      l2_launch(m, k_cg32s_spmv<ColRel, true>, g, 256, m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, m->val32,
-                m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl, m->red.partials, m->red.counter);
+      l2_launch(m, m->val32, k_cg32s_spmv<ColRel, true>, g, 256, m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, m->val32,
+                m->v32[7], m->v32[4], (const float *)nullptr, m->v32[5], m->scal, m->ictl, m->red.partials,
+                m->red.counter);
     else
-      l2_launch(m, k_cg32s_spmv<ColAbs, true>, g, 256, m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val32,
-                m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl, m->red.partials, m->red.counter);
+      l2_launch(m, m->val32, k_cg32s_spmv<ColAbs, true>, g, 256, m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val32,
+                m->v32[7], m->v32[4], (const float *)nullptr, m->v32[5], m->scal, m->ictl, m->red.partials,
+                m->red.counter);
     return;
   }
   if (v >= 17) {
@@ -1557,10 +1596,12 @@ static void launch_spmv32s(fg_mesh *m, int v) {
     const unsigned g = std::min<unsigned>(grid_for(m->nv, 256), per_sm * (unsigned)std::max(m->sm_count, 1));
     if (m->use_dcol)
       pdl_launch(pdl, k_cg32s_spmv<ColRel, true>, g, 256, 0, m->stream, m->nv, m->sl_ptr, m->sl_len, m->sl_dcol,
-                 m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl, m->red.partials, m->red.counter);
+                 m->val32, m->v32[7], m->v32[4], (const float *)nullptr, m->v32[5], m->scal, m->ictl,
+                 m->red.partials, m->red.counter);
     else
       pdl_launch(pdl, k_cg32s_spmv<ColAbs, true>, g, 256, 0, m->stream, m->nv, m->sl_ptr, m->sl_len, m->sl_col,
-                 m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl, m->red.partials, m->red.counter);
+                 m->val32, m->v32[7], m->v32[4], (const float *)nullptr, m->v32[5], m->scal, m->ictl,
+                 m->red.partials, m->red.counter);
   } else if (v == 7 && m->halo_col)
     halo_launch<Spmv32sHalo>(m, sizeof(float), m->nv, (const int *)m->sl_ptr, (const int *)m->sl_len,
                              (const uint16_t *)m->sl_lcol, (const float *)m->val32, (const int *)m->halo_col,
@@ -1568,16 +1609,16 @@ static void launch_spmv32s(fg_mesh *m, int v) {
                              m->v32[5], m->scal, m->ictl, m->red.partials, m->red.counter);
   else if (m->use_dcol)
     pdl_launch(false, k_cg32s_spmv<ColRel, false>, grid_for(m->nv, 256), 256, 0, m->stream, m->nv, m->sl_ptr,
-               m->sl_len, m->sl_dcol, m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl, m->red.partials,
-               m->red.counter);
+               m->sl_len, m->sl_dcol, m->val32, m->v32[7], m->v32[4], (const float *)nullptr, m->v32[5], m->scal,
+               m->ictl, m->red.partials, m->red.counter);
   else
     pdl_launch(false, k_cg32s_spmv<ColAbs, false>, grid_for(m->nv, 256), 256, 0, m->stream, m->nv, m->sl_ptr,
-               m->sl_len, m->sl_col, m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl, m->red.partials,
-               m->red.counter);
+               m->sl_len, m->sl_col, m->val32, m->v32[7], m->v32[4], (const float *)nullptr, m->v32[5], m->scal,
+               m->ictl, m->red.partials, m->red.counter);
 }
 
 static void launch_vec32s(fg_mesh *m, int v) {
-  if (v == 16) {
+  if (v == 16 || v == 20) {
     k_cg32ss_vec<<<grid_for(m->nvp / 4, 256), 256, 0, m->stream>>>(
         m->nvp / 4, reinterpret_cast<float4 *>(m->v32[4]), reinterpret_cast<const float4 *>(m->v32[5]),
         reinterpret_cast<float4 *>(m->v32[6]), reinterpret_cast<float4 *>(m->v32[1]),
@@ -1650,11 +1691,11 @@ static void launch_vec64(fg_mesh *m) {
 // buffer 0 -> 1, so the iteration blocks start reading buffer 1.
 static void start_cg(fg_mesh *m, bool mixed, const double *r64, double scale, double tol2_rel, int maxit) {
   const unsigned g = red_grid(m->nvp);
-  if (mixed && m->spmv_variant32 == 16) {
+  if (mixed && (m->spmv_variant32 == 16 || m->spmv_variant32 == 20)) {
     ensure_scaled(m);
     k_cg32ss_init<<<g, 256, 0, m->stream>>>(m->nv, m->nvp, r64, scale, m->sdiag32, m->v32[4], m->v32[6], m->v32[1],
                                             m->v32[0], tol2_rel, maxit, m->scal, m->ictl);
-    launch_spmv32s(m, 16);
+    launch_spmv32s(m, m->spmv_variant32);
   } else if (mixed && split32(m->spmv_variant32)) {
     k_cg32s_init<<<g, 256, 0, m->stream>>>(m->nv, m->nvp, r64, scale, m->dinv32, m->v32[4], m->v32[7], m->v32[6],
                                            m->v32[1], m->v32[0], tol2_rel, maxit, m->scal, m->ictl);
@@ -1743,14 +1784,16 @@ static bool capture_iterations(fg_mesh *m, GraphCache &gc, int body, bool loop, 
 // runs the whole solve; where that graph cannot be built (launch attributes the
 // conditional body does not take), and with use_graph 2, blocks of check_every
 // iterations are replayed with a host check of the done flag between them.
-static int run_cg(fg_mesh *m, bool mixed, const fg_solve_opts &o, int *status) {
+// loop_ms (may be null): device time from the first launch to the end of the last
+// one, host checks included (the autotuner's measure of a variant).
+static int run_cg(fg_mesh *m, bool mixed, const fg_solve_opts &o, int *status, float *loop_ms = nullptr) {
   int block = o.check_every > 0 ? o.check_every : 32;
   if (block & 1) ++block;
   const int per_iter = (mixed && !split32(m->spmv_variant32)) ? 1 : 2;
   GraphCache &gc = m->graph[mixed ? 1 : 0];
   const bool use_graph = o.use_graph != 0;
-  // PDL and L2-window launches keep the host-checked blocks
-  const bool want_loop = o.use_graph == 1 && !(mixed && (m->spmv_variant32 == 9 || m->spmv_variant32 == 10));
+  // programmatic-launch edges keep the host-checked blocks
+  const bool want_loop = o.use_graph == 1 && !(mixed && m->spmv_variant32 == 9);
   const int body = block;
   const void *key[5] = {mixed ? (const void *)m->val32 : (const void *)m->val64,
                         mixed ? (const void *)(intptr_t)(m->spmv_variant32 + 1) : (const void *)m->v64[0],
@@ -1778,9 +1821,11 @@ static int run_cg(fg_mesh *m, bool mixed, const fg_solve_opts &o, int *status) {
   }
   // the whole solve in one launch (bodies of an even number of iterations keep the
   // fused variants' state buffers in step); launches are counted from the bodies run
+  if (loop_ms) FG_CUDA_TRY(cudaEventRecord(m->ev0, m->stream));
   if (loop) FG_CUDA_TRY(cudaGraphLaunch(gc.exec, m->stream));
   int bodies = 0;
   for (;;) {
+    if (loop_ms) FG_CUDA_TRY(cudaEventRecord(m->ev1, m->stream));
     FG_CUDA_TRY(cudaMemcpyAsync(m->hint, m->ictl, sizeof(int) * (I_BODIES + 1), cudaMemcpyDeviceToHost,
                                 m->stream));
     fg_sync(m);
@@ -1799,7 +1844,28 @@ static int run_cg(fg_mesh *m, bool mixed, const fg_solve_opts &o, int *status) {
     if (!loop) FG_LAUNCHED((long long)per_iter * block);
   }
   if (status) *status = m->hint[I_STATUS];
+  if (loop_ms) FG_CUDA_TRY(cudaEventElapsedTime(loop_ms, m->ev0, m->ev1));
   return std::max(m->hint[I_ITERS], 0);
+}
+
+// Microseconds per iteration of the handle's current variant run the way the solver
+// runs it (start_cg, then run_cg with default options: the whole-solve graph where it
+// can be built), over `reps` iterations after an untimed run that builds the graph.
+static double loop_us_per_iteration(fg_mesh *m, bool mixed, int reps) {
+  fg_solve_opts o;
+  fg_solve_opts_default(&o);
+  if (!m->v64[5]) m->v64[5] = dev_alloc<double>(m, (size_t)m->nvp);
+  k_fill64<<<red_grid(m->nv), 256, 0, m->stream>>>(m->nv, 1.0, m->v64[5]);
+  FG_LAUNCHED(1);
+  if (mixed) ensure_cg32(m);
+  else ensure_cg64(m);
+  float ms = 0.f;
+  int its = 0;
+  for (int pass = 0; pass < 2; ++pass) {
+    start_cg(m, mixed, m->v64[5], 1.0, 0.0, reps);
+    its = run_cg(m, mixed, o, nullptr, pass == 1 ? &ms : nullptr);
+  }
+  return 1e3 * (double)ms / std::max(its, 1);
 }
 
 fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_variant);
@@ -1843,17 +1909,19 @@ static int inner_solve(fg_mesh *m, bool mixed, const double *r64, double rn, dou
       // large for shared memory) falls back to the plain gather kernel
       const int v = o.spmv - 1;
       const bool avail = v < 4 || v == 6 || v == 8 || v == 9 || (v >= 11 && v < 17) ||
-                         (v >= 17 && bulk_per_sm(m, v) > 0) || (v == 10 && prepare_l2(m)) ||
+                         (v >= 17 && v < 20 && bulk_per_sm(m, v) > 0) ||
+                         ((v == 10 || v == 20) && prepare_l2(m)) ||
                          ((v == 4 || v == 7) && m->halo_col) || (v == 5 && pipe_available(m));
       m->spmv_variant32 = avail ? v : 0;
     } else if (!m->tuned32 && !tune_cache_get(m, true)) {
       fg_autotune_spmv32(m, 20, nullptr, nullptr);
       tune_cache_put(m, true);
     }
-    if (m->spmv_variant32 == 10 && !prepare_l2(m)) m->spmv_variant32 = 8;
+    if (m->spmv_variant32 == 10 && !prepare_l2(m)) m->spmv_variant32 = 14;
+    if (m->spmv_variant32 == 20 && !prepare_l2(m)) m->spmv_variant32 = 16;
     start_cg(m, true, r64, 1.0 / rn, inner * inner, maxit);
     its = run_cg(m, true, o, ist);
-    if (m->spmv_variant32 == 16)
+    if (m->spmv_variant32 == 16 || m->spmv_variant32 == 20)
       k_axpy_scaled_to64<<<grid_for(m->nv, 256), 256, 0, m->stream>>>(m->nv, rn, m->sdiag32, m->v32[0], d_x);
     else
       k_axpy_to64<float><<<red_grid(m->nv), 256, 0, m->stream>>>(m->nv, rn, m->v32[0], d_x);
@@ -2099,6 +2167,11 @@ static void timing_state(fg_mesh *m, bool mixed) {
 fg_status fg_bench_cg_kernel(fg_mesh *m, int which, int precision, int reps, double *ms_per_launch) {
   const bool mixed = precision == FG_MIXED;
   FG_REQUIRE(mixed ? m->val32 != nullptr : m->val64 != nullptr, FG_BAD_ARG, "operator not assembled");
+  if (which == 6) {
+    // whole iterations the way the solver runs them (its graph loop), reps of them
+    *ms_per_launch = 1e-3 * loop_us_per_iteration(m, mixed, std::max(reps, 2));
+    return FG_OK;
+  }
   timing_state(m, mixed);
   const int v = m->spmv_variant32;
   auto body = [&](int n) {
@@ -2124,43 +2197,25 @@ fg_status fg_bench_cg_kernel(fg_mesh *m, int which, int precision, int reps, dou
   return FG_OK;
 }
 
-// Autotuner: times every FP32 CG iteration variant (block size x load scheduling) on
-// the handle's current operator with CUDA events and keeps the fastest for the
-// handle.  Runs once per handle at its first mixed-precision solve (or on request).
+// Autotuner: times every FP32 CG iteration variant on the handle's current operator,
+// each run as the solver runs it (CUDA events around its graph loop), and keeps the
+// fastest for the handle.  Runs at the first mixed-precision solve of an operator
+// shape (or on request).
 fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_variant) {
   FG_REQUIRE(m->val32 != nullptr, FG_BAD_ARG, "autotune: no FP32 operator assembled");
-  reps = std::max(2, reps & ~1);
+  reps = std::max(64, (reps + 31) / 32 * 32);  // whole bodies of the solver's graph loop
   int best = 0;
   double best_us = 1e30;
   for (int v = 0; v < FG_N_SPMV32; ++v) {
     if (((v == 4 || v == 7) && !m->halo_col) || (v == 5 && !pipe_available(m)) ||
-        (v == 10 && !prepare_l2(m)) || (v >= 17 && bulk_per_sm(m, v) == 0)) {  // not available here
+        ((v == 10 || v == 20) && !prepare_l2(m)) || (v >= 17 && v < 20 && bulk_per_sm(m, v) == 0)) {
       if (us_per_variant) us_per_variant[v] = 0.0;
       continue;
     }
     m->spmv_variant32 = v;
-    timing_state(m, true);
-    for (int r = 0; r < 2; ++r) launch_iter32(m, v, r == 1);
-    // timed as the solver runs them: a CUDA graph of reps iterations, replayed
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    FG_CUDA_TRY(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
-    for (int r = 0; r < reps; ++r) launch_iter32(m, v, r & 1);
-    FG_CUDA_TRY(cudaStreamEndCapture(m->stream, &graph));
-    cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
-    cudaGraphDestroy(graph);
-    FG_CUDA_TRY(ie);
-    float ms = 0.f;
-    cudaError_t le = cudaGraphLaunch(exec, m->stream);
-    if (le == cudaSuccess) le = cudaEventRecord(m->ev0, m->stream);
-    if (le == cudaSuccess) le = cudaGraphLaunch(exec, m->stream);
-    if (le == cudaSuccess) le = cudaEventRecord(m->ev1, m->stream);
-    if (le == cudaSuccess) le = cudaStreamSynchronize(m->stream);
-    if (le == cudaSuccess) le = cudaEventElapsedTime(&ms, m->ev0, m->ev1);
-    cudaGraphExecDestroy(exec);
-    FG_CUDA_TRY(le);
-    FG_LAUNCHED(2LL * reps * (split32(v) ? 2 : 1) + 2);
-    const double us = 1e3 * ms / reps;
+    // timed as the solver runs them, from an L2 without persisting lines
+    reset_persisting_l2(m);
+    const double us = loop_us_per_iteration(m, true, reps);
     if (us_per_variant) us_per_variant[v] = us;
     if (us < best_us) { best_us = us; best = v; }
   }
@@ -2174,7 +2229,7 @@ fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_v
 // persistent grid of 4 or 8 blocks per SM), timed per whole iteration.
 fg_status fg_autotune_spmv64(fg_mesh *m, int reps, int *chosen, double *us_per_variant) {
   FG_REQUIRE(m->val64 != nullptr, FG_BAD_ARG, "autotune: no FP64 operator assembled");
-  reps = std::max(2, reps);
+  reps = std::max(64, (reps + 31) / 32 * 32);
   int best = 0;
   double best_us = 1e30;
   for (int v = 0; v < FG_N_SPMV64; ++v) {
@@ -2183,29 +2238,8 @@ fg_status fg_autotune_spmv64(fg_mesh *m, int reps, int *chosen, double *us_per_v
       continue;
     }
     m->spmv_variant64 = v;
-    timing_state(m, false);
-    launch_vec64(m);
-    launch_spmv64cg(m);
-    // timed as the solver runs them: a CUDA graph of reps whole iterations, replayed
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    FG_CUDA_TRY(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
-    for (int r = 0; r < reps; ++r) { launch_vec64(m); launch_spmv64cg(m); }
-    FG_CUDA_TRY(cudaStreamEndCapture(m->stream, &graph));
-    cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
-    cudaGraphDestroy(graph);
-    FG_CUDA_TRY(ie);
-    float ms = 0.f;
-    cudaError_t le = cudaGraphLaunch(exec, m->stream);
-    if (le == cudaSuccess) le = cudaEventRecord(m->ev0, m->stream);
-    if (le == cudaSuccess) le = cudaGraphLaunch(exec, m->stream);
-    if (le == cudaSuccess) le = cudaEventRecord(m->ev1, m->stream);
-    if (le == cudaSuccess) le = cudaStreamSynchronize(m->stream);
-    if (le == cudaSuccess) le = cudaEventElapsedTime(&ms, m->ev0, m->ev1);
-    cudaGraphExecDestroy(exec);
-    FG_CUDA_TRY(le);
-    FG_LAUNCHED(4LL * reps + 2);
-    const double us = 1e3 * ms / reps;
+    // timed as the solver runs them
+    const double us = loop_us_per_iteration(m, false, reps);
     if (us_per_variant) us_per_variant[v] = us;
     if (us < best_us) { best_us = us; best = v; }
   }
@@ -2224,7 +2258,8 @@ extern "C" fg_status fg_set_cg_variant(fg_mesh *m, int32_t precision, int32_t va
       if (variant == 0) { m->tuned32 = false; return FG_OK; }
       const int v = variant - 1;
       const bool avail = v < 4 || v == 6 || v == 8 || v == 9 || (v >= 11 && v < 17) ||
-                         (v >= 17 && bulk_per_sm(m, v) > 0) || (v == 10 && prepare_l2(m)) ||
+                         (v >= 17 && v < 20 && bulk_per_sm(m, v) > 0) ||
+                         ((v == 10 || v == 20) && prepare_l2(m)) ||
                          ((v == 4 || v == 7) && m->halo_col) || (v == 5 && pipe_available(m));
       FG_REQUIRE(avail, FG_UNSUPPORTED, "fg_set_cg_variant: variant not available for this operator");
       m->spmv_variant32 = v;
@@ -2236,6 +2271,16 @@ extern "C" fg_status fg_set_cg_variant(fg_mesh *m, int32_t precision, int32_t va
       m->spmv_variant64 = variant - 1;
       m->tuned64 = true;
     }
+    return FG_OK;
+  });
+}
+
+extern "C" fg_status fg_get_cg_variant(const fg_mesh *m, int32_t precision, int32_t *variant) {
+  return fg_guard([&]() -> fg_status {
+    FG_REQUIRE(m != nullptr && variant != nullptr, FG_BAD_ARG, "fg_get_cg_variant: null argument");
+    const bool mixed = precision == FG_MIXED;
+    const bool tuned = mixed ? m->tuned32 : m->tuned64;
+    *variant = tuned ? 1 + (mixed ? m->spmv_variant32 : m->spmv_variant64) : 0;
     return FG_OK;
   });
 }

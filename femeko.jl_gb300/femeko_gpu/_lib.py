@@ -106,6 +106,7 @@ SIGNATURES = {
     "fg_mesh_layout": [_vp, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i32)],
     "fg_autotune": [_vp, _i32, C.POINTER(_i32), _vp, _i32],
     "fg_set_cg_variant": [_vp, _i32, _i32],
+    "fg_get_cg_variant": [_vp, _i32, C.POINTER(_i32)],
 }
 VOID_FUNCS = {"fg_solve_opts_default": [C.POINTER(SolveOpts)], "fg_newton_opts_default": [C.POINTER(NewtonOpts)]}
 

@@ -52,7 +52,7 @@ enum {
                           of |F(u + a du)|^2, kept in [0.1, 0.5] of the last step */
 };
 /* FP32 CG iteration kernel: FG_SPMV_AUTO lets the autotuner time the variants on
- * the first mixed solve of a handle and keep the fastest; k = 1..20 forces variant
+ * the first mixed solve of a handle and keep the fastest; k = 1..21 forces variant
  * k-1.  One fused kernel per iteration: 1: 4x-unrolled gather loop, 256 threads;
  * 2: all row loads issued first, 256 threads; 3: loop, 128 threads; 4: loop, 512
  * threads; 5: halo staging (the neighbour entries of a block of rows gathered once
@@ -60,17 +60,18 @@ enum {
  * copies and asynchronous gathers of the next row blocks).  Two kernels per
  * iteration (vector pass + SpMV): 7: direct gathers; 8: halo staging; 9: direct
  * gathers in a persistent grid (each block walks several row blocks); 10: 9 with
- * programmatic dependent launch between the two kernels; 11: 9 with the matrix
+ * programmatic dependent launch between the two kernels; 11: 15 with the matrix
  * values kept in a persisting-L2 window (the process's context sets aside L2 for
  * them while a handle uses this variant); 12-16: 9 with 4, 3, 5, 6 and 7 blocks per
  * SM; 17: plain CG on the symmetrically Jacobi-scaled system D^-1/2 A D^-1/2 (the
- * same iterates as Jacobi-PCG, no preconditioned-residual vector, stopping test on
- * the preconditioned residual norm) with the SpMV of 15; 18-20: 9 with 4, 3 and 2
+ * same iterates as Jacobi-PCG, no preconditioned-residual vector, the same stopping
+ * test on the unscaled residual) with the SpMV of 15; 18-20: 9 with 4, 3 and 2
  * blocks per SM and the matrix entries of each block's next 256 rows copied into a
  * second shared-memory stage by the bulk-copy engine while it computes the current
- * ones (available where two stages fit in shared memory).
- * The autotuner times each variant as a replayed CUDA graph of iterations, the way
- * the solver runs them. */
+ * ones (available where two stages fit in shared memory); 21: 17 with its scaled
+ * values in the persisting-L2 window.
+ * The autotuner times each variant through the solver's own graph loop (64
+ * iterations after an untimed run). */
 enum { FG_SPMV_AUTO = 0 };
 
 typedef struct fg_mesh fg_mesh;
@@ -84,7 +85,7 @@ typedef struct fg_solve_opts {
   int32_t use_graph;   /* 1: the whole CG as one CUDA graph launch (a WHILE node around
                           check_every iterations, the test on the device); 2: a graph of
                           check_every iterations per launch, tested on the host; 0: no graph */
-  int32_t spmv;        /* FG_SPMV_AUTO or a forced variant 1..20 */
+  int32_t spmv;        /* FG_SPMV_AUTO or a forced variant 1..21 */
   int32_t reserved_;
 } fg_solve_opts;
 
@@ -337,7 +338,9 @@ int64_t fg_kernel_launches(void);
  * operator: which = 0 CG SpMV with its dot products (for the fused FP32 iteration
  * variants: the whole iteration), 1 CG vector update, 2 Newton element pass + row
  * gather over all elements, 3 one whole CG iteration, 4 Newton residual on the
- * linear/nonlinear split, 5 the same with the Jacobian (4, 5: after a Newton solve).
+ * linear/nonlinear split, 5 the same with the Jacobian (4, 5: after a Newton solve),
+ * 6 one whole CG iteration run the way the solver runs it (its graph loop; reps
+ * iterations after an untimed run).
  * No reference counterpart (used for roofline reporting). */
 fg_status fg_bench_kernel(fg_mesh *m, int32_t which, int32_t precision, int32_t reps, double *ms_per_launch);
 /* Autotuner: times the CG kernel variants of one precision on the handle's current
@@ -348,12 +351,15 @@ fg_status fg_bench_kernel(fg_mesh *m, int32_t which, int32_t precision, int32_t 
  * be NULL) the measured microseconds per launch.  No reference counterpart. */
 fg_status fg_autotune(fg_mesh *m, int32_t precision, int32_t *variant, double *us_per_variant, int32_t n_slots);
 /* Fixes the CG kernel variant of one precision for the handle (the numbering of
- * fg_solve_opts.spmv: FG_MIXED 1..20, FG_FP64 1..4), or 0 to return to the
+ * fg_solve_opts.spmv: FG_MIXED 1..21, FG_FP64 1..4), or 0 to return to the
  * autotuner's choice at the next solve.  The autotuner's choices are remembered per
  * process for each operator shape (device, rows, padded entries, longest row), so a
  * new handle for a mesh of the same structure does not time the variants again.
  * No reference counterpart (profiling and tuning control). */
 fg_status fg_set_cg_variant(fg_mesh *m, int32_t precision, int32_t variant);
+/* The CG kernel variant the handle's solves of one precision use (numbering of
+ * fg_set_cg_variant), 0 while none is chosen yet.  No reference counterpart. */
+fg_status fg_get_cg_variant(const fg_mesh *m, int32_t precision, int32_t *variant);
 /* Padded sizes of the device layouts: SELL-32 matrix entries, incidence records, slices. */
 fg_status fg_mesh_layout(const fg_mesh *m, int64_t *nsell, int64_t *ninc, int32_t *nslices);
 
