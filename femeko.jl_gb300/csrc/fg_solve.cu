@@ -591,7 +591,10 @@ __global__ void __launch_bounds__(256) k_cg32s_vec(int64_t n4, float4 *__restric
 }
 
 // PERSIST: a grid of at most the resident blocks walks the 256-row blocks with a
-// grid stride, so each block reduces and arrives once for several row blocks.
+// grid stride, so each block reduces and arrives once for several row blocks.  At
+// any moment all blocks work on neighbouring rows and gather the same stretch of u
+// (contiguous row ranges per block, which spread the gathers over the whole vector,
+// measured 41 us per iteration against 36 us at 96^3).
 template <class CI, bool PERSIST>
 __global__ void __launch_bounds__(256) k_cg32s_spmv(int64_t n, const int *__restrict__ sl_ptr,
                                                     const int *__restrict__ sl_len,
@@ -1382,28 +1385,41 @@ static void pdl_launch(bool pdl, void (*kern)(KArgs...), unsigned grid, unsigned
   FG_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...));
 }
 
-// L2 residency of the FP32 matrix values (variant 10): an access-policy window on
-// the SpMV launches marks the values persisting in a set-aside part of L2, so that
-// the ~100 iterations of an inner solve read them from L2 instead of HBM.  The
-// set-aside is a limit of this process's context, sized once per device to the
-// largest operator seen and released when the last handle using it is destroyed.
+// L2 residency of the FP32 matrix values (variants 10 and 20): an access-policy
+// window on the SpMV launches marks the values persisting in a set-aside part of L2,
+// so that the iterations of an inner solve read them from L2 instead of HBM.  The
+// set-aside is a limit of this process's context.  It exists only while a solve with
+// such a variant runs: every other solve (FP64, or FP32 without the window) first
+// returns the whole L2 to normal use (l2_for_solve), and the last handle destroyed
+// releases it for good.
 namespace {
 std::mutex g_l2_lock;
 size_t g_l2_setaside[64] = {0};
 int g_l2_users[64] = {0};
 }  // namespace
 
-static bool prepare_l2(fg_mesh *m) {
-  if (m->l2_win_bytes > 0) return true;
-  if (m->l2_win_bytes < 0 || !m->val32 || m->device < 0 || m->device >= 64) return false;
+// Whether the device offers persisting L2 lines and access-policy windows.
+static bool l2_supported(fg_mesh *m) {
+  if (m->device < 0 || m->device >= 64) return false;
   int max_persist = 0, max_win = 0;
   if (cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, m->device) != cudaSuccess ||
-      cudaDeviceGetAttribute(&max_win, cudaDevAttrMaxAccessPolicyWindowSize, m->device) != cudaSuccess ||
-      max_persist <= 0 || max_win <= 0) {
+      cudaDeviceGetAttribute(&max_win, cudaDevAttrMaxAccessPolicyWindowSize, m->device) != cudaSuccess) {
     cudaGetLastError();
+    return false;
+  }
+  return max_persist > 0 && max_win > 0;
+}
+
+// Sizes the window over the FP32 values and makes sure the set-aside is in place.
+static bool prepare_l2(fg_mesh *m) {
+  if (m->l2_win_bytes < 0 || !m->val32) return false;
+  if (!l2_supported(m)) {
     m->l2_win_bytes = -1;
     return false;
   }
+  int max_persist = 0, max_win = 0;
+  cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, m->device);
+  cudaDeviceGetAttribute(&max_win, cudaDevAttrMaxAccessPolicyWindowSize, m->device);
   // the values only: a set-aside for values and columns (81 MB of the 135 MB L2 at
   // 96^3) left too little L2 for everything else and was slower
   const size_t want = sizeof(float) * (size_t)m->nsell;
@@ -1413,10 +1429,24 @@ static bool prepare_l2(fg_mesh *m) {
     FG_CUDA_TRY(cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, setaside));
     g_l2_setaside[m->device] = setaside;
   }
-  ++g_l2_users[m->device];
+  if (m->l2_win_bytes == 0) ++g_l2_users[m->device];
   m->l2_win_bytes = (int64_t)std::min(want, (size_t)max_win);
   m->l2_hit_ratio = (float)std::min(1.0, (double)g_l2_setaside[m->device] / (double)m->l2_win_bytes);
   return true;
+}
+
+// Before a solve: the set-aside for a window variant, none for any other.
+static void l2_for_solve(fg_mesh *m, bool window) {
+  if (window) {
+    prepare_l2(m);
+    return;
+  }
+  std::lock_guard<std::mutex> g(g_l2_lock);
+  if (m->device < 0 || m->device >= 64 || g_l2_setaside[m->device] == 0) return;
+  cudaCtxResetPersistingL2Cache();
+  cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
+  cudaGetLastError();
+  g_l2_setaside[m->device] = 0;
 }
 
 // Returns every line the process's context holds as persisting to normal, so that
@@ -1431,8 +1461,8 @@ static void reset_persisting_l2(fg_mesh *m) {
 void fg_release_l2(fg_mesh *m) {
   if (m->l2_win_bytes <= 0) return;
   std::lock_guard<std::mutex> g(g_l2_lock);
-  cudaCtxResetPersistingL2Cache();
-  if (--g_l2_users[m->device] == 0) {
+  if (--g_l2_users[m->device] == 0 && g_l2_setaside[m->device] > 0) {
+    cudaCtxResetPersistingL2Cache();
     cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
     g_l2_setaside[m->device] = 0;
   }
@@ -1691,6 +1721,7 @@ static void launch_vec64(fg_mesh *m) {
 // buffer 0 -> 1, so the iteration blocks start reading buffer 1.
 static void start_cg(fg_mesh *m, bool mixed, const double *r64, double scale, double tol2_rel, int maxit) {
   const unsigned g = red_grid(m->nvp);
+  l2_for_solve(m, mixed && (m->spmv_variant32 == 10 || m->spmv_variant32 == 20));
   if (mixed && (m->spmv_variant32 == 16 || m->spmv_variant32 == 20)) {
     ensure_scaled(m);
     k_cg32ss_init<<<g, 256, 0, m->stream>>>(m->nv, m->nvp, r64, scale, m->sdiag32, m->v32[4], m->v32[6], m->v32[1],
@@ -1910,7 +1941,7 @@ static int inner_solve(fg_mesh *m, bool mixed, const double *r64, double rn, dou
       const int v = o.spmv - 1;
       const bool avail = v < 4 || v == 6 || v == 8 || v == 9 || (v >= 11 && v < 17) ||
                          (v >= 17 && v < 20 && bulk_per_sm(m, v) > 0) ||
-                         ((v == 10 || v == 20) && prepare_l2(m)) ||
+                         ((v == 10 || v == 20) && l2_supported(m)) ||
                          ((v == 4 || v == 7) && m->halo_col) || (v == 5 && pipe_available(m));
       m->spmv_variant32 = avail ? v : 0;
     } else if (!m->tuned32 && !tune_cache_get(m, true)) {
@@ -2259,7 +2290,7 @@ extern "C" fg_status fg_set_cg_variant(fg_mesh *m, int32_t precision, int32_t va
       const int v = variant - 1;
       const bool avail = v < 4 || v == 6 || v == 8 || v == 9 || (v >= 11 && v < 17) ||
                          (v >= 17 && v < 20 && bulk_per_sm(m, v) > 0) ||
-                         ((v == 10 || v == 20) && prepare_l2(m)) ||
+                         ((v == 10 || v == 20) && l2_supported(m)) ||
                          ((v == 4 || v == 7) && m->halo_col) || (v == 5 && pipe_available(m));
       FG_REQUIRE(avail, FG_UNSUPPORTED, "fg_set_cg_variant: variant not available for this operator");
       m->spmv_variant32 = v;
