@@ -256,28 +256,33 @@ def run_ours(args):
     lib.fg_mesh_layout(g.h, C.byref(nsell), C.byref(ninc), C.byref(nsl))
     fg.newton_magnetostatics(mesh, nl, mu_lin, u0, precision="mixed")   # leaves J32 on the handle
     chosen = C.c_int32()
-    variants_us = np.zeros(20)
+    names = ["fused gather/256", "fused gather-hoist/256", "fused gather/128", "fused gather/512",
+             "fused halo-smem", "fused halo-smem-pipelined", "split gather/256", "split halo-smem",
+             "split gather persistent", "split gather persistent, programmatic launch",
+             "split gather persistent 6/SM, values in L2 window", "split gather persistent 4/SM",
+             "split gather persistent 3/SM", "split gather persistent 5/SM",
+             "split gather persistent 6/SM", "split gather persistent 7/SM",
+             "split, Jacobi-scaled system, persistent 6/SM",
+             "split, bulk-staged entries, persistent 4/SM", "split, bulk-staged entries, persistent 3/SM",
+             "split, bulk-staged entries, persistent 2/SM",
+             "split, Jacobi-scaled system, persistent 6/SM, values in L2 window"]
+    variants_us = np.zeros(len(names))
     # the table of every variant on the converged operator (a second timing); the
     # per-kernel figures below are for the variant the timed solves used
-    L.check(lib.fg_autotune(g.h, L.FG_MIXED, C.byref(chosen), L.ptr(variants_us), 20))
+    L.check(lib.fg_autotune(g.h, L.FG_MIXED, C.byref(chosen), L.ptr(variants_us), len(names)))
     L.check(lib.fg_set_cg_variant(g.h, L.FG_MIXED, used32.value))
     autotune = {"cg32_iteration_variants_us": [round(float(v), 2) for v in variants_us],
                 "chosen_on_converged_operator": int(chosen.value), "used_by_timed_solves": int(used32.value) - 1,
                 "used64_by_timed_solves": int(used64.value) - 1,
-                "names": ["fused gather/256", "fused gather-hoist/256", "fused gather/128", "fused gather/512",
-                          "fused halo-smem", "fused halo-smem-pipelined", "split gather/256", "split halo-smem",
-                          "split gather persistent", "split gather persistent, programmatic launch",
-                          "split gather persistent 6/SM, values in L2 window", "split gather persistent 4/SM",
-                          "split gather persistent 3/SM", "split gather persistent 5/SM",
-                          "split gather persistent 6/SM", "split gather persistent 7/SM",
-                          "split, Jacobi-scaled system, persistent 6/SM",
-                          "split, bulk-staged entries, persistent 4/SM", "split, bulk-staged entries, persistent 3/SM",
-                          "split, bulk-staged entries, persistent 2/SM",
-                          "split, Jacobi-scaled system, persistent 6/SM, values in L2 window"]}
+                "names": names}
     ms_spmv, ms_iter = C.c_double(), C.c_double()
     L.check(lib.fg_bench_kernel(g.h, 0, L.FG_MIXED, 200, C.byref(ms_spmv)))
     L.check(lib.fg_bench_kernel(g.h, 3, L.FG_MIXED, 200, C.byref(ms_iter)))
-    kernels_us = {"cg32_spmv": ms_spmv.value * 1e3, "cg32_iteration": ms_iter.value * 1e3}
+    ms_loop = C.c_double()
+    L.check(lib.fg_bench_kernel(g.h, 6, L.FG_MIXED, 256, C.byref(ms_loop)))
+    # cg32_iteration: direct launches; cg32_iteration_in_loop: the solver's graph loop
+    kernels_us = {"cg32_spmv": ms_spmv.value * 1e3, "cg32_iteration": ms_iter.value * 1e3,
+                  "cg32_iteration_in_loop": ms_loop.value * 1e3}
     for name, which in (("newton_element_pass_all_f32", 2), ("newton_residual_split", 4),
                         ("newton_residual_jacobian_split_f32", 5)):
         t = C.c_double()
@@ -289,9 +294,9 @@ def run_ours(args):
     L.check(lib.fg_set_cg_variant(g.h, L.FG_FP64, used64.value))
     autotune["cg64_spmv_variants_us"] = [round(float(v), 2) for v in us64]
     autotune["chosen64_on_converged_operator"] = int(ch64.value)
-    for name, which in (("cg64_spmv", 0), ("cg64_update", 1)):
+    for name, which, reps in (("cg64_spmv", 0, 200), ("cg64_update", 1, 200), ("cg64_iteration_in_loop", 6, 256)):
         t = C.c_double()
-        L.check(lib.fg_bench_kernel(g.h, which, L.FG_FP64, 200, C.byref(t)))
+        L.check(lib.fg_bench_kernel(g.h, which, L.FG_FP64, reps, C.byref(t)))
         kernels_us[name] = t.value * 1e3
     fg.newton_magnetostatics(mesh, nl, mu_lin, u0, precision="mixed")
     n = mesh.nv
@@ -314,10 +319,18 @@ def run_ours(args):
         alg_bytes = g.nnz * 6 + 48 * n
         kname = {4: "k_cg32_iter_halo", 5: "k_cg32_iter_pipe"}.get(v, "k_cg32_iter")
     achieved = alg_bytes / (ms_spmv.value * 1e-3) / 1e9
+    # DRAM bytes per launch of the same kernel from an ncu capture at 96^3: 10 = the
+    # L2-window variant (warm L2), 14 = the same grid without the window (cold);
+    # other variants: none captured
+    traffic, traffic_src = args.spmv_traffic, "--spmv-traffic" if args.spmv_traffic else None
+    if traffic is None and args.cells == 96 and v in (10, 14):
+        traffic = {10: 70.73e6, 14: 97.07e6}[v]
+        traffic_src = "ncu dram__bytes_read.sum + dram__bytes_write.sum of this kernel at 96^3"
     roofline = {"bound": "hbm", "kernel": kname, "variant": autotune["names"][v],
                 "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                "traffic": args.spmv_traffic, "algorithmic_bytes": alg_bytes, "us_per_launch": ms_spmv.value * 1e3}
+                "traffic": traffic, "traffic_source": traffic_src, "algorithmic_bytes": alg_bytes,
+                "us_per_launch": ms_spmv.value * 1e3}
 
     # e2e through the one-shot C ABI with pinned host buffers
     e2e = None
