@@ -151,6 +151,20 @@ function set_dirichlet!(g::GPUMesh, fixed::AbstractVector{UInt8})
     check(ccall((:fg_mesh_set_dirichlet, libpath()), Cint, (Ptr{Cvoid}, Ptr{UInt8}), g.h, fixed))
 end
 
+# CG kernel variant of one precision (:mixed or :fp64): fix one (0 = autotune again)
+# or read the one the handle's solves use
+precision_code(p::Symbol) = p === :mixed ? Int32(1) : Int32(0)
+function set_cg_variant!(g::GPUMesh, precision::Symbol, variant::Integer)
+    check(ccall((:fg_set_cg_variant, libpath()), Cint, (Ptr{Cvoid}, Int32, Int32), g.h,
+                precision_code(precision), Int32(variant)))
+end
+function cg_variant(g::GPUMesh, precision::Symbol)
+    v = Ref{Int32}(0)
+    check(ccall((:fg_get_cg_variant, libpath()), Cint, (Ptr{Cvoid}, Int32, Ref{Int32}), g.h,
+                precision_code(precision), v))
+    return Int(v[])
+end
+
 csc(g::GPUMesh, vals::Vector{Float64}) =
     SparseMatrixCSC(g.nv, g.nv, copy(g.colptr), Int64.(g.rowval), vals)
 

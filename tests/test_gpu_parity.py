@@ -157,6 +157,58 @@ def test_resident_newton_same_as_one_call():
         assert np.array_equal(u2, ug) and np.array_equal(H2, Hg) and np.array_equal(mu2, mug)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_cg_graph_modes_same_iterates(tet, precision):
+    """The whole-solve WHILE-loop graph (use_graph 1), host-checked graph blocks (2)
+    and plain launches (0) run the same kernels in the same order: bit-identical
+    solutions and the same iteration counts, for several check_every."""
+    K = O.stiffnessMatrix(tet) + O.massMatrix(tet)
+    b = np.random.default_rng(11).normal(size=tet.nv)
+    runs = [fg.cg(K, b, reltol=1e-10, precision=precision, use_graph=g, check_every=c, return_stats=True)
+            for g, c in ((1, 32), (1, 4), (2, 32), (0, 8))]
+    x0, s0 = runs[0]
+    for x, st in runs[1:]:
+        assert st["iterations"] == s0["iterations"] and st["converged"]
+        assert np.array_equal(x.view(np.uint64), x0.view(np.uint64))
+
+
+def test_newton_phases_and_used_variant():
+    """fg_newton_stats splits the solve's device time; fg_get_cg_variant reports the
+    variant the solves used (a forced one as given)."""
+    import ctypes as C
+    import femeko_gpu._lib as L
+    m, nl, mu_lin, u0 = newton_case(10, 5)
+    r = fg.ResidentNewton(m, nl, mu_lin, u0)
+    st = r.solve(precision="mixed")
+    assert 0.0 < st["setup_ms"] < st["ms"] and 0.0 < st["cg_ms"] < st["ms"]
+    assert st["setup_ms"] + st["cg_ms"] <= st["ms"] * 1.0001
+    v = C.c_int32(-1)
+    L.check(L.lib().fg_get_cg_variant(r.g.h, L.FG_MIXED, C.byref(v)))
+    assert 1 <= v.value <= 21
+    L.check(L.lib().fg_set_cg_variant(r.g.h, L.FG_MIXED, 15))
+    st2 = r.solve(precision="mixed")
+    L.check(L.lib().fg_get_cg_variant(r.g.h, L.FG_MIXED, C.byref(v)))
+    assert v.value == 15 and st2["converged"]
+    L.check(L.lib().fg_set_cg_variant(r.g.h, L.FG_MIXED, 0))
+
+
+def test_resident_newton_new_mask_rebuilds_element_list():
+    """New inputs with another nonlinear mask on the same handle: the kept element
+    list is replaced (results equal a fresh handle's)."""
+    import femeko_gpu._lib as L
+    m, nl, mu_lin, u0 = newton_case(10, 7)
+    nl2 = nl.copy()
+    nl2[np.flatnonzero(nl)[::2]] = 0
+    r = fg.ResidentNewton(m, nl, mu_lin, u0)
+    r.solve(precision="fp64")
+    L.check(L.lib().fg_newton_set_inputs(r.g.h, L.ptr(nl2), L.ptr(mu_lin), L.ptr(u0)))
+    s2 = r.solve(precision="fp64")
+    u2, H2, mu2 = r.outputs()
+    uo, Ho, muo, so = O.newton(m, u0, nl2, mu_lin, 1.2e6, 500.0, cg_tol=1e-12, line_search="residual")
+    assert s2["converged"]
+    assert np.linalg.norm(H2 - Ho) / np.linalg.norm(Ho) < 1e-8
+
+
 def test_newton_reference_line_search_same_iterates():
     """The reference lineSearch (frozen secant, src/FEM3D.jl:123-152) converges only
     linearly; with tight inner solves the GPU follows the oracle's iterates."""
