@@ -221,16 +221,28 @@ struct fg_mesh {
   int spmv_variant32 = 0;     // FP32 CG iteration variant chosen by the autotuner
   int spmv_variant64 = 0;     // FP64 CG SpMV variant chosen by the autotuner
   bool tuned32 = false, tuned64 = false;
-  std::vector<void *> extra;  // allocations released at destroy
+  std::vector<void *> extra;  // stream-ordered allocations released at destroy
+  std::vector<void *> extra_sync;  // plain allocations (made before the stream existed)
 };
 
 // ---------------------------------------------------------------- helpers
+// Device memory of a handle comes from the device's stream-ordered pool on the
+// handle's stream (cudaMallocAsync; released with cudaFreeAsync at destroy): a
+// one-shot call that creates and destroys a handle reuses the pool's memory instead
+// of paying a synchronising cudaMalloc/cudaFree per buffer (fg_setup.cu keeps the
+// pool's memory when it is freed).
+void fg_pool_init(int device);
 template <class T>
 static inline T *dev_alloc(fg_mesh *m, size_t count) {
   void *ptr = nullptr;
   if (count == 0) count = 1;
-  FG_CUDA_TRY(cudaMalloc(&ptr, count * sizeof(T)));
-  if (m) m->extra.push_back(ptr);
+  if (m && m->stream) {
+    FG_CUDA_TRY(cudaMallocAsync(&ptr, count * sizeof(T), m->stream));
+    m->extra.push_back(ptr);
+  } else {
+    FG_CUDA_TRY(cudaMalloc(&ptr, count * sizeof(T)));
+    if (m) m->extra_sync.push_back(ptr);
+  }
   return static_cast<T *>(ptr);
 }
 

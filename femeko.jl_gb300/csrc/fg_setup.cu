@@ -427,11 +427,32 @@ static void exclusive_scan_host(const std::vector<int> &in, std::vector<int64_t>
   for (size_t i = 0; i < in.size(); ++i) out[i + 1] = out[i] + in[i];
 }
 
+// The default memory pool of a device keeps the memory freed to it (no release
+// threshold) for the next handle; set once per device for this process.
+void fg_pool_init(int device) {
+  static std::mutex lock;
+  static bool done[64] = {false};
+  if (device < 0 || device >= 64) return;
+  std::lock_guard<std::mutex> g(lock);
+  if (done[device]) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  cudaGetLastError();
+  done[device] = true;
+}
+
 static void free_mesh(fg_mesh *m) {
   if (!m) return;
   for (int g = 0; g < 4; ++g)
     if (m->graph[g].exec) cudaGraphExecDestroy(m->graph[g].exec);
-  for (void *ptr : m->extra) cudaFree(ptr);
+  if (m->stream) {
+    for (void *ptr : m->extra) cudaFreeAsync(ptr, m->stream);
+    cudaStreamSynchronize(m->stream);
+  }
+  for (void *ptr : m->extra_sync) cudaFree(ptr);
   if (m->hbuf) cudaFreeHost(m->hbuf);
   if (m->hint) cudaFreeHost(m->hint);
   if (m->ev0) cudaEventDestroy(m->ev0);
@@ -457,6 +478,7 @@ extern "C" fg_status fg_mesh_create(const double *p, int64_t nv, const int32_t *
     m = new fg_mesh();
     FG_CUDA_TRY(cudaGetDevice(&m->device));
     FG_CUDA_TRY(cudaDeviceGetAttribute(&m->sm_count, cudaDevAttrMultiProcessorCount, m->device));
+    fg_pool_init(m->device);
     FG_CUDA_TRY(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
     FG_CUDA_TRY(cudaEventCreate(&m->ev0));
     FG_CUDA_TRY(cudaEventCreate(&m->ev1));
@@ -472,17 +494,17 @@ extern "C" fg_status fg_mesh_create(const double *p, int64_t nv, const int32_t *
     m->p = dev_alloc<double>(m, 3 * (size_t)nv);
     FG_CUDA_TRY(cudaMemcpyAsync(m->p, p, sizeof(double) * 3 * (size_t)nv, cudaMemcpyHostToDevice, s));
     int32_t *traw = nullptr;
-    FG_CUDA_TRY(cudaMalloc(&traw, sizeof(int32_t) * (size_t)nt * npe));
+    FG_CUDA_TRY(cudaMallocAsync(&traw, sizeof(int32_t) * (size_t)nt * npe, s));
     FG_CUDA_TRY(cudaMemcpyAsync(traw, t, sizeof(int32_t) * (size_t)nt * npe, cudaMemcpyHostToDevice, s));
     m->t = dev_alloc<int>(m, (size_t)nt * npe);
     k_convert_t<<<grid_for(nt, 256), 256, 0, s>>>(traw, m->t, nt, npe, nv, index_base, m->flags);
     FG_CUDA_TRY(cudaGetLastError());
     fg_check_flags(m, "fg_mesh_create");
-    cudaFree(traw);
+    cudaFreeAsync(traw, s);
 
     // incidence lists
     int *deg = nullptr, *cursor = nullptr, *iptr = nullptr, *inc = nullptr;
-    FG_CUDA_TRY(cudaMalloc(&deg, sizeof(int) * (size_t)nv));
+    FG_CUDA_TRY(cudaMallocAsync(&deg, sizeof(int) * (size_t)nv, s));
     FG_CUDA_TRY(cudaMemsetAsync(deg, 0, sizeof(int) * (size_t)nv, s));
     k_count_deg<<<grid_for(nt, 256), 256, 0, s>>>(m->t, nt, npe, deg);
     std::vector<int> hdeg(nv);
@@ -493,8 +515,8 @@ extern "C" fg_status fg_mesh_create(const double *p, int64_t nv, const int32_t *
     std::vector<int> hiptr32(nv + 1);
     for (int64_t i = 0; i <= nv; ++i) hiptr32[i] = (int)hiptr[i];
     m->maxdeg = *std::max_element(hdeg.begin(), hdeg.end());
-    FG_CUDA_TRY(cudaMalloc(&iptr, sizeof(int) * (size_t)(nv + 1)));
-    FG_CUDA_TRY(cudaMalloc(&inc, sizeof(int) * (size_t)nt * npe));
+    FG_CUDA_TRY(cudaMallocAsync(&iptr, sizeof(int) * (size_t)(nv + 1), s));
+    FG_CUDA_TRY(cudaMallocAsync(&inc, sizeof(int) * (size_t)nt * npe, s));
     FG_CUDA_TRY(cudaMemcpyAsync(iptr, hiptr32.data(), sizeof(int) * (size_t)(nv + 1), cudaMemcpyHostToDevice, s));
     cursor = deg;
     FG_CUDA_TRY(cudaMemsetAsync(cursor, 0, sizeof(int) * (size_t)nv, s));
@@ -598,9 +620,9 @@ extern "C" fg_status fg_mesh_create(const double *p, int64_t nv, const int32_t *
       k_geom_tri<<<grid_for(nt, 256), 256, 0, s>>>(m->p, m->t, nt, m->geo, m->flags);
     FG_CUDA_TRY(cudaGetLastError());
     fg_check_flags(m, "fg_mesh_create");
-    cudaFree(deg);
-    cudaFree(iptr);
-    cudaFree(inc);
+    cudaFreeAsync(deg, s);
+    cudaFreeAsync(iptr, s);
+    cudaFreeAsync(inc, s);
 
     // control and reduction workspace
     // one slot of 4 per CTA of any row kernel (CTAs of 32 rows or more)

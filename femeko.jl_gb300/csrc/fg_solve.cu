@@ -2052,6 +2052,7 @@ static fg_mesh *matrix_handle(int64_t n, const int64_t *colptr, const int64_t *r
   try {
     FG_CUDA_TRY(cudaGetDevice(&m->device));
     FG_CUDA_TRY(cudaDeviceGetAttribute(&m->sm_count, cudaDevAttrMultiProcessorCount, m->device));
+    fg_pool_init(m->device);
     FG_CUDA_TRY(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
     FG_CUDA_TRY(cudaEventCreate(&m->ev0));
     FG_CUDA_TRY(cudaEventCreate(&m->ev1));
