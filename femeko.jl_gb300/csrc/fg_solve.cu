@@ -87,45 +87,6 @@ struct Acc<float> {
   __device__ __forceinline__ void add(float x) { v = ff_add(v, ff{x, 0.f}); }
 };
 
-// Compensated FP32 block sum of (hi, lo) pairs, returned as double in thread 0.
-template <int N>
-__device__ __forceinline__ void block_sum_ff(ff (&v)[N], double (&out)[N], ff (*sh)[32]) {
-#pragma unroll
-  for (int j = 0; j < N; ++j)
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      ff other{__shfl_down_sync(0xffffffffu, v[j].hi, o), __shfl_down_sync(0xffffffffu, v[j].lo, o)};
-      v[j] = ff_add(v[j], other);
-    }
-  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  if (l == 0)
-#pragma unroll
-    for (int j = 0; j < N; ++j) sh[j][w] = v[j];
-  __syncthreads();
-  if (w == 0) {
-    int nw = blockDim.x >> 5;
-#pragma unroll
-    for (int j = 0; j < N; ++j) {
-      v[j] = (l < nw) ? sh[j][l] : ff{0.f, 0.f};
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        ff other{__shfl_down_sync(0xffffffffu, v[j].hi, o), __shfl_down_sync(0xffffffffu, v[j].lo, o)};
-        v[j] = ff_add(v[j], other);
-      }
-      out[j] = (double)v[j].hi + (double)v[j].lo;
-    }
-  }
-}
-
-template <int N>
-__device__ __forceinline__ void block_sum_acc(const Acc<float> (&a)[N], double (&out)[N]) {
-  __shared__ ff shf[N][32];
-  ff v[N];
-#pragma unroll
-  for (int j = 0; j < N; ++j) v[j] = a[j].v;
-  block_sum_ff<N>(v, out, shf);
-}
-
 // Block partials -> one total, in two parallel levels so that no single block reads
 // every partial.  Block b writes its partial and arrives on counter[1 + b % 64]; the
 // last block of each of those groups sums the group's partials (one per thread) and
@@ -188,6 +149,102 @@ __device__ __forceinline__ bool grid_finish(const double (&v)[N], double *partia
 #pragma unroll
   for (int j = 0; j < N; ++j) tot[j] = acc[j];
   return threadIdx.x == 0;
+}
+
+// Compensated FP32 block sum kept as (hi, lo) pairs in thread 0.
+template <int N>
+__device__ __forceinline__ void block_sum_ff_pair(ff (&v)[N], ff (*sh)[32]) {
+#pragma unroll
+  for (int j = 0; j < N; ++j)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      ff other{__shfl_down_sync(0xffffffffu, v[j].hi, o), __shfl_down_sync(0xffffffffu, v[j].lo, o)};
+      v[j] = ff_add(v[j], other);
+    }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0)
+#pragma unroll
+    for (int j = 0; j < N; ++j) sh[j][w] = v[j];
+  __syncthreads();
+  if (w == 0) {
+    const int nw = blockDim.x >> 5;
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      v[j] = (l < nw) ? sh[j][l] : ff{0.f, 0.f};
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        ff other{__shfl_down_sync(0xffffffffu, v[j].hi, o), __shfl_down_sync(0xffffffffu, v[j].lo, o)};
+        v[j] = ff_add(v[j], other);
+      }
+    }
+  }
+}
+
+// grid_finish for the FP32 iterations' compensated dot products: the same two
+// levels and fixed order, with the partials kept as (hi, lo) float pairs and summed
+// on the FP32 pipe; only the totals become doubles.  GB300 runs FP64 at 1/64 of the
+// FP32 rate: two levels of double block sums on the finishing path cost ~3 us per
+// launch at 96^3.  v: the block's sums in thread 0.
+template <int N>
+__device__ __forceinline__ bool grid_finish_ff(const ff (&v)[N], float2 *partials, unsigned *counter,
+                                               double (&tot)[N]) {
+  __shared__ int s_role;
+  __shared__ ff shg[N][32], shf[N][32];
+  const unsigned G = gridDim.x;
+  const unsigned grp = blockIdx.x % FG_ARRIVE_GROUPS;
+  const unsigned ngroups = G < FG_ARRIVE_GROUPS ? G : FG_ARRIVE_GROUPS;
+  const unsigned gsize = (G - grp + FG_ARRIVE_GROUPS - 1) / FG_ARRIVE_GROUPS;
+  float2 *gpart = partials + (size_t)G * N;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int j = 0; j < N; ++j) partials[(size_t)blockIdx.x * N + j] = make_float2(v[j].hi, v[j].lo);
+    s_role = (atom_add_acq_rel(counter + 1 + grp, 1u) == gsize - 1) ? 1 : 0;
+  }
+  __syncthreads();
+  if (s_role == 0) return false;
+  __threadfence();
+  ff acc[N];
+#pragma unroll
+  for (int j = 0; j < N; ++j) acc[j] = ff{0.f, 0.f};
+  for (unsigned k = threadIdx.x; k < gsize; k += blockDim.x)
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      const float2 q = __ldcg(partials + (size_t)(grp + k * FG_ARRIVE_GROUPS) * N + j);
+      acc[j] = ff_add(acc[j], ff{q.x, q.y});
+    }
+  block_sum_ff_pair<N>(acc, shg);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int j = 0; j < N; ++j) gpart[(size_t)grp * N + j] = make_float2(acc[j].hi, acc[j].lo);
+    counter[1 + grp] = 0u;  // every member of the group has arrived
+    s_role = (atom_add_acq_rel(counter, 1u) == ngroups - 1) ? 2 : 0;
+  }
+  __syncthreads();
+  if (s_role != 2) return false;
+  __threadfence();
+#pragma unroll
+  for (int j = 0; j < N; ++j) acc[j] = ff{0.f, 0.f};
+  for (unsigned g = threadIdx.x; g < ngroups; g += blockDim.x)
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      const float2 q = __ldcg(gpart + (size_t)g * N + j);
+      acc[j] = ff_add(acc[j], ff{q.x, q.y});
+    }
+  block_sum_ff_pair<N>(acc, shf);
+  if (threadIdx.x == 0) counter[0] = 0u;
+#pragma unroll
+  for (int j = 0; j < N; ++j) tot[j] = (double)acc[j].hi + (double)acc[j].lo;
+  return threadIdx.x == 0;
+}
+
+// The three dot products of an FP32 CG iteration (per-thread compensated sums):
+// block sums, then grid_finish_ff.  True in thread 0 of the finishing block.
+__device__ __forceinline__ bool finish_dots32(const Acc<float> (&dots)[3], double *partials, unsigned *counter,
+                                              double (&tot)[3]) {
+  __shared__ ff shb[3][32];
+  ff v[3] = {dots[0].v, dots[1].v, dots[2].v};
+  block_sum_ff_pair<3>(v, shb);
+  return grid_finish_ff<3>(v, reinterpret_cast<float2 *>(partials), counter, tot);
 }
 
 // ------------------------------------------------------------------ index helpers
@@ -313,10 +370,8 @@ __global__ void __launch_bounds__(BS) k_cg32_iter(int64_t n, const int *__restri
     dots[1].add(acc * unw);
     dots[2].add(rnew * rnew);
   }
-  double part[3];
-  block_sum_acc<3>(dots, part);
   double tot[3];
-  if (grid_finish<3>(part, partials, counter, tot)) cgcg_scalars(tot, scal, ictl);
+  if (finish_dots32(dots, partials, counter, tot)) cgcg_scalars(tot, scal, ictl);
 }
 
 // The same iteration with halo staging: the CTA first turns each distinct neighbour
@@ -378,10 +433,8 @@ __global__ void __launch_bounds__(R) k_cg32_iter_halo(int64_t n, const int *__re
     dots[1].add(acc * unw);
     dots[2].add(rnew * rnew);
   }
-  double part[3];
-  block_sum_acc<3>(dots, part);
   double tot[3];
-  if (grid_finish<3>(part, partials, counter, tot)) cgcg_scalars(tot, scal, ictl);
+  if (finish_dots32(dots, partials, counter, tot)) cgcg_scalars(tot, scal, ictl);
 }
 
 // The halo iteration as a persistent, software-pipelined kernel.  Each CTA walks the
@@ -545,10 +598,8 @@ __global__ void __launch_bounds__(R) k_cg32_iter_pipe(PipeArgs a, const float4 *
       atomicExch(ictl + I_DONE, 1);
     }
   }
-  double part[3];
-  block_sum_acc<3>(dots, part);
   double tot[3];
-  if (grid_finish<3>(part, partials, counter, tot) && ok) cgcg_scalars(tot, scal, ictl);
+  if (finish_dots32(dots, partials, counter, tot) && ok) cgcg_scalars(tot, scal, ictl);
 }
 
 // Programmatic dependent launch: a kernel launched with programmatic stream
@@ -645,10 +696,8 @@ __global__ void __launch_bounds__(256) k_cg32s_spmv(int64_t n, const int *__rest
     dots[2].add(rw ? ri * ri * __ldg(rw + i) : ri * ri);
   }
   }
-  double part[3];
-  block_sum_acc<3>(dots, part);
   double tot[3];
-  if (grid_finish<3>(part, partials, counter, tot)) cgcg_scalars(tot, scal, ictl);
+  if (finish_dots32(dots, partials, counter, tot)) cgcg_scalars(tot, scal, ictl);
 }
 
 // The split SpMV with halo staging of u (4 bytes per distinct neighbour).
@@ -695,10 +744,8 @@ __global__ void __launch_bounds__(R) k_cg32s_spmv_halo(int64_t n, const int *__r
     dots[1].add(acc * ui);
     dots[2].add(ri * ri);
   }
-  double part[3];
-  block_sum_acc<3>(dots, part);
   double tot[3];
-  if (grid_finish<3>(part, partials, counter, tot)) cgcg_scalars(tot, scal, ictl);
+  if (finish_dots32(dots, partials, counter, tot)) cgcg_scalars(tot, scal, ictl);
 }
 
 // The split SpMV with the matrix entries staged by the bulk-copy engine: a persistent
@@ -809,10 +856,8 @@ __global__ void __launch_bounds__(256) k_cg32s_spmv_bulk(int64_t n, int nslices,
     }
     __syncthreads();
   }
-  double part[3];
-  block_sum_acc<3>(dots, part);
   double tot[3];
-  if (grid_finish<3>(part, partials, counter, tot) && ok) cgcg_scalars(tot, scal, ictl);
+  if (finish_dots32(dots, partials, counter, tot) && ok) cgcg_scalars(tot, scal, ictl);
 }
 
 // Jacobi-PCG as plain CG on the symmetrically scaled system (the scaled split
