@@ -265,7 +265,8 @@ def run_ours(args):
              "split, Jacobi-scaled system, persistent 6/SM",
              "split, bulk-staged entries, persistent 4/SM", "split, bulk-staged entries, persistent 3/SM",
              "split, bulk-staged entries, persistent 2/SM",
-             "split, Jacobi-scaled system, persistent 6/SM, values in L2 window"]
+             "split, Jacobi-scaled system, persistent 6/SM, values in L2 window",
+             "split, bulk-staged entries, persistent 4/SM, values in L2 window"]
     variants_us = np.zeros(len(names))
     # the table of every variant on the converged operator (a second timing); the
     # per-kernel figures below are for the variant the timed solves used
@@ -312,7 +313,7 @@ def run_ours(args):
         # (12 B).  Neighbour gathers of u are re-reads.
         alg_bytes = g.nnz * 6 + 12 * n
         kname = {7: "k_cg32s_spmv_halo", 17: "k_cg32s_spmv_bulk", 18: "k_cg32s_spmv_bulk",
-                 19: "k_cg32s_spmv_bulk"}.get(v, "k_cg32s_spmv")
+                 19: "k_cg32s_spmv_bulk", 21: "k_cg32s_spmv_bulk"}.get(v, "k_cg32s_spmv")
     else:
         # one fused iteration: matrix as above; per row the (r, w, s, dinv) state read
         # and written (16 + 16 B) and p, x read and written (8 + 8 B)
@@ -604,7 +605,7 @@ def main():
     ap.add_argument("--graph-mode", type=int, default=1, choices=[0, 1, 2],
                     help="1: whole CG in one graph launch (device-side loop); 2: host-checked graph blocks; 0: no graph")
     ap.add_argument("--cg-variant", type=int, default=0,
-                    help="fix the FP32 CG kernel variant (1..21; 0: autotuned), e.g. for profiling runs")
+                    help="fix the FP32 CG kernel variant (1..22; 0: autotuned), e.g. for profiling runs")
     ap.add_argument("--cg64-variant", type=int, default=0, help="fix the FP64 CG SpMV variant (1..4; 0: autotuned)")
     ap.add_argument("--case", choices=sorted(CASES), default=None,
                     help="run a secondary workload instead of the headline benchmark")

@@ -1300,7 +1300,12 @@ static void ensure_cg64(fg_mesh *m) {
 // programmatic dependent launch, 10 the same with the matrix values held in L2,
 // 11-15 persistent grids of 4, 3, 5, 6 and 7 blocks per SM, 16 CG on the
 // symmetrically Jacobi-scaled system with the SpMV of variant 14
-constexpr int FG_N_SPMV32 = 21;
+constexpr int FG_N_SPMV32 = 22;
+// Split FP32 variants on the scaled system, with the values in the L2 window, and
+// with the matrix entries staged by bulk copies.
+static inline bool v_scaled(int v) { return v == 16 || v == 20; }
+static inline bool v_window(int v) { return v == 10 || v == 20 || v == 21; }
+static inline bool v_bulk(int v) { return (v >= 17 && v <= 19) || v == 21; }
 static inline bool split32(int v) { return v >= 6; }
 constexpr int FG_N_SPMV64 = 4;   // 0 direct gathers, 1 halo staging, 2/3 persistent with 4/8 blocks per SM
 
@@ -1518,10 +1523,11 @@ void fg_release_l2(fg_mesh *m) {
 // A launch whose accesses to the window [win, win + l2_win_bytes) persist in L2.
 template <typename... KArgs, typename... Args>
 static void l2_launch(fg_mesh *m, const float *win, void (*kern)(KArgs...), unsigned grid, unsigned block,
-                      Args... args) {
+                      size_t smem, Args... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
   cfg.stream = m->stream;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeAccessPolicyWindow;
@@ -1567,7 +1573,7 @@ static size_t bulk_smem(const fg_mesh *m) {
 // two stages do not fit; sized once per handle.  The kernels may take up to the
 // device's opt-in shared memory (set once per process).
 static int bulk_per_sm(fg_mesh *m, int v) {
-  static const int kWant[3] = {4, 3, 2};
+  static const int kWant[5] = {4, 3, 2, 4, 4};  // 17-19, (20: not bulk), 21: 17 with the L2 window
   if (m->bulk_fit < 0) {
     static std::once_flag attr_once;
     static int dyn_max = 0;  // opt-in shared memory less the kernels' static shared memory
@@ -1608,7 +1614,17 @@ static void bulk_launch32(fg_mesh *m, int v) {
   FG_REQUIRE(per_sm > 0, FG_UNSUPPORTED, "bulk-staged SpMV: row blocks too large for shared memory");
   const unsigned g = std::min<unsigned>(grid_for(m->nv, 256), (unsigned)per_sm * (unsigned)std::max(m->sm_count, 1));
   const size_t smem = bulk_smem(m);
-  if (m->use_dcol)
+  if (v_window(v) && m->l2_win_bytes > 0) {
+    // the bulk copies of the values read them from the L2 window
+    if (m->use_dcol)
+      l2_launch(m, m->val32, k_cg32s_spmv_bulk<ColRel>, g, 256, smem, m->nv, m->nslices, m->tmax256, m->sl_ptr,
+                m->sl_len, m->sl_dcol, m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl,
+                m->red.partials, m->red.counter);
+    else
+      l2_launch(m, m->val32, k_cg32s_spmv_bulk<ColAbs>, g, 256, smem, m->nv, m->nslices, m->tmax256, m->sl_ptr,
+                m->sl_len, m->sl_col, m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl,
+                m->red.partials, m->red.counter);
+  } else if (m->use_dcol)
     k_cg32s_spmv_bulk<ColRel><<<g, 256, smem, m->stream>>>(m->nv, m->nslices, m->tmax256, m->sl_ptr, m->sl_len,
                                                            m->sl_dcol, m->val32, m->v32[7], m->v32[4], m->v32[5],
                                                            m->scal, m->ictl, m->red.partials, m->red.counter);
@@ -1624,16 +1640,16 @@ static void launch_spmv32s(fg_mesh *m, int v) {
     // the scaled system (16) with its values in the L2 window
     const unsigned g = std::min<unsigned>(grid_for(m->nv, 256), 6u * (unsigned)std::max(m->sm_count, 1));
     if (m->use_dcol)
-      l2_launch(m, m->val32s, k_cg32s_spmv<ColRel, true>, g, 256, m->nv, m->sl_ptr, m->sl_len, m->sl_dcol,
+      l2_launch(m, m->val32s, k_cg32s_spmv<ColRel, true>, g, 256, 0, m->nv, m->sl_ptr, m->sl_len, m->sl_dcol,
                 m->val32s, m->v32[4], m->v32[4], m->diag32, m->v32[5], m->scal, m->ictl, m->red.partials,
                 m->red.counter);
     else
-      l2_launch(m, m->val32s, k_cg32s_spmv<ColAbs, true>, g, 256, m->nv, m->sl_ptr, m->sl_len, m->sl_col,
+      l2_launch(m, m->val32s, k_cg32s_spmv<ColAbs, true>, g, 256, 0, m->nv, m->sl_ptr, m->sl_len, m->sl_col,
                 m->val32s, m->v32[4], m->v32[4], m->diag32, m->v32[5], m->scal, m->ictl, m->red.partials,
                 m->red.counter);
     return;
   }
-  if (v == 16 || v == 20) {
+  if (v_scaled(v)) {
     // w = A' r' with the dots r'.r', w.r' and r.r = sum D_ii r'_i^2 (u = r' on the scaled
     // system; the stopping test is on the unscaled residual, as in Jacobi-PCG)
     const unsigned g = std::min<unsigned>(grid_for(m->nv, 256), 6u * (unsigned)std::max(m->sm_count, 1));
@@ -1651,16 +1667,16 @@ static void launch_spmv32s(fg_mesh *m, int v) {
     // the persistent grid of 14 (6 blocks per SM) with the values in the L2 window
     const unsigned g = std::min<unsigned>(grid_for(m->nv, 256), 6u * (unsigned)std::max(m->sm_count, 1));
     if (m->use_dcol)
-      l2_launch(m, m->val32, k_cg32s_spmv<ColRel, true>, g, 256, m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, m->val32,
+      l2_launch(m, m->val32, k_cg32s_spmv<ColRel, true>, g, 256, 0, m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, m->val32,
                 m->v32[7], m->v32[4], (const float *)nullptr, m->v32[5], m->scal, m->ictl, m->red.partials,
                 m->red.counter);
     else
-      l2_launch(m, m->val32, k_cg32s_spmv<ColAbs, true>, g, 256, m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val32,
+      l2_launch(m, m->val32, k_cg32s_spmv<ColAbs, true>, g, 256, 0, m->nv, m->sl_ptr, m->sl_len, m->sl_col, m->val32,
                 m->v32[7], m->v32[4], (const float *)nullptr, m->v32[5], m->scal, m->ictl, m->red.partials,
                 m->red.counter);
     return;
   }
-  if (v >= 17) {
+  if (v_bulk(v)) {
     bulk_launch32(m, v);
   } else if (v >= 8) {
     // persistent: 8 (variants 8-10), 4 (11), 3 (12), 5 (13), 6 (14) or 7 (15)
@@ -1693,7 +1709,7 @@ static void launch_spmv32s(fg_mesh *m, int v) {
 }
 
 static void launch_vec32s(fg_mesh *m, int v) {
-  if (v == 16 || v == 20) {
+  if (v_scaled(v)) {
     k_cg32ss_vec<<<grid_for(m->nvp / 4, 256), 256, 0, m->stream>>>(
         m->nvp / 4, reinterpret_cast<float4 *>(m->v32[4]), reinterpret_cast<const float4 *>(m->v32[5]),
         reinterpret_cast<float4 *>(m->v32[6]), reinterpret_cast<float4 *>(m->v32[1]),
@@ -1766,8 +1782,8 @@ static void launch_vec64(fg_mesh *m) {
 // buffer 0 -> 1, so the iteration blocks start reading buffer 1.
 static void start_cg(fg_mesh *m, bool mixed, const double *r64, double scale, double tol2_rel, int maxit) {
   const unsigned g = red_grid(m->nvp);
-  l2_for_solve(m, mixed && (m->spmv_variant32 == 10 || m->spmv_variant32 == 20));
-  if (mixed && (m->spmv_variant32 == 16 || m->spmv_variant32 == 20)) {
+  l2_for_solve(m, mixed && v_window(m->spmv_variant32));
+  if (mixed && v_scaled(m->spmv_variant32)) {
     ensure_scaled(m);
     k_cg32ss_init<<<g, 256, 0, m->stream>>>(m->nv, m->nvp, r64, scale, m->sdiag32, m->v32[4], m->v32[6], m->v32[1],
                                             m->v32[0], tol2_rel, maxit, m->scal, m->ictl);
@@ -1973,6 +1989,17 @@ static void tune_cache_put(fg_mesh *m, bool mixed) {
   g_tune[tune_key(m, mixed)] = mixed ? m->spmv_variant32 : m->spmv_variant64;
 }
 
+// Whether FP32 variant v can run on this handle (the L2 window: whether the device
+// has persisting L2; the set-aside itself is made when a solve starts).
+static bool variant32_available(fg_mesh *m, int v) {
+  if (v < 0 || v >= FG_N_SPMV32) return false;
+  if ((v == 4 || v == 7) && !m->halo_col) return false;
+  if (v == 5 && !pipe_available(m)) return false;
+  if (v_bulk(v) && bulk_per_sm(m, v) == 0) return false;
+  if (v_window(v) && !l2_supported(m)) return false;
+  return true;
+}
+
 // Inner solve of A d = scale * r64 from d = 0 to relative residual `inner`, then
 // x += d / scale.  Returns iterations; *ist = 0 converged, 1 cap, 2 non-finite.
 static int inner_solve(fg_mesh *m, bool mixed, const double *r64, double rn, double inner, int maxit,
@@ -1984,20 +2011,19 @@ static int inner_solve(fg_mesh *m, bool mixed, const double *r64, double rn, dou
       // a forced variant that this operator cannot run (no halo lists, stages too
       // large for shared memory) falls back to the plain gather kernel
       const int v = o.spmv - 1;
-      const bool avail = v < 4 || v == 6 || v == 8 || v == 9 || (v >= 11 && v < 17) ||
-                         (v >= 17 && v < 20 && bulk_per_sm(m, v) > 0) ||
-                         ((v == 10 || v == 20) && l2_supported(m)) ||
-                         ((v == 4 || v == 7) && m->halo_col) || (v == 5 && pipe_available(m));
-      m->spmv_variant32 = avail ? v : 0;
+      m->spmv_variant32 = variant32_available(m, v) ? v : 0;
     } else if (!m->tuned32 && !tune_cache_get(m, true)) {
       fg_autotune_spmv32(m, 20, nullptr, nullptr);
       tune_cache_put(m, true);
     }
-    if (m->spmv_variant32 == 10 && !prepare_l2(m)) m->spmv_variant32 = 14;
-    if (m->spmv_variant32 == 20 && !prepare_l2(m)) m->spmv_variant32 = 16;
+    if (v_window(m->spmv_variant32) && !prepare_l2(m)) {
+      // no persisting L2 after all: the same variant without the window
+      const int v = m->spmv_variant32;
+      m->spmv_variant32 = (v == 10) ? 14 : (v == 20) ? 16 : 17;
+    }
     start_cg(m, true, r64, 1.0 / rn, inner * inner, maxit);
     its = run_cg(m, true, o, ist);
-    if (m->spmv_variant32 == 16 || m->spmv_variant32 == 20)
+    if (v_scaled(m->spmv_variant32))
       k_axpy_scaled_to64<<<grid_for(m->nv, 256), 256, 0, m->stream>>>(m->nv, rn, m->sdiag32, m->v32[0], d_x);
     else
       k_axpy_to64<float><<<red_grid(m->nv), 256, 0, m->stream>>>(m->nv, rn, m->v32[0], d_x);
@@ -2284,8 +2310,7 @@ fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_v
   int best = 0;
   double best_us = 1e30;
   for (int v = 0; v < FG_N_SPMV32; ++v) {
-    if (((v == 4 || v == 7) && !m->halo_col) || (v == 5 && !pipe_available(m)) ||
-        ((v == 10 || v == 20) && !prepare_l2(m)) || (v >= 17 && v < 20 && bulk_per_sm(m, v) == 0)) {
+    if (!variant32_available(m, v) || (v_window(v) && !prepare_l2(m))) {  // not available here
       if (us_per_variant) us_per_variant[v] = 0.0;
       continue;
     }
@@ -2334,11 +2359,8 @@ extern "C" fg_status fg_set_cg_variant(fg_mesh *m, int32_t precision, int32_t va
       FG_REQUIRE(variant >= 0 && variant <= FG_N_SPMV32, FG_BAD_ARG, "fg_set_cg_variant: no such variant");
       if (variant == 0) { m->tuned32 = false; return FG_OK; }
       const int v = variant - 1;
-      const bool avail = v < 4 || v == 6 || v == 8 || v == 9 || (v >= 11 && v < 17) ||
-                         (v >= 17 && v < 20 && bulk_per_sm(m, v) > 0) ||
-                         ((v == 10 || v == 20) && l2_supported(m)) ||
-                         ((v == 4 || v == 7) && m->halo_col) || (v == 5 && pipe_available(m));
-      FG_REQUIRE(avail, FG_UNSUPPORTED, "fg_set_cg_variant: variant not available for this operator");
+      FG_REQUIRE(variant32_available(m, v), FG_UNSUPPORTED,
+                 "fg_set_cg_variant: variant not available for this operator");
       m->spmv_variant32 = v;
       m->tuned32 = true;
     } else {
