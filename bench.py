@@ -321,11 +321,11 @@ def run_ours(args):
         kname = {4: "k_cg32_iter_halo", 5: "k_cg32_iter_pipe"}.get(v, "k_cg32_iter")
     achieved = alg_bytes / (ms_spmv.value * 1e-3) / 1e9
     # DRAM bytes per launch of the same kernel from an ncu capture at 96^3: 10 and 20 =
-    # the L2-window variants (warm L2), 14 = the grid of 10 without the window (cold);
-    # other variants: none captured
+    # the L2-window variants (warm L2), 14 = the grid of 10 without the window and
+    # 17 = the bulk-staged SpMV (cold); other variants: none captured
     traffic, traffic_src = args.spmv_traffic, "--spmv-traffic" if args.spmv_traffic else None
-    if traffic is None and args.cells == 96 and v in (10, 14, 20):
-        traffic = {10: 70.73e6, 14: 97.07e6, 20: 69.70e6}[v]
+    if traffic is None and args.cells == 96 and v in (10, 14, 17, 20):
+        traffic = {10: 70.73e6, 14: 97.07e6, 17: 97.38e6, 20: 69.70e6}[v]
         traffic_src = "ncu dram__bytes_read.sum + dram__bytes_write.sum of this kernel at 96^3"
     roofline = {"bound": "hbm", "kernel": kname, "variant": autotune["names"][v],
                 "achieved": achieved, "peak": peak,

@@ -2145,6 +2145,9 @@ static fg_mesh *matrix_handle(int64_t n, const int64_t *colptr, const int64_t *r
     }
     sl_ptr[m->nslices] = (int)acc;
     m->nsell = acc;
+    // largest 256-row block in padded entries (the bulk-staged SpMV stages one)
+    for (int s0 = 0; s0 < m->nslices; s0 += 256 / FG_SLICE)
+      m->tmax256 = std::max(m->tmax256, sl_ptr[std::min(s0 + 256 / FG_SLICE, m->nslices)] - sl_ptr[s0]);
     std::vector<int> col(acc);
     std::vector<int16_t> dcol(acc, 0);
     std::vector<double> val(acc, 0.0);
