@@ -147,6 +147,7 @@ struct fg_mesh {
   int bulk_fit = -1;  // resident CTAs per SM of the bulk-staged SpMV (-1: not sized yet)
   int pipe_grid = 0;  // CTAs of the persistent pipelined iteration (0: not sized yet, -1: does not fit)
   int *halo_col = nullptr, *halo_len = nullptr;
+  bool halo_tried = false;   // the halo lists are built at the first variant that needs them
   uint16_t *sl_lcol = nullptr;
   bool use_dcol = false;
   int64_t nsell = 0;
@@ -260,6 +261,9 @@ void fg_release_l2(fg_mesh *m);
 void fg_sync(fg_mesh *m);
 // Builds the halo lists and local column indices (needs sl_ptr/sl_len/sl_col, maxrow4).
 void fg_build_halo(fg_mesh *m);
+// The halo lists, built on first use (not inside a stream capture); false when the
+// rows are too long for halo staging.
+bool fg_ensure_halo(fg_mesh *m);
 
 // assembly (fg_assemble.cu)
 enum AsmKind { ASM_STIFF = 0, ASM_MASS = 1, ASM_TANGENT = 2, ASM_HEAT = 3 };

@@ -283,6 +283,21 @@ __global__ void __launch_bounds__(FG_HALO_THREADS)
   }
 }
 
+bool fg_ensure_halo(fg_mesh *m) {
+  if (!m->halo_tried) {
+    m->halo_tried = true;
+    if (m->maxrow4 <= FG_MAX_ROW) {
+      try {
+        fg_build_halo(m);
+      } catch (const FgError &e) {
+        if (e.code != FG_BAD_MESH) throw;  // rows too long for staging: no halo variants
+        m->halo_col = nullptr;
+      }
+    }
+  }
+  return m->halo_col != nullptr;
+}
+
 void fg_build_halo(fg_mesh *m) {
   const int slots = std::max(m->maxrow4, FG_GROUP);
   // rows per CTA: the largest power of two in [32, 512] whose keys fit 8192 slots
@@ -606,7 +621,6 @@ extern "C" fg_status fg_mesh_create(const double *p, int64_t nv, const int32_t *
       fg_sync(m);
       m->use_dcol = (wide == 0);  // 16-bit column offsets when the bandwidth allows
     }
-    fg_build_halo(m);
     k_slots<<<grid_for(nv, 128), 128, 0, s>>>(iptr, inc, m->t, nt, npe, nv, m->rowptr, m->colidx, m->in_ptr,
                                               m->in_len, m->recpos, m->in_slot);
     FG_CUDA_TRY(cudaGetLastError());

@@ -1358,7 +1358,7 @@ struct Iter32Pipe {
 // as fit on the GPU at once (never more than there are row blocks).  Sized on first
 // use; pipe_grid = -1 when one CTA's stages do not fit in shared memory.
 static bool pipe_available(fg_mesh *m) {
-  if (!m->halo_col) return false;
+  if (!fg_ensure_halo(m)) return false;
   if (m->pipe_grid != 0) return m->pipe_grid > 0;
   const int HM = (m->hmax + 3) & ~3;
   const size_t smem = 2 * pipe_stage_bytes(HM, m->tmax);
@@ -1964,14 +1964,15 @@ fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_v
 fg_status fg_autotune_spmv64(fg_mesh *m, int reps, int *chosen, double *us_per_variant);
 
 // Process-wide memory of the autotuner's choices, keyed by the device and the shape
-// of the operator (rows, padded entries, longest row, halo rows per block, column
-// format): a new handle for a mesh of the same structure (the one-shot entry points
-// create one per call) reuses the choice instead of timing the variants again.
+// of the operator (rows, padded entries, longest row, column format; the halo rows
+// per block follow from the longest row): a new handle for a mesh of the same
+// structure (the one-shot entry points create one per call) reuses the choice
+// instead of timing the variants again.
 namespace {
 std::mutex g_tune_lock;
-std::map<std::tuple<int, int64_t, int64_t, int, int, int, bool>, int> g_tune;
-std::tuple<int, int64_t, int64_t, int, int, int, bool> tune_key(const fg_mesh *m, bool mixed) {
-  return std::make_tuple(m->device, m->nv, m->nsell, m->maxrow4, m->hrows, (int)m->use_dcol, mixed);
+std::map<std::tuple<int, int64_t, int64_t, int, int, bool>, int> g_tune;
+std::tuple<int, int64_t, int64_t, int, int, bool> tune_key(const fg_mesh *m, bool mixed) {
+  return std::make_tuple(m->device, m->nv, m->nsell, m->maxrow4, (int)m->use_dcol, mixed);
 }
 }  // namespace
 
@@ -1993,7 +1994,7 @@ static void tune_cache_put(fg_mesh *m, bool mixed) {
 // has persisting L2; the set-aside itself is made when a solve starts).
 static bool variant32_available(fg_mesh *m, int v) {
   if (v < 0 || v >= FG_N_SPMV32) return false;
-  if ((v == 4 || v == 7) && !m->halo_col) return false;
+  if ((v == 4 || v == 7) && !fg_ensure_halo(m)) return false;
   if (v == 5 && !pipe_available(m)) return false;
   if (v_bulk(v) && bulk_per_sm(m, v) == 0) return false;
   if (v_window(v) && !l2_supported(m)) return false;
@@ -2204,7 +2205,6 @@ static fg_mesh *matrix_handle(int64_t n, const int64_t *colptr, const int64_t *r
     for (int64_t r = 0; r < n; ++r) mr = std::max<int64_t>(mr, colptr[r + 1] - colptr[r]);
     m->maxrow = (int)mr;
     m->maxrow4 = (int)((mr + FG_GROUP - 1) / FG_GROUP * FG_GROUP);
-    if (m->maxrow4 <= 252) fg_build_halo(m);
     fg_sync(m);
   } catch (...) {
     fg_mesh_destroy(m);
@@ -2338,7 +2338,7 @@ fg_status fg_autotune_spmv64(fg_mesh *m, int reps, int *chosen, double *us_per_v
   int best = 0;
   double best_us = 1e30;
   for (int v = 0; v < FG_N_SPMV64; ++v) {
-    if (v == 1 && !m->halo_col) {
+    if (v == 1 && !fg_ensure_halo(m)) {
       if (us_per_variant) us_per_variant[v] = 0.0;
       continue;
     }
@@ -2369,7 +2369,7 @@ extern "C" fg_status fg_set_cg_variant(fg_mesh *m, int32_t precision, int32_t va
     } else {
       FG_REQUIRE(variant >= 0 && variant <= FG_N_SPMV64, FG_BAD_ARG, "fg_set_cg_variant: no such variant");
       if (variant == 0) { m->tuned64 = false; return FG_OK; }
-      FG_REQUIRE(variant != 2 || m->halo_col, FG_UNSUPPORTED, "fg_set_cg_variant: variant not available");
+      FG_REQUIRE(variant != 2 || fg_ensure_halo(m), FG_UNSUPPORTED, "fg_set_cg_variant: variant not available");
       m->spmv_variant64 = variant - 1;
       m->tuned64 = true;
     }
