@@ -952,6 +952,26 @@ void fg_set_nl_host(fg_mesh *m, const uint8_t *nl) {
 
 // The nonlinear element list of a mask and, when it differs from the list the maps
 // were built for, the slot and row maps of the split residual / Jacobian.
+// Indices 0..n-1 ordered by key (non-negative), equal keys in index order: an LSD
+// radix sort on 11-bit digits (a stable comparison sort of the ~16 entries per
+// nonlinear element took milliseconds on the host with the device idle).
+static std::vector<int> order_by_key(const std::vector<int> &key) {
+  const size_t n = key.size();
+  std::vector<int> ord(n), tmp(n);
+  for (size_t q = 0; q < n; ++q) ord[q] = (int)q;
+  int kmax = 0;
+  for (int k : key) kmax = std::max(kmax, k);
+  std::vector<size_t> count(2049);
+  for (int shift = 0; shift < 31 && (kmax >> shift) > 0; shift += 11) {
+    std::fill(count.begin(), count.end(), 0);
+    for (size_t q = 0; q < n; ++q) ++count[1 + ((key[ord[q]] >> shift) & 2047)];
+    for (int d = 0; d < 2048; ++d) count[d + 1] += count[d];
+    for (size_t q = 0; q < n; ++q) tmp[count[(key[ord[q]] >> shift) & 2047]++] = ord[q];
+    ord.swap(tmp);
+  }
+  return ord;
+}
+
 static void nl_maps(fg_mesh *m, const uint8_t *nl_host) {
   const int64_t nt = m->nt;
   // eight mask bytes per test: a sparse mask (a few nonlinear parts in a large
@@ -999,9 +1019,7 @@ static void nl_maps(fg_mesh *m, const uint8_t *nl_host) {
                                   m->stream));
       fg_sync(m);
       // slots: sources (e, a, b) grouped by position, in source order within a position
-      std::vector<int> ord(pos.size());
-      for (size_t q = 0; q < ord.size(); ++q) ord[q] = (int)q;
-      std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return pos[x] < pos[y]; });
+      const std::vector<int> ord = order_by_key(pos);
       std::vector<int> spos, sptr, scode, ssrc(ord.size());
       for (size_t q = 0; q < ord.size(); ++q) {
         const int src = ord[q];
@@ -1016,9 +1034,7 @@ static void nl_maps(fg_mesh *m, const uint8_t *nl_host) {
       }
       sptr.push_back((int)ord.size());
       // rows: sources (e, a) grouped by row
-      std::vector<int> rord(rows.size());
-      for (size_t q = 0; q < rord.size(); ++q) rord[q] = (int)q;
-      std::stable_sort(rord.begin(), rord.end(), [&](int x, int y) { return rows[x] < rows[y]; });
+      const std::vector<int> rord = order_by_key(rows);
       std::vector<int> rlist, rptr;
       for (size_t q = 0; q < rord.size(); ++q)
         if (q == 0 || rows[rord[q]] != rows[rord[q - 1]]) {
