@@ -41,12 +41,14 @@ import scipy.sparse as sp
 
 from . import _lib as L
 from .mesh import MESH, MU0, box_tet_mesh, box_tri_mesh  # noqa: F401
+from .meshio import load_mesh, save_mesh, save2file, load2array  # noqa: F401
 
 __all__ = [
     "GPUMesh", "gpu_mesh", "lagrange", "BoundaryIntegral", "stiffnessMatrix", "localStiffnessMatrix", "tangentialStiffnessMatrix", "massMatrix",
     "stiffnessMatrix2D", "massMatrix2D", "quadraticStiffnessMatrix", "quadraticMassMatrix",
     "quadraticStiffnessMatrix2D", "quadraticMassMatrix2D", "cg", "spmv", "magnetostatics_linear",
     "newton_magnetostatics", "ResidentNewton", "hfield", "heat_be", "adjoint_dJdmu", "magnetostaticField", "batch_magnetostatics_linear", "magnetostatics_sweep", "solve_opts", "newton_opts", "MESH", "MU0", "box_tet_mesh", "box_tri_mesh",
+    "load_mesh", "save_mesh", "save2file", "load2array",
 ]
 
 

@@ -306,6 +306,27 @@ function newton_magnetostatics(mesh, fixed::Vector{UInt8}, nl::Vector{UInt8}, mu
     return u, H, mu, s[]
 end
 
+# ---------------------------------------------------------------- mesh files
+# The arrays Femeko's `Mesh(...; saveMesh=true)` writes with save2file
+# (src/mesh.jl:233-242, src/geometry.jl:237-245: one line per row, entries joined by
+# " , "), read back as the fields of a MESH (1-based, as Julia holds them), so that a
+# mesh saved on a machine with Gmsh can be solved on the GPU elsewhere.
+function read_save2file(path::AbstractString, ::Type{T}=Float64) where {T}
+    rows = [parse.(T, strip.(split(l, ","))) for l in eachline(path) if !isempty(strip(l))]
+    isempty(rows) && return T[]
+    all(length(r) == length(rows[1]) for r in rows) || error("$path: rows of different lengths")
+    length(rows[1]) == 1 && return [r[1] for r in rows]
+    return permutedims(reduce(hcat, rows))
+end
+
+function load_saved_mesh(folder::AbstractString)
+    rd(name, T=Float64) = read_save2file(joinpath(folder, name * ".txt"), T)
+    asmat(a) = a isa AbstractVector ? reshape(a, :, 1) : a
+    return (t = Int32.(asmat(rd("t", Int64))), p = asmat(rd("p")), surfaceT = Int32.(asmat(rd("surfaceT", Int64))),
+            InsideNodes = Int32.(rd("InsideNodes", Int64)), InsideElements = Int32.(rd("InsideElements", Int64)),
+            VE = rd("VE"), AE = rd("AE"), normal = asmat(rd("normal")))
+end
+
 # ---------------------------------------------------------------- differentiation
 struct AdjointStats
     forward_iters::Int32
