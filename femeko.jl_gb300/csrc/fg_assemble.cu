@@ -194,9 +194,17 @@ __constant__ double c_gq2_w[6] = {0.223381589678011, 0.223381589678011, 0.223381
 // (src/FEM3D.jl:344-364).  ASM_MASS: 15-point rule, w = W_q/6 * VE * F
 // (src/FEM3D.jl:518-541); full_phi = 0 evaluates only S1 + S2 x + S3 y + S4 z of
 // each basis polynomial in global coordinates, as the reference's line break at
-// :529-531 makes Julia do.
+// :529-531 makes Julia do.  ASM_CONV: the convection matrix of
+// src/FEM3D.jl:563-648, C_ij = sum_q w (u_avg . grad phi_j) phi_i F with u_avg the
+// mean of the nodal velocity vel (3 x nv) over the 4 vertices, the same rule and the
+// same phi (truncated at :610-613 unless full_phi), grad phi the full quadratic's.
+// The reference flattens Ck column-major (:640) but scatters entry n = 10(i-1)+j to
+// (t_i, t_j) (:644-648), so its global C[t_i, t_j] sums Ck[j, i].  The row gather of
+// untransposed records therefore builds C^T, whose rows are C's CSC columns (the
+// export); transpose = 1 records Ck^T, giving the rows of C itself for a solve.
 __global__ void k_elem_tet10(int kind, int full_phi, int64_t nt, const double *__restrict__ p,
                              const int *__restrict__ t, const double *__restrict__ geo, const double *__restrict__ f,
+                             const double *__restrict__ vel, int transpose, int accumulate,
                              const int *__restrict__ recpos, double *__restrict__ rec, int *flags) {
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nt) return;
@@ -232,6 +240,49 @@ __global__ void k_elem_tet10(int kind, int full_phi, int64_t nt, const double *_
     }
     for (int i = 0; i < 10; ++i)
       for (int j = i; j < 10; ++j) { Ke[i][j] = Ke[i][j] / 10.0 * fk * VE; Ke[j][i] = Ke[i][j]; }
+  } else if (kind == ASM_CONV) {
+    double ua[3];
+    for (int c = 0; c < 3; ++c)
+      ua[c] = 0.25 * (vel[3 * nds[0] + c] + vel[3 * nds[1] + c] + vel[3 * nds[2] + c] + vel[3 * nds[3] + c]);
+    double e1 = p[3 * nds[1]] - x0, e2 = p[3 * nds[2]] - x0, e3 = p[3 * nds[3]] - x0;
+    double f1 = p[3 * nds[1] + 1] - y0, f2 = p[3 * nds[2] + 1] - y0, f3 = p[3 * nds[3] + 1] - y0;
+    double g1 = p[3 * nds[1] + 2] - z0, g2 = p[3 * nds[2] + 2] - z0, g3 = p[3 * nds[3] + 2] - z0;
+    for (int q = 0; q < 15; ++q) {
+      const double xi = c_gq3_pts[q][0], eta = c_gq3_pts[q][1], ze = c_gq3_pts[q][2];
+      const double Xq = e1 * xi + e2 * eta + e3 * ze, Yq = f1 * xi + f2 * eta + f3 * ze,
+                   Zq = g1 * xi + g2 * eta + g3 * ze;
+      double phi[10], gu[10];
+      for (int a = 0; a < 10; ++a) {
+        const double s0 = S[a], s1 = S[10 + a], s2 = S[20 + a], s3 = S[30 + a], s4 = S[40 + a], s5 = S[50 + a],
+                     s6 = S[60 + a], s7 = S[70 + a], s8 = S[80 + a], s9 = S[90 + a];
+        if (full_phi) {
+          phi[a] = s0 + s1 * Xq + s2 * Yq + s3 * Zq + s4 * Xq * Xq + s5 * Xq * Yq + s6 * Xq * Zq + s7 * Yq * Yq +
+                   s8 * Yq * Zq + s9 * Zq * Zq;
+        } else {
+          // the constant and linear coefficients of the polynomial in global
+          // coordinates (value and gradient at the origin), evaluated at x_q
+          const double ox = -x0, oy = -y0, oz = -z0;
+          const double c0 = s0 + s1 * ox + s2 * oy + s3 * oz + s4 * ox * ox + s5 * ox * oy + s6 * ox * oz +
+                            s7 * oy * oy + s8 * oy * oz + s9 * oz * oz;
+          const double cx = s1 + 2 * s4 * ox + s5 * oy + s6 * oz, cy = s2 + 2 * s7 * oy + s5 * ox + s8 * oz,
+                       cz = s3 + 2 * s9 * oz + s6 * ox + s8 * oy;
+          phi[a] = c0 + cx * (Xq + x0) + cy * (Yq + y0) + cz * (Zq + z0);
+        }
+        const double gx = s1 + 2 * s4 * Xq + s5 * Yq + s6 * Zq, gy = s2 + 2 * s7 * Yq + s5 * Xq + s8 * Zq,
+                     gz = s3 + 2 * s9 * Zq + s6 * Xq + s8 * Yq;
+        gu[a] = ua[0] * gx + ua[1] * gy + ua[2] * gz;
+      }
+      const double w = c_gq3_w[q] / 6.0 * VE;
+      for (int i = 0; i < 10; ++i)
+        for (int j = 0; j < 10; ++j) Ke[i][j] += w * gu[j] * phi[i] * fk;
+    }
+    if (transpose)
+      for (int i = 0; i < 10; ++i)
+        for (int j = i + 1; j < 10; ++j) {
+          const double tmp = Ke[i][j];
+          Ke[i][j] = Ke[j][i];
+          Ke[j][i] = tmp;
+        }
   } else {
     // global-coordinate constant and linear coefficients (value and gradient at the origin)
     double e1 = p[3 * nds[1]] - x0, e2 = p[3 * nds[2]] - x0, e3 = p[3 * nds[3]] - x0;
@@ -271,7 +322,14 @@ __global__ void k_elem_tet10(int kind, int full_phi, int64_t nt, const double *_
     for (int i = 0; i < 10; ++i)
       for (int j = i + 1; j < 10; ++j) Ke[j][i] = Ke[i][j];
   }
-  for (int a = 0; a < 10; ++a) store_row<10, double>(rec, recpos[(int64_t)a * nt + k], Ke[a]);
+  if (accumulate) {
+    for (int a = 0; a < 10; ++a) {
+      double *r = rec + (int64_t)recpos[(int64_t)a * nt + k] * 10;
+      for (int j = 0; j < 10; ++j) r[j] += Ke[a][j];
+    }
+  } else {
+    for (int a = 0; a < 10; ++a) store_row<10, double>(rec, recpos[(int64_t)a * nt + k], Ke[a]);
+  }
 }
 
 // P2 triangle (6 nodes).  ASM_STIFF: 6-node equal-weight rule, /6
@@ -854,7 +912,7 @@ static void launch_row_any(fg_mesh *m, const R *rec, const double *rec_r, int ap
 
 // Element pass (FP64 records) for the given kind.
 static void launch_elem(fg_mesh *m, int kind, const double *d_f, const double *d_H, const double *d_dmu, double cm,
-                        double cs, int full_phi) {
+                        double cs, int full_phi, bool transpose) {
   fg_ensure_records(m);
   double *rec = static_cast<double *>(m->rec);
   unsigned g = grid_for(m->nt, 128);
@@ -865,9 +923,11 @@ static void launch_elem(fg_mesh *m, int kind, const double *d_f, const double *d
       k_elem_tri3<double><<<g, 128, 0, m->stream>>>(kind, m->nt, m->geo, d_f, cm, cs, m->recpos, rec);
       break;
     case 10:
-      FG_REQUIRE(kind == ASM_STIFF || kind == ASM_MASS, FG_UNSUPPORTED, "P2: stiffness and mass only");
+      FG_REQUIRE(kind == ASM_STIFF || kind == ASM_MASS || kind == ASM_CONV, FG_UNSUPPORTED,
+                 "P2 tetrahedra: stiffness, mass and convection only");
       k_elem_tet10<<<grid_for(m->nt, 64), 64, 0, m->stream>>>(kind, full_phi, m->nt, m->p, m->t, m->geo, d_f,
-                                                               m->recpos, rec, m->flags);
+                                                               kind == ASM_CONV ? d_H : nullptr, transpose ? 1 : 0,
+                                                               0, m->recpos, rec, m->flags);
       break;
     default:
       FG_REQUIRE(kind == ASM_STIFF || kind == ASM_MASS, FG_UNSUPPORTED, "P2: stiffness and mass only");
@@ -883,7 +943,7 @@ void fg_assemble_operator(fg_mesh *m, int kind, const double *d_f, const double 
                           double c_mass, double c_stiff, int full_phi, int layout, bool want64, bool want32,
                           bool apply_bc) {
   if (layout != OUT_CSR) { m->op_tag = 0; ++m->op_version; }
-  launch_elem(m, kind, d_f, d_H, d_dmu, c_mass, c_stiff, full_phi);
+  launch_elem(m, kind, d_f, d_H, d_dmu, c_mass, c_stiff, full_phi, kind == ASM_CONV && layout != OUT_CSR);
   const double *rec = static_cast<const double *>(m->rec);
   if (layout == OUT_CSR) {
     if (!m->csrval) m->csrval = dev_alloc<double>(m, (size_t)m->nnz);
@@ -893,6 +953,95 @@ void fg_assemble_operator(fg_mesh *m, int kind, const double *d_f, const double 
     launch_row_any<double, double>(m, rec, nullptr, apply_bc ? 1 : 0, want64 ? m->val64 : nullptr,
                                    want32 ? m->val32 : nullptr, nullptr, m->dinv64, m->dinv32, nullptr, 0.0, 0);
   }
+}
+
+void fg_transport_operator(fg_mesh *m, const double *d_rhocp, const double *d_kdt, const double *d_vel,
+                           const double *d_fdt, int full_phi) {
+  FG_REQUIRE(m->npe == 10, FG_UNSUPPORTED, "transport operator: P2 tetrahedra only");
+  m->op_tag = 0;
+  ++m->op_version;
+  fg_ensure_records(m);
+  ensure_operator(m, true, false);
+  if (!m->mval) m->mval = dev_alloc<double>(m, (size_t)m->nsell);
+  double *rec = static_cast<double *>(m->rec);
+  const unsigned g = grid_for(m->nt, 64);
+  // records: M; gathered alone into mval, then + K + C^ on the same records
+  k_elem_tet10<<<g, 64, 0, m->stream>>>(ASM_MASS, full_phi, m->nt, m->p, m->t, m->geo, d_rhocp, nullptr, 0, 0,
+                                        m->recpos, rec, m->flags);
+  FG_CUDA_TRY(cudaGetLastError());
+  launch_row_any<double, double>(m, rec, nullptr, 0, m->mval, nullptr, nullptr, nullptr, nullptr, nullptr, 0.0, 0);
+  k_elem_tet10<<<g, 64, 0, m->stream>>>(ASM_STIFF, full_phi, m->nt, m->p, m->t, m->geo, d_kdt, nullptr, 0, 1,
+                                        m->recpos, rec, m->flags);
+  FG_CUDA_TRY(cudaGetLastError());
+  k_elem_tet10<<<g, 64, 0, m->stream>>>(ASM_CONV, full_phi, m->nt, m->p, m->t, m->geo, d_fdt, d_vel, 1, 1,
+                                        m->recpos, rec, m->flags);
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(3);
+  launch_row_any<double, double>(m, rec, nullptr, 0, m->val64, nullptr, nullptr, m->dinv64, nullptr, nullptr, 0.0, 0);
+}
+
+// src/FEM3D.jl:300-322 quadraticBoundaryMassMatrix: face-local matrix (1/180) c_ij
+// with c = 6 on the vertex diagonal, -1 between vertices, -4 between a vertex and
+// the midpoint of the opposite edge, 0 between a vertex and an adjacent midpoint,
+// 32 on the midpoint diagonal and 16 between midpoints; face nodes ordered
+// (v1, v2, v3, m12, m23, m31); entry AE[s] Mk[i,j] F[s].
+__device__ __forceinline__ double face_mass_coef(int i, int j) {
+  if (i < 3 && j < 3) return i == j ? 6.0 : -1.0;
+  if (i >= 3 && j >= 3) return i == j ? 32.0 : 16.0;
+  const int v = i < 3 ? i : j, e = (i < 3 ? j : i) - 3;
+  return ((e + 2) % 3 == v) ? -4.0 : 0.0;
+}
+
+// One thread per listed row: adds its faces' entries, in face order, into the row
+// (SELL values, then the Jacobi inverse from the row's diagonal slot; or CSR values).
+__global__ void k_face_mass(int64_t nrows, const int *__restrict__ rows, const int *__restrict__ fptr,
+                            const int *__restrict__ flist, const int *__restrict__ faces,
+                            const double *__restrict__ AE, const double *__restrict__ F, double scale,
+                            const int *__restrict__ sl_ptr, const int *__restrict__ sl_col,
+                            const int16_t *__restrict__ sl_dcol, const int *__restrict__ rowlen,
+                            const uint8_t *__restrict__ diagk, double *__restrict__ val, double *__restrict__ dinv,
+                            const int *__restrict__ rowptr, const int *__restrict__ colidx, double *__restrict__ csr,
+                            int *flags) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= nrows) return;
+  const int r = rows[idx];
+  const int s = r >> 5, lane = r & 31;
+  for (int e = fptr[idx]; e < fptr[idx + 1]; ++e) {
+    const int face = flist[e] >> 3, li = flist[e] & 7;
+    for (int j = 0; j < 6; ++j) {
+      const double c = face_mass_coef(li, j);
+      if (c == 0.0) continue;
+      const double v = scale * (AE[face] * ((1.0 / 180.0) * c) * F[face]);
+      const int col = faces[6 * (int64_t)face + j];
+      int64_t pos = -1;
+      if (csr) {
+        for (int q = rowptr[r]; q < rowptr[r + 1]; ++q)
+          if (colidx[q] == col) { pos = q; break; }
+      } else {
+        for (int q = 0; q < rowlen[r]; ++q) {
+          const int64_t sp = sell_pos(sl_ptr[s], lane, q);
+          const int cq = sl_col ? sl_col[sp] : r + (int)sl_dcol[sp];
+          if (cq == col) { pos = sp; break; }
+        }
+      }
+      if (pos < 0) { atomicOr(flags, FLAG_BAD_FACE); continue; }
+      if (csr) csr[pos] += v; else val[pos] += v;
+    }
+  }
+  if (!csr) dinv[r] = 1.0 / val[sell_pos(sl_ptr[s], lane, diagk[r])];
+}
+
+void fg_face_mass(fg_mesh *m, bool sell, const int *d_rows, int64_t nrows, const int *d_fptr, const int *d_flist,
+                  const int *d_faces, const double *d_AE, const double *d_F, double scale) {
+  if (nrows == 0) return;
+  FG_REQUIRE(!sell || m->val64, FG_BAD_ARG, "boundary mass: no FP64 operator assembled");
+  if (!sell && !m->csrval) m->csrval = dev_alloc<double>(m, (size_t)m->nnz);
+  k_face_mass<<<grid_for(nrows, 128), 128, 0, m->stream>>>(
+      nrows, d_rows, d_fptr, d_flist, d_faces, d_AE, d_F, scale, m->sl_ptr, m->use_dcol ? nullptr : m->sl_col,
+      m->sl_dcol, m->rowlen, m->diagk, m->val64, m->dinv64, m->rowptr, m->colidx, sell ? nullptr : m->csrval,
+      m->flags);
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(1);
 }
 
 void fg_newton_assemble(fg_mesh *m, const double *d_u, double Ms, double Hk, bool mixed, double *d_F,
@@ -1259,6 +1408,22 @@ extern "C" fg_status fg_mass(fg_mesh *m, const double *f, int32_t full_phi, doub
     return export_csr(m, nzval, "fg_mass");
   });
   if (tf) cudaFree(tf);
+  return st;
+}
+
+extern "C" fg_status fg_convection(fg_mesh *m, const double *vel, const double *f, int32_t full_phi,
+                                   double *nzval) {
+  double *tf = nullptr, *tv = nullptr;
+  fg_status st = fg_guard([&]() -> fg_status {
+    FG_REQUIRE(m && vel && nzval, FG_BAD_ARG, "fg_convection: null pointer");
+    FG_REQUIRE(m->npe == 10, FG_UNSUPPORTED, "fg_convection: P2 tetrahedra only (src/FEM3D.jl:563-648)");
+    double *df = upload_opt(m, f, (size_t)m->nt, tf);
+    double *dv = upload_opt(m, vel, 3 * (size_t)m->nv, tv);
+    fg_assemble_operator(m, ASM_CONV, df, dv, nullptr, 0.0, 0.0, full_phi, OUT_CSR, false, false, false);
+    return export_csr(m, nzval, "fg_convection");
+  });
+  if (tf) cudaFree(tf);
+  if (tv) cudaFree(tv);
   return st;
 }
 

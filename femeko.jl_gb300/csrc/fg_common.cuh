@@ -54,7 +54,8 @@ enum {
   FLAG_DEGENERATE = 2,  // zero-volume element
   FLAG_ROW_OVERFLOW = 4,// a row longer than the supported maximum
   FLAG_NAN = 8,         // NaN/Inf in a permeability or residual
-  FLAG_DUP_NODE = 16    // an element lists the same node twice
+  FLAG_DUP_NODE = 16,   // an element lists the same node twice
+  FLAG_BAD_FACE = 32    // a boundary face pair that is not in the matrix pattern
 };
 
 // Longest matrix row the pattern builder accepts (slot positions fit a byte).
@@ -197,6 +198,12 @@ struct fg_mesh {
 
   // vectors
   double *v64[16] = {nullptr};
+  // BiCGStab vectors (padded to nvp), the mass values of the transport operator
+  // (SELL layout) and the captured iteration graph
+  double *bcg[10] = {nullptr};
+  double *mval = nullptr;
+  cudaGraphExec_t bcg_exec = nullptr;
+  bool bcg_dcol = false;
   float *v32[8] = {nullptr};
 
   // reductions and CG control
@@ -266,7 +273,7 @@ void fg_build_halo(fg_mesh *m);
 bool fg_ensure_halo(fg_mesh *m);
 
 // assembly (fg_assemble.cu)
-enum AsmKind { ASM_STIFF = 0, ASM_MASS = 1, ASM_TANGENT = 2, ASM_HEAT = 3 };
+enum AsmKind { ASM_STIFF = 0, ASM_MASS = 1, ASM_TANGENT = 2, ASM_HEAT = 3, ASM_CONV = 4 };
 enum OutLayout { OUT_SELL = 0, OUT_CSR = 1 };
 void fg_assemble_operator(fg_mesh *m, int kind, const double *d_f, const double *d_H, const double *d_dmu,
                           double c_mass, double c_stiff, int full_phi, int layout, bool want64, bool want32,
@@ -322,3 +329,19 @@ void fg_raise_flags(fg_mesh *m, int h, const char *where);
 int fg_pcg_solve(fg_mesh *m, const double *d_b, double *d_x, const fg_solve_opts &o, fg_solve_stats *st,
                  bool newton_inner, double b_norm = -1.0);
 void fg_spmv64_dev(fg_mesh *m, const double *x, double *y);
+// y = A x with the given SELL values and no Dirichlet masking
+void fg_spmv64_plain(fg_mesh *m, const double *vals, const double *x, double *y);
+// Jacobi right-preconditioned BiCGStab on the FP64 operator (val64, dinv64), no
+// Dirichlet rows; d_x holds the initial guess and receives the solution.
+// Returns 0 converged, 1 iteration limit, 2 breakdown.
+int fg_bicgstab_solve(fg_mesh *m, const double *d_b, double *d_x, const fg_solve_opts &o, fg_solve_stats *st);
+// Backward-Euler transport operator of P2 tetrahedra: mval = M(rho_cp) and
+// val64/dinv64 = M(rho_cp) + K(kdt) + C^(fdt) (the reference's convection matrix with
+// the factor fdt), no boundary conditions.
+void fg_transport_operator(fg_mesh *m, const double *d_rhocp, const double *d_kdt, const double *d_vel,
+                           const double *d_fdt, int full_phi);
+// Adds scale * (the P2 boundary mass of the listed faces) into val64 (refreshing
+// dinv64) when sell, else writes it alone into csrval.  Row list rows[0..nrows), each
+// row's (face << 3 | face-local node) entries in flist[fptr[i]..fptr[i+1]).
+void fg_face_mass(fg_mesh *m, bool sell, const int *d_rows, int64_t nrows, const int *d_fptr, const int *d_flist,
+                  const int *d_faces, const double *d_AE, const double *d_F, double scale);

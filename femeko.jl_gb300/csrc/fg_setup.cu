@@ -67,6 +67,7 @@ void fg_raise_flags(fg_mesh *m, int h, const char *where) {
   if (h & FLAG_DEGENERATE) throw FgError{FG_BAD_MESH, w + ": degenerate (zero-volume) element"};
   if (h & FLAG_ROW_OVERFLOW) throw FgError{FG_BAD_MESH, w + ": a matrix row exceeds 255 entries"};
   if (h & FLAG_NAN) throw FgError{FG_NAN, w + ": NaN/Inf in permeability or residual"};
+  if (h & FLAG_BAD_FACE) throw FgError{FG_BAD_ARG, w + ": a boundary face is not a face of an element"};
   throw FgError{FG_BAD_MESH, w + ": device error flag"};
 }
 
@@ -463,6 +464,7 @@ static void free_mesh(fg_mesh *m) {
   if (!m) return;
   for (int g = 0; g < 4; ++g)
     if (m->graph[g].exec) cudaGraphExecDestroy(m->graph[g].exec);
+  if (m->bcg_exec) cudaGraphExecDestroy(m->bcg_exec);
   if (m->stream) {
     for (void *ptr : m->extra) cudaFreeAsync(ptr, m->stream);
     cudaStreamSynchronize(m->stream);

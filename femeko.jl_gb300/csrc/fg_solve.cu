@@ -2408,3 +2408,257 @@ extern "C" fg_status fg_autotune(fg_mesh *m, int32_t precision, int32_t *variant
     return st;
   });
 }
+
+// ------------------------------------------------------------------ BiCGStab (FP64)
+// Jacobi right-preconditioned BiCGStab (van der Vorst 1992) for the nonsymmetric
+// backward-Euler transport operator.  One iteration is five kernels, each reading
+// the scalars the previous one finished on the device:
+//   p = r + beta (p - omega v), ph = D p          k_bcg_p
+//   v = A ph, alpha = rho / (rh . v)              k_bcg_spmv<0>
+//   s = r - alpha v, sh = D s                     k_bcg_s
+//   t = A sh, omega = (t . s) / (t . t)           k_bcg_spmv<1>
+//   x += alpha ph + omega sh, r = s - omega t,
+//   rho' = rh . r, beta = (rho'/rho)(alpha/omega) k_bcg_update
+// Every kernel returns at once when the control word says the solve is done, so a
+// captured body of several iterations can run past convergence at no cost.
+enum { Q_RHO = 0, Q_ALPHA, Q_OMEGA, Q_BETA, Q_RR, Q_TOL2, Q_BB };
+enum { BCG_X = 0, BCG_R, BCG_RH, BCG_P, BCG_PH, BCG_V, BCG_S, BCG_SH, BCG_T, BCG_B, BCG_NVEC };
+constexpr int FG_BCG_BODY = 8;  // iterations per captured graph body
+
+__global__ void __launch_bounds__(256) k_bcg_start(int64_t n, const double *__restrict__ b,
+                                                   const double *__restrict__ r, double *__restrict__ rh,
+                                                   double *__restrict__ p, double *__restrict__ v, double tol, int maxit,
+                                                   double *scal, int *ictl, double *partials, unsigned *counter) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double d[2] = {0.0, 0.0};
+  if (i < n) {
+    const double ri = r[i], bi = b[i];
+    rh[i] = ri;
+    p[i] = 0.0;
+    v[i] = 0.0;
+    d[0] = ri * ri;
+    d[1] = bi * bi;
+  }
+  __shared__ double sh[2][32];
+  block_sum<2>(d, sh);
+  double tot[2];
+  if (grid_finish<2>(d, partials, counter, tot)) {
+    const double tol2 = tol * tol * tot[1];
+    scal[Q_RHO] = tot[0];
+    scal[Q_ALPHA] = 1.0;
+    scal[Q_OMEGA] = 1.0;
+    scal[Q_BETA] = 0.0;
+    scal[Q_RR] = tot[0];
+    scal[Q_BB] = tot[1];
+    scal[Q_TOL2] = tol2;
+    ictl[I_ITERS] = 0;
+    ictl[I_MAXIT] = maxit;
+    ictl[I_STATUS] = isfinite(tot[0]) ? 0 : 2;
+    ictl[I_DONE] = (tot[0] <= tol2 || !isfinite(tot[0])) ? 1 : 0;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_bcg_p(int64_t n, const double *__restrict__ r, const double *__restrict__ v,
+                                               double *__restrict__ p, double *__restrict__ ph,
+                                               const double *__restrict__ dinv, const double *scal, const int *ictl) {
+  if (ictl[I_DONE]) return;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double beta = scal[Q_BETA], omega = scal[Q_OMEGA];
+  const double pi = r[i] + beta * (p[i] - omega * v[i]);
+  p[i] = pi;
+  ph[i] = dinv[i] * pi;
+}
+
+// MODE 0: y = v = A ph, alpha = rho / (rh . v).  MODE 1: y = t = A sh, omega = (t.s)/(t.t).
+template <class CI, int MODE>
+__global__ void __launch_bounds__(256) k_bcg_spmv(int64_t n, const int *__restrict__ sl_ptr,
+                                                  const int *__restrict__ sl_len, const typename CI::T *__restrict__ col,
+                                                  const double *__restrict__ val, const double *__restrict__ x,
+                                                  double *__restrict__ y, const double *__restrict__ w,
+                                                  double *scal, int *ictl, double *partials, unsigned *counter) {
+  if (ictl[I_DONE]) return;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double d[2] = {0.0, 0.0};
+  if (i < n) {
+    const int s = (int)(i >> 5), lane = (int)(i & 31);
+    const int64_t base = (int64_t)sl_ptr[s] + lane * FG_GROUP;
+    const int G = sl_len[s];
+    double acc = 0.0;
+    for (int g = 0; g < G; ++g) {
+      const typename CI::T4 cc = ld_cols(reinterpret_cast<const typename CI::T4 *>(col + base) + (int64_t)g * FG_SLICE);
+      const double *vg = val + base + (int64_t)g * FG_GROUP * FG_SLICE;
+      acc = fma(vg[0], x[CI::col(cc.x, i)], acc);
+      acc = fma(vg[1], x[CI::col(cc.y, i)], acc);
+      acc = fma(vg[2], x[CI::col(cc.z, i)], acc);
+      acc = fma(vg[3], x[CI::col(cc.w, i)], acc);
+    }
+    y[i] = acc;
+    d[0] = w[i] * acc;          // rh . v  or  s . t
+    d[1] = MODE ? acc * acc : 0.0;
+  }
+  __shared__ double sh[2][32];
+  block_sum<2>(d, sh);
+  double tot[2];
+  if (grid_finish<2>(d, partials, counter, tot)) {
+    if (MODE == 0) {
+      if (tot[0] == 0.0 || !isfinite(tot[0])) {
+        ictl[I_STATUS] = 2;
+        ictl[I_DONE] = 1;
+      } else {
+        scal[Q_ALPHA] = scal[Q_RHO] / tot[0];
+      }
+    } else {
+      scal[Q_OMEGA] = tot[1] > 0.0 ? tot[0] / tot[1] : 0.0;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_bcg_s(int64_t n, const double *__restrict__ r, const double *__restrict__ v,
+                                               double *__restrict__ s, double *__restrict__ sh,
+                                               const double *__restrict__ dinv, const double *scal, const int *ictl) {
+  if (ictl[I_DONE]) return;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double si = r[i] - scal[Q_ALPHA] * v[i];
+  s[i] = si;
+  sh[i] = dinv[i] * si;
+}
+
+__global__ void __launch_bounds__(256) k_bcg_update(int64_t n, double *__restrict__ x, double *__restrict__ r,
+                                                    const double *__restrict__ ph, const double *__restrict__ sh,
+                                                    const double *__restrict__ s, const double *__restrict__ t,
+                                                    const double *__restrict__ rh, double *scal, int *ictl,
+                                                    double *partials, unsigned *counter) {
+  if (ictl[I_DONE]) return;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double d[2] = {0.0, 0.0};
+  if (i < n) {
+    const double alpha = scal[Q_ALPHA], omega = scal[Q_OMEGA];
+    x[i] += alpha * ph[i] + omega * sh[i];
+    const double ri = s[i] - omega * t[i];
+    r[i] = ri;
+    d[0] = rh[i] * ri;
+    d[1] = ri * ri;
+  }
+  __shared__ double shd[2][32];
+  block_sum<2>(d, shd);
+  double tot[2];
+  if (grid_finish<2>(d, partials, counter, tot)) {
+    const int it = ++ictl[I_ITERS];
+    const double omega = scal[Q_OMEGA];
+    scal[Q_RR] = tot[1];
+    if (tot[1] <= scal[Q_TOL2]) {
+      ictl[I_STATUS] = 0;
+      ictl[I_DONE] = 1;
+    } else if (!isfinite(tot[1]) || tot[0] == 0.0 || omega == 0.0) {
+      ictl[I_STATUS] = 2;
+      ictl[I_DONE] = 1;
+    } else if (it >= ictl[I_MAXIT]) {
+      ictl[I_STATUS] = 1;
+      ictl[I_DONE] = 1;
+    } else {
+      scal[Q_BETA] = (tot[0] / scal[Q_RHO]) * (scal[Q_ALPHA] / omega);
+      scal[Q_RHO] = tot[0];
+    }
+  }
+}
+
+void fg_spmv64_plain(fg_mesh *m, const double *vals, const double *x, double *y) {
+  if (m->use_dcol)
+    k_spmv64<ColRel><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, vals, x, nullptr, y,
+                                                         nullptr, -1, m->scal, m->red.partials, m->red.counter);
+  else
+    k_spmv64<ColAbs><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col, vals, x, nullptr, y,
+                                                         nullptr, -1, m->scal, m->red.partials, m->red.counter);
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(1);
+}
+
+template <class CI>
+static void bcg_enqueue_body(fg_mesh *m, const typename CI::T *col) {
+  double **v = m->bcg;
+  const unsigned g = row_grid(m);
+  const int64_t n = m->nv;
+  for (int k = 0; k < FG_BCG_BODY; ++k) {
+    k_bcg_p<<<g, 256, 0, m->stream>>>(n, v[BCG_R], v[BCG_V], v[BCG_P], v[BCG_PH], m->dinv64, m->scal, m->ictl);
+    k_bcg_spmv<CI, 0><<<g, 256, 0, m->stream>>>(n, m->sl_ptr, m->sl_len, col, m->val64, v[BCG_PH], v[BCG_V],
+                                                v[BCG_RH], m->scal, m->ictl, m->red.partials, m->red.counter);
+    k_bcg_s<<<g, 256, 0, m->stream>>>(n, v[BCG_R], v[BCG_V], v[BCG_S], v[BCG_SH], m->dinv64, m->scal, m->ictl);
+    k_bcg_spmv<CI, 1><<<g, 256, 0, m->stream>>>(n, m->sl_ptr, m->sl_len, col, m->val64, v[BCG_SH], v[BCG_T],
+                                                v[BCG_S], m->scal, m->ictl, m->red.partials, m->red.counter);
+    k_bcg_update<<<g, 256, 0, m->stream>>>(n, v[BCG_X], v[BCG_R], v[BCG_PH], v[BCG_SH], v[BCG_S], v[BCG_T],
+                                           v[BCG_RH], m->scal, m->ictl, m->red.partials, m->red.counter);
+  }
+}
+
+static void bcg_body(fg_mesh *m) {
+  if (m->use_dcol) bcg_enqueue_body<ColRel>(m, m->sl_dcol);
+  else bcg_enqueue_body<ColAbs>(m, m->sl_col);
+}
+
+int fg_bicgstab_solve(fg_mesh *m, const double *d_b, double *d_x, const fg_solve_opts &o, fg_solve_stats *st) {
+  FG_REQUIRE(m->val64 && m->dinv64, FG_BAD_ARG, "BiCGStab: no FP64 operator assembled");
+  for (int j = 0; j < BCG_NVEC; ++j)
+    if (!m->bcg[j]) {
+      m->bcg[j] = dev_alloc<double>(m, (size_t)m->nvp);
+      FG_CUDA_TRY(cudaMemsetAsync(m->bcg[j], 0, sizeof(double) * (size_t)m->nvp, m->stream));
+    }
+  double **v = m->bcg;
+  const int64_t n = m->nv;
+  if (d_x != v[BCG_X])
+    FG_CUDA_TRY(cudaMemcpyAsync(v[BCG_X], d_x, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, m->stream));
+  if (d_b != v[BCG_B])
+    FG_CUDA_TRY(cudaMemcpyAsync(v[BCG_B], d_b, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, m->stream));
+  // r = b - A x
+  if (m->use_dcol)
+    k_spmv64<ColRel><<<row_grid(m), 256, 0, m->stream>>>(n, m->sl_ptr, m->sl_len, m->sl_dcol, m->val64, v[BCG_X],
+                                                         v[BCG_B], v[BCG_R], nullptr, -1, m->scal, m->red.partials,
+                                                         m->red.counter);
+  else
+    k_spmv64<ColAbs><<<row_grid(m), 256, 0, m->stream>>>(n, m->sl_ptr, m->sl_len, m->sl_col, m->val64, v[BCG_X],
+                                                         v[BCG_B], v[BCG_R], nullptr, -1, m->scal, m->red.partials,
+                                                         m->red.counter);
+  const int maxit = o.maxiter > 0 ? o.maxiter : (int)std::min<int64_t>(2 * n + 10, 1 << 30);
+  k_bcg_start<<<row_grid(m), 256, 0, m->stream>>>(n, v[BCG_B], v[BCG_R], v[BCG_RH], v[BCG_P], v[BCG_V], o.rtol, maxit,
+                                                  m->scal, m->ictl, m->red.partials, m->red.counter);
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(2);
+  if (!m->bcg_exec || m->bcg_dcol != m->use_dcol) {
+    if (m->bcg_exec) cudaGraphExecDestroy(m->bcg_exec);
+    m->bcg_exec = nullptr;
+    cudaGraph_t graph = nullptr;
+    FG_CUDA_TRY(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
+    bcg_body(m);
+    FG_CUDA_TRY(cudaStreamEndCapture(m->stream, &graph));
+    const cudaError_t e = cudaGraphInstantiate(&m->bcg_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    FG_CUDA_TRY(e);
+    m->bcg_dcol = m->use_dcol;
+  }
+  int *h = m->hint;
+  const int64_t max_bodies = maxit / FG_BCG_BODY + 2;
+  for (int64_t b = 0; b < max_bodies; ++b) {
+    FG_CUDA_TRY(cudaGraphLaunch(m->bcg_exec, m->stream));
+    FG_LAUNCHED(5 * FG_BCG_BODY);
+    FG_CUDA_TRY(cudaMemcpyAsync(h, m->ictl, sizeof(int) * 4, cudaMemcpyDeviceToHost, m->stream));
+    fg_sync(m);
+    if (h[I_DONE]) break;
+  }
+  FG_CUDA_TRY(cudaMemcpyAsync(m->hbuf, m->scal, sizeof(double) * 8, cudaMemcpyDeviceToHost, m->stream));
+  FG_CUDA_TRY(cudaMemcpyAsync(h, m->ictl, sizeof(int) * 4, cudaMemcpyDeviceToHost, m->stream));
+  if (d_x != v[BCG_X])
+    FG_CUDA_TRY(cudaMemcpyAsync(d_x, v[BCG_X], sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, m->stream));
+  fg_sync(m);
+  const int status = h[I_DONE] ? h[I_STATUS] : 1;
+  if (st) {
+    st->iterations = h[I_ITERS];
+    st->refinements = 0;
+    st->converged = status == 0;
+    st->pad_ = 0;
+    const double bb = m->hbuf[Q_BB];
+    st->relres = bb > 0.0 ? std::sqrt(m->hbuf[Q_RR] / bb) : std::sqrt(m->hbuf[Q_RR]);
+    st->ms = 0.f;
+  }
+  return status;
+}

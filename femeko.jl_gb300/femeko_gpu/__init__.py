@@ -40,11 +40,11 @@ import numpy as np
 import scipy.sparse as sp
 
 from . import _lib as L
-from .mesh import MESH, MU0, box_tet_mesh, box_tri_mesh  # noqa: F401
+from .mesh import MESH, MU0, box_tet_mesh, box_tri_mesh, surface_faces6  # noqa: F401
 from .meshio import load_mesh, save_mesh, save2file, load2array  # noqa: F401
 
 __all__ = [
-    "GPUMesh", "gpu_mesh", "lagrange", "BoundaryIntegral", "stiffnessMatrix", "localStiffnessMatrix", "tangentialStiffnessMatrix", "massMatrix",
+    "GPUMesh", "gpu_mesh", "lagrange", "BoundaryIntegral", "stiffnessMatrix", "localStiffnessMatrix", "tangentialStiffnessMatrix", "quadraticConvectionMatrix", "quadraticBoundaryMassMatrix", "transport_be", "surface_faces6", "massMatrix",
     "stiffnessMatrix2D", "massMatrix2D", "quadraticStiffnessMatrix", "quadraticMassMatrix",
     "quadraticStiffnessMatrix2D", "quadraticMassMatrix2D", "cg", "spmv", "magnetostatics_linear",
     "newton_magnetostatics", "ResidentNewton", "hfield", "heat_be", "adjoint_dJdmu", "magnetostaticField", "batch_magnetostatics_linear", "magnetostatics_sweep", "solve_opts", "newton_opts", "MESH", "MU0", "box_tet_mesh", "box_tri_mesh",
@@ -140,6 +140,15 @@ def massMatrix(mesh: MESH, F=None, full_phi: bool = False):
 massMatrix2D = massMatrix
 quadraticMassMatrix = massMatrix
 quadraticMassMatrix2D = massMatrix
+
+
+def quadraticConvectionMatrix(mesh: MESH, u, F=None, full_phi: bool = False):
+    """Global P2 convection matrix of the nodal velocity ``u`` (3 x nv), as
+    src/FEM3D.jl:563-648 builds it (entry (t_i, t_j) sums the local Ck[j, i];
+    ``full_phi=False`` keeps the reference's linear-part-only phi)."""
+    uv = _c(np.asarray(u, dtype=np.float64).T, np.float64)   # 3 x nv column-major
+    fv = None if F is None else _c(F, np.float64)
+    return _assemble(mesh, L.lib().fg_convection, L.ptr(uv), L.ptr(fv), int(full_phi))
 
 
 def tangentialStiffnessMatrix(mesh: MESH, H_vec, dmu):
@@ -272,6 +281,48 @@ def heat_be(mesh: MESH, T0, kappa, rho_c=1.0, dt=1e-3, nsteps=100, every=10, pre
                             L.ptr(snaps) if nsnap else None, C.byref(o), C.byref(s))
     L.check(st, allow_not_converged=True)
     return T, snaps[:nsnap], L.stats_dict(s)
+
+
+def quadraticBoundaryMassMatrix(mesh: MESH, F=None, faces=None):
+    """P2 boundary mass of the surface triangles (src/FEM3D.jl:300-322) with the
+    per-face factor F (ns, default ones); ``faces`` (6 x ns) defaults to
+    ``surface_faces6(mesh)``."""
+    g = gpu_mesh(mesh)
+    f6 = surface_faces6(mesh) if faces is None else np.asarray(faces)
+    ns = f6.shape[1]
+    vals = np.zeros(g.nnz)
+    Fv = None if F is None else _c(F, np.float64)
+    L.check(L.lib().fg_boundary_mass(g.h, L.ptr(_c(f6.T, np.int32)), L.ptr(_c(mesh.AE[:ns], np.float64)),
+                                     L.ptr(Fv), ns, L.ptr(vals)))
+    return g.csc(vals)
+
+
+def transport_be(mesh: MESH, T0, rho_cp, kappa, u, dt, nsteps, face_F=None, faces=None, full_phi=True, every=0,
+                 rtol=1e-10, maxiter=10_000):
+    """Backward-Euler transport steps T <- LM \\ (M T), LM = M + dt (A + R + C)
+    (Transport/main3D.jl:143-213) with Jacobi-BiCGStab on the GPU.  u: 3 x nv velocity;
+    face_F: per-surface-face penalty factor (the reference's intakeBC; None = no R).
+    Returns (T_final, snapshots every `every` steps, stats with "status" 0/1/2)."""
+    g = gpu_mesh(mesh)
+    T = _c(T0, np.float64).copy()
+    nsnap = nsteps // every if every > 0 else 0
+    snaps = np.zeros((max(nsnap, 1), mesh.nv))
+    if face_F is None:
+        f6, AE, Fv, nf = None, None, None, 0
+    else:
+        f6 = _c((surface_faces6(mesh) if faces is None else np.asarray(faces)).T, np.int32)
+        nf = f6.shape[0]
+        AE, Fv = _c(mesh.AE[:nf], np.float64), _c(face_F, np.float64)
+    uv = _c(np.asarray(u, dtype=np.float64).T, np.float64)
+    o = solve_opts(precision="fp64", rtol=rtol, maxiter=maxiter)
+    s = L.SolveStats()
+    st = L.lib().fg_transport_be(g.h, L.ptr(_c(rho_cp, np.float64)), L.ptr(_c(kappa, np.float64)), L.ptr(uv),
+                                 L.ptr(f6), L.ptr(AE), L.ptr(Fv), nf, float(dt), int(nsteps), int(full_phi),
+                                 L.ptr(T), every, L.ptr(snaps) if nsnap else None, C.byref(o), C.byref(s))
+    L.check(st, allow_not_converged=True)
+    d = L.stats_dict(s)
+    d["status"] = s.pad_
+    return T, snaps[:nsnap], d
 
 
 def magnetostatics_sweep(mesh: MESH, mu, H0, rtol=1e-10, inner_rtol=1e-5, maxiter=1_000_000, check_every=16):

@@ -82,6 +82,7 @@ SIGNATURES = {
     "fg_stiffness": [_vp, _vp, _vp],
     "fg_mass": [_vp, _vp, _i32, _vp],
     "fg_tangent": [_vp, _vp, _vp, _vp],
+    "fg_convection": [_vp, _vp, _vp, _i32, _vp],
     "fg_local_stiffness": [_vp, _vp, _vp],
     "fg_lagrange": [_vp, _vp],
     "fg_boundary_integral": [_vp, _vp, _i64, _i32, _vp, _vp, _vp, _vp, _i32, _vp],
@@ -96,6 +97,9 @@ SIGNATURES = {
     "fg_newton_solve_resident": [_vp, C.POINTER(NewtonOpts), C.POINTER(NewtonStats)],
     "fg_newton_get_outputs": [_vp, _vp, _vp, _vp],
     "fg_heat_be": [_vp, _vp, _d, _d, _i32, _vp, _i32, _vp, C.POINTER(SolveOpts), C.POINTER(SolveStats)],
+    "fg_boundary_mass": [_vp, _vp, _vp, _vp, _i64, _vp],
+    "fg_transport_be": [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _d, _i32, _i32, _vp, _i32, _vp,
+                        C.POINTER(SolveOpts), C.POINTER(SolveStats)],
     "fg_batch_magnetostatics_linear": [_vp, _i32, _vp, _vp, C.POINTER(SolveOpts), _vp, _vp, C.POINTER(BatchStats)],
     "fg_magnetostatics_sweep": [_vp, _vp, _i32, _vp, C.POINTER(SolveOpts), _vp, C.POINTER(SolveStats)],
     "fg_adjoint_dJdmu": [_vp, _vp, _vp, _vp, _vp, C.POINTER(NewtonOpts), _d, C.POINTER(_d), _vp, _vp,

@@ -290,3 +290,30 @@ def box_tri_mesh(n: int, seed: int = 0, jitter: float = 0.1, half_width: float =
                 surfaceT=surfaceT, elementID=elementID, InsideElements=inside_el,
                 InsideNodes=inside_nodes, VE=VE, AE=AE, normal=normal, shell_id=(1,),
                 boundary_nodes=np.sort(boundary).astype(np.int32), cells=n, half_width=half_width)
+
+
+def surface_faces6(mesh) -> np.ndarray:
+    """6 x ns face nodes of a P2 tetrahedral mesh's surface triangles, in the order of
+    the reference's P2 ``surfaceT`` rows 1-6: the three vertices, then the midpoints of
+    edges 12, 23 and 31 (``src/FEM3D.jl:300-322`` reads them so).  The midpoints are
+    found among the elements' edge nodes."""
+    if mesh.t.shape[0] != 10:
+        raise ValueError("surface_faces6: P2 tetrahedra only")
+    t = np.asarray(mesh.t, dtype=np.int64)
+    nv = mesh.nv
+    va = np.concatenate([t[a] for a, b in TET10_EDGES])
+    vb = np.concatenate([t[b] for a, b in TET10_EDGES])
+    mid = np.concatenate([t[4 + e] for e in range(len(TET10_EDGES))])
+    key = np.minimum(va, vb) * nv + np.maximum(va, vb)
+    order = np.argsort(key, kind="stable")
+    key, mid = key[order], mid[order]
+    fv = np.asarray(mesh.surfaceT[:3], dtype=np.int64)
+    out = np.zeros((6, fv.shape[1]), dtype=np.int32)
+    out[:3] = fv
+    for r, (i, j) in enumerate(((0, 1), (1, 2), (2, 0))):
+        fk = np.minimum(fv[i], fv[j]) * nv + np.maximum(fv[i], fv[j])
+        pos = np.minimum(np.searchsorted(key, fk), key.size - 1)
+        if np.any(key[pos] != fk):
+            raise ValueError("surface_faces6: a surface edge is not an element edge")
+        out[3 + r] = mid[pos]
+    return out

@@ -173,6 +173,12 @@ fg_status fg_stiffness(fg_mesh *m, const double *f, double *nzval);
  * reference's linear-part-only phi of :529-531, 1 evaluates the full quadratic),
  * src/FEM2D.jl:163-229 quadraticMassMatrix2D.  f: per-element factor or NULL. */
 fg_status fg_mass(fg_mesh *m, const double *f, int32_t full_phi, double *nzval);
+/* src/FEM3D.jl:563-648 quadraticConvectionMatrix (P2 tetrahedra): vel is the
+ * nodal velocity, 3 x nv column-major; f per-element factor or NULL; full_phi as
+ * for fg_mass (the reference's phi at :610-613 keeps the linear part only).  The
+ * values are those of the reference's C, whose entry (t_i, t_j) sums the local
+ * Ck[j, i] (:640-648), in the order of fg_csc_pattern. */
+fg_status fg_convection(fg_mesh *m, const double *vel, const double *f, int32_t full_phi, double *nzval);
 /* src/FEM3D.jl:79-119 tangentialStiffnessMatrix (P1 tet): H is 3 x nt, dmu nt.
  * Where |H| = 0 the stored term is its limit 0. */
 fg_status fg_tangent(fg_mesh *m, const double *H, const double *dmu, double *nzval);
@@ -245,6 +251,32 @@ fg_status fg_newton_magnetostatics(fg_mesh *m, const uint8_t *nl, const double *
  * stats accumulate over the steps. */
 fg_status fg_heat_be(fg_mesh *m, const double *kappa, double rho_c, double dt, int32_t nsteps, double *T,
                      int32_t every, double *snapshots, const fg_solve_opts *o, fg_solve_stats *s);
+
+/* src/FEM3D.jl:300-322 quadraticBoundaryMassMatrix: faces is 6 x nfaces (0-based,
+ * column-major; the first six rows of the reference's P2 surfaceT: vertices, then the
+ * midpoints of edges 12, 23, 31), AE the face areas, F the per-face factor (NULL =
+ * ones).  Entry AE[s] Mk[i,j] F[s] with Mk the P2 triangle mass of :303-308; values in
+ * the order of fg_csc_pattern (a face pair outside the pattern is FG_BAD_ARG). */
+fg_status fg_boundary_mass(fg_mesh *m, const int32_t *faces, const double *AE, const double *F, int64_t nfaces,
+                           double *nzval);
+
+/* Heat transport with convection on P2 tetrahedra (Transport/main3D.jl:143-213):
+ * LM = M(rho_cp) + dt (A(kappa) + R + C(vel, rho_cp)), then nsteps steps of
+ * T <- LM \ (M T) (main3D.jl:199-204), each solved by Jacobi-preconditioned BiCGStab
+ * (FP64, started from the previous T) to ||M T_n - LM T|| <= o->rtol ||M T_n||
+ * (o->maxiter iterations per step; precision, spmv and graph options are ignored).
+ * rho_cp, kappa: nt; vel: 3 x nv column-major; faces/AE/F: the penalty faces and
+ * factors of fg_boundary_mass (nfaces may be 0).  full_phi as for fg_mass: the
+ * reference's linear-part-only phi (0) gives an operator on which the iteration can
+ * fail where the reference's direct solve does not; 1 is the full P2 basis.  T (nv)
+ * holds the initial field and receives the last one; snapshots as for fg_heat_be.
+ * stats: iterations summed over the steps, the last step's relres, ms the device time
+ * from the assembly to the last solve; FG_NOT_CONVERGED if a step stopped short
+ * (pad_ = 1 iteration limit, 2 breakdown). */
+fg_status fg_transport_be(fg_mesh *m, const double *rho_cp, const double *kappa, const double *vel,
+                          const int32_t *faces, const double *AE, const double *F, int64_t nfaces, double dt,
+                          int32_t nsteps, int32_t full_phi, double *T, int32_t every, double *snapshots,
+                          const fg_solve_opts *o, fg_solve_stats *s);
 
 /* A sweep of applied fields on one linear mesh (the hysteresis-loop use of
  * Magnetostatics/magneticField.jl:89-132): for field c, K(mu) u_c = 0 on the free

@@ -429,6 +429,59 @@ long or_p2_mass(const double *p, const int *t, int nv, long nt, const double *VE
   return nnz;
 }
 
+/* src/FEM3D.jl:563-648 quadraticConvectionMatrix.  u is the nodal velocity     */
+/* (3 x nv, column k at u + 3k); u_avg is the mean over the 4 vertices           */
+/* (src/FEM.jl:13-30: ((u1 + u2) + u3) + u4, then /4).  phi as in the mass       */
+/* matrix (linear part only unless full_phi, :610-613), gradPhi the full         */
+/* quadratic's (:616-618), w = weights[q] VE, Ck[i][j] += w (u_avg . gradPhi_j)   */
+/* phi_i F.  The reference flattens Ck column-major (:640) and scatters entry    */
+/* n = 10(i-1)+j to (t_i, t_j) (:644-648), so C[t_i, t_j] sums Ck[j][i]: the      */
+/* local values below are stored transposed to build that same C.               */
+long or_p2_convection(const double *p, const int *t, int nv, long nt, const double *VE, const double *u,
+                      const double *F, int full_phi, long *colptr, int *rowval, double *nzval) {
+  double *Ck = (double *)malloc(sizeof(double) * 100 * (size_t)nt);
+#pragma omp parallel for schedule(static)
+  for (long k = 0; k < nt; ++k) {
+    const int *nds = t + 10 * k;
+    double zero[3] = {0, 0, 0};
+    double S[10][10];
+    for (int a = 0; a < 10; ++a) p2_basis3d(p, nds, a, zero, S[a]);
+    const double *v1 = p + 3 * nds[0], *v2 = p + 3 * nds[1], *v3 = p + 3 * nds[2], *v4 = p + 3 * nds[3];
+    double J[3][3];
+    for (int r = 0; r < 3; ++r) { J[r][0] = v2[r] - v1[r]; J[r][1] = v3[r] - v1[r]; J[r][2] = v4[r] - v1[r]; }
+    double ua[3];
+    for (int c = 0; c < 3; ++c)
+      ua[c] = (((u[3 * nds[0] + c] + u[3 * nds[1] + c]) + u[3 * nds[2] + c]) + u[3 * nds[3] + c]) / 4.0;
+    double C[10][10];
+    memset(C, 0, sizeof(C));
+    double f = F ? F[k] : 1.0;
+    for (int q = 0; q < 15; ++q) {
+      double xi = GQ3_PTS[q][0], eta = GQ3_PTS[q][1], ze = GQ3_PTS[q][2];
+      double x = v1[0] + J[0][0] * xi + J[0][1] * eta + J[0][2] * ze;
+      double y = v1[1] + J[1][0] * xi + J[1][1] * eta + J[1][2] * ze;
+      double z = v1[2] + J[2][0] * xi + J[2][1] * eta + J[2][2] * ze;
+      double phi[10], gu[10];
+      for (int i = 0; i < 10; ++i) {
+        const double *s = S[i];
+        phi[i] = s[0] + s[1] * x + s[2] * y + s[3] * z;
+        if (full_phi) phi[i] += s[4] * x * x + s[5] * x * y + s[6] * x * z + s[7] * y * y + s[8] * y * z + s[9] * z * z;
+        double gx = s[1] + 2 * s[4] * x + s[5] * y + s[6] * z;
+        double gy = s[2] + 2 * s[7] * y + s[5] * x + s[8] * z;
+        double gz = s[3] + 2 * s[9] * z + s[6] * x + s[8] * y;
+        gu[i] = ua[0] * gx + ua[1] * gy + ua[2] * gz;
+      }
+      double w = GQ3_W[q] / 6.0 * VE[k];
+      for (int j = 0; j < 10; ++j)
+        for (int i = 0; i < 10; ++i) C[i][j] += w * gu[j] * phi[i] * f;
+    }
+    for (int i = 0; i < 10; ++i)
+      for (int j = 0; j < 10; ++j) Ck[100 * k + 10 * i + j] = C[j][i];
+  }
+  long nnz = or_assemble_csc(nv, nt, 10, t, Ck, 0, colptr, rowval, nzval);
+  free(Ck);
+  return nnz;
+}
+
 /* src/FEM2D.jl:28-45 quadraticBasis2D: 6x6 Vandermonde [1 x y x^2 xy y^2]. */
 static int p2_basis2d(const double *p, const int *nds, int a, const double *x0, double *S) {
   int order[6], m = 1;

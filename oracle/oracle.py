@@ -69,6 +69,8 @@ def lib():
         L.or_p2_stiffness.argtypes = [_dp, _ip, C.c_int, C.c_long, _dp, _vp, C.c_int] + csc_out
         L.or_p2_mass.restype = C.c_long
         L.or_p2_mass.argtypes = [_dp, _ip, C.c_int, C.c_long, _dp, _vp, C.c_int] + csc_out
+        L.or_p2_convection.restype = C.c_long
+        L.or_p2_convection.argtypes = [_dp, _ip, C.c_int, C.c_long, _dp, _dp, _vp, C.c_int] + csc_out
         L.or_p2_stiffness2d.restype = C.c_long
         L.or_p2_stiffness2d.argtypes = [_dp, _ip, C.c_int, C.c_long, _dp, _vp, C.c_int] + csc_out
         L.or_p2_mass2d.restype = C.c_long
@@ -216,6 +218,55 @@ def quadraticMassMatrix(mesh, F=None, full_phi=False):
     fv = None if F is None else _c(F, np.float64)
     return _assemble(lib().or_p2_mass, mesh, 10, p, t, mesh.nv, mesh.nt, _c(mesh.VE, np.float64), _ptr(fv),
                      int(full_phi))
+
+
+def quadraticConvectionMatrix(mesh, u, F=None, full_phi=False):
+    """``src/FEM3D.jl:563-648``; u is the nodal velocity (3 x nv)."""
+    p, t = _pt(mesh)
+    uv = _c(np.asarray(u, dtype=np.float64).T, np.float64)
+    fv = None if F is None else _c(F, np.float64)
+    return _assemble(lib().or_p2_convection, mesh, 10, p, t, mesh.nv, mesh.nt, _c(mesh.VE, np.float64), uv,
+                     _ptr(fv), int(full_phi))
+
+
+# src/FEM3D.jl:303-308: the P2 triangle mass, nodes (v1, v2, v3, m12, m23, m31), times 180.
+_FACE_MK = np.array([[6, -1, -1, 0, -4, 0],
+                     [-1, 6, -1, 0, 0, -4],
+                     [-1, -1, 6, -4, 0, 0],
+                     [0, 0, -4, 32, 16, 16],
+                     [-4, 0, 0, 16, 32, 16],
+                     [0, -4, 0, 16, 16, 32]], dtype=np.float64)
+
+
+def quadraticBoundaryMassMatrix(mesh, faces6, F=None):
+    """``src/FEM3D.jl:300-322``: M[nds[i], nds[j]] += AE[s] Mk[i,j] F[s] over the
+    surface faces (faces6: 6 x ns, 0-based), Mk = (1/180) c."""
+    ns = faces6.shape[1]
+    F = np.ones(ns) if F is None else np.asarray(F, dtype=np.float64)
+    Mk = (1.0 / 180.0) * _FACE_MK
+    rows = np.repeat(faces6, 6, axis=0)            # (36, ns): row node of entry (i, j)
+    cols = np.tile(faces6, (6, 1))                 # (36, ns): column node
+    vals = (np.asarray(mesh.AE[:ns])[None, :] * Mk.reshape(36, 1)) * F[None, :]
+    return sp.csc_matrix((vals.ravel(), (rows.ravel(), cols.ravel())), shape=(mesh.nv, mesh.nv))
+
+
+def transport_be(mesh, T0, rhoCp, kappa, u, dt, nsteps, faces6=None, face_F=None, full_phi=True):
+    """``Transport/main3D.jl:155-213``: LM = M + dt (A + R + C) and nsteps direct
+    solves T = LM \\ (M T) (scipy's sparse LU standing in for Julia's ``\\``).
+    Returns the list of fields after each step."""
+    import scipy.sparse.linalg as spla
+    M = quadraticMassMatrix(mesh, rhoCp, full_phi=full_phi)
+    A = quadraticStiffnessMatrix(mesh, kappa)
+    Cm = quadraticConvectionMatrix(mesh, u, rhoCp, full_phi=full_phi)
+    R = sp.csc_matrix((mesh.nv, mesh.nv)) if face_F is None else quadraticBoundaryMassMatrix(mesh, faces6, face_F)
+    LM = (M + dt * (A + R + Cm)).tocsc()
+    lu = spla.splu(LM)
+    T = np.asarray(T0, dtype=np.float64).copy()
+    out = []
+    for _ in range(nsteps):
+        T = lu.solve(M @ T)
+        out.append(T.copy())
+    return out
 
 
 def quadraticStiffnessMatrix2D(mesh, mu=None, shift=True):

@@ -81,6 +81,19 @@ def test_p2_tets():
         assert rel(Mg.data, Mo.data) < (1e-11 if full else 1e-9)
 
 
+def test_p2_convection():
+    m = fg.box_tet_mesh(3, seed=4, order=2)
+    rng = np.random.default_rng(11)
+    u, F = rng.normal(size=(3, m.nv)), rng.uniform(0.5, 2.0, m.nt)
+    for full in (False, True):
+        Cg = fg.quadraticConvectionMatrix(m, u, F, full_phi=full)
+        Co = O.quadraticConvectionMatrix(m, u, F, full_phi=full)
+        assert same_pattern(Cg, Co)
+        assert rel(Cg.data, Co.data) < (1e-11 if full else 1e-9)
+    with pytest.raises(RuntimeError):   # P1 mesh: the convection matrix is defined for P2
+        fg.quadraticConvectionMatrix(fg.box_tet_mesh(2, seed=1), np.zeros((3, 27)))
+
+
 def test_p2_triangles():
     m = fg.box_tri_mesh(4, seed=4, order=2)
     Kg, Ko = fg.quadraticStiffnessMatrix2D(m), O.quadraticStiffnessMatrix2D(m)

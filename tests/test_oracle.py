@@ -110,6 +110,26 @@ def test_p2_patch_and_partition():
     del q
 
 
+@pytest.mark.parametrize("full_phi", [True, False])
+def test_p2_convection_known_answers(full_phi):
+    """C[r, c] = int (u . grad phi_r) phi_c (the reference's scatter of Ck[j, i],
+    src/FEM3D.jl:640-648): its columns sum to 0 (sum_r phi_r = 1) and, for a constant
+    velocity and a linear T = a . x, (C^T T)_c = (u . a) int phi_c = (u . a) (M 1)_c.
+    Both hold for the linear-part-only phi too, whose basis still sums to 1."""
+    m = box_tet_mesh(3, seed=1, order=2)
+    rng = np.random.default_rng(5)
+    C = O.quadraticConvectionMatrix(m, rng.normal(size=(3, m.nv)), full_phi=full_phi)
+    assert np.abs(np.asarray(C.sum(axis=0))).max() < 1e-12 * np.abs(C.data).max()
+    uc = np.tile(np.array([[0.3], [-1.2], [0.7]]), m.nv)
+    a = np.array([2.0, -1.0, 0.5])
+    C = O.quadraticConvectionMatrix(m, uc, full_phi=full_phi)
+    M = O.quadraticMassMatrix(m, full_phi=full_phi)
+    lhs, rhs = C.T @ (a @ m.p), (uc[:, 0] @ a) * (M @ np.ones(m.nv))
+    assert np.abs(lhs - rhs).max() < (1e-12 if full_phi else 1e-9) * np.abs(rhs).max()
+    # the other orientation is not the reference's matrix
+    assert np.abs(C @ (a @ m.p) - rhs).max() > 1e-3 * np.abs(rhs).max()
+
+
 def test_tangent_zero_field_and_symmetry(mesh6):
     rng = np.random.default_rng(0)
     H = rng.normal(size=(3, mesh6.nt))
