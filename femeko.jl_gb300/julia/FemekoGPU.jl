@@ -186,6 +186,48 @@ function massMatrix(mesh; F::Vector{Float64}=ones(size(mesh.t, 2)), full_phi::Bo
 end
 massMatrix2D(mesh) = massMatrix(mesh)
 quadraticMassMatrix(mesh, S, F::Vector{Float64}=ones(size(mesh.t, 2))) = massMatrix(mesh; F=F)
+
+"""quadraticConvectionMatrix(mesh, S, u, F) -- src/FEM3D.jl:563-648 on the GPU (S is
+not used: the basis is built per element on the device).  u: 3 x nv velocity."""
+function quadraticConvectionMatrix(mesh, S, u::Matrix{Float64}, F::Vector{Float64}=ones(size(mesh.t, 2));
+                                   full_phi::Bool=false)
+    g = gpu(mesh); v = zeros(g.nnz)
+    check(ccall((:fg_convection, libpath()), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Int32, Ptr{Float64}),
+                g.h, u, F, full_phi ? 1 : 0, v))
+    return csc(g, v)
+end
+
+"""quadraticBoundaryMassMatrix(mesh, F) -- src/FEM3D.jl:300-322 on the GPU; reads the
+six node rows of the P2 mesh.surfaceT (1-based) and mesh.AE."""
+function quadraticBoundaryMassMatrix(mesh, F::Vector{Float64}=ones(mesh.ns))
+    g = gpu(mesh); v = zeros(g.nnz)
+    faces = Int32.(mesh.surfaceT[1:6, :] .- 1)
+    check(ccall((:fg_boundary_mass, libpath()), Cint,
+                (Ptr{Cvoid}, Ptr{Int32}, Ptr{Float64}, Ptr{Float64}, Int64, Ptr{Float64}),
+                g.h, faces, mesh.AE, F, size(faces, 2), v))
+    return csc(g, v)
+end
+
+"""transport_be(mesh, T0, rhoCp, conductivity, u, intakeBC; dt, nsteps) -- the time
+loop of Transport/main3D.jl:155-213 (LM = M + dt (A + R + C), T = LM \\ (M T)) on the
+GPU, one Jacobi-BiCGStab solve per step; returns (T, snapshots every `every` steps, stats)."""
+function transport_be(mesh, T0::Vector{Float64}, rhoCp::Vector{Float64}, conductivity::Vector{Float64},
+                      u::Matrix{Float64}, intakeBC::Vector{Float64}; dt=0.01, nsteps::Integer=100,
+                      every::Integer=0, full_phi::Bool=true, rtol=1e-10, maxiter::Integer=10_000)
+    g = gpu(mesh)
+    T = copy(T0)
+    snaps = zeros(g.nv, every > 0 ? nsteps ÷ every : 0)
+    faces = Int32.(mesh.surfaceT[1:6, :] .- 1)
+    o = Ref(solve_opts(precision=:fp64, rtol=rtol, maxiter=maxiter))
+    s = Ref{SolveStats}()
+    st = ccall((:fg_transport_be, libpath()), Cint,
+               (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Int32}, Ptr{Float64}, Ptr{Float64}, Int64,
+                Float64, Int32, Int32, Ptr{Float64}, Int32, Ptr{Float64}, Ref{SolveOpts}, Ref{SolveStats}),
+               g.h, rhoCp, conductivity, u, faces, mesh.AE, intakeBC, size(faces, 2), dt, nsteps,
+               full_phi ? 1 : 0, T, every, isempty(snaps) ? C_NULL : snaps, o, s)
+    check(st; allow_not_converged=true)
+    return T, snaps, s[]
+end
 quadraticMassMatrix2D(mesh) = massMatrix(mesh)
 
 function tangentialStiffnessMatrix(mesh, H_vec::Matrix{Float64}, dmu::Vector{Float64})
