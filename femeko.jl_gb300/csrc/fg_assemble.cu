@@ -913,6 +913,7 @@ static void launch_row_any(fg_mesh *m, const R *rec, const double *rec_r, int ap
 // Element pass (FP64 records) for the given kind.
 static void launch_elem(fg_mesh *m, int kind, const double *d_f, const double *d_H, const double *d_dmu, double cm,
                         double cs, int full_phi, bool transpose) {
+  FG_REQUIRE(!m->edge, FG_UNSUPPORTED, "nodal element matrices on a Nedelec (edge) handle");
   fg_ensure_records(m);
   double *rec = static_cast<double *>(m->rec);
   unsigned g = grid_for(m->nt, 128);
@@ -953,6 +954,153 @@ void fg_assemble_operator(fg_mesh *m, int kind, const double *d_f, const double 
     launch_row_any<double, double>(m, rec, nullptr, apply_bc ? 1 : 0, want64 ? m->val64 : nullptr,
                                    want32 ? m->val32 : nullptr, nullptr, m->dinv64, m->dinv32, nullptr, 0.0, 0);
   }
+}
+
+// ------------------------------------------------------------------ Nedelec edge elements
+// Whitney edge elements on P1 tetrahedra (src/FEM3D.jl:155-271,
+// Magnetostatics/nedelec3D.jl:106-221).  Local edge e joins local vertices
+// (i_e, j_e) = (1,2), (2,3), (3,1), (4,1), (3,4), (2,4) (src/mesh.jl:603-630, Gmsh's
+// order) and curl N_e = 2 l_e (grad lambda_i x grad lambda_j) with l_e = |x_j - x_i|,
+// in the element's local orientation as the reference uses it.
+__constant__ int c_ned_i[6] = {0, 1, 2, 3, 2, 1};
+__constant__ int c_ned_j[6] = {1, 2, 0, 0, 3, 3};
+
+__device__ __forceinline__ void ned_curls(int64_t k, int64_t nt, const double *__restrict__ p,
+                                          const int *__restrict__ tv, const double *__restrict__ geo,
+                                          double (&cN)[6][3]) {
+  int v[4];
+  for (int a = 0; a < 4; ++a) v[a] = tv[(int64_t)a * nt + k];
+  for (int e = 0; e < 6; ++e) {
+    const int i = c_ned_i[e], j = c_ned_j[e];
+    const double dx = p[3 * v[j]] - p[3 * v[i]], dy = p[3 * v[j] + 1] - p[3 * v[i] + 1],
+                 dz = p[3 * v[j] + 2] - p[3 * v[i] + 2];
+    const double l2 = 2.0 * sqrt(dx * dx + dy * dy + dz * dz);
+    const double gix = geo[(int64_t)(3 * i) * nt + k], giy = geo[(int64_t)(3 * i + 1) * nt + k],
+                 giz = geo[(int64_t)(3 * i + 2) * nt + k];
+    const double gjx = geo[(int64_t)(3 * j) * nt + k], gjy = geo[(int64_t)(3 * j + 1) * nt + k],
+                 gjz = geo[(int64_t)(3 * j + 2) * nt + k];
+    cN[e][0] = l2 * (giy * gjz - giz * gjy);
+    cN[e][1] = l2 * (giz * gjx - gix * gjz);
+    cN[e][2] = l2 * (gix * gjy - giy * gjx);
+  }
+}
+
+__device__ __forceinline__ double dot3(const double *a, const double *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+// Element records: nu VE curlN_i.curlN_j (nu = 1 when null; src/FEM3D.jl:155-191 and the
+// `.*nu` of nedelec3D.jl:172) plus, with dnu, the tangential term
+// VE (curlN_i.B)(curlN_j.B) dnu / |B| of src/FEM3D.jl:194-271 (0 where |B| = 0).
+// With bext, the load VE Bext.curlN_e of nedelec3D.jl:109-139 in the vector records.
+__global__ void k_elem_ned(int64_t nt, const double *__restrict__ p, const int *__restrict__ tv,
+                           const double *__restrict__ geo, const double *__restrict__ nu, int with_stiff,
+                           const double *__restrict__ dnu, const double *__restrict__ Bf, const double *__restrict__ Bn,
+                           double bx, double by, double bz, int with_load, const int *__restrict__ recpos,
+                           double *__restrict__ rec, double *__restrict__ rec_r) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt) return;
+  double cN[6][3];
+  ned_curls(k, nt, p, tv, geo, cN);
+  const double VE = geo[12 * nt + k];
+  if (with_load) {
+    const double be[3] = {bx, by, bz};
+    for (int e = 0; e < 6; ++e) rec_r[recpos[(int64_t)e * nt + k]] = VE * dot3(be, cN[e]);
+  }
+  if (!rec) return;
+  double Ke[6][6];
+  const double nk = nu ? nu[k] : 1.0;
+  for (int i = 0; i < 6; ++i)
+    for (int j = 0; j < 6; ++j) Ke[i][j] = with_stiff ? VE * dot3(cN[i], cN[j]) * nk : 0.0;
+  if (dnu) {
+    const double b[3] = {Bf[3 * k], Bf[3 * k + 1], Bf[3 * k + 2]};
+    const double bn = Bn[k];
+    if (bn != 0.0) {
+      double cb[6];
+      for (int e = 0; e < 6; ++e) cb[e] = dot3(cN[e], b);
+      for (int i = 0; i < 6; ++i)
+        for (int j = i; j < 6; ++j) {
+          const double a = VE * cb[i] * cb[j] * dnu[k] / bn;
+          Ke[i][j] += a;
+          if (j != i) Ke[j][i] += a;
+        }
+    }
+  }
+  for (int e = 0; e < 6; ++e) store_row<6, double>(rec, recpos[(int64_t)e * nt + k], Ke[e]);
+}
+
+// Element blocks Ak (36 x nt, column k = the 6 x 6 matrix row-major) of
+// src/FEM3D.jl:155-191 nedelecLocalStiffness.
+__global__ void k_ned_local(int64_t nt, const double *__restrict__ p, const int *__restrict__ tv,
+                            const double *__restrict__ geo, double *__restrict__ Ak) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt) return;
+  double cN[6][3];
+  ned_curls(k, nt, p, tv, geo, cN);
+  const double VE = geo[12 * nt + k];
+  for (int i = 0; i < 6; ++i)
+    for (int j = 0; j < 6; ++j) Ak[36 * k + 6 * i + j] = VE * dot3(cN[i], cN[j]);
+}
+
+// B on each element: sum_e u[edge_e] curlN_e and its norm (nedelec3D.jl:190-221).
+__global__ void k_ned_bfield(int64_t nt, const double *__restrict__ p, const int *__restrict__ tv,
+                             const double *__restrict__ geo, const int *__restrict__ t, const double *__restrict__ u,
+                             double *__restrict__ Bf, double *__restrict__ Bn) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt) return;
+  double cN[6][3];
+  ned_curls(k, nt, p, tv, geo, cN);
+  double b[3] = {0.0, 0.0, 0.0};
+  for (int e = 0; e < 6; ++e) {
+    const double ue = u[t[(int64_t)e * nt + k]];
+    for (int c = 0; c < 3; ++c) b[c] += ue * cN[e][c];
+  }
+  for (int c = 0; c < 3; ++c) Bf[3 * k + c] = b[c];
+  if (Bn) Bn[k] = sqrt(b[0] * b[0] + b[1] * b[1] + b[2] * b[2]);
+}
+
+void fg_nedelec_operator(fg_mesh *m, const double *d_nu, bool with_stiff, const double *d_dnu, const double *d_Bf,
+                         const double *d_Bn, int layout, bool want32) {
+  FG_REQUIRE(m->edge, FG_UNSUPPORTED, "Nedelec operator: needs a handle from fg_edge_mesh_create");
+  if (layout != OUT_CSR) { m->op_tag = 0; ++m->op_version; }
+  fg_ensure_records(m);
+  double *rec = static_cast<double *>(m->rec);
+  k_elem_ned<<<grid_for(m->nt, 128), 128, 0, m->stream>>>(m->nt, m->p, m->tv, m->geo, d_nu, with_stiff ? 1 : 0,
+                                                           d_dnu, d_Bf, d_Bn, 0.0, 0.0, 0.0, 0, m->recpos, rec,
+                                                           nullptr);
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(1);
+  if (layout == OUT_CSR) {
+    if (!m->csrval) m->csrval = dev_alloc<double>(m, (size_t)m->nnz);
+    launch_row_any<double, double>(m, rec, nullptr, 0, nullptr, nullptr, m->csrval, nullptr, nullptr, nullptr, 0.0, 0);
+  } else {
+    ensure_operator(m, true, want32);
+    launch_row_any<double, double>(m, rec, nullptr, 0, m->val64, want32 ? m->val32 : nullptr, nullptr, m->dinv64,
+                                   want32 ? m->dinv32 : nullptr, nullptr, 0.0, 0);
+  }
+}
+
+void fg_nedelec_load_dev(fg_mesh *m, const double bext[3], double *d_rhs) {
+  FG_REQUIRE(m->edge, FG_UNSUPPORTED, "Nedelec load: needs a handle from fg_edge_mesh_create");
+  fg_ensure_records(m);
+  k_elem_ned<<<grid_for(m->nt, 128), 128, 0, m->stream>>>(m->nt, m->p, m->tv, m->geo, nullptr, 0, nullptr, nullptr,
+                                                           nullptr, bext[0], bext[1], bext[2], 1, m->recpos, nullptr,
+                                                           m->rec_r);
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(1);
+  launch_row<6, double, double>(m, nullptr, m->rec_r, 0, nullptr, nullptr, nullptr, nullptr, nullptr, d_rhs, 1.0, 0);
+}
+
+void fg_nedelec_bfield_dev(fg_mesh *m, const double *d_u, double *d_Bf, double *d_Bn) {
+  FG_REQUIRE(m->edge, FG_UNSUPPORTED, "Nedelec B field: needs a handle from fg_edge_mesh_create");
+  k_ned_bfield<<<grid_for(m->nt, 128), 128, 0, m->stream>>>(m->nt, m->p, m->tv, m->geo, m->t, d_u, d_Bf, d_Bn);
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(1);
+}
+
+void fg_nedelec_local_dev(fg_mesh *m, double *d_Ak) {
+  FG_REQUIRE(m->edge, FG_UNSUPPORTED, "Nedelec local stiffness: needs a handle from fg_edge_mesh_create");
+  k_ned_local<<<grid_for(m->nt, 128), 128, 0, m->stream>>>(m->nt, m->p, m->tv, m->geo, d_Ak);
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(1);
 }
 
 void fg_transport_operator(fg_mesh *m, const double *d_rhocp, const double *d_kdt, const double *d_vel,

@@ -116,6 +116,11 @@ struct fg_mesh {
   // mesh on the device
   double *p = nullptr;       // 3 x nv (AoS, as given)
   int *t = nullptr;          // npe x nt stored SoA: t[a*nt + k]
+  // Nedelec handles: t lists the 6 edge unknowns of each tetrahedron (local edges
+  // 12, 23, 31, 41, 34, 24), tv its 4 vertices (SoA) into the np points p
+  bool edge = false;
+  int *tv = nullptr;
+  int64_t np = 0;
   uint8_t *fixed = nullptr;  // nv Dirichlet mask (0/1)
   bool has_fixed = false;
   double *geo = nullptr;     // P1: SoA per element, (nvert*dim gradients + volume) x nt
@@ -335,6 +340,15 @@ void fg_spmv64_plain(fg_mesh *m, const double *vals, const double *x, double *y)
 // Dirichlet rows; d_x holds the initial guess and receives the solution.
 // Returns 0 converged, 1 iteration limit, 2 breakdown.
 int fg_bicgstab_solve(fg_mesh *m, const double *d_b, double *d_x, const fg_solve_opts &o, fg_solve_stats *st);
+// Nedelec edge elements (handles from fg_edge_mesh_create): the operator
+// nu-weighted curl-curl (with_stiff) plus the tangential term when d_dnu is given, to
+// SELL (val64/dinv64, val32/dinv32 when want32) or to csrval; the load vector
+// Bext.curlN; B per element from the edge values.
+void fg_nedelec_operator(fg_mesh *m, const double *d_nu, bool with_stiff, const double *d_dnu, const double *d_Bf,
+                         const double *d_Bn, int layout, bool want32);
+void fg_nedelec_load_dev(fg_mesh *m, const double bext[3], double *d_rhs);
+void fg_nedelec_bfield_dev(fg_mesh *m, const double *d_u, double *d_Bf, double *d_Bn);
+void fg_nedelec_local_dev(fg_mesh *m, double *d_Ak);
 // Backward-Euler transport operator of P2 tetrahedra: mval = M(rho_cp) and
 // val64/dinv64 = M(rho_cp) + K(kdt) + C^(fdt) (the reference's convection matrix with
 // the factor fdt), no boundary conditions.

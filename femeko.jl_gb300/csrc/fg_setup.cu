@@ -478,8 +478,12 @@ static void free_mesh(fg_mesh *m) {
   delete m;
 }
 
-extern "C" fg_status fg_mesh_create(const double *p, int64_t nv, const int32_t *t, int64_t nt,
-                                    int32_t nodes_per_elem, int32_t index_base, fg_mesh **out) {
+// Builds a handle whose matrix rows are the nv degrees of freedom listed by t
+// (nodes_per_elem x nt).  With tv (4 x nt vertex indices into the np points p) the
+// degrees of freedom are the 6 edges of each tetrahedron (Nedelec elements) and the
+// geometry comes from tv; otherwise they are the nodes themselves (np = nv).
+static fg_status create_impl(const double *p, int64_t np, const int32_t *t, int64_t nt, int32_t nodes_per_elem,
+                             int64_t nv, const int32_t *tv, int32_t index_base, fg_mesh **out) {
   fg_mesh *m = nullptr;
   fg_status st = fg_guard([&]() -> fg_status {
     FG_REQUIRE(out != nullptr && p != nullptr && t != nullptr, FG_BAD_ARG, "fg_mesh_create: null pointer");
@@ -487,6 +491,8 @@ extern "C" fg_status fg_mesh_create(const double *p, int64_t nv, const int32_t *
     int npe = nodes_per_elem;
     FG_REQUIRE(npe == 3 || npe == 4 || npe == 6 || npe == 10, FG_BAD_ARG,
                "fg_mesh_create: nodes_per_elem must be 3, 4, 6 or 10");
+    FG_REQUIRE(!tv || npe == 6, FG_BAD_ARG, "fg_edge_mesh_create: six edges per tetrahedron");
+    FG_REQUIRE(np > 0 && np < (int64_t)1 << 30, FG_BAD_ARG, "fg_mesh_create: bad point count");
     FG_REQUIRE(index_base == 0 || index_base == 1, FG_BAD_ARG, "fg_mesh_create: index_base must be 0 or 1");
     FG_REQUIRE(nv > 0 && nt > 0, FG_BAD_ARG, "fg_mesh_create: empty mesh");
     FG_REQUIRE(nv < (int64_t)1 << 30 && nt * npe < (int64_t)1 << 31, FG_BAD_ARG, "fg_mesh_create: mesh too large");
@@ -502,14 +508,25 @@ extern "C" fg_status fg_mesh_create(const double *p, int64_t nv, const int32_t *
     m->nv = nv;
     m->nt = nt;
     m->npe = npe;
-    m->dim = (npe == 3 || npe == 6) ? 2 : 3;
+    m->edge = tv != nullptr;
+    m->dim = ((npe == 3 || npe == 6) && !m->edge) ? 2 : 3;
     m->nvert = m->dim + 1;
+    m->np = np;
     cudaStream_t s = m->stream;
 
     m->flags = dev_alloc<int>(m, 4);
     FG_CUDA_TRY(cudaMemsetAsync(m->flags, 0, 4 * sizeof(int), s));
-    m->p = dev_alloc<double>(m, 3 * (size_t)nv);
-    FG_CUDA_TRY(cudaMemcpyAsync(m->p, p, sizeof(double) * 3 * (size_t)nv, cudaMemcpyHostToDevice, s));
+    m->p = dev_alloc<double>(m, 3 * (size_t)np);
+    FG_CUDA_TRY(cudaMemcpyAsync(m->p, p, sizeof(double) * 3 * (size_t)np, cudaMemcpyHostToDevice, s));
+    if (tv) {
+      int32_t *tvraw = nullptr;
+      FG_CUDA_TRY(cudaMallocAsync(&tvraw, sizeof(int32_t) * (size_t)nt * 4, s));
+      FG_CUDA_TRY(cudaMemcpyAsync(tvraw, tv, sizeof(int32_t) * (size_t)nt * 4, cudaMemcpyHostToDevice, s));
+      m->tv = dev_alloc<int>(m, (size_t)nt * 4);
+      k_convert_t<<<grid_for(nt, 256), 256, 0, s>>>(tvraw, m->tv, nt, 4, np, index_base, m->flags);
+      FG_CUDA_TRY(cudaGetLastError());
+      cudaFreeAsync(tvraw, s);
+    }
     int32_t *traw = nullptr;
     FG_CUDA_TRY(cudaMallocAsync(&traw, sizeof(int32_t) * (size_t)nt * npe, s));
     FG_CUDA_TRY(cudaMemcpyAsync(traw, t, sizeof(int32_t) * (size_t)nt * npe, cudaMemcpyHostToDevice, s));
@@ -631,7 +648,7 @@ extern "C" fg_status fg_mesh_create(const double *p, int64_t nv, const int32_t *
     m->ngeo = (m->dim == 3) ? 23 : 7;
     m->geo = dev_alloc<double>(m, (size_t)m->ngeo * nt);
     if (m->dim == 3)
-      k_geom_tet<<<grid_for(nt, 256), 256, 0, s>>>(m->p, m->t, nt, m->geo, m->flags);
+      k_geom_tet<<<grid_for(nt, 256), 256, 0, s>>>(m->p, m->edge ? m->tv : m->t, nt, m->geo, m->flags);
     else
       k_geom_tri<<<grid_for(nt, 256), 256, 0, s>>>(m->p, m->t, nt, m->geo, m->flags);
     FG_CUDA_TRY(cudaGetLastError());
@@ -656,6 +673,22 @@ extern "C" fg_status fg_mesh_create(const double *p, int64_t nv, const int32_t *
   });
   if (m) free_mesh(m);
   return st;
+}
+
+extern "C" fg_status fg_mesh_create(const double *p, int64_t nv, const int32_t *t, int64_t nt,
+                                    int32_t nodes_per_elem, int32_t index_base, fg_mesh **out) {
+  return create_impl(p, nv, t, nt, nodes_per_elem, nv, nullptr, index_base, out);
+}
+
+extern "C" fg_status fg_edge_mesh_create(const double *p, int64_t nv, const int32_t *t, const int32_t *edges,
+                                         int64_t nt, int64_t ne, int32_t index_base, fg_mesh **out) {
+  if (!t || !edges || ne <= 0 || ne >= (int64_t)1 << 30) {
+    if (out) *out = nullptr;
+    return fg_guard([&]() -> fg_status {
+      throw FgError{FG_BAD_ARG, "fg_edge_mesh_create: need t, edges and 0 < ne < 2^30"};
+    });
+  }
+  return create_impl(p, nv, edges, nt, 6, ne, t, index_base, out);
 }
 
 extern "C" fg_status fg_mesh_destroy(fg_mesh *m) {

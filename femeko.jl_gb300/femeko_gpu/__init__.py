@@ -427,3 +427,7 @@ def hfield(mesh: MESH, u):
     H = np.zeros(3 * mesh.nt)
     L.check(L.lib().fg_hfield(g.h, L.ptr(_c(u, np.float64)), L.ptr(H)))
     return H.reshape(mesh.nt, 3).T
+
+
+from .nedelec import (edge_mesh, nedelec_edges, nedelecLocalStiffness, nedelecStiffness,  # noqa: E402,F401
+                      nedelecTangentialStiffness, nedelec_load, nedelec_bfield, nedelec_linear)

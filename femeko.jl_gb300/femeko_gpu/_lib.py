@@ -98,6 +98,13 @@ SIGNATURES = {
     "fg_newton_get_outputs": [_vp, _vp, _vp, _vp],
     "fg_heat_be": [_vp, _vp, _d, _d, _i32, _vp, _i32, _vp, C.POINTER(SolveOpts), C.POINTER(SolveStats)],
     "fg_boundary_mass": [_vp, _vp, _vp, _vp, _i64, _vp],
+    "fg_edge_mesh_create": [_vp, _i64, _vp, _vp, _i64, _i64, _i32, C.POINTER(_vp)],
+    "fg_nedelec_local_stiffness": [_vp, _vp],
+    "fg_nedelec_stiffness": [_vp, _vp, _vp],
+    "fg_nedelec_tangent": [_vp, _vp, _vp, _vp, _vp],
+    "fg_nedelec_load": [_vp, _vp, _vp],
+    "fg_nedelec_bfield": [_vp, _vp, _vp, _vp],
+    "fg_nedelec_linear": [_vp, _vp, _vp, _vp, _vp, _vp, C.POINTER(SolveOpts), C.POINTER(SolveStats)],
     "fg_transport_be": [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _d, _i32, _i32, _vp, _i32, _vp,
                         C.POINTER(SolveOpts), C.POINTER(SolveStats)],
     "fg_batch_magnetostatics_linear": [_vp, _i32, _vp, _vp, C.POINTER(SolveOpts), _vp, _vp, C.POINTER(BatchStats)],

@@ -152,6 +152,15 @@ fg_status fg_device_info(char *name, int32_t name_len, int32_t *sm_count);
  * 6 (P2 tri).  p is 3 x nv (z ignored for triangles). */
 fg_status fg_mesh_create(const double *p, int64_t nv, const int32_t *t, int64_t nt, int32_t nodes_per_elem,
                          int32_t index_base, fg_mesh **out);
+/* A handle whose unknowns are the edges of a tetrahedral mesh (Nedelec elements,
+ * Magnetostatics/nedelec3D.jl): t (4 x nt) the vertices into the nv points p, edges
+ * (6 x nt) each element's edge unknowns 0..ne-1 (the reference's
+ * edge2localMap[t[5:10, k]], src/mesh.jl:168-183), local edge e joining local vertices
+ * (1,2), (2,3), (3,1), (4,1), (3,4), (2,4) (src/mesh.jl:603-630).  The pattern,
+ * records and solvers of the handle run over the ne edges; only the fg_nedelec_*
+ * assembly entry points accept it. */
+fg_status fg_edge_mesh_create(const double *p, int64_t nv, const int32_t *t, const int32_t *edges, int64_t nt,
+                              int64_t ne, int32_t index_base, fg_mesh **out);
 fg_status fg_mesh_destroy(fg_mesh *m);
 /* nnz of the structural pattern and the longest row. */
 fg_status fg_mesh_nnz(const fg_mesh *m, int64_t *nnz, int32_t *max_row);
@@ -259,6 +268,29 @@ fg_status fg_heat_be(fg_mesh *m, const double *kappa, double rho_c, double dt, i
  * the order of fg_csc_pattern (a face pair outside the pattern is FG_BAD_ARG). */
 fg_status fg_boundary_mass(fg_mesh *m, const int32_t *faces, const double *AE, const double *F, int64_t nfaces,
                            double *nzval);
+
+/* ------------------------------------------------------------------ Nedelec */
+/* Edge-element routines on a handle from fg_edge_mesh_create.  curlN_e =
+ * 2 l_e (grad lambda_i x grad lambda_j) in the element's local edge orientation. */
+/* src/FEM3D.jl:155-191 nedelecLocalStiffness: Ak 36 x nt (column k = 6 x 6 block). */
+fg_status fg_nedelec_local_stiffness(fg_mesh *m, double *Ak);
+/* The global matrix sum sparse(edge_i, edge_j, Ak .* nu) of
+ * Magnetostatics/nedelec3D.jl:168-178 (nu per element, NULL = ones), values in the
+ * order of fg_csc_pattern. */
+fg_status fg_nedelec_stiffness(fg_mesh *m, const double *nu, double *nzval);
+/* src/FEM3D.jl:194-271 nedelecTangentialStiffness: VE (curlN_i.B)(curlN_j.B) dnu/|B|
+ * (Bfield 3 x nt, B = |B| nt); elements with |B| = 0 contribute 0. */
+fg_status fg_nedelec_tangent(fg_mesh *m, const double *dnu, const double *Bfield, const double *B, double *nzval);
+/* nedelec3D.jl:106-139: rhs[e] = sum over elements of VE Bext.curlN_e (ne values). */
+fg_status fg_nedelec_load(fg_mesh *m, const double *Bext, double *rhs);
+/* nedelec3D.jl:190-221: B per element (3 x nt) and |B| (nt, may be NULL) from u (ne). */
+fg_status fg_nedelec_bfield(fg_mesh *m, const double *u, double *Bfield, double *B);
+/* The first Newton step of nedelec3D.jl (u = 0, At = 0): A(nu) u = RHS(Bext) by the
+ * Jacobi-PCG of fg_pcg (the curl-curl matrix is singular with a consistent right-hand
+ * side: u is one solution, B = curl u is unique); Bfield/B (may be NULL) as in
+ * fg_nedelec_bfield. */
+fg_status fg_nedelec_linear(fg_mesh *m, const double *nu, const double *Bext, double *u, double *Bfield, double *B,
+                            const fg_solve_opts *o, fg_solve_stats *s);
 
 /* Heat transport with convection on P2 tetrahedra (Transport/main3D.jl:143-213):
  * LM = M(rho_cp) + dt (A(kappa) + R + C(vel, rho_cp)), then nsteps steps of

@@ -482,6 +482,94 @@ long or_p2_convection(const double *p, const int *t, int nv, long nt, const doub
   return nnz;
 }
 
+/* Nedelec (Whitney) edge elements, src/FEM3D.jl:155-271 and                     */
+/* Magnetostatics/nedelec3D.jl:106-221.  abcd (src/FEM3D.jl:5-17) solves           */
+/* [1 x y z] r = e1 over the node and the other three (in element order); local    */
+/* edge e joins local nodes (1,2), (2,3), (3,1), (4,1), (3,4), (2,4)                */
+/* (src/mesh.jl:603-630); curlN_e = 2 |x_j - x_i| (grad_i x grad_j).              */
+/* t: 4 (or more) node rows per element, element-major with stride ni.            */
+static const int NED_I[6] = {0, 1, 2, 3, 2, 1}, NED_J[6] = {1, 2, 0, 0, 3, 3};
+
+static void ned_curls(const double *p, const int *nds, double cN[6][3]) {
+  double g[4][3];
+  for (int a = 0; a < 4; ++a) {
+    int order[4], m = 1;
+    order[0] = nds[a];
+    for (int b = 0; b < 4; ++b) if (b != a) order[m++] = nds[b];
+    double A[16], r[4] = {1.0, 0.0, 0.0, 0.0};
+    for (int q = 0; q < 4; ++q) {
+      A[4 * q] = 1.0;
+      A[4 * q + 1] = p[3 * order[q]];
+      A[4 * q + 2] = p[3 * order[q] + 1];
+      A[4 * q + 3] = p[3 * order[q] + 2];
+    }
+    lu_solve(4, A, r);
+    g[a][0] = r[1]; g[a][1] = r[2]; g[a][2] = r[3];
+  }
+  for (int e = 0; e < 6; ++e) {
+    int i = NED_I[e], j = NED_J[e];
+    double dx = p[3 * nds[j]] - p[3 * nds[i]], dy = p[3 * nds[j] + 1] - p[3 * nds[i] + 1],
+           dz = p[3 * nds[j] + 2] - p[3 * nds[i] + 2];
+    double l = sqrt(dx * dx + dy * dy + dz * dz);
+    double cx = g[i][1] * g[j][2] - g[i][2] * g[j][1];
+    double cy = g[i][2] * g[j][0] - g[i][0] * g[j][2];
+    double cz = g[i][0] * g[j][1] - g[i][1] * g[j][0];
+    cN[e][0] = 2.0 * l * cx; cN[e][1] = 2.0 * l * cy; cN[e][2] = 2.0 * l * cz;
+  }
+}
+
+/* Element blocks: mode 0 nedelecLocalStiffness VE curlN_i.curlN_j (times nu when    */
+/* given); mode 1 the tangential block VE (curlN_i.B)(curlN_j.B) dnu / |B| of       */
+/* src/FEM3D.jl:236-243 (0 where |B| = 0).  Ak[36k + 6i + j].                        */
+void or_nedelec_local(const double *p, const int *t, int ni, long nt, const double *VE, const double *nu, int mode,
+                      const double *dnu, const double *Bf, const double *Bn, double *Ak) {
+#pragma omp parallel for schedule(static)
+  for (long k = 0; k < nt; ++k) {
+    double cN[6][3];
+    ned_curls(p, t + (long)ni * k, cN);
+    for (int i = 0; i < 6; ++i)
+      for (int j = 0; j < 6; ++j) {
+        double v;
+        if (mode == 0) {
+          v = VE[k] * (cN[i][0] * cN[j][0] + cN[i][1] * cN[j][1] + cN[i][2] * cN[j][2]);
+          if (nu) v *= nu[k];
+        } else {
+          const double *b = Bf + 3 * k;
+          double ci = cN[i][0] * b[0] + cN[i][1] * b[1] + cN[i][2] * b[2];
+          double cj = cN[j][0] * b[0] + cN[j][1] * b[1] + cN[j][2] * b[2];
+          v = Bn[k] != 0.0 ? VE[k] * ci * cj * dnu[k] / Bn[k] : 0.0;
+        }
+        Ak[36 * k + 6 * i + j] = v;
+      }
+  }
+}
+
+/* nedelec3D.jl:106-139: RHS[e] += VE Bext.curlN_e, elements then local edges in    */
+/* order; edges: 6 x nt element-major edge indices (0-based).                      */
+void or_nedelec_load(const double *p, const int *t, int ni, long nt, const double *VE, const int *edges,
+                     const double *bext, double *rhs) {
+  for (long k = 0; k < nt; ++k) {
+    double cN[6][3];
+    ned_curls(p, t + (long)ni * k, cN);
+    for (int e = 0; e < 6; ++e)
+      rhs[edges[6 * k + e]] += VE[k] * (bext[0] * cN[e][0] + bext[1] * cN[e][1] + bext[2] * cN[e][2]);
+  }
+}
+
+/* nedelec3D.jl:190-221: B_k = sum_e u[edge_e] curlN_e and its norm.               */
+void or_nedelec_bfield(const double *p, const int *t, int ni, long nt, const int *edges, const double *u,
+                       double *Bf, double *Bn) {
+#pragma omp parallel for schedule(static)
+  for (long k = 0; k < nt; ++k) {
+    double cN[6][3], b[3] = {0.0, 0.0, 0.0};
+    ned_curls(p, t + (long)ni * k, cN);
+    for (int e = 0; e < 6; ++e)
+      for (int c = 0; c < 3; ++c) b[c] += u[edges[6 * k + e]] * cN[e][c];
+    for (int c = 0; c < 3; ++c) Bf[3 * k + c] = b[c];
+    Bn[k] = sqrt(b[0] * b[0] + b[1] * b[1] + b[2] * b[2]);
+  }
+}
+
 /* src/FEM2D.jl:28-45 quadraticBasis2D: 6x6 Vandermonde [1 x y x^2 xy y^2]. */
 static int p2_basis2d(const double *p, const int *nds, int a, const double *x0, double *S) {
   int order[6], m = 1;

@@ -71,6 +71,9 @@ def lib():
         L.or_p2_mass.argtypes = [_dp, _ip, C.c_int, C.c_long, _dp, _vp, C.c_int] + csc_out
         L.or_p2_convection.restype = C.c_long
         L.or_p2_convection.argtypes = [_dp, _ip, C.c_int, C.c_long, _dp, _dp, _vp, C.c_int] + csc_out
+        L.or_nedelec_local.argtypes = [_dp, _ip, C.c_int, C.c_long, _dp, _vp, C.c_int, _vp, _vp, _vp, _dp]
+        L.or_nedelec_load.argtypes = [_dp, _ip, C.c_int, C.c_long, _dp, _ip, _dp, _dp]
+        L.or_nedelec_bfield.argtypes = [_dp, _ip, C.c_int, C.c_long, _ip, _dp, _dp, _dp]
         L.or_p2_stiffness2d.restype = C.c_long
         L.or_p2_stiffness2d.argtypes = [_dp, _ip, C.c_int, C.c_long, _dp, _vp, C.c_int] + csc_out
         L.or_p2_mass2d.restype = C.c_long
@@ -267,6 +270,76 @@ def transport_be(mesh, T0, rhoCp, kappa, u, dt, nsteps, faces6=None, face_F=None
         T = lu.solve(M @ T)
         out.append(T.copy())
     return out
+
+
+def nedelec_edges(mesh):
+    """Edge unknowns of a P2 tetrahedral mesh as src/mesh.jl:168-183 numbers them:
+    ``unique(t[5:10, :])`` in first-appearance order (element by element) mapped to
+    1..ne (here 0..ne-1).  Returns (edges 6 x nt, ne)."""
+    mids = np.asarray(mesh.t[4:10], dtype=np.int64)
+    flat = mids.T.ravel()
+    _, first = np.unique(flat, return_index=True)
+    order = np.sort(first)
+    rank = np.full(int(flat.max()) + 1, -1, dtype=np.int64)
+    rank[flat[order]] = np.arange(order.size)
+    return rank[mids].astype(np.int32), int(order.size)
+
+
+def _ned_args(mesh):
+    p = _c(mesh.p.T, np.float64)
+    t4 = _c(np.asarray(mesh.t[:4]).T, np.int32)
+    return p, t4
+
+
+def nedelecLocalStiffness(mesh, nu=None):
+    """``src/FEM3D.jl:155-191``: Ak (36 x nt; column k the 6 x 6 block row-major)."""
+    p, t4 = _ned_args(mesh)
+    Ak = np.zeros(36 * mesh.nt)
+    nv_ = None if nu is None else _c(nu, np.float64)
+    lib().or_nedelec_local(p, t4, 4, mesh.nt, _c(mesh.VE, np.float64), _ptr(nv_), 0, None, None, None, Ak)
+    return Ak.reshape(mesh.nt, 36).T
+
+
+def _ned_global(mesh, Ak, edges, ne):
+    e = _c(edges.T, np.int32)
+    m = 36 * mesh.nt
+    cp, ri, v = np.zeros(ne + 1, dtype=np.int64), np.zeros(m, dtype=np.int32), np.zeros(m)
+    V = _c(np.asarray(Ak).T, np.float64)
+    nnz = lib().or_assemble_csc(ne, mesh.nt, 6, e, V, 0, cp, ri, v)
+    return _csc(ne, nnz, cp, ri, v)
+
+
+def nedelecStiffness(mesh, nu=None):
+    """Global curl-curl matrix sum sparse(edge_i, edge_j, Ak .* nu) (nedelec3D.jl:168-178)."""
+    edges, ne = nedelec_edges(mesh)
+    return _ned_global(mesh, nedelecLocalStiffness(mesh, nu), edges, ne)
+
+
+def nedelecTangentialStiffness(mesh, dnu, Bfield, B):
+    """``src/FEM3D.jl:194-271`` (0 where |B| = 0)."""
+    edges, ne = nedelec_edges(mesh)
+    p, t4 = _ned_args(mesh)
+    Ak = np.zeros(36 * mesh.nt)
+    lib().or_nedelec_local(p, t4, 4, mesh.nt, _c(mesh.VE, np.float64), None, 1, _ptr(_c(dnu, np.float64)),
+                           _ptr(_c(np.asarray(Bfield).T, np.float64)), _ptr(_c(B, np.float64)), Ak)
+    return _ned_global(mesh, Ak.reshape(mesh.nt, 36).T, edges, ne)
+
+
+def nedelec_load(mesh, Bext):
+    edges, ne = nedelec_edges(mesh)
+    p, t4 = _ned_args(mesh)
+    rhs = np.zeros(ne)
+    lib().or_nedelec_load(p, t4, 4, mesh.nt, _c(mesh.VE, np.float64), _c(edges.T, np.int32),
+                          _c(Bext, np.float64), rhs)
+    return rhs
+
+
+def nedelec_bfield(mesh, u):
+    edges, _ = nedelec_edges(mesh)
+    p, t4 = _ned_args(mesh)
+    Bf, Bn = np.zeros(3 * mesh.nt), np.zeros(mesh.nt)
+    lib().or_nedelec_bfield(p, t4, 4, mesh.nt, _c(edges.T, np.int32), _c(u, np.float64), Bf, Bn)
+    return Bf.reshape(mesh.nt, 3).T, Bn
 
 
 def quadraticStiffnessMatrix2D(mesh, mu=None, shift=True):

@@ -298,3 +298,44 @@ def test_demag_field_matches_direct_solve():
     ok = np.isfinite(Hnd[0])
     assert np.array_equal(np.isfinite(Hn), np.isfinite(Hnd))
     assert np.linalg.norm(Hn[:, ok] - Hnd[:, ok]) / np.linalg.norm(Hnd[:, ok]) < 1e-10
+
+
+def test_nedelec_known_answers():
+    """Whitney edge elements (src/FEM3D.jl:155-191): every element block is symmetric
+    and annihilates the edge values of a gradient, (phi_j - phi_i) / l_e in the local
+    orientation; on one element, the edge values of A = B0 x x / 2 (midpoint rule,
+    exact for a linear A) give B = curl A = B0 exactly, and the load vector is
+    Ak-consistent: RHS = Ak u for that A."""
+    rng = np.random.default_rng(3)
+    m = box_tet_mesh(2, seed=5, order=2)
+    Ak = O.nedelecLocalStiffness(m)
+    I, J = [0, 1, 2, 3, 2, 1], [1, 2, 0, 0, 3, 3]
+    for k in range(m.nt):
+        blk = Ak[:, k].reshape(6, 6)
+        assert np.abs(blk - blk.T).max() <= 1e-12 * np.abs(blk).max()
+        v = m.t[:4, k]
+        phi = rng.normal(size=4)
+        le = np.linalg.norm(m.p[:, v[J]] - m.p[:, v[I]], axis=0)
+        g = (phi[J] - phi[I]) / le
+        assert np.abs(blk @ g).max() <= 1e-10 * np.abs(blk).max() * np.abs(g).max()
+    # one element
+    p = rng.normal(size=(3, 4))
+    mids = [(0, 1), (1, 2), (2, 0), (3, 0), (3, 2), (3, 1)]
+    P = np.hstack([p, np.stack([(p[:, a] + p[:, b]) / 2 for a, b in mids], axis=1)])
+    t = np.arange(10, dtype=np.int32).reshape(10, 1)
+    one = MESH(order=2, dim=3, p=P, t=t, surfaceT=np.zeros((4, 0), np.int32), elementID=np.ones(1, np.int32),
+               InsideElements=np.zeros(0, np.int32), InsideNodes=np.zeros(0, np.int32),
+               VE=element_volumes(P, t[:4]), AE=np.zeros(0), normal=np.zeros((3, 0)), shell_id=(1,),
+               boundary_nodes=np.zeros(0, np.int64))
+    edges, ne = O.nedelec_edges(one)
+    assert ne == 6 and np.array_equal(edges[:, 0], np.arange(6))
+    B0 = np.array([0.5, -0.2, 0.3])
+    u = np.zeros(6)
+    for e in range(6):
+        xm = 0.5 * (p[:, I[e]] + p[:, J[e]])
+        d = p[:, J[e]] - p[:, I[e]]
+        u[e] = 0.5 * np.cross(B0, xm) @ d / np.linalg.norm(d)
+    Bf, Bn = O.nedelec_bfield(one, u)
+    assert np.allclose(Bf[:, 0], B0, rtol=0, atol=1e-12) and abs(Bn[0] - np.linalg.norm(B0)) < 1e-12
+    rhs = O.nedelec_load(one, B0)
+    assert np.allclose(O.nedelecLocalStiffness(one)[:, 0].reshape(6, 6) @ u, rhs, rtol=0, atol=1e-12 * np.abs(rhs).max())
