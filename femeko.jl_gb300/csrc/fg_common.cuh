@@ -334,6 +334,8 @@ void fg_raise_flags(fg_mesh *m, int h, const char *where);
 int fg_pcg_solve(fg_mesh *m, const double *d_b, double *d_x, const fg_solve_opts &o, fg_solve_stats *st,
                  bool newton_inner, double b_norm = -1.0);
 void fg_spmv64_dev(fg_mesh *m, const double *x, double *y);
+// r = b - A x with the given SELL values (no Dirichlet masking); returns ||r|| (syncs)
+double fg_residual_norm(fg_mesh *m, const double *vals, const double *x, const double *b, double *r);
 // y = A x with the given SELL values and no Dirichlet masking
 void fg_spmv64_plain(fg_mesh *m, const double *vals, const double *x, double *y);
 // Jacobi right-preconditioned BiCGStab on the FP64 operator (val64, dinv64), no

@@ -2662,3 +2662,19 @@ int fg_bicgstab_solve(fg_mesh *m, const double *d_b, double *d_x, const fg_solve
   }
   return status;
 }
+
+// r = b - A x with the given SELL values (no Dirichlet masking); returns ||r||.
+double fg_residual_norm(fg_mesh *m, const double *vals, const double *x, const double *b, double *r) {
+  constexpr int slot = 9;
+  if (m->use_dcol)
+    k_spmv64<ColRel><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_dcol, vals, x, b, r,
+                                                         nullptr, slot, m->scal, m->red.partials, m->red.counter);
+  else
+    k_spmv64<ColAbs><<<row_grid(m), 256, 0, m->stream>>>(m->nv, m->sl_ptr, m->sl_len, m->sl_col, vals, x, b, r,
+                                                         nullptr, slot, m->scal, m->red.partials, m->red.counter);
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(1);
+  FG_CUDA_TRY(cudaMemcpyAsync(m->hbuf, m->scal + slot, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+  fg_sync(m);
+  return std::sqrt(m->hbuf[0]);
+}

@@ -430,4 +430,4 @@ def hfield(mesh: MESH, u):
 
 
 from .nedelec import (edge_mesh, nedelec_edges, nedelecLocalStiffness, nedelecStiffness,  # noqa: E402,F401
-                      nedelecTangentialStiffness, nedelec_load, nedelec_bfield, nedelec_linear)
+                      nedelecTangentialStiffness, nedelec_load, nedelec_bfield, nedelec_linear, nedelec_newton)

@@ -105,6 +105,8 @@ SIGNATURES = {
     "fg_nedelec_load": [_vp, _vp, _vp],
     "fg_nedelec_bfield": [_vp, _vp, _vp, _vp],
     "fg_nedelec_linear": [_vp, _vp, _vp, _vp, _vp, _vp, C.POINTER(SolveOpts), C.POINTER(SolveStats)],
+    "fg_nedelec_newton": [_vp, _vp, _vp, _vp, _vp, _vp, _i32, _d, _i32, _d, _vp, _vp, _vp, _vp, _vp,
+                          C.POINTER(SolveOpts), C.POINTER(SolveStats)],
     "fg_transport_be": [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _d, _i32, _i32, _vp, _i32, _vp,
                         C.POINTER(SolveOpts), C.POINTER(SolveStats)],
     "fg_batch_magnetostatics_linear": [_vp, _i32, _vp, _vp, C.POINTER(SolveOpts), _vp, _vp, C.POINTER(BatchStats)],

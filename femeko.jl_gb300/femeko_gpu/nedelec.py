@@ -136,3 +136,30 @@ def nedelec_linear(mesh: MESH, Bext, nu=None, precision="fp64", rtol=1e-10, maxi
                                    C.byref(o), C.byref(s))
     L.check(st, allow_not_converged=True)
     return u, Bf.reshape(mesh.nt, 3).T, B, L.stats_dict(s)
+
+
+def nedelec_newton(mesh: MESH, Bext, curve_B, curve_nu, nonlinear=None, nu_lin=None, tol=1e-4, max_newton=100,
+                   min_step=1e-4, precision="fp64", rtol=1e-10, maxiter=1_000_000):
+    """The Newton loop of Magnetostatics/nedelec3D.jl:149-231 on the GPU with the
+    material curve nu(B) given as a table (not-a-knot cubic interpolant, as Dierckx's
+    Spline1D(B, nu)).  nonlinear: element mask (default: ``mesh.InsideElements``).
+    Returns (u, Bfield 3 x nt, |B|, nu, newton steps, stats)."""
+    from . import solve_opts
+    g = edge_mesh(mesh)
+    if nonlinear is None:
+        nonlinear = np.zeros(mesh.nt, dtype=np.uint8)
+        nonlinear[np.asarray(mesh.InsideElements, dtype=np.int64)] = 1
+    u = np.zeros(g.ne)
+    Bf, B, nu = np.zeros(3 * mesh.nt), np.zeros(mesh.nt), np.zeros(mesh.nt)
+    it = C.c_int32()
+    o = solve_opts(precision=precision, rtol=rtol, maxiter=maxiter)
+    s = L.SolveStats()
+    nl_ = None if nu_lin is None else _c(nu_lin, np.float64)
+    cb, cn = _c(curve_B, np.float64), _c(curve_nu, np.float64)
+    st = L.lib().fg_nedelec_newton(g.h, L.ptr(_c(Bext, np.float64)), L.ptr(_c(nonlinear, np.uint8)), L.ptr(nl_),
+                                   L.ptr(cb), L.ptr(cn), int(cb.size), float(tol), int(max_newton), float(min_step),
+                                   L.ptr(u), L.ptr(Bf), L.ptr(B), L.ptr(nu), C.byref(it), C.byref(o), C.byref(s))
+    L.check(st, allow_not_converged=True)
+    d = L.stats_dict(s)
+    d["short_inner_solves"] = s.pad_
+    return u, Bf.reshape(mesh.nt, 3).T, B, nu, it.value, d

@@ -288,9 +288,30 @@ fg_status fg_nedelec_bfield(fg_mesh *m, const double *u, double *Bfield, double 
 /* The first Newton step of nedelec3D.jl (u = 0, At = 0): A(nu) u = RHS(Bext) by the
  * Jacobi-PCG of fg_pcg (the curl-curl matrix is singular with a consistent right-hand
  * side: u is one solution, B = curl u is unique); Bfield/B (may be NULL) as in
- * fg_nedelec_bfield. */
+ * fg_nedelec_bfield.  Runs in FP64 whatever o->precision says: the mixed path's FP32
+ * inner iterations stall on this singular system at high permeability contrast. */
 fg_status fg_nedelec_linear(fg_mesh *m, const double *nu, const double *Bext, double *u, double *Bfield, double *B,
                             const fg_solve_opts *o, fg_solve_stats *s);
+
+/* The Newton loop of Magnetostatics/nedelec3D.jl:149-231 on the GPU: nu = 1 (nu_lin
+ * on the elements outside `nonlinear`, NULL = ones), u = 0; per step A(nu), At (from
+ * the second step), du = PCG(A + At, RHS - A u) (o->rtol), the line search of
+ * src/FEM3D.jl:122-151 (steps x0.9 down to min_step), B = curl u, then on the
+ * `nonlinear` elements nu = spl(|B|), dnu = spl_dnu(|B|), until max |B - B_prev| <= tol
+ * or max_newton steps.  spl is the not-a-knot interpolating cubic through
+ * (curve_B, curve_nu) (the interpolant of Dierckx's Spline1D(B, nu), s = 0), spl_dnu
+ * the same through the finite-difference gradient of src/FEM.jl:66-92; both are held
+ * at their end values outside the data (bc = "nearest").  ncurve >= 4, curve_B
+ * increasing.  Outputs: u (ne), Bfield (3 x nt), B (nt), nu_out (nt) (each may be NULL
+ * but u), newton_iters; stats: iterations = CG iterations in total, refinements =
+ * Newton steps, relres = the last line-search residual ||RHS - A u||, pad_ = inner
+ * solves that stopped short of o->rtol (their corrections are used, as the
+ * reference's cg returns what it has); FG_NOT_CONVERGED when max_newton steps end
+ * with max |B - B_prev| > tol. */
+fg_status fg_nedelec_newton(fg_mesh *m, const double *Bext, const uint8_t *nonlinear, const double *nu_lin,
+                            const double *curve_B, const double *curve_nu, int32_t ncurve, double tol,
+                            int32_t max_newton, double min_step, double *u, double *Bfield, double *B,
+                            double *nu_out, int32_t *newton_iters, const fg_solve_opts *o, fg_solve_stats *s);
 
 /* Heat transport with convection on P2 tetrahedra (Transport/main3D.jl:143-213):
  * LM = M(rho_cp) + dt (A(kappa) + R + C(vel, rho_cp)), then nsteps steps of

@@ -342,6 +342,64 @@ def nedelec_bfield(mesh, u):
     return Bf.reshape(mesh.nt, 3).T, Bn
 
 
+def fd_gradient(x, y):
+    """``src/FEM.jl:66-92``: one-sided differences at the ends, central inside."""
+    x, y = np.asarray(x, dtype=np.float64), np.asarray(y, dtype=np.float64)
+    z = np.empty_like(y)
+    z[0] = (y[1] - y[0]) / (x[1] - x[0])
+    z[-1] = (y[-1] - y[-2]) / (x[-1] - x[-2])
+    z[1:-1] = (y[2:] - y[:-2]) / (x[2:] - x[:-2])
+    return z
+
+
+def nedelec_splines(curve_B, curve_nu):
+    """spl, spl_dnu of nedelec3D.jl:45-49: not-a-knot interpolating cubics (Dierckx
+    Spline1D with s = 0), held at their end values outside the data (bc "nearest")."""
+    from scipy.interpolate import CubicSpline
+    x = np.asarray(curve_B, dtype=np.float64)
+    s1 = CubicSpline(x, curve_nu, bc_type="not-a-knot")
+    s2 = CubicSpline(x, fd_gradient(x, curve_nu), bc_type="not-a-knot")
+    return (lambda b: s1(np.clip(b, x[0], x[-1]))), (lambda b: s2(np.clip(b, x[0], x[-1])))
+
+
+def nedelec_newton(mesh, Bext, curve_B, curve_nu, nonlinear, nu_lin=None, tol=1e-4, max_newton=100, min_step=1e-4,
+                   cg_rtol=1e-12):
+    """Magnetostatics/nedelec3D.jl:149-231 with scipy's CG for the corrections."""
+    import scipy.sparse.linalg as spla
+    spl, spl_dnu = nedelec_splines(curve_B, curve_nu)
+    nl = np.asarray(nonlinear, dtype=bool)
+    nt = mesh.nt
+    nu = np.ones(nt)
+    if nu_lin is not None:
+        nu[~nl] = np.asarray(nu_lin)[~nl]
+    dnu = np.zeros(nt)
+    rhs = nedelec_load(mesh, Bext)
+    u = np.zeros(rhs.size)
+    Bf, B = np.zeros((3, nt)), np.zeros(nt)
+    att, div = 0, np.inf
+    while div > tol and att < max_newton:
+        att += 1
+        Bold = B.copy()
+        A = nedelecStiffness(mesh, nu)
+        K = A + nedelecTangentialStiffness(mesh, dnu, Bf, B) if att > 1 else A
+        du, _ = spla.cg(K, rhs - A @ u, rtol=cg_rtol, maxiter=100000)
+        res_old = np.linalg.norm(rhs - A @ u)
+        alf = 1.0
+        trial = u + du
+        res = np.linalg.norm(rhs - A @ trial)
+        while res > res_old and alf > min_step:
+            alf *= 0.9
+            trial = u + alf * du
+            res = np.linalg.norm(rhs - A @ trial)
+        if not alf < min_step:
+            u = trial
+        Bf, B = nedelec_bfield(mesh, u)
+        nu[nl] = spl(B[nl])
+        dnu[nl] = spl_dnu(B[nl])
+        div = np.abs(B - Bold).max()
+    return u, Bf, B, nu, att
+
+
 def quadraticStiffnessMatrix2D(mesh, mu=None, shift=True):
     """``src/FEM2D.jl:80-137``."""
     p, t = _pt(mesh)
