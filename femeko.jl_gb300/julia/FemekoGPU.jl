@@ -187,6 +187,69 @@ end
 massMatrix2D(mesh) = massMatrix(mesh)
 quadraticMassMatrix(mesh, S, F::Vector{Float64}=ones(size(mesh.t, 2))) = massMatrix(mesh; F=F)
 
+# ---------------------------------------------------------------- Nedelec edge elements
+const EDGE_HANDLES = WeakKeyDict{Any,GPUMesh}()
+
+"""A handle over the edges of a second-order mesh (the unknowns of
+Magnetostatics/nedelec3D.jl): mesh.edge2localMap[mesh.t[5:10, :]], 1-based."""
+function EdgeGPUMesh(mesh)
+    edges = Int32.(mesh.edge2localMap[mesh.t[5:10, :]])
+    t4 = Int32.(mesh.t[1:4, :])
+    ne = Int(mesh.ne)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:fg_edge_mesh_create, libpath()), Cint,
+                (Ptr{Float64}, Int64, Ptr{Int32}, Ptr{Int32}, Int64, Int64, Int32, Ref{Ptr{Cvoid}}),
+                mesh.p, size(mesh.p, 2), t4, edges, size(mesh.t, 2), ne, 1, h))
+    nnz = Ref{Int64}(0); mr = Ref{Int32}(0)
+    check(ccall((:fg_mesh_nnz, libpath()), Cint, (Ptr{Cvoid}, Ref{Int64}, Ref{Int32}), h[], nnz, mr))
+    colptr = zeros(Int64, ne + 1)
+    rowval = zeros(Int32, nnz[])
+    check(ccall((:fg_csc_pattern, libpath()), Cint, (Ptr{Cvoid}, Ptr{Int64}, Ptr{Int32}, Int32),
+                h[], colptr, rowval, 1))
+    g = GPUMesh(h[], ne, size(mesh.t, 2), nnz[], colptr, rowval)
+    finalizer(g) do x
+        x.h != C_NULL && ccall((:fg_mesh_destroy, libpath()), Cint, (Ptr{Cvoid},), x.h)
+        x.h = C_NULL
+    end
+    return g
+end
+
+edgegpu(mesh) = get!(() -> EdgeGPUMesh(mesh), EDGE_HANDLES, mesh)
+
+"""nedelecLocalStiffness(mesh) -- src/FEM3D.jl:155-191 on the GPU (36 x nt)."""
+function nedelecLocalStiffness(mesh)
+    g = edgegpu(mesh); Ak = zeros(36, g.nt)
+    check(ccall((:fg_nedelec_local_stiffness, libpath()), Cint, (Ptr{Cvoid}, Ptr{Float64}), g.h, Ak))
+    return Ak
+end
+
+"""nedelecTangentialStiffness(mesh, dnu, Bfield, B) -- src/FEM3D.jl:194-271 on the GPU."""
+function nedelecTangentialStiffness(mesh, dnu::Vector{Float64}, Bfield::Matrix{Float64}, B::Vector{Float64})
+    g = edgegpu(mesh); v = zeros(g.nnz)
+    check(ccall((:fg_nedelec_tangent, libpath()), Cint,
+                (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}), g.h, dnu, Bfield, B, v))
+    return csc(g, v)
+end
+
+"""nedelec_newton(mesh, Bext, curve_B, curve_nu) -- the Newton loop of
+Magnetostatics/nedelec3D.jl:149-231 on the GPU, nu(B) the not-a-knot cubic through the
+table (Spline1D(B, nu)); returns (u, Bfield, B, nu, steps, stats)."""
+function nedelec_newton(mesh, Bext::Vector{Float64}, curve_B::Vector{Float64}, curve_nu::Vector{Float64};
+                        tol=1e-4, maxAtt::Integer=100, minStep=1e-4, rtol=1e-10)
+    g = edgegpu(mesh)
+    nl = zeros(UInt8, g.nt); nl[mesh.InsideElements] .= 1
+    u = zeros(g.nv); Bf = zeros(3, g.nt); B = zeros(g.nt); nu = zeros(g.nt); it = Ref{Int32}(0)
+    o = Ref(solve_opts(precision=:fp64, rtol=rtol))
+    s = Ref{SolveStats}()
+    st = ccall((:fg_nedelec_newton, libpath()), Cint,
+               (Ptr{Cvoid}, Ptr{Float64}, Ptr{UInt8}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int32, Float64, Int32,
+                Float64, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ref{Int32}, Ref{SolveOpts},
+                Ref{SolveStats}),
+               g.h, Bext, nl, C_NULL, curve_B, curve_nu, length(curve_B), tol, maxAtt, minStep, u, Bf, B, nu, it, o, s)
+    check(st; allow_not_converged=true)
+    return u, Bf, B, nu, Int(it[]), s[]
+end
+
 """quadraticConvectionMatrix(mesh, S, u, F) -- src/FEM3D.jl:563-648 on the GPU (S is
 not used: the basis is built per element on the device).  u: 3 x nv velocity."""
 function quadraticConvectionMatrix(mesh, S, u::Matrix{Float64}, F::Vector{Float64}=ones(size(mesh.t, 2));
