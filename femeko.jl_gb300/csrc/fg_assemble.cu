@@ -332,10 +332,20 @@ __global__ void k_elem_tet10(int kind, int full_phi, int64_t nt, const double *_
   }
 }
 
+// 4-point rule of src/FEM2D.jl:477-484 (GaussQuadrature2D(3)), weights summing to 1.
+__constant__ double c_gq2c_pts[4][2] = {{1.0 / 3.0, 1.0 / 3.0}, {0.2, 0.2}, {0.6, 0.2}, {0.2, 0.6}};
+__constant__ double c_gq2c_w[4] = {-27.0 / 48.0, 25.0 / 48.0, 25.0 / 48.0, 25.0 / 48.0};
+
 // P2 triangle (6 nodes).  ASM_STIFF: 6-node equal-weight rule, /6
 // (src/FEM2D.jl:95-107).  ASM_MASS: 6-point rule, w = weight * VE (src/FEM2D.jl:192-212).
+// ASM_CONV: src/FEM2D.jl:231-319, the velocity (vel, 3 x nv, z unused) interpolated
+// with the P2 basis at each point of the 4-point rule, w = weight * VE; the reference's
+// Ck[i,j] = w (grad phi_i . u) phi_j scattered from its column-major flattening gives
+// C[t_i, t_j] = sum w (u . grad phi_j) phi_i, whose rows are recorded here
+// (transpose = 1 records the rows of C^T, the CSC export).
 __global__ void k_elem_tri6(int kind, int64_t nt, const double *__restrict__ p, const int *__restrict__ t,
                             const double *__restrict__ geo, const double *__restrict__ f,
+                            const double *__restrict__ vel, int transpose, int accumulate,
                             const int *__restrict__ recpos, double *__restrict__ rec, int *flags) {
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nt) return;
@@ -366,6 +376,31 @@ __global__ void k_elem_tri6(int kind, int64_t nt, const double *__restrict__ p, 
     }
     for (int i = 0; i < 6; ++i)
       for (int j = i; j < 6; ++j) { Ke[i][j] = Ke[i][j] / 6.0 * VE * fk; Ke[j][i] = Ke[i][j]; }
+  } else if (kind == ASM_CONV) {
+    const double e1 = p[3 * nds[1]] - x0, e2 = p[3 * nds[2]] - x0;
+    const double f1 = p[3 * nds[1] + 1] - y0, f2 = p[3 * nds[2] + 1] - y0;
+    for (int q = 0; q < 4; ++q) {
+      const double xi = c_gq2c_pts[q][0], eta = c_gq2c_pts[q][1];
+      const double Xq = e1 * xi + e2 * eta, Yq = f1 * xi + f2 * eta;
+      double phi[6], gx[6], gy[6], ux = 0.0, uy = 0.0;
+      for (int a = 0; a < 6; ++a) {
+        phi[a] = S[a] + S[6 + a] * Xq + S[12 + a] * Yq + S[18 + a] * Xq * Xq + S[24 + a] * Xq * Yq + S[30 + a] * Yq * Yq;
+        ux += vel[3 * nds[a]] * phi[a];
+        uy += vel[3 * nds[a] + 1] * phi[a];
+        gx[a] = S[6 + a] + 2 * S[18 + a] * Xq + S[24 + a] * Yq;
+        gy[a] = S[12 + a] + 2 * S[30 + a] * Yq + S[24 + a] * Xq;
+      }
+      const double w = c_gq2c_w[q] * VE;
+      for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) Ke[i][j] += w * (gx[j] * ux + gy[j] * uy) * phi[i] * fk;
+    }
+    if (transpose)
+      for (int i = 0; i < 6; ++i)
+        for (int j = i + 1; j < 6; ++j) {
+          const double tmp = Ke[i][j];
+          Ke[i][j] = Ke[j][i];
+          Ke[j][i] = tmp;
+        }
   } else {
     double e1 = p[3 * nds[1]] - x0, e2 = p[3 * nds[2]] - x0;
     double f1 = p[3 * nds[1] + 1] - y0, f2 = p[3 * nds[2] + 1] - y0;
@@ -382,7 +417,14 @@ __global__ void k_elem_tri6(int kind, int64_t nt, const double *__restrict__ p, 
     for (int i = 0; i < 6; ++i)
       for (int j = i + 1; j < 6; ++j) Ke[j][i] = Ke[i][j];
   }
-  for (int a = 0; a < 6; ++a) store_row<6, double>(rec, recpos[(int64_t)a * nt + k], Ke[a]);
+  if (accumulate) {
+    for (int a = 0; a < 6; ++a) {
+      double *r = rec + (int64_t)recpos[(int64_t)a * nt + k] * 6;
+      for (int j = 0; j < 6; ++j) r[j] += Ke[a][j];
+    }
+  } else {
+    for (int a = 0; a < 6; ++a) store_row<6, double>(rec, recpos[(int64_t)a * nt + k], Ke[a]);
+  }
 }
 
 // ------------------------------------------------------------------ Newton element pass
@@ -931,9 +973,11 @@ static void launch_elem(fg_mesh *m, int kind, const double *d_f, const double *d
                                                                0, m->recpos, rec, m->flags);
       break;
     default:
-      FG_REQUIRE(kind == ASM_STIFF || kind == ASM_MASS, FG_UNSUPPORTED, "P2: stiffness and mass only");
-      k_elem_tri6<<<grid_for(m->nt, 64), 64, 0, m->stream>>>(kind, m->nt, m->p, m->t, m->geo, d_f, m->recpos, rec,
-                                                              m->flags);
+      FG_REQUIRE(kind == ASM_STIFF || kind == ASM_MASS || kind == ASM_CONV, FG_UNSUPPORTED,
+                 "P2 triangles: stiffness, mass and convection only");
+      k_elem_tri6<<<grid_for(m->nt, 64), 64, 0, m->stream>>>(kind, m->nt, m->p, m->t, m->geo, d_f,
+                                                              kind == ASM_CONV ? d_H : nullptr, transpose ? 1 : 0, 0,
+                                                              m->recpos, rec, m->flags);
       break;
   }
   FG_CUDA_TRY(cudaGetLastError());
@@ -944,7 +988,10 @@ void fg_assemble_operator(fg_mesh *m, int kind, const double *d_f, const double 
                           double c_mass, double c_stiff, int full_phi, int layout, bool want64, bool want32,
                           bool apply_bc) {
   if (layout != OUT_CSR) { m->op_tag = 0; ++m->op_version; }
-  launch_elem(m, kind, d_f, d_H, d_dmu, c_mass, c_stiff, full_phi, kind == ASM_CONV && layout != OUT_CSR);
+  // convection: the 3D records are the rows of the reference's C^T, the 2D records
+  // the rows of its C (see the element kernels); transpose to what the layout needs
+  const bool tr = kind == ASM_CONV && ((m->npe == 10) == (layout != OUT_CSR));
+  launch_elem(m, kind, d_f, d_H, d_dmu, c_mass, c_stiff, full_phi, tr);
   const double *rec = static_cast<const double *>(m->rec);
   if (layout == OUT_CSR) {
     if (!m->csrval) m->csrval = dev_alloc<double>(m, (size_t)m->nnz);
@@ -1105,7 +1152,8 @@ void fg_nedelec_local_dev(fg_mesh *m, double *d_Ak) {
 
 void fg_transport_operator(fg_mesh *m, const double *d_rhocp, const double *d_kdt, const double *d_vel,
                            const double *d_fdt, int full_phi) {
-  FG_REQUIRE(m->npe == 10, FG_UNSUPPORTED, "transport operator: P2 tetrahedra only");
+  FG_REQUIRE(!m->edge && (m->npe == 10 || m->npe == 6), FG_UNSUPPORTED,
+             "transport operator: P2 tetrahedra or P2 triangles only");
   m->op_tag = 0;
   ++m->op_version;
   fg_ensure_records(m);
@@ -1113,17 +1161,20 @@ void fg_transport_operator(fg_mesh *m, const double *d_rhocp, const double *d_kd
   if (!m->mval) m->mval = dev_alloc<double>(m, (size_t)m->nsell);
   double *rec = static_cast<double *>(m->rec);
   const unsigned g = grid_for(m->nt, 64);
-  // records: M; gathered alone into mval, then + K + C^ on the same records
-  k_elem_tet10<<<g, 64, 0, m->stream>>>(ASM_MASS, full_phi, m->nt, m->p, m->t, m->geo, d_rhocp, nullptr, 0, 0,
-                                        m->recpos, rec, m->flags);
-  FG_CUDA_TRY(cudaGetLastError());
+  // records: M; gathered alone into mval, then + K + C on the same records (the rows
+  // of the reference's C: transposed records in 3D, as they come in 2D)
+  auto elem = [&](int kind, const double *f, const double *vel, int acc) {
+    if (m->npe == 10)
+      k_elem_tet10<<<g, 64, 0, m->stream>>>(kind, full_phi, m->nt, m->p, m->t, m->geo, f, vel, kind == ASM_CONV ? 1 : 0,
+                                            acc, m->recpos, rec, m->flags);
+    else
+      k_elem_tri6<<<g, 64, 0, m->stream>>>(kind, m->nt, m->p, m->t, m->geo, f, vel, 0, acc, m->recpos, rec, m->flags);
+    FG_CUDA_TRY(cudaGetLastError());
+  };
+  elem(ASM_MASS, d_rhocp, nullptr, 0);
   launch_row_any<double, double>(m, rec, nullptr, 0, m->mval, nullptr, nullptr, nullptr, nullptr, nullptr, 0.0, 0);
-  k_elem_tet10<<<g, 64, 0, m->stream>>>(ASM_STIFF, full_phi, m->nt, m->p, m->t, m->geo, d_kdt, nullptr, 0, 1,
-                                        m->recpos, rec, m->flags);
-  FG_CUDA_TRY(cudaGetLastError());
-  k_elem_tet10<<<g, 64, 0, m->stream>>>(ASM_CONV, full_phi, m->nt, m->p, m->t, m->geo, d_fdt, d_vel, 1, 1,
-                                        m->recpos, rec, m->flags);
-  FG_CUDA_TRY(cudaGetLastError());
+  elem(ASM_STIFF, d_kdt, nullptr, 1);
+  elem(ASM_CONV, d_fdt, d_vel, 1);
   FG_LAUNCHED(3);
   launch_row_any<double, double>(m, rec, nullptr, 0, m->val64, nullptr, nullptr, m->dinv64, nullptr, nullptr, 0.0, 0);
 }
@@ -1140,10 +1191,19 @@ __device__ __forceinline__ double face_mass_coef(int i, int j) {
   return ((e + 2) % 3 == v) ? -4.0 : 0.0;
 }
 
+// src/FEM2D.jl:394-419 quadraticMassMatrix1D: (1/30) [4 2 -1; 2 16 2; -1 2 4] by the
+// position of the node in the face's three surfaceT rows, entry AE[s] Mk[i,j] h[s].
+__device__ __forceinline__ double line_mass_coef(int i, int j) {
+  if (i == 1 && j == 1) return 16.0;
+  if (i == j) return 4.0;
+  if (i == 1 || j == 1) return 2.0;
+  return -1.0;
+}
+
 // One thread per listed row: adds its faces' entries, in face order, into the row
 // (SELL values, then the Jacobi inverse from the row's diagonal slot; or CSR values).
 __global__ void k_face_mass(int64_t nrows, const int *__restrict__ rows, const int *__restrict__ fptr,
-                            const int *__restrict__ flist, const int *__restrict__ faces,
+                            const int *__restrict__ flist, const int *__restrict__ faces, int fw,
                             const double *__restrict__ AE, const double *__restrict__ F, double scale,
                             const int *__restrict__ sl_ptr, const int *__restrict__ sl_col,
                             const int16_t *__restrict__ sl_dcol, const int *__restrict__ rowlen,
@@ -1156,11 +1216,12 @@ __global__ void k_face_mass(int64_t nrows, const int *__restrict__ rows, const i
   const int s = r >> 5, lane = r & 31;
   for (int e = fptr[idx]; e < fptr[idx + 1]; ++e) {
     const int face = flist[e] >> 3, li = flist[e] & 7;
-    for (int j = 0; j < 6; ++j) {
-      const double c = face_mass_coef(li, j);
+    for (int j = 0; j < fw; ++j) {
+      const double c = fw == 6 ? face_mass_coef(li, j) : line_mass_coef(li, j);
       if (c == 0.0) continue;
-      const double v = scale * (AE[face] * ((1.0 / 180.0) * c) * F[face]);
-      const int col = faces[6 * (int64_t)face + j];
+      const double mk = fw == 6 ? (1.0 / 180.0) * c : (1.0 / 30.0) * c;
+      const double v = scale * (AE[face] * mk * F[face]);
+      const int col = faces[fw * (int64_t)face + j];
       int64_t pos = -1;
       if (csr) {
         for (int q = rowptr[r]; q < rowptr[r + 1]; ++q)
@@ -1181,11 +1242,12 @@ __global__ void k_face_mass(int64_t nrows, const int *__restrict__ rows, const i
 
 void fg_face_mass(fg_mesh *m, bool sell, const int *d_rows, int64_t nrows, const int *d_fptr, const int *d_flist,
                   const int *d_faces, const double *d_AE, const double *d_F, double scale) {
+  const int fw = m->npe == 10 ? 6 : 3;
   if (nrows == 0) return;
   FG_REQUIRE(!sell || m->val64, FG_BAD_ARG, "boundary mass: no FP64 operator assembled");
   if (!sell && !m->csrval) m->csrval = dev_alloc<double>(m, (size_t)m->nnz);
   k_face_mass<<<grid_for(nrows, 128), 128, 0, m->stream>>>(
-      nrows, d_rows, d_fptr, d_flist, d_faces, d_AE, d_F, scale, m->sl_ptr, m->use_dcol ? nullptr : m->sl_col,
+      nrows, d_rows, d_fptr, d_flist, d_faces, fw, d_AE, d_F, scale, m->sl_ptr, m->use_dcol ? nullptr : m->sl_col,
       m->sl_dcol, m->rowlen, m->diagk, m->val64, m->dinv64, m->rowptr, m->colidx, sell ? nullptr : m->csrval,
       m->flags);
   FG_CUDA_TRY(cudaGetLastError());
@@ -1564,7 +1626,8 @@ extern "C" fg_status fg_convection(fg_mesh *m, const double *vel, const double *
   double *tf = nullptr, *tv = nullptr;
   fg_status st = fg_guard([&]() -> fg_status {
     FG_REQUIRE(m && vel && nzval, FG_BAD_ARG, "fg_convection: null pointer");
-    FG_REQUIRE(m->npe == 10, FG_UNSUPPORTED, "fg_convection: P2 tetrahedra only (src/FEM3D.jl:563-648)");
+    FG_REQUIRE(!m->edge && (m->npe == 10 || m->npe == 6), FG_UNSUPPORTED,
+               "fg_convection: P2 tetrahedra (src/FEM3D.jl:563-648) or P2 triangles (src/FEM2D.jl:231-319)");
     double *df = upload_opt(m, f, (size_t)m->nt, tf);
     double *dv = upload_opt(m, vel, 3 * (size_t)m->nv, tv);
     fg_assemble_operator(m, ASM_CONV, df, dv, nullptr, 0.0, 0.0, full_phi, OUT_CSR, false, false, false);

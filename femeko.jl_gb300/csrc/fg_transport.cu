@@ -1,4 +1,5 @@
-// Heat transport with convection on P2 tetrahedra (Transport/main3D.jl:143-213):
+// Heat transport with convection on P2 tetrahedra (Transport/main3D.jl:143-213) and
+// P2 triangles (Transport/main2D.jl:150-190, with the 2D matrices of src/FEM2D.jl):
 // intake faces carry a penalty boundary mass R (src/FEM3D.jl:300-322), and every step
 // solves the backward-Euler system
 //   LM T_{n+1} = M T_n,   LM = M(rho_cp) + dt (A(kappa) + R + C(u, rho_cp))
@@ -15,21 +16,22 @@ namespace {
 
 // Host-side incidence of the faces that carry a nonzero factor: the distinct nodes
 // they touch (rows) and, per row, its (face << 3 | face-local node) entries in face
-// order.  faces is 6 x nf column-major, 0-based.
+// order.  faces is fw x nf column-major, 0-based (fw = 6: P2 triangles of a
+// tetrahedral mesh, 3: P2 lines of a triangle mesh).
 struct FaceRows {
   std::vector<int> rows, fptr, flist;
 };
 
-FaceRows face_rows(const int32_t *faces, const double *AE, const double *F, int64_t nf, int64_t nv) {
+FaceRows face_rows(const int32_t *faces, int fw, const double *AE, const double *F, int64_t nf, int64_t nv) {
   FaceRows fr;
   std::vector<int> count((size_t)nv, 0), slot((size_t)nv, -1);
   for (int64_t s = 0; s < nf; ++s) {
     if (AE[s] * F[s] == 0.0) continue;
-    for (int i = 0; i < 6; ++i) {
-      const int64_t v = faces[6 * s + i];
+    for (int i = 0; i < fw; ++i) {
+      const int64_t v = faces[fw * s + i];
       FG_REQUIRE(v >= 0 && v < nv, FG_BAD_ARG, "boundary faces: node index out of range");
       for (int j = 0; j < i; ++j)
-        FG_REQUIRE(faces[6 * s + j] != v, FG_BAD_ARG, "boundary faces: a face repeats a node");
+        FG_REQUIRE(faces[fw * s + j] != v, FG_BAD_ARG, "boundary faces: a face repeats a node");
       ++count[(size_t)v];
     }
   }
@@ -45,7 +47,7 @@ FaceRows face_rows(const int32_t *faces, const double *AE, const double *F, int6
   for (int64_t s = 0; s < nf; ++s) {
     if (AE[s] * F[s] == 0.0) continue;
     FG_REQUIRE(s < (1 << 28), FG_BAD_ARG, "boundary faces: too many faces");
-    for (int i = 0; i < 6; ++i) fr.flist[(size_t)cur[(size_t)slot[(size_t)faces[6 * s + i]]]++] = (int)(s << 3 | i);
+    for (int i = 0; i < fw; ++i) fr.flist[(size_t)cur[(size_t)slot[(size_t)faces[fw * s + i]]]++] = (int)(s << 3 | i);
   }
   return fr;
 }
@@ -65,14 +67,14 @@ T *upload(fg_mesh *m, const T *h, size_t n) {
   return d;
 }
 
-FaceDev face_upload(fg_mesh *m, const FaceRows &fr, const int32_t *faces, const double *AE, const double *F,
+FaceDev face_upload(fg_mesh *m, const FaceRows &fr, const int32_t *faces, int fw, const double *AE, const double *F,
                     int64_t nf) {
   FaceDev d;
   d.nrows = (int64_t)fr.rows.size();
   d.rows = upload(m, fr.rows.data(), fr.rows.size());
   d.fptr = upload(m, fr.fptr.data(), fr.fptr.size());
   d.flist = upload(m, fr.flist.data(), fr.flist.size());
-  d.faces = upload(m, faces, 6 * (size_t)nf);
+  d.faces = upload(m, faces, (size_t)fw * (size_t)nf);
   d.AE = upload(m, AE, (size_t)nf);
   d.F = upload(m, F, (size_t)nf);
   return d;
@@ -91,16 +93,18 @@ extern "C" fg_status fg_boundary_mass(fg_mesh *m, const int32_t *faces, const do
   FaceDev d;
   fg_status st = fg_guard([&]() -> fg_status {
     FG_REQUIRE(m && nzval && (nfaces == 0 || (faces && AE)), FG_BAD_ARG, "fg_boundary_mass: null pointer");
-    FG_REQUIRE(m->npe == 10, FG_UNSUPPORTED, "fg_boundary_mass: P2 tetrahedra only (src/FEM3D.jl:300-322)");
+    FG_REQUIRE(!m->edge && (m->npe == 10 || m->npe == 6), FG_UNSUPPORTED,
+               "fg_boundary_mass: P2 tetrahedra (src/FEM3D.jl:300-322) or P2 triangles (src/FEM2D.jl:394-419)");
+    const int fw = m->npe == 10 ? 6 : 3;
     std::vector<double> ones;
     if (!F) {
       ones.assign((size_t)nfaces, 1.0);
       F = ones.data();
     }
-    const FaceRows fr = face_rows(faces, AE, F, nfaces, m->nv);
+    const FaceRows fr = face_rows(faces, fw, AE, F, nfaces, m->nv);
     if (!m->csrval) m->csrval = dev_alloc<double>(m, (size_t)m->nnz);
     FG_CUDA_TRY(cudaMemsetAsync(m->csrval, 0, sizeof(double) * (size_t)m->nnz, m->stream));
-    d = face_upload(m, fr, faces, AE, F, nfaces);
+    d = face_upload(m, fr, faces, fw, AE, F, nfaces);
     fg_face_mass(m, false, d.rows, d.nrows, d.fptr, d.flist, d.faces, d.AE, d.F, 1.0);
     FG_CUDA_TRY(cudaMemcpyAsync(nzval, m->csrval, sizeof(double) * (size_t)m->nnz, cudaMemcpyDeviceToHost, m->stream));
     fg_sync(m);
@@ -120,7 +124,9 @@ extern "C" fg_status fg_transport_be(fg_mesh *m, const double *rho_cp, const dou
   fg_status st = fg_guard([&]() -> fg_status {
     FG_REQUIRE(m && rho_cp && kappa && vel && T, FG_BAD_ARG, "fg_transport_be: null pointer");
     FG_REQUIRE(nfaces == 0 || (faces && AE && F), FG_BAD_ARG, "fg_transport_be: null face arrays");
-    FG_REQUIRE(m->npe == 10, FG_UNSUPPORTED, "fg_transport_be: P2 tetrahedra only");
+    FG_REQUIRE(!m->edge && (m->npe == 10 || m->npe == 6), FG_UNSUPPORTED,
+               "fg_transport_be: P2 tetrahedra or P2 triangles only");
+    const int fw = m->npe == 10 ? 6 : 3;
     FG_REQUIRE(dt > 0.0 && nsteps >= 0 && nfaces >= 0, FG_BAD_ARG, "fg_transport_be: need dt > 0, nsteps >= 0");
     FG_REQUIRE(!snapshots || every > 0, FG_BAD_ARG, "fg_transport_be: snapshots need every > 0");
     fg_solve_opts opts;
@@ -143,8 +149,8 @@ extern "C" fg_status fg_transport_be(fg_mesh *m, const double *rho_cp, const dou
     FG_CUDA_TRY(cudaEventRecord(e0, m->stream));
     fg_transport_operator(m, tmp[0], tmp[1], tmp[3], tmp[2], full_phi);
     if (nfaces > 0) {
-      const FaceRows fr = face_rows(faces, AE, F, nfaces, nv);
-      fd = face_upload(m, fr, faces, AE, F, nfaces);
+      const FaceRows fr = face_rows(faces, fw, AE, F, nfaces, nv);
+      fd = face_upload(m, fr, faces, fw, AE, F, nfaces);
       fg_face_mass(m, true, fd.rows, fd.nrows, fd.fptr, fd.flist, fd.faces, fd.AE, fd.F, dt);
     }
     fg_check_flags(m, "fg_transport_be");

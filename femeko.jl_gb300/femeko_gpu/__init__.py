@@ -40,7 +40,7 @@ import numpy as np
 import scipy.sparse as sp
 
 from . import _lib as L
-from .mesh import MESH, MU0, box_tet_mesh, box_tri_mesh, surface_faces6  # noqa: F401
+from .mesh import MESH, MU0, box_tet_mesh, box_tri_mesh, surface_faces6, surface_lines3, surface_faces_p2  # noqa: F401
 from .meshio import load_mesh, save_mesh, save2file, load2array  # noqa: F401
 
 __all__ = [
@@ -144,8 +144,10 @@ quadraticMassMatrix2D = massMatrix
 
 def quadraticConvectionMatrix(mesh: MESH, u, F=None, full_phi: bool = False):
     """Global P2 convection matrix of the nodal velocity ``u`` (3 x nv), as
-    src/FEM3D.jl:563-648 builds it (entry (t_i, t_j) sums the local Ck[j, i];
-    ``full_phi=False`` keeps the reference's linear-part-only phi)."""
+    src/FEM3D.jl:563-648 builds it for tetrahedra (entry (t_i, t_j) sums the local
+    Ck[j, i]; ``full_phi=False`` keeps the reference's linear-part-only phi) and
+    src/FEM2D.jl:231-319 for triangles (u interpolated with the P2 basis; F should be
+    None: the 2D reference has no factor)."""
     uv = _c(np.asarray(u, dtype=np.float64).T, np.float64)   # 3 x nv column-major
     fv = None if F is None else _c(F, np.float64)
     return _assemble(mesh, L.lib().fg_convection, L.ptr(uv), L.ptr(fv), int(full_phi))
@@ -284,17 +286,22 @@ def heat_be(mesh: MESH, T0, kappa, rho_c=1.0, dt=1e-3, nsteps=100, every=10, pre
 
 
 def quadraticBoundaryMassMatrix(mesh: MESH, F=None, faces=None):
-    """P2 boundary mass of the surface triangles (src/FEM3D.jl:300-322) with the
-    per-face factor F (ns, default ones); ``faces`` (6 x ns) defaults to
-    ``surface_faces6(mesh)``."""
+    """P2 boundary mass with the per-face factor F (ns, default ones): surface
+    triangles of a tetrahedral mesh (src/FEM3D.jl:300-322, ``faces`` 6 x ns) or
+    boundary lines of a triangle mesh (quadraticMassMatrix1D, src/FEM2D.jl:394-419,
+    ``faces`` 3 x ns); ``faces`` defaults to ``surface_faces_p2(mesh)``."""
     g = gpu_mesh(mesh)
-    f6 = surface_faces6(mesh) if faces is None else np.asarray(faces)
+    f6 = surface_faces_p2(mesh) if faces is None else np.asarray(faces)
     ns = f6.shape[1]
     vals = np.zeros(g.nnz)
     Fv = None if F is None else _c(F, np.float64)
     L.check(L.lib().fg_boundary_mass(g.h, L.ptr(_c(f6.T, np.int32)), L.ptr(_c(mesh.AE[:ns], np.float64)),
                                      L.ptr(Fv), ns, L.ptr(vals)))
     return g.csc(vals)
+
+
+quadraticMassMatrix1D = quadraticBoundaryMassMatrix
+quadraticConvectionMatrix2D = quadraticConvectionMatrix
 
 
 def transport_be(mesh: MESH, T0, rho_cp, kappa, u, dt, nsteps, face_F=None, faces=None, full_phi=True, every=0,
@@ -310,7 +317,7 @@ def transport_be(mesh: MESH, T0, rho_cp, kappa, u, dt, nsteps, face_F=None, face
     if face_F is None:
         f6, AE, Fv, nf = None, None, None, 0
     else:
-        f6 = _c((surface_faces6(mesh) if faces is None else np.asarray(faces)).T, np.int32)
+        f6 = _c((surface_faces_p2(mesh) if faces is None else np.asarray(faces)).T, np.int32)
         nf = f6.shape[0]
         AE, Fv = _c(mesh.AE[:nf], np.float64), _c(face_F, np.float64)
     uv = _c(np.asarray(u, dtype=np.float64).T, np.float64)

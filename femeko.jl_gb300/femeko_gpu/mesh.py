@@ -317,3 +317,32 @@ def surface_faces6(mesh) -> np.ndarray:
             raise ValueError("surface_faces6: a surface edge is not an element edge")
         out[3 + r] = mid[pos]
     return out
+
+
+def surface_lines3(mesh) -> np.ndarray:
+    """3 x ns boundary-edge nodes of a P2 triangle mesh in the order of the reference's
+    P2 ``surfaceT`` rows 1-3 (Gmsh's 3-node line: the two vertices, then the midpoint),
+    which ``src/FEM2D.jl:394-419`` reads.  The midpoints are found among the elements'
+    edge nodes."""
+    if mesh.t.shape[0] != 6:
+        raise ValueError("surface_lines3: P2 triangles only")
+    t = np.asarray(mesh.t, dtype=np.int64)
+    nv = mesh.nv
+    va = np.concatenate([t[a] for a, b in TRI6_EDGES])
+    vb = np.concatenate([t[b] for a, b in TRI6_EDGES])
+    mid = np.concatenate([t[3 + e] for e in range(len(TRI6_EDGES))])
+    key = np.minimum(va, vb) * nv + np.maximum(va, vb)
+    order = np.argsort(key, kind="stable")
+    key, mid = key[order], mid[order]
+    ev = np.asarray(mesh.surfaceT[:2], dtype=np.int64)
+    fk = np.minimum(ev[0], ev[1]) * nv + np.maximum(ev[0], ev[1])
+    pos = np.minimum(np.searchsorted(key, fk), key.size - 1)
+    if np.any(key[pos] != fk):
+        raise ValueError("surface_lines3: a boundary edge is not an element edge")
+    return np.vstack([ev, mid[pos][None, :]]).astype(np.int32)
+
+
+def surface_faces_p2(mesh) -> np.ndarray:
+    """The P2 boundary faces the boundary mass reads: ``surface_faces6`` for
+    tetrahedra, ``surface_lines3`` for triangles."""
+    return surface_faces6(mesh) if mesh.t.shape[0] == 10 else surface_lines3(mesh)

@@ -260,6 +260,25 @@ function quadraticConvectionMatrix(mesh, S, u::Matrix{Float64}, F::Vector{Float6
     return csc(g, v)
 end
 
+"""quadraticConvectionMatrix2D(mesh, u) -- src/FEM2D.jl:231-319 on the GPU (u: 2 x nv)."""
+function quadraticConvectionMatrix2D(mesh, u::Matrix{Float64})
+    g = gpu(mesh); v = zeros(g.nnz)
+    u3 = vcat(u[1:2, :], zeros(1, size(u, 2)))
+    check(ccall((:fg_convection, libpath()), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Int32, Ptr{Float64}),
+                g.h, u3, C_NULL, 0, v))
+    return csc(g, v)
+end
+
+"""quadraticMassMatrix1D(mesh, h) -- src/FEM2D.jl:394-419 on the GPU (surfaceT rows 1-3)."""
+function quadraticMassMatrix1D(mesh, h::Vector{Float64}=ones(mesh.ns))
+    g = gpu(mesh); v = zeros(g.nnz)
+    faces = Int32.(mesh.surfaceT[1:3, :] .- 1)
+    check(ccall((:fg_boundary_mass, libpath()), Cint,
+                (Ptr{Cvoid}, Ptr{Int32}, Ptr{Float64}, Ptr{Float64}, Int64, Ptr{Float64}),
+                g.h, faces, mesh.AE, h, size(faces, 2), v))
+    return csc(g, v)
+end
+
 """quadraticBoundaryMassMatrix(mesh, F) -- src/FEM3D.jl:300-322 on the GPU; reads the
 six node rows of the P2 mesh.surfaceT (1-based) and mesh.AE."""
 function quadraticBoundaryMassMatrix(mesh, F::Vector{Float64}=ones(mesh.ns))
@@ -280,7 +299,7 @@ function transport_be(mesh, T0::Vector{Float64}, rhoCp::Vector{Float64}, conduct
     g = gpu(mesh)
     T = copy(T0)
     snaps = zeros(g.nv, every > 0 ? nsteps ÷ every : 0)
-    faces = Int32.(mesh.surfaceT[1:6, :] .- 1)
+    faces = Int32.(mesh.surfaceT[1:(size(mesh.t, 1) == 10 ? 6 : 3), :] .- 1)
     o = Ref(solve_opts(precision=:fp64, rtol=rtol, maxiter=maxiter))
     s = Ref{SolveStats}()
     st = ccall((:fg_transport_be, libpath()), Cint,

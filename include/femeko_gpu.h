@@ -188,6 +188,10 @@ fg_status fg_mass(fg_mesh *m, const double *f, int32_t full_phi, double *nzval);
  * values are those of the reference's C, whose entry (t_i, t_j) sums the local
  * Ck[j, i] (:640-648), in the order of fg_csc_pattern. */
 fg_status fg_convection(fg_mesh *m, const double *vel, const double *f, int32_t full_phi, double *nzval);
+/* (On a P2 triangle handle fg_convection is src/FEM2D.jl:231-319
+ * quadraticConvectionMatrix2D: vel 3 x nv with z unused, interpolated with the P2
+ * basis at the 4-point rule; its C[t_i, t_j] = sum w (u . grad phi_j) phi_i; f should
+ * be NULL (the 2D reference has no factor); full_phi is ignored.) */
 /* src/FEM3D.jl:79-119 tangentialStiffnessMatrix (P1 tet): H is 3 x nt, dmu nt.
  * Where |H| = 0 the stored term is its limit 0. */
 fg_status fg_tangent(fg_mesh *m, const double *H, const double *dmu, double *nzval);
@@ -268,6 +272,10 @@ fg_status fg_heat_be(fg_mesh *m, const double *kappa, double rho_c, double dt, i
  * the order of fg_csc_pattern (a face pair outside the pattern is FG_BAD_ARG). */
 fg_status fg_boundary_mass(fg_mesh *m, const int32_t *faces, const double *AE, const double *F, int64_t nfaces,
                            double *nzval);
+/* (On a P2 triangle handle: src/FEM2D.jl:394-419 quadraticMassMatrix1D, faces 3 x
+ * nfaces = the reference's surfaceT rows 1-3 (Gmsh line order: vertex, vertex,
+ * midpoint), Mk = (1/30) [4 2 -1; 2 16 2; -1 2 4] by that position, as the
+ * reference applies it.) */
 
 /* ------------------------------------------------------------------ Nedelec */
 /* Edge-element routines on a handle from fg_edge_mesh_create.  curlN_e =
@@ -313,7 +321,9 @@ fg_status fg_nedelec_newton(fg_mesh *m, const double *Bext, const uint8_t *nonli
                             int32_t max_newton, double min_step, double *u, double *Bfield, double *B,
                             double *nu_out, int32_t *newton_iters, const fg_solve_opts *o, fg_solve_stats *s);
 
-/* Heat transport with convection on P2 tetrahedra (Transport/main3D.jl:143-213):
+/* Heat transport with convection on P2 tetrahedra (Transport/main3D.jl:143-213;
+ * on P2 triangles the same loop of Transport/main2D.jl:150-190 with the 2D matrices
+ * and 3-node boundary lines, rho_cp = ones for the reference's unweighted 2D M):
  * LM = M(rho_cp) + dt (A(kappa) + R + C(vel, rho_cp)), then nsteps steps of
  * T <- LM \ (M T) (main3D.jl:199-204), each solved by Jacobi-preconditioned BiCGStab
  * (FP64, started from the previous T) to ||M T_n - LM T|| <= o->rtol ||M T_n||

@@ -623,6 +623,53 @@ static const double GQ2_PTS[6][2] = {{0.445948490915965, 0.445948490915965}, {0.
                                      {0.108103018168070, 0.445948490915965}, {0.091576213509771, 0.091576213509771},
                                      {0.091576213509771, 0.816847572980459}, {0.816847572980459, 0.091576213509771}};
 
+/* src/FEM2D.jl:453-506 GaussQuadrature2D(3): 4 points, weights summing to 1.       */
+static const double GQ2C_W[4] = {-27.0 / 48.0, 25.0 / 48.0, 25.0 / 48.0, 25.0 / 48.0};
+static const double GQ2C_PTS[4][2] = {{1.0 / 3.0, 1.0 / 3.0}, {0.2, 0.2}, {0.6, 0.2}, {0.2, 0.6}};
+
+/* src/FEM2D.jl:231-319 quadraticConvectionMatrix2D: u (3 x nv, z unused)           */
+/* interpolated with the P2 basis at each point, Ck[i][j] += w (gradPhi_i . u)       */
+/* phi_j with w = weight * VE; Clocal = vec(Ck) scattered with n = 6(i-1)+j to       */
+/* (t_i, t_j), so C[t_i, t_j] sums Ck[j][i].                                       */
+long or_p2_convection2d(const double *p, const int *t, int nv, long nt, const double *VE, const double *u,
+                        long *colptr, int *rowval, double *nzval) {
+  double *Cv = (double *)malloc(sizeof(double) * 36 * (size_t)nt);
+#pragma omp parallel for schedule(static)
+  for (long k = 0; k < nt; ++k) {
+    const int *nds = t + 6 * k;
+    double zero[3] = {0, 0, 0};
+    double S[6][6];
+    for (int a = 0; a < 6; ++a) p2_basis2d(p, nds, a, zero, S[a]);
+    const double *v1 = p + 3 * nds[0], *v2 = p + 3 * nds[1], *v3 = p + 3 * nds[2];
+    double J11 = v2[0] - v1[0], J12 = v3[0] - v1[0], J21 = v2[1] - v1[1], J22 = v3[1] - v1[1];
+    double Ck[6][6];
+    memset(Ck, 0, sizeof(Ck));
+    for (int q = 0; q < 4; ++q) {
+      double xi = GQ2C_PTS[q][0], eta = GQ2C_PTS[q][1];
+      double x = v1[0] + J11 * xi + J12 * eta, y = v1[1] + J21 * xi + J22 * eta;
+      double phi[6], gx[6], gy[6], ux = 0.0, uy = 0.0;
+      for (int i = 0; i < 6; ++i) {
+        const double *s = S[i];
+        phi[i] = s[0] + s[1] * x + s[2] * y + s[3] * x * x + s[4] * x * y + s[5] * y * y;
+        ux += u[3 * nds[i]] * phi[i];
+        uy += u[3 * nds[i] + 1] * phi[i];
+        gx[i] = s[1] + 2 * s[3] * x + s[4] * y;
+        gy[i] = s[2] + 2 * s[5] * y + s[4] * x;
+      }
+      double w = GQ2C_W[q] * VE[k];
+      for (int i = 0; i < 6; ++i) {
+        double gi = gx[i] * ux + gy[i] * uy;
+        for (int j = 0; j < 6; ++j) Ck[i][j] += w * gi * phi[j];
+      }
+    }
+    for (int i = 0; i < 6; ++i)
+      for (int j = 0; j < 6; ++j) Cv[36 * k + 6 * i + j] = Ck[j][i];
+  }
+  long nnz = or_assemble_csc(nv, nt, 6, t, Cv, 0, colptr, rowval, nzval);
+  free(Cv);
+  return nnz;
+}
+
 /* src/FEM2D.jl:163-229 quadraticMassMatrix2D (full quadratic phi, w = weight*VE). */
 long or_p2_mass2d(const double *p, const int *t, int nv, long nt, const double *VE, long *colptr, int *rowval,
                   double *nzval) {

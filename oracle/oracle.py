@@ -71,6 +71,8 @@ def lib():
         L.or_p2_mass.argtypes = [_dp, _ip, C.c_int, C.c_long, _dp, _vp, C.c_int] + csc_out
         L.or_p2_convection.restype = C.c_long
         L.or_p2_convection.argtypes = [_dp, _ip, C.c_int, C.c_long, _dp, _dp, _vp, C.c_int] + csc_out
+        L.or_p2_convection2d.restype = C.c_long
+        L.or_p2_convection2d.argtypes = [_dp, _ip, C.c_int, C.c_long, _dp, _dp] + csc_out
         L.or_nedelec_local.argtypes = [_dp, _ip, C.c_int, C.c_long, _dp, _vp, C.c_int, _vp, _vp, _vp, _dp]
         L.or_nedelec_load.argtypes = [_dp, _ip, C.c_int, C.c_long, _dp, _ip, _dp, _dp]
         L.or_nedelec_bfield.argtypes = [_dp, _ip, C.c_int, C.c_long, _ip, _dp, _dp, _dp]
@@ -241,6 +243,31 @@ _FACE_MK = np.array([[6, -1, -1, 0, -4, 0],
                      [0, -4, 0, 16, 16, 32]], dtype=np.float64)
 
 
+def quadraticConvectionMatrix2D(mesh, u):
+    """``src/FEM2D.jl:231-319``; u is the nodal velocity (2 or 3 x nv)."""
+    p, t = _pt(mesh)
+    u = np.asarray(u, dtype=np.float64)
+    u3 = np.vstack([u[:2], np.zeros((1, u.shape[1]))])
+    return _assemble(lib().or_p2_convection2d, mesh, 6, p, t, mesh.nv, mesh.nt, _c(mesh.VE, np.float64),
+                     _c(u3.T, np.float64))
+
+
+# src/FEM2D.jl:397-399: the 3-node line mass, by position in surfaceT rows 1-3, times 30.
+_LINE_MK = np.array([[4, 2, -1], [2, 16, 2], [-1, 2, 4]], dtype=np.float64)
+
+
+def quadraticMassMatrix1D(mesh, faces3, h=None):
+    """``src/FEM2D.jl:394-419``: M[nds[i], nds[j]] += AE[s] Mk[i,j] h[s] over the
+    boundary lines (faces3: 3 x ns, 0-based), Mk = (1/30) c."""
+    ns = faces3.shape[1]
+    h = np.ones(ns) if h is None else np.asarray(h, dtype=np.float64)
+    Mk = (1.0 / 30.0) * _LINE_MK
+    rows = np.repeat(faces3, 3, axis=0)
+    cols = np.tile(faces3, (3, 1))
+    vals = (np.asarray(mesh.AE[:ns])[None, :] * Mk.reshape(9, 1)) * h[None, :]
+    return sp.csc_matrix((vals.ravel(), (rows.ravel(), cols.ravel())), shape=(mesh.nv, mesh.nv))
+
+
 def quadraticBoundaryMassMatrix(mesh, faces6, F=None):
     """``src/FEM3D.jl:300-322``: M[nds[i], nds[j]] += AE[s] Mk[i,j] F[s] over the
     surface faces (faces6: 6 x ns, 0-based), Mk = (1/180) c."""
@@ -258,10 +285,18 @@ def transport_be(mesh, T0, rhoCp, kappa, u, dt, nsteps, faces6=None, face_F=None
     solves T = LM \\ (M T) (scipy's sparse LU standing in for Julia's ``\\``).
     Returns the list of fields after each step."""
     import scipy.sparse.linalg as spla
-    M = quadraticMassMatrix(mesh, rhoCp, full_phi=full_phi)
-    A = quadraticStiffnessMatrix(mesh, kappa)
-    Cm = quadraticConvectionMatrix(mesh, u, rhoCp, full_phi=full_phi)
-    R = sp.csc_matrix((mesh.nv, mesh.nv)) if face_F is None else quadraticBoundaryMassMatrix(mesh, faces6, face_F)
+    if mesh.t.shape[0] == 6:
+        # Transport/main2D.jl:162-190: M, A(epsi), C(u), R = quadraticMassMatrix1D(intakeBC)
+        M = quadraticMassMatrix2D(mesh)
+        A = quadraticStiffnessMatrix2D(mesh, kappa)
+        Cm = quadraticConvectionMatrix2D(mesh, u)
+        R = (sp.csc_matrix((mesh.nv, mesh.nv)) if face_F is None
+             else quadraticMassMatrix1D(mesh, faces6, face_F))
+    else:
+        M = quadraticMassMatrix(mesh, rhoCp, full_phi=full_phi)
+        A = quadraticStiffnessMatrix(mesh, kappa)
+        Cm = quadraticConvectionMatrix(mesh, u, rhoCp, full_phi=full_phi)
+        R = sp.csc_matrix((mesh.nv, mesh.nv)) if face_F is None else quadraticBoundaryMassMatrix(mesh, faces6, face_F)
     LM = (M + dt * (A + R + Cm)).tocsc()
     lu = spla.splu(LM)
     T = np.asarray(T0, dtype=np.float64).copy()

@@ -97,3 +97,53 @@ def test_transport_repeatable_and_limits():
     with pytest.raises(RuntimeError):     # P1 mesh
         pm = fg.box_tet_mesh(2, seed=1)
         fg.transport_be(pm, np.zeros(pm.nv), np.ones(pm.nt), np.ones(pm.nt), np.zeros((3, pm.nv)), 0.1, 1)
+
+
+# ---------------------------------------------------------------- 2D (Transport/main2D.jl)
+def problem2d(n=4, seed=3):
+    m = fg.box_tri_mesh(n, seed=seed, order=2)
+    rng = np.random.default_rng(seed)
+    u = np.vstack([np.full(m.nv, 1.0), 0.3 * np.sin(m.p[0]), np.zeros(m.nv)])
+    kap = rng.uniform(0.02, 0.08, m.nt)
+    T0 = np.exp(-(m.p[0] ** 2 + m.p[1] ** 2) / 4)
+    return m, u, kap, T0
+
+
+def intake2d(m):
+    from femeko_gpu.mesh import surface_lines3
+    f3 = surface_lines3(m)
+    xmin = m.p[0].min()
+    on = np.all(np.isclose(m.p[0][f3[:2]], xmin), axis=0)
+    return f3, np.where(on, 1e6, 0.0)
+
+
+def test_convection2d_known_answers():
+    """2D C[r, c] = int phi_r (u . grad phi_c) (src/FEM2D.jl:231-319 after its scatter):
+    rows sum to 0 and, for constant u and linear T = a . x, C T = (u . a) M 1."""
+    m, _, _, _ = problem2d()
+    uc = np.vstack([np.full(m.nv, 0.7), np.full(m.nv, -0.4), np.zeros(m.nv)])
+    C = O.quadraticConvectionMatrix2D(m, uc)
+    a = np.array([1.5, -2.0])
+    T = a @ m.p[:2]
+    rhs = (np.array([0.7, -0.4]) @ a) * (O.quadraticMassMatrix2D(m) @ np.ones(m.nv))
+    assert np.abs(C @ T - rhs).max() <= 1e-12 * np.abs(rhs).max()
+    assert np.abs(np.asarray(C.sum(axis=1))).max() <= 1e-12 * np.abs(C.data).max()
+    f3, F = intake2d(m)
+    R = O.quadraticMassMatrix1D(m, f3, F)
+    assert abs(R.sum() - (m.AE * F).sum()) <= 1e-12 * (m.AE * F).sum()
+
+
+@pytest.mark.gpu
+def test_transport2d_parity():
+    m, u, kap, T0 = problem2d()
+    Cg, Co = fg.quadraticConvectionMatrix(m, u), O.quadraticConvectionMatrix2D(m, u)
+    assert np.array_equal(Cg.indptr, Co.indptr) and np.array_equal(Cg.indices, Co.indices)
+    assert np.abs(Cg.data - Co.data).max() <= 1e-11 * np.abs(Co.data).max()
+    f3, F = intake2d(m)
+    Rg, Ro = fg.quadraticBoundaryMassMatrix(m, F, faces=f3), O.quadraticMassMatrix1D(m, f3, F)
+    assert abs(Rg - Ro).max() <= 1e-13 * abs(Ro).max()
+    ones = np.ones(m.nt)
+    T, _, st = fg.transport_be(m, T0, ones, kap, u, 0.05, 4, face_F=F, faces=f3, rtol=1e-13)
+    ref = O.transport_be(m, T0, ones, kap, u, 0.05, 4, f3, F)
+    assert st["converged"]
+    assert np.abs(T - ref[-1]).max() <= 1e-9 * np.abs(ref[-1]).max()
