@@ -22,6 +22,7 @@ import argparse
 import ctypes as C
 import json
 import os
+import tempfile
 import statistics
 import subprocess
 import sys
@@ -70,7 +71,10 @@ class Clocks:
     def __init__(self, dev: int = 0):
         self.dev = dev
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        # raw samples go to FG_CLOCKS_DIR (default: the system temporary folder); the
+        # JSON line carries their summary
+        self.path = os.path.join(os.environ.get("FG_CLOCKS_DIR", tempfile.gettempdir()),
+                                 f"fg_clocks_{os.getpid()}.csv")
 
     def __enter__(self):
         os.makedirs(os.path.dirname(self.path), exist_ok=True)
