@@ -640,17 +640,25 @@ def case_nedelec(args):
     nu_tab = 0.002 + 0.998 * q / (1.0 + q)
     nl = (mesh.elementID == 2).astype(np.uint8)
     Bext = np.array([0.8, 0.0, 0.0])
-    fg.nedelec_newton(mesh, Bext, b, nu_tab, nonlinear=nl, max_newton=2)                     # warm-up
-    u, Bf, B, nu, steps, st = fg.nedelec_newton(mesh, Bext, b, nu_tab, nonlinear=nl, tol=1e-4,
-                                                rtol=float(np.sqrt(np.finfo(np.float64).eps)))
+    rtol = float(np.sqrt(np.finfo(np.float64).eps))
+    res = {}
+    for prec in ("fp64", "mixed"):
+        fg.nedelec_newton(mesh, Bext, b, nu_tab, nonlinear=nl, max_newton=2, precision=prec)      # warm-up
+        res[prec] = fg.nedelec_newton(mesh, Bext, b, nu_tab, nonlinear=nl, tol=1e-4, rtol=rtol, precision=prec)
+    u, Bf, B, nu, steps, st = res["mixed"]
+    _, Bf64, _, _, steps64, st64 = res["fp64"]
     g = fg.edge_mesh(mesh)
-    _line("Nedelec Newton solves/s (edge elements, FP64)", 1e3 / st["ms"], "solves/s", True,
+    _line("Nedelec Newton solves/s (edge elements, mixed FP32 CG + FP64 refinement)", 1e3 / st["ms"], "solves/s", True,
           {"workload": f"Nedelec vector-potential Newton, Kuhn tets {cells}^3 cells, iron cube", "tets": int(mesh.nt),
            "edges": int(g.ne), "nnz": int(g.nnz)},
           {"ms": st["ms"], "newton_steps": steps, "cg_iterations": st["iterations"],
            "short_inner_solves": st["short_inner_solves"],
            "us_per_cg_iteration": st["ms"] * 1e3 / max(st["iterations"], 1), "converged": bool(st["converged"]),
-           "B_iron_max_T": float(B[nl == 1].max())})
+           "B_iron_max_T": float(B[nl == 1].max()),
+           "fp64": {"solves_per_s": 1e3 / st64["ms"], "ms": st64["ms"], "newton_steps": steps64,
+                    "cg_iterations": st64["iterations"]},
+           "mixed_over_fp64": st64["ms"] / st["ms"],
+           "B_rel_diff_mixed_vs_fp64": float(np.abs(Bf - Bf64).max() / np.abs(Bf64).max())})
 
 
 CASES = {"cg-kernel": case_cg_kernel, "cg-loop": case_cg_loop, "newton-kernels": case_newton_kernels, "heat": case_heat,

@@ -157,6 +157,24 @@ void need_edge(fg_mesh *m, const char *w) {
   FG_REQUIRE(m->edge, FG_UNSUPPORTED, std::string(w) + ": needs a handle from fg_edge_mesh_create");
 }
 
+// The mixed path (FP32 CG inside FP64 refinement) first; on this singular
+// (gradient null space) system its FP32 inner iterations can stall short of a tight
+// rtol at high permeability contrast, and then FP64 PCG continues from where it
+// stopped (the operator holds both precisions).  Iterations of both are counted.
+int solve_with_fallback(fg_mesh *m, const double *d_b, double *d_x, const fg_solve_opts &o, fg_solve_stats *st) {
+  int rc = fg_pcg_solve(m, d_b, d_x, o, st, false);
+  if (rc == 0 || o.precision != FG_MIXED) return rc;
+  fg_solve_opts o64 = o;
+  o64.precision = FG_FP64;
+  fg_solve_stats s2{};
+  rc = fg_pcg_solve(m, d_b, d_x, o64, &s2, false);
+  st->iterations += s2.iterations;
+  st->refinements += 1;
+  st->converged = s2.converged;
+  st->relres = s2.relres;
+  return rc;
+}
+
 fg_status export_nz(fg_mesh *m, double *nzval, const char *w) {
   FG_CUDA_TRY(cudaMemcpyAsync(nzval, m->csrval, sizeof(double) * (size_t)m->nnz, cudaMemcpyDeviceToHost, m->stream));
   fg_sync(m);
@@ -253,10 +271,7 @@ extern "C" fg_status fg_nedelec_linear(fg_mesh *m, const double *nu, const doubl
     fg_solve_opts opts;
     fg_solve_opts_default(&opts);
     if (o) opts = *o;
-    // FP64 only: on the singular curl-curl system with a permeability contrast of 500
-    // the FP32 inner iterations of the mixed path stall short of 1e-12 (measured)
-    opts.precision = FG_FP64;
-    const bool mixed = false;
+    const bool mixed = opts.precision == FG_MIXED;
     dn = upload_d(m, nu, (size_t)m->nt);
     FG_CUDA_TRY(cudaMallocAsync(&drhs, sizeof(double) * (size_t)m->nvp, m->stream));
     FG_CUDA_TRY(cudaMallocAsync(&du, sizeof(double) * (size_t)m->nvp, m->stream));
@@ -269,7 +284,7 @@ extern "C" fg_status fg_nedelec_linear(fg_mesh *m, const double *nu, const doubl
     fg_nedelec_operator(m, dn, true, nullptr, nullptr, nullptr, OUT_SELL, mixed);
     fg_nedelec_load_dev(m, Bext, drhs);
     fg_solve_stats st0{};
-    rc = fg_pcg_solve(m, drhs, du, opts, &st0, false);
+    rc = solve_with_fallback(m, drhs, du, opts, &st0);
     if (Bfield) {
       FG_CUDA_TRY(cudaMallocAsync(&dB, sizeof(double) * 3 * (size_t)m->nt, m->stream));
       FG_CUDA_TRY(cudaMallocAsync(&dBn, sizeof(double) * (size_t)m->nt, m->stream));
@@ -321,8 +336,7 @@ extern "C" fg_status fg_nedelec_newton(fg_mesh *m, const double *Bext, const uin
     fg_solve_opts opts;
     fg_solve_opts_default(&opts);
     if (o) opts = *o;
-    opts.precision = FG_FP64;  // as fg_nedelec_linear
-    const bool mixed = false;
+    const bool mixed = opts.precision == FG_MIXED;
     const int64_t ne = m->nv, nt = m->nt;
     tab = upload_d(m, htab.data(), htab.size());
     dnl = upload_d(m, nu_lin, (size_t)nt);
@@ -368,7 +382,7 @@ extern "C" fg_status fg_nedelec_newton(fg_mesh *m, const double *Bext, const uin
       fg_solve_stats cs{};
       // an inner solve that stops short of rtol still gives a correction (the
       // reference's cg returns what it has as well); it is counted, not fatal
-      if (fg_pcg_solve(m, r, du_, opts, &cs, false) != 0) ++status;
+      if (solve_with_fallback(m, r, du_, opts, &cs) != 0) ++status;
       cg_iters += cs.iterations;
       // line search of src/FEM3D.jl:122-151 on ||RHS - A u||
       double alf = 1.0;

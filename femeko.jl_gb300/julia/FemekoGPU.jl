@@ -235,11 +235,12 @@ end
 Magnetostatics/nedelec3D.jl:149-231 on the GPU, nu(B) the not-a-knot cubic through the
 table (Spline1D(B, nu)); returns (u, Bfield, B, nu, steps, stats)."""
 function nedelec_newton(mesh, Bext::Vector{Float64}, curve_B::Vector{Float64}, curve_nu::Vector{Float64};
-                        tol=1e-4, maxAtt::Integer=100, minStep=1e-4, rtol=1e-10)
+                        tol=1e-4, maxAtt::Integer=100, minStep=1e-4, rtol=sqrt(eps(Float64)),
+                        precision::Symbol=:mixed)
     g = edgegpu(mesh)
     nl = zeros(UInt8, g.nt); nl[mesh.InsideElements] .= 1
     u = zeros(g.nv); Bf = zeros(3, g.nt); B = zeros(g.nt); nu = zeros(g.nt); it = Ref{Int32}(0)
-    o = Ref(solve_opts(precision=:fp64, rtol=rtol))
+    o = Ref(solve_opts(precision=precision, rtol=rtol))
     s = Ref{SolveStats}()
     st = ccall((:fg_nedelec_newton, libpath()), Cint,
                (Ptr{Cvoid}, Ptr{Float64}, Ptr{UInt8}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int32, Float64, Int32,

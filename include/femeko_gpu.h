@@ -296,8 +296,9 @@ fg_status fg_nedelec_bfield(fg_mesh *m, const double *u, double *Bfield, double 
 /* The first Newton step of nedelec3D.jl (u = 0, At = 0): A(nu) u = RHS(Bext) by the
  * Jacobi-PCG of fg_pcg (the curl-curl matrix is singular with a consistent right-hand
  * side: u is one solution, B = curl u is unique); Bfield/B (may be NULL) as in
- * fg_nedelec_bfield.  Runs in FP64 whatever o->precision says: the mixed path's FP32
- * inner iterations stall on this singular system at high permeability contrast. */
+ * fg_nedelec_bfield.  With o->precision = FG_MIXED a solve whose FP32 inner
+ * iterations stall on this singular system (high permeability contrast, tight rtol)
+ * is finished by FP64 PCG from where it stopped (refinements + 1). */
 fg_status fg_nedelec_linear(fg_mesh *m, const double *nu, const double *Bext, double *u, double *Bfield, double *B,
                             const fg_solve_opts *o, fg_solve_stats *s);
 

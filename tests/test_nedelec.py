@@ -63,11 +63,11 @@ def test_nedelec_linear_solve(precision):
     A, rhs = O.nedelecStiffness(m, nu), O.nedelec_load(m, Bext)
     assert np.linalg.norm(A @ u - rhs) <= 1e-10 * np.linalg.norm(rhs)
     uo, info = spla.cg(A, rhs, rtol=1e-13, maxiter=20000)
-    # a mixed-precision request runs in FP64 (the FP32 inner solves stall on this
-    # singular system), so it gives the same iterates
-    u2, Bf2, _, st2 = fg.nedelec_linear(m, Bext, nu, precision="mixed" if precision == "fp64" else "fp64",
-                                        rtol=1e-12)
-    assert np.array_equal(u2, u) and st2["iterations"] == st["iterations"]
+    # mixed precision: FP32 inner CG in FP64 refinement, finished in FP64 where the
+    # FP32 iterations stall on this singular system; the same B
+    u2, Bf2, _, st2 = fg.nedelec_linear(m, Bext, nu, precision="mixed", rtol=1e-12)
+    assert st2["converged"] and np.linalg.norm(A @ u2 - rhs) <= 1e-10 * np.linalg.norm(rhs)
+    assert rel(Bf2, Bf) < 1e-8
     Bo, _ = O.nedelec_bfield(m, uo)
     assert rel(Bf, Bo) < 1e-7
     assert np.allclose(B, np.linalg.norm(Bf, axis=0), rtol=1e-14, atol=0)
@@ -102,7 +102,7 @@ def test_nedelec_spline_matches_scipy_not_a_knot():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision", ["fp64"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_nedelec_newton_parity(precision):
     m, _, _ = mesh_and_fields(n=4)
     b, nu_tab = iron_curve()
