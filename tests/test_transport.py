@@ -147,3 +147,22 @@ def test_transport2d_parity():
     ref = O.transport_be(m, T0, ones, kap, u, 0.05, 4, f3, F)
     assert st["converged"]
     assert np.abs(T - ref[-1]).max() <= 1e-9 * np.abs(ref[-1]).max()
+
+
+@pytest.mark.gpu
+def test_transport_edge_cases():
+    """Zero steps return T unchanged; faces whose factor is 0 change nothing (bit for
+    bit); a face list given with no nonzero factor equals no faces at all."""
+    m, u, rho, kap, T0 = problem(n=2)
+    T, snaps, st = fg.transport_be(m, T0, rho, kap, u, 0.05, 0)
+    assert np.array_equal(T, T0) and st["iterations"] == 0 and snaps.shape[0] == 0
+    f6, F = intake(m)
+    a = fg.transport_be(m, T0, rho, kap, u, 0.05, 2, rtol=1e-12)[0]
+    b = fg.transport_be(m, T0, rho, kap, u, 0.05, 2, face_F=np.zeros_like(F), faces=f6, rtol=1e-12)[0]
+    assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+    c = fg.transport_be(m, T0, rho, kap, u, 0.05, 2, face_F=F, faces=f6, rtol=1e-12)[0]
+    assert np.abs(c - a).max() > 0.0          # the intake penalty acts
+    bad = f6.copy()
+    bad[0, 0] = bad[1, 0]                     # a face repeating a node
+    with pytest.raises(RuntimeError):
+        fg.transport_be(m, T0, rho, kap, u, 0.05, 1, face_F=np.ones_like(F), faces=bad)
