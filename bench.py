@@ -643,8 +643,10 @@ def case_nedelec(args):
     rtol = float(np.sqrt(np.finfo(np.float64).eps))
     res = {}
     for prec in ("fp64", "mixed"):
-        fg.nedelec_newton(mesh, Bext, b, nu_tab, nonlinear=nl, max_newton=2, precision=prec)      # warm-up
-        res[prec] = fg.nedelec_newton(mesh, Bext, b, nu_tab, nonlinear=nl, tol=1e-4, rtol=rtol, precision=prec)
+        fg.nedelec_newton(mesh, Bext, b, nu_tab, nonlinear=nl, max_newton=2, precision=prec,
+                          use_graph=args.graph_mode)                                              # warm-up
+        res[prec] = fg.nedelec_newton(mesh, Bext, b, nu_tab, nonlinear=nl, tol=1e-4, rtol=rtol, precision=prec,
+                                      use_graph=args.graph_mode)
     u, Bf, B, nu, steps, st = res["mixed"]
     _, Bf64, _, _, steps64, st64 = res["fp64"]
     g = fg.edge_mesh(mesh)

@@ -139,7 +139,7 @@ def nedelec_linear(mesh: MESH, Bext, nu=None, precision="fp64", rtol=1e-10, maxi
 
 
 def nedelec_newton(mesh: MESH, Bext, curve_B, curve_nu, nonlinear=None, nu_lin=None, tol=1e-4, max_newton=100,
-                   min_step=1e-4, precision="fp64", rtol=1e-10, maxiter=1_000_000):
+                   min_step=1e-4, precision="fp64", rtol=1e-10, maxiter=1_000_000, use_graph=1):
     """The Newton loop of Magnetostatics/nedelec3D.jl:149-231 on the GPU with the
     material curve nu(B) given as a table (not-a-knot cubic interpolant, as Dierckx's
     Spline1D(B, nu)).  nonlinear: element mask (default: ``mesh.InsideElements``).
@@ -152,7 +152,7 @@ def nedelec_newton(mesh: MESH, Bext, curve_B, curve_nu, nonlinear=None, nu_lin=N
     u = np.zeros(g.ne)
     Bf, B, nu = np.zeros(3 * mesh.nt), np.zeros(mesh.nt), np.zeros(mesh.nt)
     it = C.c_int32()
-    o = solve_opts(precision=precision, rtol=rtol, maxiter=maxiter)
+    o = solve_opts(precision=precision, rtol=rtol, maxiter=maxiter, use_graph=use_graph)
     s = L.SolveStats()
     nl_ = None if nu_lin is None else _c(nu_lin, np.float64)
     cb, cn = _c(curve_B, np.float64), _c(curve_nu, np.float64)
