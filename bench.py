@@ -13,8 +13,11 @@ timed with CUDA events on the library's stream, inputs resident in HBM.
 fp64: the same solve with an FP64 inner CG (the plain FP64 GPU path).
 e2e: the one-shot C-ABI call fg_scalar_potential_newton from pinned host buffers
 (mesh upload, pattern build, solve, download of u/H/mu inside the timed region).
---impl reference: the CPU restatement of the reference algorithm (oracle port, all
-host threads) on a bounded sample, extrapolated to solves/s.
+cpu_baseline / accuracy_vs_oracle: one full Newton solve of the CPU restatement of
+the reference algorithm (oracle port, FP64, all host threads, the same Newton
+settings), timed, and its u, H and magnetic energy as the FP64 reference for both
+GPU solves.
+--impl reference: the same full oracle solve(s), timed, as the reference arm.
 """
 from __future__ import annotations
 
@@ -130,15 +133,49 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def cpu_sample(mesh, nl, mu_lin, u0, counts, threads, cg_iters=100):
-    """Bounded CPU sample of the oracle port, extrapolated to one full solve."""
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the platform string)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu model")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+# The Newton settings both the GPU path and the oracle run: Eisenstat-Walker inner
+# tolerances (choice 2, gamma 0.9) in [1e-6, 0.1], two Picard (secant) steps, alpha =
+# 0.9^k backtracking on the true nonlinear residual, stop at |alpha du| <= 1e-8 |u|.
+NEWTON_SETTINGS = dict(tol_update=1e-8, line_search="residual", forcing="ew", eta_min=1e-6, eta_max=0.1,
+                       picard_steps=2)
+
+
+def cpu_full_solve(mesh, nl, mu_lin, u0, threads):
+    """One full FP64 Newton solve of the oracle port (the reference algorithm of
+    Magnetostatics/NewtonRaphson.jl:109-214 with its per-iteration sparse assembly),
+    wall-clock timed on `threads` OpenMP threads.  Returns (u, H, mu, stats, seconds)."""
     import oracle as O
     O.set_threads(threads)
-    s = O.newton_sample(mesh, u0, nl, mu_lin, MS, HK, cg_iters)
-    per_cg = s["cg_s"] / max(s["cg_iters"], 1)
-    n_it, trials, cg_total = counts
-    est = (1 + trials) * s["state_s"] + n_it * s["tangent_s"] + cg_total * per_cg
-    return 1.0 / est, s, est
+    t0 = time.perf_counter()
+    u, H, mu, st = O.newton(mesh, u0, nl, mu_lin, MS, HK, **NEWTON_SETTINGS)
+    sec = time.perf_counter() - t0
+    if not st["converged"]:
+        raise RuntimeError(f"oracle Newton did not converge: {st}")
+    return u, H, mu, st, sec
+
+
+def oracle_energy(mesh, H, nl, mu_lin):
+    import oracle as O
+    return O.energy(mesh, H, nl, mu_lin, MS, HK)
 
 
 def run_reference(args):
@@ -147,24 +184,30 @@ def run_reference(args):
         return
     threads = os.cpu_count() or 1
     mesh, nl, mu_lin, u0 = workload(args.cells)
-    # iteration counts of the same algorithm (FP64 Newton, inner rtol 1e-4, residual
-    # backtracking) measured on this workload by the GPU FP64 path; stored so that the
-    # reference arm needs no GPU.
-    counts = tuple(args.ref_counts)
-    vals = []
-    for step in range(args.warmup + args.steps):
-        v, s, est = cpu_sample(mesh, nl, mu_lin, u0, counts, threads, cg_iters=args.cpu_cg_iters)
-        if step >= args.warmup:
-            vals.append(v)
-    value = statistics.median(vals)
-    sample = (f"per step: one Newton state evaluation, one tangent assembly and {args.cpu_cg_iters} PCG iterations "
-              f"of the oracle port on the 96^3 workload, extrapolated with the solve's counts "
-              f"(newton, line-search trials, CG) = {counts}")
+    # warm-up: the same solve on the 24^3-cell plate (loads the library, starts the
+    # OpenMP threads, faults in the allocator); a CPU solve keeps no other state
+    wmesh, wnl, wmu, wu0 = workload(24)
+    cpu_full_solve(wmesh, wnl, wmu, wu0, threads)
+    # timed: full solves of the 96^3 workload; each takes about a minute on 16 cores,
+    # so at most --ref-steps of the requested --steps are run (stated on the line)
+    nsteps = max(1, min(args.steps, args.ref_steps))
+    secs, st = [], None
+    for _ in range(nsteps):
+        _, _, _, st, sec = cpu_full_solve(mesh, nl, mu_lin, u0, threads)
+        secs.append(sec)
+    total = sum(secs)
+    value = nsteps / total
+    sample = (f"{nsteps} full FP64 Newton solve(s) of the oracle port (the reference algorithm, sparse assembly per "
+              f"iteration) on the whole {args.cells}^3 workload, measured, not extrapolated: "
+              f"{st['newton_iters']} Newton iterations, {st['cg_iters']} PCG iterations per solve")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
+            "steps": nsteps, "steps_requested": args.steps, "warmup": 1,
+            "warmup_what": "one full solve of the 24^3-cell plate (same settings)",
+            "ms_per_step": 1000.0 * total / nsteps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": config(args.cells, mesh),
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                             "cpu_model": cpu_model(), "measured": True},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -379,17 +422,27 @@ def run_ours(args):
                "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
                "what": "fg_scalar_potential_newton: upload + pattern build + solve + download per step"}
 
-    cpu = None
+    cpu, acc_oracle = None, None
     if rank == 0 and not args.no_cpu_baseline:
-        st = res["fp64"]["stats"]
-        counts = (st["newton_iters"], st["trials"], st["cg_iters"])
         threads = os.cpu_count() or 1
-        v, s, est = cpu_sample(mesh, nl, mu_lin, u0, counts, threads, cg_iters=args.cpu_cg_iters)
-        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": (f"one Newton state evaluation ({s['state_s']:.2f} s), one tangent assembly "
-                          f"({s['tangent_s']:.2f} s) and {s['cg_iters']} PCG iterations ({s['cg_s']:.2f} s) of the "
-                          f"oracle port on this workload, extrapolated with the FP64 solve's counts "
-                          f"(newton, trials, cg) = {counts} to {est:.1f} s per solve")}
+        uo, Ho, muo, so, sec = cpu_full_solve(mesh, nl, mu_lin, u0, threads)
+        Wo = oracle_energy(mesh, Ho, nl, mu_lin)
+        acc_oracle = {}
+        for prec in ("mixed", "fp64"):
+            r = res[prec]
+            acc_oracle[prec] = {
+                "H_rel": float(np.linalg.norm(r["H"] - Ho) / np.linalg.norm(Ho)),
+                "u_rel": float(np.linalg.norm(r["u"] - uo) / np.linalg.norm(uo)),
+                "mu_rel_max": float(np.abs(r["mu"] - muo).max() / np.abs(muo).max()),
+                "energy_rel": float(abs(r["stats"]["energy"] - Wo) / abs(Wo))}
+        acc_oracle["oracle"] = {"newton_iters": so["newton_iters"], "cg_iters": so["cg_iters"], "energy_J": Wo,
+                                "settings": "FP64, the same Newton settings as the GPU solves"}
+        acc_oracle["H_err_le_1e-8"] = all(acc_oracle[p]["H_rel"] <= 1e-8 for p in ("mixed", "fp64"))
+        cpu = {"value": 1.0 / sec, "unit": UNIT, "cores": threads, "kind": "port", "measured": True,
+               "cpu_model": cpu_model(),
+               "sample": (f"one full FP64 Newton solve of the oracle port on the whole {args.cells}^3 workload "
+                          f"({sec:.1f} s wall, {so['newton_iters']} Newton / {so['cg_iters']} PCG iterations, "
+                          f"{threads} OpenMP threads), measured, not extrapolated")}
 
     sm = res["mixed"]["stats"]
 
@@ -408,6 +461,7 @@ def run_ours(args):
                      "phases_ms": phases(res["fp64"]["stats"])},
             "phases_ms": phases(sm),
             "mixed_over_fp64": value / fp64_value,
+            "accuracy_vs_oracle": acc_oracle,
             "accuracy_vs_fp64_gpu": {"H_rel": herr, "u_rel": uerr, "energy_rel": werr},
             "newton_iters": sm["newton_iters"], "cg_iters": sm["cg_iters"], "trials": sm["trials"],
             "roofline": roofline, "kernels_us": kernels_us, "autotune": autotune, "cpu_baseline": cpu, "e2e": e2e,
@@ -679,11 +733,10 @@ def main():
     ap.add_argument("--cells", type=int, default=96)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-cg-iters", type=int, default=100)
+    ap.add_argument("--ref-steps", type=int, default=1,
+                    help="--impl reference: full CPU solves timed (at most --steps; about a minute each at 96^3)")
     ap.add_argument("--spmv-traffic", type=float, default=None,
                     help="DRAM bytes per SpMV launch from an ncu capture (reported as roofline.traffic)")
-    ap.add_argument("--ref-counts", type=int, nargs=3, default=[11, 39, 1324],
-                    help="(newton iterations, line-search trials, CG iterations) of the solve; default: the FP64 GPU solve at 96^3")
     ap.add_argument("--check-every", type=int, default=32,
                     help="CG iterations between convergence tests (the body of the solve's graph loop)")
     ap.add_argument("--graph-mode", type=int, default=1, choices=[0, 1, 2],

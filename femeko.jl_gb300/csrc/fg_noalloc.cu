@@ -38,7 +38,8 @@ enum { SC_RZ = 0, SC_ALPHA, SC_BETA, SC_RR, SC_TOL2, SC_RR0 };
 // the whole control block before its first launch, and the last block of each
 // reduction puts C_ARRIVE back to zero.
 enum { C_ARRIVE = 0, C_DONE, C_ITERS, C_STATUS, C_MAXIT };
-enum { ST_RUNNING = 0, ST_CONVERGED = 1, ST_NAN = 2, ST_MAXIT = 3, ST_BAD_INDEX = 4 };
+enum { ST_RUNNING = 0, ST_CONVERGED = 1, ST_NAN = 2, ST_MAXIT = 3, ST_BAD_INDEX = 4, ST_BAD_DIAG = 5,
+       ST_BREAKDOWN = 6 };
 
 }  // namespace
 
@@ -140,7 +141,10 @@ __global__ void __launch_bounds__(NA_THREADS)
       }
     }
     const double r = b[i] - ax;
-    const double dinv = diag != 0.0 ? 1.0 / diag : 0.0;
+    // a Jacobi preconditioner needs a nonzero finite diagonal (a symmetric positive
+    // definite matrix has a positive one): report the row instead of dividing by zero
+    if (!(diag != 0.0) || !isfinite(diag)) atomicExch(P.ctl + C_STATUS, (unsigned)ST_BAD_DIAG);
+    const double dinv = (diag != 0.0 && isfinite(diag)) ? 1.0 / diag : 0.0;
     const double z = dinv * r;
     na_vec(P, NA_R)[i] = r;
     na_vec(P, NA_Z)[i] = z;
@@ -160,7 +164,7 @@ __global__ void __launch_bounds__(NA_THREADS)
     P.scal[SC_BETA] = 0.0;
     P.ctl[C_ITERS] = 0u;
     P.ctl[C_MAXIT] = (unsigned)maxit;
-    unsigned st = P.ctl[C_STATUS];
+    unsigned st = __ldcg(P.ctl + C_STATUS);  // set by any block before it arrived
     if (st == ST_RUNNING) {
       if (!isfinite(trr) || !isfinite(trz)) st = ST_NAN;
       else if (trr == 0.0) st = ST_CONVERGED;
@@ -201,8 +205,11 @@ __global__ void __launch_bounds__(NA_THREADS)
   double tpq, unused;
   if (na_reduce2(pq, 0.0, P, tpq, unused)) {
     if (!isfinite(tpq) || tpq <= 0.0) {
-      P.ctl[C_STATUS] = isfinite(tpq) ? ST_CONVERGED : ST_NAN;  // p.q = 0: nothing left to reduce
-      if (isfinite(tpq) && tpq < 0.0) P.ctl[C_STATUS] = ST_NAN;  // not positive definite
+      // p.q = 0 ends the iteration: converged only if the residual already meets the
+      // tolerance, a breakdown otherwise; p.q < 0: the matrix is not positive definite
+      unsigned stop = ST_NAN;
+      if (isfinite(tpq) && tpq == 0.0) stop = (P.scal[SC_RR] <= P.scal[SC_TOL2]) ? ST_CONVERGED : ST_BREAKDOWN;
+      P.ctl[C_STATUS] = stop;
       P.ctl[C_DONE] = 1u;
     } else {
       P.scal[SC_ALPHA] = P.scal[SC_RZ] / tpq;
@@ -256,13 +263,17 @@ fg_status na_fail(fg_status code, const char *msg) {
   return code;
 }
 
-bool na_device_pointer(const void *p) {
+// True when the kernels, launched on device `dev`, can read and write p: managed
+// memory or memory of `dev` itself.  Another device's memory is refused even where
+// peer access would reach it: the check stays a pure query of the pointer.
+bool na_device_pointer(const void *p, int dev) {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+  if (a.type == cudaMemoryTypeManaged) return true;
+  return a.type == cudaMemoryTypeDevice && a.device == dev;
 }
 
 }  // namespace
@@ -286,14 +297,18 @@ extern "C" fg_status fg_cg_csc_noalloc(int64_t n, const int64_t *colptr, const i
   if (opts.precision != FG_FP64) return na_fail(FG_UNSUPPORTED, "fg_cg_csc_noalloc: FP64 only");
   if (!(opts.rtol >= 0.0)) return na_fail(FG_BAD_ARG, "fg_cg_csc_noalloc: rtol must be >= 0");
   const int check = opts.check_every > 0 ? opts.check_every : 32;
-  const int maxit = opts.maxiter > 0 ? opts.maxiter : 0;
+  // maxiter <= 0 means "no cap given": the default of fg_solve_opts_default, as with o == NULL
+  fg_solve_opts dflt;
+  fg_solve_opts_default(&dflt);
+  const int maxit = opts.maxiter > 0 ? opts.maxiter : dflt.maxiter;
 
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NA_MAX_DEVICES)
     return na_fail(FG_NO_DEVICE, "fg_cg_csc_noalloc: no current CUDA device");
-  if (!na_device_pointer(colptr) || !na_device_pointer(rowval) || !na_device_pointer(nzval) ||
-      !na_device_pointer(b) || !na_device_pointer(x))
-    return na_fail(FG_BAD_ARG, "fg_cg_csc_noalloc: every array must be device (or managed) memory");
+  if (!na_device_pointer(colptr, dev) || !na_device_pointer(rowval, dev) || !na_device_pointer(nzval, dev) ||
+      !na_device_pointer(b, dev) || !na_device_pointer(x, dev))
+    return na_fail(FG_BAD_ARG,
+                   "fg_cg_csc_noalloc: every array must be managed memory or memory of the current device");
 
   std::lock_guard<std::mutex> guard(g_na_lock[dev]);
   if (!g_na_ptr[dev]) {
@@ -328,7 +343,7 @@ extern "C" fg_status fg_cg_csc_noalloc(int64_t n, const int64_t *colptr, const i
                                           maxit, scr);
   FG_LAUNCHED(1);
   unsigned hc[8] = {0};
-  int launched = 0;
+  int64_t launched = 0;
   for (;;) {
     for (int k = 0; k < check; ++k, ++launched) {
       const int pin = (launched & 1) ? NA_P1 : NA_P0;
@@ -342,7 +357,7 @@ extern "C" fg_status fg_cg_csc_noalloc(int64_t n, const int64_t *colptr, const i
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "CG iterations");
     if (hc[C_DONE]) break;
-    if (launched > maxit + check) break;  // the device stops at maxit; never reached
+    if (launched > (int64_t)maxit + check) break;  // the device stops at maxit; never reached
   }
   double hs[8] = {0};
   e = cudaMemcpyAsync(hs, scr + NA_SCAL, sizeof hs, cudaMemcpyDeviceToHost, st);
@@ -361,6 +376,9 @@ extern "C" fg_status fg_cg_csc_noalloc(int64_t n, const int64_t *colptr, const i
     case ST_CONVERGED: return FG_OK;
     case ST_NAN: return na_fail(FG_NAN, "fg_cg_csc_noalloc: CG produced a non-finite or non-positive curvature");
     case ST_BAD_INDEX: return na_fail(FG_BAD_ARG, "fg_cg_csc_noalloc: colptr/rowval not a valid CSC structure");
+    case ST_BAD_DIAG: return na_fail(FG_BAD_ARG, "fg_cg_csc_noalloc: a zero or non-finite diagonal entry");
+    case ST_BREAKDOWN:
+      return na_fail(FG_NOT_CONVERGED, "fg_cg_csc_noalloc: p.q = 0 before the residual met the tolerance");
     default: return na_fail(FG_NOT_CONVERGED, "fg_cg_csc_noalloc: iteration cap reached");
   }
 }

@@ -121,6 +121,9 @@ extern "C" fg_status fg_transport_be(fg_mesh *m, const double *rho_cp, const dou
                                      double *snapshots, const fg_solve_opts *o, fg_solve_stats *s) {
   FaceDev fd;
   double *tmp[4] = {nullptr, nullptr, nullptr, nullptr};
+  // created outside the guarded body so that the cleanup below also runs when the
+  // body leaves early with an error
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
   fg_status st = fg_guard([&]() -> fg_status {
     FG_REQUIRE(m && rho_cp && kappa && vel && T, FG_BAD_ARG, "fg_transport_be: null pointer");
     FG_REQUIRE(nfaces == 0 || (faces && AE && F), FG_BAD_ARG, "fg_transport_be: null face arrays");
@@ -143,7 +146,6 @@ extern "C" fg_status fg_transport_be(fg_mesh *m, const double *rho_cp, const dou
     tmp[1] = upload(m, kdt.data(), (size_t)nt);
     tmp[2] = upload(m, fdt.data(), (size_t)nt);
     tmp[3] = upload(m, vel, 3 * (size_t)nv);
-    cudaEvent_t e0, e1;
     FG_CUDA_TRY(cudaEventCreate(&e0));
     FG_CUDA_TRY(cudaEventCreate(&e1));
     FG_CUDA_TRY(cudaEventRecord(e0, m->stream));
@@ -187,8 +189,6 @@ extern "C" fg_status fg_transport_be(fg_mesh *m, const double *rho_cp, const dou
     fg_sync(m);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     if (s) {
       s->iterations = iters;
       s->refinements = 0;
@@ -199,6 +199,8 @@ extern "C" fg_status fg_transport_be(fg_mesh *m, const double *rho_cp, const dou
     }
     return status == 0 ? FG_OK : FG_NOT_CONVERGED;
   });
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
   if (m) {
     face_free(m, fd);
     for (double *p : tmp)

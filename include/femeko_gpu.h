@@ -233,9 +233,13 @@ fg_status fg_spmv_csc(int64_t n, const int64_t *colptr, const int64_t *rowval, c
  * The first call on each device (with that device current) looks up the scratch
  * address; make that first call before any stream capture.  Calls that overlap on
  * one device would race on the shared scratch: a per-device host lock serialises
- * them.  colptr/rowval/nzval/b/x are device (or managed) pointers; x holds the
- * initial guess and receives the solution; stream may be NULL (default stream);
- * o->precision must be FG_FP64 (o may be NULL: defaults); s->ms is host wall time. */
+ * them.  colptr/rowval/nzval/b/x are managed pointers or pointers to memory of the
+ * current device (another device's memory returns FG_BAD_ARG); x holds the initial
+ * guess and receives the solution; stream may be NULL (default stream);
+ * o->precision must be FG_FP64 (o may be NULL: defaults; o->maxiter <= 0 takes the
+ * default cap too); s->ms is host wall time.  A column range or row index outside
+ * the matrix, or a zero diagonal entry, returns FG_BAD_ARG (checked on the device
+ * before any access); p.q = 0 before the tolerance is met returns FG_NOT_CONVERGED. */
 #define FG_NOALLOC_MAX_ROWS ((int64_t)131072)
 fg_status fg_cg_csc_noalloc(int64_t n, const int64_t *colptr, const int64_t *rowval, const double *nzval,
                             int32_t index_base, const double *b, double *x, const fg_solve_opts *o, void *stream,

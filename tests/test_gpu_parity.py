@@ -158,6 +158,38 @@ def test_newton(precision):
     assert np.abs(mug - muo).max() / muo.max() < 1e-8
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_newton_magnetic_energy(precision):
+    """Magnetic energy (src/magneticProperties.jl:252-309: 1/2 mu H^2 VE on linear
+    elements, the integral of H dB on Froehlich ones) reported by the GPU Newton solve:
+    against the oracle's energy of its own FP64 Newton solution (1e-8), and against
+    the oracle's energy of the GPU's own H (1e-12: the energy kernel alone)."""
+    m, nl, mu_lin, u0 = newton_case()
+    ug, Hg, mug, st = fg.newton_magnetostatics(m, nl, mu_lin, u0, precision=precision)
+    uo, Ho, muo, so = O.newton(m, u0, nl, mu_lin, 1.2e6, 500.0, cg_tol=1e-12, line_search="residual")
+    W_oracle = O.energy(m, Ho, nl, mu_lin, 1.2e6, 500.0)
+    W_same_H = O.energy(m, Hg, nl, mu_lin, 1.2e6, 500.0)
+    assert st["converged"] and W_oracle > 0.0
+    assert abs(st["energy"] - W_oracle) / W_oracle < 1e-8
+    assert abs(st["energy"] - W_same_H) / W_same_H < 1e-12
+
+
+def test_linear_plate_magnetic_energy():
+    """Linear elements only (mu_r = 1000 plate in air, no Froehlich element): the
+    Newton entry point converges in one step and its energy is 1/2 mu H^2 VE summed."""
+    m = fg.box_tet_mesh(10, seed=3)
+    nl = np.zeros(m.nt, dtype=np.uint8)
+    mu_lin = np.where(m.elementID == 2, 1000 * fg.MU0, fg.MU0)
+    u0 = -(np.array([8e4, 0.0, 0.0])[:, None] * m.p).sum(axis=0)
+    ug, Hg, mug, st = fg.newton_magnetostatics(m, nl, mu_lin, u0, precision="fp64")
+    uo, Ho, it = O.linear_magnetostatics(m, u0, mu_lin, cg_tol=1e-12)
+    W_oracle = O.energy(m, Ho, None, mu_lin)
+    assert st["converged"]
+    assert abs(st["energy"] - W_oracle) / W_oracle < 1e-8
+    W_direct = 0.5 * float((mu_lin * (Hg * Hg).sum(axis=0) * m.VE).sum())
+    assert abs(st["energy"] - W_direct) / W_direct < 1e-12
+
+
 def test_resident_newton_same_as_one_call():
     """set inputs once / solve on the device / get outputs == the one-call entry point."""
     m, nl, mu_lin, u0 = newton_case()
