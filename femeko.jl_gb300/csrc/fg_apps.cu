@@ -104,15 +104,31 @@ extern "C" fg_status fg_lagrange(fg_mesh *m, double *C) {
 // src/FEM3D.jl:284-297 BoundaryIntegral: RHS[face nodes] += (n . F) AE / 3 over the
 // boundary faces whose id is in shell_id.  Per face value, then per node the sum
 // over its faces in face order (a node -> face list built on the host).
+// With AE == NULL the face area is computed from the node coordinates p (3 x np), as
+// areaTriangle does in the C++ reference (src/FEMc.cpp:44-53): |AB x AC| / 2.
 __global__ void k_face_flux(int64_t ns, const int *__restrict__ sT, const double *__restrict__ normal,
-                            const double *__restrict__ AE, double F0, double F1, double F2,
-                            const int *__restrict__ shell, int nshell, double *__restrict__ v) {
+                            const double *__restrict__ AE, const double *__restrict__ p, double F0, double F1,
+                            double F2, const int *__restrict__ shell, int nshell, double *__restrict__ v) {
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= ns) return;
   const int id = sT[4 * s + 3];
   bool hit = false;
   for (int q = 0; q < nshell; ++q) hit |= (id == shell[q]);
-  v[s] = hit ? (normal[3 * s] * F0 + normal[3 * s + 1] * F1 + normal[3 * s + 2] * F2) * AE[s] / 3.0 : 0.0;
+  double area = 0.0;
+  if (hit) {
+    if (AE) {
+      area = AE[s];
+    } else {
+      const double *a = p + 3 * (int64_t)sT[4 * s], *b = p + 3 * (int64_t)sT[4 * s + 1],
+                   *c = p + 3 * (int64_t)sT[4 * s + 2];
+      const double ab[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+      const double ac[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+      const double cx = ab[1] * ac[2] - ab[2] * ac[1], cy = ab[2] * ac[0] - ab[0] * ac[2],
+                   cz = ab[0] * ac[1] - ab[1] * ac[0];
+      area = 0.5 * sqrt(cx * cx + cy * cy + cz * cz);
+    }
+  }
+  v[s] = hit ? (normal[3 * s] * F0 + normal[3 * s + 1] * F1 + normal[3 * s + 2] * F2) * area / 3.0 : 0.0;
 }
 
 __global__ void k_node_faces(int64_t nv, const int *__restrict__ ptr, const int *__restrict__ face,
@@ -124,67 +140,83 @@ __global__ void k_node_faces(int64_t nv, const int *__restrict__ ptr, const int 
   out[i] = acc;
 }
 
+// Device form of the boundary integral: writes all nv entries of d_out (device).
+// AE may be NULL: the face areas then come from the mesh's coordinates.
+void fg_boundary_rhs_dev(fg_mesh *m, const int32_t *surfaceT, int64_t ns, int32_t index_base, const double *normal,
+                         const double *AE, const double *F, const int32_t *shell_id, int32_t nshell,
+                         double *d_out) {
+  FG_REQUIRE(F && (ns == 0 || (surfaceT && normal)), FG_BAD_ARG, "boundary integral: null pointer");
+  FG_REQUIRE(ns >= 0 && nshell >= 0 && (nshell == 0 || shell_id), FG_BAD_ARG, "boundary integral: bad sizes");
+  FG_REQUIRE(index_base == 0 || index_base == 1, FG_BAD_ARG, "boundary integral: index_base must be 0 or 1");
+  const int64_t nv = m->nv;
+  // node -> faces (face order), 0-based copy of the faces
+  std::vector<int> st((size_t)4 * ns), cnt((size_t)nv + 1, 0);
+  for (int64_t s = 0; s < ns; ++s) {
+    for (int a = 0; a < 3; ++a) {
+      const int64_t node = (int64_t)surfaceT[4 * s + a] - index_base;
+      FG_REQUIRE(node >= 0 && node < nv, FG_BAD_MESH, "boundary integral: face node out of range");
+      st[4 * s + a] = (int)node;
+      ++cnt[node + 1];
+    }
+    st[4 * s + 3] = surfaceT[4 * s + 3];
+  }
+  for (int64_t i = 0; i < nv; ++i) cnt[i + 1] += cnt[i];
+  std::vector<int> face((size_t)3 * ns), fill(cnt.begin(), cnt.end() - 1);
+  for (int64_t s = 0; s < ns; ++s)
+    for (int a = 0; a < 3; ++a) face[fill[st[4 * s + a]]++] = (int)s;
+  // device work space for this call
+  std::vector<void *> tmp;
+  struct Free {
+    fg_mesh *m;
+    std::vector<void *> &v;
+    ~Free() {
+      cudaStreamSynchronize(m->stream);
+      for (void *p : v) cudaFree(p);
+    }
+  } release{m, tmp};
+  auto dmalloc = [&](size_t bytes) {
+    void *p = nullptr;
+    FG_CUDA_TRY(cudaMalloc(&p, std::max<size_t>(bytes, 16)));
+    tmp.push_back(p);
+    return p;
+  };
+  int *d_st = (int *)dmalloc(sizeof(int) * st.size()), *d_ptr = (int *)dmalloc(sizeof(int) * cnt.size());
+  int *d_face = (int *)dmalloc(sizeof(int) * face.size()), *d_shell = (int *)dmalloc(sizeof(int) * (nshell + 1));
+  double *d_n = (double *)dmalloc(sizeof(double) * 3 * ns);
+  double *d_ae = AE ? (double *)dmalloc(sizeof(double) * ns) : nullptr;
+  double *d_v = (double *)dmalloc(sizeof(double) * ns);
+  auto up = [&](void *dst, const void *src, size_t bytes) {
+    if (bytes) FG_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, m->stream));
+  };
+  up(d_st, st.data(), sizeof(int) * st.size());
+  up(d_ptr, cnt.data(), sizeof(int) * cnt.size());
+  up(d_face, face.data(), sizeof(int) * face.size());
+  up(d_shell, shell_id, sizeof(int) * nshell);
+  up(d_n, normal, sizeof(double) * 3 * ns);
+  if (AE) up(d_ae, AE, sizeof(double) * ns);
+  if (ns > 0) {
+    k_face_flux<<<grid_for(ns, 256), 256, 0, m->stream>>>(ns, d_st, d_n, d_ae, m->p, F[0], F[1], F[2], d_shell,
+                                                          nshell, d_v);
+    FG_LAUNCHED(1);
+  }
+  k_node_faces<<<grid_for(nv, 256), 256, 0, m->stream>>>(nv, d_ptr, d_face, d_v, d_out);
+  FG_LAUNCHED(1);
+  FG_CUDA_TRY(cudaGetLastError());
+}
+
 extern "C" fg_status fg_boundary_integral(fg_mesh *m, const int32_t *surfaceT, int64_t ns, int32_t index_base,
                                           const double *normal, const double *AE, const double *F,
                                           const int32_t *shell_id, int32_t nshell, double *RHS) {
-  return fg_guard([&]() -> fg_status {
+  double *d_out = nullptr;
+  fg_status st = fg_guard([&]() -> fg_status {
     FG_REQUIRE(m && RHS && F && (ns == 0 || (surfaceT && normal && AE)), FG_BAD_ARG,
                "fg_boundary_integral: null pointer");
-    FG_REQUIRE(ns >= 0 && nshell >= 0 && (nshell == 0 || shell_id), FG_BAD_ARG, "fg_boundary_integral: bad sizes");
-    FG_REQUIRE(index_base == 0 || index_base == 1, FG_BAD_ARG, "fg_boundary_integral: index_base must be 0 or 1");
-    const int64_t nv = m->nv;
-    // node -> faces (face order), 0-based copy of the faces
-    std::vector<int> st((size_t)4 * ns), cnt((size_t)nv + 1, 0);
-    for (int64_t s = 0; s < ns; ++s) {
-      for (int a = 0; a < 3; ++a) {
-        const int64_t node = (int64_t)surfaceT[4 * s + a] - index_base;
-        FG_REQUIRE(node >= 0 && node < nv, FG_BAD_MESH, "fg_boundary_integral: face node out of range");
-        st[4 * s + a] = (int)node;
-        ++cnt[node + 1];
-      }
-      st[4 * s + 3] = surfaceT[4 * s + 3];
-    }
-    for (int64_t i = 0; i < nv; ++i) cnt[i + 1] += cnt[i];
-    std::vector<int> face((size_t)3 * ns), fill(cnt.begin(), cnt.end() - 1);
-    for (int64_t s = 0; s < ns; ++s)
-      for (int a = 0; a < 3; ++a) face[fill[st[4 * s + a]]++] = (int)s;
-    // device work space for this call
-    std::vector<void *> tmp;
-    struct Free {
-      std::vector<void *> &v;
-      ~Free() {
-        for (void *p : v) cudaFree(p);
-      }
-    } release{tmp};
-    auto dmalloc = [&](size_t bytes) {
-      void *p = nullptr;
-      FG_CUDA_TRY(cudaMalloc(&p, std::max<size_t>(bytes, 16)));
-      tmp.push_back(p);
-      return p;
-    };
-    int *d_st = (int *)dmalloc(sizeof(int) * st.size()), *d_ptr = (int *)dmalloc(sizeof(int) * cnt.size());
-    int *d_face = (int *)dmalloc(sizeof(int) * face.size()), *d_shell = (int *)dmalloc(sizeof(int) * (nshell + 1));
-    double *d_n = (double *)dmalloc(sizeof(double) * 3 * ns), *d_ae = (double *)dmalloc(sizeof(double) * ns);
-    double *d_v = (double *)dmalloc(sizeof(double) * ns), *d_out = (double *)dmalloc(sizeof(double) * nv);
-    auto up = [&](void *dst, const void *src, size_t bytes) {
-      if (bytes) FG_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, m->stream));
-    };
-    up(d_st, st.data(), sizeof(int) * st.size());
-    up(d_ptr, cnt.data(), sizeof(int) * cnt.size());
-    up(d_face, face.data(), sizeof(int) * face.size());
-    up(d_shell, shell_id, sizeof(int) * nshell);
-    up(d_n, normal, sizeof(double) * 3 * ns);
-    up(d_ae, AE, sizeof(double) * ns);
-    if (ns > 0) {
-      k_face_flux<<<grid_for(ns, 256), 256, 0, m->stream>>>(ns, d_st, d_n, d_ae, F[0], F[1], F[2], d_shell, nshell,
-                                                            d_v);
-      FG_LAUNCHED(1);
-    }
-    k_node_faces<<<grid_for(nv, 256), 256, 0, m->stream>>>(nv, d_ptr, d_face, d_v, d_out);
-    FG_LAUNCHED(1);
-    FG_CUDA_TRY(cudaGetLastError());
-    FG_CUDA_TRY(cudaMemcpyAsync(RHS, d_out, sizeof(double) * nv, cudaMemcpyDeviceToHost, m->stream));
+    FG_CUDA_TRY(cudaMalloc(&d_out, sizeof(double) * (size_t)std::max<int64_t>(m->nv, 1)));
+    fg_boundary_rhs_dev(m, surfaceT, ns, index_base, normal, AE, F, shell_id, nshell, d_out);
+    FG_CUDA_TRY(cudaMemcpyAsync(RHS, d_out, sizeof(double) * m->nv, cudaMemcpyDeviceToHost, m->stream));
     fg_sync(m);
     return FG_OK;
   });
+  if (d_out) cudaFree(d_out);
+  return st;
 }

@@ -301,6 +301,10 @@ void fg_newton_assemble_split(fg_mesh *m, const double *d_u, double Ms, double H
                               bool want_jacobian, bool tangent);
 // d_out[i] = sum of the vector records of row i (P1 tetrahedra), no Dirichlet masking.
 void fg_vector_gather(fg_mesh *m, double *d_out);
+// src/FEM3D.jl:284-297 / src/FEMc.cpp:170-200 BoundaryIntegral into a device vector
+// (nv entries written); AE == NULL takes the face areas from the mesh coordinates.
+void fg_boundary_rhs_dev(fg_mesh *m, const int32_t *surfaceT, int64_t ns, int32_t index_base, const double *normal,
+                         const double *AE, const double *F, const int32_t *shell_id, int32_t nshell, double *d_out);
 // Demagnetising field (Micromagnetics/LL.jl:162-211): load vector of the inside
 // elements from the nodal magnetisation, and the nodal volume average of H.
 void fg_demag_rhs_dev(fg_mesh *m, const uint8_t *d_inside, const double *d_M, double *d_b);

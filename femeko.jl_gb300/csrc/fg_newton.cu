@@ -332,6 +332,96 @@ extern "C" fg_status fg_magnetostatics_linear(fg_mesh *m, const double *mu, cons
   });
 }
 
+// Per-element factor of the stiffness for the caller's element volumes: the stored
+// geometry holds VE grad phi_a . grad phi_b with this library's VE, so f = mu VE_in / VE
+// gives mu VE_in grad phi_a . grad phi_b (src/FEMc.cpp:74-96 takes VE from the caller).
+__global__ void k_mu_caller_ve(int64_t nt, const double *__restrict__ mu, const double *__restrict__ ve_in,
+                               const double *__restrict__ geo, int vol_row, double *__restrict__ f) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt) return;
+  const double ve = geo[(int64_t)vol_row * nt + k];
+  f[k] = ve != 0.0 ? mu[k] * (ve_in[k] / ve) : 0.0;
+}
+
+// Femeko_jl_C++/Magnetostatics/magnetostatics.cpp:5-95 (scalarPotential): the linear
+// Neumann problem K(mu) u = -BoundaryIntegral(Hext) on the whole mesh, no Dirichlet
+// rows (the system is singular with the constants as null space and consistent:
+// the flux of a uniform field through the closed shell is zero), solved by
+// Jacobi-PCG from u = 0 like Eigen's ConjugateGradient with its diagonal
+// preconditioner (src/FEMc.cpp:26-38 of the caller).  t and surfaceT are 0-based as
+// Femeko_jl_C++/Magnetostatics/run.jl:49-52 passes them; surfaceT is 4 x ns (three
+// nodes and the boundary id, row 4 compared with shell_id).
+extern "C" fg_status fg_scalar_potential(double *u, const double *p, const int32_t *t, const int32_t *surfaceT,
+                                         const double *normal, int32_t nv, int32_t nt, int32_t ns, const double *VE,
+                                         const double *mu, const double *Hext, int32_t shell_id,
+                                         const fg_solve_opts *o, fg_solve_stats *s) {
+  fg_mesh *m = nullptr;
+  fg_status st = fg_guard([&]() -> fg_status {
+    FG_REQUIRE(u && p && t && VE && mu && Hext && (ns == 0 || (surfaceT && normal)), FG_BAD_ARG,
+               "fg_scalar_potential: null pointer");
+    FG_REQUIRE(nv > 0 && nt > 0 && ns >= 0, FG_BAD_ARG, "fg_scalar_potential: bad sizes");
+    return FG_OK;
+  });
+  if (st != FG_OK) return st;
+  st = fg_mesh_create(p, nv, t, nt, 4, 0, &m);
+  if (st != FG_OK) return st;
+  st = fg_guard([&]() -> fg_status {
+    fg_solve_opts opts;
+    fg_solve_opts_default(&opts);
+    if (o) {
+      opts = *o;
+    } else {
+      opts.precision = FG_MIXED;
+      opts.rtol = 1e-12;
+    }
+    const bool mixed = opts.precision == FG_MIXED;
+    ensure_element_state(m);
+    double *d_f = m->wdens, *d_b = vec64(m, 9), *d_x = vec64(m, 7);
+    upload(m, m->mu_lin, mu, sizeof(double) * (size_t)nt);
+    // the caller's volumes, staged through an element-sized buffer of the handle
+    double *d_vein = m->dmu;
+    upload(m, d_vein, VE, sizeof(double) * (size_t)nt);
+    k_mu_caller_ve<<<grid_for(nt, 256), 256, 0, m->stream>>>(nt, m->mu_lin, d_vein, m->geo, m->nvert * m->dim, d_f);
+    FG_CUDA_TRY(cudaGetLastError());
+    FG_LAUNCHED(1);
+    fg_assemble_operator(m, ASM_STIFF, d_f, nullptr, nullptr, 0.0, 0.0, 0, OUT_SELL, true, mixed, true);
+    // b = -RHS = BoundaryIntegral(-Hext): the integral is linear in the field
+    const double mF[3] = {-Hext[0], -Hext[1], -Hext[2]};
+    const int32_t shell = shell_id;
+    fg_boundary_rhs_dev(m, surfaceT, ns, 0, normal, nullptr, mF, &shell, 1, d_b);
+    FG_CUDA_TRY(cudaMemsetAsync(d_x, 0, sizeof(double) * (size_t)nv, m->stream));
+    fg_solve_stats ss{};
+    const int rc = fg_pcg_solve(m, d_b, d_x, opts, &ss, false);
+    download(m, u, d_x, sizeof(double) * (size_t)nv);
+    fg_sync(m);
+    fg_check_flags(m, "fg_scalar_potential");
+    if (s) *s = ss;
+    if (rc != 0) {
+      fg_set_error("fg_scalar_potential: CG stopped at the iteration cap before the tolerance");
+      return FG_NOT_CONVERGED;
+    }
+    return FG_OK;
+  });
+  const fg_status d = fg_mesh_destroy(m);
+  return st != FG_OK ? st : d;
+}
+
+// The reference's own entry point, same name and arguments (a void C function that
+// Julia binds with @ccall ... ::Cvoid, run.jl:66-79).  Nothing throws across it: the
+// status is kept for fg_scalar_potential_status() and the message in fg_last_error()
+// (empty after a successful call).  u receives the solution (also when the iteration
+// cap stopped the solve); on any other error u is left as it was.
+static thread_local fg_status g_sp_status = FG_OK;
+
+extern "C" void scalarPotential(double *u_in, double *p_in, int *t_in, int *surfaceT_in, double *normal_in, int nv,
+                                int nt, int ns, double *VE, double *mu, double *Hext, int shell_id) {
+  fg_set_error("");
+  g_sp_status = fg_scalar_potential(u_in, p_in, t_in, surfaceT_in, normal_in, nv, nt, ns, VE, mu, Hext, shell_id,
+                                    nullptr, nullptr);
+}
+
+extern "C" fg_status fg_scalar_potential_status(void) { return g_sp_status; }
+
 // Adjoint sensitivity of J = volume-weighted mean Hx over the target elements with
 // respect to the per-element relative permeability.  Forward: the linear solve of
 // Magnetostatics/magneticField.jl:89-132 (nl == NULL) or the Newton solve of

@@ -255,6 +255,43 @@ def magnetostatics_linear(mesh: MESH, mu, u_in, precision="fp64", rtol=1e-10, **
     return u, H.reshape(mesh.nt, 3).T, L.stats_dict(s)
 
 
+def scalarPotential(mesh: MESH, mu, Hext, shell_id, precision="mixed", rtol=1e-12, reference_call=False, **kw):
+    """Linear Neumann magnetostatics of the C++ reference's ``scalarPotential``
+    (Femeko_jl_C++/Magnetostatics/magnetostatics.cpp:5-95): u with
+    K(mu) u = -BoundaryIntegral(Hext) over the faces whose id equals ``shell_id``
+    (ids as stored in ``mesh.surfaceT`` row 4), solved from u = 0 by Jacobi-PCG.
+    reference_call=True goes through the void ``scalarPotential`` symbol with the
+    reference's 0-based argument layout (Femeko_jl_C++/Magnetostatics/run.jl:49-79);
+    otherwise through ``fg_scalar_potential`` with options.  Returns (u, stats)."""
+    # the reference's layout (run.jl:49-52): 0-based nodes, and the boundary ids and
+    # shell id shifted down by one alongside them; this mesh holds 0-based nodes and
+    # the reference's 1-based ids
+    # (column-major 3 x nv, 4 x nt, 4 x ns, 3 x ns: C order of the transposes)
+    t0 = _c(mesh.t.T, np.int32)
+    sT = np.array(mesh.surfaceT, dtype=np.int32, copy=True)
+    sT[3] -= 1
+    sT = _c(sT.T, np.int32)
+    shell = int(shell_id) - 1
+    p = _c(mesh.p.T, np.float64)
+    nrm = _c(mesh.normal.T, np.float64)
+    VE = _c(mesh.VE, np.float64)
+    muv = _c(mu, np.float64)
+    H = _c(Hext, np.float64)
+    u = np.zeros(mesh.nv)
+    lib = L.lib()
+    args = (L.ptr(u), L.ptr(p), L.ptr(t0), L.ptr(sT), L.ptr(nrm), int(mesh.nv), int(mesh.nt),
+            int(sT.shape[0]), L.ptr(VE), L.ptr(muv), L.ptr(H), shell)
+    if reference_call:
+        lib.scalarPotential(*args)
+        st = lib.fg_scalar_potential_status()
+        L.check(st, allow_not_converged=True)
+        return u, {"status": st}
+    o = solve_opts(precision=precision, rtol=rtol, **kw)
+    s = L.SolveStats()
+    L.check(lib.fg_scalar_potential(*args, C.byref(o), C.byref(s)), allow_not_converged=True)
+    return u, L.stats_dict(s)
+
+
 def newton_magnetostatics(mesh: MESH, nl, mu_lin, u0, **kw):
     """Nonlinear Newton-Raphson magnetostatics; returns (u, H, mu, stats)."""
     g = gpu_mesh(mesh)

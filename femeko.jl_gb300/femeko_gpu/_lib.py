@@ -115,13 +115,18 @@ SIGNATURES = {
                          C.POINTER(AdjointStats)],
     "fg_scalar_potential_newton": [_vp, _i64, _vp, _i64, _i32, _vp, _vp, _vp, _vp, C.POINTER(NewtonOpts), _vp, _vp,
                                    _vp, C.POINTER(NewtonStats)],
+    "fg_scalar_potential": [_vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp, _vp, _i32, C.POINTER(SolveOpts),
+                            C.POINTER(SolveStats)],
+    "fg_scalar_potential_status": [],
     "fg_bench_kernel": [_vp, _i32, _i32, _i32, C.POINTER(_d)],
     "fg_mesh_layout": [_vp, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i32)],
     "fg_autotune": [_vp, _i32, C.POINTER(_i32), _vp, _i32],
     "fg_set_cg_variant": [_vp, _i32, _i32],
     "fg_get_cg_variant": [_vp, _i32, C.POINTER(_i32)],
 }
-VOID_FUNCS = {"fg_solve_opts_default": [C.POINTER(SolveOpts)], "fg_newton_opts_default": [C.POINTER(NewtonOpts)]}
+VOID_FUNCS = {"fg_solve_opts_default": [C.POINTER(SolveOpts)], "fg_newton_opts_default": [C.POINTER(NewtonOpts)],
+              # the reference's own void entry point (Femeko_jl_C++/Magnetostatics/magnetostatics.cpp:49-61)
+              "scalarPotential": [_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, C.c_int]}
 
 _lib = None
 

@@ -421,9 +421,36 @@ fg_status fg_demag_field(fg_mesh *m, const uint8_t *inside, const double *M, con
 /* H = -sum u_a grad(phi_a) per element (Magnetostatics/magneticField.jl:111-124). */
 fg_status fg_hfield(fg_mesh *m, const double *u, double *H);
 
-/* One call from host arrays, the shape of the ccall boundary scalarPotential
- * (Femeko_jl_C++/Magnetostatics/magnetostatics.cpp:49-95, called from
- * Femeko_jl_C++/Magnetostatics/run.jl:66-79) for the Newton solve of
+/* Drop-in for the reference's own ccall entry point
+ * Femeko_jl_C++/Magnetostatics/magnetostatics.cpp:49-95 (scalarPotential, bound by
+ * Femeko_jl_C++/Magnetostatics/run.jl:66-79 with @ccall ... ::Cvoid): same name, same
+ * argument list and meaning.  Solves the linear Neumann problem of magnetostatics()
+ * (magnetostatics.cpp:5-38): RHS = BoundaryIntegral(p, surfaceT, normal, Hext,
+ * shell_id) (src/FEMc.cpp:170-200: faces whose id, row 4 of surfaceT, equals shell_id;
+ * face areas from p), A = stiffnessMatrix(p, t, VE, mu) (src/FEMc.cpp:74-125, with the
+ * caller's VE), u = CG(A) \ (-RHS) from u = 0 with the diagonal (Jacobi)
+ * preconditioner; the solution is unique up to a constant, and the zero start fixes
+ * it as Eigen's does (sum_i A_ii u_i = 0 in exact arithmetic).
+ * p 3 x nv, t 4 x nt and surfaceT 4 x ns (0-based, as run.jl:49-52 shifts them),
+ * normal 3 x ns, VE and mu nt, Hext 3; u (nv) receives the potential.
+ * Solver: FP32 Jacobi-PCG inside FP64 iterative refinement to relative residual
+ * 1e-12 (Eigen's default asks for machine epsilon, which its 2n iteration cap
+ * rarely reaches).  The reference throws C++ exceptions through this extern "C"
+ * function; here nothing is thrown: fg_scalar_potential_status() returns the status of
+ * the calling thread's last call and fg_last_error() its message (empty after
+ * success).  u is written on FG_OK and FG_NOT_CONVERGED, left as it was otherwise. */
+void scalarPotential(double *u_in, double *p_in, int *t_in, int *surfaceT_in, double *normal_in, int nv, int nt,
+                     int ns, double *VE, double *mu, double *Hext, int shell_id);
+fg_status fg_scalar_potential_status(void);
+/* The same solve with a status return, solver options (o may be NULL: the defaults
+ * of scalarPotential above) and statistics (s may be NULL). */
+fg_status fg_scalar_potential(double *u, const double *p, const int32_t *t, const int32_t *surfaceT,
+                              const double *normal, int32_t nv, int32_t nt, int32_t ns, const double *VE,
+                              const double *mu, const double *Hext, int32_t shell_id, const fg_solve_opts *o,
+                              fg_solve_stats *s);
+
+/* One call from host arrays in the shape of the ccall boundary scalarPotential
+ * above, for the nonlinear Dirichlet problem: the Newton solve of
  * Magnetostatics/NewtonRaphson.jl:109-214: uploads the P1 mesh (p 3 x nv, t 4 x nt),
  * builds the pattern, solves, downloads u/H/mu and releases the device memory.
  * fixed marks Dirichlet nodes (u0 holds their values). */

@@ -464,6 +464,27 @@ def BoundaryIntegral(mesh, F, shell_id=(1,)):
     return RHS
 
 
+def face_areas(mesh):
+    """areaTriangle of the C++ reference (src/FEMc.cpp:44-53): |AB x AC| / 2 from p."""
+    a, b, c = (mesh.p[:, mesh.surfaceT[q]] for q in range(3))
+    return 0.5 * np.linalg.norm(np.cross((b - a).T, (c - a).T), axis=1)
+
+
+def scalarPotential(mesh, mu, Hext, shell_id, tol=1e-13, maxit=1_000_000):
+    """magnetostatics() of Femeko_jl_C++/Magnetostatics/magnetostatics.cpp:5-38:
+    RHS = BoundaryIntegral(p, surfaceT, normal, Hext, shell_id) with the face areas
+    from p (src/FEMc.cpp:170-200), A = stiffnessMatrix(p, t, VE, mu) (:74-125), and
+    u = A \\ (-RHS) by diagonal-preconditioned CG from u = 0 (Eigen's
+    ConjugateGradient).  shell_id is the id as stored in surfaceT row 4.
+    Returns (u, iterations, relres)."""
+    sT = _c(mesh.surfaceT.T, np.int32)
+    RHS = np.zeros(mesh.nv)
+    lib().or_boundary_integral(sT, mesh.ns, mesh.nv, _c(mesh.normal.T, np.float64), _c(face_areas(mesh), np.float64),
+                               _c(Hext, np.float64), _c([shell_id], np.int32), 1, RHS)
+    A = stiffnessMatrix(mesh, mu)
+    return pcg(A, -RHS, tol=tol, maxit=maxit)
+
+
 def pcg(A, b, x0=None, fixed=None, tol=1e-10, maxit=100000):
     """Jacobi-PCG on a symmetric CSC matrix; returns (x, iterations, relres)."""
     A = sp.csc_matrix(A)

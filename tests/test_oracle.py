@@ -339,3 +339,15 @@ def test_nedelec_known_answers():
     assert np.allclose(Bf[:, 0], B0, rtol=0, atol=1e-12) and abs(Bn[0] - np.linalg.norm(B0)) < 1e-12
     rhs = O.nedelec_load(one, B0)
     assert np.allclose(O.nedelecLocalStiffness(one)[:, 0].reshape(6, 6) @ u, rhs, rtol=0, atol=1e-12 * np.abs(rhs).max())
+
+
+def test_oracle_scalar_potential_patch_test():
+    """magnetostatics() of the C++ reference (Neumann, no Dirichlet rows): with a
+    uniform factor mu = 1 the discrete solution is u = -Hext.x + c exactly (P1 holds
+    linear fields, and the boundary integral of a linear basis over a face is AE/3)."""
+    m = box_tet_mesh(4, seed=3)
+    Hext = np.array([0.7, -0.2, 0.4])
+    u, it, rr = O.scalarPotential(m, np.ones(m.nt), Hext, 1, tol=1e-14)
+    exact = -(Hext[:, None] * m.p).sum(axis=0)
+    d = u - exact
+    assert np.abs(d - d.mean()).max() < 1e-10 * np.abs(exact).max()
