@@ -131,10 +131,16 @@ __global__ void __launch_bounds__(NA_THREADS)
   if (i < n) {
     double ax = 0.0, diag = 0.0;
     int64_t k0, k1;
+    bool bad = true;
     if (na_col_range(colptr, i, nnz, base, k0, k1, P)) {
+      bad = false;
       for (int64_t k = k0; k < k1; ++k) {
         const int64_t j = rowval[k] - base;
-        if (j < 0 || j >= n) { atomicExch(P.ctl + C_STATUS, (unsigned)ST_BAD_INDEX); continue; }
+        if (j < 0 || j >= n) {
+          atomicExch(P.ctl + C_STATUS, (unsigned)ST_BAD_INDEX);
+          bad = true;
+          continue;
+        }
         const double a = nzval[k];
         ax = fma(a, x[j], ax);
         if (j == i) diag += a;
@@ -142,8 +148,11 @@ __global__ void __launch_bounds__(NA_THREADS)
     }
     const double r = b[i] - ax;
     // a Jacobi preconditioner needs a nonzero finite diagonal (a symmetric positive
-    // definite matrix has a positive one): report the row instead of dividing by zero
-    if (!(diag != 0.0) || !isfinite(diag)) atomicExch(P.ctl + C_STATUS, (unsigned)ST_BAD_DIAG);
+    // definite matrix has a positive one): report the row instead of dividing by zero.
+    // A structure error takes precedence (it is written unconditionally, this only
+    // over a running status), and a row with a bad index reports only that.
+    if (!bad && (!(diag != 0.0) || !isfinite(diag)))
+      atomicCAS(P.ctl + C_STATUS, (unsigned)ST_RUNNING, (unsigned)ST_BAD_DIAG);
     const double dinv = (diag != 0.0 && isfinite(diag)) ? 1.0 / diag : 0.0;
     const double z = dinv * r;
     na_vec(P, NA_R)[i] = r;
