@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfemeko_gpu.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-SOURCES = ["fg_setup.cu", "fg_assemble.cu", "fg_solve.cu", "fg_newton.cu", "fg_apps.cu", "fg_noalloc.cu", "fg_heat.cu", "fg_batch.cu", "fg_sweep.cu", "fg_transport.cu", "fg_nedelec.cu"]
+SOURCES = ["fg_setup.cu", "fg_assemble.cu", "fg_solve.cu", "fg_newton.cu", "fg_apps.cu", "fg_noalloc.cu", "fg_heat.cu", "fg_batch.cu", "fg_sweep.cu", "fg_blockcg.cu", "fg_transport.cu", "fg_nedelec.cu"]
 
 
 def nvcc() -> str:

@@ -19,11 +19,19 @@ struct FgError {
   std::string msg;
 };
 
+// The message names the failing call and its source position (file name and line).
+static inline const char *fg_basename(const char *path) {
+  const char *b = path;
+  for (const char *c = path; *c; ++c)
+    if (*c == '/') b = c + 1;
+  return b;
+}
 #define FG_CUDA_TRY(call)                                                                    \
   do {                                                                                       \
     cudaError_t e_ = (call);                                                                 \
     if (e_ != cudaSuccess)                                                                   \
-      throw FgError{FG_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)};            \
+      throw FgError{FG_CUDA, std::string(#call) + " at " + fg_basename(__FILE__) + ":" +     \
+                                 std::to_string(__LINE__) + ": " + cudaGetErrorString(e_)};  \
   } while (0)
 
 #define FG_REQUIRE(cond, code, msg)                                                          \

@@ -312,6 +312,10 @@ __global__ void k_sw_extract(int64_t n, int NR, int nfield, const double *__rest
 
 }  // namespace
 
+// fg_blockcg.cu: the rank-revealing block-CG form of the sweep
+fg_status fg_sweep_block(fg_mesh *m, int nfield, const double *H0, const fg_solve_opts &o, double *U,
+                         fg_solve_stats *s);
+
 template <int J>
 static fg_status sweep_impl(fg_mesh *m, int nfield, const double *H0, const fg_solve_opts &o, double *U,
                             fg_solve_stats *s) {
@@ -449,16 +453,20 @@ extern "C" fg_status fg_magnetostatics_sweep(fg_mesh *m, const double *mu, int32
                                              const fg_solve_opts *o, double *U, fg_solve_stats *s) {
   return fg_guard([&]() -> fg_status {
     FG_REQUIRE(m && mu && H0 && nfield > 0, FG_BAD_ARG, "fg_magnetostatics_sweep: bad arguments");
-    FG_REQUIRE(nfield <= 256, FG_BAD_ARG, "fg_magnetostatics_sweep: at most 256 fields per call");
     FG_REQUIRE(m->npe == 4 || m->npe == 3, FG_UNSUPPORTED, "fg_magnetostatics_sweep: P1 elements only");
-    FG_REQUIRE(m->maxrow4 <= 32, FG_UNSUPPORTED, "fg_magnetostatics_sweep: rows longer than 32 entries");
     fg_solve_opts opts;
     fg_solve_opts_default(&opts);
     if (o) opts = *o;
     FG_REQUIRE(opts.precision == FG_MIXED, FG_UNSUPPORTED, "fg_magnetostatics_sweep: FG_MIXED only");
+    FG_REQUIRE(opts.spmv == FG_SWEEP_BLOCK || opts.spmv == FG_SWEEP_PER_FIELD, FG_BAD_ARG,
+               "fg_magnetostatics_sweep: o->spmv selects FG_SWEEP_BLOCK (0) or FG_SWEEP_PER_FIELD (1)");
+    const bool block = opts.spmv == FG_SWEEP_BLOCK;
+    FG_REQUIRE(block || nfield <= 256, FG_BAD_ARG, "fg_magnetostatics_sweep: at most 256 fields per call per field");
+    FG_REQUIRE(block || m->maxrow4 <= 32, FG_UNSUPPORTED, "fg_magnetostatics_sweep: rows longer than 32 entries");
     if (!m->mu_lin) m->mu_lin = dev_alloc<double>(m, (size_t)m->nt);
     FG_CUDA_TRY(cudaMemcpyAsync(m->mu_lin, mu, sizeof(double) * (size_t)m->nt, cudaMemcpyHostToDevice, m->stream));
     fg_assemble_operator(m, ASM_STIFF, m->mu_lin, nullptr, nullptr, 0.0, 0.0, 0, OUT_SELL, true, true, true);
+    if (block) return fg_sweep_block(m, nfield, H0, opts, U, s);
     const int J = (nfield + 31) / 32;
     switch (J) {
       case 1: return sweep_impl<1>(m, nfield, H0, opts, U, s);

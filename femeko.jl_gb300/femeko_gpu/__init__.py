@@ -369,19 +369,27 @@ def transport_be(mesh: MESH, T0, rho_cp, kappa, u, dt, nsteps, face_F=None, face
     return T, snaps[:nsnap], d
 
 
-def magnetostatics_sweep(mesh: MESH, mu, H0, rtol=1e-10, inner_rtol=1e-5, maxiter=1_000_000, check_every=16):
-    """Linear magnetostatics for many applied fields H0 (nfield x 3) at once (one
-    multi-right-hand-side CG, FP32 inner + FP64 refinement); returns (U nv x nfield, stats)."""
+def magnetostatics_sweep(mesh: MESH, mu, H0, rtol=1e-10, inner_rtol=1e-5, maxiter=1_000_000, check_every=16,
+                         method="block"):
+    """Linear magnetostatics for many applied fields H0 (nfield x 3) at once, FP32
+    inner iterations + FP64 refinement; returns (U nv x nfield, stats).
+    method="block": the fields' rank-revealing reduction to r <= 3 field directions
+    and one block CG of width r (stats["rank"] = r); "per_field": one CG per field
+    sharing every matrix read."""
     g = gpu_mesh(mesh)
     H = _c(np.asarray(H0, dtype=np.float64).reshape(-1, 3), np.float64)   # 3 x nfield column-major
     nf = H.shape[0]
     U = np.zeros((nf, mesh.nv))                                             # column-major nv x nf
-    o = solve_opts(precision="mixed", rtol=rtol, inner_rtol=inner_rtol, maxiter=maxiter, check_every=check_every)
+    o = solve_opts(precision="mixed", rtol=rtol, inner_rtol=inner_rtol, maxiter=maxiter, check_every=check_every,
+                   spmv={"block": 0, "per_field": 1}[method])
     s = L.SolveStats()
     st = L.lib().fg_magnetostatics_sweep(g.h, L.ptr(_c(mu, np.float64)), nf, L.ptr(H), C.byref(o), L.ptr(U),
                                          C.byref(s))
     L.check(st, allow_not_converged=True)
-    return U.T, L.stats_dict(s)
+    d = L.stats_dict(s)
+    if method == "block":
+        d["rank"] = s.pad_
+    return U.T, d
 
 
 def batch_magnetostatics_linear(meshes, mus, u_ins, rtol=1e-10, maxiter=1_000_000):

@@ -348,12 +348,24 @@ fg_status fg_transport_be(fg_mesh *m, const double *rho_cp, const double *kappa,
 
 /* A sweep of applied fields on one linear mesh (the hysteresis-loop use of
  * Magnetostatics/magneticField.jl:89-132): for field c, K(mu) u_c = 0 on the free
- * rows with u_c = -H0_c . x on the Dirichlet rows of fg_mesh_set_dirichlet, all
- * fields solved together by one multi-right-hand-side Jacobi-PCG that reads the
- * matrix once per iteration for every field (FP32 matrix and inner CG, FP64
- * residual and solution by iterative refinement; o->precision must be FG_MIXED).
- * mu: nt absolute permeabilities; H0: 3 x nfield; U (nv x nfield column-major, may
- * be NULL) receives the potentials.  nfield <= 256; rows of at most 32 entries. */
+ * rows with u_c = -H0_c . x on the Dirichlet rows of fg_mesh_set_dirichlet.
+ * o->spmv selects the method:
+ *   FG_SWEEP_BLOCK (0, default): the residual block of all fields has the rank r <= 3
+ *     of H0 (the problem is linear in the field); its rank-revealing factorisation
+ *     H0 = C V^T (V: r orthonormal field directions) reduces the sweep to one block
+ *     CG of width r (O'Leary, Jacobi-preconditioned, r x r systems by Cholesky with
+ *     dropped dependent directions), and u_c = sum_k C_ck u(v_k).  Any nfield.
+ *   FG_SWEEP_PER_FIELD (1): one multi-right-hand-side Jacobi-PCG with a CG per field
+ *     that reads the matrix once per iteration for every field; nfield <= 256, rows of
+ *     at most 32 entries.
+ * Both: FP32 matrix and inner iterations, FP64 residual and solution by iterative
+ * refinement until every field's residual is below rtol of its initial one
+ * (o->precision must be FG_MIXED).  mu: nt absolute permeabilities; H0: 3 x nfield;
+ * U (nv x nfield column-major, may be NULL) receives the potentials.  s->iterations:
+ * block (or multi-field) iterations summed over the refinements; with FG_SWEEP_BLOCK
+ * s->pad_ is the rank r; s->ms covers the solve and the expansion to all fields. */
+#define FG_SWEEP_BLOCK 0
+#define FG_SWEEP_PER_FIELD 1
 fg_status fg_magnetostatics_sweep(fg_mesh *m, const double *mu, int32_t nfield, const double *H0,
                                   const fg_solve_opts *o, double *U, fg_solve_stats *s);
 
