@@ -347,6 +347,28 @@ def run_ours(args):
         L.check(lib.fg_bench_kernel(g.h, which, L.FG_FP64, reps, C.byref(t)))
         kernels_us[name] = t.value * 1e3
     fg.newton_magnetostatics(mesh, nl, mu_lin, u0, precision="mixed")
+    # P1 stiffness assembly K(mu) at the converged permeabilities into the FP64 and
+    # FP32 operator: the one-pass row gather (7) and the two-pass record form (8)
+    t_asm, t_asm2 = C.c_double(), C.c_double()
+    L.check(lib.fg_bench_kernel(g.h, 7, L.FG_MIXED, 20, C.byref(t_asm)))
+    L.check(lib.fg_bench_kernel(g.h, 8, L.FG_MIXED, 10, C.byref(t_asm2)))
+    nt, nv_ = mesh.nt, mesh.nv
+    # algorithmic bytes by the survey's model: per element connectivity (16 B) and
+    # permeability (8 B), per node the coordinates (24 B), per stored nonzero the FP64
+    # value written (8 B)
+    asm_alg = nt * 24 + nv_ * 24 + g.nnz * 8
+    # bytes this design moves (gradients are not recomputed in FP64): per element the
+    # 10-entry Gram matrix, volume and permeability (96 B), per incidence its element
+    # code and slot bytes (8 B), per stored slot the FP64 and FP32 values (12 B), per
+    # row the two Jacobi inverses (12 B)
+    asm_design = nt * 96 + ninc.value * 8 + nsell.value * 12 + nv_ * 12
+    asm_s = t_asm.value * 1e-3
+    assembly = {"kernel": "k_asm_rows_tet4<ASM_STIFF>", "elements_per_s": nt / asm_s, "us": t_asm.value * 1e3,
+                "alg_bytes": asm_alg, "achieved_GBs": asm_alg / asm_s / 1e9, "peak": peak,
+                "frac": asm_alg / asm_s / 1e9 / peak,
+                "design_bytes": asm_design, "design_GBs": asm_design / asm_s / 1e9,
+                "design_frac": asm_design / asm_s / 1e9 / peak,
+                "two_pass_us": t_asm2.value * 1e3, "speedup_vs_two_pass": t_asm2.value / t_asm.value}
     n = mesh.nv
     v = int(used32.value) - 1
     if v in (16, 20):
@@ -464,7 +486,11 @@ def run_ours(args):
             "accuracy_vs_oracle": acc_oracle,
             "accuracy_vs_fp64_gpu": {"H_rel": herr, "u_rel": uerr, "energy_rel": werr},
             "newton_iters": sm["newton_iters"], "cg_iters": sm["cg_iters"], "trials": sm["trials"],
-            "roofline": roofline, "kernels_us": kernels_us, "autotune": autotune, "cpu_baseline": cpu, "e2e": e2e,
+            "roofline": roofline, "assembly": assembly,
+            "solved_dof_per_s": {"unknowns_per_s": mesh.nv * value,
+                                 "interior_unknown_iterations_per_s":
+                                     int((~mesh.dirichlet_mask().astype(bool)).sum()) * sm["cg_iters"] * value},
+            "kernels_us": kernels_us, "autotune": autotune, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(launches), "cg_variant_fixed": {"mixed": args.cg_variant, "fp64": args.cg64_variant},
             "cg_loop": {"check_every": args.check_every, "graph_mode": args.graph_mode},
             "clocks": res["mixed"]["clocks"], "clocks_fp64": res["fp64"]["clocks"],

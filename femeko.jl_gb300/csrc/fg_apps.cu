@@ -33,7 +33,11 @@ extern "C" fg_status fg_scalar_potential_newton(const double *p, int64_t nv, con
 //   which = 3: one whole CG iteration;
 //   which = 4: Newton residual on the linear/nonlinear split (FP64 SpMV of the
 //              linear elements' operator + the nonlinear elements);
-//   which = 5: the same with the Jacobian.
+//   which = 5: the same with the Jacobian;
+//   which = 7: P1 stiffness assembly K(mu) at the handle's current permeabilities into
+//              the FP64 and FP32 SELL operator with its Jacobi diagonals (one pass,
+//              rows gather their elements' entries);
+//   which = 8: the same through element records and a row sum (the two-pass form).
 fg_status fg_bench_cg_kernel(fg_mesh *m, int which, int precision, int reps, double *ms_per_launch);
 
 extern "C" fg_status fg_bench_kernel(fg_mesh *m, int32_t which, int32_t precision, int32_t reps,
@@ -42,6 +46,24 @@ extern "C" fg_status fg_bench_kernel(fg_mesh *m, int32_t which, int32_t precisio
     FG_REQUIRE(m && ms_per_launch && reps > 0, FG_BAD_ARG, "fg_bench_kernel: bad argument");
     if (which == 0 || which == 1 || which == 3 || which == 6)
       return fg_bench_cg_kernel(m, which, precision, reps, ms_per_launch);
+    if (which == 7 || which == 8) {
+      FG_REQUIRE(m->npe == 4 && !m->edge && m->mu, FG_BAD_ARG,
+                 "fg_bench_kernel: assembly timing needs a P1 tetrahedron handle after a solve");
+      m->asm_two_pass = (which == 8);
+      auto once = [&]() {
+        fg_assemble_operator(m, ASM_STIFF, m->mu, nullptr, nullptr, 0.0, 0.0, 0, OUT_SELL, true, true, true);
+      };
+      once();
+      FG_CUDA_TRY(cudaEventRecord(m->ev0, m->stream));
+      for (int r = 0; r < reps; ++r) once();
+      FG_CUDA_TRY(cudaEventRecord(m->ev1, m->stream));
+      fg_sync(m);
+      m->asm_two_pass = false;
+      float ms = 0.f;
+      FG_CUDA_TRY(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
+      *ms_per_launch = ms / reps;
+      return FG_OK;
+    }
     FG_REQUIRE(which == 2 || which == 4 || which == 5, FG_BAD_ARG, "fg_bench_kernel: unknown kernel");
     FG_REQUIRE(m->v64[7] && m->mu, FG_BAD_ARG, "fg_bench_kernel: run a Newton solve on this handle first");
     FG_REQUIRE(which == 2 || m->nl_maps_valid, FG_BAD_ARG, "fg_bench_kernel: run a Newton solve on this handle first");

@@ -822,6 +822,37 @@ __global__ void k_hfield_tet4(int64_t nt, const double *__restrict__ geo, const 
 }
 
 // ------------------------------------------------------------------ row gather
+// The assembled row of one thread (slot accumulators acc[q * bs]) to the outputs:
+// SELL FP64 / FP32 values, CSR order, and the Jacobi inverse diagonal; a Dirichlet
+// row (bc) becomes an identity row with a zero inverse diagonal.
+template <typename A>
+__device__ __forceinline__ void row_store(int64_t i, int lane, int L, int bs, A *acc, int dk, bool bc, int64_t sb,
+                                          const int *__restrict__ rowptr, double *__restrict__ out64,
+                                          float *__restrict__ out32, double *__restrict__ outcsr,
+                                          double *__restrict__ dinv64, float *__restrict__ dinv32) {
+  if (bc)
+    for (int q = 0; q < L; ++q) acc[q * bs] = (q == dk) ? (A)1 : (A)0;
+  if (out64)
+    for (int q = 0; q < L; q += 2) {
+      int64_t p0 = sell_pos(sb, lane, q);
+      *reinterpret_cast<double2 *>(out64 + p0) = make_double2((double)acc[q * bs], (double)acc[(q + 1) * bs]);
+    }
+  if (out32)
+    for (int q = 0; q < L; q += 4) {
+      int64_t p0 = sell_pos(sb, lane, q);
+      *reinterpret_cast<float4 *>(out32 + p0) = make_float4((float)acc[q * bs], (float)acc[(q + 1) * bs],
+                                                            (float)acc[(q + 2) * bs], (float)acc[(q + 3) * bs]);
+    }
+  if (outcsr) {
+    int rb = rowptr[i], len = rowptr[i + 1] - rb;
+    for (int q = 0; q < len; ++q) outcsr[rb + q] = (double)acc[q * bs];
+  }
+  double d = (double)acc[dk * bs];
+  double di = bc ? 0.0 : (d != 0.0 ? 1.0 / d : 0.0);
+  if (dinv64) dinv64[i] = di;
+  if (dinv32) dinv32[i] = (float)di;
+}
+
 // One thread per row.  Walks the row's incidence records (SELL layout, pads marked
 // 0xFF) and accumulates into a per-thread slot array in shared memory, then writes
 // the row once: SELL (FP64 and/or FP32), or CSR order for export.  Dirichlet rows
@@ -880,29 +911,83 @@ __global__ void k_row_sum(int64_t nv, const int *__restrict__ in_ptr, const int 
   const bool fx = fixed && fixed[i];
   if (vout) vout[i] = (zero_fixed_vec && fx) ? 0.0 : vsign * vacc;
   if (!want_mat) return;
-  int dk = diagk[i];
-  if (apply_bc && fx)
-    for (int q = 0; q < L; ++q) acc[q * bs] = (q == dk) ? (A)1 : (A)0;
-  int64_t sb = sl_ptr[s];
-  if (out64)
-    for (int q = 0; q < L; q += 2) {
-      int64_t p0 = sell_pos(sb, lane, q);
-      *reinterpret_cast<double2 *>(out64 + p0) = make_double2((double)acc[q * bs], (double)acc[(q + 1) * bs]);
+  row_store<A>(i, lane, L, bs, acc, diagk[i], apply_bc && fx, sl_ptr[s], rowptr, out64, out32, outcsr, dinv64, dinv32);
+}
+
+// The element of each incidence position, 4 k + a (element k, local node a), -1 on
+// pads: the inverse of recpos, built once per handle.
+__global__ void k_inc_elem(int64_t nt, const int *__restrict__ recpos, int *__restrict__ in_elem) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // e = a nt + k
+  if (e >= 4 * nt) return;
+  const int a = (int)(e / nt);
+  const int64_t k = e - (int64_t)a * nt;
+  in_elem[recpos[e]] = (int)(4 * k + a);
+}
+
+// Positions of G_ab (b = 0..3) in the stored upper triangle of the element Gram matrix.
+__constant__ int c_gram_row[4][4] = {{0, 1, 2, 3}, {1, 4, 5, 6}, {2, 5, 7, 8}, {3, 6, 8, 9}};
+
+// P1 tetrahedra, one pass without element records: one thread per row walks the
+// row's incidences (element k, local node a) in the order the two-pass form sums
+// its records, and adds each element entry Ke[a][b] straight from the stored
+// geometry into the row's slot accumulators (FP64 fused multiply-adds, fixed order,
+// no atomics):
+//   ASM_STIFF  f_k VE_k G_k[a][b]                       (src/FEM3D.jl:59-76)
+//   ASM_MASS   f_k VE_k / 20 (1 + delta_ab)              (src/FEM3D.jl:466-492)
+//   ASM_HEAT   cm VE_k / 20 (1 + delta_ab) + cs f_k VE_k G_k[a][b]
+// G_k = grad phi_a . grad phi_b is the Gram matrix kept with the element geometry.
+// Each element's data is read by its four rows; they run at nearly the same time,
+// so the repeats are served from L2.
+template <int KIND>
+__global__ void __launch_bounds__(128) k_asm_rows_tet4(int64_t nv, int64_t nt, const int *__restrict__ in_ptr,
+                                                       const int *__restrict__ in_len,
+                                                       const uint8_t *__restrict__ in_slot,
+                                                       const int *__restrict__ in_elem, const double *__restrict__ geo,
+                                                       const double *__restrict__ f, double cm, double cs,
+                                                       const int *__restrict__ sl_ptr, const int *__restrict__ sl_len,
+                                                       const int *__restrict__ rowptr, const uint8_t *__restrict__ diagk,
+                                                       const uint8_t *__restrict__ fixed, int apply_bc,
+                                                       double *__restrict__ out64, float *__restrict__ out32,
+                                                       double *__restrict__ outcsr, double *__restrict__ dinv64,
+                                                       float *__restrict__ dinv32) {
+  extern __shared__ unsigned char smem_raw[];
+  double *acc = reinterpret_cast<double *>(smem_raw) + threadIdx.x;
+  const int bs = blockDim.x;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nv) return;
+  const int s = (int)(i / FG_SLICE), lane = (int)(i % FG_SLICE);
+  const int L = FG_GROUP * sl_len[s];
+  for (int q = 0; q < L; ++q) acc[q * bs] = 0.0;
+  const int64_t base = in_ptr[s] + lane;
+  const int ilen = in_len[s];
+  const double *VE = geo + 12 * nt;
+  for (int mm = 0; mm < ilen; ++mm) {
+    const int64_t pos = base + (int64_t)mm * FG_SLICE;
+    const int code = in_elem[pos];
+    if (code < 0) continue;  // pad
+    const uint32_t w = reinterpret_cast<const uint32_t *>(in_slot)[pos];
+    const int64_t k = code >> 2;
+    const int a = code & 3;
+    const double fk = f ? f[k] : 1.0;
+    const double ve = VE[k];
+    const int sl[4] = {(int)(w & 0xFF), (int)((w >> 8) & 0xFF), (int)((w >> 16) & 0xFF), (int)(w >> 24)};
+    if (KIND == ASM_STIFF || KIND == ASM_HEAT) {
+      const double sk = (KIND == ASM_STIFF ? fk : cs * fk) * ve;
+      double g[4];
+#pragma unroll
+      for (int b = 0; b < 4; ++b) g[b] = geo[(int64_t)(13 + c_gram_row[a][b]) * nt + k];
+#pragma unroll
+      for (int b = 0; b < 4; ++b) acc[sl[b] * bs] = fma(sk, g[b], acc[sl[b] * bs]);
     }
-  if (out32)
-    for (int q = 0; q < L; q += 4) {
-      int64_t p0 = sell_pos(sb, lane, q);
-      *reinterpret_cast<float4 *>(out32 + p0) = make_float4((float)acc[q * bs], (float)acc[(q + 1) * bs],
-                                                            (float)acc[(q + 2) * bs], (float)acc[(q + 3) * bs]);
+    if (KIND == ASM_MASS || KIND == ASM_HEAT) {
+      const double mk = (KIND == ASM_MASS ? fk : cm) * ve / 20.0;
+#pragma unroll
+      for (int b = 0; b < 4; ++b) acc[sl[b] * bs] += (b == a) ? 2.0 * mk : mk;
     }
-  if (outcsr) {
-    int rb = rowptr[i], len = rowptr[i + 1] - rb;
-    for (int q = 0; q < len; ++q) outcsr[rb + q] = (double)acc[q * bs];
   }
-  double d = (double)acc[dk * bs];
-  double di = (apply_bc && fx) ? 0.0 : (d != 0.0 ? 1.0 / d : 0.0);
-  if (dinv64) dinv64[i] = di;
-  if (dinv32) dinv32[i] = (float)di;
+  const bool fx = fixed && fixed[i];
+  row_store<double>(i, lane, L, bs, acc, diagk[i], apply_bc && fx, sl_ptr[s], rowptr, out64, out32, outcsr, dinv64,
+                    dinv32);
 }
 
 // ------------------------------------------------------------------ host side
@@ -984,10 +1069,46 @@ static void launch_elem(fg_mesh *m, int kind, const double *d_f, const double *d
   FG_LAUNCHED(1);
 }
 
+// One-pass P1-tetrahedron assembly (k_asm_rows_tet4) of stiffness, mass or heat.
+static void launch_rows_tet4(fg_mesh *m, int kind, const double *d_f, double cm, double cs, int apply_bc,
+                             double *out64, float *out32, double *outcsr, double *dinv64, float *dinv32) {
+  if (!m->in_elem) {
+    m->in_elem = dev_alloc<int>(m, (size_t)m->ninc);
+    FG_CUDA_TRY(cudaMemsetAsync(m->in_elem, 0xFF, sizeof(int) * (size_t)m->ninc, m->stream));
+    k_inc_elem<<<grid_for(4 * m->nt, 256), 256, 0, m->stream>>>(m->nt, m->recpos, m->in_elem);
+    FG_CUDA_TRY(cudaGetLastError());
+    FG_LAUNCHED(1);
+  }
+  const int L = std::max(m->maxrow4, FG_GROUP);
+  const int block = 128;
+  const size_t smem = (size_t)block * L * sizeof(double);
+  auto go = [&](auto kern) {
+    if (smem > 48 * 1024) FG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<grid_for(m->nv, block), block, smem, m->stream>>>(
+        m->nv, m->nt, m->in_ptr, m->in_len, m->in_slot, m->in_elem, m->geo, d_f, cm, cs, m->sl_ptr, m->sl_len,
+        m->rowptr, m->diagk, m->has_fixed ? m->fixed : nullptr, apply_bc, out64, out32, outcsr, dinv64, dinv32);
+  };
+  if (kind == ASM_STIFF) go(k_asm_rows_tet4<ASM_STIFF>);
+  else if (kind == ASM_MASS) go(k_asm_rows_tet4<ASM_MASS>);
+  else go(k_asm_rows_tet4<ASM_HEAT>);
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(1);
+}
+
 void fg_assemble_operator(fg_mesh *m, int kind, const double *d_f, const double *d_H, const double *d_dmu,
                           double c_mass, double c_stiff, int full_phi, int layout, bool want64, bool want32,
                           bool apply_bc) {
   if (layout != OUT_CSR) { m->op_tag = 0; ++m->op_version; }
+  if (m->npe == 4 && !m->edge && !m->asm_two_pass && (kind == ASM_STIFF || kind == ASM_MASS || kind == ASM_HEAT)) {
+    if (layout != OUT_CSR) ensure_operator(m, want64, want32);
+    else if (!m->csrval) m->csrval = dev_alloc<double>(m, (size_t)m->nnz);
+    launch_rows_tet4(m, kind, d_f, c_mass, c_stiff, layout == OUT_CSR ? 0 : (apply_bc ? 1 : 0),
+                     layout == OUT_CSR ? nullptr : (want64 ? m->val64 : nullptr),
+                     layout == OUT_CSR ? nullptr : (want32 ? m->val32 : nullptr),
+                     layout == OUT_CSR ? m->csrval : nullptr, layout == OUT_CSR ? nullptr : m->dinv64,
+                     layout == OUT_CSR ? nullptr : m->dinv32);
+    return;
+  }
   // convection: the 3D records are the rows of the reference's C^T, the 2D records
   // the rows of its C (see the element kernels); transpose to what the layout needs
   const bool tr = kind == ASM_CONV && ((m->npe == 10) == (layout != OUT_CSR));

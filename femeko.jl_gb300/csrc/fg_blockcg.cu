@@ -6,9 +6,9 @@
 // field c is R0_c = -K(-H0_c . x) = sum_k H0_c,k R0(e_k), so the residual block
 // [R0_1 .. R0_m] = [R0(e_x) R0(e_y) R0(e_z)] H0^T has rank r <= 3, the rank of H0.
 // A rank-revealing factorisation of the block is therefore that of H0 (m x 3, on
-// the host: eigen-decomposition of H0^T H0, directions whose singular value is below
-// 1e-13 of the largest dropped): H0 = C V^T with V (3 x r) orthonormal field
-// directions and C = H0 V (m x r).  One block CG of width r solves the r direction
+// the host: one-sided Jacobi SVD, directions whose singular value is below 1e-13 of
+// the largest dropped): H0 = C V^T with V (3 x r) orthonormal field directions and
+// C = H0 V (m x r).  One block CG of width r solves the r direction
 // problems together, and every field's potential is the combination
 // u_c = sum_k C_c,k u(v_k) (exact: the problem is linear in H0).
 //
@@ -424,38 +424,50 @@ __global__ void k_bc_expand(int64_t n, int nfield, const double *__restrict__ C,
   U[e] = fma(cc[0], a.x, fma(cc[1], a.y, fma(cc[2], b.x, cc[3] * b.y)));
 }
 
-// Eigen-decomposition of a symmetric 3 x 3 (cyclic Jacobi rotations): A = V diag(w) V^T.
-void sym3_eigen(double A[3][3], double w[3], double V[3][3]) {
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) V[i][j] = i == j ? 1.0 : 0.0;
-  for (int sweep = 0; sweep < 64; ++sweep) {
-    const double off = A[0][1] * A[0][1] + A[0][2] * A[0][2] + A[1][2] * A[1][2];
-    const double dia = A[0][0] * A[0][0] + A[1][1] * A[1][1] + A[2][2] * A[2][2];
-    if (off <= 1e-36 * dia || off == 0.0) break;
+// Singular value decomposition of the field block H0 (m x 3, row c = field c) by
+// one-sided Jacobi rotations (Hestenes): the three columns are rotated pairwise until
+// orthogonal, H0 V = W (columns of W orthogonal), so the singular values are the
+// column norms of W and C = W.  Unlike an eigen-decomposition of H0^T H0 this keeps
+// small singular values accurate to working precision relative to the largest, so a
+// threshold of 1e-13 separates exact rank deficiency from rounding.
+void fields_svd(const double *H0, int m, std::vector<double> &W, double V[3][3], double sig[3]) {
+  W.assign(H0, H0 + 3 * (size_t)m);  // W[3 c + a]
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) V[a][b] = a == b ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    bool rotated = false;
     for (int p = 0; p < 2; ++p)
       for (int q = p + 1; q < 3; ++q) {
-        if (A[p][q] == 0.0) continue;
-        const double th = (A[q][q] - A[p][p]) / (2.0 * A[p][q]);
+        double app = 0.0, aqq = 0.0, apq = 0.0;
+        for (int c = 0; c < m; ++c) {
+          const double x = W[3 * c + p], y = W[3 * c + q];
+          app += x * x;
+          aqq += y * y;
+          apq += x * y;
+        }
+        if (apq == 0.0 || std::fabs(apq) <= 1e-15 * std::sqrt(app * aqq)) continue;
+        rotated = true;
+        const double th = (aqq - app) / (2.0 * apq);
         const double t = (th >= 0.0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
-        const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
-        for (int k = 0; k < 3; ++k) {
-          const double akp = A[k][p], akq = A[k][q];
-          A[k][p] = c * akp - s * akq;
-          A[k][q] = s * akp + c * akq;
+        const double cs = 1.0 / std::sqrt(t * t + 1.0), sn = t * cs;
+        for (int c = 0; c < m; ++c) {
+          const double x = W[3 * c + p], y = W[3 * c + q];
+          W[3 * c + p] = cs * x - sn * y;
+          W[3 * c + q] = sn * x + cs * y;
         }
         for (int k = 0; k < 3; ++k) {
-          const double apk = A[p][k], aqk = A[q][k];
-          A[p][k] = c * apk - s * aqk;
-          A[q][k] = s * apk + c * aqk;
-        }
-        for (int k = 0; k < 3; ++k) {
-          const double vkp = V[k][p], vkq = V[k][q];
-          V[k][p] = c * vkp - s * vkq;
-          V[k][q] = s * vkp + c * vkq;
+          const double x = V[k][p], y = V[k][q];
+          V[k][p] = cs * x - sn * y;
+          V[k][q] = sn * x + cs * y;
         }
       }
+    if (!rotated) break;
   }
-  for (int i = 0; i < 3; ++i) w[i] = A[i][i];
+  for (int a = 0; a < 3; ++a) {
+    double s2 = 0.0;
+    for (int c = 0; c < m; ++c) s2 += W[3 * c + a] * W[3 * c + a];
+    sig[a] = std::sqrt(s2);
+  }
 }
 
 }  // namespace
@@ -465,29 +477,23 @@ fg_status fg_sweep_block(fg_mesh *m, int nfield, const double *H0, const fg_solv
                          fg_solve_stats *s) {
   const int64_t n = m->nv;
   cudaStream_t st = m->stream;
-  // rank-revealing factorisation of the field block: H0^T H0 = V diag(w) V^T
-  double G3[3][3] = {{0.0}};
-  for (int c = 0; c < nfield; ++c)
-    for (int a = 0; a < 3; ++a)
-      for (int b = 0; b < 3; ++b) G3[a][b] += H0[3 * c + a] * H0[3 * c + b];
-  double w[3], V[3][3];
-  sym3_eigen(G3, w, V);
+  // rank-revealing factorisation of the field block: H0 V = W, W's columns orthogonal
+  std::vector<double> W;
+  double V[3][3], sig[3];
+  fields_svd(H0, nfield, W, V, sig);
   int order[3] = {0, 1, 2};
-  std::sort(order, order + 3, [&](int a, int b) { return w[a] > w[b]; });
-  const double wmax = std::max(w[order[0]], 0.0);
+  std::sort(order, order + 3, [&](int a, int b) { return sig[a] > sig[b]; });
+  const double smax = sig[order[0]];
   int r = 0;
   Dirs dirs{};
+  std::vector<double> Cm((size_t)4 * nfield, 0.0);  // C = H0 V_r (nfield x 4, zero beyond r)
   for (int k = 0; k < 3; ++k) {
     const int e = order[k];
-    if (!(w[e] > 1e-26 * wmax) || wmax == 0.0) continue;  // singular value below 1e-13 of the largest
+    if (!(smax > 0.0) || !(sig[e] > 1e-13 * smax)) continue;  // singular value below 1e-13 of the largest
     for (int a = 0; a < 3; ++a) dirs.v[r][a] = V[a][e];
+    for (int c = 0; c < nfield; ++c) Cm[4 * c + r] = W[3 * c + e];
     ++r;
   }
-  // C = H0 V_r (nfield x 4, zero beyond r)
-  std::vector<double> Cm((size_t)4 * nfield, 0.0);
-  for (int c = 0; c < nfield; ++c)
-    for (int k = 0; k < r; ++k)
-      Cm[4 * c + k] = H0[3 * c] * dirs.v[k][0] + H0[3 * c + 1] * dirs.v[k][1] + H0[3 * c + 2] * dirs.v[k][2];
 
   std::vector<void *> tmp;
   auto alloc = [&](size_t bytes) {
@@ -542,6 +548,7 @@ fg_status fg_sweep_block(fg_mesh *m, int nfield, const double *H0, const fg_solv
     return std::max(v, 0.0);
   };
   double G[16], G0[16];
+  std::vector<double> hist;
   int total = 0, refinements = 0;
   bool all_done = false;
   double worst = 0.0;
@@ -567,6 +574,10 @@ fg_status fg_sweep_block(fg_mesh *m, int nfield, const double *H0, const fg_solv
       }
     }
     if (all_done || total >= o.maxiter) break;
+    // stagnation (a residual at the rounding level of the FP64 operator cannot be
+    // reduced further): stop when three refinements did not halve the worst field
+    hist.push_back(worst);
+    if (hist.size() >= 4 && worst > 0.5 * hist[hist.size() - 4]) break;
     double sc[4] = {0.0, 0.0, 0.0, 0.0};
     for (int k = 0; k < r; ++k)
       if (G[5 * k] > 0.0) sc[k] = 1.0 / std::sqrt(G[5 * k]);

@@ -175,6 +175,8 @@ struct fg_mesh {
   int64_t ninc = 0;          // padded count
   uint8_t *in_slot = nullptr;// ninc * npe slot positions (0xFF on pads)
   int *recpos = nullptr;     // nt * npe (SoA: [a*nt + k]) -> incidence position
+  int *in_elem = nullptr;    // ninc: 4 k + a of each incidence position, -1 on pads (P1 tetrahedra)
+  bool asm_two_pass = false; // P1 stiffness/mass/heat through element records + row sum (timing comparison)
   int maxdeg = 0;
 
   // records written by the element kernels, summed by the row kernel
