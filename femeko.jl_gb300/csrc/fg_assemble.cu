@@ -924,9 +924,6 @@ __global__ void k_inc_elem(int64_t nt, const int *__restrict__ recpos, int *__re
   in_elem[recpos[e]] = (int)(4 * k + a);
 }
 
-// Positions of G_ab (b = 0..3) in the stored upper triangle of the element Gram matrix.
-__constant__ int c_gram_row[4][4] = {{0, 1, 2, 3}, {1, 4, 5, 6}, {2, 5, 7, 8}, {3, 6, 8, 9}};
-
 // P1 tetrahedra, one pass without element records: one thread per row walks the
 // row's incidences (element k, local node a) in the order the two-pass form sums
 // its records, and adds each element entry Ke[a][b] straight from the stored
@@ -961,28 +958,56 @@ __global__ void __launch_bounds__(128) k_asm_rows_tet4(int64_t nv, int64_t nt, c
   const int64_t base = in_ptr[s] + lane;
   const int ilen = in_len[s];
   const double *VE = geo + 12 * nt;
-  for (int mm = 0; mm < ilen; ++mm) {
-    const int64_t pos = base + (int64_t)mm * FG_SLICE;
-    const int code = in_elem[pos];
-    if (code < 0) continue;  // pad
-    const uint32_t w = reinterpret_cast<const uint32_t *>(in_slot)[pos];
-    const int64_t k = code >> 2;
-    const int a = code & 3;
-    const double fk = f ? f[k] : 1.0;
-    const double ve = VE[k];
-    const int sl[4] = {(int)(w & 0xFF), (int)((w >> 8) & 0xFF), (int)((w >> 16) & 0xFF), (int)(w >> 24)};
-    if (KIND == ASM_STIFF || KIND == ASM_HEAT) {
-      const double sk = (KIND == ASM_STIFF ? fk : cs * fk) * ve;
-      double g[4];
+  const uint32_t *slot4 = reinterpret_cast<const uint32_t *>(in_slot);
+  // four incidences at a time: their element codes and slot bytes, then all their
+  // element data, are loaded before any of it is used, so that a thread keeps some
+  // twenty independent loads in flight instead of two dependent ones
+  constexpr int U = 4;
+  for (int m0 = 0; m0 < ilen; m0 += U) {
+    int code[U];
+    uint32_t w[U];
 #pragma unroll
-      for (int b = 0; b < 4; ++b) g[b] = geo[(int64_t)(13 + c_gram_row[a][b]) * nt + k];
-#pragma unroll
-      for (int b = 0; b < 4; ++b) acc[sl[b] * bs] = fma(sk, g[b], acc[sl[b] * bs]);
+    for (int j = 0; j < U; ++j) {
+      const int64_t pos = base + (int64_t)(m0 + j) * FG_SLICE;
+      code[j] = (m0 + j < ilen) ? in_elem[pos] : -1;
+      w[j] = (m0 + j < ilen) ? slot4[pos] : 0u;
     }
-    if (KIND == ASM_MASS || KIND == ASM_HEAT) {
-      const double mk = (KIND == ASM_MASS ? fk : cm) * ve / 20.0;
+    double sk[U], mk[U], g[U][4];
+    int aj[U];
 #pragma unroll
-      for (int b = 0; b < 4; ++b) acc[sl[b] * bs] += (b == a) ? 2.0 * mk : mk;
+    for (int j = 0; j < U; ++j) {
+      sk[j] = 0.0;
+      mk[j] = 0.0;
+      aj[j] = code[j] & 3;
+#pragma unroll
+      for (int b = 0; b < 4; ++b) g[j][b] = 0.0;
+      if (code[j] < 0) continue;  // pad
+      const int64_t k = code[j] >> 2;
+      const int a = aj[j];
+      const double fk = f ? f[k] : 1.0;
+      const double ve = VE[k];
+      if (KIND == ASM_STIFF || KIND == ASM_HEAT) {
+        sk[j] = (KIND == ASM_STIFF ? fk : cs * fk) * ve;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          // position of G_ab in the stored upper triangle: lo (9 - lo) / 2 + hi - lo
+          const int lo = a < b ? a : b, hi = a < b ? b : a;
+          g[j][b] = geo[(int64_t)(13 + (lo * (9 - lo)) / 2 + hi - lo) * nt + k];
+        }
+      }
+      if (KIND == ASM_MASS || KIND == ASM_HEAT) mk[j] = (KIND == ASM_MASS ? fk : cm) * ve / 20.0;
+    }
+#pragma unroll
+    for (int j = 0; j < U; ++j) {
+      if (code[j] < 0) continue;
+      const int sl[4] = {(int)(w[j] & 0xFF), (int)((w[j] >> 8) & 0xFF), (int)((w[j] >> 16) & 0xFF), (int)(w[j] >> 24)};
+#pragma unroll
+      for (int b = 0; b < 4; ++b) {
+        double v = acc[sl[b] * bs];
+        if (KIND == ASM_MASS || KIND == ASM_HEAT) v += (b == aj[j]) ? 2.0 * mk[j] : mk[j];
+        if (KIND == ASM_STIFF || KIND == ASM_HEAT) v = fma(sk[j], g[j][b], v);
+        acc[sl[b] * bs] = v;
+      }
     }
   }
   const bool fx = fixed && fixed[i];

@@ -1904,6 +1904,11 @@ static int inner_solve(fg_mesh *m, bool mixed, const double *r64, double rn, dou
     } else if (!m->tuned32 && !tune_cache_get(m, true)) {
       fg_autotune_spmv32(m, 20, nullptr, nullptr);
       tune_cache_put(m, true);
+    } else if (!variant32_available(m, m->spmv_variant32)) {
+      // a variant remembered from another handle of this operator shape that this
+      // handle cannot run as it is (its halo lists or pipeline grid not built, the
+      // stages too large): time the variants on this handle instead
+      fg_autotune_spmv32(m, 20, nullptr, nullptr);
     }
     if (v_window(m->spmv_variant32) && !prepare_l2(m)) {
       // no persisting L2 after all: the same variant without the window
@@ -1921,6 +1926,8 @@ static int inner_solve(fg_mesh *m, bool mixed, const double *r64, double rn, dou
     if (!m->tuned64 && !tune_cache_get(m, false)) {
       fg_autotune_spmv64(m, 20, nullptr, nullptr);
       tune_cache_put(m, false);
+    } else if (m->spmv_variant64 == 1 && !fg_ensure_halo(m)) {
+      m->spmv_variant64 = 0;  // the halo-staged SpMV needs this handle's halo lists
     }
     start_cg(m, false, r64, 1.0 / rn, inner * inner, maxit);
     its = run_cg(m, false, o, ist);
