@@ -92,8 +92,9 @@ enum {
 };
 // CG control words; I_FAULT is set by a kernel whose asynchronous copy did not
 // complete within its bounded wait (the solve stops and reports an error); I_BODIES
-// counts the bodies run by a whole-solve loop graph.
-enum { I_DONE = 0, I_ITERS, I_MAXIT, I_STATUS, I_FAULT, I_BODIES, I_NINT = 8 };
+// counts the bodies run by a whole-solve loop graph; I_PIPE_FIRST marks the first
+// reduction of a pipelined FP32 CG run (it turns the relative tolerance absolute).
+enum { I_DONE = 0, I_ITERS, I_MAXIT, I_STATUS, I_FAULT, I_BODIES, I_PIPE_FIRST, I_NINT = 8 };
 
 // Reduction workspace: per-block partials and an arrival counter for the
 // "last block finishes the sum" pattern (the sum runs in block order, so results
@@ -159,6 +160,7 @@ struct fg_mesh {
   int tmax = 0;       // most matrix entries (padded slots) of one row block
   int tmax256 = 0;    // most matrix entries (padded slots) of one 256-row block
   int bulk_fit = -1;  // resident CTAs per SM of the bulk-staged SpMV (-1: not sized yet)
+  int pipe_fit = -1;  // the same for the pipelined CG's SpMV
   int pipe_grid = 0;  // CTAs of the persistent pipelined iteration (0: not sized yet, -1: does not fit)
   int *halo_col = nullptr, *halo_len = nullptr;
   bool halo_tried = false;   // the halo lists are built at the first variant that needs them
@@ -220,6 +222,7 @@ struct fg_mesh {
   cudaGraphExec_t bcg_exec = nullptr;
   bool bcg_dcol = false;
   float *v32[8] = {nullptr};
+  float *pv32[3] = {nullptr};  // pipelined FP32 CG: z, n = A m, m = D w
 
   // reductions and CG control
   RedWs red{};

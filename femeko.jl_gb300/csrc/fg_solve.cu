@@ -748,6 +748,245 @@ __global__ void __launch_bounds__(256) k_cg32s_spmv_bulk(int64_t n, int nslices,
   if (finish_dots32(dots, partials, counter, tot) && ok) cgcg_scalars(tot, scal, ictl);
 }
 
+// ------------------------------------------------------------------ FP32 pipelined CG
+// Pipelined Jacobi-PCG (Ghysels and Vanroose, "Hiding global synchronization latency
+// in the preconditioned Conjugate Gradient algorithm", Parallel Computing 40, 2014):
+// the dot products of iteration i are formed by the vector pass of iteration i - 1,
+// and their grid-wide sum is finished by one extra block of the SpMV of iteration i
+// while the other blocks compute n = A m, so no block waits for a reduction tail.
+// With M = D^-1 the preconditioned vectors u = D r and q = D s need no storage:
+//   gamma = r.Dr, delta = w.Dr, |r|^2          (partials of the previous vector pass)
+//   n = A m                                    (SpMV; its extra block finishes the dots:
+//   beta = gamma / gamma_old, alpha = gamma / (delta - beta gamma / alpha_old))
+//   z = n + beta z, s = w + beta s, p = Dr + beta p,
+//   x += alpha p, r -= alpha s, w -= alpha z, m = D w     (vector pass)
+// in exact arithmetic w = A D r, s = A p, z = A D s.  Start: r = r0, m = D r, w = A m
+// (plain SpMV), then one vector pass with alpha = beta = 0 gives m = D w and the
+// first dots.  Stopping test on the recursive |r|^2, as the other variants.
+
+// r = scale * rin (FP32), m = D r, x = s = p = z = n = 0; scalars and control words.
+__global__ void k_pcg32_init(int64_t n, int64_t np, const double *__restrict__ rin, double scale,
+                             const float *__restrict__ dinv, float *__restrict__ r, float *__restrict__ m,
+                             float *__restrict__ x, float *__restrict__ s, float *__restrict__ p,
+                             float *__restrict__ z, float *__restrict__ nv, double tol2_rel, int maxit, double *scal,
+                             int *ictl) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < np; i += stride) {
+    const float ri = (i < n) ? (float)(scale * rin[i]) : 0.f;
+    r[i] = ri;
+    m[i] = dinv[i] * ri;
+    x[i] = 0.f;
+    s[i] = 0.f;
+    p[i] = 0.f;
+    z[i] = 0.f;
+    nv[i] = 0.f;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    scal[S_TOL2] = tol2_rel;
+    scal[S_ALPHA] = 0.0;
+    scal[S_BETA] = 0.0;
+    scal[S_RZ] = 0.0;
+    ictl[I_ITERS] = 0;
+    ictl[I_MAXIT] = maxit;
+    ictl[I_STATUS] = 0;
+    ictl[I_FAULT] = 0;
+    ictl[I_DONE] = 0;
+    ictl[I_BODIES] = 0;
+    ictl[I_PIPE_FIRST] = 1;
+  }
+}
+
+// Scalars of one pipelined iteration from gamma, delta and |r|^2 (one thread).
+__device__ __forceinline__ void pcg_scalars(const double (&tot)[3], double *scal, int *ictl) {
+  const double gam = tot[0], del = tot[1], rr = tot[2];
+  const int it = ictl[I_ITERS];
+  if (ictl[I_PIPE_FIRST]) {
+    scal[S_TOL2] = scal[S_TOL2] * rr;  // relative threshold -> absolute, from r0.r0
+    ictl[I_PIPE_FIRST] = 0;
+  }
+  scal[S_RR] = rr;
+  int st = -1;
+  if (!isfinite(rr) || !isfinite(gam) || !isfinite(del)) st = 2;
+  else if (rr == 0.0 || rr <= scal[S_TOL2]) st = 0;
+  else if (it >= ictl[I_MAXIT]) st = 1;
+  if (st >= 0) {
+    ictl[I_STATUS] = st;
+    ictl[I_DONE] = 1;
+    return;
+  }
+  double alpha, beta = 0.0;
+  if (it == 0) {
+    alpha = (del != 0.0) ? gam / del : 0.0;
+  } else {
+    const double gold = scal[S_RZ], aold = scal[S_ALPHA];
+    beta = (gold != 0.0) ? gam / gold : 0.0;
+    const double den = del - beta * gam / aold;
+    alpha = (den != 0.0) ? gam / den : 0.0;
+  }
+  scal[S_RZ] = gam;
+  scal[S_ALPHA] = alpha;
+  scal[S_BETA] = beta;
+  ictl[I_ITERS] = it + 1;
+}
+
+// Vector pass of the pipelined iteration, four rows per thread; each block leaves its
+// compensated partial sums of gamma, delta and |r|^2 in partials[block][3].
+__global__ void __launch_bounds__(256) k_pcg32_vec(int64_t n4, float4 *__restrict__ x, float4 *__restrict__ r,
+                                                   float4 *__restrict__ w, float4 *__restrict__ s,
+                                                   float4 *__restrict__ p, float4 *__restrict__ z,
+                                                   const float4 *__restrict__ nv, float4 *__restrict__ m,
+                                                   const float4 *__restrict__ dinv, const double *scal,
+                                                   const int *ictl, float2 *__restrict__ partials) {
+  if (ictl[I_DONE]) return;
+  const float alpha = (float)scal[S_ALPHA], beta = (float)scal[S_BETA];
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  ff acc[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+  if (j < n4) {
+    const float4 nn = nv[j], dd = dinv[j];
+    float4 zz = z[j], ww = w[j], ss = s[j], rr = r[j], pp = p[j], xx = x[j];
+    float4 mm;
+#define FG_PCG_LANE(c)                                \
+  {                                                   \
+    zz.c = fmaf(beta, zz.c, nn.c);                    \
+    ss.c = fmaf(beta, ss.c, ww.c);                    \
+    pp.c = fmaf(beta, pp.c, dd.c * rr.c);             \
+    xx.c = fmaf(alpha, pp.c, xx.c);                   \
+    rr.c = fmaf(-alpha, ss.c, rr.c);                  \
+    ww.c = fmaf(-alpha, zz.c, ww.c);                  \
+    mm.c = dd.c * ww.c;                               \
+    const float uc = dd.c * rr.c;                     \
+    acc[0] = ff_add(acc[0], ff{rr.c * uc, 0.f});      \
+    acc[1] = ff_add(acc[1], ff{ww.c * uc, 0.f});      \
+    acc[2] = ff_add(acc[2], ff{rr.c * rr.c, 0.f});    \
+  }
+    FG_PCG_LANE(x) FG_PCG_LANE(y) FG_PCG_LANE(z) FG_PCG_LANE(w)
+#undef FG_PCG_LANE
+    z[j] = zz;
+    s[j] = ss;
+    p[j] = pp;
+    x[j] = xx;
+    r[j] = rr;
+    w[j] = ww;
+    m[j] = mm;
+  }
+  __shared__ ff shb[3][32];
+  block_sum_ff_pair<3>(acc, shb);
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 3; ++k) partials[(size_t)blockIdx.x * 3 + k] = make_float2(acc[k].hi, acc[k].lo);
+}
+
+// out = A in with the matrix entries staged by bulk copies (as k_cg32s_spmv_bulk, no
+// dot products).  With nparts > 0, block 0 does no SpMV work: it sums the nparts
+// partials of the last vector pass in index order and sets the iteration's scalars,
+// while blocks 1.. walk the 256-row blocks.
+template <class CI>
+__global__ void __launch_bounds__(256) k_pcg32_spmv_bulk(int64_t n, int nslices, int cap,
+                                                         const int *__restrict__ sl_ptr,
+                                                         const int *__restrict__ sl_len,
+                                                         const typename CI::T *__restrict__ col,
+                                                         const float *__restrict__ val, const float *__restrict__ in,
+                                                         float *__restrict__ out, double *scal, int *ictl,
+                                                         const float2 *__restrict__ partials, int nparts) {
+  using T = typename CI::T;
+  using T4 = typename CI::T4;
+  extern __shared__ __align__(128) unsigned char sm_bulk[];
+  __shared__ __align__(8) uint64_t bar[2];
+  if (ictl[I_DONE]) return;
+  const int tid = threadIdx.x;
+  if (nparts > 0 && blockIdx.x == 0) {
+    ff acc[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    for (int k = tid; k < nparts; k += 256)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const float2 q = __ldcg(partials + (size_t)k * 3 + j);
+        acc[j] = ff_add(acc[j], ff{q.x, q.y});
+      }
+    __shared__ ff shr[3][32];
+    block_sum_ff_pair<3>(acc, shr);
+    if (tid == 0) {
+      double tot[3];
+      for (int j = 0; j < 3; ++j) tot[j] = (double)acc[j].hi + (double)acc[j].lo;
+      pcg_scalars(tot, scal, ictl);
+    }
+    return;
+  }
+  const int off = nparts > 0 ? 1 : 0;
+  const int nb = (int)gridDim.x - off, b = (int)blockIdx.x - off;
+  const size_t o_col = pipe_align((size_t)cap * 4);
+  const size_t stage = o_col + pipe_align((size_t)cap * sizeof(T));
+  const int64_t nrb = (n + 255) / 256;
+  const int K = (int)((nrb - (int64_t)b + nb - 1) / nb);
+  auto rowblock = [&](int k) { return (int64_t)b + (int64_t)k * nb; };
+  auto issue = [&](int k, int st) {
+    const int s0 = (int)(rowblock(k) * (256 / FG_SLICE)), s1 = min(s0 + 256 / FG_SLICE, nslices);
+    const int e0 = sl_ptr[s0], e1 = sl_ptr[s1];
+    const uint32_t vb = (uint32_t)(e1 - e0) * 4u, cb = (uint32_t)(e1 - e0) * (uint32_t)sizeof(T);
+    fence_proxy_async_smem();
+    mbar_arrive_expect_tx(&bar[st], vb + cb);
+    bulk_g2s(sm_bulk + st * stage, val + e0, vb, &bar[st]);
+    bulk_g2s(sm_bulk + st * stage + o_col, col + e0, cb, &bar[st]);
+  };
+  uint32_t inflight = 0u;
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_proxy_async_smem();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    if (K > 0) issue(0, 0);
+    if (K > 1) issue(1, 1);
+  }
+  inflight = (K > 1) ? 3u : (K > 0 ? 1u : 0u);
+  uint32_t phase = 0u;
+  bool ok = true;
+  for (int k = 0; k < K; ++k) {
+    const int st = k & 1;
+    const int64_t rb = rowblock(k);
+    const int64_t i = rb * 256 + tid;
+    const bool row = i < n;
+    int G = 0, base = 0;
+    if (row) {
+      const int sl = (int)(i >> 5);
+      G = sl_len[sl];
+      base = sl_ptr[sl] - sl_ptr[rb * (256 / FG_SLICE)] + (tid & 31) * FG_GROUP;
+    }
+    const bool got = mbar_wait(&bar[st], (phase >> st) & 1u);
+    if (got) {
+      phase ^= 1u << st;
+      inflight &= ~(1u << st);
+    }
+    if (__syncthreads_or(!got)) { ok = false; break; }
+    if (row) {
+      const float *v = reinterpret_cast<const float *>(sm_bulk + st * stage);
+      const T *c = reinterpret_cast<const T *>(sm_bulk + st * stage + o_col);
+      float acc = 0.f;
+#pragma unroll 4
+      for (int g = 0; g < G; ++g) {
+        const float4 vv = *reinterpret_cast<const float4 *>(v + base + g * FG_SLICE * FG_GROUP);
+        const T4 cc = *reinterpret_cast<const T4 *>(c + base + g * FG_SLICE * FG_GROUP);
+        acc = fmaf(vv.x, __ldg(in + CI::col(cc.x, i)), acc);
+        acc = fmaf(vv.y, __ldg(in + CI::col(cc.y, i)), acc);
+        acc = fmaf(vv.z, __ldg(in + CI::col(cc.z, i)), acc);
+        acc = fmaf(vv.w, __ldg(in + CI::col(cc.w, i)), acc);
+      }
+      out[i] = acc;
+    }
+    __syncthreads();
+    if (k + 2 < K) {
+      if (tid == 0) issue(k + 2, st);
+      inflight |= 1u << st;
+    }
+  }
+  if (!ok && tid == 0) {
+    // a stage did not arrive: wait (bounded) for the copies in flight, stop the CG
+    for (int st = 0; st < 2; ++st)
+      if (inflight & (1u << st)) mbar_wait(&bar[st], (phase >> st) & 1u, 1 << 20);
+    atomicExch(ictl + I_FAULT, 1);
+    atomicExch(ictl + I_DONE, 1);
+  }
+}
+
 // Jacobi-PCG as plain CG on the symmetrically scaled system (the scaled split
 // variant): A' = S A S with S = D^-1/2 (sdiag = sqrt of the Jacobi inverse, 0 on
 // Dirichlet rows), b' = S b, x = S y.  The iterates are those of Jacobi-PCG; the
@@ -1171,6 +1410,11 @@ static void ensure_cg32(fg_mesh *m) {
       m->v32[j] = dev_alloc<float>(m, len);
       FG_CUDA_TRY(cudaMemsetAsync(m->v32[j], 0, sizeof(float) * len, m->stream));
     }
+  for (int j = 0; j < 3; ++j)
+    if (!m->pv32[j]) {
+      m->pv32[j] = dev_alloc<float>(m, (size_t)m->nvp);
+      FG_CUDA_TRY(cudaMemsetAsync(m->pv32[j], 0, sizeof(float) * (size_t)m->nvp, m->stream));
+    }
 }
 static void ensure_cg64(fg_mesh *m) {
   const int idx[6] = {0, 1, 2, 3, 4, 12};
@@ -1187,14 +1431,18 @@ static void ensure_cg64(fg_mesh *m) {
 // staging, 8 split with direct gathers in a persistent grid, 9 the same launched with
 // programmatic dependent launch, 10 the same with the matrix values held in L2,
 // 11-15 persistent grids of 4, 3, 5, 6 and 7 blocks per SM, 16 CG on the
-// symmetrically Jacobi-scaled system with the SpMV of variant 14
-constexpr int FG_N_SPMV32 = 22;
+// symmetrically Jacobi-scaled system with the SpMV of variant 14, 17-19 split with
+// the matrix entries staged by bulk copies (4, 3, 2 blocks per SM), 20 and 21 variants
+// 16 and 17 with the matrix values held in L2, 22 and 23 the pipelined CG (its dot
+// products finished by one block of the bulk-staged SpMV; 4 and 3 blocks per SM)
+constexpr int FG_N_SPMV32 = 24;
 // Split FP32 variants on the scaled system, with the values in the L2 window, and
 // with the matrix entries staged by bulk copies.
 static inline bool v_scaled(int v) { return v == 16 || v == 20; }
 static inline bool v_window(int v) { return v == 10 || v == 20 || v == 21; }
 static inline bool v_bulk(int v) { return (v >= 17 && v <= 19) || v == 21; }
 static inline bool split32(int v) { return v >= 6; }
+static inline bool v_pipe(int v) { return v == 22 || v == 23; }
 constexpr int FG_N_SPMV64 = 4;   // 0 direct gathers, 1 halo staging, 2/3 persistent with 4/8 blocks per SM
 
 template <class CI>
@@ -1522,7 +1770,85 @@ static void bulk_launch32(fg_mesh *m, int v) {
                                                            m->scal, m->ictl, m->red.partials, m->red.counter);
 }
 
+// Blocks per SM of the pipelined variants 22 and 23 (4, 3 wanted), or 0 where two
+// stages of a 256-row block do not fit; sized once per handle.
+static int pipe_per_sm(fg_mesh *m, int v) {
+  if (m->pipe_fit < 0) {
+    static std::once_flag attr_once;
+    static int dyn_max = 0;
+    std::call_once(attr_once, [&]() {
+      int dev_max = 0;
+      cudaFuncAttributes fa[2];
+      if (cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, m->device) != cudaSuccess ||
+          cudaFuncGetAttributes(&fa[0], k_pcg32_spmv_bulk<ColRel>) != cudaSuccess ||
+          cudaFuncGetAttributes(&fa[1], k_pcg32_spmv_bulk<ColAbs>) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+      }
+      const int d = dev_max - (int)std::max(fa[0].sharedSizeBytes, fa[1].sharedSizeBytes);
+      if (cudaFuncSetAttribute(k_pcg32_spmv_bulk<ColRel>, cudaFuncAttributeMaxDynamicSharedMemorySize, d) !=
+              cudaSuccess ||
+          cudaFuncSetAttribute(k_pcg32_spmv_bulk<ColAbs>, cudaFuncAttributeMaxDynamicSharedMemorySize, d) !=
+              cudaSuccess) {
+        cudaGetLastError();
+        return;
+      }
+      dyn_max = d;
+    });
+    const size_t smem = bulk_smem(m);
+    int per_sm = 0;
+    if (m->tmax256 > 0 && smem <= (size_t)dyn_max) {
+      if (m->use_dcol)
+        FG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg32_spmv_bulk<ColRel>, 256, smem));
+      else
+        FG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg32_spmv_bulk<ColAbs>, 256, smem));
+    }
+    m->pipe_fit = per_sm;
+  }
+  return std::min(m->pipe_fit, v == 22 ? 4 : 3);
+}
+
+// Blocks of the pipelined variants' vector pass (four rows per thread), also the
+// number of dot-product partials the next SpMV's first block sums.
+static unsigned pipe_vec_grid(const fg_mesh *m) { return grid_for(m->nvp / 4, 256); }
+
+// out = A in for the pipelined variants; with `reduce` the first block finishes the
+// dot products of the last vector pass instead of taking rows.  The grid never
+// exceeds the resident blocks, so that reducing block runs from the start.
+static void pipe_spmv32(fg_mesh *m, int v, bool reduce, const float *in, float *out) {
+  const int per_sm = pipe_per_sm(m, v);
+  FG_REQUIRE(per_sm > 0, FG_UNSUPPORTED, "pipelined CG: row blocks too large for shared memory");
+  const unsigned resident = (unsigned)per_sm * (unsigned)std::max(m->sm_count, 1);
+  const unsigned rows = grid_for(m->nv, 256);
+  const unsigned g = reduce ? std::min(rows + 1, resident) : std::min(rows, resident);
+  const size_t smem = bulk_smem(m);
+  const int nparts = reduce ? (int)pipe_vec_grid(m) : 0;
+  const float2 *parts = reinterpret_cast<const float2 *>(m->red.partials);
+  if (m->use_dcol)
+    k_pcg32_spmv_bulk<ColRel><<<g, 256, smem, m->stream>>>(m->nv, m->nslices, m->tmax256, m->sl_ptr, m->sl_len,
+                                                           m->sl_dcol, m->val32, in, out, m->scal, m->ictl, parts,
+                                                           nparts);
+  else
+    k_pcg32_spmv_bulk<ColAbs><<<g, 256, smem, m->stream>>>(m->nv, m->nslices, m->tmax256, m->sl_ptr, m->sl_len,
+                                                           m->sl_col, m->val32, in, out, m->scal, m->ictl, parts,
+                                                           nparts);
+}
+
+static void pipe_vec32(fg_mesh *m) {
+  k_pcg32_vec<<<pipe_vec_grid(m), 256, 0, m->stream>>>(
+      m->nvp / 4, reinterpret_cast<float4 *>(m->v32[0]), reinterpret_cast<float4 *>(m->v32[4]),
+      reinterpret_cast<float4 *>(m->v32[5]), reinterpret_cast<float4 *>(m->v32[6]),
+      reinterpret_cast<float4 *>(m->v32[1]), reinterpret_cast<float4 *>(m->pv32[0]),
+      reinterpret_cast<const float4 *>(m->pv32[1]), reinterpret_cast<float4 *>(m->pv32[2]),
+      reinterpret_cast<const float4 *>(m->dinv32), (const double *)m->scal, (const int *)m->ictl,
+      reinterpret_cast<float2 *>(m->red.partials));
+}
+
 static void launch_spmv32s(fg_mesh *m, int v) {
+  if (v_pipe(v)) {
+    pipe_spmv32(m, v, true, m->pv32[2], m->pv32[1]);
+    return;
+  }
   const bool pdl = (v == 9);
   if (v == 20 && m->l2_win_bytes > 0) {
     // the scaled system (16) with its values in the L2 window
@@ -1597,6 +1923,10 @@ static void launch_spmv32s(fg_mesh *m, int v) {
 }
 
 static void launch_vec32s(fg_mesh *m, int v) {
+  if (v_pipe(v)) {
+    pipe_vec32(m);
+    return;
+  }
   if (v_scaled(v)) {
     k_cg32ss_vec<<<grid_for(m->nvp / 4, 256), 256, 0, m->stream>>>(
         m->nvp / 4, reinterpret_cast<float4 *>(m->v32[4]), reinterpret_cast<const float4 *>(m->v32[5]),
@@ -1613,6 +1943,13 @@ static void launch_vec32s(fg_mesh *m, int v) {
 }
 
 static void launch_iter32(fg_mesh *m, int v, bool from_first_buffer) {
+  if (v_pipe(v)) {
+    // the SpMV (its first block finishing the last vector pass's dots), then the
+    // vector pass with those scalars
+    launch_spmv32s(m, v);
+    launch_vec32s(m, v);
+    return;
+  }
   if (split32(v)) {
     launch_vec32s(m, v);
     launch_spmv32s(m, v);
@@ -1676,6 +2013,15 @@ static void start_cg(fg_mesh *m, bool mixed, const double *r64, double scale, do
     k_cg32ss_init<<<g, 256, 0, m->stream>>>(m->nv, m->nvp, r64, scale, m->sdiag32, m->v32[4], m->v32[6], m->v32[1],
                                             m->v32[0], tol2_rel, maxit, m->scal, m->ictl);
     launch_spmv32s(m, m->spmv_variant32);
+  } else if (mixed && v_pipe(m->spmv_variant32)) {
+    // r, m = D r; w = A m; one vector pass with alpha = beta = 0 gives m = D w and the
+    // partials of the first dot products
+    k_pcg32_init<<<g, 256, 0, m->stream>>>(m->nv, m->nvp, r64, scale, m->dinv32, m->v32[4], m->pv32[2], m->v32[0],
+                                           m->v32[6], m->v32[1], m->pv32[0], m->pv32[1], tol2_rel, maxit, m->scal,
+                                           m->ictl);
+    pipe_spmv32(m, m->spmv_variant32, false, m->pv32[2], m->v32[5]);
+    pipe_vec32(m);
+    FG_LAUNCHED(1);
   } else if (mixed && split32(m->spmv_variant32)) {
     k_cg32s_init<<<g, 256, 0, m->stream>>>(m->nv, m->nvp, r64, scale, m->dinv32, m->v32[4], m->v32[7], m->v32[6],
                                            m->v32[1], m->v32[0], tol2_rel, maxit, m->scal, m->ictl);
@@ -1885,6 +2231,7 @@ static bool variant32_available(fg_mesh *m, int v) {
   if ((v == 4 || v == 7) && !fg_ensure_halo(m)) return false;
   if (v == 5 && !pipe_available(m)) return false;
   if (v_bulk(v) && bulk_per_sm(m, v) == 0) return false;
+  if (v_pipe(v) && pipe_per_sm(m, v) == 0) return false;
   if (v_window(v) && !l2_supported(m)) return false;
   return true;
 }
