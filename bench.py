@@ -660,7 +660,7 @@ def case_sweep(args):
 
 def case_batch(args):
     """64 independent linear problems, cells per side ~ U{8..40}, mur ~ U[1,1000] per
-    element, one persistent graph-captured launch."""
+    element, one graph launch (a thread-block cluster per problem, sized by its rows)."""
     import femeko_gpu as fg
     from femeko_gpu.mesh import box_tet_mesh
     rng = np.random.default_rng(SEED)
@@ -670,32 +670,87 @@ def case_batch(args):
     u0s = [-m.p[0].copy() for m in meshes]
     fg.batch_magnetostatics_linear(meshes, mus, u0s, rtol=1e-10)              # warm-up (assembly, handles)
     us, its, st = fg.batch_magnetostatics_linear(meshes, mus, u0s, rtol=1e-10)
-    _line("batched independent solves/s (64 meshes, one persistent launch)", 64 / (st["ms"] * 1e-3), "solves/s",
+    big = int(np.argmax(ns))
+    fg.batch_magnetostatics_linear([meshes[big]], [mus[big]], [u0s[big]], rtol=1e-10)
+    _, its1, st1 = fg.batch_magnetostatics_linear([meshes[big]], [mus[big]], [u0s[big]], rtol=1e-10)
+    # algorithmic bytes per FP64 CG iteration of one problem: value and column of each
+    # stored nonzero (12 B), the vectors x, r, z, p_old, p_new, q, diagonal (read and
+    # written, 80 B per row)
+    nnz = np.array([fg.gpu_mesh(m).nnz for m in meshes], dtype=np.float64)
+    nv = np.array([m.nv for m in meshes], dtype=np.float64)
+    work = float((its * (12 * nnz + 80 * nv)).sum())
+    peak = measured_peaks()[0]
+    ach = work / (st["ms"] * 1e-3) / 1e9
+    _line("batched independent solves/s (64 meshes, one graph launch)", 64 / (st["ms"] * 1e-3), "solves/s",
           True, {"workload": "64 linear problems, Kuhn tets 8..40 cells per side", "cells": [int(n) for n in ns],
                  "total_nodes": int(sum(m.nv for m in meshes))},
           {"ms": st["ms"], "max_iterations": st["max_iterations"], "total_iterations": st["total_iterations"],
-           "converged": st["converged"]})
+           "converged": st["converged"], "largest_cluster_ctas": st["cluster_ctas"],
+           "largest_mesh_alone_ms": st1["ms"], "largest_mesh_cells": int(ns[big]),
+           "alg_bytes": work, "achieved_GBs": ach, "frac_of_measured_hbm": ach / peak,
+           "note": "FP64 SpMVs of 8-16 SMs per problem are FP64-pipe bound; the vectors stay in L2"})
+
+
+def _mean_hx(fg, mesh, target, u):
+    """J = volume-weighted mean of H_x over the target elements (NewtonRaphson.jl:234-240)."""
+    H = fg.hfield(mesh, u)
+    sel = target.astype(bool)
+    return float((mesh.VE[sel] * H[0, sel]).sum() / mesh.VE[sel].sum())
 
 
 def case_adjoint(args):
     """dJ/dmur for J = mean Hx over elements with centroid in |x| < 0.5 on the 64^3
-    linear mesh (mur ~ U[1,1000]): adjoint cost against the forward solve."""
+    mesh, mur ~ U[1,1000]: adjoint cost against the forward solve, and central
+    differences (relative step 1e-6) on 32 elements.  --nonlinear: the same through
+    the converged Newton Jacobian with the Froehlich plate of the 96^3 workload."""
     import femeko_gpu as fg
     from femeko_gpu.mesh import box_tet_mesh
     cells = args.cells if args.cells != 96 else 64
     mesh = box_tet_mesh(cells, seed=SEED)
     rng = np.random.default_rng(SEED)
+    nl = (mesh.elementID == 2).astype(np.uint8) if args.nonlinear else None
     mur = rng.uniform(1, 1000, mesh.nt)
+    if args.nonlinear:
+        mur = np.where(nl == 1, 1.0, mur)
     c = mesh.centroids()
     target = (np.sqrt((c * c).sum(axis=0)) < 0.5).astype(np.uint8)
-    u0 = -mesh.p[0].copy()
-    fg.adjoint_dJdmu(mesh, mur, u0, target, precision="mixed", rtol=1e-10)     # warm-up
-    J, grad, u, st = fg.adjoint_dJdmu(mesh, mur, u0, target, precision="mixed", rtol=1e-10)
+    u0 = -(H0[:, None] * mesh.p).sum(axis=0) if args.nonlinear else -mesh.p[0].copy()
+    kw = dict(nl=nl, precision="mixed", rtol=1e-10)
+    if args.nonlinear:
+        kw.update(tol_update=1e-10)
+    fg.adjoint_dJdmu(mesh, mur, u0, target, **kw)                           # warm-up
+    J, grad, u, st = fg.adjoint_dJdmu(mesh, mur, u0, target, **kw)
+    # central differences on 32 elements among those with at least 1% of the largest
+    # sensitivity; each perturbed solve starts from the converged u (FP64, tight)
+    pool = np.flatnonzero(np.abs(grad) >= 1e-2 * np.abs(grad).max())
+    if args.nonlinear:
+        pool = pool[nl[pool] == 0]
+    picks = np.random.default_rng(11).choice(pool, min(32, pool.size), replace=False)
+    errs = []
+    for k in picks:
+        d = 1e-6 * mur[k]
+        us = []
+        for sgn in (+1, -1):
+            mu2 = mur * fg.MU0
+            mu2[k] = (mur[k] + sgn * d) * fg.MU0
+            if args.nonlinear:
+                u2, _, _, s2 = fg.newton_magnetostatics(mesh, nl, mu2, u, precision="fp64", tol_update=1e-13,
+                                                        forcing="fixed", inner_rtol=1e-13, picard_steps=0)
+            else:
+                u2, _, s2 = fg.magnetostatics_linear(mesh, mu2, u, precision="fp64", rtol=1e-12)
+            us.append(u2)
+        fd = _mean_hx(fg, mesh, target, us[0] - us[1]) / (2 * d)
+        errs.append(abs(fd - grad[k]) / abs(grad[k]))
+    what = "Froehlich-plate Newton magnetostatics" if args.nonlinear else "linear magnetostatics"
     _line("adjoint dJ/dmur cost relative to the forward solve", st["adjoint_ms"] / st["forward_ms"], "x forward",
-          False, {"workload": f"linear magnetostatics, Kuhn tets {cells}^3 cells, mur ~ U[1,1000], |x| < 0.5 target",
-                  "tets": int(mesh.nt), "nodes": int(mesh.nv), "target_elements": int(target.sum())},
+          False, {"workload": f"{what}, Kuhn tets {cells}^3 cells, mur ~ U[1,1000], |x| < 0.5 target",
+                  "tets": int(mesh.nt), "nodes": int(mesh.nv), "target_elements": int(target.sum()),
+                  "nonlinear": bool(args.nonlinear)},
           {"J": J, "forward_ms": st["forward_ms"], "adjoint_ms": st["adjoint_ms"],
-           "forward_iters": st["forward_iters"], "adjoint_iters": st["adjoint_iters"]})
+           "forward_iters": st["forward_iters"], "adjoint_iters": st["adjoint_iters"],
+           "newton_iters": st["newton_iters"],
+           "central_differences": {"elements": int(len(picks)), "rel_step": 1e-6,
+                                   "max_rel_err": float(max(errs)), "median_rel_err": float(np.median(errs))}})
 
 
 def case_transport(args):
@@ -809,6 +864,7 @@ def main():
     ap.add_argument("--variant", type=int, default=6, help="--case cg-kernel: forced CG kernel variant (1..6)")
     ap.add_argument("--iters", type=int, default=200, help="--case cg-kernel: CG iterations")
     ap.add_argument("--rhs", choices=["random", "ones"], default="random", help="--case cg-loop: right-hand side")
+    ap.add_argument("--nonlinear", action="store_true", help="--case adjoint: through the Newton Jacobian")
     args = ap.parse_args()
     if args.fp64_steps is None:
         args.fp64_steps = args.steps

@@ -1120,6 +1120,13 @@ static void launch_rows_tet4(fg_mesh *m, int kind, const double *d_f, double cm,
   FG_LAUNCHED(1);
 }
 
+// The P1-tetrahedron mass matrix (unit coefficient) into SELL values out64, no
+// boundary rows applied: for products M x repeated with one matrix.
+void fg_assemble_mass_sell(fg_mesh *m, double *out64) {
+  FG_REQUIRE(m->npe == 4 && !m->edge, FG_UNSUPPORTED, "mass operator: P1 tetrahedra only");
+  launch_rows_tet4(m, ASM_MASS, nullptr, 0.0, 0.0, 0, out64, nullptr, nullptr, nullptr, nullptr);
+}
+
 void fg_assemble_operator(fg_mesh *m, int kind, const double *d_f, const double *d_H, const double *d_dmu,
                           double c_mass, double c_stiff, int full_phi, int layout, bool want64, bool want32,
                           bool apply_bc) {

@@ -1,11 +1,15 @@
 // Many independent linear magnetostatic problems (meshes of uneven size) solved in
-// ONE persistent launch: each problem gets a thread-block cluster of FG_BATCH_CL
-// CTAs that runs its whole Jacobi-PCG (Magnetostatics/magneticField.jl:89-132 per
-// mesh, the solve IterativeSolvers.cg does there) without returning to the host.
-// The cluster's CTAs split the problem's rows; dot products are reduced through
-// distributed shared memory (every CTA reads the CTAs' partials in rank order, so
-// all of them get the same value), and the cluster barrier separates the phases.
-// The launch is captured in a CUDA graph and replayed.
+// ONE graph launch: each problem gets a thread-block cluster that runs its whole
+// Jacobi-PCG (Magnetostatics/magneticField.jl:89-132 per mesh, the solve
+// IterativeSolvers.cg does there) without returning to the host.  The cluster's CTAs
+// split the problem's rows; dot products are reduced through distributed shared
+// memory (every CTA reads the CTAs' partials in rank order, so all of them get the
+// same value), and the cluster barrier separates the phases.
+// Load balance: a problem's work grows with its rows (and its iteration count with
+// them), so the cluster size follows the rows: 16, 8, 4 or 2 CTAs, the largest problem
+// getting 16 where the device places 16-CTA clusters.  One launch per cluster size,
+// the launches on parallel branches of one captured graph, largest problems first in
+// each.
 #include <cooperative_groups.h>
 
 #include <algorithm>
@@ -17,8 +21,7 @@
 
 namespace cgrp = cooperative_groups;
 
-// CTAs per problem: the portable cluster size 8 (16-CTA clusters of 1024 threads
-// measured 2x slower on the 64-mesh batch: 64 registers per thread spill)
+// Threads per CTA (1024-thread CTAs spilled registers: 64 per thread at most)
 constexpr int FG_BATCH_THREADS = 512;
 
 struct BatchProb {
@@ -59,6 +62,7 @@ __device__ __forceinline__ void cluster_sum2(cgrp::cluster_group &cl, double a, 
   __threadfence();
   cl.sync();
   double sa = 0.0, sb = 0.0;
+#pragma unroll 4
   for (int rank = 0; rank < CL; ++rank) {
     const double *remote = cl.map_shared_rank(&slot[which][0], rank);
     sa += remote[0];
@@ -69,7 +73,7 @@ __device__ __forceinline__ void cluster_sum2(cgrp::cluster_group &cl, double a, 
 }
 
 template <int CL>
-__global__ void __launch_bounds__(FG_BATCH_THREADS) k_batch_pcg64(const BatchProb *__restrict__ probs) {
+__global__ void __launch_bounds__(FG_BATCH_THREADS, 2) k_batch_pcg64(const BatchProb *__restrict__ probs) {
   cgrp::cluster_group cl = cgrp::this_cluster();
   __shared__ double slot[2][2];
   const int rank = (int)cl.block_rank();
@@ -230,22 +234,71 @@ extern "C" fg_status fg_batch_magnetostatics_linear(fg_mesh *const *meshes, int3
       for (int j = 0; j < k; ++j)
         FG_REQUIRE(meshes[j] != meshes[k], FG_BAD_ARG, "fg_batch_magnetostatics_linear: a mesh handle appears twice");
     }
-    // largest problems first: clusters are dispatched in index order
+    // cluster size per problem from its rows: the largest problem gets the largest
+    // cluster the device places (16 where allowed, else 8), the others in proportion
+    // to their rows (at least 2 CTAs)
+    auto fits = [&](int cl) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.blockDim = dim3(FG_BATCH_THREADS);
+      cfg.gridDim = dim3((unsigned)cl);
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = (unsigned)cl;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      int fit = 0;
+      cudaError_t e = cudaSuccess;
+      if (cl == 16) {
+        e = cudaFuncSetAttribute(k_batch_pcg64<16>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveClusters(&fit, k_batch_pcg64<16>, &cfg);
+      } else if (cl == 8) {
+        e = cudaOccupancyMaxActiveClusters(&fit, k_batch_pcg64<8>, &cfg);
+      } else if (cl == 4) {
+        e = cudaOccupancyMaxActiveClusters(&fit, k_batch_pcg64<4>, &cfg);
+      } else {
+        e = cudaOccupancyMaxActiveClusters(&fit, k_batch_pcg64<2>, &cfg);
+      }
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+      }
+      return fit > 0;
+    };
+    const int cl_max = fits(16) ? 16 : 8;
+    FG_REQUIRE(fits(8), FG_UNSUPPORTED, "fg_batch_magnetostatics_linear: the device cannot place an 8-CTA cluster");
+    int64_t nmax = 1;
+    for (int k = 0; k < count; ++k) nmax = std::max(nmax, hp[k].n);
+    std::vector<int> clk(count);
+    for (int k = 0; k < count; ++k) {
+      const double want = (double)cl_max * (double)hp[k].n / (double)nmax;
+      int c = 2;
+      while (c < cl_max && c < want) c *= 2;
+      clk[k] = c;
+    }
+    // problems ordered by cluster size, then largest first within one size
     std::vector<int> order(count);
     std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return hp[a].n > hp[b].n; });
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+      return clk[a] != clk[b] ? clk[a] > clk[b] : hp[a].n > hp[b].n;
+    });
     int *d_out = nullptr;
     BatchProb *d_probs = nullptr;
     double *d_rel = nullptr;
-    int cluster_size = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr, fork = nullptr;
+    std::vector<cudaStream_t> side;
+    std::vector<cudaEvent_t> joins;
     auto cleanup = [&]() {
       if (exec) cudaGraphExecDestroy(exec);
       if (graph) cudaGraphDestroy(graph);
       if (e0) cudaEventDestroy(e0);
       if (e1) cudaEventDestroy(e1);
+      if (fork) cudaEventDestroy(fork);
+      for (cudaEvent_t e : joins) cudaEventDestroy(e);
+      for (cudaStream_t q : side) cudaStreamDestroy(q);
       cudaFree(d_out);
       cudaFree(d_probs);
       cudaFree(d_rel);
@@ -263,27 +316,57 @@ extern "C" fg_status fg_batch_magnetostatics_linear(fg_mesh *const *meshes, int3
       }
       cudaStream_t st = m0->stream;
       FG_CUDA_TRY(cudaMemcpyAsync(d_probs, sorted.data(), sizeof(BatchProb) * count, cudaMemcpyHostToDevice, st));
-      cudaLaunchConfig_t cfg = {};
-      cfg.blockDim = dim3(FG_BATCH_THREADS);
-      cfg.dynamicSmemBytes = 0;
-      cfg.stream = st;
-      cudaLaunchAttribute attr[1];
-      attr[0].id = cudaLaunchAttributeClusterDimension;
-      attr[0].val.clusterDim.y = 1;
-      attr[0].val.clusterDim.z = 1;
-      cfg.attrs = attr;
-      cfg.numAttrs = 1;
-      const int cl = 8;
-      int fit = 0;
-      cfg.gridDim = dim3((unsigned)(count * cl));
-      attr[0].val.clusterDim.x = cl;
-      FG_CUDA_TRY(cudaOccupancyMaxActiveClusters(&fit, k_batch_pcg64<8>, &cfg));
-      FG_REQUIRE(fit > 0, FG_UNSUPPORTED, "fg_batch_magnetostatics_linear: the device cannot place one cluster");
-      cluster_size = cl;
+      // one launch per cluster size: [first, first + n) of the sorted problems
+      struct Group {
+        int cl, first, n;
+      };
+      std::vector<Group> groups;
+      for (int j = 0; j < count;) {
+        int e = j;
+        while (e < count && clk[order[e]] == clk[order[j]]) ++e;
+        groups.push_back(Group{clk[order[j]], j, e - j});
+        j = e;
+      }
       FG_CUDA_TRY(cudaEventCreate(&e0));
       FG_CUDA_TRY(cudaEventCreate(&e1));
+      FG_CUDA_TRY(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+      for (size_t gi = 1; gi < groups.size(); ++gi) {
+        cudaStream_t q;
+        FG_CUDA_TRY(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
+        side.push_back(q);
+        cudaEvent_t ev;
+        FG_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        joins.push_back(ev);
+      }
+      auto launch = [&](const Group &g, cudaStream_t q) -> cudaError_t {
+        cudaLaunchConfig_t cfg = {};
+        cfg.blockDim = dim3(FG_BATCH_THREADS);
+        cfg.gridDim = dim3((unsigned)(g.n * g.cl));
+        cfg.stream = q;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = (unsigned)g.cl;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        const BatchProb *pp = d_probs + g.first;
+        switch (g.cl) {
+          case 16: return cudaLaunchKernelEx(&cfg, k_batch_pcg64<16>, pp);
+          case 8: return cudaLaunchKernelEx(&cfg, k_batch_pcg64<8>, pp);
+          case 4: return cudaLaunchKernelEx(&cfg, k_batch_pcg64<4>, pp);
+          default: return cudaLaunchKernelEx(&cfg, k_batch_pcg64<2>, pp);
+        }
+      };
       FG_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-      cudaError_t le = cudaLaunchKernelEx(&cfg, k_batch_pcg64<8>, (const BatchProb *)d_probs);
+      cudaError_t le = cudaEventRecord(fork, st);
+      for (size_t gi = 1; gi < groups.size() && le == cudaSuccess; ++gi) le = cudaStreamWaitEvent(side[gi - 1], fork, 0);
+      if (le == cudaSuccess) le = launch(groups[0], st);
+      for (size_t gi = 1; gi < groups.size() && le == cudaSuccess; ++gi) {
+        le = launch(groups[gi], side[gi - 1]);
+        if (le == cudaSuccess) le = cudaEventRecord(joins[gi - 1], side[gi - 1]);
+        if (le == cudaSuccess) le = cudaStreamWaitEvent(st, joins[gi - 1], 0);
+      }
       cudaError_t ce = cudaStreamEndCapture(st, &graph);
       FG_CUDA_TRY(le);
       FG_CUDA_TRY(ce);
@@ -291,7 +374,7 @@ extern "C" fg_status fg_batch_magnetostatics_linear(fg_mesh *const *meshes, int3
       FG_CUDA_TRY(cudaEventRecord(e0, st));
       FG_CUDA_TRY(cudaGraphLaunch(exec, st));
       FG_CUDA_TRY(cudaEventRecord(e1, st));
-      FG_LAUNCHED(1);
+      FG_LAUNCHED((long long)groups.size());
       std::vector<int> hout(2 * count);
       std::vector<double> hrel(count);
       FG_CUDA_TRY(cudaMemcpyAsync(hout.data(), d_out, sizeof(int) * 2 * count, cudaMemcpyDeviceToHost, st));
@@ -317,7 +400,7 @@ extern "C" fg_status fg_batch_magnetostatics_linear(fg_mesh *const *meshes, int3
         s->problems = count;
         s->converged = conv;
         s->max_iterations = maxit;
-        s->cluster_ctas = cluster_size;
+        s->cluster_ctas = cl_max;
         s->total_iterations = tot;
         s->ms = ms;
       }

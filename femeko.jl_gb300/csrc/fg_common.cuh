@@ -297,6 +297,8 @@ void fg_assemble_operator(fg_mesh *m, int kind, const double *d_f, const double 
                           double c_mass, double c_stiff, int full_phi, int layout, bool want64, bool want32,
                           bool apply_bc);
 void fg_ensure_records(fg_mesh *m);
+// P1-tetrahedron mass matrix (unit coefficient, no boundary rows) into SELL values.
+void fg_assemble_mass_sell(fg_mesh *m, double *out64);
 // Element pass + row gather at potential d_u: element state (H, mu, dmu, energy
 // density), the residual F = -K(mu(u)) u (FP64) and, when want_jacobian, the
 // Jacobian K + At in the operator (FP32 when mixed) with its Jacobi diagonal.

@@ -2,14 +2,20 @@
 // T <- (M + dt A) \ (M T)), with a volumetric heat capacity rho_c, per-element
 // conductivity kappa and T = 0 on the Dirichlet nodes:
 //   (rho_c M + dt K(kappa)) T_{n+1} = rho_c M T_n.
-// The operator is assembled once (FP64, plus FP32 when mixed); every step applies the
-// mass matrix matrix-free (element pass + row gather) and solves with the previous
+// The operator and the mass matrix are assembled once (FP64, plus FP32 operator when
+// mixed); every step forms b = rho_c M T with one SpMV and solves with the previous
 // temperature as the initial guess.
 #include "fg_common.cuh"
 
 __global__ void k_zero_fixed(int64_t n, const uint8_t *__restrict__ fixed, double *__restrict__ x) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n && fixed[i]) x[i] = 0.0;
+}
+
+// b = c b on free rows, 0 on the Dirichlet rows (fixed may be NULL).
+__global__ void k_scale_free(int64_t n, const uint8_t *__restrict__ fixed, double c, double *__restrict__ b) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (fixed && fixed[i]) ? 0.0 : c * b[i];
 }
 
 extern "C" fg_status fg_heat_be(fg_mesh *m, const double *kappa, double rho_c, double dt, int32_t nsteps, double *T,
@@ -39,11 +45,15 @@ extern "C" fg_status fg_heat_be(fg_mesh *m, const double *kappa, double rho_c, d
     FG_CUDA_TRY(cudaEventCreate(&e1));
     FG_CUDA_TRY(cudaEventRecord(e0, m->stream));
     fg_assemble_operator(m, ASM_HEAT, d_k, nullptr, nullptr, rho_c, dt, 0, OUT_SELL, true, mixed, true);
+    if (!m->mval) m->mval = dev_alloc<double>(m, (size_t)m->nsell);
+    fg_assemble_mass_sell(m, m->mval);
     int iters = 0, refinements = 0, status = 0, snap = 0;
     double relres = 0.0;
     for (int step = 1; step <= nsteps; ++step) {
-      // b = rho_c M T (Dirichlet rows 0): the heat element pass with a zero stiffness factor
-      fg_apply_operator_vec(m, ASM_HEAT, d_k, rho_c, 0.0, d_T, d_b, true);
+      // b = rho_c M T (Dirichlet rows 0): one SpMV with the mass matrix
+      fg_spmv64_plain(m, m->mval, d_T, d_b);
+      k_scale_free<<<grid_for(nv, 256), 256, 0, m->stream>>>(nv, m->has_fixed ? m->fixed : nullptr, rho_c, d_b);
+      FG_LAUNCHED(1);
       fg_solve_stats st{};
       const int rc = fg_pcg_solve(m, d_b, d_T, opts, &st, false);
       iters += st.iterations;

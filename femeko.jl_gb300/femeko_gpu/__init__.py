@@ -307,14 +307,17 @@ def newton_magnetostatics(mesh: MESH, nl, mu_lin, u0, **kw):
     return u, H.reshape(mesh.nt, 3).T, mu, L.stats_dict(s)
 
 
-def heat_be(mesh: MESH, T0, kappa, rho_c=1.0, dt=1e-3, nsteps=100, every=10, precision="fp64", rtol=1e-10, **kw):
+def heat_be(mesh: MESH, T0, kappa, rho_c=1.0, dt=1e-3, nsteps=100, every=10, precision="fp64", rtol=1e-10,
+            check_every=8, **kw):
     """Backward-Euler heat steps (Heat/heat3D.jl:50-90) with T = 0 on the Dirichlet
-    nodes; returns (T_final, snapshots every `every` steps, stats)."""
+    nodes; returns (T_final, snapshots every `every` steps, stats).  Each step's solve
+    takes a few tens of CG iterations, so its graph loop tests for convergence every
+    `check_every` = 8 iterations (fewer idle launches after convergence)."""
     g = gpu_mesh(mesh)
     T = _c(T0, np.float64).copy()
     nsnap = nsteps // every if every > 0 else 0
     snaps = np.zeros((max(nsnap, 1), mesh.nv))
-    o = solve_opts(precision=precision, rtol=rtol, **kw)
+    o = solve_opts(precision=precision, rtol=rtol, check_every=check_every, **kw)
     s = L.SolveStats()
     st = L.lib().fg_heat_be(g.h, L.ptr(_c(kappa, np.float64)), rho_c, dt, nsteps, L.ptr(T), every,
                             L.ptr(snaps) if nsnap else None, C.byref(o), C.byref(s))

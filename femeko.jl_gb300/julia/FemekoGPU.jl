@@ -490,8 +490,10 @@ function __init__()
     if Base.find_package("ChainRulesCore") !== nothing
         @eval begin
             import ChainRulesCore
-            function ChainRulesCore.rrule(::typeof(mean_Hx_value), mesh, mur, fixed, u0, target)
-                J, grad = mean_Hx(mesh, mur, fixed, u0, target)
+            # keywords (nl for the Newton problem, precision, rtol) pass through to the
+            # adjoint: with nl given, the gradient comes through the converged Newton Jacobian
+            function ChainRulesCore.rrule(::typeof(mean_Hx_value), mesh, mur, fixed, u0, target; kw...)
+                J, grad = mean_Hx(mesh, mur, fixed, u0, target; kw...)
                 pullback(dJ) = (ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent(), dJ .* grad,
                                 ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent())
                 return J, pullback
@@ -500,7 +502,8 @@ function __init__()
     end
 end
 
-"""The scalar J alone (the function the rrule differentiates)."""
-mean_Hx_value(mesh, mur, fixed, u0, target) = mean_Hx(mesh, mur, fixed, u0, target)[1]
+"""The scalar J alone (the function the rrule differentiates); keywords as mean_Hx
+(nl = Froehlich mask for the nonlinear problem)."""
+mean_Hx_value(mesh, mur, fixed, u0, target; kw...) = mean_Hx(mesh, mur, fixed, u0, target; kw...)[1]
 
 end # module

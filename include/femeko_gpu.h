@@ -377,15 +377,18 @@ typedef struct fg_batch_stats {
   int32_t problems;
   int32_t converged;       /* problems that reached rtol */
   int32_t max_iterations;  /* largest CG iteration count of a problem */
-  int32_t cluster_ctas;    /* CTAs per problem (thread-block cluster size) */
+  int32_t cluster_ctas;    /* CTAs of the largest problem's cluster (16 or 8; smaller problems get
+                              fewer in proportion to their rows, at least 2) */
   int64_t total_iterations;
-  double ms;               /* device time of the one persistent launch */
+  double ms;               /* device time of the graph launch */
 } fg_batch_stats;
 
 /* count independent linear magnetostatic problems (Magnetostatics/magneticField.jl:89-132
  * on each mesh: K(mu) u = 0 on free rows, u = u_in on the Dirichlet rows set by
- * fg_mesh_set_dirichlet) solved by FP64 Jacobi-PCG in ONE persistent kernel launch,
- * replayed from a CUDA graph: each problem runs on its own thread-block cluster.
+ * fg_mesh_set_dirichlet) solved by FP64 Jacobi-PCG in ONE graph launch: each problem
+ * runs its whole solve on its own thread-block cluster, whose size follows the
+ * problem's rows (16, 8, 4 or 2 CTAs; one persistent kernel per cluster size, the
+ * kernels on parallel branches of the graph).
  * mu[k] (nt_k, absolute permeability), u_in[k] and u_out[k] (nv_k) are host arrays
  * per mesh; iterations (count, may be NULL) receives each problem's CG iterations.
  * All meshes on the current device; o->precision must be FG_FP64. */
