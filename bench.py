@@ -314,8 +314,10 @@ def run_ours(args):
              "split, bulk-staged entries, persistent 2/SM",
              "split, Jacobi-scaled system, persistent 6/SM, values in L2 window",
              "split, bulk-staged entries, persistent 4/SM, values in L2 window",
-             "pipelined CG, bulk-staged SpMV 4/SM, dots finished by one SpMV block",
-             "pipelined CG, bulk-staged SpMV 3/SM, dots finished by one SpMV block"]
+             "split, bulk-staged entries, persistent 4/SM, dots finished by a one-block kernel",
+             "split, bulk-staged entries, persistent 3/SM, dots finished by a one-block kernel",
+             "pipelined CG, bulk-staged SpMV 4/SM, dots finished by one SpMV block (forced only)",
+             "pipelined CG, bulk-staged SpMV 3/SM, dots finished by one SpMV block (forced only)"]
     variants_us = np.zeros(len(names))
     # the table of every variant on the converged operator (a second timing); the
     # per-kernel figures below are for the variant the timed solves used
@@ -373,7 +375,7 @@ def run_ours(args):
                 "two_pass_us": t_asm2.value * 1e3, "speedup_vs_two_pass": t_asm2.value / t_asm.value}
     n = mesh.nv
     v = int(used32.value) - 1
-    if v in (22, 23):
+    if v in (24, 25):
         # pipelined CG, dominant kernel n = A m: FP32 value and 16-bit column per
         # stored nonzero; per row m read once and n written (8 B); no dot products
         alg_bytes = g.nnz * 6 + 8 * n
@@ -389,7 +391,9 @@ def run_ours(args):
         # (12 B).  Neighbour gathers of u are re-reads.
         alg_bytes = g.nnz * 6 + 12 * n
         kname = {7: "k_cg32s_spmv_halo", 17: "k_cg32s_spmv_bulk", 18: "k_cg32s_spmv_bulk",
-                 19: "k_cg32s_spmv_bulk", 21: "k_cg32s_spmv_bulk"}.get(v, "k_cg32s_spmv")
+                 19: "k_cg32s_spmv_bulk", 21: "k_cg32s_spmv_bulk",
+                 22: "k_cg32s_spmv_bulk<split> + k_cg32_dots_finish",
+                 23: "k_cg32s_spmv_bulk<split> + k_cg32_dots_finish"}.get(v, "k_cg32s_spmv")
     else:
         # one fused iteration: matrix as above; per row the (r, w, s, dinv) state read
         # and written (16 + 16 B) and p, x read and written (8 + 8 B)
@@ -857,7 +861,7 @@ def main():
     ap.add_argument("--graph-mode", type=int, default=1, choices=[0, 1, 2],
                     help="1: whole CG in one graph launch (device-side loop); 2: host-checked graph blocks; 0: no graph")
     ap.add_argument("--cg-variant", type=int, default=0,
-                    help="fix the FP32 CG kernel variant (1..24; 0: autotuned), e.g. for profiling runs")
+                    help="fix the FP32 CG kernel variant (1..26; 0: autotuned), e.g. for profiling runs")
     ap.add_argument("--cg64-variant", type=int, default=0, help="fix the FP64 CG SpMV variant (1..4; 0: autotuned)")
     ap.add_argument("--case", choices=sorted(CASES), default=None,
                     help="run a secondary workload instead of the headline benchmark")

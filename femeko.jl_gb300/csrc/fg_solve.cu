@@ -643,7 +643,7 @@ __global__ void __launch_bounds__(R) k_cg32s_spmv_halo(int64_t n, const int *__r
 // mbarrier).  Threads read their row's entries from shared memory and gather u from
 // global memory.  cap: the most padded entries of one 256-row block.  A stage that
 // does not arrive within the bounded wait stops the CG with I_FAULT set.
-template <class CI>
+template <class CI, bool SPLIT = false>
 __global__ void __launch_bounds__(256) k_cg32s_spmv_bulk(int64_t n, int nslices, int cap,
                                                          const int *__restrict__ sl_ptr,
                                                          const int *__restrict__ sl_len,
@@ -744,8 +744,43 @@ __global__ void __launch_bounds__(256) k_cg32s_spmv_bulk(int64_t n, int nslices,
     }
     __syncthreads();
   }
+  if (SPLIT) {
+    // the block's compensated sums only; k_cg32_dots_finish adds them up
+    __shared__ ff shs[3][32];
+    ff v[3] = {dots[0].v, dots[1].v, dots[2].v};
+    block_sum_ff_pair<3>(v, shs);
+    if (tid == 0) {
+      float2 *fp = reinterpret_cast<float2 *>(partials);
+      for (int j = 0; j < 3; ++j) fp[(size_t)blockIdx.x * 3 + j] = make_float2(v[j].hi, v[j].lo);
+    }
+    return;
+  }
   double tot[3];
   if (finish_dots32(dots, partials, counter, tot) && ok) cgcg_scalars(tot, scal, ictl);
+}
+
+// The dot products of the split-reduction SpMV (k_cg32s_spmv_bulk<CI, true>): one
+// block sums the nparts per-block partials in index order and sets the iteration's
+// scalars.  A kernel of its own instead of the last-arriving block of the SpMV: no
+// block of the SpMV waits on arrival counters, and the sum starts once every block
+// has finished, in one block, without the two-level arrival chain.
+__global__ void __launch_bounds__(256) k_cg32_dots_finish(const float2 *__restrict__ partials, int nparts,
+                                                          double *scal, int *ictl) {
+  if (ictl[I_DONE]) return;
+  ff acc[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+  for (int k = threadIdx.x; k < nparts; k += 256)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const float2 q = __ldcg(partials + (size_t)k * 3 + j);
+      acc[j] = ff_add(acc[j], ff{q.x, q.y});
+    }
+  __shared__ ff shr[3][32];
+  block_sum_ff_pair<3>(acc, shr);
+  if (threadIdx.x == 0) {
+    double tot[3];
+    for (int j = 0; j < 3; ++j) tot[j] = (double)acc[j].hi + (double)acc[j].lo;
+    cgcg_scalars(tot, scal, ictl);
+  }
 }
 
 // ------------------------------------------------------------------ FP32 pipelined CG
@@ -1433,16 +1468,22 @@ static void ensure_cg64(fg_mesh *m) {
 // 11-15 persistent grids of 4, 3, 5, 6 and 7 blocks per SM, 16 CG on the
 // symmetrically Jacobi-scaled system with the SpMV of variant 14, 17-19 split with
 // the matrix entries staged by bulk copies (4, 3, 2 blocks per SM), 20 and 21 variants
-// 16 and 17 with the matrix values held in L2, 22 and 23 the pipelined CG (its dot
-// products finished by one block of the bulk-staged SpMV; 4 and 3 blocks per SM)
-constexpr int FG_N_SPMV32 = 24;
+// 16 and 17 with the matrix values held in L2, 22 and 23 variants 17 and 18 with the
+// dot products finished by a one-block kernel after the SpMV, 24 and 25 the
+// pipelined CG (its dot products finished by one block of the bulk-staged SpMV; 4
+// and 3 blocks per SM).  The pipelined variants are timed by the autotuner but
+// never chosen by it: in FP32 their recurrences lose accuracy faster than CG's, so
+// inner solves asked for 1e-6 stall (Newton's tight Eisenstat-Walker steps), and on
+// singular systems they diverge; they run only when forced.
+constexpr int FG_N_SPMV32 = 26;
 // Split FP32 variants on the scaled system, with the values in the L2 window, and
 // with the matrix entries staged by bulk copies.
 static inline bool v_scaled(int v) { return v == 16 || v == 20; }
 static inline bool v_window(int v) { return v == 10 || v == 20 || v == 21; }
-static inline bool v_bulk(int v) { return (v >= 17 && v <= 19) || v == 21; }
+static inline bool v_bulk(int v) { return (v >= 17 && v <= 19) || v == 21 || v == 22 || v == 23; }
+static inline bool v_splitred(int v) { return v == 22 || v == 23; }
 static inline bool split32(int v) { return v >= 6; }
-static inline bool v_pipe(int v) { return v == 22 || v == 23; }
+static inline bool v_pipe(int v) { return v == 24 || v == 25; }
 constexpr int FG_N_SPMV64 = 4;   // 0 direct gathers, 1 halo staging, 2/3 persistent with 4/8 blocks per SM
 
 template <class CI>
@@ -1709,7 +1750,9 @@ static size_t bulk_smem(const fg_mesh *m) {
 // two stages do not fit; sized once per handle.  The kernels may take up to the
 // device's opt-in shared memory (set once per process).
 static int bulk_per_sm(fg_mesh *m, int v) {
-  static const int kWant[5] = {4, 3, 2, 4, 4};  // 17-19, (20: not bulk), 21: 17 with the L2 window
+  // 17-19, (20: not bulk), 21: 17 with the L2 window, 22 and 23: 17 and 18 with the
+  // split reduction
+  static const int kWant[7] = {4, 3, 2, 4, 4, 4, 3};
   if (m->bulk_fit < 0) {
     static std::once_flag attr_once;
     static int dyn_max = 0;  // opt-in shared memory less the kernels' static shared memory
@@ -1726,6 +1769,10 @@ static int bulk_per_sm(fg_mesh *m, int v) {
       if (cudaFuncSetAttribute(k_cg32s_spmv_bulk<ColRel>, cudaFuncAttributeMaxDynamicSharedMemorySize, d) !=
               cudaSuccess ||
           cudaFuncSetAttribute(k_cg32s_spmv_bulk<ColAbs>, cudaFuncAttributeMaxDynamicSharedMemorySize, d) !=
+              cudaSuccess ||
+          cudaFuncSetAttribute(k_cg32s_spmv_bulk<ColRel, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, d) !=
+              cudaSuccess ||
+          cudaFuncSetAttribute(k_cg32s_spmv_bulk<ColAbs, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, d) !=
               cudaSuccess) {
         cudaGetLastError();
         return;
@@ -1760,6 +1807,18 @@ static void bulk_launch32(fg_mesh *m, int v) {
       l2_launch(m, m->val32, k_cg32s_spmv_bulk<ColAbs>, g, 256, smem, m->nv, m->nslices, m->tmax256, m->sl_ptr,
                 m->sl_len, m->sl_col, m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl,
                 m->red.partials, m->red.counter);
+  } else if (v_splitred(v)) {
+    // per-block partials, then one block adds them and sets the scalars
+    if (m->use_dcol)
+      k_cg32s_spmv_bulk<ColRel, true><<<g, 256, smem, m->stream>>>(
+          m->nv, m->nslices, m->tmax256, m->sl_ptr, m->sl_len, m->sl_dcol, m->val32, m->v32[7], m->v32[4],
+          m->v32[5], m->scal, m->ictl, m->red.partials, m->red.counter);
+    else
+      k_cg32s_spmv_bulk<ColAbs, true><<<g, 256, smem, m->stream>>>(
+          m->nv, m->nslices, m->tmax256, m->sl_ptr, m->sl_len, m->sl_col, m->val32, m->v32[7], m->v32[4],
+          m->v32[5], m->scal, m->ictl, m->red.partials, m->red.counter);
+    k_cg32_dots_finish<<<1, 256, 0, m->stream>>>(reinterpret_cast<const float2 *>(m->red.partials), (int)g, m->scal,
+                                                 m->ictl);
   } else if (m->use_dcol)
     k_cg32s_spmv_bulk<ColRel><<<g, 256, smem, m->stream>>>(m->nv, m->nslices, m->tmax256, m->sl_ptr, m->sl_len,
                                                            m->sl_dcol, m->val32, m->v32[7], m->v32[4], m->v32[5],
@@ -1770,7 +1829,7 @@ static void bulk_launch32(fg_mesh *m, int v) {
                                                            m->scal, m->ictl, m->red.partials, m->red.counter);
 }
 
-// Blocks per SM of the pipelined variants 22 and 23 (4, 3 wanted), or 0 where two
+// Blocks per SM of the pipelined variants 24 and 25 (4, 3 wanted), or 0 where two
 // stages of a 256-row block do not fit; sized once per handle.
 static int pipe_per_sm(fg_mesh *m, int v) {
   if (m->pipe_fit < 0) {
@@ -1805,7 +1864,7 @@ static int pipe_per_sm(fg_mesh *m, int v) {
     }
     m->pipe_fit = per_sm;
   }
-  return std::min(m->pipe_fit, v == 22 ? 4 : 3);
+  return std::min(m->pipe_fit, v == 24 ? 4 : 3);
 }
 
 // Blocks of the pipelined variants' vector pass (four rows per thread), also the
@@ -2115,7 +2174,7 @@ static bool capture_iterations(fg_mesh *m, GraphCache &gc, int body, bool loop, 
 static int run_cg(fg_mesh *m, bool mixed, const fg_solve_opts &o, int *status, float *loop_ms = nullptr) {
   int block = o.check_every > 0 ? o.check_every : 32;
   if (block & 1) ++block;
-  const int per_iter = (mixed && !split32(m->spmv_variant32)) ? 1 : 2;
+  const int per_iter = (mixed && !split32(m->spmv_variant32)) ? 1 : (mixed && v_splitred(m->spmv_variant32)) ? 3 : 2;
   GraphCache &gc = m->graph[mixed ? 1 : 0];
   const bool use_graph = o.use_graph != 0;
   // programmatic-launch edges keep the host-checked blocks
@@ -2564,7 +2623,7 @@ fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_v
     reset_persisting_l2(m);
     const double us = loop_us_per_iteration(m, true, reps);
     if (us_per_variant) us_per_variant[v] = us;
-    if (us < best_us) { best_us = us; best = v; }
+    if (us < best_us && !v_pipe(v)) { best_us = us; best = v; }
   }
   m->spmv_variant32 = best;
   m->tuned32 = true;
@@ -2588,7 +2647,7 @@ fg_status fg_autotune_spmv64(fg_mesh *m, int reps, int *chosen, double *us_per_v
     // timed as the solver runs them
     const double us = loop_us_per_iteration(m, false, reps);
     if (us_per_variant) us_per_variant[v] = us;
-    if (us < best_us) { best_us = us; best = v; }
+    if (us < best_us && !v_pipe(v)) { best_us = us; best = v; }
   }
   m->spmv_variant64 = best;
   m->tuned64 = true;

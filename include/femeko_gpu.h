@@ -52,7 +52,7 @@ enum {
                           of |F(u + a du)|^2, kept in [0.1, 0.5] of the last step */
 };
 /* FP32 CG iteration kernel: FG_SPMV_AUTO lets the autotuner time the variants on
- * the first mixed solve of a handle and keep the fastest; k = 1..24 forces variant
+ * the first mixed solve of a handle and keep the fastest; k = 1..26 forces variant
  * k-1.  One fused kernel per iteration: 1: 4x-unrolled gather loop, 256 threads;
  * 2: all row loads issued first, 256 threads; 3: loop, 128 threads; 4: loop, 512
  * threads; 5: halo staging (the neighbour entries of a block of rows gathered once
@@ -70,10 +70,14 @@ enum {
  * second shared-memory stage by the bulk-copy engine while it computes the current
  * ones (available where two stages fit in shared memory); 21: 17 with its scaled
  * values in the persisting-L2 window; 22: 18 with the values in the window;
- * 23, 24: pipelined Jacobi-PCG (Ghysels-Vanroose): the dot products of an iteration
+ * 23, 24: 18 and 19 with each block of the SpMV leaving its partial dot products and
+ * a one-block kernel adding them (no arrival chain at the end of the SpMV);
+ * 25, 26: pipelined Jacobi-PCG (Ghysels-Vanroose): the dot products of an iteration
  * come from the previous vector pass and one block of the bulk-staged SpMV (4 or 3
  * blocks per SM) finishes their sum while the other blocks multiply, so no kernel
- * ends with a grid-wide reduction.
+ * ends with a grid-wide reduction.  25 and 26 are timed by the autotuner but never
+ * chosen by it (their FP32 recurrences stall above tolerances near 1e-6 and diverge
+ * on singular systems): they run only when forced.
  * The autotuner times each variant through the solver's own graph loop (64
  * iterations after an untimed run). */
 enum { FG_SPMV_AUTO = 0 };
@@ -89,7 +93,7 @@ typedef struct fg_solve_opts {
   int32_t use_graph;   /* 1: the whole CG as one CUDA graph launch (a WHILE node around
                           check_every iterations, the test on the device); 2: a graph of
                           check_every iterations per launch, tested on the host; 0: no graph */
-  int32_t spmv;        /* FG_SPMV_AUTO or a forced variant 1..24 */
+  int32_t spmv;        /* FG_SPMV_AUTO or a forced variant 1..26 */
   int32_t reserved_;
 } fg_solve_opts;
 
@@ -499,7 +503,7 @@ fg_status fg_bench_kernel(fg_mesh *m, int32_t which, int32_t precision, int32_t 
  * be NULL) the measured microseconds per launch.  No reference counterpart. */
 fg_status fg_autotune(fg_mesh *m, int32_t precision, int32_t *variant, double *us_per_variant, int32_t n_slots);
 /* Fixes the CG kernel variant of one precision for the handle (the numbering of
- * fg_solve_opts.spmv: FG_MIXED 1..24, FG_FP64 1..4), or 0 to return to the
+ * fg_solve_opts.spmv: FG_MIXED 1..26, FG_FP64 1..4), or 0 to return to the
  * autotuner's choice at the next solve.  The autotuner's choices are remembered per
  * process for each operator shape (device, rows, padded entries, longest row), so a
  * new handle for a mesh of the same structure does not time the variants again.
