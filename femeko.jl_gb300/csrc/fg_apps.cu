@@ -37,14 +37,16 @@ extern "C" fg_status fg_scalar_potential_newton(const double *p, int64_t nv, con
 //   which = 7: P1 stiffness assembly K(mu) at the handle's current permeabilities into
 //              the FP64 and FP32 SELL operator with its Jacobi diagonals (one pass,
 //              rows gather their elements' entries);
-//   which = 8: the same through element records and a row sum (the two-pass form).
+//   which = 8: the same through element records and a row sum (the two-pass form);
+//   which = 9: the one-block kernel that finishes the dot products of the
+//              split-reduction FP32 variants (which = 0 times their SpMV alone).
 fg_status fg_bench_cg_kernel(fg_mesh *m, int which, int precision, int reps, double *ms_per_launch);
 
 extern "C" fg_status fg_bench_kernel(fg_mesh *m, int32_t which, int32_t precision, int32_t reps,
                                      double *ms_per_launch) {
   return fg_guard([&]() -> fg_status {
     FG_REQUIRE(m && ms_per_launch && reps > 0, FG_BAD_ARG, "fg_bench_kernel: bad argument");
-    if (which == 0 || which == 1 || which == 3 || which == 6)
+    if (which == 0 || which == 1 || which == 3 || which == 6 || which == 9)
       return fg_bench_cg_kernel(m, which, precision, reps, ms_per_launch);
     if (which == 7 || which == 8) {
       FG_REQUIRE(m->npe == 4 && !m->edge && m->mu, FG_BAD_ARG,

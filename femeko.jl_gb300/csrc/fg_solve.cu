@@ -1903,6 +1903,28 @@ static void pipe_vec32(fg_mesh *m) {
       reinterpret_cast<float2 *>(m->red.partials));
 }
 
+// One of the two kernels of the split-reduction variants alone (for timing): the
+// SpMV that leaves per-block partials, or (finish) the one-block sum of them.
+static void launch_split_parts(fg_mesh *m, int v, bool finish) {
+  const int per_sm = bulk_per_sm(m, v);
+  FG_REQUIRE(per_sm > 0, FG_UNSUPPORTED, "bulk-staged SpMV: row blocks too large for shared memory");
+  const unsigned g = std::min<unsigned>(grid_for(m->nv, 256), (unsigned)per_sm * (unsigned)std::max(m->sm_count, 1));
+  if (finish) {
+    k_cg32_dots_finish<<<1, 256, 0, m->stream>>>(reinterpret_cast<const float2 *>(m->red.partials), (int)g, m->scal,
+                                                 m->ictl);
+    return;
+  }
+  const size_t smem = bulk_smem(m);
+  if (m->use_dcol)
+    k_cg32s_spmv_bulk<ColRel, true><<<g, 256, smem, m->stream>>>(
+        m->nv, m->nslices, m->tmax256, m->sl_ptr, m->sl_len, m->sl_dcol, m->val32, m->v32[7], m->v32[4], m->v32[5],
+        m->scal, m->ictl, m->red.partials, m->red.counter);
+  else
+    k_cg32s_spmv_bulk<ColAbs, true><<<g, 256, smem, m->stream>>>(
+        m->nv, m->nslices, m->tmax256, m->sl_ptr, m->sl_len, m->sl_col, m->val32, m->v32[7], m->v32[4], m->v32[5],
+        m->scal, m->ictl, m->red.partials, m->red.counter);
+}
+
 static void launch_spmv32s(fg_mesh *m, int v) {
   if (v_pipe(v)) {
     pipe_spmv32(m, v, true, m->pv32[2], m->pv32[1]);
@@ -2584,6 +2606,7 @@ fg_status fg_bench_cg_kernel(fg_mesh *m, int which, int precision, int reps, dou
   auto body = [&](int n) {
     for (int r = 0; r < n; ++r) {
       if (mixed && (!split32(v) || which == 3)) launch_iter32(m, v, (r & 1) != 0);
+      else if (mixed && (which == 0 || which == 9) && v_splitred(v)) launch_split_parts(m, v, which == 9);
       else if (mixed && which == 0) launch_spmv32s(m, v);
       else if (mixed) launch_vec32s(m, v);
       else if (which == 0) launch_spmv64cg(m);

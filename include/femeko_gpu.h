@@ -492,7 +492,9 @@ int64_t fg_kernel_launches(void);
  * 6 one whole CG iteration run the way the solver runs it (its graph loop; reps
  * iterations after an untimed run), 7 the P1 stiffness assembly K(mu) at the
  * handle's current permeabilities into the FP64 and FP32 operator (one pass over the
- * rows, after a solve), 8 the same assembly through element records and a row sum.
+ * rows, after a solve), 8 the same assembly through element records and a row sum,
+ * 9 the one-block kernel that adds the SpMV's per-block dot products in the
+ * split-reduction FP32 variants (for those, 0 times the SpMV kernel alone).
  * No reference counterpart (used for roofline reporting). */
 fg_status fg_bench_kernel(fg_mesh *m, int32_t which, int32_t precision, int32_t reps, double *ms_per_launch);
 /* Autotuner: times the CG kernel variants of one precision on the handle's current

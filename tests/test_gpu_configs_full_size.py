@@ -151,7 +151,7 @@ def test_c5_adjoint_64cube_linear_vs_cpu_adjoint_and_central_differences(adjoint
         for s in (+1, -1):
             mu2 = mur * MU0
             mu2[k] = (mur[k] + s * d) * MU0
-            u2, _, s2 = fg.magnetostatics_linear(m, mu2, u, precision="fp64", rtol=1e-12)
+            u2, _, s2 = fg.magnetostatics_linear(m, mu2, u, precision="fp64", rtol=1e-14)
             assert s2["converged"]
             us.append(u2)
         fd = O.objective_hx(m, target, us[0] - us[1]) / (2 * d)
