@@ -317,7 +317,8 @@ def run_ours(args):
              "split, bulk-staged entries, persistent 4/SM, dots finished by a one-block kernel",
              "split, bulk-staged entries, persistent 3/SM, dots finished by a one-block kernel",
              "pipelined CG, bulk-staged SpMV 4/SM, dots finished by one SpMV block (forced only)",
-             "pipelined CG, bulk-staged SpMV 3/SM, dots finished by one SpMV block (forced only)"]
+             "pipelined CG, bulk-staged SpMV 3/SM, dots finished by one SpMV block (forced only)",
+             "split iteration in one persistent cooperative launch, grid barriers, 4/SM"]
     variants_us = np.zeros(len(names))
     # the table of every variant on the converged operator (a second timing); the
     # per-kernel figures below are for the variant the timed solves used
@@ -381,7 +382,13 @@ def run_ours(args):
                 "two_pass_us": t_asm2.value * 1e3, "speedup_vs_two_pass": t_asm2.value / t_asm.value}
     n = mesh.nv
     v = int(used32.value) - 1
-    if v in (24, 25):
+    if v == 26:
+        # one launch runs whole iterations: the vector pass (28 B read, 20 B written per
+        # row) and w = A u with its dots (6 B per stored nonzero, u and r read, w
+        # written: 12 B per row); timed per iteration inside the solver's loop
+        alg_bytes = g.nnz * 6 + 60 * n
+        kname = "k_cg32_coop"
+    elif v in (24, 25):
         # pipelined CG, dominant kernel n = A m: FP32 value and 16-bit column per
         # stored nonzero; per row m read once and n written (8 B); no dot products
         alg_bytes = g.nnz * 6 + 8 * n
@@ -404,7 +411,8 @@ def run_ours(args):
         # and written (16 + 16 B) and p, x read and written (8 + 8 B)
         alg_bytes = g.nnz * 6 + 48 * n
         kname = {4: "k_cg32_iter_halo", 5: "k_cg32_iter_pipe"}.get(v, "k_cg32_iter")
-    achieved = alg_bytes / (ms_spmv.value * 1e-3) / 1e9
+    t_dom = ms_loop.value if v == 26 else ms_spmv.value
+    achieved = alg_bytes / (t_dom * 1e-3) / 1e9
     # DRAM bytes per launch of the same kernel from an ncu capture at 96^3: 10 and 20 =
     # the L2-window variants (warm L2), 14 = the grid of 10 without the window and
     # 17 = the bulk-staged SpMV (cold); other variants: none captured
@@ -416,7 +424,9 @@ def run_ours(args):
                 "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                 "traffic": traffic, "traffic_source": traffic_src, "algorithmic_bytes": alg_bytes,
-                "us_per_launch": ms_spmv.value * 1e3}
+                "us_per_launch": t_dom * 1e3,
+                "timing": ("one CG iteration of the persistent launch, in the solver's loop" if v == 26
+                           else "one launch, CUDA events on the library's stream")}
 
     # e2e through the one-shot C ABI with pinned host buffers
     e2e = None
@@ -866,7 +876,7 @@ def main():
     ap.add_argument("--graph-mode", type=int, default=1, choices=[0, 1, 2],
                     help="1: whole CG in one graph launch (device-side loop); 2: host-checked graph blocks; 0: no graph")
     ap.add_argument("--cg-variant", type=int, default=0,
-                    help="fix the FP32 CG kernel variant (1..26; 0: autotuned), e.g. for profiling runs")
+                    help="fix the FP32 CG kernel variant (1..27; 0: autotuned), e.g. for profiling runs")
     ap.add_argument("--cg64-variant", type=int, default=0, help="fix the FP64 CG SpMV variant (1..4; 0: autotuned)")
     ap.add_argument("--case", choices=sorted(CASES), default=None,
                     help="run a secondary workload instead of the headline benchmark")

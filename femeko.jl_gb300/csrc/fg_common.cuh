@@ -161,6 +161,8 @@ struct fg_mesh {
   int tmax256 = 0;    // most matrix entries (padded slots) of one 256-row block
   int bulk_fit = -1;  // resident CTAs per SM of the bulk-staged SpMV (-1: not sized yet)
   int pipe_fit = -1;  // the same for the pipelined CG's SpMV
+  int coop_fit = -1;  // the same for the cooperative persistent CG
+  unsigned *coop_bar = nullptr;  // its grid barrier: arrivals, generation
   int pipe_grid = 0;  // CTAs of the persistent pipelined iteration (0: not sized yet, -1: does not fit)
   int *halo_col = nullptr, *halo_len = nullptr;
   bool halo_tried = false;   // the halo lists are built at the first variant that needs them

@@ -783,6 +783,216 @@ __global__ void __launch_bounds__(256) k_cg32_dots_finish(const float2 *__restri
   }
 }
 
+// ------------------------------------------------------------------ FP32 CG, one launch
+// The split FP32 iteration (vector pass, then w = A u with its dot products) run by
+// ONE persistent cooperative launch for many iterations: the grid barrier between
+// the two phases and the one closing an iteration replace two kernel boundaries, the
+// last block to reach the closing barrier finishes the dot products (fixed order)
+// and sets the scalars before it releases the others, and each block's first two
+// row blocks of matrix entries are already in flight (bulk copies) while the vector
+// pass and the barriers run.  Every block handles the same 256-row blocks in both
+// phases, so a block reads back only its own vector writes; the gathers of u, written
+// by other blocks in this launch, bypass L1 (ld.global.cg).  Every wait is bounded:
+// a barrier or a copy that does not complete stops the CG with I_FAULT set.
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Waits (bounded) until the barrier generation differs from g; false on timeout.
+__device__ __forceinline__ bool coop_wait_gen(const unsigned *gen, unsigned g) {
+  for (int it = 0; it < (1 << 24); ++it) {
+    if (ld_acquire_u32(gen) != g) return true;
+    __nanosleep(32);
+  }
+  return false;
+}
+
+template <class CI>
+__global__ void __launch_bounds__(256) k_cg32_coop(int64_t n, int nslices, int cap, const int *__restrict__ sl_ptr,
+                                                   const int *__restrict__ sl_len,
+                                                   const typename CI::T *__restrict__ col,
+                                                   const float *__restrict__ val, float *__restrict__ r,
+                                                   float *__restrict__ w, float *__restrict__ s,
+                                                   float *__restrict__ p, float *__restrict__ u,
+                                                   float *__restrict__ x, const float *__restrict__ dinv,
+                                                   double *scal, int *ictl, float2 *partials, unsigned *bar,
+                                                   int iters) {
+  using T = typename CI::T;
+  using T4 = typename CI::T4;
+  extern __shared__ __align__(128) unsigned char sm_bulk[];
+  __shared__ __align__(8) uint64_t mbar[2];
+  __shared__ int s_last, s_ok;
+  const int tid = threadIdx.x;
+  const unsigned G = gridDim.x;
+  unsigned *count = bar, *gen = bar + 1;
+  const size_t o_col = pipe_align((size_t)cap * 4);
+  const size_t stage = o_col + pipe_align((size_t)cap * sizeof(T));
+  const int64_t nrb = (n + 255) / 256;
+  const int K = (int)((nrb - (int64_t)blockIdx.x + G - 1) / G);
+  auto rowblock = [&](int k) { return (int64_t)blockIdx.x + (int64_t)k * G; };
+  // matrix items are consumed in the order (iteration, row block); item q uses stage
+  // q & 1 and holds row block q mod K
+  const int64_t nitems = (int64_t)iters * K;
+  auto issue = [&](int64_t q) {
+    const int st = (int)(q & 1);
+    const int s0 = (int)(rowblock((int)(q % K)) * (256 / FG_SLICE)), s1 = min(s0 + 256 / FG_SLICE, nslices);
+    const int e0 = sl_ptr[s0], e1 = sl_ptr[s1];
+    const uint32_t vb = (uint32_t)(e1 - e0) * 4u, cb = (uint32_t)(e1 - e0) * (uint32_t)sizeof(T);
+    fence_proxy_async_smem();
+    mbar_arrive_expect_tx(&mbar[st], vb + cb);
+    bulk_g2s(sm_bulk + st * stage, val + e0, vb, &mbar[st]);
+    bulk_g2s(sm_bulk + st * stage + o_col, col + e0, cb, &mbar[st]);
+  };
+  if (tid == 0) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    fence_proxy_async_smem();
+  }
+  __syncthreads();
+  uint32_t inflight = 0u, phase = 0u;
+  // the first two items are in flight from the start, during the first vector pass
+  for (int64_t q = 0; q < 2 && q < nitems; ++q) {
+    if (tid == 0) issue(q);
+    inflight |= 1u << (q & 1);
+  }
+  int64_t qc = 0;  // items consumed
+  unsigned g_seen = ld_acquire_u32(gen);
+  bool ok = true;
+  // a barrier of every block (false when a wait ran out); with reduce_last, the last
+  // block to arrive adds the blocks' dot-product partials and sets the scalars first
+  auto barrier = [&](bool reduce_last) -> bool {
+    __syncthreads();
+    if (tid == 0) s_last = (atom_add_acq_rel(count, 1u) == G - 1) ? 1 : 0;
+    __syncthreads();
+    const bool last = s_last != 0;
+    if (last) {
+      if (reduce_last) {
+        ff acc[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+        for (unsigned k = tid; k < G; k += 256)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            const float2 v2 = __ldcg(partials + (size_t)k * 3 + j);
+            acc[j] = ff_add(acc[j], ff{v2.x, v2.y});
+          }
+        __shared__ ff shr[3][32];
+        block_sum_ff_pair<3>(acc, shr);
+        if (tid == 0) {
+          double tot[3];
+          for (int j = 0; j < 3; ++j) tot[j] = (double)acc[j].hi + (double)acc[j].lo;
+          cgcg_scalars(tot, scal, ictl);
+        }
+      }
+      if (tid == 0) {
+        *count = 0u;
+        st_release_u32(gen, g_seen + 1u);
+        s_ok = 1;
+      }
+    } else if (tid == 0) {
+      s_ok = coop_wait_gen(gen, g_seen) ? 1 : 0;
+    }
+    __syncthreads();
+    ++g_seen;
+    return s_ok != 0;
+  };
+  for (int itn = 0; itn < iters && ok; ++itn) {
+    if (__ldcg(ictl + I_DONE)) break;
+    // ---- vector pass on this block's rows
+    const float alpha = (float)__ldcg(scal + S_ALPHA), beta = (float)__ldcg(scal + S_BETA);
+    for (int k = 0; k < K; ++k) {
+      const int64_t i = rowblock(k) * 256 + tid;
+      if (i < n) {
+        const float ww = w[i], dd = dinv[i];
+        float ss = s[i], pp = p[i], xx = x[i], rr = r[i];
+        const float uu = u[i];
+        ss = fmaf(beta, ss, ww);
+        pp = fmaf(beta, pp, uu);
+        xx = fmaf(alpha, pp, xx);
+        rr = fmaf(-alpha, ss, rr);
+        s[i] = ss;
+        p[i] = pp;
+        x[i] = xx;
+        r[i] = rr;
+        u[i] = dd * rr;
+      }
+    }
+    if (!barrier(false)) { ok = false; break; }
+    // ---- w = A u and the dot products on this block's rows
+    Acc<float> dots[3];
+    for (int k = 0; k < K; ++k, ++qc) {
+      const int st = (int)(qc & 1);
+      const int64_t rb = rowblock(k);
+      const int64_t i = rb * 256 + tid;
+      const bool row = i < n;
+      int Gs = 0, base = 0;
+      float ui = 0.f, ri = 0.f;
+      if (row) {
+        const int sl = (int)(i >> 5);
+        Gs = sl_len[sl];
+        base = sl_ptr[sl] - sl_ptr[rb * (256 / FG_SLICE)] + (tid & 31) * FG_GROUP;
+        ui = u[i];
+        ri = r[i];
+      }
+      const bool got = mbar_wait(&mbar[st], (phase >> st) & 1u);
+      if (got) {
+        phase ^= 1u << st;
+        inflight &= ~(1u << st);
+      }
+      if (__syncthreads_or(!got)) { ok = false; break; }
+      if (row) {
+        const float *v = reinterpret_cast<const float *>(sm_bulk + st * stage);
+        const T *c = reinterpret_cast<const T *>(sm_bulk + st * stage + o_col);
+        float acc = 0.f;
+#pragma unroll 4
+        for (int gg = 0; gg < Gs; ++gg) {
+          const float4 vv = *reinterpret_cast<const float4 *>(v + base + gg * FG_SLICE * FG_GROUP);
+          const T4 cc = *reinterpret_cast<const T4 *>(c + base + gg * FG_SLICE * FG_GROUP);
+          acc = fmaf(vv.x, __ldcg(u + CI::col(cc.x, i)), acc);
+          acc = fmaf(vv.y, __ldcg(u + CI::col(cc.y, i)), acc);
+          acc = fmaf(vv.z, __ldcg(u + CI::col(cc.z, i)), acc);
+          acc = fmaf(vv.w, __ldcg(u + CI::col(cc.w, i)), acc);
+        }
+        w[i] = acc;
+        dots[0].add(ri * ui);
+        dots[1].add(acc * ui);
+        dots[2].add(ri * ri);
+      }
+      // every thread is done with the stage: refill it with item qc + 2 (the row
+      // block after next, or one of the next iteration's first two: the matrix does
+      // not change)
+      __syncthreads();
+      if (qc + 2 < nitems) {
+        if (tid == 0) issue(qc + 2);
+        inflight |= 1u << st;
+      }
+    }
+    if (!ok) break;
+    {
+      __shared__ ff shb[3][32];
+      ff v3[3] = {dots[0].v, dots[1].v, dots[2].v};
+      block_sum_ff_pair<3>(v3, shb);
+      if (tid == 0)
+        for (int j = 0; j < 3; ++j) partials[(size_t)blockIdx.x * 3 + j] = make_float2(v3[j].hi, v3[j].lo);
+    }
+    if (!barrier(true)) { ok = false; break; }
+  }
+  // drain the copies still in flight (the prefetch for an iteration that did not run)
+  if (tid == 0) {
+    for (int st = 0; st < 2; ++st)
+      if (inflight & (1u << st))
+        if (mbar_wait(&mbar[st], (phase >> st) & 1u, 1 << 20)) inflight &= ~(1u << st);
+    if (!ok || inflight) {
+      atomicExch(ictl + I_FAULT, 1);
+      atomicExch(ictl + I_DONE, 1);
+    }
+  }
+  __syncthreads();
+}
+
 // ------------------------------------------------------------------ FP32 pipelined CG
 // Pipelined Jacobi-PCG (Ghysels and Vanroose, "Hiding global synchronization latency
 // in the preconditioned Conjugate Gradient algorithm", Parallel Computing 40, 2014):
@@ -1474,8 +1684,10 @@ static void ensure_cg64(fg_mesh *m) {
 // and 3 blocks per SM).  The pipelined variants are timed by the autotuner but
 // never chosen by it: in FP32 their recurrences lose accuracy faster than CG's, so
 // inner solves asked for 1e-6 stall (Newton's tight Eisenstat-Walker steps), and on
-// singular systems they diverge; they run only when forced.
-constexpr int FG_N_SPMV32 = 26;
+// singular systems they diverge; they run only when forced.  26: the split iteration
+// of 22 run by one persistent cooperative launch for many iterations (grid barriers
+// in place of kernel boundaries, the matrix prefetched across them).
+constexpr int FG_N_SPMV32 = 27;
 // Split FP32 variants on the scaled system, with the values in the L2 window, and
 // with the matrix entries staged by bulk copies.
 static inline bool v_scaled(int v) { return v == 16 || v == 20; }
@@ -1484,6 +1696,7 @@ static inline bool v_bulk(int v) { return (v >= 17 && v <= 19) || v == 21 || v =
 static inline bool v_splitred(int v) { return v == 22 || v == 23; }
 static inline bool split32(int v) { return v >= 6; }
 static inline bool v_pipe(int v) { return v == 24 || v == 25; }
+static inline bool v_coop(int v) { return v == 26; }
 constexpr int FG_N_SPMV64 = 4;   // 0 direct gathers, 1 halo staging, 2/3 persistent with 4/8 blocks per SM
 
 template <class CI>
@@ -1926,6 +2139,12 @@ static void launch_split_parts(fg_mesh *m, int v, bool finish) {
 }
 
 static void launch_spmv32s(fg_mesh *m, int v) {
+  if (v_coop(v)) {
+    // outside the persistent launch (the first SpMV of a solve, kernel timings): the
+    // split-reduction SpMV and its one-block finish
+    bulk_launch32(m, 22);
+    return;
+  }
   if (v_pipe(v)) {
     pipe_spmv32(m, v, true, m->pv32[2], m->pv32[1]);
     return;
@@ -2193,7 +2412,86 @@ static bool capture_iterations(fg_mesh *m, GraphCache &gc, int body, bool loop, 
 // iterations are replayed with a host check of the done flag between them.
 // loop_ms (may be null): device time from the first launch to the end of the last
 // one, host checks included (the autotuner's measure of a variant).
+// Blocks per SM of the cooperative variant (4 wanted; 0 where two stages do not fit
+// or the device has no cooperative launch); sized once per handle.
+static int coop_per_sm(fg_mesh *m) {
+  if (m->coop_fit < 0) {
+    int coop = 0;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, m->device) != cudaSuccess) {
+      cudaGetLastError();
+      coop = 0;
+    }
+    int per_sm = 0;
+    const size_t smem = bulk_smem(m);
+    int dev_max = 0;
+    FG_CUDA_TRY(cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, m->device));
+    if (coop && m->tmax256 > 0 && smem + 1024 <= (size_t)dev_max) {
+      auto size = [&](auto kern) {
+        FG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        FG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem));
+      };
+      if (m->use_dcol) size(k_cg32_coop<ColRel>);
+      else size(k_cg32_coop<ColAbs>);
+    }
+    m->coop_fit = per_sm;
+  }
+  return std::min(m->coop_fit, 4);
+}
+
+// Launches the persistent cooperative CG for at most `iters` iterations (it stops
+// earlier at convergence, the cap or a fault).  Every block is resident (cooperative
+// launch), so its grid barriers cannot wait on a block that never runs.
+static void coop_launch32(fg_mesh *m, int iters) {
+  const int per_sm = coop_per_sm(m);
+  FG_REQUIRE(per_sm > 0, FG_UNSUPPORTED, "cooperative CG: not available on this operator or device");
+  const unsigned g = std::min<unsigned>(grid_for(m->nv, 256), (unsigned)per_sm * (unsigned)std::max(m->sm_count, 1));
+  if (!m->coop_bar) m->coop_bar = dev_alloc<unsigned>(m, 2);
+  FG_CUDA_TRY(cudaMemsetAsync(m->coop_bar, 0, 2 * sizeof(unsigned), m->stream));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(g);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = bulk_smem(m);
+  cfg.stream = m->stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  float2 *parts = reinterpret_cast<float2 *>(m->red.partials);
+  if (m->use_dcol)
+    FG_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_cg32_coop<ColRel>, (int64_t)m->nv, m->nslices, m->tmax256,
+                                   (const int *)m->sl_ptr, (const int *)m->sl_len, (const int16_t *)m->sl_dcol,
+                                   (const float *)m->val32, m->v32[4], m->v32[5], m->v32[6], m->v32[1], m->v32[7],
+                                   m->v32[0], (const float *)m->dinv32, m->scal, m->ictl, parts, m->coop_bar, iters));
+  else
+    FG_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_cg32_coop<ColAbs>, (int64_t)m->nv, m->nslices, m->tmax256,
+                                   (const int *)m->sl_ptr, (const int *)m->sl_len, (const int *)m->sl_col,
+                                   (const float *)m->val32, m->v32[4], m->v32[5], m->v32[6], m->v32[1], m->v32[7],
+                                   m->v32[0], (const float *)m->dinv32, m->scal, m->ictl, parts, m->coop_bar, iters));
+  FG_LAUNCHED(1);
+}
+
+// The solve loop of the cooperative variant: launches of up to 1024 iterations with a
+// host check of the done flag between them (no graph).
+static int run_cg_coop(fg_mesh *m, int *status, float *loop_ms) {
+  if (loop_ms) FG_CUDA_TRY(cudaEventRecord(m->ev0, m->stream));
+  for (;;) {
+    coop_launch32(m, 1024);
+    if (loop_ms) FG_CUDA_TRY(cudaEventRecord(m->ev1, m->stream));
+    FG_CUDA_TRY(cudaMemcpyAsync(m->hint, m->ictl, sizeof(int) * (I_BODIES + 1), cudaMemcpyDeviceToHost,
+                                m->stream));
+    fg_sync(m);
+    FG_REQUIRE(m->hint[I_FAULT] == 0, FG_CUDA,
+               "CG kernel: an asynchronous shared-memory copy or a grid barrier did not complete");
+    if (m->hint[I_DONE]) break;
+  }
+  if (status) *status = m->hint[I_STATUS];
+  if (loop_ms) FG_CUDA_TRY(cudaEventElapsedTime(loop_ms, m->ev0, m->ev1));
+  return std::max(m->hint[I_ITERS], 0);
+}
+
 static int run_cg(fg_mesh *m, bool mixed, const fg_solve_opts &o, int *status, float *loop_ms = nullptr) {
+  if (mixed && v_coop(m->spmv_variant32)) return run_cg_coop(m, status, loop_ms);
   int block = o.check_every > 0 ? o.check_every : 32;
   if (block & 1) ++block;
   const int per_iter = (mixed && !split32(m->spmv_variant32)) ? 1 : (mixed && v_splitred(m->spmv_variant32)) ? 3 : 2;
@@ -2313,6 +2611,7 @@ static bool variant32_available(fg_mesh *m, int v) {
   if (v == 5 && !pipe_available(m)) return false;
   if (v_bulk(v) && bulk_per_sm(m, v) == 0) return false;
   if (v_pipe(v) && pipe_per_sm(m, v) == 0) return false;
+  if (v_coop(v) && (coop_per_sm(m) == 0 || bulk_per_sm(m, 22) == 0)) return false;
   if (v_window(v) && !l2_supported(m)) return false;
   return true;
 }
