@@ -588,7 +588,8 @@ def case_newton_kernels(args):
         u, H, mu, st = fg.newton_magnetostatics(mesh, nl, mu_lin, u0, precision=prec)
         P = L.FG_MIXED if prec == "mixed" else L.FG_FP64
         for which, name in ((0, "cg_spmv"), (1, "cg_update"), (2, "newton_element_pass_all"),
-                            (4, "newton_residual_split"), (5, "newton_residual_jacobian_split")):
+                            (4, "newton_residual_split"), (5, "newton_residual_jacobian_split"),
+                            (7, "stiffness_assembly_one_pass")):
             t = C.c_double()
             L.check(lib.fg_bench_kernel(g.h, which, P, 5 if which < 2 else 3, C.byref(t)))
             out[f"{prec}_{name}_us"] = t.value * 1e3

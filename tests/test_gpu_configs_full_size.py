@@ -139,14 +139,16 @@ def test_c5_adjoint_64cube_linear_vs_cpu_adjoint_and_central_differences(adjoint
     go = go * MU0
     assert abs(J - O.objective_hx(m, target, uo)) <= 1e-9 * abs(J)
     assert np.abs(grad - go).max() <= 1e-7 * np.abs(go).max()
-    # central differences, relative step 1e-6, on 32 elements whose sensitivity is at
-    # least 1% of the largest; each perturbed solve starts from the converged u, so
-    # its relative tolerance applies to the perturbation itself
+    # central differences on 32 elements whose sensitivity is at least 1% of the
+    # largest.  Relative step 1e-4: the truncation error of a central difference is
+    # O(1e-8) relative, while the perturbed solves (from the converged u, stopped at
+    # 1e-14 of the right-hand side) leave a noise of about 1e-14 / 1e-4 relative in
+    # the difference; a step of 1e-6 raised that noise to 2e-5.
     rng = np.random.default_rng(11)
     pool = np.flatnonzero(np.abs(grad) >= 1e-2 * np.abs(grad).max())
     assert pool.size >= 32
     for k in rng.choice(pool, 32, replace=False):
-        d = 1e-6 * mur[k]
+        d = 1e-4 * mur[k]
         us = []
         for s in (+1, -1):
             mu2 = mur * MU0
