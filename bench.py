@@ -318,7 +318,9 @@ def run_ours(args):
              "split, bulk-staged entries, persistent 3/SM, dots finished by a one-block kernel",
              "pipelined CG, bulk-staged SpMV 4/SM, dots finished by one SpMV block (forced only)",
              "pipelined CG, bulk-staged SpMV 3/SM, dots finished by one SpMV block (forced only)",
-             "split iteration in one persistent cooperative launch, grid barriers, 4/SM"]
+             "split iteration in one persistent cooperative launch, grid barriers, 4/SM",
+             "split, bulk-staged entries, persistent 4/SM, dots finished by every block of the vector pass",
+             "split, bulk-staged entries, persistent 3/SM, dots finished by every block of the vector pass"]
     variants_us = np.zeros(len(names))
     # the table of every variant on the converged operator (a second timing); the
     # per-kernel figures below are for the variant the timed solves used
@@ -342,6 +344,11 @@ def run_ours(args):
         ms_fin = C.c_double()
         L.check(lib.fg_bench_kernel(g.h, 9, L.FG_MIXED, 200, C.byref(ms_fin)))
         kernels_us["cg32_dots_finish"] = ms_fin.value * 1e3
+    if int(used32.value) - 1 in (27, 28):
+        # the vector pass that first adds the SpMV's per-block partials (every block)
+        ms_vf = C.c_double()
+        L.check(lib.fg_bench_kernel(g.h, 1, L.FG_MIXED, 200, C.byref(ms_vf)))
+        kernels_us["cg32_vector_pass_with_dots_finish"] = ms_vf.value * 1e3
     for name, which in (("newton_element_pass_all_f32", 2), ("newton_residual_split", 4),
                         ("newton_residual_jacobian_split_f32", 5)):
         t = C.c_double()
@@ -405,7 +412,8 @@ def run_ours(args):
         alg_bytes = g.nnz * 6 + 12 * n
         kname = {7: "k_cg32s_spmv_halo", 17: "k_cg32s_spmv_bulk", 18: "k_cg32s_spmv_bulk",
                  19: "k_cg32s_spmv_bulk", 21: "k_cg32s_spmv_bulk",
-                 22: "k_cg32s_spmv_bulk<split>", 23: "k_cg32s_spmv_bulk<split>"}.get(v, "k_cg32s_spmv")
+                 22: "k_cg32s_spmv_bulk<split>", 23: "k_cg32s_spmv_bulk<split>",
+                 27: "k_cg32s_spmv_bulk<split>", 28: "k_cg32s_spmv_bulk<split>"}.get(v, "k_cg32s_spmv")
     else:
         # one fused iteration: matrix as above; per row the (r, w, s, dinv) state read
         # and written (16 + 16 B) and p, x read and written (8 + 8 B)
@@ -466,9 +474,31 @@ def run_ours(args):
         e2e_sec = max(ev0.elapsed_time(ev1) / 1000.0, time.time() - w0)
         h2d = p_np.nbytes + t_np.nbytes + fx_np.nbytes + nl_np.nbytes + mu_np.nbytes + u0_np.nbytes
         d2h = uo_np.nbytes + Ho_np.nbytes + muo_np.nbytes
+        # where an end-to-end call's time goes: the same four calls the one-shot entry
+        # point makes, each timed on the host after the device is idle (untimed above)
+        phases = {}
+        hm = C.c_void_p()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        L.check(lib.fg_mesh_create(L.ptr(p_np), mesh.nv, L.ptr(t_np), mesh.nt, 4, 0, C.byref(hm)))
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        L.check(lib.fg_mesh_set_dirichlet(hm, L.ptr(fx_np)))
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        L.check(lib.fg_newton_magnetostatics(hm, L.ptr(nl_np), L.ptr(mu_np), L.ptr(u0_np), C.byref(o), L.ptr(uo_np),
+                                             L.ptr(Ho_np), L.ptr(muo_np), C.byref(s)))
+        torch.cuda.synchronize()
+        t3 = time.perf_counter()
+        L.check(lib.fg_mesh_destroy(hm))
+        torch.cuda.synchronize()
+        t4 = time.perf_counter()
+        phases = {"mesh_create_upload_pattern": 1e3 * (t1 - t0), "set_dirichlet": 1e3 * (t2 - t1),
+                  "newton_solve_with_io": 1e3 * (t3 - t2), "destroy": 1e3 * (t4 - t3)}
         e2e = {"value": ws * args.e2e_steps / e2e_sec, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
-               "what": "fg_scalar_potential_newton: upload + pattern build + solve + download per step"}
+               "what": "fg_scalar_potential_newton: upload + pattern build + solve + download per step",
+               "phases_ms_one_call": {k: round(v, 3) for k, v in phases.items()}}
 
     cpu, acc_oracle = None, None
     if rank == 0 and not args.no_cpu_baseline:
@@ -612,8 +642,8 @@ def case_heat(args):
     T0 = np.exp(-(((mesh.p - x0[:, None]) ** 2).sum(axis=0)) / 0.5 ** 2)
     res = {}
     for prec in ("fp64", "mixed"):
-        fg.heat_be(mesh, T0, kappa, nsteps=2, every=0, precision=prec)          # warm-up
-        T, snaps, st = fg.heat_be(mesh, T0, kappa, nsteps=100, every=10, precision=prec)
+        fg.heat_be(mesh, T0, kappa, nsteps=2, every=0, precision=prec, use_graph=args.graph_mode)   # warm-up
+        T, snaps, st = fg.heat_be(mesh, T0, kappa, nsteps=100, every=10, precision=prec, use_graph=args.graph_mode)
         res[prec] = (snaps, st)
     err = [float(np.linalg.norm(a - b) / np.linalg.norm(b)) for a, b in zip(res["mixed"][0], res["fp64"][0])]
     ms_m, ms_d = res["mixed"][1]["ms"], res["fp64"][1]["ms"]
@@ -877,7 +907,7 @@ def main():
     ap.add_argument("--graph-mode", type=int, default=1, choices=[0, 1, 2],
                     help="1: whole CG in one graph launch (device-side loop); 2: host-checked graph blocks; 0: no graph")
     ap.add_argument("--cg-variant", type=int, default=0,
-                    help="fix the FP32 CG kernel variant (1..27; 0: autotuned), e.g. for profiling runs")
+                    help="fix the FP32 CG kernel variant (1..29; 0: autotuned), e.g. for profiling runs")
     ap.add_argument("--cg64-variant", type=int, default=0, help="fix the FP64 CG SpMV variant (1..4; 0: autotuned)")
     ap.add_argument("--case", choices=sorted(CASES), default=None,
                     help="run a secondary workload instead of the headline benchmark")

@@ -995,7 +995,10 @@ __global__ void __launch_bounds__(128) k_asm_rows_tet4(int64_t nv, int64_t nt, c
           g[j][b] = geo[(int64_t)(13 + (lo * (9 - lo)) / 2 + hi - lo) * nt + k];
         }
       }
-      if (KIND == ASM_MASS || KIND == ASM_HEAT) mk[j] = (KIND == ASM_MASS ? fk : cm) * ve / 20.0;
+      // times 1/20 rather than a division: an FP64 division is a long instruction
+      // sequence on a pipe that runs at 1/64 of the FP32 rate (the product differs from
+      // the quotient by at most an ulp)
+      if (KIND == ASM_MASS || KIND == ASM_HEAT) mk[j] = (KIND == ASM_MASS ? fk : cm) * ve * 0.05;
     }
 #pragma unroll
     for (int j = 0; j < U; ++j) {
