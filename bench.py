@@ -318,9 +318,7 @@ def run_ours(args):
              "split, bulk-staged entries, persistent 3/SM, dots finished by a one-block kernel",
              "pipelined CG, bulk-staged SpMV 4/SM, dots finished by one SpMV block (forced only)",
              "pipelined CG, bulk-staged SpMV 3/SM, dots finished by one SpMV block (forced only)",
-             "split iteration in one persistent cooperative launch, grid barriers, 4/SM",
-             "split, bulk-staged entries, persistent 4/SM, dots finished by every block of the vector pass",
-             "split, bulk-staged entries, persistent 3/SM, dots finished by every block of the vector pass"]
+             "split iteration in one persistent cooperative launch, grid barriers, 4/SM"]
     variants_us = np.zeros(len(names))
     # the table of every variant on the converged operator (a second timing); the
     # per-kernel figures below are for the variant the timed solves used
@@ -344,11 +342,6 @@ def run_ours(args):
         ms_fin = C.c_double()
         L.check(lib.fg_bench_kernel(g.h, 9, L.FG_MIXED, 200, C.byref(ms_fin)))
         kernels_us["cg32_dots_finish"] = ms_fin.value * 1e3
-    if int(used32.value) - 1 in (27, 28):
-        # the vector pass that first adds the SpMV's per-block partials (every block)
-        ms_vf = C.c_double()
-        L.check(lib.fg_bench_kernel(g.h, 1, L.FG_MIXED, 200, C.byref(ms_vf)))
-        kernels_us["cg32_vector_pass_with_dots_finish"] = ms_vf.value * 1e3
     for name, which in (("newton_element_pass_all_f32", 2), ("newton_residual_split", 4),
                         ("newton_residual_jacobian_split_f32", 5)):
         t = C.c_double()
@@ -412,8 +405,7 @@ def run_ours(args):
         alg_bytes = g.nnz * 6 + 12 * n
         kname = {7: "k_cg32s_spmv_halo", 17: "k_cg32s_spmv_bulk", 18: "k_cg32s_spmv_bulk",
                  19: "k_cg32s_spmv_bulk", 21: "k_cg32s_spmv_bulk",
-                 22: "k_cg32s_spmv_bulk<split>", 23: "k_cg32s_spmv_bulk<split>",
-                 27: "k_cg32s_spmv_bulk<split>", 28: "k_cg32s_spmv_bulk<split>"}.get(v, "k_cg32s_spmv")
+                 22: "k_cg32s_spmv_bulk<split>", 23: "k_cg32s_spmv_bulk<split>"}.get(v, "k_cg32s_spmv")
     else:
         # one fused iteration: matrix as above; per row the (r, w, s, dinv) state read
         # and written (16 + 16 B) and p, x read and written (8 + 8 B)
@@ -428,13 +420,30 @@ def run_ours(args):
     if traffic is None and args.cells == 96 and v in (10, 14, 17, 20):
         traffic = {10: 70.73e6, 14: 97.07e6, 17: 97.38e6, 20: 69.70e6}[v]
         traffic_src = "ncu dram__bytes_read.sum + dram__bytes_write.sum of this kernel at 96^3"
+    # the whole CG iteration in the solver's loop (every kernel of it): the dominant
+    # SpMV's bytes plus the vector pass's (split: 28 B read + 20 B written per row;
+    # Jacobi-scaled system: 20 + 16 B; fused: counted in the kernel above)
+    if v in (24, 25):
+        it_bytes = None
+    elif v in (16, 20):
+        it_bytes = g.nnz * 6 + 12 * n + 36 * n
+    elif v >= 6 and v != 26:
+        it_bytes = g.nnz * 6 + 12 * n + 48 * n
+    else:
+        it_bytes = alg_bytes
+    it_roof = None
+    if it_bytes is not None:
+        it_gbs = it_bytes / (ms_loop.value * 1e-3) / 1e9
+        it_roof = {"algorithmic_bytes": it_bytes, "us_per_iteration": ms_loop.value * 1e3, "achieved": it_gbs,
+                   "frac": it_gbs / peak, "timing": "CG iterations in the solver's graph loop, CUDA events"}
     roofline = {"bound": "hbm", "kernel": kname, "variant": autotune["names"][v],
                 "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                 "traffic": traffic, "traffic_source": traffic_src, "algorithmic_bytes": alg_bytes,
                 "us_per_launch": t_dom * 1e3,
                 "timing": ("one CG iteration of the persistent launch, in the solver's loop" if v == 26
-                           else "one launch, CUDA events on the library's stream")}
+                           else "one launch, CUDA events on the library's stream"),
+                "cg_iteration": it_roof}
 
     # e2e through the one-shot C ABI with pinned host buffers
     e2e = None
@@ -907,7 +916,7 @@ def main():
     ap.add_argument("--graph-mode", type=int, default=1, choices=[0, 1, 2],
                     help="1: whole CG in one graph launch (device-side loop); 2: host-checked graph blocks; 0: no graph")
     ap.add_argument("--cg-variant", type=int, default=0,
-                    help="fix the FP32 CG kernel variant (1..29; 0: autotuned), e.g. for profiling runs")
+                    help="fix the FP32 CG kernel variant (1..27; 0: autotuned), e.g. for profiling runs")
     ap.add_argument("--cg64-variant", type=int, default=0, help="fix the FP64 CG SpMV variant (1..4; 0: autotuned)")
     ap.add_argument("--case", choices=sorted(CASES), default=None,
                     help="run a secondary workload instead of the headline benchmark")

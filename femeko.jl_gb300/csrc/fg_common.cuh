@@ -163,7 +163,6 @@ struct fg_mesh {
   int pipe_fit = -1;  // the same for the pipelined CG's SpMV
   int coop_fit = -1;  // the same for the cooperative persistent CG
   unsigned *coop_bar = nullptr;  // its grid barrier: arrivals, generation
-  double *cgslot = nullptr;      // FP32 CG finished by the vector pass: scalar state by iteration parity
   int pipe_grid = 0;  // CTAs of the persistent pipelined iteration (0: not sized yet, -1: does not fit)
   int *halo_col = nullptr, *halo_len = nullptr;
   bool halo_tried = false;   // the halo lists are built at the first variant that needs them

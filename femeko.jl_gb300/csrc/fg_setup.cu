@@ -110,10 +110,27 @@ __global__ void k_fill_inc(const int *__restrict__ t, int64_t nt, int npe, const
 
 // Sort each node's incidence list by (element, local) so that every later pass
 // visits contributions in one fixed order (deterministic sums).
+// Lists of up to 64 incidences are sorted in a thread-local array (one read and one
+// write of the list in global memory instead of a dependent global round trip per
+// shift); longer ones in place.
 __global__ void k_sort_inc(const int *__restrict__ iptr, int *__restrict__ inc, int64_t nv) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nv) return;
-  int b = iptr[i], e = iptr[i + 1];
+  const int b = iptr[i], e = iptr[i + 1];
+  constexpr int CAP = 64;
+  if (e - b <= CAP) {
+    int loc[CAP];
+    const int n = e - b;
+    for (int q = 0; q < n; ++q) loc[q] = inc[b + q];
+    for (int q = 1; q < n; ++q) {
+      const int key = loc[q];
+      int r = q - 1;
+      while (r >= 0 && loc[r] > key) { loc[r + 1] = loc[r]; --r; }
+      loc[r + 1] = key;
+    }
+    for (int q = 0; q < n; ++q) inc[b + q] = loc[q];
+    return;
+  }
   for (int q = b + 1; q < e; ++q) {
     int key = inc[q];
     int r = q - 1;

@@ -826,89 +826,6 @@ __global__ void __launch_bounds__(256) k_cg32_dots_finish(const float2 *__restri
   }
 }
 
-// The vector pass of the split-reduction SpMV variants that finish the dot products
-// themselves: every block sums the SpMV's nparts per-block partials, in the order and
-// with the arithmetic of k_cg32_dots_finish (so the scalars, and the iterates, are
-// bit-identical to that variant's), derives alpha and beta, and applies the update;
-// the one-block kernel and its two kernel boundaries per iteration go away.  The
-// partials (a few kB) come from L2 while the block's first vector loads are in
-// flight.  A grid of resident blocks (4 per SM) walks the rows with a grid stride, so
-// each block sums the partials once.
-// Blocks of one launch must not read a scalar state that another block of the same
-// launch writes, so the state (previous gamma and alpha, threshold, count) is kept in
-// two slots by iteration parity: blocks read slots[4 * parity], block 0 writes
-// slots[4 * (1 - parity)] and the run's scalars (read by the host and by the loop's
-// done test).  A block that finds the run done (an earlier iteration, or block 0 of
-// this launch that has just set it: the same decision every block reaches) leaves
-// without writing; the exit is decided block-wide.
-__device__ __forceinline__ void cg32_vec_update(float alpha, float beta, float4 ww, float4 dd, float4 uu, float4 ss,
-                                                float4 pp, float4 xx, float4 rr, float4 *__restrict__ r,
-                                                float4 *__restrict__ s, float4 *__restrict__ p,
-                                                float4 *__restrict__ u, float4 *__restrict__ x, int64_t j) {
-  ss.x = fmaf(beta, ss.x, ww.x); ss.y = fmaf(beta, ss.y, ww.y); ss.z = fmaf(beta, ss.z, ww.z); ss.w = fmaf(beta, ss.w, ww.w);
-  pp.x = fmaf(beta, pp.x, uu.x); pp.y = fmaf(beta, pp.y, uu.y); pp.z = fmaf(beta, pp.z, uu.z); pp.w = fmaf(beta, pp.w, uu.w);
-  xx.x = fmaf(alpha, pp.x, xx.x); xx.y = fmaf(alpha, pp.y, xx.y); xx.z = fmaf(alpha, pp.z, xx.z); xx.w = fmaf(alpha, pp.w, xx.w);
-  rr.x = fmaf(-alpha, ss.x, rr.x); rr.y = fmaf(-alpha, ss.y, rr.y); rr.z = fmaf(-alpha, ss.z, rr.z); rr.w = fmaf(-alpha, ss.w, rr.w);
-  s[j] = ss;
-  p[j] = pp;
-  x[j] = xx;
-  r[j] = rr;
-  u[j] = make_float4(dd.x * rr.x, dd.y * rr.y, dd.z * rr.z, dd.w * rr.w);
-}
-
-__global__ void __launch_bounds__(256, 4) k_cg32s_vec_fin(int64_t n4, float4 *__restrict__ r,
-                                                          const float4 *__restrict__ w, float4 *__restrict__ s,
-                                                          float4 *__restrict__ p, float4 *__restrict__ u,
-                                                          float4 *__restrict__ x, const float4 *__restrict__ dinv,
-                                                          const float2 *__restrict__ partials, int nparts,
-                                                          double *scal, int *ictl, double *slots, int parity) {
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  // the flag, the first vectors and the partials are loaded together
-  const int done = ictl[I_DONE];
-  float4 ww = {}, dd = {}, uu = {}, ss = {}, pp = {}, xx = {}, rr = {};
-  if (j < n4) {
-    ww = w[j];
-    dd = dinv[j];
-    uu = u[j];
-    ss = s[j];
-    pp = p[j];
-    xx = x[j];
-    rr = r[j];
-  }
-  ff acc[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-  sum_partials_ff3<3>(partials, nparts, acc);
-  if (__syncthreads_or(done)) return;
-  __shared__ ff shr[3][32];
-  __shared__ float s_ab[2];
-  __shared__ int s_skip;
-  block_sum_ff_pair<3>(acc, shr);
-  if (threadIdx.x == 0) {
-    double tot[3];
-#pragma unroll
-    for (int q3 = 0; q3 < 3; ++q3) tot[q3] = (double)acc[q3].hi + (double)acc[q3].lo;
-    const double *in = slots + 4 * parity;
-    const CgNext o = cgcg_next(tot, in[0], in[1], in[2], (int)in[3], ictl[I_MAXIT]);
-    if (blockIdx.x == 0) {
-      double *out = slots + 4 * (1 - parity);
-      out[0] = o.gam;
-      out[1] = o.alpha;
-      out[2] = o.tol2;
-      out[3] = (double)o.it;
-      cgcg_store(o, scal, ictl);
-    }
-    s_ab[0] = (float)o.alpha;
-    s_ab[1] = (float)o.beta;
-    s_skip = (o.done == 1) ? 1 : 0;
-  }
-  __syncthreads();
-  if (s_skip) return;
-  const float alpha = s_ab[0], beta = s_ab[1];
-  if (j < n4) cg32_vec_update(alpha, beta, ww, dd, uu, ss, pp, xx, rr, r, s, p, u, x, j);
-  for (j += stride; j < n4; j += stride)
-    cg32_vec_update(alpha, beta, w[j], dinv[j], u[j], s[j], p[j], x[j], r[j], r, s, p, u, x, j);
-}
-
 // ------------------------------------------------------------------ FP32 CG, one launch
 // The split FP32 iteration (vector pass, then w = A u with its dot products) run by
 // ONE persistent cooperative launch for many iterations: the grid barrier between
@@ -1446,7 +1363,7 @@ __global__ void k_axpy_scaled_to64(int64_t n, double scale, const float *__restr
 __global__ void k_cg32s_init(int64_t n, int64_t np, const double *__restrict__ rin, double scale,
                              const float *__restrict__ dinv, float *__restrict__ r, float *__restrict__ u,
                              float *__restrict__ s, float *__restrict__ p, float *__restrict__ x, double tol2_rel,
-                             int maxit, double *scal, int *ictl, double *slots) {
+                             int maxit, double *scal, int *ictl) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < np; i += stride) {
     const float ri = (i < n) ? (float)(scale * rin[i]) : 0.f;
@@ -1457,12 +1374,6 @@ __global__ void k_cg32s_init(int64_t n, int64_t np, const double *__restrict__ r
     x[i] = 0.f;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    if (slots) {  // the state the first vector pass with finish reads (parity 0)
-      slots[0] = 0.0;
-      slots[1] = 0.0;
-      slots[2] = tol2_rel;
-      slots[3] = -1.0;
-    }
     scal[S_TOL2] = tol2_rel;
     scal[S_ALPHA] = 0.0;
     scal[S_BETA] = 0.0;
@@ -1792,10 +1703,6 @@ static void ensure_cg32(fg_mesh *m) {
       m->pv32[j] = dev_alloc<float>(m, (size_t)m->nvp);
       FG_CUDA_TRY(cudaMemsetAsync(m->pv32[j], 0, sizeof(float) * (size_t)m->nvp, m->stream));
     }
-  if (!m->cgslot) {
-    m->cgslot = dev_alloc<double>(m, 8);
-    FG_CUDA_TRY(cudaMemsetAsync(m->cgslot, 0, 8 * sizeof(double), m->stream));
-  }
 }
 static void ensure_cg64(fg_mesh *m) {
   const int idx[6] = {0, 1, 2, 3, 4, 12};
@@ -1822,18 +1729,14 @@ static void ensure_cg64(fg_mesh *m) {
 // inner solves asked for 1e-6 stall (Newton's tight Eisenstat-Walker steps), and on
 // singular systems they diverge; they run only when forced.  26: the split iteration
 // of 22 run by one persistent cooperative launch for many iterations (grid barriers
-// in place of kernel boundaries, the matrix prefetched across them).  27 and 28:
-// variants 22 and 23 with the dot products finished by every block of the next
-// vector pass instead of a one-block kernel (bit-identical iterates, one kernel less
-// per iteration).
-constexpr int FG_N_SPMV32 = 29;
+// in place of kernel boundaries, the matrix prefetched across them).
+constexpr int FG_N_SPMV32 = 27;
 // Split FP32 variants on the scaled system, with the values in the L2 window, and
 // with the matrix entries staged by bulk copies.
 static inline bool v_scaled(int v) { return v == 16 || v == 20; }
 static inline bool v_window(int v) { return v == 10 || v == 20 || v == 21; }
-static inline bool v_bulk(int v) { return (v >= 17 && v <= 19) || (v >= 21 && v <= 23) || v == 27 || v == 28; }
-static inline bool v_splitred(int v) { return v == 22 || v == 23 || v == 27 || v == 28; }
-static inline bool v_vecfin(int v) { return v == 27 || v == 28; }
+static inline bool v_bulk(int v) { return (v >= 17 && v <= 19) || (v >= 21 && v <= 23); }
+static inline bool v_splitred(int v) { return v == 22 || v == 23; }
 static inline bool split32(int v) { return v >= 6; }
 static inline bool v_pipe(int v) { return v == 24 || v == 25; }
 static inline bool v_coop(int v) { return v == 26; }
@@ -2104,9 +2007,8 @@ static size_t bulk_smem(const fg_mesh *m) {
 // device's opt-in shared memory (set once per process).
 static int bulk_per_sm(fg_mesh *m, int v) {
   // 17-19, (20: not bulk), 21: 17 with the L2 window, 22 and 23: 17 and 18 with the
-  // split reduction, (24-26: sized elsewhere), 27 and 28: 22 and 23 finished by the
-  // vector pass
-  static const int kWant[12] = {4, 3, 2, 4, 4, 4, 3, 4, 3, 4, 4, 3};
+  // split reduction
+  static const int kWant[7] = {4, 3, 2, 4, 4, 4, 3};
   if (m->bulk_fit < 0) {
     static std::once_flag attr_once;
     static int dyn_max = 0;  // opt-in shared memory less the kernels' static shared memory
@@ -2171,9 +2073,8 @@ static void bulk_launch32(fg_mesh *m, int v) {
       k_cg32s_spmv_bulk<ColAbs, true><<<g, 256, smem, m->stream>>>(
           m->nv, m->nslices, m->tmax256, m->sl_ptr, m->sl_len, m->sl_col, m->val32, m->v32[7], m->v32[4],
           m->v32[5], m->scal, m->ictl, m->red.partials, m->red.counter);
-    if (!v_vecfin(v))
-      k_cg32_dots_finish<<<1, 256, 0, m->stream>>>(reinterpret_cast<const float2 *>(m->red.partials), (int)g,
-                                                   m->scal, m->ictl);
+    k_cg32_dots_finish<<<1, 256, 0, m->stream>>>(reinterpret_cast<const float2 *>(m->red.partials), (int)g, m->scal,
+                                                 m->ictl);
   } else if (m->use_dcol)
     k_cg32s_spmv_bulk<ColRel><<<g, 256, smem, m->stream>>>(m->nv, m->nslices, m->tmax256, m->sl_ptr, m->sl_len,
                                                            m->sl_dcol, m->val32, m->v32[7], m->v32[4], m->v32[5],
@@ -2364,24 +2265,9 @@ static void launch_spmv32s(fg_mesh *m, int v) {
                m->ictl, m->red.partials, m->red.counter);
 }
 
-// Grid of the bulk-staged SpMV of variant v (its number of per-block partials).
-static unsigned bulk_grid(fg_mesh *m, int v) {
-  return std::min<unsigned>(grid_for(m->nv, 256), (unsigned)bulk_per_sm(m, v) * (unsigned)std::max(m->sm_count, 1));
-}
-
-static void launch_vec32s(fg_mesh *m, int v, int parity) {
+static void launch_vec32s(fg_mesh *m, int v) {
   if (v_pipe(v)) {
     pipe_vec32(m);
-    return;
-  }
-  if (v_vecfin(v)) {
-    const unsigned g = std::min<unsigned>(grid_for(m->nvp / 4, 256), 4u * (unsigned)std::max(m->sm_count, 1));
-    k_cg32s_vec_fin<<<g, 256, 0, m->stream>>>(
-        m->nvp / 4, reinterpret_cast<float4 *>(m->v32[4]), reinterpret_cast<const float4 *>(m->v32[5]),
-        reinterpret_cast<float4 *>(m->v32[6]), reinterpret_cast<float4 *>(m->v32[1]),
-        reinterpret_cast<float4 *>(m->v32[7]), reinterpret_cast<float4 *>(m->v32[0]),
-        reinterpret_cast<const float4 *>(m->dinv32), reinterpret_cast<const float2 *>(m->red.partials),
-        (int)bulk_grid(m, v), m->scal, m->ictl, m->cgslot, parity & 1);
     return;
   }
   if (v_scaled(v)) {
@@ -2404,11 +2290,11 @@ static void launch_iter32(fg_mesh *m, int v, bool from_first_buffer) {
     // the SpMV (its first block finishing the last vector pass's dots), then the
     // vector pass with those scalars
     launch_spmv32s(m, v);
-    launch_vec32s(m, v, 0);
+    launch_vec32s(m, v);
     return;
   }
   if (split32(v)) {
-    launch_vec32s(m, v, from_first_buffer ? 1 : 0);
+    launch_vec32s(m, v);
     launch_spmv32s(m, v);
     return;
   }
@@ -2480,10 +2366,8 @@ static void start_cg(fg_mesh *m, bool mixed, const double *r64, double scale, do
     pipe_vec32(m);
     FG_LAUNCHED(1);
   } else if (mixed && split32(m->spmv_variant32)) {
-    ensure_cg32(m);
     k_cg32s_init<<<g, 256, 0, m->stream>>>(m->nv, m->nvp, r64, scale, m->dinv32, m->v32[4], m->v32[7], m->v32[6],
-                                           m->v32[1], m->v32[0], tol2_rel, maxit, m->scal, m->ictl,
-                                           v_vecfin(m->spmv_variant32) ? m->cgslot : nullptr);
+                                           m->v32[1], m->v32[0], tol2_rel, maxit, m->scal, m->ictl);
     launch_spmv32s(m, m->spmv_variant32);
   } else if (mixed) {
     k_cg32_init<<<g, 256, 0, m->stream>>>(m->nv, m->nvp, r64, scale, m->dinv32,
@@ -2653,8 +2537,7 @@ static int run_cg(fg_mesh *m, bool mixed, const fg_solve_opts &o, int *status, f
   if (mixed && v_coop(m->spmv_variant32)) return run_cg_coop(m, status, loop_ms);
   int block = o.check_every > 0 ? o.check_every : 32;
   if (block & 1) ++block;
-  const int v32 = m->spmv_variant32;
-  const int per_iter = (mixed && !split32(v32)) ? 1 : (mixed && v_splitred(v32) && !v_vecfin(v32)) ? 3 : 2;
+  const int per_iter = (mixed && !split32(m->spmv_variant32)) ? 1 : (mixed && v_splitred(m->spmv_variant32)) ? 3 : 2;
   GraphCache &gc = m->graph[mixed ? 1 : 0];
   const bool use_graph = o.use_graph != 0;
   // programmatic-launch edges keep the host-checked blocks
@@ -3067,7 +2950,7 @@ fg_status fg_bench_cg_kernel(fg_mesh *m, int which, int precision, int reps, dou
       if (mixed && (!split32(v) || which == 3)) launch_iter32(m, v, (r & 1) != 0);
       else if (mixed && (which == 0 || which == 9) && v_splitred(v)) launch_split_parts(m, v, which == 9);
       else if (mixed && which == 0) launch_spmv32s(m, v);
-      else if (mixed) launch_vec32s(m, v, r & 1);
+      else if (mixed) launch_vec32s(m, v);
       else if (which == 0) launch_spmv64cg(m);
       else if (which == 1) launch_vec64(m);
       else { launch_vec64(m); launch_spmv64cg(m); }
@@ -3089,12 +2972,16 @@ fg_status fg_bench_cg_kernel(fg_mesh *m, int which, int precision, int reps, dou
 // Autotuner: times every FP32 CG iteration variant on the handle's current operator,
 // each run as the solver runs it (CUDA events around its graph loop), and keeps the
 // fastest for the handle.  Runs at the first mixed-precision solve of an operator
-// shape (or on request).
+// shape (or on request).  The variants that hold their values in a persisting-L2
+// window set L2 aside for the whole context (every other kernel of the process
+// loses it): one is kept only when it beats the fastest variant without a window
+// by more than kWindowMargin.  The pipelined variants are never kept.
+constexpr double kWindowMargin = 0.05;
 fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_variant) {
   FG_REQUIRE(m->val32 != nullptr, FG_BAD_ARG, "autotune: no FP32 operator assembled");
   reps = std::max(64, (reps + 31) / 32 * 32);  // whole bodies of the solver's graph loop
-  int best = 0;
-  double best_us = 1e30;
+  int best = 0, best_win = -1;
+  double best_us = 1e30, best_win_us = 1e30;
   for (int v = 0; v < FG_N_SPMV32; ++v) {
     if (!variant32_available(m, v) || (v_window(v) && !prepare_l2(m))) {  // not available here
       if (us_per_variant) us_per_variant[v] = 0.0;
@@ -3105,8 +2992,15 @@ fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_v
     reset_persisting_l2(m);
     const double us = loop_us_per_iteration(m, true, reps);
     if (us_per_variant) us_per_variant[v] = us;
-    if (us < best_us && !v_pipe(v)) { best_us = us; best = v; }
+    if (v_pipe(v)) continue;
+    if (v_window(v)) {
+      if (us < best_win_us) { best_win_us = us; best_win = v; }
+    } else if (us < best_us) {
+      best_us = us;
+      best = v;
+    }
   }
+  if (best_win >= 0 && best_win_us < (1.0 - kWindowMargin) * best_us) best = best_win;
   m->spmv_variant32 = best;
   m->tuned32 = true;
   if (chosen) *chosen = best;

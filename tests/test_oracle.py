@@ -351,3 +351,51 @@ def test_oracle_scalar_potential_patch_test():
     exact = -(Hext[:, None] * m.p).sum(axis=0)
     d = u - exact
     assert np.abs(d - d.mean()).max() < 1e-10 * np.abs(exact).max()
+
+
+def test_nedelec_reference_orientation_null_space():
+    """The reference orients each element's six edges locally (src/mesh.jl:603-630),
+    so elements sharing an edge may disagree: its curl-curl matrix is not that of a
+    conforming edge space.  With one orientation per edge (low to high vertex) the
+    null space is the discrete gradients, (vertices - 1)-dimensional; with the
+    reference's it is smaller and the gradients are not in it."""
+    import scipy.linalg as la
+    m = box_tet_mesh(3, seed=6, order=2)
+    edges, ne = O.nedelec_edges(m)
+    t = np.asarray(m.t[:4])
+    loc = [(0, 1), (1, 2), (2, 0), (3, 0), (2, 3), (1, 3)]
+    A = O.nedelecStiffness(m).toarray()
+    Ak = O.nedelecLocalStiffness(m)
+    S = np.array([np.where(t[a] < t[b], 1.0, -1.0) for a, b in loc])
+    Akc = Ak * np.stack([S[i] * S[j] for i in range(6) for j in range(6)])
+    Ac = O._ned_global(m, Akc, edges, ne).toarray()
+
+    def nullity(M):
+        w = la.eigvalsh(M)
+        return int((np.abs(w) < 1e-10 * np.abs(w).max()).sum())
+
+    nvert = int(t.max()) + 1
+    assert nullity(Ac) == nvert - 1
+    assert nullity(A) < nvert - 1
+    # discrete gradient oriented by each edge's first use, scaled by 1/length (the
+    # edge unknowns are mean tangential components: curl N_e = 2 l_e grad l_i x grad l_j)
+    G = np.zeros((ne, m.nv))
+    seen = np.zeros(ne, dtype=bool)
+    for k in range(m.nt):
+        for le, (a, b) in enumerate(loc):
+            e = edges[le, k]
+            if not seen[e]:
+                seen[e] = True
+                ia, ib = t[a, k], t[b, k]
+                ln = np.linalg.norm(m.p[:, ib] - m.p[:, ia])
+                G[e, ib], G[e, ia] = 1.0 / ln, -1.0 / ln
+    Gc = np.zeros((ne, m.nv))
+    for k in range(m.nt):
+        for le, (a, b) in enumerate(loc):
+            e = edges[le, k]
+            lo, hi = sorted((t[a, k], t[b, k]))
+            ln = np.linalg.norm(m.p[:, hi] - m.p[:, lo])
+            Gc[e] = 0.0
+            Gc[e, hi], Gc[e, lo] = 1.0 / ln, -1.0 / ln
+    assert np.abs(Ac @ Gc).max() <= 1e-10 * np.abs(Ac).max()
+    assert np.abs(A @ G).max() > 0.1 * np.abs(A).max()
