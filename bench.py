@@ -476,8 +476,11 @@ def run_ours(args):
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         w0 = time.time()
         ev0.record()
+        call_ms = []
         for _ in range(args.e2e_steps):
+            c0 = time.perf_counter()
             one()
+            call_ms.append(1e3 * (time.perf_counter() - c0))
         ev1.record()
         barrier()
         e2e_sec = max(ev0.elapsed_time(ev1) / 1000.0, time.time() - w0)
@@ -503,9 +506,11 @@ def run_ours(args):
         torch.cuda.synchronize()
         t4 = time.perf_counter()
         phases = {"mesh_create_upload_pattern": 1e3 * (t1 - t0), "set_dirichlet": 1e3 * (t2 - t1),
-                  "newton_solve_with_io": 1e3 * (t3 - t2), "destroy": 1e3 * (t4 - t3)}
+                  "newton_solve_with_io": 1e3 * (t3 - t2), "of_which_newton_device_ms": s.ms,
+                  "of_which_newton_setup_ms": s.setup_ms, "destroy": 1e3 * (t4 - t3)}
         e2e = {"value": ws * args.e2e_steps / e2e_sec, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
+               "call_ms": [round(c, 2) for c in call_ms],
                "what": "fg_scalar_potential_newton: upload + pattern build + solve + download per step",
                "phases_ms_one_call": {k: round(v, 3) for k, v in phases.items()}}
 
@@ -902,7 +907,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--fp64-steps", type=int, default=None)
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cells", type=int, default=96)
     ap.add_argument("--no-e2e", action="store_true")

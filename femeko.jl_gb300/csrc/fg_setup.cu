@@ -453,12 +453,121 @@ __global__ void k_geom_tri(const double *__restrict__ p, const int *__restrict__
   geo[6 * nt + k] = 0.5 * fabs(det);
 }
 
-// ------------------------------------------------------------------ host side
-static void exclusive_scan_host(const std::vector<int> &in, std::vector<int64_t> &out) {
-  out.resize(in.size() + 1);
-  out[0] = 0;
-  for (size_t i = 0; i < in.size(); ++i) out[i + 1] = out[i] + in[i];
+// ------------------------------------------------------------------ pattern sizes
+// Exclusive scans of int arrays on the device (three passes: 1024-element block
+// scans, one block over the block totals, the offsets written back as int32 with the
+// total at out[n]); the int64 total is left on the device for the host to check
+// against 2^31 before anything uses the offsets.
+__device__ __forceinline__ int64_t block_incl_scan_1024(int64_t v, int64_t *ws) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int64_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) ws[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int64_t w = ws[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    ws[lane] = w;
+  }
+  __syncthreads();
+  const int64_t r = x + (wid > 0 ? ws[wid - 1] : 0);
+  __syncthreads();  // ws is reused by the next call
+  return r;
 }
+
+__global__ void __launch_bounds__(1024) k_scan_local(const int *__restrict__ in, int64_t n, int64_t *__restrict__ tmp,
+                                                     int64_t *__restrict__ bsum) {
+  __shared__ int64_t ws[32];
+  const int64_t i = (int64_t)blockIdx.x * 1024 + threadIdx.x;
+  const int64_t v = (i < n) ? (int64_t)in[i] : 0;
+  const int64_t incl = block_incl_scan_1024(v, ws);
+  if (i < n) tmp[i] = incl - v;
+  if (threadIdx.x == 1023) bsum[blockIdx.x] = incl;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_bsum(int64_t *__restrict__ bsum, int nb, int64_t *__restrict__ total) {
+  __shared__ int64_t ws[32];
+  __shared__ int64_t carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < nb; base += 1024) {
+    const int j = base + (int)threadIdx.x;
+    const int64_t v = (j < nb) ? bsum[j] : 0;
+    const int64_t incl = block_incl_scan_1024(v, ws);
+    const int64_t c = carry;
+    if (j < nb) bsum[j] = c + incl - v;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry = c + incl;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void k_scan_apply(const int64_t *__restrict__ tmp, const int64_t *__restrict__ bsum, int64_t n,
+                             const int64_t *__restrict__ total, int *__restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (int)(tmp[i] + bsum[i / 1024]);
+  if (i == 0) out[n] = (int)*total;
+}
+
+// Per SELL slice of 32 rows: its groups of 4 slots (longest row), its incidence
+// depth (largest node degree), their padded sizes for the offset scans, and the
+// longest row and degree overall.
+__global__ void k_slice_meta(const int *__restrict__ rowlen, const int *__restrict__ deg, int64_t nv, int nslices,
+                             int *__restrict__ sl_len, int *__restrict__ in_len, int *__restrict__ slsize,
+                             int *__restrict__ insize, int64_t *__restrict__ meta) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nslices) return;
+  int mx = 0, md = 0;
+  const int64_t r1 = nv < (int64_t)(s + 1) * FG_SLICE ? nv : (int64_t)(s + 1) * FG_SLICE;
+  for (int64_t r = (int64_t)s * FG_SLICE; r < r1; ++r) {
+    mx = max(mx, rowlen[r]);
+    md = max(md, deg[r]);
+  }
+  const int groups = max(1, (mx + FG_GROUP - 1) / FG_GROUP);
+  sl_len[s] = groups;
+  in_len[s] = md;
+  slsize[s] = groups * FG_GROUP * FG_SLICE;
+  insize[s] = md * FG_SLICE;
+  atomicMax(reinterpret_cast<unsigned long long *>(meta + 3), (unsigned long long)mx);
+  atomicMax(reinterpret_cast<unsigned long long *>(meta + 4), (unsigned long long)md);
+}
+
+// The most padded entries of one 256-row block (the bulk-staged SpMV stages one).
+__global__ void k_tmax256(const int *__restrict__ sl_ptr, int nslices, int64_t *__restrict__ meta) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s0 = b * (256 / FG_SLICE);
+  if (s0 >= nslices) return;
+  const int s1 = min(s0 + 256 / FG_SLICE, nslices);
+  atomicMax(reinterpret_cast<unsigned long long *>(meta + 5), (unsigned long long)(sl_ptr[s1] - sl_ptr[s0]));
+}
+
+// ------------------------------------------------------------------ host side
+
+// Temporary device buffers from the stream-ordered pool, released on the stream when
+// the holder goes out of scope (normally or by an exception).
+struct StreamScratch {
+  cudaStream_t s;
+  std::vector<void *> held;
+  template <class T>
+  T *get(size_t count) {
+    void *q = nullptr;
+    FG_CUDA_TRY(cudaMallocAsync(&q, sizeof(T) * std::max<size_t>(count, 1), s));
+    held.push_back(q);
+    return static_cast<T *>(q);
+  }
+  ~StreamScratch() {
+    for (void *q : held) cudaFreeAsync(q, s);
+  }
+};
 
 // The default memory pool of a device keeps the memory freed to it (no release
 // threshold) for the next handle; set once per device for this process.
@@ -554,95 +663,95 @@ static fg_status create_impl(const double *p, int64_t np, const int32_t *t, int6
     cudaFreeAsync(traw, s);
 
     // incidence lists
-    int *deg = nullptr, *cursor = nullptr, *iptr = nullptr, *inc = nullptr;
-    FG_CUDA_TRY(cudaMallocAsync(&deg, sizeof(int) * (size_t)nv, s));
+    FG_CUDA_TRY(cudaMallocHost(&m->hbuf, 64 * sizeof(double)));
+    FG_CUDA_TRY(cudaMallocHost(&m->hint, 16 * sizeof(int)));
+    m->nslices = (int)((nv + FG_SLICE - 1) / FG_SLICE);
+    const int nsl = m->nslices;
+    // work space of the pattern build, released on the stream when this scope ends
+    // (also when it ends by an error)
+    StreamScratch scratch{s, {}};
+    int *deg = scratch.get<int>((size_t)nv);
+    int *iptr = scratch.get<int>((size_t)nv + 1);
+    int *inc = scratch.get<int>((size_t)nt * npe);
+    int *slsize = scratch.get<int>((size_t)nsl);
+    int *insize = scratch.get<int>((size_t)nsl);
+    int64_t *scan_tmp = scratch.get<int64_t>((size_t)nv);
+    int64_t *scan_bsum = scratch.get<int64_t>((size_t)((nv + 1023) / 1024));
+    // meta: totals of the scans (0 incidences, 1 nnz, 2 padded entries, 6 incidence
+    // slots) and maxima (3 longest row, 4 largest degree, 5 entries of a 256-row block)
+    int64_t *meta = scratch.get<int64_t>(8);
+    FG_CUDA_TRY(cudaMemsetAsync(meta, 0, sizeof(int64_t) * 8, s));
+    auto scan = [&](const int *in, int64_t n, int *out, int64_t *total) {
+      const int nb = (int)((n + 1023) / 1024);
+      k_scan_local<<<nb, 1024, 0, s>>>(in, n, scan_tmp, scan_bsum);
+      k_scan_bsum<<<1, 1024, 0, s>>>(scan_bsum, nb, total);
+      k_scan_apply<<<grid_for(n, 256), 256, 0, s>>>(scan_tmp, scan_bsum, n, total, out);
+    };
     FG_CUDA_TRY(cudaMemsetAsync(deg, 0, sizeof(int) * (size_t)nv, s));
     k_count_deg<<<grid_for(nt, 256), 256, 0, s>>>(m->t, nt, npe, deg);
-    std::vector<int> hdeg(nv);
-    FG_CUDA_TRY(cudaMemcpyAsync(hdeg.data(), deg, sizeof(int) * (size_t)nv, cudaMemcpyDeviceToHost, s));
-    fg_sync(m);
-    std::vector<int64_t> hiptr;
-    exclusive_scan_host(hdeg, hiptr);
-    std::vector<int> hiptr32(nv + 1);
-    for (int64_t i = 0; i <= nv; ++i) hiptr32[i] = (int)hiptr[i];
-    m->maxdeg = *std::max_element(hdeg.begin(), hdeg.end());
-    FG_CUDA_TRY(cudaMallocAsync(&iptr, sizeof(int) * (size_t)(nv + 1), s));
-    FG_CUDA_TRY(cudaMallocAsync(&inc, sizeof(int) * (size_t)nt * npe, s));
-    FG_CUDA_TRY(cudaMemcpyAsync(iptr, hiptr32.data(), sizeof(int) * (size_t)(nv + 1), cudaMemcpyHostToDevice, s));
-    cursor = deg;
-    FG_CUDA_TRY(cudaMemsetAsync(cursor, 0, sizeof(int) * (size_t)nv, s));
-    k_fill_inc<<<grid_for(nt, 256), 256, 0, s>>>(m->t, nt, npe, iptr, cursor, inc);
+    scan(deg, nv, iptr, meta + 0);
+    // the fill counts each node's list up from 0 again: deg ends as it was
+    FG_CUDA_TRY(cudaMemsetAsync(deg, 0, sizeof(int) * (size_t)nv, s));
+    k_fill_inc<<<grid_for(nt, 256), 256, 0, s>>>(m->t, nt, npe, iptr, deg, inc);
     k_sort_inc<<<grid_for(nv, 128), 128, 0, s>>>(iptr, inc, nv);
     FG_CUDA_TRY(cudaGetLastError());
 
-    // row lengths of the structural pattern
+    // row lengths of the structural pattern, the SELL-32 slices of the matrix and of
+    // the incidence records, and their offsets, all on the device; the host reads the
+    // sizes back once (rows longer than 128 entries: once more, with the long-row
+    // kernel)
     m->rowlen = dev_alloc<int>(m, (size_t)nv);
-    int cap_needed = std::min<int64_t>((int64_t)m->maxdeg * npe, FG_MAX_ROW);
-    bool big = cap_needed > 128;
-    if (big)
-      k_row_count<FG_MAX_ROW><<<grid_for(nv, 64), 64, 0, s>>>(iptr, inc, m->t, nt, npe, nv, m->rowlen, m->flags);
-    else
-      k_row_count<128><<<grid_for(nv, 128), 128, 0, s>>>(iptr, inc, m->t, nt, npe, nv, m->rowlen, m->flags);
-    FG_CUDA_TRY(cudaGetLastError());
-    fg_check_flags(m, "fg_mesh_create");
-    std::vector<int> hrl(nv);
-    FG_CUDA_TRY(cudaMemcpyAsync(hrl.data(), m->rowlen, sizeof(int) * (size_t)nv, cudaMemcpyDeviceToHost, s));
-    fg_sync(m);
-    std::vector<int64_t> hrowptr;
-    exclusive_scan_host(hrl, hrowptr);
-    m->nnz = hrowptr[nv];
-    FG_REQUIRE(m->nnz < ((int64_t)1 << 31), FG_BAD_ARG, "fg_mesh_create: pattern too large");
-    m->maxrow = *std::max_element(hrl.begin(), hrl.end());
-    std::vector<int> hrp32(nv + 1);
-    for (int64_t i = 0; i <= nv; ++i) hrp32[i] = (int)hrowptr[i];
-
-    // SELL-32 slices for the matrix and for the incidence records
-    m->nslices = (int)((nv + FG_SLICE - 1) / FG_SLICE);
-    std::vector<int> hsl_len(m->nslices), hin_len(m->nslices), hsl_ptr(m->nslices + 1), hin_ptr(m->nslices + 1);
-    int64_t acc = 0, acc2 = 0;
-    for (int sl = 0; sl < m->nslices; ++sl) {
-      int mx = 0, md = 0;
-      for (int64_t r = (int64_t)sl * FG_SLICE; r < std::min<int64_t>(nv, (int64_t)(sl + 1) * FG_SLICE); ++r) {
-        mx = std::max(mx, hrl[r]);
-        md = std::max(md, hdeg[r]);
-      }
-      int groups = std::max(1, (mx + FG_GROUP - 1) / FG_GROUP);
-      hsl_len[sl] = groups;
-      hin_len[sl] = md;
-      hsl_ptr[sl] = (int)acc;
-      hin_ptr[sl] = (int)acc2;
-      acc += (int64_t)groups * FG_GROUP * FG_SLICE;
-      acc2 += (int64_t)md * FG_SLICE;
-      FG_REQUIRE(acc < ((int64_t)1 << 31) && acc2 * npe < ((int64_t)1 << 31), FG_BAD_ARG,
-                 "fg_mesh_create: padded layout too large");
-    }
-    hsl_ptr[m->nslices] = (int)acc;
-    hin_ptr[m->nslices] = (int)acc2;
-    // largest 256-row block in padded entries (the bulk-staged SpMV stages one)
-    m->tmax256 = 0;
-    for (int s0 = 0; s0 < m->nslices; s0 += 256 / FG_SLICE)
-      m->tmax256 = std::max(m->tmax256, hsl_ptr[std::min(s0 + 256 / FG_SLICE, m->nslices)] - hsl_ptr[s0]);
-    m->nsell = acc;
-    m->ninc = acc2;
-
     m->rowptr = dev_alloc<int>(m, (size_t)nv + 1);
+    m->sl_ptr = dev_alloc<int>(m, (size_t)nsl + 1);
+    m->sl_len = dev_alloc<int>(m, (size_t)nsl);
+    m->in_ptr = dev_alloc<int>(m, (size_t)nsl + 1);
+    m->in_len = dev_alloc<int>(m, (size_t)nsl);
+    bool big = false;
+    int64_t hm[8];
+    for (;;) {
+      FG_CUDA_TRY(cudaMemsetAsync(meta + 1, 0, sizeof(int64_t) * 7, s));
+      if (big)
+        k_row_count<FG_MAX_ROW><<<grid_for(nv, 64), 64, 0, s>>>(iptr, inc, m->t, nt, npe, nv, m->rowlen, m->flags);
+      else
+        k_row_count<128><<<grid_for(nv, 128), 128, 0, s>>>(iptr, inc, m->t, nt, npe, nv, m->rowlen, m->flags);
+      scan(m->rowlen, nv, m->rowptr, meta + 1);
+      k_slice_meta<<<grid_for(nsl, 128), 128, 0, s>>>(m->rowlen, deg, nv, nsl, m->sl_len, m->in_len, slsize, insize,
+                                                      meta);
+      scan(slsize, nsl, m->sl_ptr, meta + 2);
+      scan(insize, nsl, m->in_ptr, meta + 6);
+      k_tmax256<<<grid_for((nsl + 256 / FG_SLICE - 1) / (256 / FG_SLICE), 128), 128, 0, s>>>(m->sl_ptr, nsl, meta);
+      FG_CUDA_TRY(cudaGetLastError());
+      FG_CUDA_TRY(cudaMemcpyAsync(m->hbuf, meta, sizeof(int64_t) * 8, cudaMemcpyDeviceToHost, s));
+      FG_CUDA_TRY(cudaMemcpyAsync(m->hint, m->flags, sizeof(int), cudaMemcpyDeviceToHost, s));
+      fg_sync(m);
+      std::memcpy(hm, m->hbuf, sizeof hm);
+      const int h = m->hint[0];
+      if ((h & FLAG_ROW_OVERFLOW) && !big && (h & ~FLAG_ROW_OVERFLOW) == 0) {
+        FG_CUDA_TRY(cudaMemsetAsync(m->flags, 0, sizeof(int), s));
+        big = true;
+        continue;
+      }
+      fg_raise_flags(m, h, "fg_mesh_create");
+      break;
+    }
+    m->nnz = hm[1];
+    m->nsell = hm[2];
+    m->maxrow = (int)hm[3];
+    m->maxdeg = (int)hm[4];
+    m->tmax256 = (int)hm[5];
+    m->ninc = hm[6];
+    FG_REQUIRE(m->nnz < ((int64_t)1 << 31), FG_BAD_ARG, "fg_mesh_create: pattern too large");
+    FG_REQUIRE(m->nsell < ((int64_t)1 << 31) && m->ninc * npe < ((int64_t)1 << 31), FG_BAD_ARG,
+               "fg_mesh_create: padded layout too large");
+
     m->colidx = dev_alloc<int>(m, (size_t)m->nnz);
-    m->sl_ptr = dev_alloc<int>(m, (size_t)m->nslices + 1);
-    m->sl_len = dev_alloc<int>(m, (size_t)m->nslices);
     m->sl_col = dev_alloc<int>(m, (size_t)m->nsell);
     m->sl_dcol = dev_alloc<int16_t>(m, (size_t)m->nsell);
-    m->nvp = (int64_t)m->nslices * FG_SLICE;
+    m->nvp = (int64_t)nsl * FG_SLICE;
     m->maxrow4 = (m->maxrow + FG_GROUP - 1) / FG_GROUP * FG_GROUP;
     m->diagk = dev_alloc<uint8_t>(m, (size_t)nv);
-    m->in_ptr = dev_alloc<int>(m, (size_t)m->nslices + 1);
-    m->in_len = dev_alloc<int>(m, (size_t)m->nslices);
     m->in_slot = dev_alloc<uint8_t>(m, (size_t)m->ninc * npe);
     m->recpos = dev_alloc<int>(m, (size_t)nt * npe);
-    FG_CUDA_TRY(cudaMemcpyAsync(m->rowptr, hrp32.data(), sizeof(int) * (size_t)(nv + 1), cudaMemcpyHostToDevice, s));
-    FG_CUDA_TRY(cudaMemcpyAsync(m->sl_ptr, hsl_ptr.data(), sizeof(int) * (m->nslices + 1), cudaMemcpyHostToDevice, s));
-    FG_CUDA_TRY(cudaMemcpyAsync(m->sl_len, hsl_len.data(), sizeof(int) * m->nslices, cudaMemcpyHostToDevice, s));
-    FG_CUDA_TRY(cudaMemcpyAsync(m->in_ptr, hin_ptr.data(), sizeof(int) * (m->nslices + 1), cudaMemcpyHostToDevice, s));
-    FG_CUDA_TRY(cudaMemcpyAsync(m->in_len, hin_len.data(), sizeof(int) * m->nslices, cudaMemcpyHostToDevice, s));
     if (big)
       k_row_fill<FG_MAX_ROW><<<grid_for(nv, 64), 64, 0, s>>>(iptr, inc, m->t, nt, npe, nv, m->rowptr, m->sl_ptr,
                                                              m->sl_len, m->colidx, m->sl_col, m->sl_dcol, m->diagk,
@@ -651,12 +760,6 @@ static fg_status create_impl(const double *p, int64_t np, const int32_t *t, int6
       k_row_fill<128><<<grid_for(nv, 128), 128, 0, s>>>(iptr, inc, m->t, nt, npe, nv, m->rowptr, m->sl_ptr,
                                                          m->sl_len, m->colidx, m->sl_col, m->sl_dcol, m->diagk,
                                                          m->flags);
-    {
-      int wide = 0;
-      FG_CUDA_TRY(cudaMemcpyAsync(&wide, m->flags + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
-      fg_sync(m);
-      m->use_dcol = (wide == 0);  // 16-bit column offsets when the bandwidth allows
-    }
     k_slots<<<grid_for(nv, 128), 128, 0, s>>>(iptr, inc, m->t, nt, npe, nv, m->rowptr, m->colidx, m->in_ptr,
                                               m->in_len, m->recpos, m->in_slot);
     FG_CUDA_TRY(cudaGetLastError());
@@ -669,10 +772,6 @@ static fg_status create_impl(const double *p, int64_t np, const int32_t *t, int6
     else
       k_geom_tri<<<grid_for(nt, 256), 256, 0, s>>>(m->p, m->t, nt, m->geo, m->flags);
     FG_CUDA_TRY(cudaGetLastError());
-    fg_check_flags(m, "fg_mesh_create");
-    cudaFreeAsync(deg, s);
-    cudaFreeAsync(iptr, s);
-    cudaFreeAsync(inc, s);
 
     // control and reduction workspace
     // one slot of 4 per CTA of any row kernel (CTAs of 32 rows or more)
@@ -681,9 +780,12 @@ static fg_status create_impl(const double *p, int64_t np, const int32_t *t, int6
     FG_CUDA_TRY(cudaMemsetAsync(m->red.counter, 0, 128 * sizeof(unsigned int), s));
     m->scal = dev_alloc<double>(m, S_NSCAL);
     m->ictl = dev_alloc<int>(m, I_NINT);
-    FG_CUDA_TRY(cudaMallocHost(&m->hbuf, 64 * sizeof(double)));
-    FG_CUDA_TRY(cudaMallocHost(&m->hint, 16 * sizeof(int)));
+    // the error flags of the fill and geometry kernels, and whether some column is
+    // more than 32767 rows from its row (then 32-bit columns), in the last round trip
+    FG_CUDA_TRY(cudaMemcpyAsync(m->hint, m->flags, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
     fg_sync(m);
+    fg_raise_flags(m, m->hint[0], "fg_mesh_create");
+    m->use_dcol = (m->hint[1] == 0);  // 16-bit column offsets when the bandwidth allows
     *out = m;
     m = nullptr;
     return FG_OK;

@@ -358,3 +358,37 @@ def test_bad_mesh_reports_error():
     with pytest.raises(L.FemekoGPUError) as e:
         fg.GPUMesh(m)
     assert e.value.status == L.FG_BAD_MESH
+
+
+def _fan_mesh(k):
+    """k tetrahedra above and k below a ring of k nodes around a centre node: the
+    centre's row holds k + 3 entries, the apexes' k + 2."""
+    from femeko_gpu.mesh import MESH, element_volumes
+    ang = 2.0 * np.pi * np.arange(k) / k
+    p = np.zeros((3, k + 3))
+    p[:, 1], p[:, 2] = (0.0, 0.0, 1.0), (0.0, 0.0, -1.0)
+    p[0, 3:], p[1, 3:] = np.cos(ang), np.sin(ang)
+    ring, nxt = 3 + np.arange(k), 3 + (np.arange(k) + 1) % k
+    zero = np.zeros(k, dtype=np.int64)
+    t = np.concatenate([np.stack([zero, ring, nxt, zero + 1]), np.stack([zero, ring, nxt, zero + 2])], axis=1)
+    t = np.ascontiguousarray(t.astype(np.int32))
+    return MESH(order=1, dim=3, p=p, t=t, surfaceT=np.zeros((4, 0), dtype=np.int32),
+                elementID=np.ones(2 * k, dtype=np.int32), InsideElements=np.zeros(0, dtype=np.int32),
+                InsideNodes=np.zeros(0, dtype=np.int32), VE=element_volumes(p, t), AE=np.zeros(0),
+                normal=np.zeros((3, 0)))
+
+
+def test_rows_longer_than_128_entries():
+    """The pattern build counts rows with the 128-entry kernels first and redoes the
+    count with the long-row ones when a row is longer."""
+    m = _fan_mesh(150)
+    Kg, Ko = fg.stiffnessMatrix(m), O.stiffnessMatrix(m)
+    assert same_pattern(Kg, Ko) and rel(Kg.data, Ko.data) < REL_VAL
+    assert np.diff(Kg.indptr).max() == 153
+
+
+def test_rows_beyond_the_supported_length_are_refused():
+    import femeko_gpu._lib as L
+    with pytest.raises(L.FemekoGPUError) as e:
+        fg.stiffnessMatrix(_fan_mesh(260))
+    assert e.value.status == L.FG_BAD_MESH
