@@ -364,9 +364,9 @@ def run_ours(args):
     L.check(lib.fg_bench_kernel(g.h, 7, L.FG_MIXED, 20, C.byref(t_asm)))
     L.check(lib.fg_bench_kernel(g.h, 8, L.FG_MIXED, 10, C.byref(t_asm2)))
     nt, nv_ = mesh.nt, mesh.nv
-    # algorithmic bytes by the survey's model: per element connectivity (16 B) and
-    # permeability (8 B), per node the coordinates (24 B), per stored nonzero the FP64
-    # value written (8 B)
+    # algorithmic bytes of the reference path's per-element model: per element
+    # connectivity (16 B) and permeability (8 B), per node the coordinates (24 B), per
+    # stored nonzero the FP64 value written (8 B)
     asm_alg = nt * 24 + nv_ * 24 + g.nnz * 8
     # bytes this design moves (gradients are not recomputed in FP64): per element the
     # 10-entry Gram matrix, volume and permeability (96 B), per incidence its element

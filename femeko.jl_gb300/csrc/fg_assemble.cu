@@ -1444,11 +1444,6 @@ void fg_newton_assemble(fg_mesh *m, const double *d_u, double Ms, double Hk, boo
   }
 }
 
-__global__ void k_negate64(int64_t n, double *__restrict__ x) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) x[i] = -x[i];
-}
-
 __global__ void k_linear_coef(int64_t nt, const double *__restrict__ mu_lin, const uint8_t *__restrict__ nl,
                               double *__restrict__ coef, double *__restrict__ mu, double *__restrict__ dmu) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1578,7 +1573,8 @@ static void nl_maps(fg_mesh *m, const uint8_t *nl_host) {
 
 void fg_nl_setup(fg_mesh *m, const uint8_t *nl_host, bool mixed) {
   FG_REQUIRE(m->npe == 4, FG_UNSUPPORTED, "Newton magnetostatics needs P1 tetrahedra");
-  fg_ensure_records(m);
+  // no incidence records: the linear operator is assembled in one pass and the
+  // nonlinear elements keep their own blocks (nl_re, nl_ke)
   const int64_t nt = m->nt;
   // the mask of the handle's inputs, unchanged since its list was built, needs no
   // scan (a scan of millions of elements takes milliseconds on the host, with the
@@ -1626,9 +1622,8 @@ void fg_newton_assemble_split(fg_mesh *m, const double *d_u, double Ms, double H
                                                                   m->nl_row_src, m->nl_re, fx, d_F);
     FG_LAUNCHED(2);
   }
-  k_negate64<<<grid_for(m->nv, 256), 256, 0, m->stream>>>(m->nv, d_F);
-  FG_CUDA_TRY(cudaGetLastError());
-  FG_LAUNCHED(1);
+  // F <- -F, with |F|^2 in scal[FG_SLOT_FNORM2] (the Dirichlet rows are 0)
+  fg_negate_norm2_enqueue(m, d_F);
   if (!want_jacobian) return;
   m->op_tag = 0;
   ++m->op_version;

@@ -260,6 +260,13 @@ struct fg_mesh {
 // of paying a synchronising cudaMalloc/cudaFree per buffer (fg_setup.cu keeps the
 // pool's memory when it is freed).
 void fg_pool_init(int device);
+// Pinned host blocks of FG_PINNED_BLOCK bytes for a handle's small read-backs
+// (hbuf: 64 doubles, hint: 16 ints after it), recycled across handles:
+// cudaMallocHost pins pages and cudaFreeHost waits for the device, both per handle
+// otherwise.
+constexpr size_t FG_PINNED_BLOCK = 1024;
+void *fg_pinned_block_get();
+void fg_pinned_block_put(void *block);
 template <class T>
 static inline T *dev_alloc(fg_mesh *m, size_t count) {
   void *ptr = nullptr;
@@ -346,6 +353,11 @@ double fg_norm2_dev(fg_mesh *m, const double *x, int64_t n, bool mask_fixed);
 double fg_dot_dev(fg_mesh *m, const double *x, const double *y, int64_t n, bool mask_fixed);
 // Enqueues x.y into scal[slot] (slots 10-15 are free for callers) without waiting.
 void fg_dot_enqueue(fg_mesh *m, const double *x, const double *y, int64_t n, bool mask_fixed, int slot);
+// F <- -F over the handle's rows with |F|^2 left in scal[FG_SLOT_FNORM2]; the square
+// root of that slot read back (one host wait).
+constexpr int FG_SLOT_FNORM2 = 12;
+void fg_negate_norm2_enqueue(fg_mesh *m, double *F);
+double fg_slot_sqrt(fg_mesh *m, int slot);
 // Throws the error that a device flag word h reports (no-op for 0).
 void fg_raise_flags(fg_mesh *m, int h, const char *where);
 // Solves A x = b (A = the handle's operator, SELL layout) on free rows.  b, x are FP64

@@ -95,7 +95,7 @@ static int newton_dev(fg_mesh *m, double *d_u, const uint8_t *nl_host, const fg_
   fg_newton_assemble_split(m, d_u, o.Ms, o.Hk, mixed, d_F, true, o.picard_steps <= 0);
   FG_CUDA_TRY(cudaEventRecord(es, m->stream));
   fg_check_flags(m, "fg_newton_magnetostatics");
-  double rF = fg_norm2_dev(m, d_F, nv, true);
+  double rF = fg_slot_sqrt(m, FG_SLOT_FNORM2);
   float setup_ms = 0.f, cg_ms = 0.f;
   cudaEventElapsedTime(&setup_ms, e0, es);
   int it = 0, cg_total = 0, trials = 0, converged = 0, status = 0;
@@ -136,7 +136,7 @@ static int newton_dev(fg_mesh *m, double *d_u, const uint8_t *nl_host, const fg_
         k_axpby64<<<g, 256, 0, m->stream>>>(nv, 1.0, d_u, alpha, d_du, d_ut);
         FG_LAUNCHED(1);
         fg_newton_assemble_split(m, d_ut, o.Ms, o.Hk, mixed, d_Ft, trial_jacobian, next_tangent);
-        rt = fg_norm2_dev(m, d_Ft, nv, true);
+        rt = fg_slot_sqrt(m, FG_SLOT_FNORM2);
         ++trials;
         if (o.line_search == FG_LS_NONE || !(rt > rF && alpha > o.min_step)) break;
         if (o.line_search == FG_LS_QUADRATIC) {
@@ -180,7 +180,7 @@ static int newton_dev(fg_mesh *m, double *d_u, const uint8_t *nl_host, const fg_
       k_axpby64<<<g, 256, 0, m->stream>>>(nv, 1.0, d_u, alpha, d_du, d_u);
       FG_LAUNCHED(1);
       fg_newton_assemble_split(m, d_u, o.Ms, o.Hk, mixed, d_F, true, next_tangent);
-      rF = fg_norm2_dev(m, d_F, nv, true);
+      rF = fg_slot_sqrt(m, FG_SLOT_FNORM2);
     }
     // |du|, |u| and the device error flags in one round trip
     fg_dot_enqueue(m, d_du, d_du, nv, false, 10);

@@ -586,6 +586,29 @@ void fg_pool_init(int device) {
   done[device] = true;
 }
 
+static std::mutex g_pinned_lock;
+static std::vector<void *> g_pinned_free;
+
+void *fg_pinned_block_get() {
+  {
+    std::lock_guard<std::mutex> g(g_pinned_lock);
+    if (!g_pinned_free.empty()) {
+      void *b = g_pinned_free.back();
+      g_pinned_free.pop_back();
+      return b;
+    }
+  }
+  void *b = nullptr;
+  FG_CUDA_TRY(cudaMallocHost(&b, FG_PINNED_BLOCK));
+  return b;
+}
+
+void fg_pinned_block_put(void *block) {
+  if (!block) return;
+  std::lock_guard<std::mutex> g(g_pinned_lock);
+  g_pinned_free.push_back(block);
+}
+
 static void free_mesh(fg_mesh *m) {
   if (!m) return;
   for (int g = 0; g < 4; ++g)
@@ -596,8 +619,7 @@ static void free_mesh(fg_mesh *m) {
     cudaStreamSynchronize(m->stream);
   }
   for (void *ptr : m->extra_sync) cudaFree(ptr);
-  if (m->hbuf) cudaFreeHost(m->hbuf);
-  if (m->hint) cudaFreeHost(m->hint);
+  fg_pinned_block_put(m->hbuf);  // hint lives in the same block
   if (m->ev0) cudaEventDestroy(m->ev0);
   if (m->ev1) cudaEventDestroy(m->ev1);
   if (m->stream) cudaStreamDestroy(m->stream);
@@ -663,8 +685,8 @@ static fg_status create_impl(const double *p, int64_t np, const int32_t *t, int6
     cudaFreeAsync(traw, s);
 
     // incidence lists
-    FG_CUDA_TRY(cudaMallocHost(&m->hbuf, 64 * sizeof(double)));
-    FG_CUDA_TRY(cudaMallocHost(&m->hint, 16 * sizeof(int)));
+    m->hbuf = static_cast<double *>(fg_pinned_block_get());
+    m->hint = reinterpret_cast<int *>(m->hbuf + 64);
     m->nslices = (int)((nv + FG_SLICE - 1) / FG_SLICE);
     const int nsl = m->nslices;
     // work space of the pattern build, released on the stream when this scope ends

@@ -1623,6 +1623,23 @@ __global__ void __launch_bounds__(256) k_dot64(int64_t n, const double *__restri
   if (grid_finish<1>(part, partials, counter, tot)) scal[slot] = tot[0];
 }
 
+// F <- -F with the sum of squares of the result (one pass instead of a negation and
+// a separate dot product)
+__global__ void __launch_bounds__(256) k_negate_norm64(int64_t n, double *__restrict__ F, int slot, double *scal,
+                                                       double *partials, unsigned *counter) {
+  double acc = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double f = -F[i];
+    F[i] = f;
+    acc += f * f;
+  }
+  __shared__ double shd[1][32];
+  double part[1] = {acc};
+  block_sum<1>(part, shd);
+  double tot[1];
+  if (grid_finish<1>(part, partials, counter, tot)) scal[slot] = tot[0];
+}
+
 // x += scale * d
 template <typename S>
 __global__ void k_axpy_to64(int64_t n, double scale, const S *__restrict__ d, double *__restrict__ x) {
@@ -1642,11 +1659,31 @@ static unsigned red_grid(int64_t n) {
 }
 static unsigned row_grid(const fg_mesh *m) { return grid_for(m->nv, 256); }
 
+// Grid of the FP64 vector reductions: resident blocks walking the vector with a grid
+// stride (4 per SM), so that each block reduces once for several thousand entries and
+// the arrival chain at the end is short.
+static unsigned dot_grid(const fg_mesh *m, int64_t n) {
+  return std::min<unsigned>(red_grid(n), 4u * (unsigned)std::max(m->sm_count, 1));
+}
+
 void fg_dot_enqueue(fg_mesh *m, const double *x, const double *y, int64_t n, bool mask_fixed, int slot) {
-  k_dot64<<<red_grid(n), 256, 0, m->stream>>>(n, x, y, (mask_fixed && m->has_fixed) ? m->fixed : nullptr, slot,
-                                              m->scal, m->red.partials, m->red.counter);
+  k_dot64<<<dot_grid(m, n), 256, 0, m->stream>>>(n, x, y, (mask_fixed && m->has_fixed) ? m->fixed : nullptr, slot,
+                                                 m->scal, m->red.partials, m->red.counter);
   FG_CUDA_TRY(cudaGetLastError());
   FG_LAUNCHED(1);
+}
+
+void fg_negate_norm2_enqueue(fg_mesh *m, double *F) {
+  k_negate_norm64<<<dot_grid(m, m->nv), 256, 0, m->stream>>>(m->nv, F, FG_SLOT_FNORM2, m->scal, m->red.partials,
+                                                              m->red.counter);
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(1);
+}
+
+double fg_slot_sqrt(fg_mesh *m, int slot) {
+  FG_CUDA_TRY(cudaMemcpyAsync(m->hbuf, m->scal + slot, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+  fg_sync(m);
+  return std::sqrt(m->hbuf[0]);
 }
 
 double fg_dot_dev(fg_mesh *m, const double *x, const double *y, int64_t n, bool mask_fixed) {
@@ -2864,8 +2901,8 @@ static fg_mesh *matrix_handle(int64_t n, const int64_t *colptr, const int64_t *r
     m->ictl = dev_alloc<int>(m, I_NINT);
     m->flags = dev_alloc<int>(m, 4);
     FG_CUDA_TRY(cudaMemsetAsync(m->flags, 0, 4 * sizeof(int), m->stream));
-    FG_CUDA_TRY(cudaMallocHost(&m->hbuf, 64 * sizeof(double)));
-    FG_CUDA_TRY(cudaMallocHost(&m->hint, 16 * sizeof(int)));
+    m->hbuf = static_cast<double *>(fg_pinned_block_get());
+    m->hint = reinterpret_cast<int *>(m->hbuf + 64);
     int64_t mr = 1;
     for (int64_t r = 0; r < n; ++r) mr = std::max<int64_t>(mr, colptr[r + 1] - colptr[r]);
     m->maxrow = (int)mr;
