@@ -414,11 +414,12 @@ def run_ours(args):
     t_dom = ms_loop.value if v == 26 else ms_spmv.value
     achieved = alg_bytes / (t_dom * 1e-3) / 1e9
     # DRAM bytes per launch of the same kernel from an ncu capture at 96^3: 10 and 20 =
-    # the L2-window variants (warm L2), 14 = the grid of 10 without the window and
-    # 17 = the bulk-staged SpMV (cold); other variants: none captured
+    # the L2-window variants (warm L2), 14 = the grid of 10 without the window, 17 =
+    # the bulk-staged SpMV and 22 = its split-reduction form (cold); other variants:
+    # none captured
     traffic, traffic_src = args.spmv_traffic, "--spmv-traffic" if args.spmv_traffic else None
-    if traffic is None and args.cells == 96 and v in (10, 14, 17, 20):
-        traffic = {10: 70.73e6, 14: 97.07e6, 17: 97.38e6, 20: 69.70e6}[v]
+    if traffic is None and args.cells == 96 and v in (10, 14, 17, 20, 22):
+        traffic = {10: 70.73e6, 14: 97.07e6, 17: 97.38e6, 20: 69.70e6, 22: 97.66e6}[v]
         traffic_src = "ncu dram__bytes_read.sum + dram__bytes_write.sum of this kernel at 96^3"
     # the whole CG iteration in the solver's loop (every kernel of it): the dominant
     # SpMV's bytes plus the vector pass's (split: 28 B read + 20 B written per row;
