@@ -662,12 +662,25 @@ def case_heat(args):
         res[prec] = (snaps, st)
     err = [float(np.linalg.norm(a - b) / np.linalg.norm(b)) for a, b in zip(res["mixed"][0], res["fp64"][0])]
     ms_m, ms_d = res["mixed"][1]["ms"], res["fp64"][1]["ms"]
+    # bandwidth per CG iteration with the whole step time charged to the iterations
+    # (right-hand side, refinements and host checks included: a lower bound on the
+    # iterations' own rate): FP32 split iteration 6 B per stored nonzero + 60 B per row,
+    # FP64 iteration 10 B per stored nonzero + 24 B (SpMV) + 96 B (vector pass) per row
+    peak, peak_kind = measured_peaks()
+    nnz = int(fg.gpu_mesh(mesh).nnz)
+    roof = {}
+    for prec, per_nz, per_row in (("mixed", 6, 60), ("fp64", 10, 120)):
+        its = max(res[prec][1]["iterations"], 1)
+        gbs = (per_nz * nnz + per_row * mesh.nv) * its / (res[prec][1]["ms"] * 1e-3) / 1e9
+        roof[prec] = {"bytes_per_iteration": per_nz * nnz + per_row * mesh.nv, "achieved_GBs": gbs,
+                      "frac": gbs / peak, "us_per_iteration_with_step_overheads": 1e3 * res[prec][1]["ms"] / its}
     _line("heat BE steps/s (mixed FP32+FP64 refinement)", 100 / (ms_m * 1e-3), "steps/s", True,
           {"workload": f"backward-Euler heat, Kuhn tets {cells}^3 cells, 100 steps", "tets": int(mesh.nt),
            "nodes": int(mesh.nv)},
           {"fp64_steps_per_s": 100 / (ms_d * 1e-3), "mixed_over_fp64": ms_d / ms_m,
            "cg_iters": {"mixed": res["mixed"][1]["iterations"], "fp64": res["fp64"][1]["iterations"]},
-           "rel_err_mixed_vs_fp64_every_10th_step": err})
+           "rel_err_mixed_vs_fp64_every_10th_step": err,
+           "roofline": {"bound": "hbm", "peak": peak, "peak_source": peak_kind, **roof}})
 
 
 def case_sweep(args):
@@ -766,7 +779,7 @@ def _mean_hx(fg, mesh, target, u):
 def case_adjoint(args):
     """dJ/dmur for J = mean Hx over elements with centroid in |x| < 0.5 on the 64^3
     mesh, mur ~ U[1,1000]: adjoint cost against the forward solve, and central
-    differences (relative step 1e-6) on 32 elements.  --nonlinear: the same through
+    differences (relative step 1e-4) on 32 elements.  --nonlinear: the same through
     the converged Newton Jacobian with the Froehlich plate of the 96^3 workload."""
     import femeko_gpu as fg
     from femeko_gpu.mesh import box_tet_mesh
@@ -786,14 +799,18 @@ def case_adjoint(args):
     fg.adjoint_dJdmu(mesh, mur, u0, target, **kw)                           # warm-up
     J, grad, u, st = fg.adjoint_dJdmu(mesh, mur, u0, target, **kw)
     # central differences on 32 elements among those with at least 1% of the largest
-    # sensitivity; each perturbed solve starts from the converged u (FP64, tight)
+    # sensitivity; each perturbed solve starts from the converged u (FP64, tight).
+    # Relative step 1e-4: the perturbed solves stop at 1e-14 of the right-hand side,
+    # which leaves a noise of about 1e-14 / step in the difference, while the
+    # truncation error of a central difference is of order step^2
+    rel_step = 1e-4
     pool = np.flatnonzero(np.abs(grad) >= 1e-2 * np.abs(grad).max())
     if args.nonlinear:
         pool = pool[nl[pool] == 0]
     picks = np.random.default_rng(11).choice(pool, min(32, pool.size), replace=False)
     errs = []
     for k in picks:
-        d = 1e-6 * mur[k]
+        d = rel_step * mur[k]
         us = []
         for sgn in (+1, -1):
             mu2 = mur * fg.MU0
@@ -814,7 +831,7 @@ def case_adjoint(args):
           {"J": J, "forward_ms": st["forward_ms"], "adjoint_ms": st["adjoint_ms"],
            "forward_iters": st["forward_iters"], "adjoint_iters": st["adjoint_iters"],
            "newton_iters": st["newton_iters"],
-           "central_differences": {"elements": int(len(picks)), "rel_step": 1e-6,
+           "central_differences": {"elements": int(len(picks)), "rel_step": rel_step,
                                    "max_rel_err": float(max(errs)), "median_rel_err": float(np.median(errs))}})
 
 
