@@ -68,6 +68,23 @@ def dist_env():
     return ws, rank
 
 
+def replica_seconds(local_sec: float, device: str = "cuda") -> float:
+    """The job's timed seconds with one independent replica per GPU: the maximum over
+    the ranks (the job ends with its slowest replica); the local value alone."""
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return local_sec
+    import torch
+    t = torch.tensor([local_sec], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world_size: int, steps: int, seconds: float) -> float:
+    """Whole-job solves/s: every replica runs `steps` solves in at most `seconds`."""
+    return world_size * steps / seconds
+
+
 class Clocks:
     """nvidia-smi sampling during the timed region."""
 
@@ -277,20 +294,15 @@ def run_ours(args):
         u, H, mu = resident.outputs()
         if prec == "mixed":
             launches = lib.fg_kernel_launches() - launches0
-        tot = sum(ms) / 1000.0
-        if ws > 1:
-            import torch.distributed as dist
-            tt = torch.tensor([tot], device="cuda", dtype=torch.float64)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            tot = float(tt.item())
+        tot = replica_seconds(sum(ms) / 1000.0)
         res[prec] = dict(u=u, H=H, mu=mu, stats=stats, sec=tot, wall=wall, steps=steps, clocks=clk.summary())
 
     Hm, Hd = res["mixed"]["H"], res["fp64"]["H"]
     herr = float(np.linalg.norm(Hm - Hd) / np.linalg.norm(Hd))
     uerr = float(np.linalg.norm(res["mixed"]["u"] - res["fp64"]["u"]) / np.linalg.norm(res["fp64"]["u"]))
     werr = abs(res["mixed"]["stats"]["energy"] - res["fp64"]["stats"]["energy"]) / abs(res["fp64"]["stats"]["energy"])
-    value = ws * args.steps / res["mixed"]["sec"]
-    fp64_value = ws * args.fp64_steps / res["fp64"]["sec"]
+    value = job_rate(ws, args.steps, res["mixed"]["sec"])
+    fp64_value = job_rate(ws, args.fp64_steps, res["fp64"]["sec"])
 
     # the CG variants the timed solves ran (autotuned at the first solve of the handle)
     used32, used64 = C.c_int32(), C.c_int32()
