@@ -646,7 +646,7 @@ def case_newton_kernels(args):
         P = L.FG_MIXED if prec == "mixed" else L.FG_FP64
         for which, name in ((0, "cg_spmv"), (1, "cg_update"), (2, "newton_element_pass_all"),
                             (4, "newton_residual_split"), (5, "newton_residual_jacobian_split"),
-                            (7, "stiffness_assembly_one_pass")):
+                            (7, "stiffness_assembly_one_pass"), (8, "stiffness_assembly_two_pass")):
             t = C.c_double()
             L.check(lib.fg_bench_kernel(g.h, which, P, 5 if which < 2 else 3, C.byref(t)))
             out[f"{prec}_{name}_us"] = t.value * 1e3
@@ -812,8 +812,9 @@ def case_adjoint(args):
     J, grad, u, st = fg.adjoint_dJdmu(mesh, mur, u0, target, **kw)
     # central differences on 32 elements among those with at least 1% of the largest
     # sensitivity; each perturbed solve starts from the converged u (FP64, tight).
-    # Relative step 1e-4: the perturbed solves stop at 1e-14 of the right-hand side,
-    # which leaves a noise of about 1e-14 / step in the difference, while the
+    # Relative step 1e-4: the perturbed solves reduce the perturbation's residual, and
+    # FP64 rounding in forming it from the whole field limits the perturbation's
+    # accuracy to about eps * |b| / |r0|, which grows as the step shrinks; the
     # truncation error of a central difference is of order step^2
     rel_step = 1e-4
     pool = np.flatnonzero(np.abs(grad) >= 1e-2 * np.abs(grad).max())

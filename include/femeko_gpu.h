@@ -91,7 +91,7 @@ typedef struct fg_mesh fg_mesh;
 
 typedef struct fg_solve_opts {
   int32_t precision;   /* FG_FP64 or FG_MIXED (FP32 matrix/vectors, FP64 refinement) */
-  double rtol;         /* FP64 relative residual target ||b - A x|| <= rtol ||b|| */
+  double rtol;         /* FP64 relative residual target ||b - A x|| <= rtol ||b - A x0|| */
   int32_t maxiter;     /* cap on CG iterations (inner iterations in total) */
   double inner_rtol;   /* mixed: FP32 PCG target per refinement step */
   int32_t check_every; /* iterations between convergence checks (even) */

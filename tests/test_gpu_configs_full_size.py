@@ -141,9 +141,10 @@ def test_c5_adjoint_64cube_linear_vs_cpu_adjoint_and_central_differences(adjoint
     assert np.abs(grad - go).max() <= 1e-7 * np.abs(go).max()
     # central differences on 32 elements whose sensitivity is at least 1% of the
     # largest.  Relative step 1e-4: the truncation error of a central difference is
-    # O(1e-8) relative, while the perturbed solves (from the converged u, stopped at
-    # 1e-14 of the right-hand side) leave a noise of about 1e-14 / 1e-4 relative in
-    # the difference; a step of 1e-6 raised that noise to 2e-5.
+    # O(1e-8) relative.  The perturbed solves start from the converged u, so the
+    # residual they reduce is the perturbation's; FP64 rounding in forming it from the
+    # whole field limits the perturbation's accuracy to about eps * |b| / |r0|, which
+    # grows as the step shrinks: at a step of 1e-6 it reached 2e-5 of the difference.
     rng = np.random.default_rng(11)
     pool = np.flatnonzero(np.abs(grad) >= 1e-2 * np.abs(grad).max())
     assert pool.size >= 32
