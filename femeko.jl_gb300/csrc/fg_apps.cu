@@ -188,21 +188,10 @@ void fg_boundary_rhs_dev(fg_mesh *m, const int32_t *surfaceT, int64_t ns, int32_
   std::vector<int> face((size_t)3 * ns), fill(cnt.begin(), cnt.end() - 1);
   for (int64_t s = 0; s < ns; ++s)
     for (int a = 0; a < 3; ++a) face[fill[st[4 * s + a]]++] = (int)s;
-  // device work space for this call
-  std::vector<void *> tmp;
-  struct Free {
-    fg_mesh *m;
-    std::vector<void *> &v;
-    ~Free() {
-      cudaStreamSynchronize(m->stream);
-      for (void *p : v) cudaFree(p);
-    }
-  } release{m, tmp};
+  // device work space for this call, from the stream-ordered pool
+  StreamScratch scratch{m->stream, {}};
   auto dmalloc = [&](size_t bytes) {
-    void *p = nullptr;
-    FG_CUDA_TRY(cudaMalloc(&p, std::max<size_t>(bytes, 16)));
-    tmp.push_back(p);
-    return p;
+    return static_cast<void *>(scratch.get<unsigned char>(std::max<size_t>(bytes, 16)));
   };
   int *d_st = (int *)dmalloc(sizeof(int) * st.size()), *d_ptr = (int *)dmalloc(sizeof(int) * cnt.size());
   int *d_face = (int *)dmalloc(sizeof(int) * face.size()), *d_shell = (int *)dmalloc(sizeof(int) * (nshell + 1));

@@ -68,8 +68,12 @@ __device__ __forceinline__ float4 vecmat(const float4 &v, const float (&M)[16]) 
 
 // X = S^-1 M for a symmetric positive semi-definite S (4 x 4) by Cholesky; a pivot
 // below tol * max(diag S) drops its direction (its rows of X are zero).
+// One reciprocal per pivot, multiplications elsewhere: an FP64 division is a long
+// instruction sequence on a pipe that runs at 1/64 of the FP32 rate, and this runs in
+// one thread at the end of every block iteration.
 __device__ void chol_solve_drop(const double *S, const double *M, double *X) {
   double L[4][4] = {{0.0}};
+  double inv[4] = {0.0, 0.0, 0.0, 0.0};
   bool keep[4];
   double smax = 0.0;
   for (int j = 0; j < 4; ++j) smax = fmax(smax, S[5 * j]);
@@ -81,11 +85,12 @@ __device__ void chol_solve_drop(const double *S, const double *M, double *X) {
     keep[j] = smax > 0.0 && d > tol && isfinite(d);
     if (!keep[j]) continue;
     L[j][j] = sqrt(d);
+    inv[j] = 1.0 / L[j][j];
     for (int i = j + 1; i < 4; ++i) {
       double v = S[4 * i + j];
       for (int k = 0; k < j; ++k)
         if (keep[k]) v -= L[i][k] * L[j][k];
-      L[i][j] = v / L[j][j];
+      L[i][j] = v * inv[j];
     }
   }
   double Y[4][4];
@@ -95,7 +100,7 @@ __device__ void chol_solve_drop(const double *S, const double *M, double *X) {
       double v = M[4 * i + c];
       for (int k = 0; k < i; ++k)
         if (keep[k]) v -= L[i][k] * Y[k][c];
-      Y[i][c] = v / L[i][i];
+      Y[i][c] = v * inv[i];
     }
   for (int i = 3; i >= 0; --i)
     for (int c = 0; c < 4; ++c) {
@@ -103,7 +108,7 @@ __device__ void chol_solve_drop(const double *S, const double *M, double *X) {
       double v = Y[i][c];
       for (int k = i + 1; k < 4; ++k)
         if (keep[k]) v -= L[k][i] * X[4 * k + c];
-      X[4 * i + c] = v / L[i][i];
+      X[4 * i + c] = v * inv[i];
     }
 }
 
@@ -495,21 +500,9 @@ fg_status fg_sweep_block(fg_mesh *m, int nfield, const double *H0, const fg_solv
     ++r;
   }
 
-  std::vector<void *> tmp;
-  auto alloc = [&](size_t bytes) {
-    void *ptr = nullptr;
-    FG_CUDA_TRY(cudaMalloc(&ptr, std::max<size_t>(bytes, 16)));
-    tmp.push_back(ptr);
-    return ptr;
-  };
-  struct Free {
-    cudaStream_t s;
-    std::vector<void *> &v;
-    ~Free() {
-      cudaStreamSynchronize(s);
-      for (void *p : v) cudaFree(p);
-    }
-  } release{st, tmp};
+  // work space from the device's stream-ordered pool, released on the stream at exit
+  StreamScratch scratch{st, {}};
+  auto alloc = [&](size_t bytes) { return static_cast<void *>(scratch.get<unsigned char>(std::max<size_t>(bytes, 16))); };
   const unsigned nb = grid_for(n, BC_T);
   double *X = (double *)alloc(sizeof(double) * 4 * n), *R = (double *)alloc(sizeof(double) * 4 * n);
   float4 *r32 = (float4 *)alloc(sizeof(float4) * n), *z32 = (float4 *)alloc(sizeof(float4) * n);
@@ -552,7 +545,24 @@ fg_status fg_sweep_block(fg_mesh *m, int nfield, const double *H0, const fg_solv
   int total = 0, refinements = 0;
   bool all_done = false;
   double worst = 0.0;
-  const int check = std::max(4, o.check_every);
+  // an even number of iterations per host check: the two direction buffers return
+  // to their roles, so one captured graph of `check` iterations serves every check
+  const int check = (std::max(4, o.check_every) + 1) & ~1;
+  cudaGraphExec_t body = nullptr;
+  struct BodyGraph {
+    cudaGraphExec_t &g;
+    ~BodyGraph() {
+      if (g) cudaGraphExecDestroy(g);
+    }
+  } body_guard{body};
+  auto enqueue_body = [&]() {
+    float4 *po = p0, *pn = p1;
+    for (int k = 0; k < check; ++k) {
+      k_bc_spmm32<<<nb, BC_T, 0, st>>>(A, m->val32, z32, po, pn, q32, scal, ctl, fpart, counter);
+      k_bc_update32<<<nb, BC_T, 0, st>>>(n, m->dinv32, pn, q32, r32, z32, x32, scal, ctl, fpart, counter);
+      std::swap(po, pn);
+    }
+  };
   for (int ref = 0; ref < 50; ++ref) {
     k_bc_resid64<<<nb, BC_T, 0, st>>>(A, m->val64, X, R, gpart);
     k_bc_gram<<<1, 32 * BC_SYM, 0, st>>>(gpart, (int)nb, gram);
@@ -585,14 +595,23 @@ fg_status fg_sweep_block(fg_mesh *m, int nfield, const double *H0, const fg_solv
     k_bc_init32<<<nb, BC_T, 0, st>>>(n, R, Col4{{sc[0], sc[1], sc[2], sc[3]}}, inner * inner,
                                      o.maxiter - total, m->dinv32, r32, z32, p0, x32, scal, ctl, fpart, counter);
     FG_LAUNCHED(1);
-    float4 *pold = p0, *pnew = p1;
     int it = 0;
-    for (;;) {
-      for (int k = 0; k < check; ++k) {
-        k_bc_spmm32<<<nb, BC_T, 0, st>>>(A, m->val32, z32, pold, pnew, q32, scal, ctl, fpart, counter);
-        k_bc_update32<<<nb, BC_T, 0, st>>>(n, m->dinv32, pnew, q32, r32, z32, x32, scal, ctl, fpart, counter);
-        std::swap(pold, pnew);
+    if (!body) {
+      // the iterations of one host check as one graph launch
+      cudaGraph_t graph = nullptr;
+      FG_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      enqueue_body();
+      const cudaError_t ce = cudaStreamEndCapture(st, &graph);
+      const cudaError_t ie = (ce == cudaSuccess) ? cudaGraphInstantiate(&body, graph, 0) : ce;
+      if (graph) cudaGraphDestroy(graph);
+      if (ie != cudaSuccess) {
+        body = nullptr;
+        cudaGetLastError();
       }
+    }
+    for (;;) {
+      if (body) FG_CUDA_TRY(cudaGraphLaunch(body, st));
+      else enqueue_body();
       FG_LAUNCHED(2LL * check);
       FG_CUDA_TRY(cudaGetLastError());
       FG_CUDA_TRY(cudaMemcpyAsync(m->hint, ctl, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));

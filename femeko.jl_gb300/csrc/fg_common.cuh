@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -260,6 +261,22 @@ struct fg_mesh {
 // of paying a synchronising cudaMalloc/cudaFree per buffer (fg_setup.cu keeps the
 // pool's memory when it is freed).
 void fg_pool_init(int device);
+// Temporary device buffers from the stream-ordered pool, released on the stream when
+// the holder goes out of scope (normally or by an exception).
+struct StreamScratch {
+  cudaStream_t s;
+  std::vector<void *> held;
+  template <class T>
+  T *get(size_t count) {
+    void *q = nullptr;
+    FG_CUDA_TRY(cudaMallocAsync(&q, sizeof(T) * std::max<size_t>(count, 1), s));
+    held.push_back(q);
+    return static_cast<T *>(q);
+  }
+  ~StreamScratch() {
+    for (void *q : held) cudaFreeAsync(q, s);
+  }
+};
 // Pinned host blocks of FG_PINNED_BLOCK bytes for a handle's small read-backs
 // (hbuf: 64 doubles, hint: 16 ints after it), recycled across handles:
 // cudaMallocHost pins pages and cudaFreeHost waits for the device, both per handle

@@ -552,23 +552,6 @@ __global__ void k_tmax256(const int *__restrict__ sl_ptr, int nslices, int64_t *
 
 // ------------------------------------------------------------------ host side
 
-// Temporary device buffers from the stream-ordered pool, released on the stream when
-// the holder goes out of scope (normally or by an exception).
-struct StreamScratch {
-  cudaStream_t s;
-  std::vector<void *> held;
-  template <class T>
-  T *get(size_t count) {
-    void *q = nullptr;
-    FG_CUDA_TRY(cudaMallocAsync(&q, sizeof(T) * std::max<size_t>(count, 1), s));
-    held.push_back(q);
-    return static_cast<T *>(q);
-  }
-  ~StreamScratch() {
-    for (void *q : held) cudaFreeAsync(q, s);
-  }
-};
-
 // The default memory pool of a device keeps the memory freed to it (no release
 // threshold) for the next handle; set once per device for this process.
 void fg_pool_init(int device) {

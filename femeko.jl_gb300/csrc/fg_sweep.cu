@@ -322,21 +322,12 @@ static fg_status sweep_impl(fg_mesh *m, int nfield, const double *H0, const fg_s
   constexpr int NR = 32 * J;
   const int64_t n = m->nv;
   const size_t blk = (size_t)n * NR;
-  // work space, released at the end of the call
-  std::vector<void *> tmp;
-  auto alloc = [&](size_t bytes) {
-    void *ptr = nullptr;
-    FG_CUDA_TRY(cudaMalloc(&ptr, std::max<size_t>(bytes, 16)));
-    tmp.push_back(ptr);
-    return ptr;
-  };
-  struct Free {
-    std::vector<void *> &v;
-    ~Free() {
-      for (void *p : v) cudaFree(p);
-    }
-  } release{tmp};
+  // work space from the stream-ordered pool, released on the stream at the end of the call
   cudaStream_t st = m->stream;
+  StreamScratch scratch{st, {}};
+  auto alloc = [&](size_t bytes) {
+    return static_cast<void *>(scratch.get<unsigned char>(std::max<size_t>(bytes, 16)));
+  };
   const int nblocks = std::max(1, std::min<int>(m->sm_count * 8, (int)((n + SW_WARPS - 1) / SW_WARPS)));
   double *X = (double *)alloc(sizeof(double) * blk), *R = (double *)alloc(sizeof(double) * blk);
   float *r = (float *)alloc(sizeof(float) * blk), *p0 = (float *)alloc(sizeof(float) * blk);
