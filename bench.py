@@ -791,7 +791,7 @@ def _mean_hx(fg, mesh, target, u):
 def case_adjoint(args):
     """dJ/dmur for J = mean Hx over elements with centroid in |x| < 0.5 on the 64^3
     mesh, mur ~ U[1,1000]: adjoint cost against the forward solve, and central
-    differences (relative step 1e-4) on 32 elements.  --nonlinear: the same through
+    differences (relative step 1e-6) on 32 elements.  --nonlinear: the same through
     the converged Newton Jacobian with the Froehlich plate of the 96^3 workload."""
     import femeko_gpu as fg
     from femeko_gpu.mesh import box_tet_mesh
@@ -810,30 +810,51 @@ def case_adjoint(args):
         kw.update(tol_update=1e-10)
     fg.adjoint_dJdmu(mesh, mur, u0, target, **kw)                           # warm-up
     J, grad, u, st = fg.adjoint_dJdmu(mesh, mur, u0, target, **kw)
-    # central differences on 32 elements among those with at least 1% of the largest
-    # sensitivity; each perturbed solve starts from the converged u (FP64, tight).
-    # Relative step 1e-4: the perturbed solves reduce the perturbation's residual, and
-    # FP64 rounding in forming it from the whole field limits the perturbation's
-    # accuracy to about eps * |b| / |r0|, which grows as the step shrinks; the
-    # truncation error of a central difference is of order step^2
-    rel_step = 1e-4
+    # central differences with relative step 1e-6 on 32 elements among those with at
+    # least 1% of the largest sensitivity.  Linear: each perturbed solution is u + du
+    # with A(mu +- d) du = -(+-d) dA/dmur_k u on the free nodes (a right-hand side
+    # local to element k, free of the cancellation that forming b - A(mu +- d) u from
+    # the whole field would bring); J is linear in u.  Nonlinear: perturbed Newton
+    # solves (FP64, tight) from the converged u.
+    rel_step = 1e-6
     pool = np.flatnonzero(np.abs(grad) >= 1e-2 * np.abs(grad).max())
     if args.nonlinear:
         pool = pool[nl[pool] == 0]
     picks = np.random.default_rng(11).choice(pool, min(32, pool.size), replace=False)
     errs = []
+    if not args.nonlinear:
+        import scipy.sparse as sp
+        fixed = mesh.dirichlet_mask().astype(bool)
+        free = np.flatnonzero(~fixed)
+        Kff = fg.stiffnessMatrix(mesh, mur * fg.MU0).tocsr()[free][:, free].tocsc()
+        pos = np.full(mesh.nv, -1)
+        pos[free] = np.arange(free.size)
     for k in picks:
         d = rel_step * mur[k]
         us = []
+        if not args.nonlinear:
+            nodes = mesh.t[:4, k]
+            Pm = np.vstack([np.ones(4), mesh.p[:, nodes]])
+            Gk = np.linalg.inv(Pm)[:, 1:4]
+            Ek = fg.MU0 * mesh.VE[k] * (Gk @ Gk.T)            # dA/dmur_k on the element
+            gk = Ek @ u[nodes]
+            keep = pos[nodes] >= 0
+            fi = pos[nodes][keep]
+            Pk = sp.csc_matrix((Ek[np.ix_(keep, keep)].ravel(), (np.repeat(fi, fi.size), np.tile(fi, fi.size))),
+                               shape=Kff.shape)
         for sgn in (+1, -1):
-            mu2 = mur * fg.MU0
-            mu2[k] = (mur[k] + sgn * d) * fg.MU0
             if args.nonlinear:
+                mu2 = mur * fg.MU0
+                mu2[k] = (mur[k] + sgn * d) * fg.MU0
                 u2, _, _, s2 = fg.newton_magnetostatics(mesh, nl, mu2, u, precision="fp64", tol_update=1e-14,
                                                         forcing="fixed", inner_rtol=1e-14, picard_steps=0)
+                us.append(u2)
             else:
-                u2, _, s2 = fg.magnetostatics_linear(mesh, mu2, u, precision="fp64", rtol=1e-14)
-            us.append(u2)
+                rhs = np.zeros(free.size)
+                rhs[fi] = -sgn * d * gk[keep]
+                du = np.zeros(mesh.nv)
+                du[free] = fg.cg(Kff + sgn * d * Pk, rhs, reltol=1e-12, precision="fp64")
+                us.append(du)
         fd = _mean_hx(fg, mesh, target, us[0] - us[1]) / (2 * d)
         errs.append(abs(fd - grad[k]) / abs(grad[k]))
     what = "Froehlich-plate Newton magnetostatics" if args.nonlinear else "linear magnetostatics"
