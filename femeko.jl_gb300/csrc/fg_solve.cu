@@ -3012,13 +3012,21 @@ fg_status fg_bench_cg_kernel(fg_mesh *m, int which, int precision, int reps, dou
 // shape (or on request).  The variants that hold their values in a persisting-L2
 // window set L2 aside for the whole context (every other kernel of the process
 // loses it): one is kept only when it beats the fastest variant without a window
-// by more than kWindowMargin.  The pipelined variants are never kept.
+// by more than kWindowMargin.  The pipelined variants are never kept, and neither are
+// those on the Jacobi-scaled system (16, 20): the same iterates as Jacobi-PCG in exact
+// arithmetic, but in FP32 a 96^3 Newton solve took 1,427 CG iterations with them
+// against 1,329, which a per-iteration timing does not see.
+// Near-ties (within kTieMargin of the fastest) go to the bulk-staged split variants
+// with the split reduction (22, then 23): entries staged through shared memory, the
+// SpMV nearest the copy bandwidth when timed alone, so that the choice between
+// variants a few tenths of a microsecond apart does not follow timing noise.
 constexpr double kWindowMargin = 0.05;
+constexpr double kTieMargin = 0.03;
 fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_variant) {
   FG_REQUIRE(m->val32 != nullptr, FG_BAD_ARG, "autotune: no FP32 operator assembled");
   reps = std::max(64, (reps + 31) / 32 * 32);  // whole bodies of the solver's graph loop
-  int best = 0, best_win = -1;
-  double best_us = 1e30, best_win_us = 1e30;
+  int best = 0, best_win = -1, best_pref = -1;
+  double best_us = 1e30, best_win_us = 1e30, best_pref_us = 1e30;
   for (int v = 0; v < FG_N_SPMV32; ++v) {
     if (!variant32_available(m, v) || (v_window(v) && !prepare_l2(m))) {  // not available here
       if (us_per_variant) us_per_variant[v] = 0.0;
@@ -3029,15 +3037,18 @@ fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_v
     reset_persisting_l2(m);
     const double us = loop_us_per_iteration(m, true, reps);
     if (us_per_variant) us_per_variant[v] = us;
-    if (v_pipe(v)) continue;
+    if (v_pipe(v) || v_scaled(v)) continue;
     if (v_window(v)) {
       if (us < best_win_us) { best_win_us = us; best_win = v; }
     } else if (us < best_us) {
       best_us = us;
       best = v;
     }
+    if (v_splitred(v) && us < best_pref_us) { best_pref_us = us; best_pref = v; }
   }
-  if (best_win >= 0 && best_win_us < (1.0 - kWindowMargin) * best_us) best = best_win;
+  double chosen_us = best_us;
+  if (best_win >= 0 && best_win_us < (1.0 - kWindowMargin) * best_us) { best = best_win; chosen_us = best_win_us; }
+  if (best_pref >= 0 && best_pref_us <= (1.0 + kTieMargin) * chosen_us) best = best_pref;
   m->spmv_variant32 = best;
   m->tuned32 = true;
   if (chosen) *chosen = best;

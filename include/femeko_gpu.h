@@ -84,7 +84,9 @@ enum {
  * The autotuner times each variant through the solver's own graph loop (64
  * iterations after an untimed run) and keeps the fastest; a variant with an L2
  * window (11, 21, 22), which sets L2 aside for the whole context, only when it is
- * more than 5 % faster than every variant without one. */
+ * more than 5 % faster than every variant without one; the Jacobi-scaled ones (17,
+ * 21) are timed but not kept (in FP32 their iterates need more iterations); within
+ * 3 % of the fastest, 23 or 24 is kept. */
 enum { FG_SPMV_AUTO = 0 };
 
 typedef struct fg_mesh fg_mesh;
