@@ -330,7 +330,9 @@ def run_ours(args):
              "split, bulk-staged entries, persistent 3/SM, dots finished by a one-block kernel",
              "pipelined CG, bulk-staged SpMV 4/SM, dots finished by one SpMV block (forced only)",
              "pipelined CG, bulk-staged SpMV 3/SM, dots finished by one SpMV block (forced only)",
-             "split iteration in one persistent cooperative launch, grid barriers, 4/SM"]
+             "split iteration in one persistent cooperative launch, grid barriers, 4/SM",
+             "split, bulk-staged entries, persistent 4/SM, dots finished by the last SpMV block",
+             "split, bulk-staged entries, persistent 3/SM, dots finished by the last SpMV block"]
     variants_us = np.zeros(len(names))
     # the table of every variant on the converged operator (a second timing); the
     # per-kernel figures below are for the variant the timed solves used
@@ -417,7 +419,9 @@ def run_ours(args):
         alg_bytes = g.nnz * 6 + 12 * n
         kname = {7: "k_cg32s_spmv_halo", 17: "k_cg32s_spmv_bulk", 18: "k_cg32s_spmv_bulk",
                  19: "k_cg32s_spmv_bulk", 21: "k_cg32s_spmv_bulk",
-                 22: "k_cg32s_spmv_bulk<split>", 23: "k_cg32s_spmv_bulk<split>"}.get(v, "k_cg32s_spmv")
+                 22: "k_cg32s_spmv_bulk<split>", 23: "k_cg32s_spmv_bulk<split>",
+                 27: "k_cg32s_spmv_bulk<split, last-block finish>",
+                 28: "k_cg32s_spmv_bulk<split, last-block finish>"}.get(v, "k_cg32s_spmv")
     else:
         # one fused iteration: matrix as above; per row the (r, w, s, dinv) state read
         # and written (16 + 16 B) and p, x read and written (8 + 8 B)
@@ -444,6 +448,18 @@ def run_ours(args):
         it_bytes = g.nnz * 6 + 12 * n + 48 * n
     else:
         it_bytes = alg_bytes
+    # the last-block-finish variants: their SpMV code without the finishing tail (the
+    # split sibling, 22 or 23, whose kernel is the same up to the partials) timed alone
+    spmv_part = None
+    if v in (27, 28):
+        ms_part = C.c_double()
+        L.check(lib.fg_set_cg_variant(g.h, L.FG_MIXED, v - 5 + 1))
+        L.check(lib.fg_bench_kernel(g.h, 0, L.FG_MIXED, 200, C.byref(ms_part)))
+        L.check(lib.fg_set_cg_variant(g.h, L.FG_MIXED, v + 1))
+        part_gbs = alg_bytes / (ms_part.value * 1e-3) / 1e9
+        spmv_part = {"us_per_launch": ms_part.value * 1e3, "achieved": part_gbs, "frac": part_gbs / peak,
+                     "finish_tail_us": (t_dom - ms_part.value) * 1e3,
+                     "what": "the same SpMV without its last-block finish (the split variant's kernel), timed alone"}
     it_roof = None
     if it_bytes is not None:
         it_gbs = it_bytes / (ms_loop.value * 1e-3) / 1e9
@@ -456,7 +472,7 @@ def run_ours(args):
                 "us_per_launch": t_dom * 1e3,
                 "timing": ("one CG iteration of the persistent launch, in the solver's loop" if v == 26
                            else "one launch, CUDA events on the library's stream"),
-                "cg_iteration": it_roof}
+                "cg_iteration": it_roof, "spmv_without_finish": spmv_part}
 
     # e2e through the one-shot C ABI with pinned host buffers
     e2e = None
@@ -973,7 +989,7 @@ def main():
     ap.add_argument("--graph-mode", type=int, default=1, choices=[0, 1, 2],
                     help="1: whole CG in one graph launch (device-side loop); 2: host-checked graph blocks; 0: no graph")
     ap.add_argument("--cg-variant", type=int, default=0,
-                    help="fix the FP32 CG kernel variant (1..27; 0: autotuned), e.g. for profiling runs")
+                    help="fix the FP32 CG kernel variant (1..29; 0: autotuned), e.g. for profiling runs")
     ap.add_argument("--cg64-variant", type=int, default=0, help="fix the FP64 CG SpMV variant (1..4; 0: autotuned)")
     ap.add_argument("--case", choices=sorted(CASES), default=None,
                     help="run a secondary workload instead of the headline benchmark")

@@ -23,6 +23,9 @@ __device__ __forceinline__ ff ff_add(ff a, ff b) {
 // Group totals sit right after the block partials (gridDim.x * N doubles).  Returns
 // true in thread 0 of the finishing block, with the totals in tot.
 constexpr int FG_ARRIVE_GROUPS = 64;
+// The arrival counter of single-level "last block finishes" reductions (above the
+// counters the two-level reduction uses, 0..FG_ARRIVE_GROUPS).
+constexpr int FG_LAST1_COUNTER = 100;
 
 // Arrival: an atomic add with release (the partials written before it are visible to
 // whoever acquires the counter later) and acquire semantics at GPU scope; lighter

@@ -662,14 +662,40 @@ __global__ void __launch_bounds__(R) k_cg32s_spmv_halo(int64_t n, const int *__r
   if (finish_dots32(dots, partials, counter, tot)) cgcg_scalars(tot, scal, ictl);
 }
 
+// Thread-level part of the sum of nparts per-block (hi, lo) partials of three dot
+// products by a 256-thread block: thread t adds partials t, t + 256, t + 512, ... in
+// that order, with the loads of U consecutive ones issued before any add (a block
+// that waits on L2 once instead of U times).
+template <int U>
+__device__ __forceinline__ void sum_partials_ff3(const float2 *__restrict__ partials, int nparts, ff (&acc)[3]) {
+  for (int base = threadIdx.x; base < nparts; base += 256 * U) {
+    float2 q[U][3];
+#pragma unroll
+    for (int i = 0; i < U; ++i) {
+      const int k = base + 256 * i;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) q[i][j] = (k < nparts) ? __ldcg(partials + (size_t)k * 3 + j) : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int i = 0; i < U; ++i)
+      if (base + 256 * i < nparts)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) acc[j] = ff_add(acc[j], ff{q[i][j].x, q[i][j].y});
+  }
+}
+
 // The split SpMV with the matrix entries staged by the bulk-copy engine: a persistent
 // grid whose blocks walk their 256-row blocks; while a block computes one, the values
 // and column offsets of its next one (two contiguous ranges of the SELL layout) are
 // in flight into the other shared-memory stage (cp.async.bulk completing on an
 // mbarrier).  Threads read their row's entries from shared memory and gather u from
 // global memory.  cap: the most padded entries of one 256-row block.  A stage that
-// does not arrive within the bounded wait stops the CG with I_FAULT set.
-template <class CI, bool SPLIT = false>
+// does not arrive within the bounded wait stops the CG with I_FAULT set.  SPLIT: each
+// block leaves its compensated partials (float pairs) and returns; with LAST1 the
+// last block to arrive (one counter) then adds all of them, in the order and with the
+// arithmetic of k_cg32_dots_finish, and sets the scalars: one level of arrivals and no
+// separate finishing launch.
+template <class CI, bool SPLIT = false, bool LAST1 = false>
 __global__ void __launch_bounds__(256) k_cg32s_spmv_bulk(int64_t n, int nslices, int cap,
                                                          const int *__restrict__ sl_ptr,
                                                          const int *__restrict__ sl_len,
@@ -779,32 +805,28 @@ __global__ void __launch_bounds__(256) k_cg32s_spmv_bulk(int64_t n, int nslices,
       float2 *fp = reinterpret_cast<float2 *>(partials);
       for (int j = 0; j < 3; ++j) fp[(size_t)blockIdx.x * 3 + j] = make_float2(v[j].hi, v[j].lo);
     }
+    if (!LAST1) return;
+    __shared__ int s_last;
+    if (tid == 0) {
+      // release: the partials above are visible to the block that arrives last
+      s_last = (atom_add_acq_rel(counter + FG_LAST1_COUNTER, 1u) == gridDim.x - 1) ? 1 : 0;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    ff acc[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    sum_partials_ff3<4>(reinterpret_cast<const float2 *>(partials), (int)gridDim.x, acc);
+    block_sum_ff_pair<3>(acc, shs);
+    if (tid == 0) {
+      counter[FG_LAST1_COUNTER] = 0u;
+      double tot[3];
+      for (int j = 0; j < 3; ++j) tot[j] = (double)acc[j].hi + (double)acc[j].lo;
+      cgcg_scalars(tot, scal, ictl);
+    }
     return;
   }
   double tot[3];
   if (finish_dots32(dots, partials, counter, tot) && ok) cgcg_scalars(tot, scal, ictl);
-}
-
-// Thread-level part of the sum of nparts per-block (hi, lo) partials of three dot
-// products by a 256-thread block: thread t adds partials t, t + 256, t + 512, ... in
-// that order, with the loads of U consecutive ones issued before any add (a block
-// that waits on L2 once instead of U times).
-template <int U>
-__device__ __forceinline__ void sum_partials_ff3(const float2 *__restrict__ partials, int nparts, ff (&acc)[3]) {
-  for (int base = threadIdx.x; base < nparts; base += 256 * U) {
-    float2 q[U][3];
-#pragma unroll
-    for (int i = 0; i < U; ++i) {
-      const int k = base + 256 * i;
-#pragma unroll
-      for (int j = 0; j < 3; ++j) q[i][j] = (k < nparts) ? __ldcg(partials + (size_t)k * 3 + j) : make_float2(0.f, 0.f);
-    }
-#pragma unroll
-    for (int i = 0; i < U; ++i)
-      if (base + 256 * i < nparts)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) acc[j] = ff_add(acc[j], ff{q[i][j].x, q[i][j].y});
-  }
 }
 
 // The dot products of the split-reduction SpMV (k_cg32s_spmv_bulk<CI, true>): one
@@ -1766,14 +1788,17 @@ static void ensure_cg64(fg_mesh *m) {
 // inner solves asked for 1e-6 stall (Newton's tight Eisenstat-Walker steps), and on
 // singular systems they diverge; they run only when forced.  26: the split iteration
 // of 22 run by one persistent cooperative launch for many iterations (grid barriers
-// in place of kernel boundaries, the matrix prefetched across them).
-constexpr int FG_N_SPMV32 = 27;
+// in place of kernel boundaries, the matrix prefetched across them).  27 and 28:
+// variants 22 and 23 with the partials added by the last SpMV block to arrive instead
+// of a one-block kernel (one launch fewer per iteration, the same iterates).
+constexpr int FG_N_SPMV32 = 29;
 // Split FP32 variants on the scaled system, with the values in the L2 window, and
 // with the matrix entries staged by bulk copies.
 static inline bool v_scaled(int v) { return v == 16 || v == 20; }
 static inline bool v_window(int v) { return v == 10 || v == 20 || v == 21; }
-static inline bool v_bulk(int v) { return (v >= 17 && v <= 19) || (v >= 21 && v <= 23); }
+static inline bool v_bulk(int v) { return (v >= 17 && v <= 19) || (v >= 21 && v <= 23) || v == 27 || v == 28; }
 static inline bool v_splitred(int v) { return v == 22 || v == 23; }
+static inline bool v_last1(int v) { return v == 27 || v == 28; }
 static inline bool split32(int v) { return v >= 6; }
 static inline bool v_pipe(int v) { return v == 24 || v == 25; }
 static inline bool v_coop(int v) { return v == 26; }
@@ -2044,8 +2069,9 @@ static size_t bulk_smem(const fg_mesh *m) {
 // device's opt-in shared memory (set once per process).
 static int bulk_per_sm(fg_mesh *m, int v) {
   // 17-19, (20: not bulk), 21: 17 with the L2 window, 22 and 23: 17 and 18 with the
-  // split reduction
-  static const int kWant[7] = {4, 3, 2, 4, 4, 4, 3};
+  // split reduction, (24-26 sized elsewhere), 27 and 28: 22 and 23 finished by the
+  // last block
+  static const int kWant[12] = {4, 3, 2, 4, 4, 4, 3, 4, 3, 4, 4, 3};
   if (m->bulk_fit < 0) {
     static std::once_flag attr_once;
     static int dyn_max = 0;  // opt-in shared memory less the kernels' static shared memory
@@ -2066,7 +2092,11 @@ static int bulk_per_sm(fg_mesh *m, int v) {
           cudaFuncSetAttribute(k_cg32s_spmv_bulk<ColRel, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, d) !=
               cudaSuccess ||
           cudaFuncSetAttribute(k_cg32s_spmv_bulk<ColAbs, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, d) !=
-              cudaSuccess) {
+              cudaSuccess ||
+          cudaFuncSetAttribute(k_cg32s_spmv_bulk<ColRel, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               d) != cudaSuccess ||
+          cudaFuncSetAttribute(k_cg32s_spmv_bulk<ColAbs, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               d) != cudaSuccess) {
         cudaGetLastError();
         return;
       }
@@ -2100,6 +2130,16 @@ static void bulk_launch32(fg_mesh *m, int v) {
       l2_launch(m, m->val32, k_cg32s_spmv_bulk<ColAbs>, g, 256, smem, m->nv, m->nslices, m->tmax256, m->sl_ptr,
                 m->sl_len, m->sl_col, m->val32, m->v32[7], m->v32[4], m->v32[5], m->scal, m->ictl,
                 m->red.partials, m->red.counter);
+  } else if (v_last1(v)) {
+    // per-block partials; the last block to arrive adds them and sets the scalars
+    if (m->use_dcol)
+      k_cg32s_spmv_bulk<ColRel, true, true><<<g, 256, smem, m->stream>>>(
+          m->nv, m->nslices, m->tmax256, m->sl_ptr, m->sl_len, m->sl_dcol, m->val32, m->v32[7], m->v32[4],
+          m->v32[5], m->scal, m->ictl, m->red.partials, m->red.counter);
+    else
+      k_cg32s_spmv_bulk<ColAbs, true, true><<<g, 256, smem, m->stream>>>(
+          m->nv, m->nslices, m->tmax256, m->sl_ptr, m->sl_len, m->sl_col, m->val32, m->v32[7], m->v32[4],
+          m->v32[5], m->scal, m->ictl, m->red.partials, m->red.counter);
   } else if (v_splitred(v)) {
     // per-block partials, then one block adds them and sets the scalars
     if (m->use_dcol)
@@ -3044,7 +3084,7 @@ fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_v
       best_us = us;
       best = v;
     }
-    if (v_splitred(v) && us < best_pref_us) { best_pref_us = us; best_pref = v; }
+    if ((v_splitred(v) || v_last1(v)) && us < best_pref_us) { best_pref_us = us; best_pref = v; }
   }
   double chosen_us = best_us;
   if (best_win >= 0 && best_win_us < (1.0 - kWindowMargin) * best_us) { best = best_win; chosen_us = best_win_us; }

@@ -189,7 +189,7 @@ def BoundaryIntegral(mesh: MESH, F, shell_id=(1,)):
 
 def solve_opts(precision="fp64", rtol=1e-10, maxiter=1_000_000, inner_rtol=1e-5, check_every=32, use_graph=True,
                spmv=0):
-    """Linear-solve options; spmv = 0 autotunes the FP32 CG iteration kernel, 1..27 forces a variant."""
+    """Linear-solve options; spmv = 0 autotunes the FP32 CG iteration kernel, 1..29 forces a variant."""
     o = L.SolveOpts()
     L.lib().fg_solve_opts_default(C.byref(o))
     o.precision = L.FG_MIXED if precision == "mixed" else L.FG_FP64

@@ -52,7 +52,7 @@ enum {
                           of |F(u + a du)|^2, kept in [0.1, 0.5] of the last step */
 };
 /* FP32 CG iteration kernel: FG_SPMV_AUTO lets the autotuner time the variants on
- * the first mixed solve of a handle and keep the fastest; k = 1..27 forces variant
+ * the first mixed solve of a handle and keep the fastest; k = 1..29 forces variant
  * k-1.  One fused kernel per iteration: 1: 4x-unrolled gather loop, 256 threads;
  * 2: all row loads issued first, 256 threads; 3: loop, 128 threads; 4: loop, 512
  * threads; 5: halo staging (the neighbour entries of a block of rows gathered once
@@ -80,13 +80,15 @@ enum {
  * on singular systems): they run only when forced; 27: the iteration of 23 run by ONE
  * persistent cooperative launch for up to 1024 iterations (grid barriers in place of
  * kernel boundaries; the last block at the closing barrier adds the dot products;
- * each block's matrix entries prefetched across the barriers).
+ * each block's matrix entries prefetched across the barriers); 28, 29: 23 and 24 with
+ * the partials added by the last SpMV block to arrive (one arrival counter) instead of
+ * a separate one-block kernel: the same iterates, one launch fewer per iteration.
  * The autotuner times each variant through the solver's own graph loop (64
  * iterations after an untimed run) and keeps the fastest; a variant with an L2
  * window (11, 21, 22), which sets L2 aside for the whole context, only when it is
  * more than 5 % faster than every variant without one; the Jacobi-scaled ones (17,
  * 21) are timed but not kept (in FP32 their iterates need more iterations); within
- * 3 % of the fastest, 23 or 24 is kept. */
+ * 3 % of the fastest, 23, 24, 28 or 29 is kept. */
 enum { FG_SPMV_AUTO = 0 };
 
 typedef struct fg_mesh fg_mesh;
@@ -100,7 +102,7 @@ typedef struct fg_solve_opts {
   int32_t use_graph;   /* 1: the whole CG as one CUDA graph launch (a WHILE node around
                           check_every iterations, the test on the device); 2: a graph of
                           check_every iterations per launch, tested on the host; 0: no graph */
-  int32_t spmv;        /* FG_SPMV_AUTO or a forced variant 1..27 */
+  int32_t spmv;        /* FG_SPMV_AUTO or a forced variant 1..29 */
   int32_t reserved_;
 } fg_solve_opts;
 
@@ -512,7 +514,7 @@ fg_status fg_bench_kernel(fg_mesh *m, int32_t which, int32_t precision, int32_t 
  * be NULL) the measured microseconds per launch.  No reference counterpart. */
 fg_status fg_autotune(fg_mesh *m, int32_t precision, int32_t *variant, double *us_per_variant, int32_t n_slots);
 /* Fixes the CG kernel variant of one precision for the handle (the numbering of
- * fg_solve_opts.spmv: FG_MIXED 1..27, FG_FP64 1..4), or 0 to return to the
+ * fg_solve_opts.spmv: FG_MIXED 1..29, FG_FP64 1..4), or 0 to return to the
  * autotuner's choice at the next solve.  The autotuner's choices are remembered per
  * process for each operator shape (device, rows, padded entries, longest row), so a
  * new handle for a mesh of the same structure does not time the variants again.
