@@ -684,10 +684,16 @@ def case_heat(args):
     x0 = rng.uniform(-2.5, 2.5, 3)
     T0 = np.exp(-(((mesh.p - x0[:, None]) ** 2).sum(axis=0)) / 0.5 ** 2)
     res = {}
+    variant = {}
     for prec in ("fp64", "mixed"):
         fg.heat_be(mesh, T0, kappa, nsteps=2, every=0, precision=prec, use_graph=args.graph_mode)   # warm-up
         T, snaps, st = fg.heat_be(mesh, T0, kappa, nsteps=100, every=10, precision=prec, use_graph=args.graph_mode)
         res[prec] = (snaps, st)
+        import femeko_gpu._lib as L
+        vv = C.c_int32(-1)
+        L.check(L.lib().fg_get_cg_variant(fg.gpu_mesh(mesh).h, L.FG_MIXED if prec == "mixed" else L.FG_FP64,
+                                          C.byref(vv)))
+        variant[prec] = int(vv.value)
     err = [float(np.linalg.norm(a - b) / np.linalg.norm(b)) for a, b in zip(res["mixed"][0], res["fp64"][0])]
     ms_m, ms_d = res["mixed"][1]["ms"], res["fp64"][1]["ms"]
     # bandwidth per CG iteration with the whole step time charged to the iterations
@@ -707,7 +713,7 @@ def case_heat(args):
            "nodes": int(mesh.nv)},
           {"fp64_steps_per_s": 100 / (ms_d * 1e-3), "mixed_over_fp64": ms_d / ms_m,
            "cg_iters": {"mixed": res["mixed"][1]["iterations"], "fp64": res["fp64"][1]["iterations"]},
-           "rel_err_mixed_vs_fp64_every_10th_step": err,
+           "rel_err_mixed_vs_fp64_every_10th_step": err, "cg_variant_forced_index": variant,
            "roofline": {"bound": "hbm", "peak": peak, "peak_source": peak_kind, **roof}})
 
 

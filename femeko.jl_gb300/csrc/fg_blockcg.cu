@@ -511,11 +511,11 @@ fg_status fg_sweep_block(fg_mesh *m, int nfield, const double *H0, const fg_solv
   double *gpart = (double *)alloc(sizeof(double) * BC_SYM * nb);
   double *gram = (double *)alloc(sizeof(double) * 16);
   float2 *fpart = (float2 *)alloc(sizeof(float2) * (BC_SYM + 4) * ((size_t)nb + FG_ARRIVE_GROUPS));
-  unsigned *counter = (unsigned *)alloc(sizeof(unsigned) * (FG_ARRIVE_GROUPS + 1));
+  unsigned *counter = (unsigned *)alloc(sizeof(unsigned) * 128);  // above FG_LAST1_COUNTER
   double *scal = (double *)alloc(sizeof(double) * B_NSCAL);
   int *ctl = (int *)alloc(sizeof(int) * C_NCTL);
   double *dC = (double *)alloc(sizeof(double) * Cm.size());
-  FG_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned) * (FG_ARRIVE_GROUPS + 1), st));
+  FG_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned) * 128, st));
   FG_CUDA_TRY(cudaMemcpyAsync(dC, Cm.data(), sizeof(double) * Cm.size(), cudaMemcpyHostToDevice, st));
   const BcOp A{n, m->sl_ptr, m->sl_len, m->sl_col, m->has_fixed ? m->fixed : nullptr};
 

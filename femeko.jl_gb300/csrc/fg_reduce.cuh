@@ -70,12 +70,43 @@ __device__ __forceinline__ void block_sum_ff_pair(ff (&v)[N], ff (*sh)[32]) {
 // on the FP32 pipe; only the totals become doubles.  GB300 runs FP64 at 1/64 of the
 // FP32 rate: two levels of double block sums on the finishing path cost ~3 us per
 // launch at 96^3.  v: the block's sums in thread 0.
+// Grids of at most FG_LAST1_MAX_BLOCKS blocks finish in one level instead: every
+// block arrives on one counter and the last one adds all partials (index order,
+// strided over its threads), which at a few hundred blocks ends sooner than two
+// chained levels of arrivals; larger grids keep the two levels.  The counter array
+// holds at least FG_LAST1_COUNTER + 1 entries.
+constexpr unsigned FG_LAST1_MAX_BLOCKS = 1024;
 template <int N>
 __device__ __forceinline__ bool grid_finish_ff(const ff (&v)[N], float2 *partials, unsigned *counter,
                                                double (&tot)[N]) {
   __shared__ int s_role;
   __shared__ ff shg[N][32], shf[N][32];
   const unsigned G = gridDim.x;
+  if (G <= FG_LAST1_MAX_BLOCKS) {
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (int j = 0; j < N; ++j) partials[(size_t)blockIdx.x * N + j] = make_float2(v[j].hi, v[j].lo);
+      s_role = (atom_add_acq_rel(counter + FG_LAST1_COUNTER, 1u) == G - 1) ? 1 : 0;
+    }
+    __syncthreads();
+    if (s_role == 0) return false;
+    __threadfence();
+    ff acc[N];
+#pragma unroll
+    for (int j = 0; j < N; ++j) acc[j] = ff{0.f, 0.f};
+    for (unsigned k = threadIdx.x; k < G; k += blockDim.x) {
+      float2 q[N];
+#pragma unroll
+      for (int j = 0; j < N; ++j) q[j] = __ldcg(partials + (size_t)k * N + j);
+#pragma unroll
+      for (int j = 0; j < N; ++j) acc[j] = ff_add(acc[j], ff{q[j].x, q[j].y});
+    }
+    block_sum_ff_pair<N>(acc, shf);
+    if (threadIdx.x == 0) counter[FG_LAST1_COUNTER] = 0u;
+#pragma unroll
+    for (int j = 0; j < N; ++j) tot[j] = (double)acc[j].hi + (double)acc[j].lo;
+    return threadIdx.x == 0;
+  }
   const unsigned grp = blockIdx.x % FG_ARRIVE_GROUPS;
   const unsigned ngroups = G < FG_ARRIVE_GROUPS ? G : FG_ARRIVE_GROUPS;
   const unsigned gsize = (G - grp + FG_ARRIVE_GROUPS - 1) / FG_ARRIVE_GROUPS;

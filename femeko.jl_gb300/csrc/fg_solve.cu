@@ -77,14 +77,36 @@ struct Acc<float> {
   __device__ __forceinline__ void add(float x) { v = ff_add(v, ff{x, 0.f}); }
 };
 
-// The two-level grid reduction of fg_reduce.cuh with FP64 partials: true in thread 0
-// of the finishing block, with the totals in tot.
+// The grid reduction of fg_reduce.cuh with FP64 partials (one level up to
+// FG_LAST1_MAX_BLOCKS blocks, two above): true in thread 0 of the finishing block,
+// with the totals in tot.
 template <int N>
 __device__ __forceinline__ bool grid_finish(const double (&v)[N], double *partials, unsigned *counter,
                                             double (&tot)[N]) {
   __shared__ int s_role;
   __shared__ double shg[N][32], shf[N][32];
   const unsigned G = gridDim.x;
+  if (G <= FG_LAST1_MAX_BLOCKS) {
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (int j = 0; j < N; ++j) partials[(size_t)blockIdx.x * N + j] = v[j];
+      s_role = (atom_add_acq_rel(counter + FG_LAST1_COUNTER, 1u) == G - 1) ? 1 : 0;
+    }
+    __syncthreads();
+    if (s_role == 0) return false;
+    __threadfence();
+    double acc[N];
+#pragma unroll
+    for (int j = 0; j < N; ++j) acc[j] = 0.0;
+    for (unsigned k = threadIdx.x; k < G; k += blockDim.x)
+#pragma unroll
+      for (int j = 0; j < N; ++j) acc[j] += __ldcg(partials + (size_t)k * N + j);
+    block_sum<N>(acc, shf);
+    if (threadIdx.x == 0) counter[FG_LAST1_COUNTER] = 0u;
+#pragma unroll
+    for (int j = 0; j < N; ++j) tot[j] = acc[j];
+    return threadIdx.x == 0;
+  }
   const unsigned grp = blockIdx.x % FG_ARRIVE_GROUPS;
   const unsigned ngroups = G < FG_ARRIVE_GROUPS ? G : FG_ARRIVE_GROUPS;
   const unsigned gsize = (G - grp + FG_ARRIVE_GROUPS - 1) / FG_ARRIVE_GROUPS;
@@ -3057,11 +3079,11 @@ fg_status fg_bench_cg_kernel(fg_mesh *m, int which, int precision, int reps, dou
 // arithmetic, but in FP32 a 96^3 Newton solve took 1,427 CG iterations with them
 // against 1,329, which a per-iteration timing does not see.
 // Near-ties (within kTieMargin of the fastest) go to the bulk-staged split variants
-// with the split reduction (22, then 23): entries staged through shared memory, the
+// with the split reduction (22, 23, 27, 28): entries staged through shared memory, the
 // SpMV nearest the copy bandwidth when timed alone, so that the choice between
 // variants a few tenths of a microsecond apart does not follow timing noise.
 constexpr double kWindowMargin = 0.05;
-constexpr double kTieMargin = 0.03;
+constexpr double kTieMargin = 0.015;
 fg_status fg_autotune_spmv32(fg_mesh *m, int reps, int *chosen, double *us_per_variant) {
   FG_REQUIRE(m->val32 != nullptr, FG_BAD_ARG, "autotune: no FP32 operator assembled");
   reps = std::max(64, (reps + 31) / 32 * 32);  // whole bodies of the solver's graph loop

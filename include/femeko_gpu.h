@@ -88,7 +88,7 @@ enum {
  * window (11, 21, 22), which sets L2 aside for the whole context, only when it is
  * more than 5 % faster than every variant without one; the Jacobi-scaled ones (17,
  * 21) are timed but not kept (in FP32 their iterates need more iterations); within
- * 3 % of the fastest, 23, 24, 28 or 29 is kept. */
+ * 1.5 % of the fastest, 23, 24, 28 or 29 is kept. */
 enum { FG_SPMV_AUTO = 0 };
 
 typedef struct fg_mesh fg_mesh;
