@@ -772,7 +772,8 @@ def case_sweep(args):
 
 def case_batch(args):
     """64 independent linear problems, cells per side ~ U{8..40}, mur ~ U[1,1000] per
-    element, one graph launch (a thread-block cluster per problem, sized by its rows)."""
+    element, one graph launch (a thread-block cluster per problem, sized by its rows),
+    in mixed precision (FP32 PCG inside FP64 refinement on each cluster) and in FP64."""
     import femeko_gpu as fg
     from femeko_gpu.mesh import box_tet_mesh
     rng = np.random.default_rng(SEED)
@@ -780,27 +781,56 @@ def case_batch(args):
     meshes = [box_tet_mesh(int(n), seed=SEED + k) for k, n in enumerate(ns)]
     mus = [rng.uniform(1, 1000, m.nt) * fg.MU0 for m in meshes]
     u0s = [-m.p[0].copy() for m in meshes]
-    fg.batch_magnetostatics_linear(meshes, mus, u0s, rtol=1e-10)              # warm-up (assembly, handles)
-    us, its, st = fg.batch_magnetostatics_linear(meshes, mus, u0s, rtol=1e-10)
     big = int(np.argmax(ns))
-    fg.batch_magnetostatics_linear([meshes[big]], [mus[big]], [u0s[big]], rtol=1e-10)
-    _, its1, st1 = fg.batch_magnetostatics_linear([meshes[big]], [mus[big]], [u0s[big]], rtol=1e-10)
-    # algorithmic bytes per FP64 CG iteration of one problem: value and column of each
-    # stored nonzero (12 B), the vectors x, r, z, p_old, p_new, q, diagonal (read and
-    # written, 80 B per row)
     nnz = np.array([fg.gpu_mesh(m).nnz for m in meshes], dtype=np.float64)
     nv = np.array([m.nv for m in meshes], dtype=np.float64)
-    work = float((its * (12 * nnz + 80 * nv)).sum())
     peak = measured_peaks()[0]
-    ach = work / (st["ms"] * 1e-3) / 1e9
-    _line("batched independent solves/s (64 meshes, one graph launch)", 64 / (st["ms"] * 1e-3), "solves/s",
+    res = {}
+    for prec in ("mixed", "fp64"):
+        fg.batch_magnetostatics_linear(meshes, mus, u0s, rtol=1e-10, precision=prec)   # warm-up (assembly)
+        us, its, st = fg.batch_magnetostatics_linear(meshes, mus, u0s, rtol=1e-10, precision=prec)
+        fg.batch_magnetostatics_linear([meshes[big]], [mus[big]], [u0s[big]], rtol=1e-10, precision=prec)
+        _, its1, st1 = fg.batch_magnetostatics_linear([meshes[big]], [mus[big]], [u0s[big]], rtol=1e-10,
+                                                      precision=prec)
+        # algorithmic bytes per CG iteration of one problem: FP64, value and column of
+        # each stored nonzero (12 B) and the vectors x, r, z, p, q, diagonal (80 B per
+        # row); FP32 inner, 8 B per nonzero and 52 B per row
+        per_nz, per_row = (12, 80) if prec == "fp64" else (8, 52)
+        work = float((its * (per_nz * nnz + per_row * nv)).sum())
+        ach = work / (st["ms"] * 1e-3) / 1e9
+        res[prec] = {"ms": st["ms"], "solves_per_s": 64 / (st["ms"] * 1e-3), "max_iterations": st["max_iterations"],
+                     "total_iterations": st["total_iterations"], "max_refinements": st["max_refinements"],
+                     "converged": st["converged"], "largest_cluster_ctas": st["cluster_ctas"],
+                     "largest_mesh_alone_ms": st1["ms"], "largest_mesh_alone_iterations": int(its1[0]),
+                     "alg_bytes": work, "achieved_GBs": ach, "frac_of_measured_hbm": ach / peak}
+    mx = res["mixed"]
+    _line("batched independent solves/s (64 meshes, one graph launch)", mx["solves_per_s"], "solves/s",
           True, {"workload": "64 linear problems, Kuhn tets 8..40 cells per side", "cells": [int(n) for n in ns],
-                 "total_nodes": int(sum(m.nv for m in meshes))},
-          {"ms": st["ms"], "max_iterations": st["max_iterations"], "total_iterations": st["total_iterations"],
-           "converged": st["converged"], "largest_cluster_ctas": st["cluster_ctas"],
-           "largest_mesh_alone_ms": st1["ms"], "largest_mesh_cells": int(ns[big]),
-           "alg_bytes": work, "achieved_GBs": ach, "frac_of_measured_hbm": ach / peak,
-           "note": "FP64 SpMVs of 8-16 SMs per problem are FP64-pipe bound; the vectors stay in L2"})
+                 "total_nodes": int(sum(m.nv for m in meshes)), "precision": "mixed (FP32 PCG, FP64 refinement)",
+                 "largest_mesh_cells": int(ns[big])},
+          {**mx, "fp64": res["fp64"], "mixed_vs_fp64": res["fp64"]["ms"] / mx["ms"],
+           "note": "the vectors and operators stay in L2; FP64 arithmetic issues at 1/64 of the FP32 rate"})
+
+
+def case_batch_single(args):
+    """One linear problem of --cells per side through the batch launch (one 16- or
+    8-CTA cluster), mixed then FP64: per-iteration time of the cluster PCG (the ncu
+    capture target of the batch kernels)."""
+    import femeko_gpu as fg
+    from femeko_gpu.mesh import box_tet_mesh
+    rng = np.random.default_rng(SEED)
+    m = box_tet_mesh(args.cells, seed=SEED)
+    mu = rng.uniform(1, 1000, m.nt) * fg.MU0
+    u0 = -m.p[0].copy()
+    out = {}
+    for prec in ("mixed", "fp64"):
+        fg.batch_magnetostatics_linear([m], [mu], [u0], rtol=1e-10, precision=prec)
+        _, its, st = fg.batch_magnetostatics_linear([m], [mu], [u0], rtol=1e-10, precision=prec)
+        out[prec] = {"ms": st["ms"], "iterations": int(its[0]), "refinements": st["max_refinements"],
+                     "us_per_iteration": st["ms"] * 1e3 / max(int(its[0]), 1), "cluster_ctas": st["cluster_ctas"]}
+    _line("one problem through the batch launch, us per CG iteration (mixed)", out["mixed"]["us_per_iteration"],
+          "us", False, {"workload": f"linear problem, Kuhn tets {args.cells} cells per side", "rows": int(m.nv)},
+          out)
 
 
 def _mean_hx(fg, mesh, target, u):
@@ -971,7 +1001,7 @@ def case_nedelec(args):
 
 
 CASES = {"cg-kernel": case_cg_kernel, "cg-loop": case_cg_loop, "newton-kernels": case_newton_kernels, "heat": case_heat,
-         "sweep": case_sweep, "batch": case_batch, "adjoint": case_adjoint, "transport": case_transport,
+         "sweep": case_sweep, "batch": case_batch, "batch-single": case_batch_single, "adjoint": case_adjoint, "transport": case_transport,
          "nedelec": case_nedelec}
 
 

@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <cmath>
 #include <numeric>
+#include <type_traits>
 #include <vector>
 
 #include "fg_common.cuh"
@@ -23,59 +24,152 @@ namespace cgrp = cooperative_groups;
 
 // Threads per CTA (1024-thread CTAs spilled registers: 64 per thread at most)
 constexpr int FG_BATCH_THREADS = 512;
+constexpr int FG_BATCH_WARPS = FG_BATCH_THREADS / 32;
+// FP64 refinement steps of a mixed-precision problem at most (as the single-mesh solver)
+constexpr int FG_BATCH_MAX_REF = 50;
 
 struct BatchProb {
   int64_t n;
   int nslices;
   const int *sl_ptr, *sl_len, *sl_col;
   const double *val, *dinv;
-  const uint8_t *fixed;  // may be null
-  double *x, *r, *z, *p0, *p1, *q;
+  const float *val32, *dinv32;  // FP32 operator (mixed precision; null in FP64)
+  const uint8_t *fixed;         // may be null
+  double *x, *r, *z, *p, *q;    // FP64 vectors (mixed: x and the FP64 residual r only)
+  float *r32, *z32, *pa32, *pb32, *q32, *d32;  // FP32 inner vectors (mixed)
   double tol2_rel;
+  double inner_rtol;  // mixed: relative target of each inner FP32 solve at least
   int maxit;
-  int *iters;       // out: iterations
+  int *iters;       // out: iterations (mixed: inner FP32 iterations in total)
   double *relres;   // out: ||r|| / ||r0||
   int *status;      // out: 0 converged, 1 cap, 2 non-finite / breakdown
+  int *refs;        // out: FP64 refinement steps (mixed), 0 in FP64
 };
 
-// Block sum of two values, then the cluster-wide sum of the CTAs' block sums (read
-// from every CTA's shared slot in rank order).  slot alternates between calls so a
-// slot is rewritten only after the next cluster barrier.
-template <int CL>
-__device__ __forceinline__ void cluster_sum2(cgrp::cluster_group &cl, double a, double b, double (*slot)[2],
-                                             int which, double &ta, double &tb) {
-  __shared__ double wsum[2][FG_BATCH_THREADS / 32];
-  for (int o = 16; o > 0; o >>= 1) {
-    a += __shfl_down_sync(0xffffffffu, a, o);
-    b += __shfl_down_sync(0xffffffffu, b, o);
-  }
+// One CTA's shared state for the cluster reductions: the per-thread (FP64) or per-warp
+// (FP32) partials, the CTA's published sums (read by the other CTAs of the cluster; two
+// slots used alternately) and the scalars thread 0 broadcasts to the CTA.
+template <int NV>
+struct BatchShared {
+  double part[NV][FG_BATCH_THREADS];
+  double slot[2][NV];
+  double bc[4];
+};
+
+// Cluster-wide sums of NV values held by every thread.  Inside the CTA, FP32 values are
+// added by warp shuffles and the 16 warp sums by warp 0 in FP64; FP64 values are stored
+// per thread and warp 0 adds them (lane l: threads l, l + 32, ... in order, then a
+// shuffle tree), so the FP64 additions run on one warp instead of all 512 threads (FP64
+// issues at 1/64 of the FP32 rate).  The CTA's sums go to its slot; after the cluster
+// barrier warp 0 of every CTA reads the CL slots (lane k: rank k) and adds them by the
+// same shuffle tree, so all CTAs of the cluster get the same bits and take the same
+// branches.  Result: tot[] in every lane of warp 0 (undefined in the other warps).
+// `which` alternates between calls: a CTA rewrites a slot only after the next cluster
+// barrier, when every reader of the slot's previous value is done.
+template <int CL, int NV, int NS, typename T>
+__device__ __forceinline__ void cluster_sums(cgrp::cluster_group &cl, BatchShared<NS> &sh, const T (&v)[NV],
+                                             int which, double (&tot)[NV]) {
+  static_assert(NV <= NS, "more values than shared slots");
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  if (l == 0) { wsum[0][w] = a; wsum[1][w] = b; }
+  if constexpr (std::is_same<T, float>::value) {
+    float a[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) a[k] = v[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+      for (int k = 0; k < NV; ++k) a[k] += __shfl_down_sync(0xffffffffu, a[k], o);
+    if (l == 0)
+#pragma unroll
+      for (int k = 0; k < NV; ++k) sh.part[k][w] = (double)a[k];
+  } else {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) sh.part[k][threadIdx.x] = v[k];
+  }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double sa = 0.0, sb = 0.0;
-    for (int k = 0; k < FG_BATCH_THREADS / 32; ++k) { sa += wsum[0][k]; sb += wsum[1][k]; }
-    slot[which][0] = sa;
-    slot[which][1] = sb;
-    __threadfence();  // this CTA's global vector writes before the cluster barrier
-  }
-  __threadfence();
-  cl.sync();
-  double sa = 0.0, sb = 0.0;
+  if (w == 0) {
+    double s[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      if constexpr (std::is_same<T, float>::value) {
+        s[k] = l < FG_BATCH_WARPS ? sh.part[k][l] : 0.0;
+      } else {
+        s[k] = 0.0;
 #pragma unroll 4
-  for (int rank = 0; rank < CL; ++rank) {
-    const double *remote = cl.map_shared_rank(&slot[which][0], rank);
-    sa += remote[0];
-    sb += remote[1];
+        for (int j = l; j < FG_BATCH_THREADS; j += 32) s[k] += sh.part[k][j];
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+      for (int k = 0; k < NV; ++k) s[k] += __shfl_down_sync(0xffffffffu, s[k], o);
+    if (l == 0)
+#pragma unroll
+      for (int k = 0; k < NV; ++k) sh.slot[which][k] = s[k];
   }
-  ta = sa;
-  tb = sb;
+  __threadfence();  // this CTA's global vector writes before the cluster barrier
+  cl.sync();
+  if (w == 0) {
+    double t[NV];
+    const double *remote = l < CL ? cl.map_shared_rank(&sh.slot[which][0], l) : nullptr;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) t[k] = l < CL ? remote[k] : 0.0;
+#pragma unroll
+    for (int o = CL / 2; o > 0; o >>= 1)
+#pragma unroll
+      for (int k = 0; k < NV; ++k) t[k] += __shfl_down_sync(0xffffffffu, t[k], o);
+#pragma unroll
+    for (int k = 0; k < NV; ++k) tot[k] = __shfl_sync(0xffffffffu, t[k], 0);
+  }
 }
 
+// Barrier between a pass that writes vector entries and one that reads other CTAs'
+// entries.
+__device__ __forceinline__ void cluster_barrier(cgrp::cluster_group &cl) {
+  __threadfence();
+  cl.sync();
+}
+
+// Row i of the SELL-32x4 operator applied to the vector entries get(j): the row's groups
+// of four slots lie 128 entries apart, one 16-byte load of columns and one (FP32) or two
+// (FP64) of values per group.
+template <typename V, typename Get>
+__device__ __forceinline__ auto sell_row(const int *__restrict__ sl_ptr, const int *__restrict__ sl_len,
+                                         const int *__restrict__ sl_col, const V *__restrict__ val, int64_t i,
+                                         Get get) -> decltype(get(0)) {
+  using A = decltype(get(0));
+  const int s = (int)(i >> 5);
+  const int64_t base = (int64_t)sl_ptr[s] + (i & 31) * FG_GROUP;
+  const int G = sl_len[s];
+  A acc = 0;
+  for (int g = 0; g < G; ++g) {
+    const int64_t e = base + (int64_t)g * FG_SLICE * FG_GROUP;
+    const int4 c = *reinterpret_cast<const int4 *>(sl_col + e);
+    if constexpr (std::is_same<V, float>::value) {
+      const float4 a = *reinterpret_cast<const float4 *>(val + e);
+      acc = fmaf(a.x, get(c.x), acc);
+      acc = fmaf(a.y, get(c.y), acc);
+      acc = fmaf(a.z, get(c.z), acc);
+      acc = fmaf(a.w, get(c.w), acc);
+    } else {
+      const double2 a0 = *reinterpret_cast<const double2 *>(val + e);
+      const double2 a1 = *reinterpret_cast<const double2 *>(val + e + 2);
+      acc = fma(a0.x, get(c.x), acc);
+      acc = fma(a0.y, get(c.y), acc);
+      acc = fma(a1.x, get(c.z), acc);
+      acc = fma(a1.y, get(c.w), acc);
+    }
+  }
+  return acc;
+}
+
+// FP64 Jacobi-PCG of one problem per cluster.  Each iteration: p = z + beta p (own
+// rows), barrier, q = A p with p.q, then x, r, z with r.z and r.r; the scalars come
+// from thread 0 of each CTA (the same bits in every CTA) through shared memory.
 template <int CL>
 __global__ void __launch_bounds__(FG_BATCH_THREADS, 2) k_batch_pcg64(const BatchProb *__restrict__ probs) {
   cgrp::cluster_group cl = cgrp::this_cluster();
-  __shared__ double slot[2][2];
+  __shared__ BatchShared<2> sh;
   const int rank = (int)cl.block_rank();
   const BatchProb *pp = probs + blockIdx.x / CL;
   const int64_t n = pp->n;
@@ -86,104 +180,295 @@ __global__ void __launch_bounds__(FG_BATCH_THREADS, 2) k_batch_pcg64(const Batch
   const double *__restrict__ val = pp->val;
   const double *__restrict__ dinv = pp->dinv;
   const uint8_t *__restrict__ fixed = pp->fixed;
-  double *x = pp->x, *r = pp->r, *z = pp->z, *q = pp->q;
-  double *pold = pp->p0, *pnew = pp->p1;
+  double *x = pp->x, *r = pp->r, *z = pp->z, *p = pp->p, *q = pp->q;
   // this CTA's rows: a contiguous run of whole slices
   const int per = (nslices + CL - 1) / CL;
   const int s0 = min(rank * per, nslices), s1 = min(s0 + per, nslices);
   const int64_t i0 = (int64_t)s0 * FG_SLICE, i1 = min((int64_t)s1 * FG_SLICE, n);
+  const int maxit = pp->maxit;
   // r = -A x on free rows (the right-hand side is 0), z = D^-1 r, p = 0
   double prz = 0.0, prr = 0.0;
   for (int64_t i = i0 + threadIdx.x; i < i1; i += FG_BATCH_THREADS) {
     double ri = 0.0;
-    if (!(fixed && fixed[i])) {
-      const int s = (int)(i >> 5);
-      const int64_t base = (int64_t)sl_ptr[s] + (i & 31) * FG_GROUP;
-      const int G = sl_len[s];
-      double acc = 0.0;
-      for (int g = 0; g < G; ++g) {
-        const int64_t e = base + (int64_t)g * FG_SLICE * FG_GROUP;
-#pragma unroll
-        for (int c = 0; c < FG_GROUP; ++c) acc = fma(val[e + c], x[sl_col[e + c]], acc);
-      }
-      ri = -acc;
-    }
+    if (!(fixed && fixed[i])) ri = -sell_row(sl_ptr, sl_len, sl_col, val, i, [&](int j) { return x[j]; });
     const double zi = dinv[i] * ri;
     r[i] = ri;
     z[i] = zi;
-    pold[i] = 0.0;
-    pnew[i] = 0.0;
-    prz += ri * zi;
-    prr += ri * ri;
+    p[i] = 0.0;
+    prz = fma(ri, zi, prz);
+    prr = fma(ri, ri, prr);
   }
-  int which = 0;
-  double rz, rr;
-  cluster_sum2<CL>(cl, prz, prr, slot, which, rz, rr);
-  which ^= 1;
-  const double rr0 = rr, tol2 = pp->tol2_rel * rr0;
-  const int maxit = pp->maxit;
-  int it = 0, status = (rr0 == 0.0) ? 0 : -1;
-  if (!isfinite(rr0)) status = 2;
+  int which = 0, it = 0, st;
+  double tot[2];
+  // thread 0's scalar state (the same in every CTA of the cluster)
+  double rz = 0.0, rr = 0.0, rr0 = 0.0, tol2 = 0.0;
+  {
+    const double v[2] = {prz, prr};
+    cluster_sums<CL>(cl, sh, v, which, tot);
+    which ^= 1;
+  }
+  if (threadIdx.x == 0) {
+    rz = tot[0];
+    rr = rr0 = tot[1];
+    tol2 = pp->tol2_rel * rr0;
+    const int s = !isfinite(rr0) ? 2 : (rr0 == 0.0 ? 0 : (maxit <= 0 ? 1 : -1));
+    sh.bc[0] = s;
+  }
+  __syncthreads();
+  st = (int)sh.bc[0];
   double beta = 0.0;
-  while (status < 0) {
-    if (it >= maxit) { status = 1; break; }
-    // p_new = z + beta p_old; q = A p_new (neighbours formed from z and p_old); p.q
+  while (st < 0) {
+    // p = z + beta p on this CTA's rows
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += FG_BATCH_THREADS)
+      p[i] = (fixed && fixed[i]) ? 0.0 : fma(beta, p[i], z[i]);
+    cluster_barrier(cl);
+    // q = A p, p.q
     double ppq = 0.0;
     for (int64_t i = i0 + threadIdx.x; i < i1; i += FG_BATCH_THREADS) {
-      double qi = 0.0, pi = 0.0;
-      if (!(fixed && fixed[i])) {
-        const int s = (int)(i >> 5);
-        const int64_t base = (int64_t)sl_ptr[s] + (i & 31) * FG_GROUP;
-        const int G = sl_len[s];
-        for (int g = 0; g < G; ++g) {
-          const int64_t e = base + (int64_t)g * FG_SLICE * FG_GROUP;
-#pragma unroll
-          for (int c = 0; c < FG_GROUP; ++c) {
-            const int j = sl_col[e + c];
-            qi = fma(val[e + c], fma(beta, pold[j], z[j]), qi);
-          }
-        }
-        pi = fma(beta, pold[i], z[i]);
-      }
-      pnew[i] = pi;
+      double qi = 0.0;
+      if (!(fixed && fixed[i])) qi = sell_row(sl_ptr, sl_len, sl_col, val, i, [&](int j) { return p[j]; });
       q[i] = qi;
-      ppq += pi * qi;
+      ppq = fma(p[i], qi, ppq);
     }
-    double pq, unused;
-    cluster_sum2<CL>(cl, ppq, 0.0, slot, which, pq, unused);
-    which ^= 1;
-    if (!(pq > 0.0) || !isfinite(pq)) { status = (pq == 0.0) ? 0 : 2; break; }
-    const double alpha = rz / pq;
+    {
+      const double v[1] = {ppq};
+      double t1[1];
+      cluster_sums<CL>(cl, sh, v, which, t1);
+      which ^= 1;
+      if (threadIdx.x == 0) {
+        const double pq = t1[0];
+        int s = -1;
+        if (!(pq > 0.0) || !isfinite(pq)) s = (pq == 0.0) ? 0 : 2;
+        sh.bc[0] = s;
+        sh.bc[1] = s < 0 ? rz / pq : 0.0;
+      }
+    }
+    __syncthreads();
+    st = (int)sh.bc[0];
+    if (st >= 0) break;
+    const double alpha = sh.bc[1];
     // x += alpha p; r -= alpha q; z = D^-1 r
     prz = 0.0;
     prr = 0.0;
     for (int64_t i = i0 + threadIdx.x; i < i1; i += FG_BATCH_THREADS) {
-      x[i] = fma(alpha, pnew[i], x[i]);
+      x[i] = fma(alpha, p[i], x[i]);
       const double ri = fma(-alpha, q[i], r[i]);
       const double zi = dinv[i] * ri;
       r[i] = ri;
       z[i] = zi;
-      prz += ri * zi;
-      prr += ri * ri;
+      prz = fma(ri, zi, prz);
+      prr = fma(ri, ri, prr);
     }
-    double rzn;
-    cluster_sum2<CL>(cl, prz, prr, slot, which, rzn, rr);
-    which ^= 1;
+    {
+      const double v[2] = {prz, prr};
+      cluster_sums<CL>(cl, sh, v, which, tot);
+      which ^= 1;
+    }
     ++it;
-    if (!isfinite(rr)) { status = 2; break; }
-    if (rr <= tol2) { status = 0; break; }
-    beta = rzn / rz;
-    rz = rzn;
-    double *t = pold;
-    pold = pnew;
-    pnew = t;
+    if (threadIdx.x == 0) {
+      const double rzn = tot[0];
+      rr = tot[1];
+      const int s = !isfinite(rr) ? 2 : (rr <= tol2 ? 0 : (it >= maxit ? 1 : -1));
+      sh.bc[0] = s;
+      sh.bc[1] = rzn / rz;
+      rz = rzn;
+    }
+    __syncthreads();
+    st = (int)sh.bc[0];
+    beta = sh.bc[1];
   }
   if (rank == 0 && threadIdx.x == 0) {
     *pp->iters = it;
     *pp->relres = rr0 > 0.0 ? sqrt(rr / rr0) : 0.0;
-    *pp->status = status;
+    *pp->status = st;
+    *pp->refs = 0;
   }
   cl.sync();  // no CTA leaves while another may still read its shared slots
+}
+
+// Mixed precision: FP64 iterative refinement around FP32 Jacobi-PCG, the single-mesh
+// solver's scheme (FP64 residual r = -A x, inner FP32 solve of A d = r / ||r|| to
+// max(rtol ||r0|| / ||r||, inner_rtol), x += ||r|| d, until ||r|| <= rtol ||r0||) run
+// by one cluster per problem.  The inner iteration forms p = z + beta p_old at every
+// stored entry instead of in a pass of its own (FP32 arithmetic is cheap, a cluster
+// barrier is not).
+template <int CL>
+__global__ void __launch_bounds__(FG_BATCH_THREADS, 2) k_batch_pcg_mixed(const BatchProb *__restrict__ probs) {
+  cgrp::cluster_group cl = cgrp::this_cluster();
+  __shared__ BatchShared<2> sh;
+  const int rank = (int)cl.block_rank();
+  const BatchProb *pp = probs + blockIdx.x / CL;
+  const int64_t n = pp->n;
+  const int nslices = pp->nslices;
+  const int *__restrict__ sl_ptr = pp->sl_ptr;
+  const int *__restrict__ sl_len = pp->sl_len;
+  const int *__restrict__ sl_col = pp->sl_col;
+  const double *__restrict__ val = pp->val;
+  const float *__restrict__ val32 = pp->val32;
+  const float *__restrict__ dinv32 = pp->dinv32;
+  const uint8_t *__restrict__ fixed = pp->fixed;
+  double *x = pp->x, *r = pp->r;
+  float *r32 = pp->r32, *z32 = pp->z32, *q32 = pp->q32, *d32 = pp->d32;
+  const int per = (nslices + CL - 1) / CL;
+  const int s0 = min(rank * per, nslices), s1 = min(s0 + per, nslices);
+  const int64_t i0 = (int64_t)s0 * FG_SLICE, i1 = min((int64_t)s1 * FG_SLICE, n);
+  const int maxit = pp->maxit;
+  int which = 0, it = 0, ref = 0, st = -1;
+  // thread 0's scalar state (the same in every CTA of the cluster)
+  double rr0 = -1.0, rrt = 0.0, irz = 0.0, itol2 = 0.0;
+  while (true) {
+    // FP64 residual r = -A x on the free rows (the right-hand side is 0)
+    double prr = 0.0;
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += FG_BATCH_THREADS) {
+      double ri = 0.0;
+      if (!(fixed && fixed[i])) ri = -sell_row(sl_ptr, sl_len, sl_col, val, i, [&](int j) { return x[j]; });
+      r[i] = ri;
+      prr = fma(ri, ri, prr);
+    }
+    {
+      const double v[1] = {prr};
+      double t1[1];
+      cluster_sums<CL>(cl, sh, v, which, t1);
+      which ^= 1;
+      if (threadIdx.x == 0) {
+        rrt = t1[0];
+        if (rr0 < 0.0) rr0 = rrt;
+        const double tol2 = pp->tol2_rel * rr0;
+        int s = -1;
+        if (!isfinite(rrt)) s = 2;
+        else if (rrt <= tol2 || rrt == 0.0) s = 0;
+        else if (it >= maxit || ref >= FG_BATCH_MAX_REF) s = 1;
+        const double rn = sqrt(rrt);
+        const double inner = fmax(sqrt(tol2 / rrt), pp->inner_rtol);
+        sh.bc[0] = s;
+        sh.bc[1] = s < 0 ? 1.0 / rn : 0.0;
+        sh.bc[2] = rn;
+        itol2 = inner * inner;
+      }
+    }
+    __syncthreads();
+    st = (int)sh.bc[0];
+    if (st >= 0) break;
+    const double scale = sh.bc[1], rn = sh.bc[2];
+    // inner FP32 start: r32 = r / ||r||, z = D^-1 r32, d = 0, p = 0
+    float frz = 0.f, frr = 0.f;
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += FG_BATCH_THREADS) {
+      const float ri = (float)(r[i] * scale);
+      const float zi = dinv32[i] * ri;
+      r32[i] = ri;
+      z32[i] = zi;
+      d32[i] = 0.f;
+      pp->pa32[i] = 0.f;
+      pp->pb32[i] = 0.f;
+      frz = fmaf(ri, zi, frz);
+      frr = fmaf(ri, ri, frr);
+    }
+    double tot[2];
+    {
+      const float v[2] = {frz, frr};
+      cluster_sums<CL>(cl, sh, v, which, tot);
+      which ^= 1;
+    }
+    if (threadIdx.x == 0) {
+      irz = tot[0];
+      itol2 *= tot[1];
+      sh.bc[0] = (tot[1] > 0.0) ? -1 : 0;
+    }
+    __syncthreads();
+    int ist = (int)sh.bc[0];
+    float beta = 0.f;
+    float *pold = pp->pa32, *pnew = pp->pb32;
+    while (ist < 0 && it < maxit) {
+      // p = z + beta p_old (formed at every entry from z and p_old); q = A p; p.q
+      float fpq = 0.f;
+      for (int64_t i = i0 + threadIdx.x; i < i1; i += FG_BATCH_THREADS) {
+        float qi = 0.f, pi = 0.f;
+        if (!(fixed && fixed[i])) {
+          qi = sell_row(sl_ptr, sl_len, sl_col, val32, i, [&](int j) { return fmaf(beta, pold[j], z32[j]); });
+          pi = fmaf(beta, pold[i], z32[i]);
+        }
+        pnew[i] = pi;
+        q32[i] = qi;
+        fpq = fmaf(pi, qi, fpq);
+      }
+      {
+        const float v[1] = {fpq};
+        double t1[1];
+        cluster_sums<CL>(cl, sh, v, which, t1);
+        which ^= 1;
+        if (threadIdx.x == 0) {
+          const double pq = t1[0];
+          int s = -1;
+          if (!(pq > 0.0) || !isfinite(pq)) s = (pq == 0.0) ? 0 : 2;
+          sh.bc[0] = s;
+          sh.bc[1] = s < 0 ? irz / pq : 0.0;
+        }
+      }
+      __syncthreads();
+      ist = (int)sh.bc[0];
+      if (ist >= 0) break;
+      const float alpha = (float)sh.bc[1];
+      // d += alpha p; r -= alpha q; z = D^-1 r
+      frz = 0.f;
+      frr = 0.f;
+      for (int64_t i = i0 + threadIdx.x; i < i1; i += FG_BATCH_THREADS) {
+        d32[i] = fmaf(alpha, pnew[i], d32[i]);
+        const float ri = fmaf(-alpha, q32[i], r32[i]);
+        const float zi = dinv32[i] * ri;
+        r32[i] = ri;
+        z32[i] = zi;
+        frz = fmaf(ri, zi, frz);
+        frr = fmaf(ri, ri, frr);
+      }
+      {
+        const float v[2] = {frz, frr};
+        cluster_sums<CL>(cl, sh, v, which, tot);
+        which ^= 1;
+      }
+      ++it;
+      if (threadIdx.x == 0) {
+        const double rzn = tot[0], rri = tot[1];
+        sh.bc[0] = !isfinite(rri) ? 2 : (rri <= itol2 ? 0 : -1);
+        sh.bc[1] = rzn / irz;
+        irz = rzn;
+      }
+      __syncthreads();
+      ist = (int)sh.bc[0];
+      beta = (float)sh.bc[1];
+      float *t = pold;
+      pold = pnew;
+      pnew = t;
+    }
+    // x += ||r|| d
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += FG_BATCH_THREADS) x[i] = fma(rn, (double)d32[i], x[i]);
+    if (ist == 2) {
+      st = 2;
+      break;
+    }
+    ++ref;
+    cluster_barrier(cl);  // x complete before the next residual reads the neighbours' entries
+  }
+  if (rank == 0 && threadIdx.x == 0) {
+    *pp->iters = it;
+    *pp->relres = rr0 > 0.0 ? sqrt(rrt / rr0) : 0.0;
+    *pp->status = st;
+    *pp->refs = ref;
+  }
+  cl.sync();  // no CTA leaves while another may still read its shared slots
+}
+
+template <int CL>
+static const void *batch_fn(bool mixed) {
+  return mixed ? reinterpret_cast<const void *>(k_batch_pcg_mixed<CL>)
+               : reinterpret_cast<const void *>(k_batch_pcg64<CL>);
+}
+static const void *batch_kernel(int cl, bool mixed) {
+  switch (cl) {
+    case 16: return batch_fn<16>(mixed);
+    case 8: return batch_fn<8>(mixed);
+    case 4: return batch_fn<4>(mixed);
+    default: return batch_fn<2>(mixed);
+  }
 }
 
 extern "C" fg_status fg_batch_magnetostatics_linear(fg_mesh *const *meshes, int32_t count, const double *const *mu,
@@ -195,7 +480,9 @@ extern "C" fg_status fg_batch_magnetostatics_linear(fg_mesh *const *meshes, int3
     fg_solve_opts opts;
     fg_solve_opts_default(&opts);
     if (o) opts = *o;
-    FG_REQUIRE(opts.precision == FG_FP64, FG_UNSUPPORTED, "fg_batch_magnetostatics_linear: FP64 only");
+    FG_REQUIRE(opts.precision == FG_FP64 || opts.precision == FG_MIXED, FG_BAD_ARG,
+               "fg_batch_magnetostatics_linear: precision must be FG_FP64 or FG_MIXED");
+    const bool mixed = opts.precision == FG_MIXED;
     fg_mesh *m0 = meshes[0];
     FG_REQUIRE(m0 != nullptr, FG_BAD_ARG, "fg_batch_magnetostatics_linear: null mesh");
     std::vector<BatchProb> hp(count);
@@ -206,9 +493,18 @@ extern "C" fg_status fg_batch_magnetostatics_linear(fg_mesh *const *meshes, int3
       FG_REQUIRE(m->npe == 4 || m->npe == 3, FG_UNSUPPORTED, "fg_batch_magnetostatics_linear: P1 elements only");
       if (!m->mu_lin) m->mu_lin = dev_alloc<double>(m, (size_t)m->nt);
       FG_CUDA_TRY(cudaMemcpyAsync(m->mu_lin, mu[k], sizeof(double) * (size_t)m->nt, cudaMemcpyHostToDevice, m->stream));
-      fg_assemble_operator(m, ASM_STIFF, m->mu_lin, nullptr, nullptr, 0.0, 0.0, 0, OUT_SELL, true, false, true);
-      for (int j : {7, 0, 1, 2, 3, 4, 5})
+      fg_assemble_operator(m, ASM_STIFF, m->mu_lin, nullptr, nullptr, 0.0, 0.0, 0, OUT_SELL, true, mixed, true);
+      for (int j : {7, 0, 1, 2, 3})
         if (!m->v64[j]) m->v64[j] = dev_alloc<double>(m, (size_t)m->nvp);
+      // FP32 inner vectors: the split FP32 CG's and the pipelined CG's scratch (each
+      // nvp long, zeroed when first made; every solve initialises what it reads)
+      float **f32[6] = {&m->v32[4], &m->v32[5], &m->v32[6], &m->v32[7], &m->pv32[0], &m->pv32[1]};
+      if (mixed)
+        for (float **f : f32)
+          if (!*f) {
+            *f = dev_alloc<float>(m, (size_t)m->nvp);
+            FG_CUDA_TRY(cudaMemsetAsync(*f, 0, sizeof(float) * (size_t)m->nvp, m->stream));
+          }
       FG_CUDA_TRY(cudaMemcpyAsync(m->v64[7], u_in[k], sizeof(double) * (size_t)m->nv, cudaMemcpyHostToDevice,
                                   m->stream));
       BatchProb &b = hp[k];
@@ -219,14 +515,22 @@ extern "C" fg_status fg_batch_magnetostatics_linear(fg_mesh *const *meshes, int3
       b.sl_col = m->sl_col;
       b.val = m->val64;
       b.dinv = m->dinv64;
+      b.val32 = mixed ? m->val32 : nullptr;
+      b.dinv32 = mixed ? m->dinv32 : nullptr;
       b.fixed = m->has_fixed ? m->fixed : nullptr;
       b.x = m->v64[7];
       b.r = m->v64[0];
       b.z = m->v64[1];
-      b.p0 = m->v64[2];
-      b.p1 = m->v64[3];
-      b.q = m->v64[4];
+      b.p = m->v64[2];
+      b.q = m->v64[3];
+      b.r32 = mixed ? *f32[0] : nullptr;
+      b.z32 = mixed ? *f32[1] : nullptr;
+      b.pa32 = mixed ? *f32[2] : nullptr;
+      b.pb32 = mixed ? *f32[3] : nullptr;
+      b.q32 = mixed ? *f32[4] : nullptr;
+      b.d32 = mixed ? *f32[5] : nullptr;
       b.tol2_rel = opts.rtol * opts.rtol;
+      b.inner_rtol = opts.inner_rtol;
       b.maxit = opts.maxiter;
     }
     for (int k = 0; k < count; ++k) {
@@ -249,17 +553,10 @@ extern "C" fg_status fg_batch_magnetostatics_linear(fg_mesh *const *meshes, int3
       cfg.attrs = at;
       cfg.numAttrs = 1;
       int fit = 0;
+      const void *fn = batch_kernel(cl, mixed);
       cudaError_t e = cudaSuccess;
-      if (cl == 16) {
-        e = cudaFuncSetAttribute(k_batch_pcg64<16>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveClusters(&fit, k_batch_pcg64<16>, &cfg);
-      } else if (cl == 8) {
-        e = cudaOccupancyMaxActiveClusters(&fit, k_batch_pcg64<8>, &cfg);
-      } else if (cl == 4) {
-        e = cudaOccupancyMaxActiveClusters(&fit, k_batch_pcg64<4>, &cfg);
-      } else {
-        e = cudaOccupancyMaxActiveClusters(&fit, k_batch_pcg64<2>, &cfg);
-      }
+      if (cl == 16) e = cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+      if (e == cudaSuccess) e = cudaOccupancyMaxActiveClusters(&fit, fn, &cfg);
       if (e != cudaSuccess) {
         cudaGetLastError();
         return false;
@@ -304,7 +601,7 @@ extern "C" fg_status fg_batch_magnetostatics_linear(fg_mesh *const *meshes, int3
       cudaFree(d_rel);
     };
     try {
-      FG_CUDA_TRY(cudaMalloc(&d_out, sizeof(int) * 2 * count));
+      FG_CUDA_TRY(cudaMalloc(&d_out, sizeof(int) * 3 * count));
       FG_CUDA_TRY(cudaMalloc(&d_rel, sizeof(double) * count));
       FG_CUDA_TRY(cudaMalloc(&d_probs, sizeof(BatchProb) * count));
       std::vector<BatchProb> sorted(count);
@@ -313,6 +610,7 @@ extern "C" fg_status fg_batch_magnetostatics_linear(fg_mesh *const *meshes, int3
         sorted[j].iters = d_out + j;
         sorted[j].status = d_out + count + j;
         sorted[j].relres = d_rel + j;
+        sorted[j].refs = d_out + 2 * count + j;
       }
       cudaStream_t st = m0->stream;
       FG_CUDA_TRY(cudaMemcpyAsync(d_probs, sorted.data(), sizeof(BatchProb) * count, cudaMemcpyHostToDevice, st));
@@ -351,12 +649,8 @@ extern "C" fg_status fg_batch_magnetostatics_linear(fg_mesh *const *meshes, int3
         cfg.attrs = at;
         cfg.numAttrs = 1;
         const BatchProb *pp = d_probs + g.first;
-        switch (g.cl) {
-          case 16: return cudaLaunchKernelEx(&cfg, k_batch_pcg64<16>, pp);
-          case 8: return cudaLaunchKernelEx(&cfg, k_batch_pcg64<8>, pp);
-          case 4: return cudaLaunchKernelEx(&cfg, k_batch_pcg64<4>, pp);
-          default: return cudaLaunchKernelEx(&cfg, k_batch_pcg64<2>, pp);
-        }
+        void *args[1] = {&pp};
+        return cudaLaunchKernelExC(&cfg, batch_kernel(g.cl, mixed), args);
       };
       FG_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
       cudaError_t le = cudaEventRecord(fork, st);
@@ -375,14 +669,14 @@ extern "C" fg_status fg_batch_magnetostatics_linear(fg_mesh *const *meshes, int3
       FG_CUDA_TRY(cudaGraphLaunch(exec, st));
       FG_CUDA_TRY(cudaEventRecord(e1, st));
       FG_LAUNCHED((long long)groups.size());
-      std::vector<int> hout(2 * count);
+      std::vector<int> hout(3 * count);
       std::vector<double> hrel(count);
-      FG_CUDA_TRY(cudaMemcpyAsync(hout.data(), d_out, sizeof(int) * 2 * count, cudaMemcpyDeviceToHost, st));
+      FG_CUDA_TRY(cudaMemcpyAsync(hout.data(), d_out, sizeof(int) * 3 * count, cudaMemcpyDeviceToHost, st));
       FG_CUDA_TRY(cudaMemcpyAsync(hrel.data(), d_rel, sizeof(double) * count, cudaMemcpyDeviceToHost, st));
       FG_CUDA_TRY(cudaStreamSynchronize(st));
       float ms = 0.f;
       cudaEventElapsedTime(&ms, e0, e1);
-      int conv = 0, maxit = 0, nan = 0;
+      int conv = 0, maxit = 0, nan = 0, maxref = 0;
       long long tot = 0;
       for (int j = 0; j < count; ++j) {
         const int k = order[j];
@@ -390,6 +684,7 @@ extern "C" fg_status fg_batch_magnetostatics_linear(fg_mesh *const *meshes, int3
         conv += hout[count + j] == 0;
         nan += hout[count + j] == 2;
         maxit = std::max(maxit, hout[j]);
+        maxref = std::max(maxref, hout[2 * count + j]);
         tot += hout[j];
       }
       for (int k = 0; k < count; ++k)
@@ -403,6 +698,8 @@ extern "C" fg_status fg_batch_magnetostatics_linear(fg_mesh *const *meshes, int3
         s->cluster_ctas = cl_max;
         s->total_iterations = tot;
         s->ms = ms;
+        s->max_refinements = maxref;
+        s->reserved_ = 0;
       }
       cleanup();
       if (nan) return FG_NAN;

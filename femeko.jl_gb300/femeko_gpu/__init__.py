@@ -395,9 +395,12 @@ def magnetostatics_sweep(mesh: MESH, mu, H0, rtol=1e-10, inner_rtol=1e-5, maxite
     return U.T, d
 
 
-def batch_magnetostatics_linear(meshes, mus, u_ins, rtol=1e-10, maxiter=1_000_000):
+def batch_magnetostatics_linear(meshes, mus, u_ins, rtol=1e-10, maxiter=1_000_000, precision="fp64",
+                                inner_rtol=1e-5):
     """Independent linear magnetostatic problems (one per mesh, Dirichlet rows from
-    each mesh) in one persistent GPU launch; returns (list of u, iterations, stats)."""
+    each mesh) in one persistent GPU launch; returns (list of u, iterations, stats).
+    precision "mixed" runs FP32 PCG inside FP64 refinement on each problem's cluster
+    (iterations are then the inner FP32 iterations)."""
     gs = [gpu_mesh(m) for m in meshes]
     n = len(meshes)
     mus_c = [_c(mu, np.float64) for mu in mus]
@@ -408,7 +411,7 @@ def batch_magnetostatics_linear(meshes, mus, u_ins, rtol=1e-10, maxiter=1_000_00
     UI = (C.c_void_p * n)(*[a.ctypes.data for a in uin_c])
     UO = (C.c_void_p * n)(*[a.ctypes.data for a in outs])
     its = np.zeros(n, dtype=np.int32)
-    o = solve_opts(precision="fp64", rtol=rtol, maxiter=maxiter)
+    o = solve_opts(precision=precision, rtol=rtol, maxiter=maxiter, inner_rtol=inner_rtol)
     s = L.BatchStats()
     st = L.lib().fg_batch_magnetostatics_linear(H, n, MU, UI, C.byref(o), UO, L.ptr(its), C.byref(s))
     L.check(st, allow_not_converged=True)

@@ -58,7 +58,8 @@ class AdjointStats(C.Structure):
 
 class BatchStats(C.Structure):
     _fields_ = [("problems", C.c_int32), ("converged", C.c_int32), ("max_iterations", C.c_int32),
-                ("cluster_ctas", C.c_int32), ("total_iterations", C.c_int64), ("ms", C.c_double)]
+                ("cluster_ctas", C.c_int32), ("total_iterations", C.c_int64), ("ms", C.c_double),
+                ("max_refinements", C.c_int32), ("reserved_", C.c_int32)]
 
 
 def stats_dict(s) -> dict:

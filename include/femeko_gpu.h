@@ -394,17 +394,22 @@ typedef struct fg_batch_stats {
                               fewer in proportion to their rows, at least 2) */
   int64_t total_iterations;
   double ms;               /* device time of the graph launch */
+  int32_t max_refinements; /* FG_MIXED: most FP64 refinement steps of a problem (0 in FP64) */
+  int32_t reserved_;
 } fg_batch_stats;
 
 /* count independent linear magnetostatic problems (Magnetostatics/magneticField.jl:89-132
  * on each mesh: K(mu) u = 0 on free rows, u = u_in on the Dirichlet rows set by
- * fg_mesh_set_dirichlet) solved by FP64 Jacobi-PCG in ONE graph launch: each problem
+ * fg_mesh_set_dirichlet) solved by Jacobi-PCG in ONE graph launch: each problem
  * runs its whole solve on its own thread-block cluster, whose size follows the
  * problem's rows (16, 8, 4 or 2 CTAs; one persistent kernel per cluster size, the
  * kernels on parallel branches of the graph).
  * mu[k] (nt_k, absolute permeability), u_in[k] and u_out[k] (nv_k) are host arrays
  * per mesh; iterations (count, may be NULL) receives each problem's CG iterations.
- * All meshes on the current device; o->precision must be FG_FP64. */
+ * o->precision: FG_FP64 (FP64 PCG to rtol) or FG_MIXED (on each cluster, FP64
+ * iterative refinement around FP32 PCG solves of inner relative target
+ * max(rtol ||r0|| / ||r||, o->inner_rtol), as fg_solve; iterations are then the inner
+ * FP32 iterations).  All meshes on the current device. */
 fg_status fg_batch_magnetostatics_linear(fg_mesh *const *meshes, int32_t count, const double *const *mu,
                                          const double *const *u_in, const fg_solve_opts *o, double *const *u_out,
                                          int32_t *iterations, fg_batch_stats *s);

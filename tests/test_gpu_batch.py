@@ -46,3 +46,34 @@ def test_batch_sixty_four_uneven_meshes_twice():
     k = int(np.argmax([m.nv for m in meshes]))
     uo, _, _ = O.linear_magnetostatics(meshes[k], u0s[k], mus[k], cg_tol=1e-12)
     assert np.linalg.norm(us1[k] - uo) / np.linalg.norm(uo) < 1e-7
+
+
+def test_batch_mixed_precision_matches_single_solves():
+    """FP32 PCG inside FP64 refinement on each cluster reaches the FP64 answer."""
+    meshes, mus, u0s = batch_case(12, 3, 14, seed=11)
+    us, its, st = fg.batch_magnetostatics_linear(meshes, mus, u0s, rtol=1e-10, precision="mixed")
+    assert st["problems"] == 12 and st["converged"] == 12
+    assert st["max_refinements"] >= 2          # inner solves stop at 1e-5: two or more refinements
+    assert st["max_iterations"] == its.max() and st["total_iterations"] == its.sum()
+    u64, its64, st64 = fg.batch_magnetostatics_linear(meshes, mus, u0s, rtol=1e-10)
+    assert st64["max_refinements"] == 0
+    for m, mu, u0, u, v in zip(meshes, mus, u0s, us, u64):
+        uo, _, _ = O.linear_magnetostatics(m, u0, mu, cg_tol=1e-13)
+        assert np.linalg.norm(u - uo) / np.linalg.norm(uo) < 1e-8
+        assert np.linalg.norm(v - uo) / np.linalg.norm(uo) < 1e-8
+        fx = m.dirichlet_mask().astype(bool)
+        assert np.array_equal(u[fx], u0[fx])
+    us2, its2, _ = fg.batch_magnetostatics_linear(meshes, mus, u0s, rtol=1e-10, precision="mixed")
+    assert np.array_equal(its, its2)
+    for a, b in zip(us, us2):
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batch_iteration_cap_is_reported(precision):
+    meshes, mus, u0s = batch_case(4, 6, 9, seed=5)
+    us, its, st = fg.batch_magnetostatics_linear(meshes, mus, u0s, rtol=1e-12, maxiter=7, precision=precision)
+    assert st["converged"] == 0
+    assert (its <= 7).all() and its.max() == 7
+    for u in us:
+        assert np.isfinite(u).all()

@@ -102,13 +102,14 @@ def test_c4a_sweep_48cube_256_fields():
         assert rel(U[:, c], uo) < 1e-8, c
 
 
-def test_c4b_batch_64_meshes_8_to_40_cells():
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_c4b_batch_64_meshes_8_to_40_cells(precision):
     rng = np.random.default_rng(SEED)
     ns = rng.integers(8, 41, 64)
     meshes = [fg.box_tet_mesh(int(n), seed=SEED + k) for k, n in enumerate(ns)]
     mus = [rng.uniform(1, 1000, m.nt) * MU0 for m in meshes]
     u0s = [-m.p[0].copy() for m in meshes]
-    us, its, st = fg.batch_magnetostatics_linear(meshes, mus, u0s, rtol=1e-10)
+    us, its, st = fg.batch_magnetostatics_linear(meshes, mus, u0s, rtol=1e-10, precision=precision)
     assert st["problems"] == 64 and st["converged"] == 64
     order = np.argsort(ns)
     sample = sorted({int(order[0]), int(order[-1]), int(order[32]), *map(int, np.random.default_rng(5).choice(64, 3,
