@@ -36,7 +36,8 @@ struct BatchProb {
   const float *val32, *dinv32;  // FP32 operator (mixed precision; null in FP64)
   const uint8_t *fixed;         // may be null
   double *x, *r, *z, *p, *q;    // FP64 vectors (mixed: x and the FP64 residual r only)
-  float *r32, *z32, *pa32, *pb32, *q32, *d32;  // FP32 inner vectors (mixed)
+  float4 *sa32, *sb32;  // mixed: the two buffers of the inner rows' state (r, w, s, D^-1)
+  float *p32, *d32;     // mixed: inner search direction and correction
   double tol2_rel;
   double inner_rtol;  // mixed: relative target of each inner FP32 solve at least
   int maxit;
@@ -55,6 +56,13 @@ struct BatchShared {
   double slot[2][NV];
   double bc[4];
 };
+
+// Cluster barrier with release (arrive) and acquire (wait) semantics at cluster scope:
+// the global and shared writes of every thread before it are visible to every thread of
+// the cluster after it (the default semantics of barrier.cluster, spelled out).
+__device__ __forceinline__ void cluster_sync_acqrel() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
 
 // Cluster-wide sums of NV values held by every thread.  Inside the CTA, FP32 values are
 // added by warp shuffles and the 16 warp sums by warp 0 in FP64; FP64 values are stored
@@ -107,8 +115,7 @@ __device__ __forceinline__ void cluster_sums(cgrp::cluster_group &cl, BatchShare
 #pragma unroll
       for (int k = 0; k < NV; ++k) sh.slot[which][k] = s[k];
   }
-  __threadfence();  // this CTA's global vector writes before the cluster barrier
-  cl.sync();
+  cluster_sync_acqrel();
   if (w == 0) {
     double t[NV];
     const double *remote = l < CL ? cl.map_shared_rank(&sh.slot[which][0], l) : nullptr;
@@ -123,17 +130,63 @@ __device__ __forceinline__ void cluster_sums(cgrp::cluster_group &cl, BatchShare
   }
 }
 
+// FP32 form for the inner iterations of the mixed-precision solve: warp shuffles, warp
+// 0 adds the 16 warp sums into the CTA's slot, and after the cluster barrier EVERY warp
+// reads the CL slots and adds them by the same shuffle tree, so all threads of the
+// cluster hold the same bits without a broadcast through shared memory (one CTA
+// barrier and one cluster barrier per call).
+template <int NV>
+struct BatchShared32 {
+  float wsum[NV][FG_BATCH_WARPS];
+  float slot[2][NV];
+};
+template <int CL, int NV, int NS>
+__device__ __forceinline__ void cluster_sums_f32(cgrp::cluster_group &cl, BatchShared32<NS> &sh, const float (&v)[NV],
+                                                 int which, float (&tot)[NV]) {
+  static_assert(NV <= NS, "more values than shared slots");
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  float a[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) a[k] = v[k];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) a[k] += __shfl_down_sync(0xffffffffu, a[k], o);
+  if (l == 0)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) sh.wsum[k][w] = a[k];
+  __syncthreads();
+  if (w == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) a[k] = l < FG_BATCH_WARPS ? sh.wsum[k][l] : 0.f;
+#pragma unroll
+    for (int o = FG_BATCH_WARPS / 2; o > 0; o >>= 1)
+#pragma unroll
+      for (int k = 0; k < NV; ++k) a[k] += __shfl_down_sync(0xffffffffu, a[k], o);
+    if (l == 0)
+#pragma unroll
+      for (int k = 0; k < NV; ++k) sh.slot[which][k] = a[k];
+  }
+  cluster_sync_acqrel();
+  const float *remote = cl.map_shared_rank(&sh.slot[which][0], l < CL ? l : 0);
+#pragma unroll
+  for (int k = 0; k < NV; ++k) a[k] = l < CL ? remote[k] : 0.f;
+#pragma unroll
+  for (int o = CL / 2; o > 0; o >>= 1)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) a[k] += __shfl_down_sync(0xffffffffu, a[k], o);
+#pragma unroll
+  for (int k = 0; k < NV; ++k) tot[k] = __shfl_sync(0xffffffffu, a[k], 0);
+}
+
 // Barrier between a pass that writes vector entries and one that reads other CTAs'
 // entries.
-__device__ __forceinline__ void cluster_barrier(cgrp::cluster_group &cl) {
-  __threadfence();
-  cl.sync();
-}
+__device__ __forceinline__ void cluster_barrier(cgrp::cluster_group &) { cluster_sync_acqrel(); }
 
 // Row i of the SELL-32x4 operator applied to the vector entries get(j): the row's groups
 // of four slots lie 128 entries apart, one 16-byte load of columns and one (FP32) or two
 // (FP64) of values per group.
-template <typename V, typename Get>
+template <int U, typename V, typename Get>
 __device__ __forceinline__ auto sell_row(const int *__restrict__ sl_ptr, const int *__restrict__ sl_len,
                                          const int *__restrict__ sl_col, const V *__restrict__ val, int64_t i,
                                          Get get) -> decltype(get(0)) {
@@ -142,6 +195,7 @@ __device__ __forceinline__ auto sell_row(const int *__restrict__ sl_ptr, const i
   const int64_t base = (int64_t)sl_ptr[s] + (i & 31) * FG_GROUP;
   const int G = sl_len[s];
   A acc = 0;
+#pragma unroll U
   for (int g = 0; g < G; ++g) {
     const int64_t e = base + (int64_t)g * FG_SLICE * FG_GROUP;
     const int4 c = *reinterpret_cast<const int4 *>(sl_col + e);
@@ -190,7 +244,7 @@ __global__ void __launch_bounds__(FG_BATCH_THREADS, 2) k_batch_pcg64(const Batch
   double prz = 0.0, prr = 0.0;
   for (int64_t i = i0 + threadIdx.x; i < i1; i += FG_BATCH_THREADS) {
     double ri = 0.0;
-    if (!(fixed && fixed[i])) ri = -sell_row(sl_ptr, sl_len, sl_col, val, i, [&](int j) { return x[j]; });
+    if (!(fixed && fixed[i])) ri = -sell_row<2>(sl_ptr, sl_len, sl_col, val, i, [&](int j) { return x[j]; });
     const double zi = dinv[i] * ri;
     r[i] = ri;
     z[i] = zi;
@@ -226,7 +280,7 @@ __global__ void __launch_bounds__(FG_BATCH_THREADS, 2) k_batch_pcg64(const Batch
     double ppq = 0.0;
     for (int64_t i = i0 + threadIdx.x; i < i1; i += FG_BATCH_THREADS) {
       double qi = 0.0;
-      if (!(fixed && fixed[i])) qi = sell_row(sl_ptr, sl_len, sl_col, val, i, [&](int j) { return p[j]; });
+      if (!(fixed && fixed[i])) qi = sell_row<2>(sl_ptr, sl_len, sl_col, val, i, [&](int j) { return p[j]; });
       q[i] = qi;
       ppq = fma(p[i], qi, ppq);
     }
@@ -289,13 +343,18 @@ __global__ void __launch_bounds__(FG_BATCH_THREADS, 2) k_batch_pcg64(const Batch
 // Mixed precision: FP64 iterative refinement around FP32 Jacobi-PCG, the single-mesh
 // solver's scheme (FP64 residual r = -A x, inner FP32 solve of A d = r / ||r|| to
 // max(rtol ||r0|| / ||r||, inner_rtol), x += ||r|| d, until ||r|| <= rtol ||r0||) run
-// by one cluster per problem.  The inner iteration forms p = z + beta p_old at every
-// stored entry instead of in a pass of its own (FP32 arithmetic is cheap, a cluster
-// barrier is not).
+// by one cluster per problem.
+// The inner solve is Chronopoulos–Gear PCG (one reduction of r.u, w.u, r.r per
+// iteration, u = D^-1 r, w = A u) in ONE pass over the rows per iteration: each row's
+// state (r, w, s, D^-1) is a float4 in two buffers; a pass reads the old state of its
+// rows and of their neighbours and writes the new state of its rows, forming each
+// neighbour's new u = D^-1 (r - alpha (w + beta s)) from its old state at the stored
+// entry, so w_new = A u_new needs no barrier of its own.  p and d are the row's own.
 template <int CL>
 __global__ void __launch_bounds__(FG_BATCH_THREADS, 2) k_batch_pcg_mixed(const BatchProb *__restrict__ probs) {
   cgrp::cluster_group cl = cgrp::this_cluster();
-  __shared__ BatchShared<2> sh;
+  __shared__ BatchShared<1> sh;     // FP64 residual norms
+  __shared__ BatchShared32<3> sf;   // inner FP32 sums
   const int rank = (int)cl.block_rank();
   const BatchProb *pp = probs + blockIdx.x / CL;
   const int64_t n = pp->n;
@@ -308,20 +367,20 @@ __global__ void __launch_bounds__(FG_BATCH_THREADS, 2) k_batch_pcg_mixed(const B
   const float *__restrict__ dinv32 = pp->dinv32;
   const uint8_t *__restrict__ fixed = pp->fixed;
   double *x = pp->x, *r = pp->r;
-  float *r32 = pp->r32, *z32 = pp->z32, *q32 = pp->q32, *d32 = pp->d32;
+  float *pv = pp->p32, *dv = pp->d32;
   const int per = (nslices + CL - 1) / CL;
   const int s0 = min(rank * per, nslices), s1 = min(s0 + per, nslices);
   const int64_t i0 = (int64_t)s0 * FG_SLICE, i1 = min((int64_t)s1 * FG_SLICE, n);
   const int maxit = pp->maxit;
-  int which = 0, it = 0, ref = 0, st = -1;
-  // thread 0's scalar state (the same in every CTA of the cluster)
-  double rr0 = -1.0, rrt = 0.0, irz = 0.0, itol2 = 0.0;
+  int which = 0, whichf = 0, it = 0, ref = 0, st = -1;
+  // thread 0's FP64 state (the same in every CTA of the cluster)
+  double rr0 = -1.0, rrt = 0.0;
   while (true) {
     // FP64 residual r = -A x on the free rows (the right-hand side is 0)
     double prr = 0.0;
     for (int64_t i = i0 + threadIdx.x; i < i1; i += FG_BATCH_THREADS) {
       double ri = 0.0;
-      if (!(fixed && fixed[i])) ri = -sell_row(sl_ptr, sl_len, sl_col, val, i, [&](int j) { return x[j]; });
+      if (!(fixed && fixed[i])) ri = -sell_row<2>(sl_ptr, sl_len, sl_col, val, i, [&](int j) { return x[j]; });
       r[i] = ri;
       prr = fma(ri, ri, prr);
     }
@@ -343,104 +402,107 @@ __global__ void __launch_bounds__(FG_BATCH_THREADS, 2) k_batch_pcg_mixed(const B
         sh.bc[0] = s;
         sh.bc[1] = s < 0 ? 1.0 / rn : 0.0;
         sh.bc[2] = rn;
-        itol2 = inner * inner;
+        sh.bc[3] = inner * inner;
       }
     }
     __syncthreads();
     st = (int)sh.bc[0];
     if (st >= 0) break;
     const double scale = sh.bc[1], rn = sh.bc[2];
-    // inner FP32 start: r32 = r / ||r||, z = D^-1 r32, d = 0, p = 0
-    float frz = 0.f, frr = 0.f;
+    const float inner2 = (float)sh.bc[3];
+    float4 *so = pp->sa32, *sn = pp->sb32;
+    // inner start: r0 = r / ||r||, state (r0, 0, 0, D^-1), p = d = 0
     for (int64_t i = i0 + threadIdx.x; i < i1; i += FG_BATCH_THREADS) {
-      const float ri = (float)(r[i] * scale);
-      const float zi = dinv32[i] * ri;
-      r32[i] = ri;
-      z32[i] = zi;
-      d32[i] = 0.f;
-      pp->pa32[i] = 0.f;
-      pp->pb32[i] = 0.f;
-      frz = fmaf(ri, zi, frz);
-      frr = fmaf(ri, ri, frr);
+      so[i] = make_float4((float)(r[i] * scale), 0.f, 0.f, dinv32[i]);
+      pv[i] = 0.f;
+      dv[i] = 0.f;
     }
-    double tot[2];
+    cluster_barrier(cl);
+    // w0 = A u0 and the first sums (the scalars: every thread holds the same bits)
+    float g = 0.f, dl = 0.f, rr = 0.f;
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += FG_BATCH_THREADS) {
+      const float4 o = so[i];
+      float wi = 0.f;
+      if (!(fixed && fixed[i]))
+        wi = sell_row<4>(sl_ptr, sl_len, sl_col, val32, i, [&](int j) {
+          const float4 t = so[j];
+          return t.w * t.x;
+        });
+      const float ui = o.w * o.x;
+      sn[i] = make_float4(o.x, wi, 0.f, o.w);
+      g = fmaf(o.x, ui, g);
+      dl = fmaf(wi, ui, dl);
+      rr = fmaf(o.x, o.x, rr);
+    }
+    float tot[3];
     {
-      const float v[2] = {frz, frr};
-      cluster_sums<CL>(cl, sh, v, which, tot);
-      which ^= 1;
+      const float v[3] = {g, dl, rr};
+      cluster_sums_f32<CL>(cl, sf, v, whichf, tot);
+      whichf ^= 1;
     }
-    if (threadIdx.x == 0) {
-      irz = tot[0];
-      itol2 *= tot[1];
-      sh.bc[0] = (tot[1] > 0.0) ? -1 : 0;
+    {
+      float4 *t = so;
+      so = sn;
+      sn = t;
     }
-    __syncthreads();
-    int ist = (int)sh.bc[0];
-    float beta = 0.f;
-    float *pold = pp->pa32, *pnew = pp->pb32;
+    float gam = tot[0];
+    const float itol2 = inner2 * tot[2];
+    int ist = -1;
+    if (!(tot[2] > 0.f)) ist = 0;
+    else if (!(tot[1] > 0.f) || !isfinite(tot[1])) ist = (tot[1] == 0.f) ? 0 : 2;
+    float alpha = ist < 0 ? gam / tot[1] : 0.f, beta = 0.f;
     while (ist < 0 && it < maxit) {
-      // p = z + beta p_old (formed at every entry from z and p_old); q = A p; p.q
-      float fpq = 0.f;
+      // s = w + beta s; p = u + beta p; d += alpha p; r -= alpha s; u = D^-1 r; w = A u
+      g = 0.f;
+      dl = 0.f;
+      rr = 0.f;
       for (int64_t i = i0 + threadIdx.x; i < i1; i += FG_BATCH_THREADS) {
-        float qi = 0.f, pi = 0.f;
-        if (!(fixed && fixed[i])) {
-          qi = sell_row(sl_ptr, sl_len, sl_col, val32, i, [&](int j) { return fmaf(beta, pold[j], z32[j]); });
-          pi = fmaf(beta, pold[i], z32[i]);
-        }
-        pnew[i] = pi;
-        q32[i] = qi;
-        fpq = fmaf(pi, qi, fpq);
+        const float4 o = so[i];
+        const float sk = fmaf(beta, o.z, o.y);
+        const float pk = fmaf(beta, pv[i], o.w * o.x);
+        dv[i] = fmaf(alpha, pk, dv[i]);
+        pv[i] = pk;
+        const float rk = fmaf(-alpha, sk, o.x);
+        const float uk = o.w * rk;
+        float wk = 0.f;
+        if (!(fixed && fixed[i]))
+          wk = sell_row<4>(sl_ptr, sl_len, sl_col, val32, i, [&](int j) {
+            const float4 t = so[j];
+            return t.w * fmaf(-alpha, fmaf(beta, t.z, t.y), t.x);
+          });
+        sn[i] = make_float4(rk, wk, sk, o.w);
+        g = fmaf(rk, uk, g);
+        dl = fmaf(wk, uk, dl);
+        rr = fmaf(rk, rk, rr);
       }
       {
-        const float v[1] = {fpq};
-        double t1[1];
-        cluster_sums<CL>(cl, sh, v, which, t1);
-        which ^= 1;
-        if (threadIdx.x == 0) {
-          const double pq = t1[0];
-          int s = -1;
-          if (!(pq > 0.0) || !isfinite(pq)) s = (pq == 0.0) ? 0 : 2;
-          sh.bc[0] = s;
-          sh.bc[1] = s < 0 ? irz / pq : 0.0;
-        }
-      }
-      __syncthreads();
-      ist = (int)sh.bc[0];
-      if (ist >= 0) break;
-      const float alpha = (float)sh.bc[1];
-      // d += alpha p; r -= alpha q; z = D^-1 r
-      frz = 0.f;
-      frr = 0.f;
-      for (int64_t i = i0 + threadIdx.x; i < i1; i += FG_BATCH_THREADS) {
-        d32[i] = fmaf(alpha, pnew[i], d32[i]);
-        const float ri = fmaf(-alpha, q32[i], r32[i]);
-        const float zi = dinv32[i] * ri;
-        r32[i] = ri;
-        z32[i] = zi;
-        frz = fmaf(ri, zi, frz);
-        frr = fmaf(ri, ri, frr);
+        const float v[3] = {g, dl, rr};
+        cluster_sums_f32<CL>(cl, sf, v, whichf, tot);
+        whichf ^= 1;
       }
       {
-        const float v[2] = {frz, frr};
-        cluster_sums<CL>(cl, sh, v, which, tot);
-        which ^= 1;
+        float4 *t = so;
+        so = sn;
+        sn = t;
       }
       ++it;
-      if (threadIdx.x == 0) {
-        const double rzn = tot[0], rri = tot[1];
-        sh.bc[0] = !isfinite(rri) ? 2 : (rri <= itol2 ? 0 : -1);
-        sh.bc[1] = rzn / irz;
-        irz = rzn;
+      if (!isfinite(tot[2])) {
+        ist = 2;
+        break;
       }
-      __syncthreads();
-      ist = (int)sh.bc[0];
-      beta = (float)sh.bc[1];
-      float *t = pold;
-      pold = pnew;
-      pnew = t;
+      if (tot[2] <= itol2) break;
+      const float gn = tot[0];
+      beta = gn / gam;
+      const float den = tot[1] - beta * gn / alpha;  // p.A p of the next direction
+      if (!(den > 0.f) || !isfinite(den)) {
+        ist = (den == 0.f) ? 0 : 2;
+        break;
+      }
+      alpha = gn / den;
+      gam = gn;
     }
     // x += ||r|| d
-    for (int64_t i = i0 + threadIdx.x; i < i1; i += FG_BATCH_THREADS) x[i] = fma(rn, (double)d32[i], x[i]);
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += FG_BATCH_THREADS) x[i] = fma(rn, (double)dv[i], x[i]);
     if (ist == 2) {
       st = 2;
       break;
@@ -496,14 +558,15 @@ extern "C" fg_status fg_batch_magnetostatics_linear(fg_mesh *const *meshes, int3
       fg_assemble_operator(m, ASM_STIFF, m->mu_lin, nullptr, nullptr, 0.0, 0.0, 0, OUT_SELL, true, mixed, true);
       for (int j : {7, 0, 1, 2, 3})
         if (!m->v64[j]) m->v64[j] = dev_alloc<double>(m, (size_t)m->nvp);
-      // FP32 inner vectors: the split FP32 CG's and the pipelined CG's scratch (each
-      // nvp long, zeroed when first made; every solve initialises what it reads)
-      float **f32[6] = {&m->v32[4], &m->v32[5], &m->v32[6], &m->v32[7], &m->pv32[0], &m->pv32[1]};
+      // FP32 inner vectors: the fused FP32 CG's row-state buffers (4 nvp floats each)
+      // and its x and p vectors (nvp), zeroed when first made as the CG solver makes
+      // them; every solve initialises what it reads
       if (mixed)
-        for (float **f : f32)
-          if (!*f) {
-            *f = dev_alloc<float>(m, (size_t)m->nvp);
-            FG_CUDA_TRY(cudaMemsetAsync(*f, 0, sizeof(float) * (size_t)m->nvp, m->stream));
+        for (int j = 0; j < 4; ++j)
+          if (!m->v32[j]) {
+            const size_t len = (size_t)m->nvp * ((j == 2 || j == 3) ? 4 : 1);
+            m->v32[j] = dev_alloc<float>(m, len);
+            FG_CUDA_TRY(cudaMemsetAsync(m->v32[j], 0, sizeof(float) * len, m->stream));
           }
       FG_CUDA_TRY(cudaMemcpyAsync(m->v64[7], u_in[k], sizeof(double) * (size_t)m->nv, cudaMemcpyHostToDevice,
                                   m->stream));
@@ -523,12 +586,10 @@ extern "C" fg_status fg_batch_magnetostatics_linear(fg_mesh *const *meshes, int3
       b.z = m->v64[1];
       b.p = m->v64[2];
       b.q = m->v64[3];
-      b.r32 = mixed ? *f32[0] : nullptr;
-      b.z32 = mixed ? *f32[1] : nullptr;
-      b.pa32 = mixed ? *f32[2] : nullptr;
-      b.pb32 = mixed ? *f32[3] : nullptr;
-      b.q32 = mixed ? *f32[4] : nullptr;
-      b.d32 = mixed ? *f32[5] : nullptr;
+      b.sa32 = mixed ? reinterpret_cast<float4 *>(m->v32[2]) : nullptr;
+      b.sb32 = mixed ? reinterpret_cast<float4 *>(m->v32[3]) : nullptr;
+      b.p32 = mixed ? m->v32[1] : nullptr;
+      b.d32 = mixed ? m->v32[0] : nullptr;
       b.tol2_rel = opts.rtol * opts.rtol;
       b.inner_rtol = opts.inner_rtol;
       b.maxit = opts.maxiter;
