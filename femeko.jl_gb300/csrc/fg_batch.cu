@@ -22,7 +22,11 @@
 
 namespace cgrp = cooperative_groups;
 
-// Threads per CTA (1024-thread CTAs spilled registers: 64 per thread at most)
+// Threads per CTA.  The FP64 kernel runs two CTAs per SM (64 registers a thread; its
+// FP64 pipe is the limit, and two CTAs per SM pack the batch into fewer waves); the
+// mixed kernel one CTA per SM with 128 registers a thread, which keeps more of a row's
+// loads in flight (17 against 22 us per iteration on a 69k-row problem; two rows per
+// thread in flight and 16-bit column offsets were measured slower or no faster).
 constexpr int FG_BATCH_THREADS = 512;
 constexpr int FG_BATCH_WARPS = FG_BATCH_THREADS / 32;
 // FP64 refinement steps of a mixed-precision problem at most (as the single-mesh solver)
@@ -351,7 +355,7 @@ __global__ void __launch_bounds__(FG_BATCH_THREADS, 2) k_batch_pcg64(const Batch
 // neighbour's new u = D^-1 (r - alpha (w + beta s)) from its old state at the stored
 // entry, so w_new = A u_new needs no barrier of its own.  p and d are the row's own.
 template <int CL>
-__global__ void __launch_bounds__(FG_BATCH_THREADS, 2) k_batch_pcg_mixed(const BatchProb *__restrict__ probs) {
+__global__ void __launch_bounds__(FG_BATCH_THREADS, 1) k_batch_pcg_mixed(const BatchProb *__restrict__ probs) {
   cgrp::cluster_group cl = cgrp::this_cluster();
   __shared__ BatchShared<1> sh;     // FP64 residual norms
   __shared__ BatchShared32<3> sf;   // inner FP32 sums
