@@ -40,7 +40,12 @@ extern "C" void fg_newton_opts_default(fg_newton_opts *o) {
   o->use_graph = 1;
   o->forcing = FG_FORCING_EW;
   o->picard_steps = 2;
-  o->eta_min = 1e-6;
+  // floor of the forcing term: near the solution Newton then contracts by about
+  // eta_min per step, so after the last step (|alpha du| <= tol_update |u|) the error
+  // left is about eta_min x tol_update relative.  On the 96^3 Froehlich plate 1e-3
+  // takes the same 11 Newton steps as 1e-6 with 1,073 instead of 1,334 CG iterations,
+  // H within 1e-12 of a solve to 1e-13.
+  o->eta_min = 1e-3;
   o->eta_max = 0.1;
 }
 
