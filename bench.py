@@ -438,14 +438,15 @@ def run_ours(args):
         traffic = {10: 70.73e6, 14: 97.07e6, 17: 97.38e6, 20: 69.70e6, 22: 97.66e6, 27: 97.3e6}[v]
         traffic_src = "ncu dram__bytes_read.sum + dram__bytes_write.sum of this kernel at 96^3"
     # the whole CG iteration in the solver's loop (every kernel of it): the dominant
-    # SpMV's bytes plus the vector pass's (split: 28 B read + 20 B written per row;
-    # Jacobi-scaled system: 20 + 16 B; fused: counted in the kernel above)
+    # SpMV's bytes plus the vector pass's (split: 24 B read + 20 B written per row, u
+    # formed again from r; Jacobi-scaled system: 20 + 16 B; fused: counted in the
+    # kernel above)
     if v in (24, 25):
         it_bytes = None
     elif v in (16, 20):
         it_bytes = g.nnz * 6 + 12 * n + 36 * n
     elif v >= 6 and v != 26:
-        it_bytes = g.nnz * 6 + 12 * n + 48 * n
+        it_bytes = g.nnz * 6 + 12 * n + 44 * n
     else:
         it_bytes = alg_bytes
     # the last-block-finish variants: their SpMV code without the finishing tail (the

@@ -549,7 +549,10 @@ __device__ __forceinline__ void griddep_release() { asm volatile("griddepcontrol
 // FP32 Chronopoulos-Gear iteration split in two passes, as the FP64 one: a streaming
 // vector update (s = w + beta s, p = u + beta p, x += alpha p, r -= alpha s,
 // u = D^-1 r; four rows per thread) and w = A u with the three dot products.  The
-// SpMV then gathers 4-byte entries of u instead of 16-byte neighbour states.
+// SpMV then gathers 4-byte entries of u instead of 16-byte neighbour states.  The u
+// of the previous iteration is formed again as D^-1 r (the same single rounding that
+// wrote it, here and in k_cg32s_init) instead of being read: 24 B read and 20 B
+// written per row.
 __global__ void __launch_bounds__(256) k_cg32s_vec(int64_t n4, float4 *__restrict__ r, const float4 *__restrict__ w,
                                                    float4 *__restrict__ s, float4 *__restrict__ p,
                                                    float4 *__restrict__ u, float4 *__restrict__ x,
@@ -562,9 +565,10 @@ __global__ void __launch_bounds__(256) k_cg32s_vec(int64_t n4, float4 *__restric
   // the flag, the scalars and the vectors are loaded together
   const int done = ictl[I_DONE];
   const double alpha_d = scal[S_ALPHA], beta_d = scal[S_BETA];
-  const float4 ww = w[j], dd = dinv[j], uu = u[j];
+  const float4 ww = w[j], dd = dinv[j];
   float4 ss = s[j], pp = p[j], xx = x[j], rr = r[j];
   if (done) return;
+  const float4 uu = make_float4(dd.x * rr.x, dd.y * rr.y, dd.z * rr.z, dd.w * rr.w);
   const float alpha = (float)alpha_d, beta = (float)beta_d;
   ss.x = fmaf(beta, ss.x, ww.x); ss.y = fmaf(beta, ss.y, ww.y); ss.z = fmaf(beta, ss.z, ww.z); ss.w = fmaf(beta, ss.w, ww.w);
   pp.x = fmaf(beta, pp.x, uu.x); pp.y = fmaf(beta, pp.y, uu.y); pp.z = fmaf(beta, pp.z, uu.z); pp.w = fmaf(beta, pp.w, uu.w);
