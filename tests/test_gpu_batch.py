@@ -77,3 +77,34 @@ def test_batch_iteration_cap_is_reported(precision):
     assert (its <= 7).all() and its.max() == 7
     for u in us:
         assert np.isfinite(u).all()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batch_triangles_and_tetrahedra_together(precision):
+    """P1 triangle and tetrahedron meshes in one launch, each against a direct solve
+    of the oracle's stiffness matrix on the free rows."""
+    import scipy.sparse.linalg as spla
+    rng = np.random.default_rng(21)
+    meshes = [fg.box_tri_mesh(24, seed=1), fg.box_tet_mesh(7, seed=2), fg.box_tri_mesh(10, seed=3)]
+    mus = [rng.uniform(1, 1000, m.nt) * fg.MU0 for m in meshes]
+    u0s = [-m.p[0].copy() for m in meshes]
+    us, its, st = fg.batch_magnetostatics_linear(meshes, mus, u0s, rtol=1e-11, precision=precision)
+    assert st["problems"] == 3 and st["converged"] == 3
+    for m, mu, u0, u in zip(meshes, mus, u0s, us):
+        K = (O.stiffnessMatrix2D(m, mu) if m.t.shape[0] == 3 else O.stiffnessMatrix(m, mu)).tocsr()
+        fx = m.dirichlet_mask().astype(bool)
+        fr = ~fx
+        ref = u0.copy()
+        ref[fr] = spla.spsolve(K[fr][:, fr].tocsc(), -(K[fr][:, fx] @ u0[fx]))
+        assert np.linalg.norm(u - ref) / np.linalg.norm(ref) < 1e-8
+        assert np.array_equal(u[fx], u0[fx])
+
+
+def test_batch_single_problem_mixed_matches_fp64():
+    """One problem alone (the largest cluster) in both precisions."""
+    meshes, mus, u0s = batch_case(1, 16, 16, seed=13)
+    um, itm, stm = fg.batch_magnetostatics_linear(meshes, mus, u0s, rtol=1e-10, precision="mixed")
+    ud, itd, std = fg.batch_magnetostatics_linear(meshes, mus, u0s, rtol=1e-10)
+    assert stm["converged"] == 1 and std["converged"] == 1
+    assert stm["cluster_ctas"] == std["cluster_ctas"] and stm["cluster_ctas"] in (8, 16)
+    assert np.linalg.norm(um[0] - ud[0]) / np.linalg.norm(ud[0]) < 1e-8
