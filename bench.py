@@ -500,7 +500,9 @@ def run_ours(args):
             L.check(lib.fg_scalar_potential_newton(L.ptr(p_np), mesh.nv, L.ptr(t_np), mesh.nt, 0, L.ptr(fx_np),
                                                    L.ptr(nl_np), L.ptr(mu_np), L.ptr(u0_np), C.byref(o),
                                                    L.ptr(uo_np), L.ptr(Ho_np), L.ptr(muo_np), C.byref(s)))
-        for _ in range(max(1, min(args.warmup, 2))):
+        # at least three untimed calls: the first ones on a fresh process also grow the
+        # device's memory pool and the recycled pinned read-back blocks
+        for _ in range(max(3, args.warmup)):
             one()
         barrier()
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -539,7 +541,7 @@ def run_ours(args):
                   "newton_solve_with_io": 1e3 * (t3 - t2), "of_which_newton_device_ms": s.ms,
                   "of_which_newton_setup_ms": s.setup_ms, "destroy": 1e3 * (t4 - t3)}
         e2e = {"value": ws * args.e2e_steps / e2e_sec, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
+               "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps, "warmup": max(3, args.warmup),
                "call_ms": [round(c, 2) for c in call_ms],
                "what": "fg_scalar_potential_newton: upload + pattern build + solve + download per step",
                "phases_ms_one_call": {k: round(v, 3) for k, v in phases.items()}}

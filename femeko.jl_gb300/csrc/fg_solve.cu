@@ -231,6 +231,21 @@ __device__ __forceinline__ void cgcg_scalars(const double (&tot)[3], double *sca
   cgcg_store(cgcg_next(tot, scal[S_RZ], scal[S_ALPHA], scal[S_TOL2], ictl[I_ITERS], ictl[I_MAXIT]), scal, ictl);
 }
 
+// The previous scalars cgcg_next needs, loaded by a finishing thread before it sums
+// the partials (the loads then overlap those of the partials instead of following
+// the block sum).  Nothing in the running launch writes them before its finish.
+struct CgPrev {
+  double gold, aold, tol2;
+  int it, maxit;
+};
+__device__ __forceinline__ CgPrev cgcg_prev(const double *scal, const int *ictl) {
+  return CgPrev{__ldcg(scal + S_RZ), __ldcg(scal + S_ALPHA), __ldcg(scal + S_TOL2), __ldcg(ictl + I_ITERS),
+                __ldcg(ictl + I_MAXIT)};
+}
+__device__ __forceinline__ void cgcg_scalars(const double (&tot)[3], const CgPrev &pv, double *scal, int *ictl) {
+  cgcg_store(cgcg_next(tot, pv.gold, pv.aold, pv.tol2, pv.it, pv.maxit), scal, ictl);
+}
+
 // ------------------------------------------------------------------ FP32 CG (fused)
 // State per row in a float4 pair buffer: (r, w, s, dinv).  `first` computes
 // w0 = A u0 from (r0, -, -, dinv) with alpha = beta = 0 (then s stays 0); later
@@ -840,6 +855,8 @@ __global__ void __launch_bounds__(256) k_cg32s_spmv_bulk(int64_t n, int nslices,
     __syncthreads();
     if (!s_last) return;
     __threadfence();
+    CgPrev pv{};
+    if (tid == 0) pv = cgcg_prev(scal, ictl);
     ff acc[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
     sum_partials_ff3<4>(reinterpret_cast<const float2 *>(partials), (int)gridDim.x, acc);
     block_sum_ff_pair<3>(acc, shs);
@@ -847,7 +864,7 @@ __global__ void __launch_bounds__(256) k_cg32s_spmv_bulk(int64_t n, int nslices,
       counter[FG_LAST1_COUNTER] = 0u;
       double tot[3];
       for (int j = 0; j < 3; ++j) tot[j] = (double)acc[j].hi + (double)acc[j].lo;
-      cgcg_scalars(tot, scal, ictl);
+      cgcg_scalars(tot, pv, scal, ictl);
     }
     return;
   }
@@ -863,6 +880,8 @@ __global__ void __launch_bounds__(256) k_cg32s_spmv_bulk(int64_t n, int nslices,
 __global__ void __launch_bounds__(256) k_cg32_dots_finish(const float2 *__restrict__ partials, int nparts,
                                                           double *scal, int *ictl) {
   if (ictl[I_DONE]) return;
+  CgPrev pv{};
+  if (threadIdx.x == 0) pv = cgcg_prev(scal, ictl);
   ff acc[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
   sum_partials_ff3<4>(partials, nparts, acc);
   __shared__ ff shr[3][32];
@@ -870,7 +889,7 @@ __global__ void __launch_bounds__(256) k_cg32_dots_finish(const float2 *__restri
   if (threadIdx.x == 0) {
     double tot[3];
     for (int j = 0; j < 3; ++j) tot[j] = (double)acc[j].hi + (double)acc[j].lo;
-    cgcg_scalars(tot, scal, ictl);
+    cgcg_scalars(tot, pv, scal, ictl);
   }
 }
 
