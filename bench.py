@@ -57,7 +57,7 @@ def workload(cells: int):
 def config(cells, mesh):
     return {"workload": f"nonlinear Froehlich-plate magnetostatics, Kuhn tets {cells}^3 cells",
             "cells": cells, "tets": int(mesh.nt), "nodes": int(mesh.nv), "newton_tol_update": 1e-8,
-            "inner_tolerance": "Eisenstat-Walker (choice 2, gamma 0.9) in [1e-3, 0.1], both precisions",
+            "inner_tolerance": "Eisenstat-Walker (choice 2, gamma 0.9) in [1e-2, 0.3], both precisions",
             "line_search": "alpha = 0.9^k backtracking on the nonlinear residual",
             "l2": "inputs larger than L2 (operator, records and element state ~2 GB)"}
 
@@ -170,9 +170,9 @@ def cpu_model() -> str:
 
 
 # The Newton settings both the GPU path and the oracle run: Eisenstat-Walker inner
-# tolerances (choice 2, gamma 0.9) in [1e-3, 0.1], two Picard (secant) steps, alpha =
+# tolerances (choice 2, gamma 0.9) in [1e-2, 0.3], two Picard (secant) steps, alpha =
 # 0.9^k backtracking on the true nonlinear residual, stop at |alpha du| <= 1e-8 |u|.
-NEWTON_SETTINGS = dict(tol_update=1e-8, line_search="residual", forcing="ew", eta_min=1e-3, eta_max=0.1,
+NEWTON_SETTINGS = dict(tol_update=1e-8, line_search="residual", forcing="ew", eta_min=1e-2, eta_max=0.3,
                        picard_steps=2)
 
 
@@ -508,11 +508,12 @@ def run_ours(args):
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         w0 = time.time()
         ev0.record()
-        call_ms = []
+        call_ms, solve_ms = [], []
         for _ in range(args.e2e_steps):
             c0 = time.perf_counter()
             one()
             call_ms.append(1e3 * (time.perf_counter() - c0))
+            solve_ms.append(s.ms)
         ev1.record()
         barrier()
         e2e_sec = max(ev0.elapsed_time(ev1) / 1000.0, time.time() - w0)
@@ -543,6 +544,7 @@ def run_ours(args):
         e2e = {"value": ws * args.e2e_steps / e2e_sec, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps, "warmup": max(3, args.warmup),
                "call_ms": [round(c, 2) for c in call_ms],
+               "newton_device_ms": [round(c, 2) for c in solve_ms],
                "what": "fg_scalar_potential_newton: upload + pattern build + solve + download per step",
                "phases_ms_one_call": {k: round(v, 3) for k, v in phases.items()}}
 

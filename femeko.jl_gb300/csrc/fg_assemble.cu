@@ -1607,12 +1607,20 @@ void fg_nl_setup(fg_mesh *m, const uint8_t *nl_host, bool mixed) {
 }
 
 void fg_newton_assemble_split(fg_mesh *m, const double *d_u, double Ms, double Hk, bool mixed, double *d_F,
-                              bool want_jacobian, bool tangent) {
+                              bool want_jacobian, bool tangent, const double *lin_in, double *lin_out) {
   FG_REQUIRE(m->vlin64 != nullptr && m->nl_maps_valid, FG_BAD_ARG, "Newton split: no linear operator");
   const int n = m->n_nl;
   const uint8_t *fx = m->has_fixed ? m->fixed : nullptr;
   // F = -(K_lin u + the nonlinear elements' K_e(mu(u)) u_e), Dirichlet rows 0
-  fg_spmv64_vals(m, m->vlin64, d_u, d_F);
+  if (lin_in) {
+    if (lin_in != d_F)
+      FG_CUDA_TRY(cudaMemcpyAsync(d_F, lin_in, sizeof(double) * (size_t)m->nv, cudaMemcpyDeviceToDevice, m->stream));
+  } else if (lin_out) {
+    fg_spmv64_vals(m, m->vlin64, d_u, lin_out);
+    FG_CUDA_TRY(cudaMemcpyAsync(d_F, lin_out, sizeof(double) * (size_t)m->nv, cudaMemcpyDeviceToDevice, m->stream));
+  } else {
+    fg_spmv64_vals(m, m->vlin64, d_u, d_F);
+  }
   if (n > 0) {
     k_elem_newton_nl<<<grid_for(n, 128), 128, 0, m->stream>>>(n, m->nl_elems, m->nt, m->geo, m->t, d_u, Ms, Hk,
                                                               m->mu, m->dmu, m->nl_re,

@@ -217,7 +217,7 @@ struct fg_mesh {
   double *objbuf = nullptr;   // 2 x nt objective scratch (adjoint)
 
   // vectors
-  double *v64[16] = {nullptr};
+  double *v64[20] = {nullptr};
   // BiCGStab vectors (padded to nvp), the mass values of the transport operator
   // (SELL layout) and the captured iteration graph
   double *bcg[10] = {nullptr};
@@ -338,8 +338,11 @@ void fg_nl_setup(fg_mesh *m, const uint8_t *nl_host, bool mixed);
 // Stores the nonlinear mask of new Newton inputs in m->nl_host; the element list
 // built from it is kept when the mask did not change.
 void fg_set_nl_host(fg_mesh *m, const uint8_t *nl);
+// lin_in: K_lin u already known (a vector, or d_F itself when it holds it), so the
+// linear elements' SpMV is skipped; lin_out: where the SpMV also leaves K_lin u.
 void fg_newton_assemble_split(fg_mesh *m, const double *d_u, double Ms, double Hk, bool mixed, double *d_F,
-                              bool want_jacobian, bool tangent);
+                              bool want_jacobian, bool tangent, const double *lin_in = nullptr,
+                              double *lin_out = nullptr);
 // d_out[i] = sum of the vector records of row i (P1 tetrahedra), no Dirichlet masking.
 void fg_vector_gather(fg_mesh *m, double *d_out);
 // src/FEM3D.jl:284-297 / src/FEMc.cpp:170-200 BoundaryIntegral into a device vector

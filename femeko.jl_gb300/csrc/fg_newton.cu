@@ -25,6 +25,20 @@ __global__ void k_axpby64(int64_t n, double a, const double *__restrict__ x, dou
   if (i < n) out[i] = a * x[i] + b * y[i];
 }
 
+// One line-search trial point: ut = u + alpha du and, since K_lin is linear, its
+// linear elements' part K_lin ut = K_lin u + alpha K_lin du (yt, and F as the start
+// of the residual) without another SpMV of the linear operator.
+__global__ void k_newton_trial64(int64_t n, double alpha, const double *__restrict__ u, const double *__restrict__ du,
+                                 const double *__restrict__ y, const double *__restrict__ z, double *__restrict__ ut,
+                                 double *__restrict__ yt, double *__restrict__ F) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  ut[i] = 1.0 * u[i] + alpha * du[i];
+  const double v = y[i] + alpha * z[i];
+  yt[i] = v;
+  F[i] = v;
+}
+
 extern "C" void fg_newton_opts_default(fg_newton_opts *o) {
   if (!o) return;
   o->precision = FG_MIXED;
@@ -40,13 +54,14 @@ extern "C" void fg_newton_opts_default(fg_newton_opts *o) {
   o->use_graph = 1;
   o->forcing = FG_FORCING_EW;
   o->picard_steps = 2;
-  // floor of the forcing term: near the solution Newton then contracts by about
+  // forcing term in [1e-2, 0.3]: near the solution Newton then contracts by about
   // eta_min per step, so after the last step (|alpha du| <= tol_update |u|) the error
-  // left is about eta_min x tol_update relative.  On the 96^3 Froehlich plate 1e-3
-  // takes the same 11 Newton steps as 1e-6 with 1,073 instead of 1,334 CG iterations,
-  // H within 1e-12 of a solve to 1e-13.
-  o->eta_min = 1e-3;
-  o->eta_max = 0.1;
+  // left is about eta_min x tol_update relative.  Over six jittered 96^3 Froehlich
+  // plates (mixed precision) [1e-2, 0.3] took 914-1,030 CG iterations per solve
+  // (mean 31.5 ms) with H within 5.5e-11 of a tight FP64 solve; [1e-3, 0.1] took
+  // 1,012-1,292 (mean 36.0 ms, H within 3.8e-12).
+  o->eta_min = 1e-2;
+  o->eta_max = 0.3;
 }
 
 static void upload(fg_mesh *m, void *dst, const void *src, size_t bytes) {
@@ -75,6 +90,12 @@ static int newton_dev(fg_mesh *m, double *d_u, const uint8_t *nl_host, const fg_
                       fg_newton_stats *st) {
   const bool mixed = o.precision == FG_MIXED;
   double *d_du = vec64(m, 8), *d_F = vec64(m, 9), *d_ut = vec64(m, 10), *d_Ft = vec64(m, 11);
+  // residual line search: K_lin u at the current iterate (y, refreshed by an SpMV at
+  // every accepted iterate), K_lin du (z, one SpMV per step) and K_lin ut (yt), so a
+  // trial costs vector updates and the nonlinear elements, not an SpMV
+  const bool incremental = (o.line_search == FG_LS_RESIDUAL || o.line_search == FG_LS_QUADRATIC);
+  double *d_y = incremental ? vec64(m, 16) : nullptr, *d_z = incremental ? vec64(m, 17) : nullptr;
+  double *d_yt = incremental ? vec64(m, 18) : nullptr;
   fg_solve_opts so;
   fg_solve_opts_default(&so);
   so.precision = o.precision;
@@ -97,7 +118,7 @@ static int newton_dev(fg_mesh *m, double *d_u, const uint8_t *nl_host, const fg_
   // the linear elements' operator once; each residual / Jacobian below re-evaluates
   // only the nonlinear elements on top of it
   fg_nl_setup(m, nl_host, mixed);
-  fg_newton_assemble_split(m, d_u, o.Ms, o.Hk, mixed, d_F, true, o.picard_steps <= 0);
+  fg_newton_assemble_split(m, d_u, o.Ms, o.Hk, mixed, d_F, true, o.picard_steps <= 0, nullptr, d_y);
   FG_CUDA_TRY(cudaEventRecord(es, m->stream));
   fg_check_flags(m, "fg_newton_magnetostatics");
   double rF = fg_slot_sqrt(m, FG_SLOT_FNORM2);
@@ -137,10 +158,17 @@ static int newton_dev(fg_mesh *m, double *d_u, const uint8_t *nl_host, const fg_
       need_jacobian = !trial_jacobian;
       const double f0 = rF * rF;
       double rt = 0.0;
+      if (incremental) fg_spmv64_vals(m, m->vlin64, d_du, d_z);
       for (;;) {
-        k_axpby64<<<g, 256, 0, m->stream>>>(nv, 1.0, d_u, alpha, d_du, d_ut);
-        FG_LAUNCHED(1);
-        fg_newton_assemble_split(m, d_ut, o.Ms, o.Hk, mixed, d_Ft, trial_jacobian, next_tangent);
+        if (incremental) {
+          k_newton_trial64<<<g, 256, 0, m->stream>>>(nv, alpha, d_u, d_du, d_y, d_z, d_ut, d_yt, d_Ft);
+          FG_LAUNCHED(1);
+          fg_newton_assemble_split(m, d_ut, o.Ms, o.Hk, mixed, d_Ft, false, next_tangent, d_Ft);
+        } else {
+          k_axpby64<<<g, 256, 0, m->stream>>>(nv, 1.0, d_u, alpha, d_du, d_ut);
+          FG_LAUNCHED(1);
+          fg_newton_assemble_split(m, d_ut, o.Ms, o.Hk, mixed, d_Ft, trial_jacobian, next_tangent);
+        }
         rt = fg_slot_sqrt(m, FG_SLOT_FNORM2);
         ++trials;
         if (o.line_search == FG_LS_NONE || !(rt > rF && alpha > o.min_step)) break;
@@ -157,7 +185,7 @@ static int newton_dev(fg_mesh *m, double *d_u, const uint8_t *nl_host, const fg_
       }
       if (alpha < o.min_step) {
         // no decrease: keep u (src/FEM3D.jl:144-147) and restore the state at u
-        fg_newton_assemble_split(m, d_u, o.Ms, o.Hk, mixed, d_F, true, it > o.picard_steps);
+        fg_newton_assemble_split(m, d_u, o.Ms, o.Hk, mixed, d_F, true, it > o.picard_steps, nullptr, d_y);
         status = 1;
         alpha = 0.0;
         break;
@@ -167,6 +195,11 @@ static int newton_dev(fg_mesh *m, double *d_u, const uint8_t *nl_host, const fg_
       std::swap(m->v64[9], m->v64[11]);
       d_F = m->v64[9];
       d_Ft = m->v64[11];
+      if (incremental) {
+        std::swap(m->v64[16], m->v64[18]);
+        d_y = m->v64[16];
+        d_yt = m->v64[18];
+      }
       rF = rt;
     } else {
       // reference lineSearch: w = K(mu) du with the secant at the current mu
@@ -203,7 +236,7 @@ static int newton_dev(fg_mesh *m, double *d_u, const uint8_t *nl_host, const fg_
     ratio = (un > 0.0) ? dn / un : dn;
     if (!std::isfinite(ratio)) throw FgError{FG_NAN, "Newton update is not finite"};
     if (ratio <= o.tol_update) { converged = 1; break; }
-    if (need_jacobian) fg_newton_assemble_split(m, d_u, o.Ms, o.Hk, mixed, d_F, true, next_tangent);
+    if (need_jacobian) fg_newton_assemble_split(m, d_u, o.Ms, o.Hk, mixed, d_F, true, next_tangent, nullptr, d_y);
   }
   fg_energy_dev(m, d_u, o.Ms, o.Hk);
   double energy = fg_dot_dev(m, m->wdens, nullptr, m->nt, false);

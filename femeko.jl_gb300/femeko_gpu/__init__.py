@@ -200,7 +200,7 @@ def solve_opts(precision="fp64", rtol=1e-10, maxiter=1_000_000, inner_rtol=1e-5,
 
 def newton_opts(precision="mixed", tol_update=1e-8, maxit=100, inner_rtol=1e-4, cg_maxiter=200_000,
                 line_search="residual", min_step=1e-4, Ms=1.2e6, Hk=500.0, check_every=32, use_graph=True,
-                forcing="ew", eta_min=1e-3, eta_max=0.1, picard_steps=2):
+                forcing="ew", eta_min=1e-2, eta_max=0.3, picard_steps=2):
     """Newton options.  forcing="ew": Eisenstat-Walker inner tolerances in
     [eta_min, eta_max]; forcing="fixed": every inner solve to inner_rtol.
     picard_steps: first iterations without the tangent term."""

@@ -131,7 +131,7 @@ typedef struct fg_newton_opts {
   int32_t picard_steps; /* first iterations without the tangent term (secant/Picard
                            steps; the reference's first iteration is one,
                            Magnetostatics/NewtonRaphson.jl:164-168) */
-  double eta_min, eta_max;  /* defaults 1e-3 and 0.1 */
+  double eta_min, eta_max;  /* defaults 1e-2 and 0.3 */
 } fg_newton_opts;
 
 /* inner-tolerance (forcing term) rules of the Newton solver */

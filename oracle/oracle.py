@@ -520,7 +520,7 @@ LS_MODES = {"none": 0, "reference": 1, "residual": 2, "quadratic": 3}
 
 
 def newton(mesh, u0, nl, mu_lin, Ms, Hk, tol_update=1e-8, maxit=100, cg_tol=1e-12, cg_maxit=200000,
-           ref_bug_hz=False, line_search="residual", forcing="fixed", eta_min=1e-3, eta_max=0.1, picard_steps=0):
+           ref_bug_hz=False, line_search="residual", forcing="fixed", eta_min=1e-2, eta_max=0.3, picard_steps=0):
     """Dirichlet Newton-Raphson magnetostatics; returns (u, H 3 x nt, mu, stats dict).
     forcing="fixed" solves every increment to cg_tol; "ew" uses Eisenstat-Walker tolerances.
     picard_steps: first iterations with the secant operator only (no tangent term)."""

@@ -73,7 +73,7 @@ def newton48():
     mu_lin = np.full(m.nt, MU0)
     u0 = -(np.array([8e4, 0.0, 0.0])[:, None] * m.p).sum(axis=0)
     uo, Ho, muo, so = O.newton(m, u0, nl, mu_lin, MS, HK, tol_update=1e-8, line_search="residual", forcing="ew",
-                               eta_min=1e-3, eta_max=0.1, picard_steps=2)
+                               eta_min=1e-2, eta_max=0.3, picard_steps=2)
     assert so["converged"]
     return m, nl, mu_lin, u0, uo, Ho, muo, O.energy(m, Ho, nl, mu_lin, MS, HK)
 
