@@ -1611,8 +1611,11 @@ void fg_newton_assemble_split(fg_mesh *m, const double *d_u, double Ms, double H
   FG_REQUIRE(m->vlin64 != nullptr && m->nl_maps_valid, FG_BAD_ARG, "Newton split: no linear operator");
   const int n = m->n_nl;
   const uint8_t *fx = m->has_fixed ? m->fixed : nullptr;
-  // F = -(K_lin u + the nonlinear elements' K_e(mu(u)) u_e), Dirichlet rows 0
-  if (lin_in) {
+  // F = -(K_lin u + the nonlinear elements' K_e(mu(u)) u_e), Dirichlet rows 0; with
+  // d_F null only the Jacobian (the residual at u is known already)
+  if (!d_F) {
+    FG_REQUIRE(want_jacobian, FG_BAD_ARG, "Newton split: nothing to assemble");
+  } else if (lin_in) {
     if (lin_in != d_F)
       FG_CUDA_TRY(cudaMemcpyAsync(d_F, lin_in, sizeof(double) * (size_t)m->nv, cudaMemcpyDeviceToDevice, m->stream));
   } else if (lin_out) {
@@ -1626,12 +1629,15 @@ void fg_newton_assemble_split(fg_mesh *m, const double *d_u, double Ms, double H
                                                               m->mu, m->dmu, m->nl_re,
                                                               want_jacobian ? m->nl_ke : nullptr, tangent ? 1 : 0,
                                                               m->flags);
-    k_nl_rows<<<grid_for(m->n_nl_rows, 128), 128, 0, m->stream>>>(m->n_nl_rows, m->nl_rows, m->nl_row_ptr,
-                                                                  m->nl_row_src, m->nl_re, fx, d_F);
-    FG_LAUNCHED(2);
+    FG_LAUNCHED(1);
+    if (d_F) {
+      k_nl_rows<<<grid_for(m->n_nl_rows, 128), 128, 0, m->stream>>>(m->n_nl_rows, m->nl_rows, m->nl_row_ptr,
+                                                                    m->nl_row_src, m->nl_re, fx, d_F);
+      FG_LAUNCHED(1);
+    }
   }
   // F <- -F, with |F|^2 in scal[FG_SLOT_FNORM2] (the Dirichlet rows are 0)
-  fg_negate_norm2_enqueue(m, d_F);
+  if (d_F) fg_negate_norm2_enqueue(m, d_F);
   if (!want_jacobian) return;
   m->op_tag = 0;
   ++m->op_version;

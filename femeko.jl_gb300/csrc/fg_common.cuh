@@ -339,7 +339,8 @@ void fg_nl_setup(fg_mesh *m, const uint8_t *nl_host, bool mixed);
 // built from it is kept when the mask did not change.
 void fg_set_nl_host(fg_mesh *m, const uint8_t *nl);
 // lin_in: K_lin u already known (a vector, or d_F itself when it holds it), so the
-// linear elements' SpMV is skipped; lin_out: where the SpMV also leaves K_lin u.
+// linear elements' SpMV is skipped; lin_out: where the SpMV also leaves K_lin u;
+// d_F null: the Jacobian alone (element state and operator at u).
 void fg_newton_assemble_split(fg_mesh *m, const double *d_u, double Ms, double Hk, bool mixed, double *d_F,
                               bool want_jacobian, bool tangent, const double *lin_in = nullptr,
                               double *lin_out = nullptr);

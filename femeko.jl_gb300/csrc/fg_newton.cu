@@ -90,9 +90,10 @@ static int newton_dev(fg_mesh *m, double *d_u, const uint8_t *nl_host, const fg_
                       fg_newton_stats *st) {
   const bool mixed = o.precision == FG_MIXED;
   double *d_du = vec64(m, 8), *d_F = vec64(m, 9), *d_ut = vec64(m, 10), *d_Ft = vec64(m, 11);
-  // residual line search: K_lin u at the current iterate (y, refreshed by an SpMV at
-  // every accepted iterate), K_lin du (z, one SpMV per step) and K_lin ut (yt), so a
-  // trial costs vector updates and the nonlinear elements, not an SpMV
+  // residual line search: K_lin u at the current iterate (y: one SpMV at the start,
+  // then y + alpha z of each accepted trial), K_lin du (z, one SpMV per step) and
+  // K_lin ut (yt), so a trial costs vector updates and the nonlinear elements, not an
+  // SpMV, and an accepted step keeps its trial's residual
   const bool incremental = (o.line_search == FG_LS_RESIDUAL || o.line_search == FG_LS_QUADRATIC);
   double *d_y = incremental ? vec64(m, 16) : nullptr, *d_z = incremental ? vec64(m, 17) : nullptr;
   double *d_yt = incremental ? vec64(m, 18) : nullptr;
@@ -236,7 +237,10 @@ static int newton_dev(fg_mesh *m, double *d_u, const uint8_t *nl_host, const fg_
     ratio = (un > 0.0) ? dn / un : dn;
     if (!std::isfinite(ratio)) throw FgError{FG_NAN, "Newton update is not finite"};
     if (ratio <= o.tol_update) { converged = 1; break; }
-    if (need_jacobian) fg_newton_assemble_split(m, d_u, o.Ms, o.Hk, mixed, d_F, true, next_tangent, nullptr, d_y);
+    // the accepted trial left F at u (and, on the incremental path, K_lin u in y):
+    // only the Jacobian is rebuilt
+    if (need_jacobian)
+      fg_newton_assemble_split(m, d_u, o.Ms, o.Hk, mixed, incremental ? nullptr : d_F, true, next_tangent);
   }
   fg_energy_dev(m, d_u, o.Ms, o.Hk);
   double energy = fg_dot_dev(m, m->wdens, nullptr, m->nt, false);
