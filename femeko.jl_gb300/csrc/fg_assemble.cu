@@ -1576,16 +1576,10 @@ void fg_nl_setup(fg_mesh *m, const uint8_t *nl_host, bool mixed) {
   // no incidence records: the linear operator is assembled in one pass and the
   // nonlinear elements keep their own blocks (nl_re, nl_ke)
   const int64_t nt = m->nt;
-  // the mask of the handle's inputs, unchanged since its list was built, needs no
-  // scan (a scan of millions of elements takes milliseconds on the host, with the
-  // device idle)
-  const bool own = (nl_host == m->nl_host.data());
-  if (!(own && m->nl_list_current && m->nl_maps_valid)) {
-    nl_maps(m, nl_host);
-    if (own) m->nl_list_current = true;
-  }
   // the linear elements' operator (nonlinear elements contribute 0), Dirichlet rows
-  // applied; element state starts at the linear values
+  // applied; element state starts at the linear values.  Enqueued before the host
+  // builds the nonlinear element list below, so that the device assembles while the
+  // host scans the mask.
   double *coef = m->objbuf ? m->objbuf : (m->objbuf = dev_alloc<double>(m, 2 * (size_t)nt));
   k_linear_coef<<<grid_for(nt, 256), 256, 0, m->stream>>>(nt, m->mu_lin, m->nl, coef, m->mu, m->dmu);
   FG_LAUNCHED(1);
@@ -1603,6 +1597,13 @@ void fg_nl_setup(fg_mesh *m, const uint8_t *nl_host, bool mixed) {
                                 m->stream));
     FG_CUDA_TRY(cudaMemcpyAsync(m->dlin32, m->dinv32, sizeof(float) * (size_t)m->nvp, cudaMemcpyDeviceToDevice,
                                 m->stream));
+  }
+  // the mask of the handle's inputs, unchanged since its list was built, needs no
+  // scan (a scan of millions of elements takes a millisecond on the host)
+  const bool own = (nl_host == m->nl_host.data());
+  if (!(own && m->nl_list_current && m->nl_maps_valid)) {
+    nl_maps(m, nl_host);
+    if (own) m->nl_list_current = true;
   }
 }
 

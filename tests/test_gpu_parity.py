@@ -369,6 +369,21 @@ def test_bad_mesh_reports_error():
     assert e.value.status == L.FG_BAD_MESH
 
 
+def test_degenerate_element_reports_error():
+    """A zero-volume tetrahedron (two nodes of one element at the same point) is
+    flagged by the geometry kernel and the handle is refused."""
+    import femeko_gpu._lib as L
+    m = fg.box_tet_mesh(3)
+    m.p = m.p.copy()
+    a, b = int(m.t[0, 0]), int(m.t[1, 0])   # 0-based (t1 is the 1-based view)
+    m.p[:, b] = m.p[:, a]
+    with pytest.raises(L.FemekoGPUError) as e:
+        fg.GPUMesh(m)
+    assert e.value.status == L.FG_BAD_MESH
+    # an intact mesh right after the refused one builds
+    fg.GPUMesh(fg.box_tet_mesh(3))
+
+
 def _fan_mesh(k):
     """k tetrahedra above and k below a ring of k nodes around a centre node: the
     centre's row holds k + 3 entries, the apexes' k + 2."""
