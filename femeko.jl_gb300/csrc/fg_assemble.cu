@@ -564,6 +564,24 @@ __global__ void k_nl_map(int n_nl, const int *__restrict__ list, int64_t nt, con
 // The Froehlich elements of k_elem_newton: mu, dmu, the local residual VE mu G d
 // (re, 4 per element) and, when ke != null, the local Jacobian VE mu G + ct w w^T
 // (16 per element), all FP64.
+// One Froehlich element at nodal potentials uu: w = the Gram matrix times the
+// potential differences (w_a = grad phi_a . sum_b u_b grad phi_b), |H|^2 = u . w, the
+// permeability mu(|H|) and its derivative, and 1/|H|.
+__device__ __forceinline__ void nl_elem_eval(const double (&G)[10], const double (&uu)[4], double Ms, double Hk,
+                                             double (&w)[4], double &mu, double &dmu, double &ih) {
+  const double d1 = uu[1] - uu[0], d2 = uu[2] - uu[0], d3 = uu[3] - uu[0];
+  w[0] = G[1] * d1 + G[2] * d2 + G[3] * d3;
+  w[1] = G[4] * d1 + G[5] * d2 + G[6] * d3;
+  w[2] = G[5] * d1 + G[7] * d2 + G[8] * d3;
+  w[3] = G[6] * d1 + G[8] * d2 + G[9] * d3;
+  const double h2 = fmax(d1 * w[1] + d2 * w[2] + d3 * w[3], 0.0);
+  ih = rsqrt_nr(h2);
+  const double h = h2 * ih;
+  const double inv = rcp_nr(Hk + h);
+  mu = FG_MU0 * fma(Ms, inv, 1.0);
+  dmu = -FG_MU0 * Ms * inv * inv;
+}
+
 __global__ void __launch_bounds__(128) k_elem_newton_nl(int n_nl, const int *__restrict__ list, int64_t nt,
                                                         const double *__restrict__ geo, const int *__restrict__ t,
                                                         const double *__restrict__ u, double Ms, double Hk,
@@ -580,18 +598,8 @@ __global__ void __launch_bounds__(128) k_elem_newton_nl(int n_nl, const int *__r
   double uu[4];
 #pragma unroll
   for (int a = 0; a < 4; ++a) uu[a] = u[t[(int64_t)a * nt + k]];
-  const double d1 = uu[1] - uu[0], d2 = uu[2] - uu[0], d3 = uu[3] - uu[0];
-  double w[4];
-  w[0] = G[1] * d1 + G[2] * d2 + G[3] * d3;
-  w[1] = G[4] * d1 + G[5] * d2 + G[6] * d3;
-  w[2] = G[5] * d1 + G[7] * d2 + G[8] * d3;
-  w[3] = G[6] * d1 + G[8] * d2 + G[9] * d3;
-  const double h2 = fmax(d1 * w[1] + d2 * w[2] + d3 * w[3], 0.0);
-  const double ih = rsqrt_nr(h2);
-  const double h = h2 * ih;
-  const double inv = rcp_nr(Hk + h);
-  const double mu = FG_MU0 * fma(Ms, inv, 1.0);
-  const double dmu = -FG_MU0 * Ms * inv * inv;
+  double w[4], mu, dmu, ih;
+  nl_elem_eval(G, uu, Ms, Hk, w, mu, dmu, ih);
   if (!isfinite(mu) || !isfinite(dmu)) atomicOr(flags, FLAG_NAN);
   mu_out[k] = mu;
   dmu_out[k] = dmu;
@@ -605,6 +613,76 @@ __global__ void __launch_bounds__(128) k_elem_newton_nl(int n_nl, const int *__r
   for (int a = 0; a < 4; ++a)
 #pragma unroll
     for (int b = 0; b < 4; ++b) ke[16 * e + 4 * a + b] = fma(ct * w[a], w[b], vm * G[idx[a][b]]);
+}
+
+// The residual records of every nonlinear element at the candidate points
+// u + a_c du (thread per (candidate, element)): the trial point of k_newton_trial64
+// and the arithmetic of k_elem_newton_nl, without the element state writes.
+__global__ void __launch_bounds__(128) k_elem_newton_nl_cand(LsCand cand, int n_nl, const int *__restrict__ list,
+                                                             int64_t nt, const double *__restrict__ geo,
+                                                             const int *__restrict__ t, const double *__restrict__ u,
+                                                             const double *__restrict__ du, double Ms, double Hk,
+                                                             double *__restrict__ re) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= (int64_t)cand.n * n_nl) return;
+  const int c = (int)(q / n_nl), e = (int)(q - (int64_t)c * n_nl);
+  const double alpha = cand.a[c];
+  const int64_t k = list[e];
+  double G[10];
+#pragma unroll
+  for (int j = 0; j < 10; ++j) G[j] = geo[(int64_t)(13 + j) * nt + k];
+  const double VE = geo[12 * nt + k];
+  double uu[4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const int node = t[(int64_t)a * nt + k];
+    uu[a] = fma(alpha, du[node], u[node]);
+  }
+  double w[4], mu, dmu, ih;
+  nl_elem_eval(G, uu, Ms, Hk, w, mu, dmu, ih);
+  const double vm = VE * mu;
+#pragma unroll
+  for (int a = 0; a < 4; ++a) re[(int64_t)c * 4 * n_nl + 4 * e + a] = vm * w[a];
+}
+
+// Per candidate (one block each): the sum over the rows that nonlinear elements touch
+// of (fma(a_c, z_i, y_i) + the row's records at that candidate)^2, the records added
+// in the order of k_nl_rows; Dirichlet rows are 0.  Thread-strided rows, then a fixed
+// shuffle and shared-memory tree.
+__global__ void __launch_bounds__(256) k_nl_rows_cand_norm(LsCand cand, int n_rows, int n_nl,
+                                                           const int *__restrict__ rows, const int *__restrict__ ptr,
+                                                           const int *__restrict__ src, const double *__restrict__ re,
+                                                           const double *__restrict__ y, const double *__restrict__ z,
+                                                           const uint8_t *__restrict__ fixed, double *__restrict__ out) {
+  const int c = blockIdx.x;
+  if (c >= cand.n) return;
+  const double alpha = cand.a[c];
+  const double *rc = re + (int64_t)c * 4 * n_nl;
+  double acc = 0.0;
+  for (int r = threadIdx.x; r < n_rows; r += blockDim.x) {
+    const int i = rows[r];
+    if (fixed && fixed[i]) continue;
+    double s = 0.0;
+    for (int q = ptr[r]; q < ptr[r + 1]; ++q) s += rc[src[q]];
+    const double v = fma(alpha, z[i], y[i]) + s;
+    acc = fma(v, v, acc);
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  __shared__ double sh[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) sh[warp] = acc;
+  __syncthreads();
+  if (warp == 0) {
+    acc = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) out[3 + c] = acc;
+  }
+}
+
+// Rows that nonlinear elements touch, as a 0/1 mask.
+__global__ void k_mark_rows(int n_rows, const int *__restrict__ rows, uint8_t *__restrict__ mask) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < n_rows) mask[rows[r]] = 1;
 }
 
 // y[row] += the nonlinear elements' residual records of the row, in a fixed order
@@ -1566,9 +1644,38 @@ static void nl_maps(fg_mesh *m, const uint8_t *nl_host) {
       up(m->nl_row_src, rord);
       fg_sync(m);
     }
+    // the rows the nonlinear elements touch, for the batched line search
+    if (!m->nl_rowmask) m->nl_rowmask = dev_alloc<uint8_t>(m, (size_t)m->nv);
+    FG_CUDA_TRY(cudaMemsetAsync(m->nl_rowmask, 0, (size_t)m->nv, m->stream));
+    if (m->n_nl_rows > 0) {
+      k_mark_rows<<<grid_for(m->n_nl_rows, 256), 256, 0, m->stream>>>(m->n_nl_rows, m->nl_rows, m->nl_rowmask);
+      FG_CUDA_TRY(cudaGetLastError());
+      FG_LAUNCHED(1);
+    }
     m->nl_list_host = list;
     m->nl_maps_valid = true;
   }
+}
+
+void fg_newton_trial_batch(fg_mesh *m, const double *d_u, const double *d_du, const double *d_y, const double *d_z,
+                           const LsCand &cand, double Ms, double Hk, double *d_out) {
+  FG_REQUIRE(m->nl_maps_valid && m->nl_rowmask, FG_BAD_ARG, "Newton split: no nonlinear maps");
+  FG_REQUIRE(cand.n >= 1 && cand.n <= FG_LS_BATCH, FG_BAD_ARG, "batched line search: bad candidate count");
+  const int n = m->n_nl;
+  if (n > 0) {
+    if (n > m->nl_cand_cap) {
+      m->nl_re_cand = dev_alloc<double>(m, (size_t)FG_LS_BATCH * 4 * (size_t)n);
+      m->nl_cand_cap = n;
+    }
+    k_elem_newton_nl_cand<<<grid_for((int64_t)cand.n * n, 128), 128, 0, m->stream>>>(
+        cand, n, m->nl_elems, m->nt, m->geo, m->t, d_u, d_du, Ms, Hk, m->nl_re_cand);
+    FG_LAUNCHED(1);
+  }
+  // a block per candidate also when no row is touched (the sums are then 0)
+  k_nl_rows_cand_norm<<<cand.n, 256, 0, m->stream>>>(cand, m->n_nl_rows, n, m->nl_rows, m->nl_row_ptr, m->nl_row_src,
+                                                    m->nl_re_cand, d_y, d_z, m->has_fixed ? m->fixed : nullptr, d_out);
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(1);
 }
 
 void fg_nl_setup(fg_mesh *m, const uint8_t *nl_host, bool mixed) {

@@ -33,8 +33,8 @@ __global__ void k_newton_trial64(int64_t n, double alpha, const double *__restri
                                  double *__restrict__ yt, double *__restrict__ F) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  ut[i] = 1.0 * u[i] + alpha * du[i];
-  const double v = y[i] + alpha * z[i];
+  ut[i] = fma(alpha, du[i], u[i]);
+  const double v = fma(alpha, z[i], y[i]);
   yt[i] = v;
   F[i] = v;
 }
@@ -97,6 +97,10 @@ static int newton_dev(fg_mesh *m, double *d_u, const uint8_t *nl_host, const fg_
   const bool incremental = (o.line_search == FG_LS_RESIDUAL || o.line_search == FG_LS_QUADRATIC);
   double *d_y = incremental ? vec64(m, 16) : nullptr, *d_z = incremental ? vec64(m, 17) : nullptr;
   double *d_yt = incremental ? vec64(m, 18) : nullptr;
+  // the fixed backtracking alpha <- 0.9 alpha: its trials are evaluated in batches
+  const bool batched = (o.line_search == FG_LS_RESIDUAL);
+  if (batched && !m->ls_out) m->ls_out = dev_alloc<double>(m, 3 + FG_LS_BATCH);
+  double *d_ls = batched ? m->ls_out : nullptr;
   fg_solve_opts so;
   fg_solve_opts_default(&so);
   so.precision = o.precision;
@@ -160,7 +164,47 @@ static int newton_dev(fg_mesh *m, double *d_u, const uint8_t *nl_host, const fg_
       const double f0 = rF * rF;
       double rt = 0.0;
       if (incremental) fg_spmv64_vals(m, m->vlin64, d_du, d_z);
-      for (;;) {
+      if (batched) {
+        // the step sequence of the loop below (alpha, 0.9 alpha, ... until a
+        // decrease or alpha <= min_step), FG_LS_BATCH candidates per launch and one
+        // host wait per launch: |F(alpha)|^2 is the quadratic in alpha over the rows
+        // no nonlinear element touches plus the touched rows evaluated per candidate
+        fg_lin_quad_enqueue(m, d_y, d_z, m->nl_rowmask, d_ls);
+        for (;;) {
+          LsCand cand;
+          cand.n = 0;
+          double a = alpha;
+          for (;;) {
+            cand.a[cand.n++] = a;
+            if (cand.n == FG_LS_BATCH || !(a > o.min_step)) break;
+            a *= 0.9;
+          }
+          fg_newton_trial_batch(m, d_u, d_du, d_y, d_z, cand, o.Ms, o.Hk, d_ls);
+          FG_CUDA_TRY(cudaMemcpyAsync(m->hbuf, d_ls, sizeof(double) * (3 + (size_t)cand.n), cudaMemcpyDeviceToHost,
+                                      m->stream));
+          fg_sync(m);
+          const double qa = m->hbuf[0], qb = m->hbuf[1], qc = m->hbuf[2];
+          int stop = -1;
+          for (int j = 0; j < cand.n && stop < 0; ++j) {
+            ++trials;
+            const double aj = cand.a[j];
+            rt = std::sqrt(std::max(qa + aj * (2.0 * qb + aj * qc), 0.0) + m->hbuf[3 + j]);
+            if (!(rt > rF && aj > o.min_step)) stop = j;
+          }
+          if (stop >= 0) {
+            alpha = cand.a[stop];
+            break;
+          }
+          alpha = cand.a[cand.n - 1] * 0.9;
+        }
+        if (alpha >= o.min_step) {
+          // the accepted point, its residual and the element state at it
+          k_newton_trial64<<<g, 256, 0, m->stream>>>(nv, alpha, d_u, d_du, d_y, d_z, d_ut, d_yt, d_Ft);
+          FG_LAUNCHED(1);
+          fg_newton_assemble_split(m, d_ut, o.Ms, o.Hk, mixed, d_Ft, false, next_tangent, d_Ft);
+        }
+      }
+      for (; !batched;) {
         if (incremental) {
           k_newton_trial64<<<g, 256, 0, m->stream>>>(nv, alpha, d_u, d_du, d_y, d_z, d_ut, d_yt, d_Ft);
           FG_LAUNCHED(1);

@@ -1690,6 +1690,29 @@ __global__ void __launch_bounds__(256) k_dot64(int64_t n, const double *__restri
   if (grid_finish<1>(part, partials, counter, tot)) scal[slot] = tot[0];
 }
 
+// (y.y, y.z, z.z) over the rows with mask 0: the coefficients of |y + a z|^2 on those
+// rows as a quadratic in a (fixed-order grid reduction).
+__global__ void __launch_bounds__(256) k_lin_quad(int64_t n, const double *__restrict__ y, const double *__restrict__ z,
+                                                  const uint8_t *__restrict__ mask, double *out, double *partials,
+                                                  unsigned *counter) {
+  double v[3] = {0.0, 0.0, 0.0};
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (!mask || !mask[i]) {
+      const double a = y[i], b = z[i];
+      v[0] = fma(a, a, v[0]);
+      v[1] = fma(a, b, v[1]);
+      v[2] = fma(b, b, v[2]);
+    }
+  __shared__ double shd[3][32];
+  block_sum<3>(v, shd);
+  double tot[3];
+  if (grid_finish<3>(v, partials, counter, tot)) {
+    out[0] = tot[0];
+    out[1] = tot[1];
+    out[2] = tot[2];
+  }
+}
+
 // F <- -F with the sum of squares of the result (one pass instead of a negation and
 // a separate dot product)
 __global__ void __launch_bounds__(256) k_negate_norm64(int64_t n, double *__restrict__ F, int slot, double *scal,
@@ -1736,6 +1759,13 @@ static unsigned dot_grid(const fg_mesh *m, int64_t n) {
 void fg_dot_enqueue(fg_mesh *m, const double *x, const double *y, int64_t n, bool mask_fixed, int slot) {
   k_dot64<<<dot_grid(m, n), 256, 0, m->stream>>>(n, x, y, (mask_fixed && m->has_fixed) ? m->fixed : nullptr, slot,
                                                  m->scal, m->red.partials, m->red.counter);
+  FG_CUDA_TRY(cudaGetLastError());
+  FG_LAUNCHED(1);
+}
+
+void fg_lin_quad_enqueue(fg_mesh *m, const double *d_y, const double *d_z, const uint8_t *mask, double *d_out) {
+  k_lin_quad<<<dot_grid(m, m->nv), 256, 0, m->stream>>>(m->nv, d_y, d_z, mask, d_out, m->red.partials,
+                                                         m->red.counter);
   FG_CUDA_TRY(cudaGetLastError());
   FG_LAUNCHED(1);
 }
