@@ -649,7 +649,7 @@ __global__ void __launch_bounds__(128) k_elem_newton_nl_cand(LsCand cand, int n_
 // of (fma(a_c, z_i, y_i) + the row's records at that candidate)^2, the records added
 // in the order of k_nl_rows; Dirichlet rows are 0.  Thread-strided rows, then a fixed
 // shuffle and shared-memory tree.
-__global__ void __launch_bounds__(256) k_nl_rows_cand_norm(LsCand cand, int n_rows, int n_nl,
+__global__ void __launch_bounds__(1024) k_nl_rows_cand_norm(LsCand cand, int n_rows, int n_nl,
                                                            const int *__restrict__ rows, const int *__restrict__ ptr,
                                                            const int *__restrict__ src, const double *__restrict__ re,
                                                            const double *__restrict__ y, const double *__restrict__ z,
@@ -675,7 +675,7 @@ __global__ void __launch_bounds__(256) k_nl_rows_cand_norm(LsCand cand, int n_ro
   if (warp == 0) {
     acc = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if (lane == 0) out[3 + c] = acc;
+    if (lane == 0) out[FG_LS_QUAD + c] = acc;
   }
 }
 
@@ -1672,7 +1672,7 @@ void fg_newton_trial_batch(fg_mesh *m, const double *d_u, const double *d_du, co
     FG_LAUNCHED(1);
   }
   // a block per candidate also when no row is touched (the sums are then 0)
-  k_nl_rows_cand_norm<<<cand.n, 256, 0, m->stream>>>(cand, m->n_nl_rows, n, m->nl_rows, m->nl_row_ptr, m->nl_row_src,
+  k_nl_rows_cand_norm<<<cand.n, 1024, 0, m->stream>>>(cand, m->n_nl_rows, n, m->nl_rows, m->nl_row_ptr, m->nl_row_src,
                                                     m->nl_re_cand, d_y, d_z, m->has_fixed ? m->fixed : nullptr, d_out);
   FG_CUDA_TRY(cudaGetLastError());
   FG_LAUNCHED(1);

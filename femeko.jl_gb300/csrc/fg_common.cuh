@@ -213,7 +213,7 @@ struct fg_mesh {
   uint8_t *nl_rowmask = nullptr;
   double *nl_re_cand = nullptr;
   int nl_cand_cap = 0;
-  double *ls_out = nullptr;                      // 3 + FG_LS_BATCH results
+  double *ls_out = nullptr;                      // FG_LS_QUAD + FG_LS_BATCH results
   std::vector<int> nl_list_host;                 // the list the maps were built for
   std::vector<uint8_t> nl_host;                  // nonlinear mask of the current Newton inputs
   double *u0dev = nullptr;                       // Dirichlet values / initial guess of the Newton inputs
@@ -346,19 +346,22 @@ void fg_nl_setup(fg_mesh *m, const uint8_t *nl_host, bool mixed);
 void fg_set_nl_host(fg_mesh *m, const uint8_t *nl);
 // Candidate steps of one batched line-search launch.
 constexpr int FG_LS_BATCH = 8;
+constexpr int FG_LS_QUAD = 6;  // results of fg_lin_quad_enqueue ahead of the candidates'
 struct LsCand {
   double a[FG_LS_BATCH];
   int n;
 };
 // Residual norms of the trial points u + a_c du (c < cand.n) in one launch pair:
-// out[3 + c] = sum over the rows that nonlinear elements touch of F_i^2, with F_i =
-// fma(a_c, z_i, y_i) + the nonlinear elements' records at u + a_c du (the arithmetic
-// of k_newton_trial64 + k_elem_newton_nl + k_nl_rows, bit for bit).  The rest of |F|^2
-// is out[0] + 2 a out[1] + a^2 out[2] from fg_lin_quad_enqueue.
+// out[FG_LS_QUAD + c] = sum over the rows that nonlinear elements touch of F_i^2, with
+// F_i = fma(a_c, z_i, y_i) + the nonlinear elements' records at u + a_c du (the
+// arithmetic of k_newton_trial64 + k_elem_newton_nl + k_nl_rows, bit for bit).  The
+// rest of |F|^2 is out[0] + 2 a out[1] + a^2 out[2] from fg_lin_quad_enqueue.
 void fg_newton_trial_batch(fg_mesh *m, const double *d_u, const double *d_du, const double *d_y, const double *d_z,
                            const LsCand &cand, double Ms, double Hk, double *d_out);
-// out[0..2] = (y.y, y.z, z.z) over the rows with mask 0 (fixed order).
-void fg_lin_quad_enqueue(fg_mesh *m, const double *d_y, const double *d_z, const uint8_t *mask, double *d_out);
+// out[0..2] = (y.y, y.z, z.z) over the rows with mask 0, out[3..5] = (u.u, u.du,
+// du.du) over all rows (fixed order).
+void fg_lin_quad_enqueue(fg_mesh *m, const double *d_y, const double *d_z, const uint8_t *mask, const double *d_u,
+                         const double *d_du, double *d_out);
 // lin_in: K_lin u already known (a vector, or d_F itself when it holds it), so the
 // linear elements' SpMV is skipped; lin_out: where the SpMV also leaves K_lin u;
 // d_F null: the Jacobian alone (element state and operator at u).

@@ -99,7 +99,8 @@ static int newton_dev(fg_mesh *m, double *d_u, const uint8_t *nl_host, const fg_
   double *d_yt = incremental ? vec64(m, 18) : nullptr;
   // the fixed backtracking alpha <- 0.9 alpha: its trials are evaluated in batches
   const bool batched = (o.line_search == FG_LS_RESIDUAL);
-  if (batched && !m->ls_out) m->ls_out = dev_alloc<double>(m, 3 + FG_LS_BATCH);
+  double uq[3] = {0.0, 0.0, 0.0};  // |u|^2, u.du, |du|^2 of the current step (batched)
+  if (batched && !m->ls_out) m->ls_out = dev_alloc<double>(m, FG_LS_QUAD + FG_LS_BATCH);
   double *d_ls = batched ? m->ls_out : nullptr;
   fg_solve_opts so;
   fg_solve_opts_default(&so);
@@ -168,8 +169,10 @@ static int newton_dev(fg_mesh *m, double *d_u, const uint8_t *nl_host, const fg_
         // the step sequence of the loop below (alpha, 0.9 alpha, ... until a
         // decrease or alpha <= min_step), FG_LS_BATCH candidates per launch and one
         // host wait per launch: |F(alpha)|^2 is the quadratic in alpha over the rows
-        // no nonlinear element touches plus the touched rows evaluated per candidate
-        fg_lin_quad_enqueue(m, d_y, d_z, m->nl_rowmask, d_ls);
+        // no nonlinear element touches plus the touched rows evaluated per candidate;
+        // the same wait brings |u|^2, u.du and |du|^2 for the update test and the
+        // device error flags
+        fg_lin_quad_enqueue(m, d_y, d_z, m->nl_rowmask, d_u, d_du, d_ls);
         for (;;) {
           LsCand cand;
           cand.n = 0;
@@ -180,15 +183,20 @@ static int newton_dev(fg_mesh *m, double *d_u, const uint8_t *nl_host, const fg_
             a *= 0.9;
           }
           fg_newton_trial_batch(m, d_u, d_du, d_y, d_z, cand, o.Ms, o.Hk, d_ls);
-          FG_CUDA_TRY(cudaMemcpyAsync(m->hbuf, d_ls, sizeof(double) * (3 + (size_t)cand.n), cudaMemcpyDeviceToHost,
-                                      m->stream));
+          FG_CUDA_TRY(cudaMemcpyAsync(m->hbuf, d_ls, sizeof(double) * (FG_LS_QUAD + (size_t)cand.n),
+                                      cudaMemcpyDeviceToHost, m->stream));
+          FG_CUDA_TRY(cudaMemcpyAsync(m->hint + 8, m->flags, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
           fg_sync(m);
+          fg_raise_flags(m, m->hint[8], "fg_newton_magnetostatics");
           const double qa = m->hbuf[0], qb = m->hbuf[1], qc = m->hbuf[2];
+          uq[0] = m->hbuf[3];
+          uq[1] = m->hbuf[4];
+          uq[2] = m->hbuf[5];
           int stop = -1;
           for (int j = 0; j < cand.n && stop < 0; ++j) {
             ++trials;
             const double aj = cand.a[j];
-            rt = std::sqrt(std::max(qa + aj * (2.0 * qb + aj * qc), 0.0) + m->hbuf[3 + j]);
+            rt = std::sqrt(std::max(qa + aj * (2.0 * qb + aj * qc), 0.0) + m->hbuf[FG_LS_QUAD + j]);
             if (!(rt > rF && aj > o.min_step)) stop = j;
           }
           if (stop >= 0) {
@@ -265,19 +273,26 @@ static int newton_dev(fg_mesh *m, double *d_u, const uint8_t *nl_host, const fg_
       fg_newton_assemble_split(m, d_u, o.Ms, o.Hk, mixed, d_F, true, next_tangent);
       rF = fg_slot_sqrt(m, FG_SLOT_FNORM2);
     }
-    // |du|, |u| and the device error flags in one round trip
-    fg_dot_enqueue(m, d_du, d_du, nv, false, 10);
-    fg_dot_enqueue(m, d_u, d_u, nv, false, 11);
-    FG_CUDA_TRY(cudaMemcpyAsync(m->hbuf, m->scal + 10, 2 * sizeof(double), cudaMemcpyDeviceToHost, m->stream));
-    FG_CUDA_TRY(cudaMemcpyAsync(m->hint + 8, m->flags, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
-    fg_sync(m);
-    fg_raise_flags(m, m->hint[8], "fg_newton_magnetostatics");
+    double dn, un;
+    if (batched) {
+      // |u + alpha du| from the sums the line search read (u is the accepted point)
+      dn = alpha * std::sqrt(uq[2]);
+      un = std::sqrt(std::max(uq[0] + alpha * (2.0 * uq[1] + alpha * uq[2]), 0.0));
+    } else {
+      // |du|, |u| and the device error flags in one round trip
+      fg_dot_enqueue(m, d_du, d_du, nv, false, 10);
+      fg_dot_enqueue(m, d_u, d_u, nv, false, 11);
+      FG_CUDA_TRY(cudaMemcpyAsync(m->hbuf, m->scal + 10, 2 * sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+      FG_CUDA_TRY(cudaMemcpyAsync(m->hint + 8, m->flags, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
+      fg_sync(m);
+      fg_raise_flags(m, m->hint[8], "fg_newton_magnetostatics");
+      dn = alpha * std::sqrt(m->hbuf[0]);
+      un = std::sqrt(m->hbuf[1]);
+    }
     {
       float t = 0.f;
       if (cudaEventElapsedTime(&t, ec0, ec1) == cudaSuccess) cg_ms += t;
     }
-    double dn = alpha * std::sqrt(m->hbuf[0]);
-    double un = std::sqrt(m->hbuf[1]);
     ratio = (un > 0.0) ? dn / un : dn;
     if (!std::isfinite(ratio)) throw FgError{FG_NAN, "Newton update is not finite"};
     if (ratio <= o.tol_update) { converged = 1; break; }
@@ -286,6 +301,9 @@ static int newton_dev(fg_mesh *m, double *d_u, const uint8_t *nl_host, const fg_
     if (need_jacobian)
       fg_newton_assemble_split(m, d_u, o.Ms, o.Hk, mixed, incremental ? nullptr : d_F, true, next_tangent);
   }
+  // the flags of the last accepted point's element evaluation (the batched path reads
+  // them with each step's first line-search wait)
+  if (batched) fg_check_flags(m, "fg_newton_magnetostatics");
   fg_energy_dev(m, d_u, o.Ms, o.Hk);
   double energy = fg_dot_dev(m, m->wdens, nullptr, m->nt, false);
   FG_CUDA_TRY(cudaEventRecord(e1, m->stream));

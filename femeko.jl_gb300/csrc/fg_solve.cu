@@ -1691,26 +1691,48 @@ __global__ void __launch_bounds__(256) k_dot64(int64_t n, const double *__restri
 }
 
 // (y.y, y.z, z.z) over the rows with mask 0: the coefficients of |y + a z|^2 on those
-// rows as a quadratic in a (fixed-order grid reduction).
+// rows as a quadratic in a; and (u.u, u.du, du.du) over all rows, those of
+// |u + a du|^2 (fixed-order grid reduction).
 __global__ void __launch_bounds__(256) k_lin_quad(int64_t n, const double *__restrict__ y, const double *__restrict__ z,
-                                                  const uint8_t *__restrict__ mask, double *out, double *partials,
+                                                  const uint8_t *__restrict__ mask, const double *__restrict__ u,
+                                                  const double *__restrict__ du, double *out, double *partials,
                                                   unsigned *counter) {
-  double v[3] = {0.0, 0.0, 0.0};
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    if (!mask || !mask[i]) {
-      const double a = y[i], b = z[i];
+  double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  auto add = [&](double a, double b, bool in, double p, double q) {
+    if (in) {
       v[0] = fma(a, a, v[0]);
       v[1] = fma(a, b, v[1]);
       v[2] = fma(b, b, v[2]);
     }
-  __shared__ double shd[3][32];
-  block_sum<3>(v, shd);
-  double tot[3];
-  if (grid_finish<3>(v, partials, counter, tot)) {
-    out[0] = tot[0];
-    out[1] = tot[1];
-    out[2] = tot[2];
+    v[3] = fma(p, p, v[3]);
+    v[4] = fma(p, q, v[4]);
+    v[5] = fma(q, q, v[5]);
+  };
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  // four rows' loads in flight before their sums, which keep the row order of a plain
+  // grid-stride loop
+  for (; i + 3 * stride < n; i += 4 * stride) {
+    double a[4], b[4], p[4], q[4];
+    bool in[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int64_t j = i + r * stride;
+      a[r] = y[j];
+      b[r] = z[j];
+      p[r] = u[j];
+      q[r] = du[j];
+      in[r] = !mask || !mask[j];
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) add(a[r], b[r], in[r], p[r], q[r]);
   }
+  for (; i < n; i += stride) add(y[i], z[i], !mask || !mask[i], u[i], du[i]);
+  __shared__ double shd[6][32];
+  block_sum<6>(v, shd);
+  double tot[6];
+  if (grid_finish<6>(v, partials, counter, tot))
+    for (int j = 0; j < 6; ++j) out[j] = tot[j];
 }
 
 // F <- -F with the sum of squares of the result (one pass instead of a negation and
@@ -1763,8 +1785,9 @@ void fg_dot_enqueue(fg_mesh *m, const double *x, const double *y, int64_t n, boo
   FG_LAUNCHED(1);
 }
 
-void fg_lin_quad_enqueue(fg_mesh *m, const double *d_y, const double *d_z, const uint8_t *mask, double *d_out) {
-  k_lin_quad<<<dot_grid(m, m->nv), 256, 0, m->stream>>>(m->nv, d_y, d_z, mask, d_out, m->red.partials,
+void fg_lin_quad_enqueue(fg_mesh *m, const double *d_y, const double *d_z, const uint8_t *mask, const double *d_u,
+                         const double *d_du, double *d_out) {
+  k_lin_quad<<<dot_grid(m, m->nv), 256, 0, m->stream>>>(m->nv, d_y, d_z, mask, d_u, d_du, d_out, m->red.partials,
                                                          m->red.counter);
   FG_CUDA_TRY(cudaGetLastError());
   FG_LAUNCHED(1);
