@@ -4,16 +4,18 @@
 // iteration of Magnetostatics/NewtonRaphson.jl:109-214, both with Dirichlet rows.
 //
 // Newton step: the residual F = -K(mu(u)) u and the Jacobian K(mu) + At(H, dmu).  The
-// linear elements' part of K is assembled once per solve (mu fixed there); each
-// residual is that operator's FP64 SpMV plus the nonlinear (Froehlich) elements
-// re-evaluated and summed into their rows, and each Jacobian is a copy of the linear
-// operator with the nonlinear elements' entries added at their slots.  The inner
+// linear elements' part of K is assembled once per solve (mu fixed there); a residual
+// is that operator's part (K_lin u: one FP64 SpMV at the start, then K_lin u +
+// alpha K_lin du per accepted step, one SpMV for K_lin du) plus the nonlinear
+// (Froehlich) elements re-evaluated and summed into their rows, and each Jacobian is a
+// copy of the linear operator with the nonlinear elements' entries added at their
+// slots.  The inner
 // increment solve J du = F runs to a relative residual inner_rtol in FP32 (mixed)
 // or FP64; F is always FP64, so the Newton loop is the iterative refinement.
 // Step control follows src/FEM3D.jl:123-152 (alpha = 1, 0.9, 0.81, ... while the
 // residual grows and alpha > min_step), applied either to the frozen secant
 // (FG_LS_REFERENCE, the reference's lineSearch) or to the true residual
-// (FG_LS_RESIDUAL).
+// (FG_LS_RESIDUAL, up to FG_LS_BATCH steps evaluated per host wait).
 #include <cmath>
 #include <utility>
 
