@@ -21,8 +21,8 @@
 
 #include "fg_common.cuh"
 
-__global__ void k_axpby64(int64_t n, double a, const double *__restrict__ x, double b, const double *__restrict__ y,
-                          double *__restrict__ out) {
+// out = a x + b y elementwise; out may be x or y (in-place updates), so no restrict.
+__global__ void k_axpby64(int64_t n, double a, const double *x, double b, const double *y, double *out) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = a * x[i] + b * y[i];
 }
